@@ -1,0 +1,328 @@
+#!/usr/bin/env python3
+"""Benchmark of the path-tracing hot path on the 1920x1080 production scene.
+
+Workload: bonsai_gb300.scenes.production() - 64 fBm-displaced level-5 icospheres (1.31M triangles),
+2000 lognormal spheres, ground quad, 4 quad area lights; 1920x1080, 64 spp, max depth 8, Russian
+roulette after depth 3, PBRT estimator (unbiased), seeded synthetic geometry.
+
+One step = one full 64-spp render of the frame (132.7M samples).
+  value : Msamples/s on the device: samples / sum of CUDA-event render times (scene resident in
+          HBM, film left on the device), L2 flushed (512 MB write) before every step.
+  e2e   : Msamples/s through the C ABI entry point bg_render with a host film buffer: every step
+          sends the camera/options and reads the resolved 1920x1080x3 float film back.
+  roofline: dominant kernel = closest-hit traversal (k_extend).  Algorithmic bytes per ray =
+          32 (ray) + 8 (hit) + 32 V + 40 T, with V / T the mean node visits / triangle tests of the
+          reference traversal (binary SAH BVH, bucket-fixed build) counted by the CPU oracle on a
+          subsample of the same paths; achieved = bytes / summed k_extend event time.
+  cpu_baseline: the CPU oracle (C++ restatement of the reference, PBRT mode, bucket-fixed BVH) on
+          all host cores over a bounded subset of image rows.
+--impl reference times that same CPU restatement as the reference arm.
+Multi-GPU (--gpus N under torchrun): independent replicas, one per GPU ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s"
+UNIT = "Msamples/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(small: bool):
+    from bonsai_gb300 import scenes as S
+    if small:
+        return S.production(480, 270, spp=16, max_depth=8, n_ico=8, ico_level=4, n_spheres=500)
+    return S.production()
+
+
+def config_of(sd, small: bool) -> dict:
+    return {
+        "workload": ("production-small" if small else "production 1080p") +
+                    f": {sd.ntri} triangles (64 fBm icospheres L5 + ground + 4 quad lights), "
+                    f"{sd.nsph} spheres, {sd.camera.width}x{sd.camera.height}, {sd.spp} spp, max depth "
+                    f"{sd.max_depth}, RR after depth 3, PBRT estimator",
+        "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
+        "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "2-wide SAH (binned, 32 bins, <=8 prims/leaf)",
+        "l2": "flushed before every step (512 MB device write)",
+        "parallelism": "replicas",
+    }
+
+
+# ---------------------------------------------------------------- distributed (replicas only)
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0")), dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        loaded = [s for s in sm if s > 0.5 * (max(mx) if mx else 0)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle)
+def cpu_sample(sd, target_s: float, threads: int):
+    """Times the CPU restatement over every k-th image row, k chosen for ~target_s of work."""
+    import oracle as O
+    from bonsai_gb300 import _abi as A
+    t0 = time.time()
+    orc = O.OracleScene(sd, fixed_bvh=True)
+    build_s = time.time() - t0
+    H, W = sd.camera.height, sd.camera.width
+    probe_rows = (0, H, max(1, H // 8))
+    t0 = time.time()
+    orc.render(A.BG_MODE_PBRT, spp=max(1, sd.spp // 16), rows=probe_rows, threads=threads)
+    dt = max(time.time() - t0, 1e-3)
+    probe_samples = len(range(*probe_rows)) * W * max(1, sd.spp // 16)
+    rate = probe_samples / dt
+    want_rows = max(1, int(target_s * rate / (W * sd.spp)))
+    step = max(1, H // want_rows)
+    rows = (0, H, step)
+    nrows = len(range(*rows))
+    return orc, rows, nrows * W * sd.spp, build_s
+
+
+def time_cpu(orc, sd, rows, nsamples, threads):
+    from bonsai_gb300 import _abi as A
+    t0 = time.time()
+    orc.render(A.BG_MODE_PBRT, rows=rows, threads=threads)
+    dt = time.time() - t0
+    return nsamples / dt / 1e6, dt
+
+
+def traversal_counts(orc, sd):
+    """Mean node visits / primitive tests per closest-hit and any-hit ray of the reference
+    traversal, on the paths of a row subsample (1 spp)."""
+    from bonsai_gb300 import _abi as A
+    H = sd.camera.height
+    r = orc.render(A.BG_MODE_PBRT, spp=2, rows=(0, H, max(1, H // 24)), count_traversal=True)
+    c = r["counters"]
+    return {"V_ext": c[2] / max(c[0], 1), "T_ext": c[3] / max(c[0], 1),
+            "V_sh": c[4] / max(c[1], 1), "T_sh": c[5] / max(c[1], 1), "rays_counted": int(c[0] + c[1])}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- arms
+def run_reference(args):
+    rank, ws, local, dist = dist_init()
+    if rank != 0:
+        return
+    sd = workload(args.small)
+    threads = os.cpu_count() or 1
+    orc, rows, nsamples, build_s = cpu_sample(sd, min(args.cpu_seconds, 20.0), threads)
+    for _ in range(args.warmup):
+        time_cpu(orc, sd, rows, nsamples, threads)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, dt = time_cpu(orc, sd, rows, nsamples, threads)
+        vals.append(v)
+        times.append(dt)
+    total_t = sum(times)
+    value = args.steps * nsamples / total_t / 1e6
+    sample = (f"rows 0..{sd.camera.height} step {rows[2]} ({len(range(*rows))} rows x {sd.camera.width} px x "
+              f"{sd.spp} spp = {nsamples} samples per step)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": config_of(sd, args.small),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "C++ restatement of the reference PathIntegrator (oracle/), PBRT estimator, bucket-fixed "
+                 "reference BVH (the reference's own bucket bug makes a chain BVH); the Rust reference cannot "
+                 f"be built here (no Rust toolchain). Oracle BVH build {build_s:.1f} s excluded.",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    rank, ws, local, dist = dist_init()
+    sd = workload(args.small)
+    ctx = G.Context(local)
+    t0 = time.time()
+    scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    upload_build_s = time.time() - t0
+    pi = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=0)
+    samples = sd.camera.width * sd.camera.height * sd.spp
+    for _ in range(args.warmup):
+        pi.render(scene, readback=False)
+    clocks = Clocks(local)
+    barrier(dist)
+    ctx.synchronize()
+    clocks.start()
+    dev_ms, launches, wall0 = 0.0, 0, time.time()
+    for k in range(args.steps):
+        ctx.flush_l2()
+        r = pi.render(scene, readback=False, first_sample=k * sd.spp)
+        dev_ms += r.stats.device_ms
+        launches += r.stats.launches
+        if r.stats.error_word:
+            raise RuntimeError(f"device error word {r.stats.error_word}")
+    ctx.synchronize()
+    wall = time.time() - wall0
+    clk = clocks.stop()
+    barrier(dist)
+    dev_ms_max = max_over_ranks(dist, dev_ms)
+    value = ws * args.steps * samples / (dev_ms_max / 1e3) / 1e6
+
+    # end to end through the C ABI with a host film buffer (read back every step)
+    barrier(dist)
+    t0 = time.time()
+    for k in range(args.steps):
+        pi.render(scene, readback=True, first_sample=k * sd.spp)
+    e2e_s = max_over_ranks(dist, time.time() - t0)
+    e2e = ws * args.steps * samples / e2e_s / 1e6
+
+    # stage timing pass (outside the timed region): dominant-kernel duration and ray counts
+    o = A.bg_render_opts()
+    ctx.flush_l2()
+    import ctypes as C
+    cam = G.camera_struct(sd.camera)
+    o.spp, o.max_depth, o.rr_threshold, o.mode, o.seed = sd.spp, sd.max_depth, sd.rr_threshold, A.BG_MODE_PBRT, 0
+    o.flags = A.BG_RENDER_NO_READBACK | A.BG_RENDER_STAGE_TIMING
+    st = A.bg_render_stats()
+    ctx.check(ctx.lib.bg_render(ctx.h, scene.h, C.byref(cam), C.byref(o), None, C.byref(st)))
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    roof = {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
+            "kernel": "k_extend (closest-hit, 2-wide BVH)", "peak_source": peak_kind}
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        orc, rows, nsamples, build_s = cpu_sample(sd, args.cpu_seconds, threads)
+        counts = traversal_counts(orc, sd)
+        bpr = 32 + 8 + 32 * counts["V_ext"] + 40 * counts["T_ext"]
+        achieved = st.extension_rays * bpr / (st.trace_ms / 1e3) / 1e9
+        roof.update({"achieved": achieved, "frac": achieved / peak, "bytes_per_ray": bpr, **counts})
+        cv, cdt = time_cpu(orc, sd, rows, nsamples, threads)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"rows 0..{sd.camera.height} step {rows[2]} x {sd.camera.width} px x {sd.spp} spp "
+                         f"= {nsamples} samples in {cdt:.1f} s (oracle/, PBRT mode, bucket-fixed BVH)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
+        "config": config_of(sd, args.small),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
+                "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "extra": {"wall_s_timed_loop": wall, "scene_upload_and_bvh_build_s": upload_build_s,
+                  "bvh_build_ms": scene.build_ms, "bvh_nodes": int(scene.nodes),
+                  "extension_rays_per_frame": int(st.extension_rays), "shadow_rays_per_frame": int(st.shadow_rays),
+                  "Mrays_per_s": (st.extension_rays + st.shadow_rays) / (st.device_ms / 1e3) / 1e6,
+                  "stage_ms": {"extend": st.trace_ms, "shade": st.shade_ms, "shadow": st.shadow_ms,
+                               "total": st.device_ms}},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

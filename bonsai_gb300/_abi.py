@@ -1,0 +1,150 @@
+"""ctypes mirror of include/bonsai_gpu.h (the C ABI of libbonsai_gpu.so).
+
+The structures here must match the header field for field; tests/test_abi.py checks sizes and the
+exported symbol list.  Nothing here computes: it loads the in-tree shared library and declares the
+signatures.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "lib" / "libbonsai_gpu.so"
+
+BG_OK = 0
+BG_ERR_INVALID = 1
+BG_ERR_CUDA = 2
+BG_ERR_OOM = 3
+BG_ERR_TIMEOUT = 4
+BG_ERR_DEVICE = 5
+BG_ERR_UNSUPPORTED = 6
+BG_ERR_NO_DEVICE = 7
+
+BG_MODE_REF_COMPAT = 0
+BG_MODE_PBRT = 1
+
+BG_MAT_MATTE = 0
+BG_MAT_PLASTIC = 1
+BG_MAT_CONDUCTOR = 2
+BG_MAT_DIELECTRIC = 3
+
+BG_BVH_WIDE = 0
+BG_BVH_REFERENCE = 1
+BG_BVH_REFERENCE_FIXED = 2
+
+BG_RENDER_ACCUMULATE = 1
+BG_RENDER_NO_READBACK = 2
+BG_RENDER_GRAPH = 4
+BG_RENDER_STAGE_TIMING = 8
+
+F3 = C.c_float * 3
+
+
+class bg_material(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("kd", F3), ("ks", F3), ("roughness", C.c_float),
+                ("remap_roughness", C.c_uint32), ("eta", F3), ("k", F3), ("ior", C.c_float)]
+
+
+class bg_area_light(C.Structure):
+    _fields_ = [("intensity", F3), ("two_sided", C.c_uint32)]
+
+
+class bg_sphere(C.Structure):
+    _fields_ = [("center", F3), ("radius", C.c_float), ("material_id", C.c_uint32),
+                ("light_id", C.c_int32)]
+
+
+class bg_camera(C.Structure):
+    _fields_ = [("position", F3), ("look_at", F3), ("up", F3), ("fov_deg", C.c_float),
+                ("near_plane", C.c_float), ("far_plane", C.c_float), ("lens_radius", C.c_float),
+                ("focal_distance", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class bg_render_opts(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("rr_threshold", C.c_float),
+                ("mode", C.c_uint32), ("seed", C.c_uint64), ("first_sample", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class bg_render_stats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("trace_ms", C.c_double), ("shadow_ms", C.c_double),
+                ("shade_ms", C.c_double), ("samples", C.c_uint64), ("extension_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("launches", C.c_uint64), ("nan_samples", C.c_uint64),
+                ("error_word", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class bg_ray(C.Structure):
+    _fields_ = [("org", F3), ("tmax", C.c_float), ("dir", F3), ("pad", C.c_float)]
+
+
+class bg_hit(C.Structure):
+    _fields_ = [("prim", C.c_int32), ("t", C.c_float)]
+
+
+class bg_device_opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_queue_paths", C.c_uint32),
+                ("memory_cap_bytes", C.c_uint64), ("block_size", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class bg_build_stats(C.Structure):
+    _fields_ = [("build_ms", C.c_double), ("nodes", C.c_uint64), ("prims", C.c_uint64),
+                ("device_bytes", C.c_uint64)]
+
+
+P = C.c_void_p
+PP = C.POINTER(C.c_void_p)
+ST = C.c_int  # bg_status
+
+# name -> (restype, argtypes); the C-ABI surface declared in include/bonsai_gpu.h
+SIGNATURES = {
+    "bg_create": (ST, [C.POINTER(bg_device_opts), PP]),
+    "bg_destroy": (None, [P]),
+    "bg_last_error": (C.c_char_p, [P]),
+    "bg_status_string": (C.c_char_p, [C.c_int]),
+    "bg_flush_l2": (ST, [P]),
+    "bg_synchronize": (ST, [P]),
+    "bg_scene_create": (ST, [P, PP]),
+    "bg_scene_destroy": (None, [P]),
+    "bg_scene_add_material": (ST, [P, C.POINTER(bg_material), C.POINTER(C.c_uint32)]),
+    "bg_scene_add_area_light": (ST, [P, C.POINTER(bg_area_light), C.POINTER(C.c_uint32)]),
+    "bg_scene_add_triangles": (ST, [P, P, C.c_size_t, P, P]),
+    "bg_scene_add_spheres": (ST, [P, P, C.c_size_t]),
+    "bg_scene_commit": (ST, [P, C.c_uint32, C.POINTER(bg_build_stats)]),
+    "bg_render": (ST, [P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
+                       C.POINTER(bg_render_stats)]),
+    "bg_film_moments": (ST, [P, P, P, P]),
+    "bg_trace_closest": (ST, [P, P, P, C.c_size_t, P]),
+    "bg_trace_any": (ST, [P, P, P, C.c_size_t, P]),
+    "bg_trace_closest_device": (ST, [P, P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
+    "bg_trace_any_device": (ST, [P, P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
+    "bg_device_alloc": (ST, [P, C.c_size_t, PP]),
+    "bg_device_free": (ST, [P, P]),
+    "bg_memcpy_h2d": (ST, [P, P, P, C.c_size_t]),
+    "bg_memcpy_d2h": (ST, [P, P, P, C.c_size_t]),
+}
+
+_LIB = None
+
+
+def load(path: os.PathLike | str | None = None) -> C.CDLL:
+    """Load the in-tree libbonsai_gpu.so and declare every entry point.
+
+    Raises OSError when the library has not been built: there is no fallback path.
+    """
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise OSError(f"{p} is missing: build it with __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib

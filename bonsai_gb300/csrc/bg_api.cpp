@@ -1,0 +1,841 @@
+// bg_api.cpp - the C ABI of libbonsai_gpu.so (include/bonsai_gpu.h).
+//
+// Owns the CUDA context state (stream, events, device buffers with an optional memory cap),
+// the scene builder (host copies -> BVH build -> device upload) and the render driver that
+// replaces SamplerIntegrator::render (src/base/integrator.rs:35-133).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/bonsai_gpu.h"
+#include "bg_bvh.h"
+#include "bg_kernels.h"
+
+namespace {
+
+constexpr uint64_t kFaithfulMaxPrims = 200000;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct bg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t cap = 0, used = 0;
+    bg::LaunchShape shape{1, 128};
+    uint32_t max_queue = 1u << 22;
+    uint32_t* d_err = nullptr;
+    unsigned long long* d_counters = nullptr;
+    uint32_t* d_head = nullptr;
+    bg::FilmBuffers film{};
+    uint32_t film_w = 0, film_h = 0;
+    bg::WaveBuffers wave{};
+    std::vector<void*> wave_allocs;
+    std::vector<void*> film_allocs;
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    std::vector<void*> user;
+    std::unordered_map<void*, size_t> sizes;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    cudaEvent_t stage_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> timing_ev;
+    std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
+};
+
+struct bg_scene {
+    bg_ctx* ctx = nullptr;
+    std::vector<float> tri;
+    std::vector<uint32_t> tri_mat;
+    std::vector<int32_t> tri_light;
+    std::vector<bg_sphere> sph;
+    std::vector<bg_material> mats;
+    std::vector<bg_area_light> lights;
+    bool committed = false;
+    uint32_t kind = BG_BVH_WIDE;
+    bg::Scene dev{};
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+bg_status fail(bg_ctx* c, bg_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+bg_status cuda_fail(bg_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? BG_ERR_OOM : BG_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                               \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+bg_status dalloc(bg_ctx* ctx, size_t bytes, void** p, std::vector<void*>* owner) {
+    if (ctx->cap && ctx->used + bytes > ctx->cap)
+        return fail(ctx, BG_ERR_OOM, "device memory cap exceeded (" + std::to_string(ctx->used + bytes) + " > " +
+                                         std::to_string(ctx->cap) + " bytes)");
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc");
+    ctx->used += bytes;
+    ctx->sizes[*p] = bytes;
+    if (owner) owner->push_back(*p);
+    return BG_OK;
+}
+void dfree(bg_ctx* ctx, void* p) {
+    auto it = ctx->sizes.find(p);
+    if (it != ctx->sizes.end()) {
+        ctx->used -= it->second;
+        ctx->sizes.erase(it);
+    }
+    cudaFree(p);
+}
+void dfree_all(bg_ctx* ctx, std::vector<void*>& v) {
+    for (void* p : v) dfree(ctx, p);
+    v.clear();
+}
+template <class T>
+bg_status upload(bg_ctx* ctx, const std::vector<T>& h, const T** d, std::vector<void*>* owner) {
+    void* p = nullptr;
+    bg_status s = dalloc(ctx, h.size() * sizeof(T), &p, owner);
+    if (s != BG_OK) return s;
+    if (!h.empty()) {
+        cudaError_t e = cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpyAsync");
+    }
+    *d = static_cast<const T*>(p);
+    return BG_OK;
+}
+
+// ---- camera transforms (src/base/transform.rs, src/cameras/perspective.rs:49-113), f32
+struct M4 {
+    float m[4][4];
+};
+M4 ident() {
+    M4 r{};
+    for (int i = 0; i < 4; ++i) r.m[i][i] = 1.0f;
+    return r;
+}
+M4 mul(const M4& a, const M4& b) {
+    M4 r{};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j] + a.m[i][3] * b.m[3][j];
+    return r;
+}
+M4 inverse(const M4& in) {  // Gauss-Jordan with full pivoting (mat4.rs:72-140)
+    float a[4][4];
+    std::memcpy(a, in.m, sizeof(a));
+    int ic[4] = {0}, ir[4] = {0}, piv[4] = {0};
+    for (int i = 0; i < 4; ++i) {
+        int row = 0, col = 0;
+        float big = 0.0f;
+        for (int j = 0; j < 4; ++j)
+            if (piv[j] != 1)
+                for (int k = 0; k < 4; ++k)
+                    if (piv[k] == 0 && std::fabs(a[j][k]) >= big) {
+                        big = std::fabs(a[j][k]);
+                        row = j;
+                        col = k;
+                    }
+        piv[col] += 1;
+        if (row != col)
+            for (int k = 0; k < 4; ++k) std::swap(a[row][k], a[col][k]);
+        ir[i] = row;
+        ic[i] = col;
+        float pinv = 1.0f / a[col][col];
+        a[col][col] = 1.0f;
+        for (int j = 0; j < 4; ++j) a[col][j] *= pinv;
+        for (int j = 0; j < 4; ++j)
+            if (j != col) {
+                float save = a[j][col];
+                a[j][col] = 0.0f;
+                for (int k = 0; k < 4; ++k) a[j][k] -= a[col][k] * save;
+            }
+    }
+    for (int j = 3; j >= 0; --j)
+        if (ir[j] != ic[j])
+            for (int k = 0; k < 4; ++k) std::swap(a[k][ir[j]], a[k][ic[j]]);
+    M4 r;
+    std::memcpy(r.m, a, sizeof(a));
+    return r;
+}
+struct Xf {
+    M4 m, mi;
+};
+Xf xmul(const Xf& a, const Xf& b) { return {mul(a.m, b.m), mul(b.mi, a.mi)}; }
+Xf xinv(const Xf& a) { return {a.mi, a.m}; }
+Xf xscale(float x, float y, float z) {
+    Xf t{ident(), ident()};
+    t.m.m[0][0] = x;
+    t.m.m[1][1] = y;
+    t.m.m[2][2] = z;
+    t.mi.m[0][0] = 1.0f / x;
+    t.mi.m[1][1] = 1.0f / y;
+    t.mi.m[2][2] = 1.0f / z;
+    return t;
+}
+Xf xtranslate(float x, float y, float z) {
+    Xf t{ident(), ident()};
+    t.m.m[0][3] = x;
+    t.m.m[1][3] = y;
+    t.m.m[2][3] = z;
+    t.mi.m[0][3] = -x;
+    t.mi.m[1][3] = -y;
+    t.mi.m[2][3] = -z;
+    return t;
+}
+struct F3 {
+    float x, y, z;
+};
+F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+float len(F3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+F3 nrm(F3 a) {
+    float inv = 1.0f / len(a);
+    return {a.x * inv, a.y * inv, a.z * inv};
+}
+F3 crs(F3 a, F3 b) {  // vec3.rs:108-122 (f64 products, rounded once)
+    double x = a.x, y = a.y, z = a.z, vx = b.x, vy = b.y, vz = b.z;
+    return {(float)(y * vz - z * vy), (float)(z * vx - x * vz), (float)(x * vy - y * vx)};
+}
+bg::Camera make_camera(const bg_camera& c) {
+    bg::Camera out{};
+    float rx = (float)c.width, ry = (float)c.height;
+    // Transform::perspective (transform.rs:48-73)
+    M4 p = ident();
+    float f = c.far_plane, n = c.near_plane;
+    p.m[2][2] = f / (f - n);
+    p.m[2][3] = -f * n / (f - n);
+    p.m[3][2] = 1.0f;
+    p.m[3][3] = 0.0f;
+    float inv_tan = 1.0f / std::tan(c.fov_deg * (3.14159265358979323846f / 180.0f) / 2.0f);
+    Xf c2s = xmul(xscale(inv_tan, inv_tan, 1.0f), Xf{p, inverse(p)});
+    float sx0, sx1, sy0, sy1, frame = rx / ry;
+    if (frame > 1.0f) {
+        sx0 = -frame; sx1 = frame; sy0 = -1.0f; sy1 = 1.0f;
+    } else {
+        sx0 = -1.0f; sx1 = 1.0f; sy0 = -1.0f / frame; sy1 = 1.0f / frame;
+    }
+    Xf s2r = xmul(xmul(xscale(rx, ry, 1.0f), xscale(1.0f / (sx1 - sx0), 1.0f / (sy0 - sy1), 1.0f)),
+                  xtranslate(-sx0, -sy1, 0.0f));
+    Xf r2c = xmul(xinv(c2s), xinv(s2r));
+    std::memcpy(out.r2c, r2c.m.m, sizeof(out.r2c));
+    // Transform::look_at (transform.rs:152-189) = camera_to_world
+    M4 cw = ident();
+    F3 pos{c.position[0], c.position[1], c.position[2]}, look{c.look_at[0], c.look_at[1], c.look_at[2]};
+    F3 up{c.up[0], c.up[1], c.up[2]};
+    cw.m[0][3] = pos.x;
+    cw.m[1][3] = pos.y;
+    cw.m[2][3] = pos.z;
+    cw.m[3][3] = 1.0f;
+    F3 dir = nrm(sub(look, pos));
+    if (len(crs(nrm(up), dir)) != 0.0f) {
+        F3 right = nrm(crs(nrm(up), dir));
+        F3 nup = crs(dir, right);
+        cw.m[0][0] = right.x; cw.m[1][0] = right.y; cw.m[2][0] = right.z; cw.m[3][0] = 0.0f;
+        cw.m[0][1] = nup.x; cw.m[1][1] = nup.y; cw.m[2][1] = nup.z; cw.m[3][1] = 0.0f;
+        cw.m[0][2] = dir.x; cw.m[1][2] = dir.y; cw.m[2][2] = dir.z; cw.m[3][2] = 0.0f;
+    } else {
+        cw = ident();
+    }
+    std::memcpy(out.c2w, cw.m, sizeof(out.c2w));
+    out.width = c.width;
+    out.height = c.height;
+    return out;
+}
+
+// TrowbridgeReitzDistribution::roughness_to_alpha (src/base/microfacet.rs:45-53)
+float roughness_to_alpha(float r) {
+    r = std::fmax(r, 1e-3f);
+    float x = std::log(r);
+    return 1.62142f + 0.819955f * x + 0.1734f * x * x + 0.0171201f * x * x * x + 0.000640711f * x * x * x * x;
+}
+
+bg_status ensure_film(bg_ctx* ctx, uint32_t w, uint32_t h) {
+    if (ctx->film_w == w && ctx->film_h == h && ctx->film.sum) return BG_OK;
+    dfree_all(ctx, ctx->film_allocs);
+    ctx->film = bg::FilmBuffers{};
+    ctx->film_w = ctx->film_h = 0;
+    size_t npix = (size_t)w * h;
+    void *a, *b, *c, *d, *e;
+    bg_status s;
+    if ((s = dalloc(ctx, npix * 3 * sizeof(double), &a, &ctx->film_allocs)) != BG_OK) return s;
+    if ((s = dalloc(ctx, npix * 3 * sizeof(double), &b, &ctx->film_allocs)) != BG_OK) return s;
+    if ((s = dalloc(ctx, npix * sizeof(uint32_t), &c, &ctx->film_allocs)) != BG_OK) return s;
+    if ((s = dalloc(ctx, npix * 3 * sizeof(float), &d, &ctx->film_allocs)) != BG_OK) return s;
+    if ((s = dalloc(ctx, sizeof(unsigned long long), &e, &ctx->film_allocs)) != BG_OK) return s;
+    ctx->film.sum = (double*)a;
+    ctx->film.sumsq = (double*)b;
+    ctx->film.count = (uint32_t*)c;
+    ctx->film.rgb = (float*)d;
+    ctx->film.nan_count = (unsigned long long*)e;
+    ctx->film.npix = (uint32_t)npix;
+    ctx->film_w = w;
+    ctx->film_h = h;
+    bg::launch_clear_film(ctx->film, ctx->stream);
+    CK(cudaMemsetAsync(e, 0, sizeof(unsigned long long), ctx->stream));
+    return BG_OK;
+}
+
+bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
+    if (ctx->wave.capacity >= cap && ctx->wave.ray_o) return BG_OK;
+    dfree_all(ctx, ctx->wave_allocs);
+    ctx->wave = bg::WaveBuffers{};
+    bg::WaveBuffers& w = ctx->wave;
+    auto get = [&](size_t bytes, void** p) { return dalloc(ctx, bytes, p, &ctx->wave_allocs); };
+    bg_status s;
+    size_t n = cap;
+#define WB(field, bytes)                                   \
+    do {                                                   \
+        void* p_;                                          \
+        if ((s = get((bytes), &p_)) != BG_OK) return s;    \
+        w.field = (decltype(w.field))p_;                   \
+    } while (0)
+    WB(ray_o, n * sizeof(float4));
+    WB(ray_d, n * sizeof(float4));
+    WB(hit, n * sizeof(int2));
+    WB(pixel, n * sizeof(uint32_t));
+    WB(sample, n * sizeof(uint32_t));
+    WB(state, n * sizeof(uint32_t));
+    WB(beta, n * sizeof(float4));
+    WB(L, n * sizeof(float4));
+    WB(nee_beta, n * sizeof(float4));
+    WB(pending, 2 * n * sizeof(float4));
+    WB(sh_o, 2 * n * sizeof(float4));
+    WB(sh_d, 2 * n * sizeof(float4));
+    WB(sh_ref, 2 * n * sizeof(uint32_t));
+    WB(queue[0], n * sizeof(uint32_t));
+    WB(queue[1], n * sizeof(uint32_t));
+    WB(done, n * sizeof(uint32_t));
+    WB(counters, 16 * sizeof(uint32_t));
+    WB(ray_stats, 4 * sizeof(unsigned long long));
+#undef WB
+    w.capacity = cap;
+    return BG_OK;
+}
+
+bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (word) *word = e;
+    if (e) {
+        CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream));
+        return fail(ctx, BG_ERR_DEVICE, "device error word 0x" + std::to_string(e) +
+                                            " (1 stack overflow, 2 queue overflow, 4 bad prim, 8 bad node)");
+    }
+    return BG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bg_status_string(bg_status s) {
+    switch (s) {
+        case BG_OK: return "ok";
+        case BG_ERR_INVALID: return "invalid argument";
+        case BG_ERR_CUDA: return "CUDA error";
+        case BG_ERR_OOM: return "out of device memory";
+        case BG_ERR_TIMEOUT: return "device wait timed out";
+        case BG_ERR_DEVICE: return "device-side error";
+        case BG_ERR_UNSUPPORTED: return "unsupported";
+        case BG_ERR_NO_DEVICE: return "no usable CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* bg_last_error(const bg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+bg_status bg_create(const bg_device_opts* opts, bg_ctx** out) {
+    if (!out) return BG_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return BG_ERR_NO_DEVICE;
+    }
+    bg_ctx* ctx = new bg_ctx();
+    ctx->device = opts ? opts->device : 0;
+    if (ctx->device < 0 || ctx->device >= ndev) {
+        delete ctx;
+        return BG_ERR_INVALID;
+    }
+    if (opts) {
+        ctx->cap = opts->memory_cap_bytes;
+        if (opts->max_queue_paths) ctx->max_queue = opts->max_queue_paths;
+        if (opts->block_size) ctx->shape.block = (int)opts->block_size;
+    }
+    auto bail = [&](cudaError_t e) {
+        bg_status s = (e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidDevice) ? BG_ERR_NO_DEVICE
+                                                                                             : BG_ERR_CUDA;
+        bg_destroy(ctx);
+        return s;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(ctx->device)) != cudaSuccess) return bail(e);
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, ctx->device)) != cudaSuccess) return bail(e);
+    ctx->shape.sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&ctx->ev_begin)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&ctx->ev_end)) != cudaSuccess) return bail(e);
+    for (auto& ev : ctx->stage_ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e);
+    void* p;
+    if (dalloc(ctx, 64, &p, &ctx->user) != BG_OK) return bail(cudaErrorMemoryAllocation);
+    ctx->d_err = (uint32_t*)p;
+    ctx->d_counters = (unsigned long long*)((char*)p + 16);
+    ctx->d_head = (uint32_t*)((char*)p + 32);
+    if ((e = cudaMemsetAsync(p, 0, 64, ctx->stream)) != cudaSuccess) return bail(e);
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bail(e);
+    *out = ctx;
+    return BG_OK;
+}
+
+void bg_destroy(bg_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (bg_scene* s : ctx->scenes) {  // scenes outliving their context keep only host state
+        dfree_all(ctx, s->allocs);
+        s->ctx = nullptr;
+        s->committed = false;
+    }
+    ctx->scenes.clear();
+    dfree_all(ctx, ctx->wave_allocs);
+    dfree_all(ctx, ctx->film_allocs);
+    dfree_all(ctx, ctx->user);
+    if (ctx->flush) cudaFree(ctx->flush);
+    if (ctx->ev_begin) cudaEventDestroy(ctx->ev_begin);
+    if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
+    for (auto ev : ctx->stage_ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto ev : ctx->timing_ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+bg_status bg_synchronize(bg_ctx* ctx) {
+    if (!ctx) return BG_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BG_OK;
+}
+
+bg_status bg_flush_l2(bg_ctx* ctx) {
+    if (!ctx) return BG_ERR_INVALID;
+    if (!ctx->flush) {
+        ctx->flush_bytes = (size_t)512 << 20;  // > 4x the 129 MB L2
+        CK(cudaMalloc(&ctx->flush, ctx->flush_bytes));
+    }
+    static unsigned char v = 0;
+    CK(cudaMemsetAsync(ctx->flush, ++v, ctx->flush_bytes, ctx->stream));
+    return BG_OK;
+}
+
+bg_status bg_device_alloc(bg_ctx* ctx, size_t bytes, void** p) {
+    if (!ctx || !p) return BG_ERR_INVALID;
+    return dalloc(ctx, bytes, p, &ctx->user);
+}
+bg_status bg_device_free(bg_ctx* ctx, void* p) {
+    if (!ctx) return BG_ERR_INVALID;
+    auto it = std::find(ctx->user.begin(), ctx->user.end(), p);
+    if (it == ctx->user.end()) return fail(ctx, BG_ERR_INVALID, "pointer was not allocated by bg_device_alloc");
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, p);
+    ctx->user.erase(it);
+    return BG_OK;
+}
+bg_status bg_memcpy_h2d(bg_ctx* ctx, void* d, const void* h, size_t bytes) {
+    if (!ctx) return BG_ERR_INVALID;
+    CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BG_OK;
+}
+bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h, const void* d, size_t bytes) {
+    if (!ctx) return BG_ERR_INVALID;
+    CK(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BG_OK;
+}
+
+// ---------------------------------------------------------------- scene
+bg_status bg_scene_create(bg_ctx* ctx, bg_scene** out) {
+    if (!ctx || !out) return BG_ERR_INVALID;
+    *out = new bg_scene();
+    (*out)->ctx = ctx;
+    ctx->scenes.insert(*out);
+    return BG_OK;
+}
+
+void bg_scene_destroy(bg_scene* s) {
+    if (!s) return;
+    if (s->ctx) {
+        bg_ctx* ctx = s->ctx;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        dfree_all(ctx, s->allocs);
+        ctx->scenes.erase(s);
+    }
+    delete s;
+}
+
+bg_status bg_scene_add_material(bg_scene* s, const bg_material* m, uint32_t* id) {
+    if (!s || !m) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    if (m->type > BG_MAT_DIELECTRIC) return fail(s->ctx, BG_ERR_INVALID, "unknown material type");
+    if (m->type == BG_MAT_DIELECTRIC && !(m->ior > 0.0f))
+        return fail(s->ctx, BG_ERR_INVALID, "dielectric ior must be > 0");
+    s->mats.push_back(*m);
+    if (id) *id = (uint32_t)(s->mats.size() - 1);
+    return BG_OK;
+}
+
+bg_status bg_scene_add_area_light(bg_scene* s, const bg_area_light* l, uint32_t* id) {
+    if (!s || !l) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    s->lights.push_back(*l);
+    if (id) *id = (uint32_t)(s->lights.size() - 1);
+    return BG_OK;
+}
+
+bg_status bg_scene_add_triangles(bg_scene* s, const float* xyz, size_t ntri, const uint32_t* mat,
+                                 const int32_t* light) {
+    if (!s || (ntri && (!xyz || !mat))) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    if (s->tri_mat.size() + ntri >= (1ull << 31)) return fail(s->ctx, BG_ERR_INVALID, "too many triangles");
+    for (size_t i = 0; i < ntri; ++i) {
+        if (mat[i] >= s->mats.size())
+            return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has an unknown material id");
+        if (light && light[i] >= 0 && (size_t)light[i] >= s->lights.size())
+            return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has an unknown light id");
+        for (int k = 0; k < 9; ++k)
+            if (!std::isfinite(xyz[9 * i + k]))
+                return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has a non-finite vertex");
+    }
+    s->tri.insert(s->tri.end(), xyz, xyz + 9 * ntri);
+    s->tri_mat.insert(s->tri_mat.end(), mat, mat + ntri);
+    for (size_t i = 0; i < ntri; ++i) s->tri_light.push_back(light ? light[i] : -1);
+    return BG_OK;
+}
+
+bg_status bg_scene_add_spheres(bg_scene* s, const bg_sphere* sp, size_t n) {
+    if (!s || (n && !sp)) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    for (size_t i = 0; i < n; ++i) {
+        if (sp[i].material_id >= s->mats.size()) return fail(s->ctx, BG_ERR_INVALID, "sphere has an unknown material id");
+        if (sp[i].light_id >= 0)
+            return fail(s->ctx, BG_ERR_UNSUPPORTED, "spherical area lights are not supported");
+        if (!(sp[i].radius > 0.0f) || !std::isfinite(sp[i].radius))
+            return fail(s->ctx, BG_ERR_INVALID, "sphere radius must be finite and > 0");
+    }
+    s->sph.insert(s->sph.end(), sp, sp + n);
+    return BG_OK;
+}
+
+bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
+    if (!s) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    bg_ctx* ctx = s->ctx;
+    if (s->committed) return fail(ctx, BG_ERR_INVALID, "scene already committed");
+    if (kind > BG_BVH_REFERENCE_FIXED) return fail(ctx, BG_ERR_INVALID, "unknown BVH kind");
+    auto t0 = std::chrono::steady_clock::now();
+    CK(cudaSetDevice(ctx->device));
+    const uint32_t ntri = (uint32_t)s->tri_mat.size(), nsph = (uint32_t)s->sph.size();
+    bg::HostPrims hp{s->tri.data(), ntri, s->sph.data(), nsph};
+    // triangles as float4 triplets with material / emission / light-index tags
+    std::vector<float4> tri4(3 * (size_t)ntri);
+    std::vector<uint32_t> light_prims;
+    for (uint32_t i = 0; i < ntri; ++i) {
+        const float* v = &s->tri[9 * (size_t)i];
+        int32_t li = -1;
+        if (s->tri_light[i] >= 0) {
+            li = (int32_t)light_prims.size();
+            light_prims.push_back(i);
+        }
+        uint32_t m = s->tri_mat[i];
+        int32_t e = s->tri_light[i];
+        float4 a = make_float4(v[0], v[1], v[2], 0.0f), b = make_float4(v[3], v[4], v[5], 0.0f),
+               c = make_float4(v[6], v[7], v[8], 0.0f);
+        std::memcpy(&a.w, &m, 4);
+        std::memcpy(&b.w, &e, 4);
+        std::memcpy(&c.w, &li, 4);
+        tri4[3 * i] = a;
+        tri4[3 * i + 1] = b;
+        tri4[3 * i + 2] = c;
+    }
+    std::vector<float4> sph4(nsph);
+    std::vector<uint32_t> sph_mat(nsph);
+    for (uint32_t i = 0; i < nsph; ++i) {
+        sph4[i] = make_float4(s->sph[i].center[0], s->sph[i].center[1], s->sph[i].center[2], s->sph[i].radius);
+        sph_mat[i] = s->sph[i].material_id;
+    }
+    std::vector<bg::Material> mats(s->mats.size());
+    for (size_t i = 0; i < mats.size(); ++i) {
+        const bg_material& m = s->mats[i];
+        bg::Material& d = mats[i];
+        d.type = m.type;
+        std::memcpy(d.kd, m.kd, sizeof(d.kd));
+        std::memcpy(d.ks, m.ks, sizeof(d.ks));
+        float a = m.roughness;
+        if (m.type == BG_MAT_PLASTIC && m.remap_roughness) a = roughness_to_alpha(a);
+        d.alpha = std::fmax(a, 0.001f);  // TrowbridgeReitzDistribution::new (microfacet.rs:38-43)
+        std::memcpy(d.eta, m.eta, sizeof(d.eta));
+        std::memcpy(d.k, m.k, sizeof(d.k));
+        d.ior = m.ior;
+        d.pad = 0;
+    }
+    std::vector<bg::Emission> emis(s->lights.size());
+    for (size_t i = 0; i < emis.size(); ++i) {
+        std::memcpy(emis[i].intensity, s->lights[i].intensity, sizeof(emis[i].intensity));
+        emis[i].two_sided = s->lights[i].two_sided;
+    }
+    bg::Scene& d = s->dev;
+    d = bg::Scene{};
+    d.ntri = ntri;
+    d.nsph = nsph;
+    d.nlights = (uint32_t)light_prims.size();
+    bg_status st;
+    if ((st = upload(ctx, tri4, &d.tri, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, sph4, &d.sph, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, sph_mat, &d.sph_mat, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, mats, &d.mats, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, emis, &d.emis, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, light_prims, &d.light_prims, &s->allocs)) != BG_OK) return st;
+    uint64_t nodes = 0;
+    if (kind == BG_BVH_WIDE) {
+        bg::Bvh2 b;
+        bg::build_bvh2(hp, &b, 0);
+        if ((st = upload(ctx, b.nodes, (const bg::Bvh2Node**)&d.nodes, &s->allocs)) != BG_OK) return st;
+        if ((st = upload(ctx, b.leaf_prims, &d.leaf_prims, &s->allocs)) != BG_OK) return st;
+        d.n_nodes = (uint32_t)b.nodes.size();
+        nodes = b.nodes.size();
+    } else {
+        bg::RefBvh r;
+        if (!bg::build_reference_bvh(hp, kind == BG_BVH_REFERENCE, &r, kFaithfulMaxPrims))
+            return fail(ctx, BG_ERR_UNSUPPORTED,
+                        "the reference's chain-shaped BVH build is limited to " + std::to_string(kFaithfulMaxPrims) +
+                            " primitives; use BG_BVH_REFERENCE_FIXED");
+        if ((st = upload(ctx, r.nodes, &d.ref_nodes, &s->allocs)) != BG_OK) return st;
+        if ((st = upload(ctx, r.order, &d.ref_order, &s->allocs)) != BG_OK) return st;
+        d.ref_nnodes = (uint32_t)r.nodes.size();
+        nodes = r.nodes.size();
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    s->kind = kind;
+    s->committed = true;
+    if (stats) {
+        stats->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->nodes = nodes;
+        stats->prims = (uint64_t)ntri + nsph;
+        uint64_t bytes = tri4.size() * 16 + sph4.size() * 16 + nodes * (kind == BG_BVH_WIDE ? 64 : 32) +
+                ((uint64_t)ntri + nsph) * (kind == BG_BVH_WIDE ? 48 : 4);
+        stats->device_bytes = bytes;
+    }
+    return BG_OK;
+}
+
+// ---------------------------------------------------------------- ray queries
+static bg_status trace_device(bg_ctx* ctx, const bg_scene* s, const bg_ray* d_rays, size_t n, bg_hit* d_hits,
+                              uint8_t* d_occ, bool any, float* ms) {
+    if (!ctx || !s || !s->committed || s->ctx != ctx) return fail(ctx, BG_ERR_INVALID, "scene not committed on this context");
+    if (n >= (1ull << 31)) return fail(ctx, BG_ERR_INVALID, "too many rays");
+    CK(cudaSetDevice(ctx->device));
+    if (n == 0) {
+        if (ms) *ms = 0.0f;
+        return BG_OK;
+    }
+    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+    bg::launch_trace(s->dev, s->kind != BG_BVH_WIDE, any, d_rays, n, d_hits, d_occ, ctx->d_err, nullptr, ctx->d_head,
+                     ctx->shape, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    bg_status st = check_device_error(ctx, nullptr);
+    if (st != BG_OK) return st;
+    if (ms) CK(cudaEventElapsedTime(ms, ctx->ev_begin, ctx->ev_end));
+    return BG_OK;
+}
+
+bg_status bg_trace_closest_device(bg_ctx* ctx, const bg_scene* s, const bg_ray* d_rays, size_t n, bg_hit* d_hits,
+                                  float* ms) {
+    if (!ctx || (n && (!d_rays || !d_hits))) return BG_ERR_INVALID;
+    return trace_device(ctx, s, d_rays, n, d_hits, nullptr, false, ms);
+}
+bg_status bg_trace_any_device(bg_ctx* ctx, const bg_scene* s, const bg_ray* d_rays, size_t n, uint8_t* d_occ,
+                              float* ms) {
+    if (!ctx || (n && (!d_rays || !d_occ))) return BG_ERR_INVALID;
+    return trace_device(ctx, s, d_rays, n, nullptr, d_occ, true, ms);
+}
+
+static bg_status trace_host(bg_ctx* ctx, const bg_scene* s, const bg_ray* rays, size_t n, void* out, bool any) {
+    if (!ctx || !s || (n && (!rays || !out))) return BG_ERR_INVALID;
+    if (n == 0) return BG_OK;
+    CK(cudaSetDevice(ctx->device));
+    void *dr = nullptr, *dh = nullptr;
+    std::vector<void*> tmp;
+    bg_status st = dalloc(ctx, n * sizeof(bg_ray), &dr, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * (any ? 1 : sizeof(bg_hit)), &dh, &tmp);
+    if (st == BG_OK) {
+        cudaError_t e = cudaMemcpyAsync(dr, rays, n * sizeof(bg_ray), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMemcpyAsync");
+    }
+    if (st == BG_OK) st = trace_device(ctx, s, (const bg_ray*)dr, n, any ? nullptr : (bg_hit*)dh,
+                                       any ? (uint8_t*)dh : nullptr, any, nullptr);
+    if (st == BG_OK) {
+        cudaError_t e = cudaMemcpyAsync(out, dh, n * (any ? 1 : sizeof(bg_hit)), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMemcpyAsync");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    return st;
+}
+
+bg_status bg_trace_closest(bg_ctx* ctx, const bg_scene* s, const bg_ray* rays, size_t n, bg_hit* hits) {
+    return trace_host(ctx, s, rays, n, hits, false);
+}
+bg_status bg_trace_any(bg_ctx* ctx, const bg_scene* s, const bg_ray* rays, size_t n, uint8_t* occ) {
+    return trace_host(ctx, s, rays, n, occ, true);
+}
+
+// ---------------------------------------------------------------- render
+bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o, float* rgb_out,
+                    bg_render_stats* stats) {
+    if (!ctx || !s || !cam || !o) return BG_ERR_INVALID;
+    if (!s->committed || s->ctx != ctx) return fail(ctx, BG_ERR_INVALID, "scene not committed on this context");
+    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height >= (1ull << 31))
+        return fail(ctx, BG_ERR_INVALID, "bad film resolution");
+    if (cam->lens_radius != 0.0f) return fail(ctx, BG_ERR_UNSUPPORTED, "thin-lens cameras are not supported");
+    if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) return fail(ctx, BG_ERR_INVALID, "fov out of range");
+    if (o->mode > BG_MODE_PBRT) return fail(ctx, BG_ERR_INVALID, "unknown mode");
+    if (o->mode == BG_MODE_REF_COMPAT && s->kind == BG_BVH_WIDE)
+        return fail(ctx, BG_ERR_INVALID, "REF_COMPAT rendering needs a BG_BVH_REFERENCE* scene layout");
+    if (o->max_depth > 250) return fail(ctx, BG_ERR_INVALID, "max_depth must be <= 250");
+    if (!(o->flags & BG_RENDER_NO_READBACK) && !rgb_out) return BG_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    bg_status st;
+    if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
+    if (!(o->flags & BG_RENDER_ACCUMULATE)) {
+        bg::launch_clear_film(ctx->film, ctx->stream);
+        CK(cudaMemsetAsync(ctx->film.nan_count, 0, sizeof(unsigned long long), ctx->stream));
+    }
+    bg::Camera dc = make_camera(*cam);
+    bg::RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
+    const uint64_t npix = (uint64_t)cam->width * cam->height;
+    const uint64_t total = npix * o->spp;
+    uint64_t launches = 0;
+    bool wavefront = (o->mode == BG_MODE_PBRT && s->kind == BG_BVH_WIDE);
+    uint32_t cap = 0;
+    if (wavefront) {
+        cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, std::max<uint64_t>(total, 1));
+        if ((st = ensure_wave(ctx, cap)) != BG_OK) return st;
+    }
+    const bool timing = wavefront && (o->flags & BG_RENDER_STAGE_TIMING);
+    const uint64_t nwaves = wavefront ? (total + cap - 1) / cap : 0;
+    const size_t ev_per_wave = 4 * ((size_t)o->max_depth + 1);
+    if (timing) {
+        while (ctx->timing_ev.size() < nwaves * ev_per_wave) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            ctx->timing_ev.push_back(e);
+        }
+    }
+    if (wavefront) CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+    if (total > 0) {
+        if (wavefront) {
+            uint64_t w = 0;
+            for (uint64_t item0 = 0; item0 < total; item0 += cap, ++w) {
+                uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, total - item0);
+                launches += bg::launch_wave(s->dev, dc, rp, ctx->film, ctx->wave, item0, nitems, ctx->d_err,
+                                            ctx->shape, ctx->stream,
+                                            timing ? ctx->timing_ev.data() + w * ev_per_wave : nullptr);
+            }
+        } else {
+            bg::launch_megakernel(o->mode == BG_MODE_REF_COMPAT, s->dev, dc, rp, ctx->film, ctx->d_err, ctx->shape,
+                                  ctx->stream);
+            launches += 1;
+        }
+    }
+    bg::launch_resolve(ctx->film, ctx->stream);
+    launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    uint32_t word = 0;
+    st = check_device_error(ctx, &word);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev_begin, ctx->ev_end);
+        stats->device_ms = ms;
+        stats->samples = total;
+        stats->launches = launches;
+        stats->error_word = word;
+        unsigned long long nan = 0;
+        cudaMemcpy(&nan, ctx->film.nan_count, sizeof(nan), cudaMemcpyDeviceToHost);
+        stats->nan_samples = nan;
+        if (wavefront) {
+            unsigned long long rs[2] = {0, 0};
+            cudaMemcpy(rs, ctx->wave.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
+            stats->extension_rays = rs[0];
+            stats->shadow_rays = rs[1];
+        }
+        if (timing) {
+            double ext = 0, shade = 0, shadow = 0;
+            for (uint64_t w = 0; w < nwaves; ++w) {
+                cudaEvent_t* e = ctx->timing_ev.data() + w * ev_per_wave;
+                for (uint32_t b = 0; b <= o->max_depth; ++b) {
+                    float a = 0, c = 0, d = 0;
+                    cudaEventElapsedTime(&a, e[4 * b], e[4 * b + 1]);
+                    cudaEventElapsedTime(&c, e[4 * b + 1], e[4 * b + 2]);
+                    cudaEventElapsedTime(&d, e[4 * b + 2], e[4 * b + 3]);
+                    ext += a;
+                    shade += c;
+                    shadow += d;
+                }
+            }
+            stats->trace_ms = ext;
+            stats->shade_ms = shade;
+            stats->shadow_ms = shadow;
+        }
+    }
+    if (st != BG_OK) return st;
+    if (!(o->flags & BG_RENDER_NO_READBACK)) {
+        CK(cudaMemcpyAsync(rgb_out, ctx->film.rgb, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return BG_OK;
+}
+
+bg_status bg_film_moments(bg_ctx* ctx, double* sum, double* sumsq, uint32_t* count) {
+    if (!ctx) return BG_ERR_INVALID;
+    if (!ctx->film.sum) return fail(ctx, BG_ERR_INVALID, "no film rendered yet");
+    CK(cudaSetDevice(ctx->device));
+    size_t npix = ctx->film.npix;
+    if (sum) CK(cudaMemcpyAsync(sum, ctx->film.sum, npix * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (sumsq)
+        CK(cudaMemcpyAsync(sumsq, ctx->film.sumsq, npix * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (count) CK(cudaMemcpyAsync(count, ctx->film.count, npix * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BG_OK;
+}
+
+}  // extern "C"

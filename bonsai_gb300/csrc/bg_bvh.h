@@ -1,0 +1,35 @@
+// bg_bvh.h - host BVH builders.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "../../include/bonsai_gpu.h"
+#include "bg_device.h"
+
+namespace bg {
+
+struct HostPrims {
+    const float* tri;        // 9 floats per triangle
+    uint32_t ntri;
+    const bg_sphere* sph;
+    uint32_t nsph;
+};
+
+// BVH::new (src/accelerators/bvh.rs:53-269): 16-bucket SAH, leaves of up to 256 primitives,
+// DFS-preorder flattening.  faithful = true keeps the bucket index `16 * (offset as usize)`
+// (bvh.rs:154-155, which only ever yields buckets 0 and 15); false uses floor(16 * offset).
+struct RefBvh {
+    std::vector<RefNode> nodes;
+    std::vector<uint32_t> order;
+};
+bool build_reference_bvh(const HostPrims& p, bool faithful, RefBvh* out, uint64_t max_prims_faithful);
+
+// The library's own 2-wide BVH: binned SAH (32 bins per axis), up to 8 primitives per leaf,
+// children ordered for a depth-first layout; leaf primitives copied in leaf order.
+struct Bvh2 {
+    std::vector<Bvh2Node> nodes;
+    std::vector<float4> leaf_prims;  // 3 per primitive
+};
+void build_bvh2(const HostPrims& p, Bvh2* out, int threads);
+
+}  // namespace bg

@@ -1,0 +1,87 @@
+// bg_device.h - device-resident scene layout shared by the host driver and the kernels.
+//
+// HBM layout (all arrays 16-byte aligned, read with 128-bit loads):
+//   tri[3*i+k]   float4 : triangle i vertex k in insertion order; w of k=0 = material id,
+//                         w of k=1 = emission record (int, -1 none), w of k=2 = light index or -1
+//   sph[i]       float4 : sphere center.xyz, radius; sph_mat[i] material id
+//   mats[m]      Material : constant-texture parameters, alpha already remapped/clamped
+//   ref_nodes    RefNode  : binary BVH in the reference's flattened DFS order (32 B/node)
+//   ref_order    uint32   : ordered_primitives of the reference build (prim ids)
+//   nodes        Bvh2Node : 2-wide BVH, both children's boxes in the parent (64 B/node)
+//   leaf_prims   float4x3 : primitives in leaf order (48 B each; triangle p0 p1 p2, or sphere
+//                           center/radius); w of the first float4 = prim id (bit 31: sphere)
+#pragma once
+#include <cstdint>
+
+#ifndef __CUDACC__
+#include <vector_types.h>
+#endif
+
+namespace bg {
+
+struct Material {
+    uint32_t type;  // bg_material_type
+    float kd[3];
+    float ks[3];
+    float alpha;    // TR alpha: max(roughness or roughness_to_alpha(roughness), 0.001)
+    float eta[3];
+    float k[3];
+    float ior;
+    uint32_t pad;
+};
+
+struct Emission {
+    float intensity[3];
+    uint32_t two_sided;
+};
+
+struct RefNode {   // BVHNode (src/accelerators/bvh.rs:25-31), flattened like BVH::flatten
+    float mn[3];
+    float mx[3];
+    uint32_t offset;      // primitive_offset (leaf) or second_child_offset (interior)
+    uint32_t count_axis;  // (count << 2) | axis; count 0 = interior
+};
+
+struct Bvh2Node {
+    float4 c0xy;   // child0 lo.x hi.x lo.y hi.y
+    float4 c1xy;   // child1 lo.x hi.x lo.y hi.y
+    float4 c01z;   // child0 lo.z hi.z, child1 lo.z hi.z
+    int4 child;    // x,y: >=0 inner node; <0: ~first leaf prim; z,w: leaf prim counts
+};
+
+struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-175)
+    float r2c[4][4];  // raster_to_camera.m
+    float c2w[4][4];  // camera_to_world.m
+    uint32_t width, height;
+};
+
+struct Scene {
+    const float4* tri;
+    uint32_t ntri;
+    uint32_t nsph;
+    const float4* sph;
+    const uint32_t* sph_mat;
+    const Material* mats;
+    const Emission* emis;
+    const uint32_t* light_prims;  // Scene::lights order: one DiffuseAreaLight per emitting triangle
+    uint32_t nlights;
+    uint32_t pad0;
+    const RefNode* ref_nodes;
+    const uint32_t* ref_order;
+    uint32_t ref_nnodes;
+    uint32_t n_nodes;
+    const Bvh2Node* nodes;
+    const float4* leaf_prims;
+};
+
+enum : uint32_t {
+    ERR_STACK_OVERFLOW = 1u,
+    ERR_QUEUE_OVERFLOW = 2u,
+    ERR_BAD_PRIM = 4u,
+    ERR_BAD_NODE = 8u,
+};
+
+constexpr uint32_t SPHERE_BIT = 0x80000000u;
+constexpr int TRAVERSAL_STACK = 64;
+
+}  // namespace bg

@@ -1,0 +1,522 @@
+// bg_kernels.cu - ray-query kernels, the per-path megakernel and the PBRT wavefront stages.
+//
+// Wavefront (PBRT mode, 2-wide BVH):  one wave = up to `capacity` (pixel, sample) paths.
+//   generate -> [prepare -> extend -> shade -> shadow -> finalize] x (max_depth + 1)
+// Queue sizes live in device memory; every stage launches a fixed persistent grid that reads its
+// own work count, so the chain needs no host synchronisation and can be captured in a CUDA graph.
+// Traversal stages pull 32-ray batches per warp from an atomic head (dynamic load balance);
+// queues are compacted with warp ballot + popc + one atomic per warp.
+//
+// Megakernel (both modes, reference-layout BVH): one thread per (pixel, sample) runs
+// PathIntegrator::radiance end to end; it is the REF_COMPAT path and a cross-check of the
+// wavefront in PBRT mode.
+#include "bg_kernels.h"
+#include "bg_shading.cuh"
+#include "bg_traverse.cuh"
+
+namespace bg {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+BG_D uint32_t lane_id() { return threadIdx.x & 31u; }
+
+BG_D uint32_t warp_fetch(uint32_t* head) {
+    uint32_t base = 0;
+    if (lane_id() == 0) base = atomicAdd(head, 32u);
+    return __shfl_sync(FULL, base, 0);
+}
+// Warp-aggregated append: every lane of the warp must call it; returns the slot of lanes with pred.
+BG_D uint32_t warp_append(uint32_t* counter, bool pred) {
+    uint32_t mask = __ballot_sync(FULL, pred);
+    if (mask == 0) return 0;
+    uint32_t leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(FULL, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane_id()) - 1u));
+}
+
+BG_D Ray load_ray(float4 o, float4 d) {
+    Ray r;
+    r.o = f4xyz(o);
+    r.t_max = o.w;
+    r.d = f4xyz(d);
+    r.time = d.w;
+    return r;
+}
+
+// FilmTile::add_sample with the box filter (r = 0.5: weight 1 to the sample's own pixel) after
+// the radiance sanity checks of SamplerIntegrator::render (src/base/integrator.rs:91-120).
+BG_D void film_add(const FilmBuffers& f, uint32_t pix, RGB L) {
+    float y = luminance(L);
+    if (is_nan(L) || y < -1e-5f || isinf(y)) {
+        L = rgb(0.0f);
+        atomicAdd(f.nan_count, 1ull);
+    }
+    double r = L.r, g = L.g, b = L.b;
+    atomicAdd(&f.sum[3 * pix + 0], r);
+    atomicAdd(&f.sum[3 * pix + 1], g);
+    atomicAdd(&f.sum[3 * pix + 2], b);
+    atomicAdd(&f.sumsq[3 * pix + 0], r * r);
+    atomicAdd(&f.sumsq[3 * pix + 1], g * g);
+    atomicAdd(&f.sumsq[3 * pix + 2], b * b);
+    atomicAdd(&f.count[pix], 1u);
+}
+
+// ================================================================ ray queries
+template <bool REF_LAYOUT, bool ANY>
+__global__ void __launch_bounds__(128) k_trace(Scene sc, const float4* rays, uint32_t n, int2* hits, uint8_t* occ,
+                                               uint32_t* err, unsigned long long* counters, uint32_t* head) {
+    for (;;) {
+        uint32_t base = warp_fetch(head);
+        if (base >= n) break;
+        uint32_t i = base + lane_id();
+        if (i < n) {
+            Ray ray = load_ray(__ldg(&rays[2 * i]), __ldg(&rays[2 * i + 1]));
+            ray.time = 0.0f;
+            int prim = REF_LAYOUT ? ref_traverse<ANY>(sc, ray, err, counters) : bvh2_traverse<ANY>(sc, ray, err);
+            if (ANY) occ[i] = prim >= 0 ? 1 : 0;
+            else hits[i] = make_int2(prim, __float_as_int(prim >= 0 ? ray.t_max : INFINITY));
+        }
+    }
+}
+
+void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,
+                  uint8_t* occluded, uint32_t* err, unsigned long long* counters, uint32_t* work_head,
+                  const LaunchShape& ls, cudaStream_t s) {
+    cudaMemsetAsync(work_head, 0, sizeof(uint32_t), s);
+    dim3 grid(ls.sms * 8), block(128);
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    int2* h = reinterpret_cast<int2*>(hits);
+    uint32_t nn = (uint32_t)n;
+    if (ref_layout) {
+        if (any) k_trace<true, true><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+        else k_trace<true, false><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+    } else {
+        if (any) k_trace<false, true><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+        else k_trace<false, false><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+    }
+}
+
+// ================================================================ megakernel (reference layout)
+// estimate_direct (src/base/integrator.rs:330-437) over the reference BVH.
+template <bool REF>
+BG_D RGB estimate_direct_ref(const Scene& sc, const Isect& it, const BSDF& bsdf, uint32_t light_prim, float us0,
+                             float us1, float ul0, float ul1, uint32_t* err) {
+    const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
+    RGB out = rgb(0.0f);
+    LightSample ls = light_sample<REF>(sc, light_prim, it, ul0, ul1);
+    float scattering_pdf = 0.0f;
+    if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
+        RGB f = bsdf.f<REF>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
+        scattering_pdf = bsdf.pdf<REF>(it.wo, ls.wi, flags);
+        if (!is_black(f)) {
+            Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
+            if (ref_traverse<true>(sc, sr, err, nullptr) >= 0) ls.radiance = rgb(0.0f);
+            if (!is_black(ls.radiance)) {
+                float w = power_heuristic(1.0f, ls.pdf, 1.0f, scattering_pdf);
+                out = out + f * ls.radiance * w / ls.pdf;
+            }
+        }
+    }
+    BxSample bs = bsdf.sample<REF>(it.wo, us0, us1, flags);
+    RGB f = bs.f * abs_dot(bs.wi, it.ns);
+    bool sampled_specular = (bs.stype & BSDF_SPECULAR) != 0;
+    // REF (F2): ray along the light sample's direction with the light half's pdf, any emitter
+    V3 wdir = REF ? ls.wi : bs.wi;
+    float spdf = REF ? scattering_pdf : bs.pdf;
+    if (!is_black(f) && spdf > 0.0f) {
+        float w = 1.0f;
+        if (!sampled_specular) {
+            float lpdf = light_pdf<REF>(sc, light_prim, it, wdir, nullptr);
+            if (lpdf == 0.0f) return out;
+            w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
+        }
+        Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wdir, REF);
+        Ray rr = ray;
+        int prim = ref_traverse<false>(sc, rr, err, nullptr);
+        RGB li = rgb(0.0f);
+        if (prim >= 0 && (REF ? prim_emission(sc, prim) >= 0 : prim == (int)light_prim)) {
+            Isect lit;
+            if (prim_isect(sc, prim, ray, &lit)) li = emitted_radiance(sc, lit, -wdir);
+        }
+        if (!is_black(li)) out = out + f * li * w / spdf;
+    }
+    return out;
+}
+
+// PathIntegrator::radiance (src/integrators/path.rs:51-146) over the reference BVH.
+template <bool REF>
+BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_depth, float rr_threshold,
+                      uint32_t* err) {
+    RGB out = rgb(0.0f), beta = rgb(1.0f);
+    bool specular_bounce = false;
+    float eta_scale = 1.0f;
+    for (uint32_t bounces = 0;; ++bounces) {
+        Ray traced = ray;
+        int prim = ref_traverse<false>(sc, ray, err, nullptr);  // sets ray.t_max to the hit
+        bool hit = prim >= 0;
+        Isect it;
+        if (hit) hit = prim_isect(sc, prim, traced, &it);
+        if (bounces == 0 || specular_bounce) {
+            if (hit) out = out + beta * emitted_radiance(sc, it, -ray.d);
+        }
+        if (!hit || bounces >= max_depth) break;
+        BSDF bsdf = make_bsdf(sc, it);
+        const uint32_t base = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounces;
+        float u[8];
+        rng.block(base, u);
+        rng.block(base + 4, u + 4);
+        if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
+            float count = (float)sc.nlights;
+            uint32_t li = (uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f);
+            float lpdf = 1.0f / count;
+            RGB ld = estimate_direct_ref<REF>(sc, it, bsdf, sc.light_prims[li], u[BD_USCAT], u[BD_USCAT + 1],
+                                              u[BD_ULIGHT], u[BD_ULIGHT + 1], err);
+            out = out + beta * (ld / lpdf);
+        }
+        V3 wo = -ray.d;
+        BxSample bs = bsdf.sample<REF>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+        if (is_black(bs.f) || bs.pdf == 0.0f) break;
+        beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
+        specular_bounce = (bs.stype & BSDF_SPECULAR) != 0;
+        if ((bs.stype & BSDF_SPECULAR) && (bs.stype & BSDF_TRANSMISSION)) {
+            float eta = bsdf.eta;
+            eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
+        }
+        // F1: REF re-intersects the same ray (t_max already at this hit); PBRT moves on
+        if (!REF) ray = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
+        RGB rr_beta = beta * eta_scale;
+        if (max_value(rr_beta) < rr_threshold && bounces > 3) {
+            float q = rmax(1.0f - max_value(rr_beta), 0.5f);
+            if (u[BD_RR] < q) break;
+            beta = beta / (1.0f - q);
+        }
+    }
+    return out;
+}
+
+template <bool REF>
+__global__ void __launch_bounds__(128) k_megakernel(Scene sc, Camera cam, RenderParams rp, FilmBuffers film,
+                                                    uint32_t* err) {
+    const uint64_t npix = (uint64_t)rp.width * rp.height;
+    const uint64_t total = npix * rp.spp;
+    for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t pix = (uint32_t)(item % npix);
+        uint32_t s = rp.first_sample + (uint32_t)(item / npix);
+        Rng rng{pix, s, rp.seed};
+        float c[4];
+        rng.block(0, c);
+        float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
+        Ray ray = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+        RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err);
+        film_add(film, pix, L);
+    }
+}
+
+void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, const RenderParams& rp,
+                       const FilmBuffers& film, uint32_t* err, const LaunchShape& ls, cudaStream_t s) {
+    dim3 grid(ls.sms * 8), block(128);
+    if (ref_compat) k_megakernel<true><<<grid, block, 0, s>>>(sc, cam, rp, film, err);
+    else k_megakernel<false><<<grid, block, 0, s>>>(sc, cam, rp, film, err);
+}
+
+// ================================================================ wavefront (PBRT, 2-wide BVH)
+enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9 };
+enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5 };
+
+__global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
+    const uint64_t npix = (uint64_t)rp.width * rp.height;
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+        uint64_t item = item0 + i;
+        uint32_t pix = (uint32_t)(item % npix);
+        uint32_t s = rp.first_sample + (uint32_t)(item / npix);
+        Rng rng{pix, s, rp.seed};
+        float c[4];
+        rng.block(0, c);
+        float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
+        Ray r = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+        wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
+        wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
+        wb.pixel[i] = pix;
+        wb.sample[i] = s;
+        wb.state[i] = 0;
+        wb.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        wb.queue[0][i] = i;
+    }
+}
+
+__global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
+    if (threadIdx.x == 0) {
+        wb.counters[(bounce + 1) & 1] = 0;
+        wb.counters[C_SHADOW] = 0;
+        wb.counters[C_DONE] = 0;
+        wb.counters[C_EXT_HEAD] = 0;
+        wb.counters[C_SH_HEAD] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err) {
+    const uint32_t n = wb.counters[bounce & 1];
+    const uint32_t* q = wb.queue[bounce & 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
+    for (;;) {
+        uint32_t base = warp_fetch(&wb.counters[C_EXT_HEAD]);
+        if (base >= n) break;
+        uint32_t i = base + lane_id();
+        if (i < n) {
+            uint32_t slot = q[i];
+            Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
+            int prim = bvh2_traverse<false>(sc, ray, err);
+            wb.hit[slot] = make_int2(prim, __float_as_int(ray.t_max));
+        }
+    }
+}
+
+// Adds the pending next-event contribution of the previous vertex:
+// L += beta_nee * ((part0 + part1) / light_pdf)  (path.rs:107-109, integrator.rs:327).
+BG_D RGB apply_pending(const WaveBuffers& wb, uint32_t slot, RGB L, uint32_t state, uint32_t nlights) {
+    if (!(state & ST_PENDING)) return L;
+    float4 p0 = wb.pending[2 * slot], p1 = wb.pending[2 * slot + 1];
+    RGB ld = rgb(0.0f);
+    if (p0.w != 0.0f) ld = ld + rgb(p0.x, p0.y, p0.z);
+    if (p1.w != 0.0f) ld = ld + rgb(p1.x, p1.y, p1.z);
+    float4 nb = wb.nee_beta[slot];
+    float light_pdf = 1.0f / (float)nlights;
+    return L + rgb(nb.x, nb.y, nb.z) * (ld / light_pdf);
+}
+
+__global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
+                                               uint32_t bounce, uint32_t* err) {
+    const uint32_t n = wb.counters[bounce & 1];
+    const uint32_t* q = wb.queue[bounce & 1];
+    uint32_t* qn = wb.queue[(bounce + 1) & 1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // warp-uniform loop so the ballots below see all 32 lanes
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
+        uint32_t i = base + lane_id();
+        bool active = i < n;
+        uint32_t slot = active ? q[i] : 0;
+        bool cont = false, done_pending = false;
+        bool push_sh[2] = {false, false};
+        float4 sh_o[2], sh_d[2];
+        if (active) {
+            float4 ro = wb.ray_o[slot], rd = wb.ray_d[slot];
+            Ray ray = load_ray(ro, rd);
+            int prim = wb.hit[slot].x;
+            uint32_t state = wb.state[slot];
+            float4 b4 = wb.beta[slot];
+            RGB beta = rgb(b4.x, b4.y, b4.z);
+            float eta_scale = b4.w;
+            float4 l4 = wb.L[slot];
+            RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
+            state &= ~ST_PENDING;
+            bool specular_bounce = (state & ST_SPECULAR) != 0;
+            Isect it;
+            bool hit = prim >= 0 && prim_isect(sc, prim, ray, &it);
+            if (bounce == 0 || specular_bounce) {
+                if (hit) L = L + beta * emitted_radiance(sc, it, -ray.d);
+            }
+            bool finished = !hit || bounce >= rp.max_depth;
+            if (!finished) {
+                Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
+                const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
+                float u[8];
+                rng.block(ub, u);
+                rng.block(ub + 4, u + 4);
+                BSDF bsdf = make_bsdf(sc, it);
+                if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
+                    // uniform_sample_one_light + estimate_direct, occlusion deferred to k_shadow
+                    const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
+                    float count = (float)sc.nlights;
+                    uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
+                    float4 pend[2] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+                    LightSample ls = light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+                    if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
+                        RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
+                        float spdf = bsdf.pdf<false>(it.wo, ls.wi, flags);
+                        if (!is_black(f)) {
+                            float w = power_heuristic(1.0f, ls.pdf, 1.0f, spdf);
+                            RGB c = f * ls.radiance * w / ls.pdf;
+                            Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
+                            pend[0] = make_float4(c.r, c.g, c.b, 0.0f);
+                            sh_o[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.t_max);
+                            sh_d[0] = make_float4(sr.d.x, sr.d.y, sr.d.z, __int_as_float(-1));
+                            push_sh[0] = true;
+                        }
+                    }
+                    BxSample bs = bsdf.sample<false>(it.wo, u[BD_USCAT], u[BD_USCAT + 1], flags);
+                    RGB f = bs.f * abs_dot(bs.wi, it.ns);
+                    if (!is_black(f) && bs.pdf > 0.0f) {
+                        float t_light = 0.0f;
+                        float lpdf = light_pdf<false>(sc, light_prim, it, bs.wi, &t_light);
+                        if (lpdf != 0.0f) {
+                            float w = power_heuristic(1.0f, bs.pdf, 1.0f, lpdf);
+                            // the sampled direction reaches the light at t_light; it counts iff
+                            // nothing else is hit first (closest hit == this light)
+                            V3 p0, p1, p2;
+                            load_tri(sc, light_prim, &p0, &p1, &p2);
+                            V3 ln = normalize(cross(p0 - p2, p1 - p2));
+                            RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -bs.wi);
+                            if (!is_black(li)) {
+                                RGB c = f * li * w / bs.pdf;
+                                Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
+                                pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
+                                sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
+                                sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float((int)light_prim));
+                                push_sh[1] = true;
+                            }
+                        }
+                    }
+                    wb.pending[2 * slot] = pend[0];
+                    wb.pending[2 * slot + 1] = pend[1];
+                    wb.nee_beta[slot] = make_float4(beta.r, beta.g, beta.b, 0.0f);
+                    state |= ST_PENDING;
+                }
+                V3 wo = -ray.d;
+                BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+                if (is_black(bs.f) || bs.pdf == 0.0f) {
+                    finished = true;
+                } else {
+                    beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
+                    bool spec = (bs.stype & BSDF_SPECULAR) != 0;
+                    if (spec && (bs.stype & BSDF_TRANSMISSION)) {
+                        float eta = bsdf.eta;
+                        eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
+                    }
+                    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
+                    RGB rr_beta = beta * eta_scale;
+                    bool killed = false;
+                    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
+                        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
+                        if (u[BD_RR] < qq) killed = true;
+                        else beta = beta / (1.0f - qq);
+                    }
+                    if (killed) {
+                        finished = true;
+                    } else {
+                        wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
+                        wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
+                        state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
+                        cont = true;
+                    }
+                }
+            }
+            wb.state[slot] = state;
+            wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
+            wb.L[slot] = make_float4(L.r, L.g, L.b, 0.0f);
+            if (finished) {
+                if (state & ST_PENDING) done_pending = true;
+                else film_add(film, wb.pixel[slot], L);
+            }
+        }
+        // compaction (convergent)
+        uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
+        if (cont) qn[pos] = slot;
+        pos = warp_append(&wb.counters[C_DONE], done_pending);
+        if (done_pending) wb.done[pos] = slot;
+        for (int k = 0; k < 2; ++k) {
+            pos = warp_append(&wb.counters[C_SHADOW], push_sh[k]);
+            if (push_sh[k]) {
+                if (pos < 2 * wb.capacity) {
+                    wb.sh_o[pos] = sh_o[k];
+                    wb.sh_d[pos] = sh_d[k];
+                    wb.sh_ref[pos] = 2 * slot + (uint32_t)k;
+                } else {
+                    atomicOr(err, ERR_QUEUE_OVERFLOW);
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err) {
+    const uint32_t n = min(wb.counters[C_SHADOW], 2 * wb.capacity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[1], (unsigned long long)n);
+    for (;;) {
+        uint32_t base = warp_fetch(&wb.counters[C_SH_HEAD]);
+        if (base >= n) break;
+        uint32_t i = base + lane_id();
+        if (i < n) {
+            float4 o = wb.sh_o[i], d = wb.sh_d[i];
+            Ray ray;
+            ray.o = f4xyz(o);
+            ray.t_max = o.w;
+            ray.d = f4xyz(d);
+            ray.time = 0.0f;
+            int skip = __float_as_int(d.w);
+            if (bvh2_traverse<true>(sc, ray, err, skip) < 0) wb.pending[wb.sh_ref[i]].w = 1.0f;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, WaveBuffers wb) {
+    const uint32_t n = wb.counters[C_DONE];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t slot = wb.done[i];
+        float4 l4 = wb.L[slot];
+        RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), wb.state[slot], sc.nlights);
+        film_add(film, wb.pixel[slot], L);
+    }
+}
+
+int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
+                const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
+                cudaStream_t s, cudaEvent_t* ev) {
+    int launches = 0;
+    dim3 grid(ls.sms * 8), block(128);
+    k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
+    ++launches;
+    for (uint32_t b = 0; b <= rp.max_depth; ++b) {
+        k_prepare<<<1, 32, 0, s>>>(wb, b);
+        if (ev) cudaEventRecord(ev[4 * b + 0], s);
+        k_extend<<<grid, block, 0, s>>>(sc, wb, b, err);
+        if (ev) cudaEventRecord(ev[4 * b + 1], s);
+        k_shade<<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        if (ev) cudaEventRecord(ev[4 * b + 2], s);
+        k_shadow<<<grid, block, 0, s>>>(sc, wb, err);
+        if (ev) cudaEventRecord(ev[4 * b + 3], s);
+        k_finalize<<<grid, block, 0, s>>>(sc, film, wb);
+        launches += 5;
+    }
+    return launches;
+}
+
+// ================================================================ film
+__global__ void k_resolve(FilmBuffers f) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npix; p += gridDim.x * blockDim.x) {
+        // merge_film_tile's rgb_to_xyz (film.rs:138-154) then write_image (film.rs:156-202)
+        float r = (float)f.sum[3 * p], g = (float)f.sum[3 * p + 1], b = (float)f.sum[3 * p + 2];
+        float X = 0.412453f * r + 0.357580f * g + 0.180423f * b;
+        float Y = 0.212671f * r + 0.715160f * g + 0.072169f * b;
+        float Z = 0.019334f * r + 0.119193f * g + 0.950227f * b;
+        float o0 = 3.240479f * X - 1.537150f * Y - 0.498535f * Z;
+        float o1 = -0.969256f * X + 1.875991f * Y + 0.041556f * Z;
+        float o2 = 0.055648f * X - 0.204043f * Y + 1.057311f * Z;
+        float w = (float)f.count[p];
+        if (w != 0.0f) {
+            float inv = 1.0f / w;
+            o0 = fmaxf(o0 * inv, 0.0f);
+            o1 = fmaxf(o1 * inv, 0.0f);
+            o2 = fmaxf(o2 * inv, 0.0f);
+        }
+        f.rgb[3 * p] = o0;
+        f.rgb[3 * p + 1] = o1;
+        f.rgb[3 * p + 2] = o2;
+    }
+}
+
+void launch_resolve(const FilmBuffers& film, cudaStream_t s) {
+    k_resolve<<<(film.npix + 255) / 256, 256, 0, s>>>(film);
+}
+
+void launch_clear_film(const FilmBuffers& film, cudaStream_t s) {
+    cudaMemsetAsync(film.sum, 0, sizeof(double) * 3 * film.npix, s);
+    cudaMemsetAsync(film.sumsq, 0, sizeof(double) * 3 * film.npix, s);
+    cudaMemsetAsync(film.count, 0, sizeof(uint32_t) * film.npix, s);
+}
+
+}  // namespace bg

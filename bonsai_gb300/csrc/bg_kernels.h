@@ -1,0 +1,68 @@
+// bg_kernels.h - launch interface between the host driver (bg_api.cpp) and the kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bonsai_gpu.h"
+#include "bg_device.h"
+
+namespace bg {
+
+struct RenderParams {
+    uint32_t width, height, spp, max_depth, first_sample;
+    float rr_threshold;
+    uint64_t seed;
+};
+
+struct FilmBuffers {
+    double* sum;     // 3 per pixel
+    double* sumsq;   // 3 per pixel
+    uint32_t* count; // per pixel
+    float* rgb;      // resolved, 3 per pixel
+    unsigned long long* nan_count;
+    uint32_t npix;
+};
+
+// Path-state arrays of one wavefront (capacity = number of path slots).
+struct WaveBuffers {
+    uint32_t capacity;
+    float4* ray_o;      // o.xyz, t_max
+    float4* ray_d;      // d.xyz, time
+    int2* hit;          // prim, t bits
+    uint32_t* pixel;
+    uint32_t* sample;
+    uint32_t* state;    // bounce | specular flag << 8 | pending flag << 9
+    float4* beta;       // rgb, eta_scale
+    float4* L;          // rgb
+    float4* nee_beta;   // beta at the NEE vertex
+    float4* pending;    // 2 per slot: contribution rgb, w = 1 if unoccluded
+    float4* sh_o;       // 2 * capacity shadow rays: o.xyz, t_max
+    float4* sh_d;       // d.xyz, skip prim (int bits)
+    uint32_t* sh_ref;   // slot * 2 + kind
+    uint32_t* queue[2];
+    uint32_t* done;
+    uint32_t* counters; // [0,1] queue sizes, [2] shadow count, [3] done count, [4] extend head, [5] shadow head
+    unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
+};
+
+struct LaunchShape {
+    int sms;
+    int block;
+};
+
+void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,
+                  uint8_t* occluded, uint32_t* err, unsigned long long* counters, uint32_t* work_head,
+                  const LaunchShape& ls, cudaStream_t s);
+void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, const RenderParams& rp,
+                       const FilmBuffers& film, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
+// One wave of the PBRT wavefront: items [item0, item0 + nitems) of the pixel x sample space.
+// Returns the number of kernels launched.  stage_events (optional): 4 events per bounce, recorded
+// before extend, before shade, before shadow and before finalize.
+int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
+                const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
+                cudaStream_t s, cudaEvent_t* stage_events);
+void launch_resolve(const FilmBuffers& film, cudaStream_t s);
+void launch_clear_film(const FilmBuffers& film, cudaStream_t s);
+
+}  // namespace bg

@@ -1,0 +1,526 @@
+// bg_shading.cuh - BxDFs, BSDF, materials, area lights and the perspective camera on the device.
+//
+// Restates src/base/{bsdf,bxdf,microfacet,fresnel}.rs, src/bxdfs/{lambertian,microfacet,fresnel}.rs,
+// src/materials/{matte,plastic}.rs, src/lights/diffuse.rs, src/base/shape.rs:17-57,
+// src/base/sampling.rs and src/cameras/perspective.rs.  REF selects the reference's own
+// behaviour where it deviates from PBRT-v3 (F4 G1 = lambda, F5 slope_x_1, F8 component counter,
+// F12 emission toward +wi, F13 light pdf without 1/area, F14 Fresnel without |cos|).
+#pragma once
+#include "bg_device.h"
+#include "bg_math.cuh"
+#include "bg_shapes.cuh"
+
+namespace bg {
+
+enum : uint8_t {
+    BSDF_REFLECTION = 1,
+    BSDF_TRANSMISSION = 2,
+    BSDF_DIFFUSE = 4,
+    BSDF_GLOSSY = 8,
+    BSDF_SPECULAR = 16,
+    BSDF_ALL = 31
+};
+
+BG_D float cos2_theta(V3 w) { return w.z * w.z; }
+BG_D float abs_cos_theta(V3 w) { return fabsf(w.z); }
+BG_D float sin2_theta(V3 w) { return rmax(0.0f, 1.0f - cos2_theta(w)); }
+BG_D float sin_theta(V3 w) { return sqrtf(sin2_theta(w)); }
+BG_D float tan_theta(V3 w) { return sin_theta(w) / w.z; }
+BG_D float tan2_theta(V3 w) { return sin2_theta(w) / cos2_theta(w); }
+BG_D float cos_phi(V3 w) {
+    float v = sin_theta(w);
+    return v == 0.0f ? 1.0f : rclamp(w.x / v, -1.0f, 1.0f);
+}
+BG_D float sin_phi(V3 w) {
+    float v = sin_theta(w);
+    return v == 0.0f ? 0.0f : rclamp(w.y / v, -1.0f, 1.0f);
+}
+BG_D float cos2_phi(V3 w) { return cos_phi(w) * cos_phi(w); }
+BG_D float sin2_phi(V3 w) { return sin_phi(w) * sin_phi(w); }
+BG_D bool same_hemisphere(V3 a, V3 b) { return a.z * b.z > 0.0f; }
+BG_D V3 reflect(V3 wo, V3 n) { return -wo + 2.0f * dot(wo, n) * n; }
+BG_D bool refract(V3 wi, V3 n, float eta, V3* wt) {  // bxdf.rs:146-159
+    float ci = dot(n, wi);
+    float s2i = rmax(0.0f, 1.0f - ci * ci);
+    float s2t = eta * eta * s2i;
+    if (s2t >= 1.0f) return false;
+    float ct = sqrtf(1.0f - s2t);
+    *wt = eta * -wi + (eta * ci - ct) * n;
+    return true;
+}
+template <bool REF>
+BG_D float fresnel_dielectric(float ci, float ei, float et) {  // bxdf.rs:165-188
+    ci = rclamp(ci, -1.0f, 1.0f);
+    if (!(ci > 0.0f)) {
+        float t = ei;
+        ei = et;
+        et = t;
+        if (!REF) ci = fabsf(ci);
+    }
+    float si = sqrtf(rmax(0.0f, 1.0f - ci * ci));
+    float st = ei / et * si;
+    if (st >= 1.0f) return 1.0f;
+    float ct = sqrtf(rmax(0.0f, 1.0f - st * st));
+    float rpar = ((et * ci) - (ei * ct)) / ((et * ci) + (ei * ct));
+    float rperp = ((ei * ci) - (et * ct)) / ((ei * ci) + (et * ct));
+    return (rpar * rpar + rperp * rperp) / 2.0f;
+}
+BG_D RGB fresnel_conductor(float cin, RGB eta_i, RGB eta_t, RGB k) {  // bxdf.rs:190-217
+    RGB ci = rgb(rclamp(cin, -1.0f, 1.0f));
+    RGB eta = eta_t / eta_i;
+    RGB eta_k = k / eta_i;
+    RGB ci2 = ci * ci;
+    RGB si2 = rgb(1.0f) - ci2;
+    RGB eta2 = eta * eta;
+    RGB etak2 = eta_k * eta_k;
+    RGB t0 = eta2 - etak2 - si2;
+    RGB a2b2 = rgb_sqrt(t0 * t0 + eta2 * etak2 * 4.0f);
+    RGB t1 = a2b2 + ci2;
+    RGB a = rgb_sqrt((a2b2 + t0) * 0.5f);
+    RGB t2 = ci * a * 2.0f;
+    RGB rs = (t1 - t2) / (t1 + t2);
+    RGB t3 = ci2 * a2b2 + si2 * si2;
+    RGB t4 = t2 * si2;
+    RGB rp = rs * (t3 - t4) / (t3 + t4);
+    return (rp + rs) * 0.5f;
+}
+
+// TrowbridgeReitzDistribution (src/base/microfacet.rs), isotropic alpha.
+struct TR {
+    float ax, ay;
+    BG_D float D(V3 wh) const {
+        float t2 = tan2_theta(wh);
+        if (isinf(t2)) return 0.0f;
+        float cos4 = cos2_theta(wh) * cos2_theta(wh);
+        float e = (cos2_phi(wh) / (ax * ax) + sin2_phi(wh) / (ay * ay)) * t2;
+        return 1.0f / (PI * ax * ay * cos4 * (1.0f + e) * (1.0f + e));
+    }
+    BG_D float lambda(V3 w) const {
+        float at = fabsf(tan_theta(w));
+        if (isinf(at)) return 0.0f;
+        float alpha = sqrtf(cos2_phi(w) * ax * ax + sin2_phi(w) * ay * ay);
+        float a2t2 = (alpha * at) * (alpha * at);
+        return (-1.0f + sqrtf(1.0f + a2t2)) / 2.0f;
+    }
+    template <bool REF>
+    BG_D float G1(V3 w) const {  // F4
+        return REF ? 1.0f / (1.0f / lambda(w)) : 1.0f / (1.0f + lambda(w));
+    }
+    BG_D float G(V3 wo, V3 wi) const { return 1.0f / (1.0f + lambda(wo) + lambda(wi)); }
+    template <bool REF>
+    BG_D float pdf(V3 wo, V3 wh) const { return D(wh) * G1<REF>(wo) * abs_dot(wo, wh) / abs_cos_theta(wo); }
+    template <bool REF>
+    BG_D static void sample11(float cos_t, float u1, float u2, float* sxo, float* syo) {  // :55-97
+        if (cos_t > 0.9999f) {
+            float r = sqrtf(u1 / (1.0f - u1));
+            float phi = 6.28318530718f * u2;
+            *sxo = r * cosf(phi);
+            *syo = r * sinf(phi);
+            return;
+        }
+        float sin_t = sqrtf(rmax(1.0f - cos_t * cos_t, 0.0f));
+        float tan_t = sin_t / cos_t;
+        float a = 1.0f / tan_t;
+        float g1 = 2.0f / (1.0f + sqrtf(1.0f + 1.0f / (a * a)));
+        float A = 2.0f * u1 / g1 - 1.0f;
+        float tmp = 1.0f / (A * A - 1.0f);
+        if (tmp > 1e10f) tmp = 1e10f;
+        float B = tan_t;
+        float D = sqrtf(rmax(B * B * tmp * tmp - (A * A - B * B) * tmp, 0.0f));
+        float sx1 = B * tmp - D;
+        float sx2 = B * tmp + D;
+        float sx = REF ? sx1 : ((A < 0.0f || sx2 > 1.0f / tan_t) ? sx1 : sx2);  // F5
+        float S;
+        if (u2 > 0.5f) {
+            S = 1.0f;
+            u2 = 2.0f * (u2 - 0.5f);
+        } else {
+            S = -1.0f;
+            u2 = 2.0f * (0.5f - u2);
+        }
+        float z = (u2 * (u2 * (u2 * 0.27385f - 0.73369f) + 0.46341f)) /
+                  (u2 * (u2 * (u2 * 0.093073f + 0.309420f) - 1.000000f) + 0.597999f);
+        *sxo = sx;
+        *syo = S * z * sqrtf(1.0f + sx * sx);
+    }
+    template <bool REF>
+    BG_D V3 sample_wh(V3 wo, float u0, float u1) const {  // :99-112, :144-153
+        bool flip = wo.z < 0.0f;
+        V3 wi = flip ? -wo : wo;
+        V3 ws = normalize(v3(ax * wi.x, ay * wi.y, wi.z));
+        float sx, sy;
+        sample11<REF>(ws.z, u0, u1, &sx, &sy);
+        float tmp = cos_phi(ws) * sx - sin_phi(ws) * sy;
+        sy = sin_phi(ws) * sx + cos_phi(ws) * sy;
+        sx = tmp;
+        sx = ax * sx;
+        sy = ay * sy;
+        V3 wh = normalize(v3(-sx, -sy, 1.0f));
+        return flip ? -wh : wh;
+    }
+};
+
+// sampling.rs:181-198 / :238-242
+BG_D V3 cosine_sample_hemisphere(float u0, float u1) {
+    float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+    float dx = 0.0f, dy = 0.0f;
+    if (!(ox == 0.0f && oy == 0.0f)) {
+        float theta, r;
+        if (fabsf(ox) > fabsf(oy)) {
+            theta = (PI / 4.0f) * (oy / ox);
+            r = ox;
+        } else {
+            theta = PI_OVER_TWO - (PI / 4.0f) * (ox / oy);
+            r = oy;
+        }
+        dx = r * cosf(theta);
+        dy = r * sinf(theta);
+    }
+    float z = sqrtf(rmax(0.0f, 1.0f - dx * dx - dy * dy));
+    return v3(dx, dy, z);
+}
+BG_D float power_heuristic(float nf, float fp, float ng, float gp) {
+    float f = nf * fp, g = ng * gp;
+    return (f * f) / (f * f + g * g);
+}
+
+enum BxKind : uint8_t { BX_LAMBERT = 0, BX_MF_REFL = 1, BX_FRESNEL_SPEC = 2 };
+struct Bxdf {
+    uint8_t kind, type;
+    bool conductor;
+    RGB r;             // R (lambert, microfacet, specular R)
+    TR dist;
+    RGB eta_t, k;      // conductor (eta_i = 1)
+    float ei, et;      // dielectric fresnel / FresnelSpecular eta_a, eta_b
+    BG_D bool matches(uint8_t f) const { return (type & f) == type; }
+};
+struct BxSample {
+    V3 wi;
+    RGB f;
+    float pdf;
+    int stype;
+};
+
+template <bool REF>
+BG_D RGB bx_f(const Bxdf& b, V3 wo, V3 wi) {
+    if (b.kind == BX_LAMBERT) return b.r * (1.0f / PI);
+    if (b.kind == BX_MF_REFL) {  // bxdfs/microfacet.rs:69-94
+        float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
+        V3 wh = wi + wo;
+        if (ci == 0.0f || co == 0.0f) return rgb(0.0f);
+        if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return rgb(0.0f);
+        wh = normalize(wh);
+        float c = dot(wi, face_forward(wh, v3(0.0f, 0.0f, 1.0f)));
+        RGB F = b.conductor ? fresnel_conductor(fabsf(c), rgb(1.0f), b.eta_t, b.k)
+                            : rgb(fresnel_dielectric<REF>(c, b.ei, b.et));
+        return b.r * b.dist.D(wh) * b.dist.G(wo, wi) * F / (4.0f * ci * co);
+    }
+    return rgb(0.0f);
+}
+template <bool REF>
+BG_D float bx_pdf(const Bxdf& b, V3 wo, V3 wi) {
+    if (b.kind == BX_LAMBERT) return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;
+    if (b.kind == BX_MF_REFL) {
+        if (!same_hemisphere(wo, wi)) return 0.0f;
+        V3 wh = normalize(wo + wi);
+        return b.dist.pdf<REF>(wo, wh) / (4.0f * dot(wo, wh));
+    }
+    return 0.0f;
+}
+template <bool REF>
+BG_D BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1) {
+    BxSample s;
+    s.wi = v3(0, 0, 0);
+    s.f = rgb(0.0f);
+    s.pdf = 0.0f;
+    s.stype = -1;
+    if (b.kind == BX_LAMBERT) {
+        V3 wi = cosine_sample_hemisphere(u0, u1);
+        if (wo.z < 0.0f) wi.z *= -1.0f;
+        s.wi = wi;
+        s.f = bx_f<REF>(b, wo, wi);
+        s.pdf = bx_pdf<REF>(b, wo, wi);
+        return s;
+    }
+    if (b.kind == BX_MF_REFL) {
+        if (wo.z == 0.0f) return s;
+        V3 wh = b.dist.sample_wh<REF>(wo, u0, u1);
+        if (dot(wo, wh) < 0.0f) return s;
+        V3 wi = reflect(wo, wh);
+        if (!same_hemisphere(wo, wi)) return s;
+        s.wi = wi;
+        s.f = bx_f<REF>(b, wo, wi);
+        s.pdf = b.dist.pdf<REF>(wo, wh) / (4.0f * dot(wo, wh));
+        return s;
+    }
+    // FresnelSpecular (bxdfs/fresnel.rs:76-122)
+    float F = fresnel_dielectric<REF>(wo.z, b.ei, b.et);
+    if (u0 < F) {
+        V3 wi = v3(-wo.x, -wo.y, wo.z);
+        s.wi = wi;
+        s.pdf = F;
+        s.f = rgb(F) * b.r / abs_cos_theta(wi);
+        s.stype = BSDF_SPECULAR | BSDF_REFLECTION;
+        return s;
+    }
+    bool entering = wo.z > 0.0f;
+    float ei = entering ? b.ei : b.et, et = entering ? b.et : b.ei;
+    V3 wi;
+    if (!refract(wo, face_forward(v3(0.0f, 0.0f, 1.0f), wo), ei / et, &wi)) return s;
+    RGB ft = b.r * (1.0f - F);  // T = R = 1 for the dielectric
+    ft = ft * ((ei * ei) / (et * et));
+    s.wi = wi;
+    s.f = ft / abs_cos_theta(wi);
+    s.pdf = 1.0f - F;
+    s.stype = BSDF_SPECULAR | BSDF_TRANSMISSION;
+    return s;
+}
+
+struct BSDF {  // src/base/bsdf.rs
+    float eta;
+    V3 ns, ng, ss, ts;
+    Bxdf bx[2];
+    int n;
+    BG_D int num_components(uint8_t f) const {
+        int k = 0;
+        for (int i = 0; i < n; ++i) k += bx[i].matches(f);
+        return k;
+    }
+    BG_D V3 to_local(V3 v) const { return v3(dot(v, ss), dot(v, ts), dot(v, ns)); }
+    BG_D V3 to_world(V3 v) const {
+        return v3(ss.x * v.x + ts.x * v.y + ns.x * v.z, ss.y * v.x + ts.y * v.y + ns.y * v.z,
+                  ss.z * v.x + ts.z * v.y + ns.z * v.z);
+    }
+    template <bool REF>
+    BG_D RGB f(V3 wo_w, V3 wi_w, uint8_t flags) const {  // bsdf.rs:84-105
+        V3 wo = to_local(wo_w), wi = to_local(wi_w);
+        if (wo.z == 0.0f) return rgb(0.0f);
+        bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
+        RGB r = rgb(0.0f);
+        for (int i = 0; i < n; ++i)
+            if (bx[i].matches(flags) &&
+                ((refl && (bx[i].type & BSDF_REFLECTION)) || (!refl && (bx[i].type & BSDF_TRANSMISSION))))
+                r = r + bx_f<REF>(bx[i], wo, wi);
+        return r;
+    }
+    template <bool REF>
+    BG_D float pdf(V3 wo_w, V3 wi_w, uint8_t flags) const {  // bsdf.rs:234-259
+        if (n == 0) return 0.0f;
+        V3 wo = to_local(wo_w), wi = to_local(wi_w);
+        if (wo.z == 0.0f) return 0.0f;
+        float ret = 0.0f, comps = 0.0f;
+        for (int i = 0; i < n; ++i)
+            if (bx[i].matches(flags)) {
+                comps += 1.0f;
+                ret += bx_pdf<REF>(bx[i], wo, wi);
+            }
+        return comps > 0.0f ? ret / comps : 0.0f;
+    }
+    template <bool REF>
+    BG_D BxSample sample(V3 wo_w, float u0, float u1, uint8_t type) const {  // bsdf.rs:140-232
+        BxSample zero;
+        zero.wi = v3(0, 0, 0);
+        zero.f = rgb(0.0f);
+        zero.pdf = 0.0f;
+        zero.stype = 0;
+        int matches = num_components(type);
+        if (matches == 0) return zero;
+        uint32_t comp = min((uint32_t)floorf(u0 * (float)matches), (uint32_t)matches - 1);
+        uint32_t count = comp;
+        int pick = -1;
+        for (int i = 0; i < n; ++i) {
+            if (bx[i].matches(type) && count == 0) {
+                pick = i;
+                break;
+            }
+            if (REF || bx[i].matches(type)) count -= 1;  // F8
+        }
+        if (pick < 0) return zero;
+        const Bxdf& b = bx[pick];
+        float ur0 = rmin(u0 * (float)matches - (float)comp, ONE_MINUS_EPSILON);
+        V3 wo = to_local(wo_w);
+        if (wo.z == 0.0f) return zero;
+        BxSample s = bx_sample<REF>(b, wo, ur0, u1);
+        int stype = s.stype >= 0 ? s.stype : b.type;
+        if (s.pdf == 0.0f) return zero;
+        V3 wi_w = to_world(s.wi);
+        if (!(b.type & BSDF_SPECULAR) && matches > 1)
+            for (int i = 0; i < n; ++i)
+                if (i != pick && bx[i].matches(type)) s.pdf += bx_pdf<REF>(bx[i], wo, s.wi);
+        if (matches > 1) s.pdf /= (float)matches;
+        if (!(b.type & BSDF_SPECULAR)) {
+            bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
+            s.f = rgb(0.0f);
+            for (int i = 0; i < n; ++i)
+                if (bx[i].matches(type) &&
+                    ((refl && (bx[i].type & BSDF_REFLECTION)) || (!refl && (bx[i].type & BSDF_TRANSMISSION))))
+                    s.f = s.f + bx_f<REF>(bx[i], wo, s.wi);
+        }
+        s.wi = wi_w;
+        s.stype = stype;
+        return s;
+    }
+};
+
+BG_D uint32_t prim_material(const Scene& sc, int prim) {
+    return (uint32_t)prim < sc.ntri ? __float_as_uint(sc.tri[3 * prim].w) : sc.sph_mat[prim - sc.ntri];
+}
+
+// Material::compute_scattering_functions for the constant-texture materials.
+BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
+    const Material& m = sc.mats[prim_material(sc, it.prim)];
+    BSDF b;
+    b.eta = 1.0f;
+    b.n = 0;
+    b.ns = it.ns;
+    b.ng = it.n;
+    b.ss = normalize(it.dpdu);
+    b.ts = cross(b.ns, b.ss);
+    if (m.type == 0 || m.type == 1) {  // matte, plastic
+        RGB kd = rgb(rclamp(m.kd[0], 0.0f, INFINITY), rclamp(m.kd[1], 0.0f, INFINITY), rclamp(m.kd[2], 0.0f, INFINITY));
+        if (!is_black(kd)) {
+            Bxdf& l = b.bx[b.n++];
+            l.kind = BX_LAMBERT;
+            l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
+            l.r = kd;
+            l.conductor = false;
+        }
+        if (m.type == 1) {
+            RGB ks = rgb(rclamp(m.ks[0], 0.0f, INFINITY), rclamp(m.ks[1], 0.0f, INFINITY), rclamp(m.ks[2], 0.0f, INFINITY));
+            if (!is_black(ks)) {
+                Bxdf& g = b.bx[b.n++];
+                g.kind = BX_MF_REFL;
+                g.type = BSDF_REFLECTION | BSDF_GLOSSY;
+                g.r = ks;
+                g.dist = TR{m.alpha, m.alpha};
+                g.conductor = false;
+                g.ei = 1.5f;
+                g.et = 1.0f;
+            }
+        }
+    } else if (m.type == 2) {  // conductor
+        Bxdf& g = b.bx[b.n++];
+        g.kind = BX_MF_REFL;
+        g.type = BSDF_REFLECTION | BSDF_GLOSSY;
+        g.r = rgb(1.0f);
+        g.dist = TR{m.alpha, m.alpha};
+        g.conductor = true;
+        g.eta_t = rgb(m.eta[0], m.eta[1], m.eta[2]);
+        g.k = rgb(m.k[0], m.k[1], m.k[2]);
+    } else {  // dielectric
+        b.eta = m.ior;
+        Bxdf& d = b.bx[b.n++];
+        d.kind = BX_FRESNEL_SPEC;
+        d.type = BSDF_REFLECTION | BSDF_TRANSMISSION | BSDF_SPECULAR;
+        d.r = rgb(1.0f);
+        d.conductor = false;
+        d.ei = 1.0f;
+        d.et = m.ior;
+    }
+    return b;
+}
+
+// ---- lights (src/lights/diffuse.rs)
+BG_D RGB emission(const Emission& e, V3 n, V3 dir) {
+    if (e.two_sided || dot(n, dir) > 0.0f) return rgb(e.intensity[0], e.intensity[1], e.intensity[2]);
+    return rgb(0.0f);
+}
+BG_D int prim_emission(const Scene& sc, int prim) {
+    return (uint32_t)prim < sc.ntri ? __float_as_int(sc.tri[3 * prim + 1].w) : -1;
+}
+BG_D RGB emitted_radiance(const Scene& sc, const Isect& it, V3 w) {  // interaction.rs:257-266
+    int e = prim_emission(sc, it.prim);
+    if (e < 0) return rgb(0.0f);
+    return emission(sc.emis[e], it.n, w);
+}
+
+struct LightSample {
+    RGB radiance;
+    V3 wi;
+    float pdf;
+    ShapeSample pt;
+};
+// DiffuseAreaLight::sample_point + Shape::sample_from_it (diffuse.rs:54-87, shape.rs:17-34)
+template <bool REF>
+BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, float u0, float u1) {
+    LightSample ls;
+    ls.radiance = rgb(0.0f);
+    ls.wi = v3(0, 0, 0);
+    ls.pdf = 0.0f;
+    V3 p0, p1, p2;
+    load_tri(sc, prim, &p0, &p1, &p2);
+    ls.pt = tri_sample(p0, p1, p2, u0, u1);
+    V3 wi = ls.pt.p - it.p;
+    float pdf;
+    if (length_squared(wi) == 0.0f) pdf = 0.0f;
+    else {
+        wi = normalize(wi);
+        float conv = distance_squared(it.p, ls.pt.p) / abs_dot(ls.pt.n, -wi);
+        pdf = REF ? conv : ls.pt.pdf_area * conv;  // F13
+        if (isinf(pdf)) pdf = 0.0f;
+    }
+    if (pdf == 0.0f || length_squared(ls.pt.p - it.p) == 0.0f) return ls;
+    ls.wi = normalize(ls.pt.p - it.p);
+    ls.radiance = emission(sc.emis[prim_emission(sc, (int)prim)], ls.pt.n, REF ? ls.wi : -ls.wi);  // F12
+    ls.pdf = pdf;
+    return ls;
+}
+// Shape::pdf_from_it for a triangle light (shape.rs:40-57).  Also returns the hit distance.
+template <bool REF>
+BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, float* t_light) {
+    Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wi, REF);
+    V3 p0, p1, p2;
+    load_tri(sc, prim, &p0, &p1, &p2);
+    TriRay tr = make_tri_ray(ray);
+    TriHit h;
+    if (!tri_test(tr, ray.t_max, p0, p1, p2, &h)) return 0.0f;
+    Isect li;
+    tri_isect(p0, p1, p2, h, ray, &li);
+    float pdf = distance_squared(it.p, li.p) / (abs_dot(li.n, -wi) * tri_area(p0, p1, p2));
+    if (isinf(pdf)) pdf = 0.0f;
+    if (t_light) *t_light = h.t;
+    return pdf;
+}
+
+// ---- camera
+BG_D V3 xf_point(const float m[4][4], V3 p) {  // point3.rs:51-69
+    float xp = m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3];
+    float yp = m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3];
+    float zp = m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3];
+    float wp = m[3][0] * p.x + m[3][1] * p.y + m[3][2] * p.z + m[3][3];
+    if (wp == 1.0f) return v3(xp, yp, zp);
+    return v3(xp, yp, zp) / wp;
+}
+// PerspectiveCamera::generate_ray, pinhole (perspective.rs:117-175) + Ray::transform (ray.rs:50-76)
+BG_D Ray camera_ray(const Camera& c, float fx, float fy, float tu) {
+    V3 cp = xf_point(c.r2c, v3(fx, fy, 0.0f));
+    V3 d = normalize(cp);
+    const auto& m = c.c2w;
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+    float xp = (m[0][0] * x + m[0][1] * y) + (m[0][2] * z + m[0][3]);
+    float yp = (m[1][0] * x + m[1][1] * y) + (m[1][2] * z + m[1][3]);
+    float zp = (m[2][0] * x + m[2][1] * y) + (m[2][2] * z + m[2][3]);
+    float wp = (m[3][0] * x + m[3][1] * y) + (m[3][2] * z + m[3][3]);
+    float xa = fabsf(m[0][0] * x) + fabsf(m[0][1] * y) + fabsf(m[0][2] * z) + fabsf(m[0][3]);
+    float ya = fabsf(m[1][0] * x) + fabsf(m[1][1] * y) + fabsf(m[1][2] * z) + fabsf(m[1][3]);
+    float za = fabsf(m[2][0] * x) + fabsf(m[2][1] * y) + fabsf(m[2][2] * z) + fabsf(m[2][3]);
+    V3 oerr = gamma(3.0f) * v3(xa, ya, za);
+    V3 o = v3(xp, yp, zp);
+    if (wp != 1.0f) o = o / wp;
+    V3 dw = v3(m[0][0] * d.x + m[0][1] * d.y + m[0][2] * d.z, m[1][0] * d.x + m[1][1] * d.y + m[1][2] * d.z,
+               m[2][0] * d.x + m[2][1] * d.y + m[2][2] * d.z);
+    Ray r;
+    r.t_max = INFINITY;
+    float ls = length_squared(dw);
+    if (ls > 0.0f) {
+        float dt = dot(vabs(dw), oerr) / ls;
+        o = o + dw * dt;
+        r.t_max = INFINITY - dt;
+    }
+    r.o = o;
+    r.d = dw;
+    r.time = (1.0f - tu) * 0.0f + tu * 1.0f;
+    return r;
+}
+
+}  // namespace bg

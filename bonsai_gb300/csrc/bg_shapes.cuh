@@ -1,0 +1,338 @@
+// bg_shapes.cuh - triangle and sphere intersection, surface interactions, ray spawning.
+//
+// Device restatement of src/shapes/triangle.rs, src/shapes/sphere.rs,
+// src/base/interaction.rs and src/geometries/point3.rs:31-49 with the reference's f32 operation
+// order (these TUs are built with -fmad=false).  The per-ray permutation/shear constants of the
+// watertight triangle test (triangle.rs:147-171) are computed once per ray instead of once per
+// triangle: the values are identical, the work is not repeated.
+#pragma once
+#include "bg_device.h"
+#include "bg_math.cuh"
+
+namespace bg {
+
+struct Ray {
+    V3 o, d;
+    float t_max;
+    float time;
+};
+
+// Per-ray constants of the watertight test.
+struct TriRay {
+    V3 o;           // origin
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+BG_D TriRay make_tri_ray(const Ray& r) {
+    TriRay t;
+    t.o = r.o;
+    t.kz = max_dimension(vabs(r.d));
+    t.kx = t.kz + 1;
+    if (t.kx == 3) t.kx = 0;
+    t.ky = t.kx + 1;
+    if (t.ky == 3) t.ky = 0;
+    V3 d = permute(r.d, t.kx, t.ky, t.kz);
+    t.sx = -d.x / d.z;
+    t.sy = -d.y / d.z;
+    t.sz = 1.0f / d.z;
+    return t;
+}
+
+struct TriHit {
+    float t, b0, b1, b2;
+};
+
+// Triangle::intersect_test / the t part of Triangle::intersect (triangle.rs:135-268).
+BG_D bool tri_test(const TriRay& tr, float t_max, V3 p0, V3 p1, V3 p2, TriHit* out) {
+    V3 p0t = permute(p0 - tr.o, tr.kx, tr.ky, tr.kz);
+    V3 p1t = permute(p1 - tr.o, tr.kx, tr.ky, tr.kz);
+    V3 p2t = permute(p2 - tr.o, tr.kx, tr.ky, tr.kz);
+    p0t.x += tr.sx * p0t.z;
+    p0t.y += tr.sy * p0t.z;
+    p1t.x += tr.sx * p1t.z;
+    p1t.y += tr.sy * p1t.z;
+    p2t.x += tr.sx * p2t.z;
+    p2t.y += tr.sy * p2t.z;
+    float e0 = p1t.x * p2t.y - p1t.y * p2t.x;
+    float e1 = p2t.x * p0t.y - p2t.y * p0t.x;
+    float e2 = p0t.x * p1t.y - p0t.y * p1t.x;
+    if (e0 == 0.0f || e1 == 0.0f || e2 == 0.0f) {  // triangle.rs:178-190 (f64 there)
+        e0 = diff_of_products(p1t.x, p2t.y, p1t.y, p2t.x);
+        e1 = diff_of_products(p2t.x, p0t.y, p2t.y, p0t.x);
+        e2 = diff_of_products(p0t.x, p1t.y, p0t.y, p1t.x);
+    }
+    if ((e0 < 0.0f || e1 < 0.0f || e2 < 0.0f) && (e0 > 0.0f || e1 > 0.0f || e2 > 0.0f)) return false;
+    float det = e0 + e1 + e2;
+    if (det == 0.0f) return false;
+    p0t.z *= tr.sz;
+    p1t.z *= tr.sz;
+    p2t.z *= tr.sz;
+    float ts = e0 * p0t.z + e1 * p1t.z + e2 * p2t.z;
+    if (det < 0.0f && (ts >= 0.0f || ts < t_max * det)) return false;
+    else if (det > 0.0f && (ts <= 0.0f || ts > t_max * det)) return false;
+    float inv_det = 1.0f / det;
+    float t = ts * inv_det;
+    // conservative t bound (triangle.rs:219-239)
+    float max_zt = max_component(vabs(v3(p0t.z, p1t.z, p2t.z)));
+    float delta_z = gamma(3.0f) * max_zt;
+    float max_xt = max_component(vabs(v3(p0t.x, p1t.x, p2t.x)));
+    float max_yt = max_component(vabs(v3(p0t.y, p1t.y, p2t.y)));
+    float delta_x = gamma(5.0f) * (max_xt + max_zt);
+    float delta_y = gamma(5.0f) * (max_yt + max_zt);
+    float delta_e = 2.0f * (gamma(2.0f) * max_xt * max_yt + delta_y * max_xt + delta_x * max_yt);
+    float max_e = max_component(vabs(v3(e0, e1, e2)));
+    float delta_t = 3.0f * (gamma(3.0f) * max_e * max_zt + delta_e * max_zt + delta_z * max_e) * fabsf(inv_det);
+    if (t <= delta_t) return false;
+    // degenerate-triangle exit (triangle.rs:241-268 with the default uvs): rejected only when both
+    // dpdu x dpdv and (p2-p0)x(p1-p0) vanish
+    V3 ng = cross(p2 - p0, p1 - p0);
+    if (length_squared(ng) == 0.0f) {
+        V3 dp02 = p0 - p2, dp12 = p1 - p2;
+        V3 dpdu = (-1.0f * dp02 - -1.0f * dp12) * 1.0f;
+        V3 dpdv = (-0.0f * dp02 + -1.0f * dp12) * 1.0f;
+        if (length_squared(cross(dpdu, dpdv)) == 0.0f) return false;
+    }
+    if (out) {
+        out->t = t;
+        out->b0 = e0 * inv_det;
+        out->b1 = e1 * inv_det;
+        out->b2 = e2 * inv_det;
+    }
+    return true;
+}
+
+// Surface interaction (geometry part of SurfaceInteraction) used by shading.
+struct Isect {
+    V3 p, p_err, wo, n, ns, dpdu;  // dpdu = shading dpdu (BSDF s axis before normalisation)
+    float time;
+    int prim;
+};
+
+// Triangle::intersect's interaction (triangle.rs:241-307) from the barycentrics.
+BG_D void tri_isect(V3 p0, V3 p1, V3 p2, const TriHit& h, const Ray& ray, Isect* it) {
+    V3 dp02 = p0 - p2, dp12 = p1 - p2;
+    // default uvs (0,0),(1,0),(1,1): duv02=(-1,-1), duv12=(0,-1), determinant 1
+    V3 dpdu = (-1.0f * dp02 - -1.0f * dp12) * 1.0f;
+    V3 dpdv = (-0.0f * dp02 + -1.0f * dp12) * 1.0f;
+    if (length_squared(cross(dpdu, dpdv)) == 0.0f) {
+        V3 ng = normalize(cross(p2 - p0, p1 - p0));
+        // Vec3::coordinate_system (vec3.rs:25-33)
+        if (fabsf(ng.x) > fabsf(ng.y))
+            dpdu = v3(-ng.z, 0.0f, ng.x) / sqrtf(ng.x * ng.x + ng.z * ng.z);
+        else
+            dpdu = v3(0.0f, ng.z, -ng.y) / sqrtf(ng.y * ng.y + ng.z * ng.z);
+    }
+    float xs = fabsf(h.b0 * p0.x) + fabsf(h.b1 * p1.x) + fabsf(h.b2 * p2.x);
+    float ys = fabsf(h.b0 * p0.y) + fabsf(h.b1 * p1.y) + fabsf(h.b2 * p2.y);
+    float zs = fabsf(h.b0 * p0.z) + fabsf(h.b1 * p1.z) + fabsf(h.b2 * p2.z);
+    it->p_err = gamma(7.0f) * v3(xs, ys, zs);
+    it->p = h.b0 * p0 + h.b1 * p1 + h.b2 * p2;
+    it->time = ray.time;
+    it->wo = -ray.d;
+    V3 nn = normalize(cross(dp02, dp12));
+    it->n = nn;
+    it->ns = nn;
+    it->dpdu = dpdu;
+}
+
+BG_D float tri_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(p1 - p0, p2 - p0)); }
+
+// Sphere with object_to_world = translate(c): world_to_object is translate(-c) (translate(0)
+// itself when c == 0, sphere.rs:40-45).  xo = (1*x + 0*y) + (0*z + m03), as point3.rs:71-100.
+struct SphereXf {
+    V3 c;       // center (object_to_world translation)
+    V3 ci;      // world_to_object translation
+};
+BG_D SphereXf sphere_xf(float4 s) {
+    SphereXf x;
+    x.c = v3(s.x, s.y, s.z);
+    bool ident = (s.x == 0.0f && s.y == 0.0f && s.z == 0.0f);
+    x.ci = ident ? x.c : v3(-s.x, -s.y, -s.z);
+    return x;
+}
+BG_D V3 xf_point_err(V3 t, V3 p, V3* err) {  // rows (1,0,0,tx) (0,1,0,ty) (0,0,1,tz)
+    float xp = (1.0f * p.x + 0.0f * p.y) + (0.0f * p.z + t.x);
+    float yp = (0.0f * p.x + 1.0f * p.y) + (0.0f * p.z + t.y);
+    float zp = (0.0f * p.x + 0.0f * p.y) + (1.0f * p.z + t.z);
+    float xa = fabsf(1.0f * p.x) + fabsf(0.0f * p.y) + fabsf(0.0f * p.z) + fabsf(t.x);
+    float ya = fabsf(0.0f * p.x) + fabsf(1.0f * p.y) + fabsf(0.0f * p.z) + fabsf(t.y);
+    float za = fabsf(0.0f * p.x) + fabsf(0.0f * p.y) + fabsf(1.0f * p.z) + fabsf(t.z);
+    *err = gamma(3.0f) * v3(xa, ya, za);
+    return v3(xp, yp, zp);
+}
+BG_D V3 xf_vec_id(V3 v) {  // identity 3x3 rows
+    return v3(1.0f * v.x + 0.0f * v.y + 0.0f * v.z, 0.0f * v.x + 1.0f * v.y + 0.0f * v.z,
+              0.0f * v.x + 0.0f * v.y + 1.0f * v.z);
+}
+BG_D V3 xf_vec_err_id(V3 v, V3* e) {
+    float g3 = gamma(3.0f);
+    e->x = g3 * (fabsf(1.0f * v.x) + fabsf(0.0f * v.y) + fabsf(0.0f * v.z));
+    e->y = g3 * (fabsf(0.0f * v.x) + fabsf(1.0f * v.y) + fabsf(0.0f * v.z));
+    e->z = g3 * (fabsf(0.0f * v.x) + fabsf(0.0f * v.y) + fabsf(1.0f * v.z));
+    return xf_vec_id(v);
+}
+
+struct SphHit {
+    float t;
+    Ray ray_obj;  // object-space ray with the origin moved to the error bound (ray.rs:78-106)
+};
+
+// Sphere::intersect / intersect_test for a full sphere (sphere.rs:80-161, 239-326).
+BG_D bool sphere_test(float4 s, const Ray& rw, float t_max, SphHit* out) {
+    SphereXf xf = sphere_xf(s);
+    float radius = s.w;
+    V3 oe, de;
+    Ray ray;
+    ray.o = xf_point_err(xf.ci, rw.o, &oe);
+    ray.d = xf_vec_err_id(rw.d, &de);
+    ray.t_max = t_max;
+    ray.time = rw.time;
+    float ls = length_squared(ray.d);
+    if (ls > 0.0f) {
+        float dt = dot(vabs(ray.d), oe) / ls;
+        ray.o = ray.o + ray.d * dt;
+    }
+    EF ox = ef(ray.o.x, oe.x), oy = ef(ray.o.y, oe.y), oz = ef(ray.o.z, oe.z);
+    EF dx = ef(ray.d.x, de.x), dy = ef(ray.d.y, de.y), dz = ef(ray.d.z, de.z);
+    EF a = dx * dx + dy * dy + dz * dz;
+    EF b = ef(2.0f) * (dx * ox + dy * oy + dz * oz);
+    EF c = ox * ox + oy * oy + oz * oz - ef(radius) * ef(radius);
+    EF t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0.hi > t_max || t1.lo <= 0.0f) return false;
+    EF tsh = t0;
+    if (tsh.lo <= 0.0f) {
+        tsh = t1;
+        if (tsh.hi > t_max) return false;
+    }
+    // full sphere: the z-range / phi_max clipping of sphere.rs:127-161 never triggers
+    if (out) {
+        out->t = tsh.v;
+        out->ray_obj = ray;
+    }
+    return true;
+}
+
+// Sphere interaction (sphere.rs:163-236 + Interaction::transform, interaction.rs:268-300).
+BG_D void sphere_isect(float4 s, const SphHit& h, const Ray& rw, Isect* it) {
+    const float radius = s.w;
+    const float phi_max = 360.0f * (PI / 180.0f);
+    const float theta_min = acosf(rclamp(-radius / radius, -1.0f, 1.0f));
+    const float theta_max = acosf(rclamp(radius / radius, -1.0f, 1.0f));
+    V3 ph = h.ray_obj.o + h.ray_obj.d * h.t;  // refine (sphere.rs:119-124)
+    ph = ph * (radius / length(ph - v3(0.0f, 0.0f, 0.0f)));
+    if (ph.x == 0.0f && ph.y == 0.0f) ph.x = 1e-5f * radius;
+    float theta = acosf(rclamp(ph.z / radius, -1.0f, 1.0f));
+    float z_radius = sqrtf(ph.x * ph.x + ph.y * ph.y);
+    float inv_zr = 1.0f / z_radius;
+    float cos_phi = ph.x * inv_zr, sin_phi = ph.y * inv_zr;
+    V3 dpdu = v3(-phi_max * ph.y, phi_max * ph.x, 0.0f);
+    V3 dpdv = (theta_max - theta_min) * v3(ph.z * cos_phi, ph.z * sin_phi, -radius * sinf(theta));
+    V3 perr = gamma(5.0f) * vabs(ph);
+    V3 n = normalize(cross(dpdu, dpdv));
+    SphereXf xf = sphere_xf(s);
+    // transform_with_point_error (point3.rs:102-140) with translation xf.c
+    float g3 = gamma(3.0f);
+    V3 p;
+    p.x = (1.0f * ph.x + 0.0f * ph.y) + (0.0f * ph.z + xf.c.x);
+    p.y = (0.0f * ph.x + 1.0f * ph.y) + (0.0f * ph.z + xf.c.y);
+    p.z = (0.0f * ph.x + 0.0f * ph.y) + (1.0f * ph.z + xf.c.z);
+    V3 ae;
+    ae.x = (g3 + 1.0f) * (1.0f * perr.x + 0.0f * perr.y + 0.0f * perr.z) +
+           g3 * (fabsf(1.0f * ph.x) + fabsf(0.0f * ph.y) + fabsf(0.0f * ph.z) + fabsf(xf.c.x));
+    ae.y = (g3 + 1.0f) * (0.0f * perr.x + 1.0f * perr.y + 0.0f * perr.z) +
+           g3 * (fabsf(0.0f * ph.x) + fabsf(1.0f * ph.y) + fabsf(0.0f * ph.z) + fabsf(xf.c.y));
+    ae.z = (g3 + 1.0f) * (0.0f * perr.x + 0.0f * perr.y + 1.0f * perr.z) +
+           g3 * (fabsf(0.0f * ph.x) + fabsf(0.0f * ph.y) + fabsf(1.0f * ph.z) + fabsf(xf.c.z));
+    it->p = p;
+    it->p_err = ae;
+    it->time = rw.time;
+    it->wo = xf_vec_id(-h.ray_obj.d);
+    // Normal::transform uses m_inverse^T: identity 3x3 for a translation
+    V3 nt = xf_vec_id(n);
+    it->n = normalize(nt);
+    it->ns = face_forward(normalize(nt), it->n);
+    it->dpdu = xf_vec_id(dpdu);
+}
+
+// Point3::offset_ray_origin (point3.rs:31-49)
+BG_D V3 offset_ray_origin(V3 p, V3 perr, V3 n, V3 w) {
+    V3 offset = dot(vabs(n), perr) * n;
+    if (dot(w, n) < 0.0f) offset = -offset;
+    V3 po = p + offset;
+    if (offset.x > 0.0f) po.x = next_float_up(po.x);
+    else if (offset.x < 0.0f) po.x = next_float_down(po.x);
+    if (offset.y > 0.0f) po.y = next_float_up(po.y);
+    else if (offset.y < 0.0f) po.y = next_float_down(po.y);
+    if (offset.z > 0.0f) po.z = next_float_up(po.z);
+    else if (offset.z < 0.0f) po.z = next_float_down(po.z);
+    return po;
+}
+// Interaction::spawn_ray (interaction.rs:115-121): t_max 1 - 0.0001 in the reference (F3),
+// infinity in PBRT mode.
+BG_D Ray spawn_ray(V3 p, V3 perr, V3 n, float time, V3 d, bool ref_compat) {
+    Ray r;
+    r.o = offset_ray_origin(p, perr, n, d);
+    r.d = d;
+    r.t_max = ref_compat ? (1.0f - 0.0001f) : INFINITY;
+    r.time = time;
+    return r;
+}
+// Interaction::spawn_ray_to_it (interaction.rs:132-143)
+BG_D Ray spawn_ray_to(V3 p, V3 perr, V3 n, float time, V3 q, V3 qerr, V3 qn) {
+    V3 o = offset_ray_origin(p, perr, n, q - p);
+    V3 target = offset_ray_origin(q, qerr, qn, o - q);
+    Ray r;
+    r.o = o;
+    r.d = target - o;
+    r.t_max = 1.0f - 0.0001f;
+    r.time = time;
+    return r;
+}
+
+// Triangle::sample (triangle.rs:522-559) with uniform_sample_triangle (sampling.rs:233-236).
+struct ShapeSample {
+    V3 p, p_err, n;
+    float pdf_area;
+};
+BG_D ShapeSample tri_sample(V3 p0, V3 p1, V3 p2, float u0, float u1) {
+    ShapeSample s;
+    float sq = sqrtf(u0);
+    float b0 = 1.0f - sq, b1 = u1 * sq;
+    float b2 = 1.0f - b0 - b1;
+    s.p = b0 * p0 + b1 * p1 + b2 * p2;
+    s.n = normalize(cross(p1 - p0, p2 - p0));
+    V3 pabs = vabs(b0 * p0) + vabs(b1 * p1) + vabs(b2 * p2);
+    s.p_err = gamma(6.0f) * pabs;
+    s.pdf_area = 1.0f / tri_area(p0, p1, p2);
+    return s;
+}
+
+BG_D void load_tri(const Scene& sc, uint32_t prim, V3* p0, V3* p1, V3* p2) {
+    float4 a = sc.tri[3 * prim], b = sc.tri[3 * prim + 1], c = sc.tri[3 * prim + 2];
+    *p0 = f4xyz(a);
+    *p1 = f4xyz(b);
+    *p2 = f4xyz(c);
+}
+
+// Full closest-hit interaction for a primitive given the ray (re-runs the shape test with
+// t_max = infinity, which reproduces the traversal's t, barycentrics and hit side).
+BG_D bool prim_isect(const Scene& sc, int prim, const Ray& ray, Isect* it) {
+    if ((uint32_t)prim < sc.ntri) {
+        V3 p0, p1, p2;
+        load_tri(sc, (uint32_t)prim, &p0, &p1, &p2);
+        TriRay tr = make_tri_ray(ray);
+        TriHit h;
+        if (!tri_test(tr, INFINITY, p0, p1, p2, &h)) return false;
+        tri_isect(p0, p1, p2, h, ray, it);
+    } else {
+        float4 s = sc.sph[prim - sc.ntri];
+        SphHit h;
+        if (!sphere_test(s, ray, INFINITY, &h)) return false;
+        sphere_isect(s, h, ray, it);
+    }
+    it->prim = prim;
+    return true;
+}
+
+}  // namespace bg

@@ -1,0 +1,235 @@
+// bg_traverse.cuh - closest-hit and any-hit traversal of the two BVH layouts.
+//
+// RefBVH: the reference's binary BVH exactly as BVH::intersect / intersect_test walk it
+// (src/accelerators/bvh.rs:281-423): same node order, near child first by the sign of the
+// direction along the split axis, PBRT's robust slab test (src/geometries/bounds3.rs:246-288),
+// leaf primitives in ordered_primitives order, a hit at t == t_max replacing the previous one.
+// REF_COMPAT renders need this walk: whether the same camera ray re-hits its surface (the
+// reference never re-spawns its path, src/integrators/path.rs:70-143) depends on the exact leaf
+// bounds the slab test sees.
+//
+// Bvh2: the library's own 2-wide BVH (both child boxes stored in the parent, 64 B nodes read as
+// four 128-bit loads) for PBRT-mode rendering and the ray-query entry points.  Slab test uses
+// fma with a precomputed origin * inv_dir and the same (1 + 2*gamma(3)) far-bound enlargement.
+#pragma once
+#include "bg_device.h"
+#include "bg_math.cuh"
+#include "bg_shapes.cuh"
+
+namespace bg {
+
+// ---------------------------------------------------------------- reference layout
+BG_D bool ref_slab(const RefNode& nd, const Ray& ray, V3 inv, const int neg[3]) {
+    const float k = 1.0f + 2.0f * gamma(3.0f);
+    float bx0 = neg[0] ? nd.mx[0] : nd.mn[0], bx1 = neg[0] ? nd.mn[0] : nd.mx[0];
+    float by0 = neg[1] ? nd.mx[1] : nd.mn[1], by1 = neg[1] ? nd.mn[1] : nd.mx[1];
+    float bz0 = neg[2] ? nd.mx[2] : nd.mn[2], bz1 = neg[2] ? nd.mn[2] : nd.mx[2];
+    float t_min = (bx0 - ray.o.x) * inv.x;
+    float t_max = (bx1 - ray.o.x) * inv.x;
+    float ty_min = (by0 - ray.o.y) * inv.y;
+    float ty_max = (by1 - ray.o.y) * inv.y;
+    t_max *= k;
+    ty_max *= k;
+    if (t_min > ty_max || ty_min > t_max) return false;
+    if (ty_min > t_min) t_min = ty_min;
+    if (ty_max < t_max) t_max = ty_max;
+    float tz_min = (bz0 - ray.o.z) * inv.z;
+    float tz_max = (bz1 - ray.o.z) * inv.z;
+    tz_max *= k;
+    if (t_min > tz_max || tz_min > t_max) return false;
+    if (tz_min > t_min) t_min = tz_min;
+    if (tz_max < t_max) t_max = tz_max;
+    return (t_min < ray.t_max) && (t_max > 0.0f);
+}
+
+// Primitive test against the current t_max; updates ray.t_max on a closest hit.
+BG_D bool prim_hit(const Scene& sc, uint32_t prim, const TriRay& tr, Ray& ray, bool closest) {
+    if (prim < sc.ntri) {
+        V3 p0, p1, p2;
+        load_tri(sc, prim, &p0, &p1, &p2);
+        TriHit h;
+        if (!tri_test(tr, ray.t_max, p0, p1, p2, &h)) return false;
+        if (closest) ray.t_max = h.t;
+        return true;
+    }
+    SphHit h;
+    if (!sphere_test(sc.sph[prim - sc.ntri], ray, ray.t_max, closest ? &h : nullptr)) return false;
+    if (closest) ray.t_max = h.t;
+    return true;
+}
+
+// BVH::intersect: returns the hit prim (or -1) and leaves the hit distance in ray.t_max.
+// counters (optional): [0] node visits, [1] primitive tests.
+template <bool ANY>
+BG_D int ref_traverse(const Scene& sc, Ray& ray, uint32_t* err, unsigned long long* counters) {
+    if (sc.ref_nnodes == 0) return -1;
+    V3 inv = v3(1.0f / ray.d.x, 1.0f / ray.d.y, 1.0f / ray.d.z);
+    int neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+    TriRay tr = make_tri_ray(ray);
+    uint32_t stack[TRAVERSAL_STACK];
+    int sp = 0;
+    uint32_t cur = 0;
+    int hit = -1;
+    unsigned long long visits = 0, tests = 0;
+    for (;;) {
+        if (cur >= sc.ref_nnodes) {
+            atomicOr(err, ERR_BAD_NODE);
+            break;
+        }
+        const RefNode nd = sc.ref_nodes[cur];
+        ++visits;
+        uint32_t count = nd.count_axis >> 2;
+        if (ref_slab(nd, ray, inv, neg)) {
+            if (count > 0) {
+                for (uint32_t i = 0; i < count; ++i) {
+                    uint32_t prim = sc.ref_order[nd.offset + i];
+                    ++tests;
+                    if (prim_hit(sc, prim, tr, ray, !ANY)) {
+                        hit = (int)prim;
+                        if (ANY) goto done;
+                    }
+                }
+                if (sp == 0) break;
+                cur = stack[--sp];
+            } else {
+                if (sp >= TRAVERSAL_STACK) {
+                    atomicOr(err, ERR_STACK_OVERFLOW);
+                    hit = -1;
+                    break;
+                }
+                if (neg[nd.count_axis & 3]) {
+                    stack[sp++] = cur + 1;
+                    cur = nd.offset;
+                } else {
+                    stack[sp++] = nd.offset;
+                    cur = cur + 1;
+                }
+            }
+        } else {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+done:
+    if (counters) {
+        atomicAdd(&counters[0], visits);
+        atomicAdd(&counters[1], tests);
+    }
+    return hit;
+}
+
+// ---------------------------------------------------------------- 2-wide layout
+struct FastRay {
+    V3 inv, oi;  // 1/d and o/d (so t = fma(b, inv, -oi))
+};
+BG_D float safe_dir(float d) { return fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d); }
+BG_D FastRay make_fast_ray(const Ray& r) {
+    FastRay f;
+    f.inv = v3(1.0f / safe_dir(r.d.x), 1.0f / safe_dir(r.d.y), 1.0f / safe_dir(r.d.z));
+    f.oi = v3(r.o.x * f.inv.x, r.o.y * f.inv.y, r.o.z * f.inv.z);
+    return f;
+}
+// Returns entry distance, or +inf on a miss (the box must start before t_max and end after 0).
+BG_D float box_enter(float lox, float hix, float loy, float hiy, float loz, float hiz, const FastRay& f,
+                     float t_max) {
+    const float k = 1.0f + 2.0f * gamma(3.0f);
+    float tx0 = fmaf(lox, f.inv.x, -f.oi.x), tx1 = fmaf(hix, f.inv.x, -f.oi.x);
+    float ty0 = fmaf(loy, f.inv.y, -f.oi.y), ty1 = fmaf(hiy, f.inv.y, -f.oi.y);
+    float tz0 = fmaf(loz, f.inv.z, -f.oi.z), tz1 = fmaf(hiz, f.inv.z, -f.oi.z);
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1)) * k;
+    return (tn <= tf && tn < t_max) ? tn : INFINITY;
+}
+
+// Leaf slot: triangle = (p0, id) (p1, -) (p2, -); sphere = (center, id | SPHERE_BIT) (radius, -, -, -).
+BG_D bool leaf_prim_hit(const Scene& sc, uint32_t slot, const TriRay& tr, Ray& ray, bool closest, int* prim) {
+    float4 a = __ldg(&sc.leaf_prims[3 * slot]);
+    float4 b = __ldg(&sc.leaf_prims[3 * slot + 1]);
+    uint32_t id = __float_as_uint(a.w);
+    if (!(id & SPHERE_BIT)) {
+        float4 c = __ldg(&sc.leaf_prims[3 * slot + 2]);
+        TriHit h;
+        if (!tri_test(tr, ray.t_max, f4xyz(a), f4xyz(b), f4xyz(c), &h)) return false;
+        if (closest) ray.t_max = h.t;
+        *prim = (int)id;
+        return true;
+    }
+    SphHit h;
+    if (!sphere_test(make_float4(a.x, a.y, a.z, b.x), ray, ray.t_max, closest ? &h : nullptr)) return false;
+    if (closest) ray.t_max = h.t;
+    *prim = (int)(id & ~SPHERE_BIT) + (int)sc.ntri;
+    return true;
+}
+
+// While-while traversal (Aila & Laine, HPG 2009) over the 2-wide layout.  Returns the hit prim
+// (ANY: the first hit found) and leaves the closest distance in ray.t_max.  `skip` excludes one
+// primitive (any-hit only).  Stack entries: inner node index, or a leaf as (count, ~first).
+template <bool ANY>
+BG_D int bvh2_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) {
+    if (sc.n_nodes == 0) return -1;
+    FastRay f = make_fast_ray(ray);
+    TriRay tr = make_tri_ray(ray);
+    int stack[TRAVERSAL_STACK];
+    int sp = 0;
+    int node = 0;  // >= 0: inner node to visit; -1: leaf pending; -2: nothing, pop
+    int hit = -1;
+    int leaf_first = 0, leaf_count = 0;
+    for (;;) {
+        while (node >= 0) {
+            const Bvh2Node* n = sc.nodes + node;
+            float4 a = __ldg(&n->c0xy), b = __ldg(&n->c1xy), c = __ldg(&n->c01z);
+            int4 ch = __ldg(&n->child);
+            float t0 = box_enter(a.x, a.y, a.z, a.w, c.x, c.y, f, ray.t_max);
+            float t1 = box_enter(b.x, b.y, b.z, b.w, c.z, c.w, f, ray.t_max);
+            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+            if (!h0 && !h1) {
+                node = -2;
+                break;
+            }
+            int first = h0 ? ch.x : ch.y, cfirst = h0 ? ch.z : ch.w;
+            if (h0 && h1) {
+                int second = ch.y, csecond = ch.w;
+                if (t1 < t0) {
+                    first = ch.y;
+                    cfirst = ch.w;
+                    second = ch.x;
+                    csecond = ch.z;
+                }
+                if (sp + 2 > TRAVERSAL_STACK) {
+                    atomicOr(err, ERR_STACK_OVERFLOW);
+                    return hit;
+                }
+                if (second < 0) stack[sp++] = csecond;
+                stack[sp++] = second;
+            }
+            if (first < 0) {
+                leaf_first = ~first;
+                leaf_count = cfirst;
+                node = -1;
+            } else {
+                node = first;
+            }
+        }
+        if (node == -1) {
+            for (int i = 0; i < leaf_count; ++i) {
+                int prim;
+                if (leaf_prim_hit(sc, (uint32_t)(leaf_first + i), tr, ray, !ANY, &prim)) {
+                    if (ANY && prim == skip) continue;
+                    hit = prim;
+                    if (ANY) return hit;
+                }
+            }
+        }
+        if (sp == 0) return hit;
+        int e = stack[--sp];
+        if (e < 0) {
+            leaf_first = ~e;
+            leaf_count = stack[--sp];
+            node = -1;
+        } else {
+            node = e;
+        }
+    }
+}
+
+}  // namespace bg

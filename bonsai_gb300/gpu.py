@@ -1,0 +1,187 @@
+"""Python handle on libbonsai_gpu.so (ctypes over include/bonsai_gpu.h).
+
+Mirrors the reference's integrator surface: a ``Scene`` is built once from shapes, materials and
+area lights (BVH::new + Scene::new, src/accelerators/bvh.rs:53-89, src/base/scene.rs:16-33) and a
+``PathIntegrator(camera, max_depth, rr_threshold)`` renders it (src/integrators/path.rs:27-39,
+SamplerIntegrator::render, src/base/integrator.rs:35-133).  Every call goes through the C ABI;
+errors raise ``BonsaiError`` with the library's message.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import weakref
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+from . import scenes as S
+
+
+class BonsaiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{status} ({A.load().bg_status_string(status).decode()}): {msg}")
+        self.status = status
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One CUDA device + stream (bg_ctx)."""
+
+    def __init__(self, device: int = 0, max_queue_paths: int = 0, memory_cap_bytes: int = 0):
+        self.lib = A.load()
+        o = A.bg_device_opts()
+        o.device = device
+        o.max_queue_paths = max_queue_paths
+        o.memory_cap_bytes = memory_cap_bytes
+        h = C.c_void_p()
+        st = self.lib.bg_create(C.byref(o), C.byref(h))
+        if st != A.BG_OK:
+            raise BonsaiError(st, "bg_create failed")
+        self.h = h
+        self._scenes: weakref.WeakSet = weakref.WeakSet()
+
+    def check(self, st: int):
+        if st != A.BG_OK:
+            raise BonsaiError(st, self.lib.bg_last_error(self.h).decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            for sc in list(getattr(self, "_scenes", [])):
+                sc.close()
+            self.lib.bg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def flush_l2(self):
+        self.check(self.lib.bg_flush_l2(self.h))
+
+    def synchronize(self):
+        self.check(self.lib.bg_synchronize(self.h))
+
+    # raw device buffers (for device-resident timing)
+    def alloc(self, nbytes: int) -> C.c_void_p:
+        p = C.c_void_p()
+        self.check(self.lib.bg_device_alloc(self.h, nbytes, C.byref(p)))
+        return p
+
+    def free(self, p: C.c_void_p):
+        self.check(self.lib.bg_device_free(self.h, p))
+
+    def h2d(self, dst: C.c_void_p, src: np.ndarray):
+        self.check(self.lib.bg_memcpy_h2d(self.h, dst, _ptr(src), src.nbytes))
+
+    def d2h(self, dst: np.ndarray, src: C.c_void_p):
+        self.check(self.lib.bg_memcpy_d2h(self.h, _ptr(dst), src, dst.nbytes))
+
+
+class Scene:
+    """Device scene (bg_scene) built from a ``scenes.SceneData``."""
+
+    def __init__(self, ctx: Context, sd: S.SceneData, bvh: int = A.BG_BVH_WIDE):
+        self.ctx, self.sd = ctx, sd
+        lib = ctx.lib
+        h = C.c_void_p()
+        ctx.check(lib.bg_scene_create(ctx.h, C.byref(h)))
+        self.h = h
+        ctx._scenes.add(self)
+        for m in sd.materials:
+            mm = A.bg_material.from_buffer_copy(np.ascontiguousarray(m).tobytes())
+            ctx.check(lib.bg_scene_add_material(h, C.byref(mm), None))
+        for l in sd.lights:
+            ll = A.bg_area_light.from_buffer_copy(np.ascontiguousarray(l).tobytes())
+            ctx.check(lib.bg_scene_add_area_light(h, C.byref(ll), None))
+        tri = np.ascontiguousarray(sd.tri, np.float32)
+        tm = np.ascontiguousarray(sd.tri_mat, np.uint32)
+        tl = np.ascontiguousarray(sd.tri_light, np.int32)
+        ctx.check(lib.bg_scene_add_triangles(h, _ptr(tri), sd.ntri, _ptr(tm), _ptr(tl)))
+        if sd.nsph:
+            sp = np.ascontiguousarray(sd.spheres)
+            ctx.check(lib.bg_scene_add_spheres(h, _ptr(sp), sd.nsph))
+        st = A.bg_build_stats()
+        ctx.check(lib.bg_scene_commit(h, bvh, C.byref(st)))
+        self.build_ms, self.nodes, self.bvh = st.build_ms, st.nodes, bvh
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.bg_scene_destroy(self.h)  # safe after bg_destroy: the scene is orphaned
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def trace(self, rays: np.ndarray, any_hit: bool = False) -> np.ndarray:
+        rays = np.ascontiguousarray(rays)
+        if any_hit:
+            occ = np.zeros(len(rays), np.uint8)
+            self.ctx.check(self.ctx.lib.bg_trace_any(self.ctx.h, self.h, _ptr(rays), len(rays), _ptr(occ)))
+            return occ
+        hits = np.zeros(len(rays), S.HIT_DT)
+        self.ctx.check(self.ctx.lib.bg_trace_closest(self.ctx.h, self.h, _ptr(rays), len(rays), _ptr(hits)))
+        return hits
+
+    def trace_device(self, d_rays, n: int, d_out, any_hit: bool = False) -> float:
+        ms = C.c_float()
+        fn = self.ctx.lib.bg_trace_any_device if any_hit else self.ctx.lib.bg_trace_closest_device
+        self.ctx.check(fn(self.ctx.h, self.h, d_rays, n, d_out, C.byref(ms)))
+        return ms.value
+
+
+def camera_struct(cam: S.Camera) -> A.bg_camera:
+    c = A.bg_camera()
+    c.position[:] = cam.position
+    c.look_at[:] = cam.look_at
+    c.up[:] = cam.up
+    c.fov_deg = cam.fov_deg
+    c.near_plane = cam.near_plane
+    c.far_plane = cam.far_plane
+    c.lens_radius = 0.0
+    c.focal_distance = 1e6
+    c.width = cam.width
+    c.height = cam.height
+    return c
+
+
+@dataclass
+class RenderResult:
+    rgb: np.ndarray
+    stats: A.bg_render_stats
+
+
+class PathIntegrator:
+    """PathIntegrator::new(camera, sampler, max_depth, rr_threshold) rendering on the GPU."""
+
+    def __init__(self, camera: S.Camera, spp: int, max_depth: int, rr_threshold: float = 1.0,
+                 mode: int = A.BG_MODE_PBRT, seed: int = 0):
+        self.camera, self.spp, self.max_depth = camera, spp, max_depth
+        self.rr_threshold, self.mode, self.seed = rr_threshold, mode, seed
+
+    def render(self, scene: Scene, first_sample: int = 0, accumulate: bool = False, readback: bool = True,
+               spp: int | None = None) -> RenderResult:
+        ctx = scene.ctx
+        c = camera_struct(self.camera)
+        o = A.bg_render_opts()
+        o.spp = self.spp if spp is None else spp
+        o.max_depth = self.max_depth
+        o.rr_threshold = self.rr_threshold
+        o.mode = self.mode
+        o.seed = self.seed
+        o.first_sample = first_sample
+        o.flags = (A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK)
+        rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
+        st = A.bg_render_stats()
+        ctx.check(ctx.lib.bg_render(ctx.h, scene.h, C.byref(c), C.byref(o), _ptr(rgb), C.byref(st)))
+        return RenderResult(rgb, st)
+
+    @staticmethod
+    def moments(ctx: Context, width: int, height: int):
+        s1 = np.zeros((height, width, 3), np.float64)
+        s2 = np.zeros((height, width, 3), np.float64)
+        n = np.zeros((height, width), np.uint32)
+        ctx.check(ctx.lib.bg_film_moments(ctx.h, _ptr(s1), _ptr(s2), _ptr(n)))
+        return s1, s2, n

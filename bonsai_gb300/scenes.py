@@ -1,0 +1,313 @@
+"""Seeded synthetic workloads of the path-tracing hot path.
+
+No public benchmark or dataset is involved: every scene here is generated from a stated seed so
+the device path and the CPU oracle receive bit-identical float32 inputs.
+
+* ``cornell()``      - the Cornell box (256x256, 16 spp, max depth 5)
+* ``ray_soup()``     - 2M random triangles + 16M random rays (closest-hit / any-hit microbenchmark)
+* ``production()``   - 1920x1080 scene: 64 fBm-displaced level-5 icospheres (1.31M triangles),
+                       2000 lognormal spheres, ground quad, 4 quad area lights, 64 spp, depth 8
+
+Scene records use numpy structured dtypes whose layout equals the C structs of bonsai_gpu.h.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+MATERIAL_DT = np.dtype([("type", "<u4"), ("kd", "<f4", 3), ("ks", "<f4", 3), ("roughness", "<f4"),
+                        ("remap_roughness", "<u4"), ("eta", "<f4", 3), ("k", "<f4", 3),
+                        ("ior", "<f4")])
+LIGHT_DT = np.dtype([("intensity", "<f4", 3), ("two_sided", "<u4")])
+SPHERE_DT = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("material_id", "<u4"),
+                      ("light_id", "<i4")])
+RAY_DT = np.dtype([("org", "<f4", 3), ("tmax", "<f4"), ("dir", "<f4", 3), ("pad", "<f4")])
+HIT_DT = np.dtype([("prim", "<i4"), ("t", "<f4")])
+
+MATTE, PLASTIC, CONDUCTOR, DIELECTRIC = 0, 1, 2, 3
+
+# Conductor constants (copper, RGB): one fixed triple used identically on CPU and GPU.
+COPPER_ETA = (0.200438, 0.924033, 1.10221)
+COPPER_K = (3.91295, 2.45285, 2.14219)
+
+
+def material(kind: int, kd=(0, 0, 0), ks=(0, 0, 0), roughness=0.0, remap=False,
+             eta=COPPER_ETA, k=COPPER_K, ior=1.5) -> np.ndarray:
+    m = np.zeros((), MATERIAL_DT)
+    m["type"] = kind
+    m["kd"] = kd
+    m["ks"] = ks
+    m["roughness"] = roughness
+    m["remap_roughness"] = int(remap)
+    m["eta"] = eta
+    m["k"] = k
+    m["ior"] = ior
+    return m
+
+
+@dataclass
+class Camera:
+    position: tuple
+    look_at: tuple
+    up: tuple
+    fov_deg: float
+    width: int
+    height: int
+    near_plane: float = 0.01
+    far_plane: float = 1000.0
+
+
+@dataclass
+class SceneData:
+    """Flat scene: triangle soup (n, 9) + spheres + materials + emission records."""
+    tri: np.ndarray                      # (ntri, 9) float32, world space p0 p1 p2
+    tri_mat: np.ndarray                  # (ntri,) uint32
+    tri_light: np.ndarray                # (ntri,) int32, emission record or -1
+    spheres: np.ndarray                  # (nsph,) SPHERE_DT
+    materials: np.ndarray                # (nmat,) MATERIAL_DT
+    lights: np.ndarray                   # (nlights,) LIGHT_DT
+    camera: Camera | None = None
+    spp: int = 16
+    max_depth: int = 5
+    rr_threshold: float = 1.0
+    name: str = ""
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def ntri(self) -> int:
+        return int(self.tri.shape[0])
+
+    @property
+    def nsph(self) -> int:
+        return int(self.spheres.shape[0])
+
+
+def _quad(a, b, c, d, normal):
+    """Two triangles (a,b,c), (a,c,d) wound so (p1-p0)x(p2-p0) points along `normal`."""
+    a, b, c, d = (np.asarray(v, np.float32) for v in (a, b, c, d))
+    n = np.cross(b - a, c - a)
+    if np.dot(n, np.asarray(normal, np.float32)) < 0:
+        b, d = d, b
+    return np.stack([np.concatenate([a, b, c]), np.concatenate([a, c, d])]).astype(np.float32)
+
+
+def cornell(width: int = 256, height: int = 256, spp: int = 16, max_depth: int = 5) -> SceneData:
+    """Cornell box in [-1,1]^3: 5 diffuse walls (10 triangles, inward normals), a 0.5x0.5 ceiling
+    light at y=0.999 (2 triangles, emission (17,12,4)), a diffuse and a Trowbridge-Reitz
+    conductor sphere (r=0.3), pinhole camera at (0,0,3.5) looking at the origin, fov 40.
+
+    The light is two-sided: the reference's DiffuseAreaLight::sample_point evaluates emission
+    toward +wi (src/lights/diffuse.rs:67), so a one-sided light facing the room returns black
+    light samples there and the reference image would be dark apart from the light itself.
+    """
+    grey, red, green = (0.725, 0.725, 0.725), (0.63, 0.065, 0.05), (0.14, 0.45, 0.091)
+    mats = [material(MATTE, kd=grey), material(MATTE, kd=red), material(MATTE, kd=green),
+            material(CONDUCTOR, roughness=0.1), material(MATTE, kd=(0, 0, 0))]
+    tris, tmat = [], []
+
+    def add(q, m):
+        tris.append(q)
+        tmat.extend([m] * len(q))
+    add(_quad((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (0, 1, 0)), 0)   # floor
+    add(_quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), (0, -1, 0)), 0)      # ceiling
+    add(_quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1)), 0)   # back
+    add(_quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), (1, 0, 0)), 1)   # left (red)
+    add(_quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), (-1, 0, 0)), 2)      # right (green)
+    nwall = sum(len(t) for t in tris)
+    add(_quad((-0.25, 0.999, -0.25), (0.25, 0.999, -0.25), (0.25, 0.999, 0.25), (-0.25, 0.999, 0.25),
+              (0, -1, 0)), 4)
+    tri = np.concatenate(tris).astype(np.float32)
+    tri_light = np.full(len(tri), -1, np.int32)
+    tri_light[nwall:] = 0
+    sph = np.zeros(2, SPHERE_DT)
+    sph[0] = ((-0.4, -0.7, -0.3), 0.3, 0, -1)
+    sph[1] = ((0.4, -0.7, 0.3), 0.3, 3, -1)
+    lights = np.zeros(1, LIGHT_DT)
+    lights[0] = ((17.0, 12.0, 4.0), 1)
+    cam = Camera((0.0, 0.0, 3.5), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
+    return SceneData(tri, np.asarray(tmat, np.uint32), tri_light, sph, np.stack(mats), lights, cam,
+                     spp=spp, max_depth=max_depth, rr_threshold=1.0, name="cornell")
+
+
+def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def random_triangles(n: int, seed: int = 1) -> np.ndarray:
+    """n equilateral triangles: centroids U[0,1]^3, edge U[0.002,0.02], uniform random rotation."""
+    rng = np.random.default_rng(seed)
+    cen = rng.random((n, 3))
+    edge = rng.uniform(0.002, 0.02, n)
+    rot = _random_rotations(rng, n)
+    ang = np.array([0.0, 2 * np.pi / 3, 4 * np.pi / 3])
+    local = np.stack([np.cos(ang), np.sin(ang), np.zeros(3)], -1)  # (3,3) unit circumradius
+    circ = edge / np.sqrt(3.0)
+    verts = cen[:, None, :] + circ[:, None, None] * np.einsum("nij,vj->nvi", rot, local)
+    return verts.reshape(n, 9).astype(np.float32)
+
+
+def random_rays(n: int, seed: int = 2) -> np.ndarray:
+    """n rays: origins uniform on the unit cube surface (face uniform), directions uniform on S^2."""
+    rng = np.random.default_rng(seed)
+    face = rng.integers(0, 6, n)
+    uv = rng.random((n, 2))
+    org = np.empty((n, 3))
+    axis = face // 2
+    side = (face % 2).astype(np.float64)
+    for a in range(3):
+        m = axis == a
+        o = np.empty((m.sum(), 3))
+        others = [i for i in range(3) if i != a]
+        o[:, a] = side[m]
+        o[:, others[0]] = uv[m, 0]
+        o[:, others[1]] = uv[m, 1]
+        org[m] = o
+    z = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2 * np.pi, n)
+    r = np.sqrt(np.maximum(0.0, 1 - z * z))
+    d = np.stack([r * np.cos(phi), r * np.sin(phi), z], -1)
+    rays = np.zeros(n, RAY_DT)
+    rays["org"] = org.astype(np.float32)
+    rays["dir"] = d.astype(np.float32)
+    rays["tmax"] = np.float32(np.inf)
+    return rays
+
+
+def ray_soup(ntri: int = 2_097_152, nrays: int = 16_777_216):
+    """Ray/BVH microbenchmark: triangle soup (seed 1) + ray set (seed 2).  All triangles diffuse."""
+    tri = random_triangles(ntri, seed=1)
+    sd = SceneData(tri, np.zeros(ntri, np.uint32), np.full(ntri, -1, np.int32),
+                   np.zeros(0, SPHERE_DT), np.stack([material(MATTE, kd=(0.5, 0.5, 0.5))]),
+                   np.zeros(0, LIGHT_DT), name=f"ray_soup_{ntri}")
+    return sd, random_rays(nrays, seed=2)
+
+
+# ---------------------------------------------------------------- icospheres + fBm
+def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere: (vertices (V,3) float64, faces (F,3) int).  Level 5 has 20480 faces."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+         (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+         (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.asarray(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = f
+    for _ in range(level):
+        cache: dict = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.asarray(verts), np.asarray(faces, np.int64)
+
+
+def _value_noise(p: np.ndarray, perm: np.ndarray, vals: np.ndarray) -> np.ndarray:
+    """3D value noise in [-1,1]: hashed lattice values, smoothstep trilinear interpolation."""
+    pi = np.floor(p).astype(np.int64)
+    pf = p - pi
+    w = pf * pf * (3 - 2 * pf)
+    out = 0.0
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                h = perm[(perm[(perm[(pi[:, 0] + dx) & 255] + pi[:, 1] + dy) & 255] + pi[:, 2] + dz) & 255]
+                wx = w[:, 0] if dx else 1 - w[:, 0]
+                wy = w[:, 1] if dy else 1 - w[:, 1]
+                wz = w[:, 2] if dz else 1 - w[:, 2]
+                out = out + wx * wy * wz * vals[h]
+    return out
+
+
+def fbm(p: np.ndarray, seed: int, octaves: int = 5, base_freq: float = 2.0) -> np.ndarray:
+    """Fractal Brownian motion of value noise, normalised to [-1,1]."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(256)
+    vals = rng.uniform(-1, 1, 256)
+    total, amp, norm = 0.0, 1.0, 0.0
+    for o in range(octaves):
+        total = total + amp * _value_noise(p * (base_freq * 2 ** o) + 17.31 * o, perm, vals)
+        norm += amp
+        amp *= 0.5
+    return total / norm
+
+
+def production(width: int = 1920, height: int = 1080, spp: int = 64, max_depth: int = 8,
+               n_ico: int = 64, ico_level: int = 5, n_spheres: int = 2000, seed: int = 3) -> SceneData:
+    """1080p production-style scene (defaults are the full size).
+
+    64 level-5 icospheres (20480 triangles each, 1.31M total), radially displaced by seeded fBm
+    (amplitude 0.1 r, 5 octaves) on an 8x8 jittered grid; 2000 analytic spheres with lognormal radii
+    (mu=-3, sigma=0.5); a ground quad (2 triangles); 4 one-sided quad area lights facing down.
+    Materials per object (seed 3): 50% diffuse (albedo U[0.1,0.9]), 30% Trowbridge-Reitz conductor
+    (roughness U[0.05,0.5], copper eta/k), 20% dielectric (IOR 1.5).
+    """
+    rng = np.random.default_rng(seed)
+    uv, uf = icosphere(ico_level)
+    mats = [material(MATTE, kd=(0.5, 0.5, 0.5)), material(MATTE, kd=(0, 0, 0))]  # ground, light
+
+    def random_material():
+        r = rng.random()
+        if r < 0.5:
+            return material(MATTE, kd=tuple(rng.uniform(0.1, 0.9, 3)))
+        if r < 0.8:
+            return material(CONDUCTOR, roughness=float(rng.uniform(0.05, 0.5)))
+        return material(DIELECTRIC, ior=1.5)
+
+    tris, tmat = [], []
+    g = int(np.ceil(np.sqrt(n_ico)))
+    cells = np.linspace(-9, 9, g)
+    for i in range(n_ico):
+        gx, gz = cells[i % g], cells[(i // g) % g]
+        r = rng.uniform(0.6, 1.2)
+        c = np.array([gx + rng.uniform(-0.6, 0.6), r * 1.1, gz + rng.uniform(-0.6, 0.6)])
+        d = 1.0 + 0.1 * fbm(uv * 1.5, seed=seed * 1000 + i)
+        v = c + (uv * (r * d)[:, None])
+        tris.append(v[uf].reshape(-1, 9))
+        mats.append(random_material())
+        tmat.append(np.full(len(uf), len(mats) - 1, np.uint32))
+    ground = _quad((-12, 0, -12), (12, 0, -12), (12, 0, 12), (-12, 0, 12), (0, 1, 0))
+    tris.append(ground)
+    tmat.append(np.zeros(2, np.uint32))
+    nonlight = sum(len(t) for t in tris)
+    for lx in (-4.0, 4.0):
+        for lz in (-4.0, 4.0):
+            tris.append(_quad((lx - 1, 6, lz - 1), (lx + 1, 6, lz - 1), (lx + 1, 6, lz + 1),
+                              (lx - 1, 6, lz + 1), (0, -1, 0)))
+            tmat.append(np.ones(2, np.uint32))
+    tri = np.concatenate(tris).astype(np.float32)
+    tri_mat = np.concatenate(tmat).astype(np.uint32)
+    tri_light = np.full(len(tri), -1, np.int32)
+    tri_light[nonlight:] = 0
+    radii = np.exp(rng.normal(-3.0, 0.5, n_spheres))
+    sph = np.zeros(n_spheres, SPHERE_DT)
+    sph["center"][:, 0] = rng.uniform(-10, 10, n_spheres)
+    sph["center"][:, 2] = rng.uniform(-10, 10, n_spheres)
+    sph["center"][:, 1] = radii + rng.uniform(0, 2.5, n_spheres)
+    sph["radius"] = radii
+    for i in range(n_spheres):
+        mats.append(random_material())
+        sph["material_id"][i] = len(mats) - 1
+    sph["light_id"] = -1
+    lights = np.zeros(1, LIGHT_DT)
+    lights[0] = ((12.0, 12.0, 12.0), 0)
+    cam = Camera((0.0, 8.0, 14.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
+    return SceneData(tri, tri_mat, tri_light, sph, np.stack(mats), lights, cam, spp=spp,
+                     max_depth=max_depth, rr_threshold=1.0, name="production",
+                     meta={"n_ico": n_ico, "ico_level": ico_level, "n_spheres": n_spheres})

@@ -1,0 +1,227 @@
+/*
+ * bonsai_gpu.h - C ABI of the GB300 path-tracing library (libbonsai_gpu.so).
+ *
+ * The library replaces the CPU render loop of the Bonsai renderer
+ * (kazijawad/bonsai).  It sits exactly where the reference's
+ *   trait Integrator { fn render(&self, scene: &Scene); }       src/base/integrator.rs:26-28
+ *   trait SamplerIntegrator { camera(), sampler(), render(), radiance() }
+ *                                                              src/base/integrator.rs:30-141
+ *   PathIntegrator::new(camera, sampler, max_depth, rr_threshold)  src/integrators/path.rs:27-39
+ * sit: a host integrator flattens its Scene (shapes, materials, area lights) through the
+ * bg_scene_* calls once, then every bg_render call renders one film.
+ *
+ * Conventions (mirroring the reference's): the caller owns every host buffer; the library owns
+ * all device memory; every call returns a bg_status and never aborts or throws across the ABI
+ * (the reference panics instead, e.g. src/base/bsdf.rs:162).  A bg_ctx is used by one host
+ * thread at a time; all work is ordered on the context's own CUDA stream.
+ * Plain C types only: float xyz triplets, 32-bit ids, sizes.
+ */
+#ifndef BONSAI_GPU_H
+#define BONSAI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bg_status {
+    BG_OK = 0,
+    BG_ERR_INVALID = 1,     /* bad argument, size or scene record                     */
+    BG_ERR_CUDA = 2,        /* a CUDA runtime call failed (text in bg_last_error)      */
+    BG_ERR_OOM = 3,         /* device allocation failed or exceeded the memory cap     */
+    BG_ERR_TIMEOUT = 4,     /* a bounded device wait ran out                           */
+    BG_ERR_DEVICE = 5,      /* a device-side check raised the error word               */
+    BG_ERR_UNSUPPORTED = 6, /* feature the reference has but this library does not     */
+    BG_ERR_NO_DEVICE = 7    /* no CUDA device / extension built for another arch       */
+} bg_status;
+
+/* Estimator semantics.  BG_MODE_REF_COMPAT reproduces the reference PathIntegrator exactly
+ * (including its defects: the path never re-spawns, src/integrators/path.rs:70-143; the MIS
+ * BSDF branch follows the light direction, src/base/integrator.rs:400-431; spawn_ray caps
+ * t_max at 0.9999, src/base/interaction.rs:115-121; ...).  BG_MODE_PBRT is the unbiased
+ * PBRT-v3 path tracer the reference intends. */
+typedef enum bg_mode { BG_MODE_REF_COMPAT = 0, BG_MODE_PBRT = 1 } bg_mode;
+
+/* Material kinds.  MATTE = MatteMaterial with sigma 0 (src/materials/matte.rs:19-41),
+ * PLASTIC = PlasticMaterial (src/materials/plastic.rs:23-53), CONDUCTOR = BSDF{
+ * MicrofacetReflection(R=1, TrowbridgeReitz(a,a), FresnelConductor(1, eta, k))},
+ * DIELECTRIC = BSDF{FresnelSpecular(R=1, T=1, 1.0, ior, Radiance)} with BSDF eta = ior. */
+typedef enum bg_material_type {
+    BG_MAT_MATTE = 0,
+    BG_MAT_PLASTIC = 1,
+    BG_MAT_CONDUCTOR = 2,
+    BG_MAT_DIELECTRIC = 3
+} bg_material_type;
+
+typedef struct bg_material {
+    uint32_t type;            /* bg_material_type                                          */
+    float kd[3];              /* diffuse reflectance (matte, plastic)                      */
+    float ks[3];              /* specular reflectance (plastic)                            */
+    float roughness;          /* TR alpha (conductor), roughness (plastic)                 */
+    uint32_t remap_roughness; /* plastic: apply TrowbridgeReitz::roughness_to_alpha        */
+    float eta[3];             /* conductor eta                                             */
+    float k[3];               /* conductor absorption k                                    */
+    float ior;                /* dielectric index of refraction (outside medium is 1.0)    */
+} bg_material;
+
+/* DiffuseAreaLight options (src/lights/diffuse.rs:26-30). */
+typedef struct bg_area_light {
+    float intensity[3];
+    uint32_t two_sided;
+} bg_area_light;
+
+/* Sphere shape (src/shapes/sphere.rs:28-35) with a translation-only object_to_world and a full
+ * z range and phi_max of 360 degrees. */
+typedef struct bg_sphere {
+    float center[3];
+    float radius;
+    uint32_t material_id;
+    int32_t light_id; /* must be -1: spherical emitters are not supported */
+} bg_sphere;
+
+/* PerspectiveCamera options (src/cameras/perspective.rs:36-46) with the camera_to_world
+ * transform given as Transform::look_at(position, look_at, up) (src/base/transform.rs:152-189),
+ * shutter [0,1], and film Film{full_resolution=(width,height), crop [0,1]^2, BoxFilter r=0.5,
+ * scale 1, max_sample_luminance = +inf}. */
+typedef struct bg_camera {
+    float position[3];
+    float look_at[3];
+    float up[3];
+    float fov_deg;
+    float near_plane;
+    float far_plane;
+    float lens_radius;    /* must be 0: thin-lens depth of field is not supported */
+    float focal_distance;
+    uint32_t width;
+    uint32_t height;
+} bg_camera;
+
+typedef struct bg_render_opts {
+    uint32_t spp;          /* samples per pixel                                           */
+    uint32_t max_depth;    /* PathIntegrator max_depth                                    */
+    float rr_threshold;    /* PathIntegrator rr_threshold (roulette only after 3 bounces) */
+    uint32_t mode;         /* bg_mode                                                     */
+    uint64_t seed;         /* counter-RNG key                                             */
+    uint32_t first_sample; /* index of the first sample (progressive rendering)           */
+    uint32_t flags;        /* BG_RENDER_* bits                                            */
+} bg_render_opts;
+
+#define BG_RENDER_ACCUMULATE 1u  /* add to the film accumulated by earlier calls          */
+#define BG_RENDER_NO_READBACK 2u /* leave the film on the device (rgb_out may be NULL)    */
+#define BG_RENDER_GRAPH 4u       /* replay each sample pass from a captured CUDA graph     */
+#define BG_RENDER_STAGE_TIMING 8u /* time every wavefront stage with CUDA events (stats)   */
+
+typedef struct bg_render_stats {
+    double device_ms;        /* CUDA-event time of the render on the context's stream      */
+    double trace_ms;         /* time inside the closest-hit (extend) launches               */
+    double shadow_ms;        /* time inside the any-hit (shadow) launches                   */
+    double shade_ms;         /* time inside generate/shade/accumulate launches              */
+    uint64_t samples;        /* width * height * spp                                         */
+    uint64_t extension_rays; /* closest-hit queries traced                                  */
+    uint64_t shadow_rays;    /* any-hit queries traced                                      */
+    uint64_t launches;       /* kernels launched by this call                                */
+    uint64_t nan_samples;    /* samples zeroed by the NaN / negative / inf checks            */
+    uint32_t error_word;     /* device error bits (0 = none)                                 */
+    uint32_t reserved;
+} bg_render_stats;
+
+/* Ray and hit records of the trace entry points (oracle a: closest-hit / any-hit parity). */
+typedef struct bg_ray {
+    float org[3];
+    float tmax;
+    float dir[3];
+    float pad;
+} bg_ray;
+
+typedef struct bg_hit {
+    int32_t prim; /* triangles 0..ntri-1 in insertion order, then spheres; -1 = miss */
+    float t;
+} bg_hit;
+
+typedef struct bg_device_opts {
+    int32_t device;            /* CUDA ordinal                                        */
+    uint32_t max_queue_paths;  /* wavefront capacity (0 = library default)            */
+    uint64_t memory_cap_bytes; /* refuse allocations beyond this total (0 = no cap)   */
+    uint32_t block_size;       /* launch width for the wavefront stages (0 = default) */
+    uint32_t reserved;
+} bg_device_opts;
+
+/* BVH layouts the scene builder can produce. */
+typedef enum bg_bvh_kind {
+    BG_BVH_WIDE = 0,          /* 8-wide compressed BVH for the PBRT wavefront path          */
+    BG_BVH_REFERENCE = 1,     /* binary BVH laid out and ordered as the reference's         */
+    BG_BVH_REFERENCE_FIXED = 2 /* same, with the SAH bucket-index precedence bug fixed      */
+} bg_bvh_kind;
+
+typedef struct bg_build_stats {
+    double build_ms;     /* host BVH build + device upload                             */
+    uint64_t nodes;      /* nodes in the layout                                        */
+    uint64_t prims;      /* primitives                                                 */
+    uint64_t device_bytes;
+} bg_build_stats;
+
+typedef struct bg_ctx bg_ctx;
+typedef struct bg_scene bg_scene;
+
+/* ---- context ---------------------------------------------------------------------------- */
+bg_status bg_create(const bg_device_opts* opts, bg_ctx** out);
+void bg_destroy(bg_ctx* ctx);
+const char* bg_last_error(const bg_ctx* ctx);
+const char* bg_status_string(bg_status s);
+/* Overwrite a device buffer larger than L2 (used between timed passes). */
+bg_status bg_flush_l2(bg_ctx* ctx);
+bg_status bg_synchronize(bg_ctx* ctx);
+
+/* ---- scene builder (replaces building BVH::new(Vec<Arc<dyn Primitive>>),
+ *      src/accelerators/bvh.rs:53-89, and Scene::new, src/base/scene.rs:16-33) ------------- */
+bg_status bg_scene_create(bg_ctx* ctx, bg_scene** out);
+void bg_scene_destroy(bg_scene* scene);
+/* Appends a material; its id is returned in *id. */
+bg_status bg_scene_add_material(bg_scene* scene, const bg_material* m, uint32_t* id);
+/* Appends an emission record (DiffuseAreaLight options); its id is returned in *id. */
+bg_status bg_scene_add_area_light(bg_scene* scene, const bg_area_light* l, uint32_t* id);
+/* Appends ntri world-space triangles (9 floats each: p0 p1 p2), one Triangle shape per entry
+ * (src/shapes/triangle.rs:93-105).  light_ids may be NULL; otherwise light_ids[i] >= 0 makes
+ * triangle i an emitter: one DiffuseAreaLight per triangle, as GeometricPrimitive{shape,
+ * material, area_light} (src/primitives/geometric.rs:15-20). */
+bg_status bg_scene_add_triangles(bg_scene* scene, const float* xyz, size_t ntri,
+                                 const uint32_t* material_ids, const int32_t* light_ids);
+bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t n);
+/* Builds the BVH on the host, uploads scene and BVH to the device. */
+bg_status bg_scene_commit(bg_scene* scene, uint32_t bvh_kind, bg_build_stats* stats);
+
+/* ---- render: replaces SamplerIntegrator::render (src/base/integrator.rs:35-133) with
+ *      PathIntegrator::radiance (src/integrators/path.rs:51-146).  rgb_out is a host buffer of
+ *      width*height*3 floats (row-major, y down) holding Film::write_image's pixel values
+ *      (src/base/film.rs:156-202).  In REF_COMPAT mode the scene must be committed with a
+ *      BG_BVH_REFERENCE* layout; PBRT mode accepts any layout. ------------------------------- */
+bg_status bg_render(bg_ctx* ctx, const bg_scene* scene, const bg_camera* camera,
+                    const bg_render_opts* opts, float* rgb_out, bg_render_stats* stats);
+/* Per-pixel sample statistics of the film accumulated so far: sum and sum of squares of the
+ * sanitized sample radiance (double, 3 per pixel each) and the sample count (u32 per pixel).
+ * Any pointer may be NULL. */
+bg_status bg_film_moments(bg_ctx* ctx, double* sum_rgb, double* sumsq_rgb, uint32_t* count);
+
+/* ---- ray queries: BVH::intersect / intersect_test (src/accelerators/bvh.rs:281-423) over
+ *      host arrays (copies inside the call) or device arrays (no copies). ------------------- */
+bg_status bg_trace_closest(bg_ctx* ctx, const bg_scene* scene, const bg_ray* rays, size_t n,
+                           bg_hit* hits);
+bg_status bg_trace_any(bg_ctx* ctx, const bg_scene* scene, const bg_ray* rays, size_t n,
+                       uint8_t* occluded);
+bg_status bg_trace_closest_device(bg_ctx* ctx, const bg_scene* scene, const bg_ray* d_rays,
+                                  size_t n, bg_hit* d_hits, float* kernel_ms);
+bg_status bg_trace_any_device(bg_ctx* ctx, const bg_scene* scene, const bg_ray* d_rays,
+                              size_t n, uint8_t* d_occluded, float* kernel_ms);
+/* Device scratch owned by the context for the *_device calls (valid until bg_destroy). */
+bg_status bg_device_alloc(bg_ctx* ctx, size_t bytes, void** d_ptr);
+bg_status bg_device_free(bg_ctx* ctx, void* d_ptr);
+bg_status bg_memcpy_h2d(bg_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
+bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BONSAI_GPU_H */

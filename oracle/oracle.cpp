@@ -1,0 +1,1556 @@
+// CPU ORACLE - TEST INFRASTRUCTURE ONLY (the checker, never the product path).
+//
+// C++17 restatement of the path-tracing hot path of kazijawad/bonsai (Rust, f32 build).
+// Parity unpinned: the reference has no tests, golden vectors or fixtures for this path and its
+// Rust toolchain is absent here, so this restatement could not be run against reference output.
+// Every function names the reference file:line it follows.  Two estimator modes:
+//   REF_COMPAT - the reference as written, defects included (F1..F14 in the design notes);
+//   PBRT       - the same code with those defects fixed (PBRT-v3 PathIntegrator semantics).
+// Random numbers come from the counter RNG in orc_core.hpp (the reference draws from ChaCha12
+// seeded per 16x16 tile, src/base/integrator.rs:52-53; parity with it is statistical).
+#include <algorithm>
+#include <functional>
+#include <atomic>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../include/bonsai_gpu.h"
+#include "orc_core.hpp"
+
+namespace orc {
+
+enum Mode { REF = 0, PBRT = 1 };
+
+struct Ray {
+    V3 o, d;
+    float t_max = INFINITY;
+    float time = 0.0f;
+};
+
+// ---------------------------------------------------------------- Mat4 / Transform
+struct Mat4 {  // src/geometries/mat4.rs
+    float m[4][4];
+    static Mat4 identity() {
+        Mat4 r;
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) r.m[i][j] = (i == j) ? 1.0f : 0.0f;
+        return r;
+    }
+};
+static Mat4 mat_mul(const Mat4& a, const Mat4& b) {  // mat4.rs:36-48
+    Mat4 r;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j] +
+                        a.m[i][3] * b.m[3][j];
+    return r;
+}
+static Mat4 mat_inverse(const Mat4& in) {  // mat4.rs:72-140 (Gauss-Jordan, full pivoting)
+    float minv[4][4];
+    std::memcpy(minv, in.m, sizeof(minv));
+    int ic[4] = {0}, ir[4] = {0}, piv[4] = {0};
+    for (int i = 0; i < 4; ++i) {
+        int row = 0, col = 0;
+        float big = 0.0f;
+        for (int j = 0; j < 4; ++j) {
+            if (piv[j] != 1) {
+                for (int k = 0; k < 4; ++k) {
+                    if (piv[k] == 0) {
+                        if (std::fabs(minv[j][k]) >= big) {
+                            big = std::fabs(minv[j][k]);
+                            row = j;
+                            col = k;
+                        }
+                    }
+                }
+            }
+        }
+        piv[col] += 1;
+        if (row != col)
+            for (int k = 0; k < 4; ++k) std::swap(minv[row][k], minv[col][k]);
+        ir[i] = row;
+        ic[i] = col;
+        float pinv = 1.0f / minv[col][col];
+        minv[col][col] = 1.0f;
+        for (int j = 0; j < 4; ++j) minv[col][j] *= pinv;
+        for (int j = 0; j < 4; ++j) {
+            if (j != col) {
+                float save = minv[j][col];
+                minv[j][col] = 0.0f;
+                for (int k = 0; k < 4; ++k) minv[j][k] -= minv[col][k] * save;
+            }
+        }
+    }
+    for (int j = 3; j >= 0; --j)
+        if (ir[j] != ic[j])
+            for (int k = 0; k < 4; ++k) std::swap(minv[k][ir[j]], minv[k][ic[j]]);
+    Mat4 r;
+    std::memcpy(r.m, minv, sizeof(minv));
+    return r;
+}
+struct Transform {
+    Mat4 m, mi;
+};
+static Transform t_mul(const Transform& a, const Transform& b) {  // transform.rs:1629-1649
+    return {mat_mul(a.m, b.m), mat_mul(b.mi, a.mi)};
+}
+static Transform t_inverse(const Transform& t) { return {t.mi, t.m}; }
+static Transform t_scale(float x, float y, float z) {  // transform.rs:118-150
+    Transform t{Mat4::identity(), Mat4::identity()};
+    t.m.m[0][0] = x; t.m.m[1][1] = y; t.m.m[2][2] = z;
+    t.mi.m[0][0] = 1.0f / x; t.mi.m[1][1] = 1.0f / y; t.mi.m[2][2] = 1.0f / z;
+    return t;
+}
+static Transform t_translate(V3 d) {  // transform.rs:88-98
+    Transform t{Mat4::identity(), Mat4::identity()};
+    t.m.m[0][3] = d.x; t.m.m[1][3] = d.y; t.m.m[2][3] = d.z;
+    t.mi.m[0][3] = -d.x; t.mi.m[1][3] = -d.y; t.mi.m[2][3] = -d.z;
+    return t;
+}
+static bool is_identity(const Transform& t) {
+    Mat4 id = Mat4::identity();
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            if (t.m.m[i][j] != id.m[i][j]) return false;
+    return true;
+}
+static Transform t_perspective(float fov, float n, float f) {  // transform.rs:48-73
+    Mat4 mat = Mat4::identity();
+    mat.m[2][2] = f / (f - n);
+    mat.m[2][3] = -f * n / (f - n);
+    mat.m[3][2] = 1.0f;
+    mat.m[3][3] = 0.0f;
+    Mat4 inv = mat_inverse(mat);
+    float rad = fov * (PI / 180.0f);
+    float inv_tan = 1.0f / std::tan(rad / 2.0f);
+    return t_mul(t_scale(inv_tan, inv_tan, 1.0f), Transform{mat, inv});
+}
+static Transform t_look_at(V3 pos, V3 look, V3 up) {  // transform.rs:152-189 (camera_to_world)
+    Mat4 c2w = Mat4::identity();
+    c2w.m[0][3] = pos.x; c2w.m[1][3] = pos.y; c2w.m[2][3] = pos.z; c2w.m[3][3] = 1.0f;
+    V3 dir = normalize(look - pos);
+    if (length(cross(normalize(up), dir)) == 0.0f) return {Mat4::identity(), Mat4::identity()};
+    V3 right = normalize(cross(normalize(up), dir));
+    V3 new_up = cross(dir, right);
+    c2w.m[0][0] = right.x; c2w.m[1][0] = right.y; c2w.m[2][0] = right.z; c2w.m[3][0] = 0.0f;
+    c2w.m[0][1] = new_up.x; c2w.m[1][1] = new_up.y; c2w.m[2][1] = new_up.z; c2w.m[3][1] = 0.0f;
+    c2w.m[0][2] = dir.x; c2w.m[1][2] = dir.y; c2w.m[2][2] = dir.z; c2w.m[3][2] = 0.0f;
+    return {c2w, mat_inverse(c2w)};
+}
+static V3 xf_point(const Transform& t, V3 p) {  // point3.rs:51-69
+    const auto& m = t.m.m;
+    float xp = m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3];
+    float yp = m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3];
+    float zp = m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3];
+    float wp = m[3][0] * p.x + m[3][1] * p.y + m[3][2] * p.z + m[3][3];
+    if (wp == 1.0f) return {xp, yp, zp};
+    return V3(xp, yp, zp) / wp;
+}
+static V3 xf_point_err(const Transform& t, V3 p, V3* err) {  // point3.rs:71-100
+    const auto& m = t.m.m;
+    float x = p.x, y = p.y, z = p.z;
+    float xp = (m[0][0] * x + m[0][1] * y) + (m[0][2] * z + m[0][3]);
+    float yp = (m[1][0] * x + m[1][1] * y) + (m[1][2] * z + m[1][3]);
+    float zp = (m[2][0] * x + m[2][1] * y) + (m[2][2] * z + m[2][3]);
+    float wp = (m[3][0] * x + m[3][1] * y) + (m[3][2] * z + m[3][3]);
+    float xa = std::fabs(m[0][0] * x) + std::fabs(m[0][1] * y) + std::fabs(m[0][2] * z) + std::fabs(m[0][3]);
+    float ya = std::fabs(m[1][0] * x) + std::fabs(m[1][1] * y) + std::fabs(m[1][2] * z) + std::fabs(m[1][3]);
+    float za = std::fabs(m[2][0] * x) + std::fabs(m[2][1] * y) + std::fabs(m[2][2] * z) + std::fabs(m[2][3]);
+    *err = gamma(3.0f) * V3(xa, ya, za);
+    if (wp == 1.0f) return {xp, yp, zp};
+    return V3(xp, yp, zp) / wp;
+}
+static V3 xf_point_perr(const Transform& t, V3 p, V3 pe, V3* abs_err) {  // point3.rs:102-140
+    const auto& m = t.m.m;
+    float x = p.x, y = p.y, z = p.z;
+    float xp = (m[0][0] * x + m[0][1] * y) + (m[0][2] * z + m[0][3]);
+    float yp = (m[1][0] * x + m[1][1] * y) + (m[1][2] * z + m[1][3]);
+    float zp = (m[2][0] * x + m[2][1] * y) + (m[2][2] * z + m[2][3]);
+    float wp = (m[3][0] * x + m[3][1] * y) + (m[3][2] * z + m[3][3]);
+    float g3 = gamma(3.0f);
+    for (int i = 0; i < 3; ++i) {
+        (*abs_err)[i] = (g3 + 1.0f) * (std::fabs(m[i][0]) * pe.x + std::fabs(m[i][1]) * pe.y +
+                                       std::fabs(m[i][2]) * pe.z) +
+                        g3 * (std::fabs(m[i][0] * x) + std::fabs(m[i][1] * y) +
+                              std::fabs(m[i][2] * z) + std::fabs(m[i][3]));
+    }
+    if (wp == 1.0f) return {xp, yp, zp};
+    return V3(xp, yp, zp) / wp;
+}
+static V3 xf_vec(const Transform& t, V3 v) {  // vec3.rs:35-44
+    const auto& m = t.m.m;
+    return {m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+            m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z};
+}
+static V3 xf_vec_err(const Transform& t, V3 v, V3* e) {  // vec3.rs:46-64
+    const auto& m = t.m.m;
+    float g3 = gamma(3.0f);
+    e->x = g3 * (std::fabs(m[0][0] * v.x) + std::fabs(m[0][1] * v.y) + std::fabs(m[0][2] * v.z));
+    e->y = g3 * (std::fabs(m[1][0] * v.x) + std::fabs(m[1][1] * v.y) + std::fabs(m[1][2] * v.z));
+    e->z = g3 * (std::fabs(m[2][0] * v.x) + std::fabs(m[2][1] * v.y) + std::fabs(m[2][2] * v.z));
+    return xf_vec(t, v);
+}
+static V3 xf_normal(const Transform& t, V3 n) {  // normal.rs:21-30
+    const auto& mi = t.mi.m;
+    return {mi[0][0] * n.x + mi[1][0] * n.y + mi[2][0] * n.z, mi[0][1] * n.x + mi[1][1] * n.y + mi[2][1] * n.z,
+            mi[0][2] * n.x + mi[1][2] * n.y + mi[2][2] * n.z};
+}
+static Ray xf_ray(const Transform& t, const Ray& r) {  // ray.rs:50-76
+    V3 oerr;
+    V3 o = xf_point_err(t, r.o, &oerr);
+    V3 d = xf_vec(t, r.d);
+    float ls = length_squared(d);
+    float t_max = r.t_max;
+    if (ls > 0.0f) {
+        float dt = dot(vabs(d), oerr) / ls;
+        o = o + d * dt;
+        t_max -= dt;
+    }
+    return {o, d, t_max, r.time};
+}
+static Ray xf_ray_err(const Transform& t, const Ray& r, V3* oe, V3* de) {  // ray.rs:78-106
+    V3 o = xf_point_err(t, r.o, oe);
+    V3 d = xf_vec_err(t, r.d, de);
+    float ls = length_squared(d);
+    if (ls > 0.0f) {
+        float dt = dot(vabs(d), *oe) / ls;
+        o = o + d * dt;
+    }
+    return {o, d, r.t_max, r.time};
+}
+
+// ---------------------------------------------------------------- Bounds3
+struct Bounds3 {  // src/geometries/bounds3.rs; Default = (MAX, MIN) (bounds3.rs:291-298)
+    V3 mn{FLT_MAX, FLT_MAX, FLT_MAX};
+    V3 mx{-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    const V3& operator[](int i) const { return i == 0 ? mn : mx; }
+    void unite(const Bounds3& b) {
+        mn = {rmin(mn.x, b.mn.x), rmin(mn.y, b.mn.y), rmin(mn.z, b.mn.z)};
+        mx = {rmax(mx.x, b.mx.x), rmax(mx.y, b.mx.y), rmax(mx.z, b.mx.z)};
+    }
+    void unite(V3 p) {
+        mn = {rmin(mn.x, p.x), rmin(mn.y, p.y), rmin(mn.z, p.z)};
+        mx = {rmax(mx.x, p.x), rmax(mx.y, p.y), rmax(mx.z, p.z)};
+    }
+    float surface_area() const {  // bounds3.rs:160-163
+        V3 d = mx - mn;
+        return 2.0f * (d.x * d.y + d.x * d.z + d.y * d.z);
+    }
+    int maximum_extent() const {  // bounds3.rs:175-184
+        V3 d = mx - mn;
+        if (d.x > d.y && d.x > d.z) return 0;
+        if (d.y > d.z) return 1;
+        return 2;
+    }
+    V3 offset(V3 p) const {  // bounds3.rs:194-206
+        V3 o = p - mn;
+        if (mx.x > mn.x) o.x /= mx.x - mn.x;
+        if (mx.y > mn.y) o.y /= mx.y - mn.y;
+        if (mx.z > mn.z) o.z /= mx.z - mn.z;
+        return o;
+    }
+    // bounds3.rs:246-288
+    bool intersect_p(const Ray& ray, V3 inv, const int neg[3]) const {
+        float k = 1.0f + 2.0f * gamma(3.0f);
+        float t_min = ((*this)[neg[0]].x - ray.o.x) * inv.x;
+        float t_max = ((*this)[1 - neg[0]].x - ray.o.x) * inv.x;
+        float ty_min = ((*this)[neg[1]].y - ray.o.y) * inv.y;
+        float ty_max = ((*this)[1 - neg[1]].y - ray.o.y) * inv.y;
+        t_max *= k;
+        ty_max *= k;
+        if (t_min > ty_max || ty_min > t_max) return false;
+        if (ty_min > t_min) t_min = ty_min;
+        if (ty_max < t_max) t_max = ty_max;
+        float tz_min = ((*this)[neg[2]].z - ray.o.z) * inv.z;
+        float tz_max = ((*this)[1 - neg[2]].z - ray.o.z) * inv.z;
+        tz_max *= k;
+        if (t_min > tz_max || tz_min > t_max) return false;
+        if (tz_min > t_min) t_min = tz_min;
+        if (tz_max < t_max) t_max = tz_max;
+        return (t_min < ray.t_max) && (t_max > 0.0f);
+    }
+};
+
+// ---------------------------------------------------------------- Interaction
+struct Interaction {  // src/base/interaction.rs:47-54 (+ the SurfaceInteraction fields used)
+    V3 p, p_err, wo, n;
+    float time = 0.0f;
+    bool surface = false;
+    V3 dpdu, shading_n, shading_dpdu;
+    int prim = -1;
+};
+// src/geometries/point3.rs:31-49
+static V3 offset_ray_origin(V3 p, V3 perr, V3 n, V3 w) {
+    V3 offset = dot(vabs(n), perr) * n;
+    if (dot(w, n) < 0.0f) offset = -offset;
+    V3 po = p + offset;
+    for (int i = 0; i < 3; ++i) {
+        if (offset[i] > 0.0f) po[i] = next_float_up(po[i]);
+        else if (offset[i] < 0.0f) po[i] = next_float_down(po[i]);
+    }
+    return po;
+}
+// interaction.rs:115-121; F3: t_max = 1 - 0.0001 for a normalized direction (PBRT: infinity)
+static Ray spawn_ray(const Interaction& it, V3 d, Mode mode) {
+    V3 o = offset_ray_origin(it.p, it.p_err, it.n, d);
+    return {o, d, mode == REF ? (1.0f - 0.0001f) : INFINITY, it.time};
+}
+// interaction.rs:132-143
+static Ray spawn_ray_to_it(const Interaction& a, const Interaction& b) {
+    V3 o = offset_ray_origin(a.p, a.p_err, a.n, b.p - a.p);
+    V3 target = offset_ray_origin(b.p, b.p_err, b.n, o - b.p);
+    return {o, target - o, 1.0f - 0.0001f, a.time};
+}
+
+// ---------------------------------------------------------------- Scene data
+struct Sphere {  // src/shapes/sphere.rs:38-64 (translation-only object_to_world)
+    Transform o2w, w2o;
+    float radius, z_min, z_max, theta_min, theta_max, phi_max;
+    uint32_t mat;
+};
+struct Scene {
+    std::vector<V3> pos;  // 3 per triangle (TriangleMesh::position, triangle.rs:17-22)
+    int64_t ntri = 0, nsph = 0;
+    std::vector<uint32_t> tri_mat;
+    std::vector<int32_t> prim_emission;  // emission record per primitive or -1
+    std::vector<int32_t> prim_light;     // light-list index per primitive or -1
+    std::vector<Sphere> sph;
+    std::vector<bg_material> mats;
+    std::vector<bg_area_light> emis;
+    std::vector<int64_t> light_prims;  // Scene::lights (one DiffuseAreaLight per emitting shape)
+    // BVH (src/accelerators/bvh.rs:20-31)
+    struct Node {
+        Bounds3 b;
+        uint32_t offset = 0;  // primitive_offset (leaf) or second_child_offset (interior)
+        uint32_t count = 0;
+        uint32_t axis = 0;
+    };
+    std::vector<Node> nodes;
+    std::vector<uint32_t> order;  // ordered_primitives
+    int64_t nprims() const { return ntri + nsph; }
+};
+
+struct Counters {
+    int64_t ext_rays = 0, shadow_rays = 0, ext_visits = 0, ext_tests = 0, sh_visits = 0, sh_tests = 0;
+    int64_t nan_samples = 0;
+    void add(const Counters& o) {
+        ext_rays += o.ext_rays; shadow_rays += o.shadow_rays; ext_visits += o.ext_visits;
+        ext_tests += o.ext_tests; sh_visits += o.sh_visits; sh_tests += o.sh_tests;
+        nan_samples += o.nan_samples;
+    }
+};
+
+// ---------------------------------------------------------------- Triangle (triangle.rs)
+static bool tri_intersect(const Scene& s, int64_t i, const Ray& ray, float* t_hit, Interaction* it,
+                          bool test_only) {
+    const V3& p0 = s.pos[3 * i];
+    const V3& p1 = s.pos[3 * i + 1];
+    const V3& p2 = s.pos[3 * i + 2];
+    V3 p0t = p0 - ray.o, p1t = p1 - ray.o, p2t = p2 - ray.o;  // :141-145
+    int kz = max_dimension(vabs(ray.d));                      // :147-156
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    V3 d = permute(ray.d, kx, ky, kz);
+    p0t = permute(p0t, kx, ky, kz);
+    p1t = permute(p1t, kx, ky, kz);
+    p2t = permute(p2t, kx, ky, kz);
+    float sx = -d.x / d.z, sy = -d.y / d.z, sz = 1.0f / d.z;  // :162-171
+    p0t.x += sx * p0t.z; p0t.y += sy * p0t.z;
+    p1t.x += sx * p1t.z; p1t.y += sy * p1t.z;
+    p2t.x += sx * p2t.z; p2t.y += sy * p2t.z;
+    float e0 = p1t.x * p2t.y - p1t.y * p2t.x;  // :173-176
+    float e1 = p2t.x * p0t.y - p2t.y * p0t.x;
+    float e2 = p0t.x * p1t.y - p0t.y * p1t.x;
+    if (e0 == 0.0f || e1 == 0.0f || e2 == 0.0f) {  // :178-190 f64 fallback
+        double a = (double)p2t.x * (double)p1t.y, b = (double)p2t.y * (double)p1t.x;
+        e0 = (float)(b - a);
+        double c = (double)p0t.x * (double)p2t.y, dd = (double)p0t.y * (double)p2t.x;
+        e1 = (float)(dd - c);
+        double e = (double)p1t.x * (double)p0t.y, f = (double)p1t.y * (double)p0t.x;
+        e2 = (float)(f - e);
+    }
+    if ((e0 < 0.0f || e1 < 0.0f || e2 < 0.0f) && (e0 > 0.0f || e1 > 0.0f || e2 > 0.0f)) return false;
+    float det = e0 + e1 + e2;
+    if (det == 0.0f) return false;
+    p0t.z *= sz; p1t.z *= sz; p2t.z *= sz;  // :201-210
+    float t_scaled = e0 * p0t.z + e1 * p1t.z + e2 * p2t.z;
+    if (det < 0.0f && (t_scaled >= 0.0f || t_scaled < ray.t_max * det)) return false;
+    else if (det > 0.0f && (t_scaled <= 0.0f || t_scaled > ray.t_max * det)) return false;
+    float inv_det = 1.0f / det;  // :212-217
+    float b0 = e0 * inv_det, b1 = e1 * inv_det, b2 = e2 * inv_det;
+    float t = t_scaled * inv_det;
+    float max_zt = max_component(vabs(V3(p0t.z, p1t.z, p2t.z)));  // :219-239
+    float delta_z = gamma(3.0f) * max_zt;
+    float max_xt = max_component(vabs(V3(p0t.x, p1t.x, p2t.x)));
+    float max_yt = max_component(vabs(V3(p0t.y, p1t.y, p2t.y)));
+    float delta_x = gamma(5.0f) * (max_xt + max_zt);
+    float delta_y = gamma(5.0f) * (max_yt + max_zt);
+    float delta_e = 2.0f * (gamma(2.0f) * max_xt * max_yt + delta_y * max_xt + delta_x * max_yt);
+    float max_e = max_component(vabs(V3(e0, e1, e2)));
+    float delta_t = 3.0f * (gamma(3.0f) * max_e * max_zt + delta_e * max_zt + delta_z * max_e) *
+                    std::fabs(inv_det);
+    if (t <= delta_t) return false;
+    // partial derivatives with the default uvs (0,0),(1,0),(1,1) (:107-117, :241-268)
+    const float uv[3][2] = {{0.0f, 0.0f}, {1.0f, 0.0f}, {1.0f, 1.0f}};
+    float duv02[2] = {uv[0][0] - uv[2][0], uv[0][1] - uv[2][1]};
+    float duv12[2] = {uv[1][0] - uv[2][0], uv[1][1] - uv[2][1]};
+    V3 dp02 = p0 - p2, dp12 = p1 - p2;
+    float uvdet = duv02[0] * duv12[1] - duv02[1] * duv12[0];
+    bool degenerate_uv = std::fabs(uvdet) < 1e-8f;
+    V3 dpdu, dpdv;
+    if (!degenerate_uv) {
+        float invd = 1.0f / uvdet;
+        dpdu = (duv12[1] * dp02 - duv02[1] * dp12) * invd;
+        dpdv = (-duv12[0] * dp02 + duv02[0] * dp12) * invd;
+    }
+    if (degenerate_uv || length_squared(cross(dpdu, dpdv)) == 0.0f) {
+        V3 ng = cross(p2 - p0, p1 - p0);
+        if (length_squared(ng) == 0.0f) return false;
+        coordinate_system(normalize(ng), &dpdu, &dpdv);
+    }
+    if (test_only) return true;
+    // error bounds and hit point (:270-278)
+    float xs = std::fabs(b0 * p0.x) + std::fabs(b1 * p1.x) + std::fabs(b2 * p2.x);
+    float ys = std::fabs(b0 * p0.y) + std::fabs(b1 * p1.y) + std::fabs(b2 * p2.y);
+    float zs = std::fabs(b0 * p0.z) + std::fabs(b1 * p1.z) + std::fabs(b2 * p2.z);
+    V3 perr = gamma(7.0f) * V3(xs, ys, zs);
+    V3 phit = b0 * p0 + b1 * p1 + b2 * p2;
+    // Interaction::new (interaction.rs:57-100), normal overridden (:299-307)
+    it->p = phit;
+    it->p_err = perr;
+    it->time = ray.time;
+    it->wo = -ray.d;
+    it->surface = true;
+    it->dpdu = dpdu;
+    it->shading_dpdu = dpdu;
+    V3 nn = normalize(cross(dp02, dp12));
+    it->n = nn;
+    it->shading_n = nn;
+    *t_hit = t;
+    return true;
+}
+static float tri_area(const Scene& s, int64_t i) {  // triangle.rs:561-566
+    const V3& p0 = s.pos[3 * i];
+    return 0.5f * length(cross(s.pos[3 * i + 1] - p0, s.pos[3 * i + 2] - p0));
+}
+static Interaction tri_sample(const Scene& s, int64_t i, float u0, float u1, float* pdf) {  // :522-559
+    float sq = std::sqrt(u0);  // uniform_sample_triangle (sampling.rs:233-236)
+    float b0 = 1.0f - sq, b1 = u1 * sq;
+    const V3& p0 = s.pos[3 * i];
+    const V3& p1 = s.pos[3 * i + 1];
+    const V3& p2 = s.pos[3 * i + 2];
+    float b2 = 1.0f - b0 - b1;
+    Interaction r;
+    r.p = b0 * p0 + b1 * p1 + b2 * p2;
+    r.n = normalize(cross(p1 - p0, p2 - p0));
+    V3 pabs = vabs(b0 * p0) + vabs(b1 * p1) + vabs(b2 * p2);
+    r.p_err = gamma(6.0f) * pabs;
+    *pdf = 1.0f / tri_area(s, i);
+    return r;
+}
+
+// ---------------------------------------------------------------- Sphere (sphere.rs)
+static bool sphere_intersect(const Sphere& sp, const Ray& r_world, float* t_hit, Interaction* it,
+                             bool test_only) {
+    V3 oe, de;
+    Ray ray = xf_ray_err(sp.w2o, r_world, &oe, &de);  // :80-83
+    EFloat ox(ray.o.x, oe.x), oy(ray.o.y, oe.y), oz(ray.o.z, oe.z);
+    EFloat dx(ray.d.x, de.x), dy(ray.d.y, de.y), dz(ray.d.z, de.z);
+    EFloat a = dx * dx + dy * dy + dz * dz;
+    EFloat b = ef(2.0f) * (dx * ox + dy * oy + dz * oz);
+    EFloat c = ox * ox + oy * oy + oz * oz - ef(sp.radius) * ef(sp.radius);
+    EFloat t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0.high > ray.t_max || t1.low <= 0.0f) return false;  // :106-116
+    EFloat tsh = t0;
+    if (tsh.low <= 0.0f) {
+        tsh = t1;
+        if (tsh.high > ray.t_max) return false;
+    }
+    auto refine = [&](float t) {
+        V3 ph = ray.o + ray.d * t;
+        ph = ph * (sp.radius / distance(ph, V3(0, 0, 0)));
+        if (ph.x == 0.0f && ph.y == 0.0f) ph.x = 1e-5f * sp.radius;
+        return ph;
+    };
+    V3 ph = refine(tsh.v);
+    float phi = std::atan2(ph.y, ph.x);
+    if (phi < 0.0f) phi += 2.0f * PI;
+    auto clipped = [&](V3 p, float ph_) {
+        return (sp.z_min > -sp.radius && p.z < sp.z_min) || (sp.z_max < sp.radius && p.z > sp.z_max) ||
+               ph_ > sp.phi_max;
+    };
+    if (clipped(ph, phi)) {  // :127-161
+        if (tsh.v == t1.v && tsh.low == t1.low && tsh.high == t1.high) return false;
+        if (t1.high > ray.t_max) return false;
+        tsh = t1;
+        ph = refine(tsh.v);
+        phi = std::atan2(ph.y, ph.x);
+        if (phi < 0.0f) phi += 2.0f * PI;
+        if (clipped(ph, phi)) return false;
+    }
+    if (test_only) return true;
+    // parametric representation and partial derivatives (:163-176)
+    float theta = std::acos(rclamp(ph.z / sp.radius, -1.0f, 1.0f));
+    float z_radius = std::sqrt(ph.x * ph.x + ph.y * ph.y);
+    float inv_zr = 1.0f / z_radius;
+    float cos_phi = ph.x * inv_zr, sin_phi = ph.y * inv_zr;
+    V3 dpdu(-sp.phi_max * ph.y, sp.phi_max * ph.x, 0.0f);
+    V3 dpdv = (sp.theta_max - sp.theta_min) * V3(ph.z * cos_phi, ph.z * sin_phi, -sp.radius * std::sin(theta));
+    V3 perr = gamma(5.0f) * vabs(ph);  // :209
+    // Interaction::new then Interaction::transform(object_to_world) (interaction.rs:268-300)
+    V3 n = normalize(cross(dpdu, dpdv));
+    V3 abs_err;
+    it->p = xf_point_perr(sp.o2w, ph, perr, &abs_err);
+    it->p_err = abs_err;
+    it->time = ray.time;
+    it->wo = xf_vec(sp.o2w, -ray.d);
+    it->n = normalize(xf_normal(sp.o2w, n));
+    it->surface = true;
+    it->dpdu = xf_vec(sp.o2w, dpdu);
+    it->shading_n = face_forward(normalize(xf_normal(sp.o2w, n)), it->n);
+    it->shading_dpdu = xf_vec(sp.o2w, dpdu);
+    *t_hit = tsh.v;
+    return true;
+}
+
+// ---------------------------------------------------------------- primitives + BVH
+static bool prim_intersect(const Scene& s, int64_t prim, Ray& ray, Interaction* it) {
+    float t;  // GeometricPrimitive::intersect (geometric.rs:27-38)
+    bool ok = prim < s.ntri ? tri_intersect(s, prim, ray, &t, it, false)
+                            : sphere_intersect(s.sph[prim - s.ntri], ray, &t, it, false);
+    if (!ok) return false;
+    ray.t_max = t;
+    it->prim = (int)prim;
+    return true;
+}
+static bool prim_intersect_test(const Scene& s, int64_t prim, const Ray& ray) {
+    float t;
+    Interaction dummy;
+    return prim < s.ntri ? tri_intersect(s, prim, ray, &t, &dummy, true)
+                         : sphere_intersect(s.sph[prim - s.ntri], ray, &t, &dummy, true);
+}
+static Bounds3 prim_bounds(const Scene& s, int64_t prim) {
+    Bounds3 b;
+    if (prim < s.ntri) {  // triangle.rs:128-133
+        const V3& p0 = s.pos[3 * prim];
+        const V3& p1 = s.pos[3 * prim + 1];
+        const V3& p2 = s.pos[3 * prim + 2];
+        b.mn = {rmin(p0.x, p1.x), rmin(p0.y, p1.y), rmin(p0.z, p1.z)};
+        b.mx = {rmax(p0.x, p1.x), rmax(p0.y, p1.y), rmax(p0.z, p1.z)};
+        b.unite(p2);
+        return b;
+    }
+    const Sphere& sp = s.sph[prim - s.ntri];  // sphere.rs:68-78, transform.rs:75-86
+    V3 lo(-sp.radius, -sp.radius, sp.z_min), hi(sp.radius, sp.radius, sp.z_max);
+    V3 c0 = xf_point(sp.o2w, lo);
+    b.mn = c0; b.mx = c0;
+    const V3 corners[7] = {{hi.x, lo.y, lo.z}, {lo.x, hi.y, lo.z}, {lo.x, lo.y, hi.z}, {lo.x, hi.y, hi.z},
+                           {hi.x, hi.y, lo.z}, {hi.x, lo.y, hi.z}, {hi.x, hi.y, hi.z}};
+    for (const V3& c : corners) b.unite(xf_point(sp.o2w, c));
+    return b;
+}
+
+struct PrimInfo {
+    uint32_t index;
+    Bounds3 b;
+    V3 centroid;
+};
+// itertools 0.10 partition: two-pointer, elements mapping to true first.
+template <class F>
+static size_t partition_it(PrimInfo* v, size_t n, F pred) {
+    size_t front = 0, back = n, split = 0;
+    while (front < back) {
+        PrimInfo* f = &v[front++];
+        if (!pred(*f)) {
+            bool swapped = false;
+            while (front < back) {
+                PrimInfo* b = &v[--back];
+                if (pred(*b)) {
+                    std::swap(*f, *b);
+                    swapped = true;
+                    break;
+                }
+            }
+            if (!swapped) return split;
+        }
+        ++split;
+    }
+    return split;
+}
+// BVH::build (bvh.rs:91-247) as an explicit preorder work stack; `fixed` switches the bucket
+// index from `16 * (offset as usize)` (F7) to `(16.0 * offset) as usize`.  Buckets start from
+// BucketInfo::default() (the reference reads uninitialised memory there, bvh.rs:149-150).
+static void build_bvh(Scene& s, bool fixed) {
+    const int64_t n = s.nprims();
+    s.nodes.clear();
+    s.order.clear();
+    if (n == 0) return;
+    std::vector<PrimInfo> info(n);
+    for (int64_t i = 0; i < n; ++i) {
+        info[i].index = (uint32_t)i;
+        info[i].b = prim_bounds(s, i);
+        info[i].centroid = 0.5f * info[i].b.mn + 0.5f * info[i].b.mx;  // bvh.rs:443-450
+    }
+    struct Task { size_t begin, end; int64_t parent; };
+    std::vector<Task> stack;
+    stack.push_back({0, (size_t)n, -1});
+    const int NB = 16;
+    while (!stack.empty()) {
+        Task task = stack.back();
+        stack.pop_back();
+        uint32_t node_index = (uint32_t)s.nodes.size();
+        s.nodes.emplace_back();
+        if (task.parent >= 0) s.nodes[task.parent].offset = node_index;  // second_child_offset
+        PrimInfo* pi = info.data() + task.begin;
+        size_t size = task.end - task.begin;
+        Bounds3 bounds;
+        for (size_t i = 0; i < size; ++i) bounds.unite(pi[i].b);
+        auto make_leaf = [&]() {
+            Scene::Node& nd = s.nodes[node_index];
+            nd.b = bounds;
+            nd.offset = (uint32_t)s.order.size();
+            nd.count = (uint32_t)size;
+            for (size_t i = 0; i < size; ++i) s.order.push_back(pi[i].index);
+        };
+        if (size == 1) { make_leaf(); continue; }
+        Bounds3 cb;
+        for (size_t i = 0; i < size; ++i) cb.unite(pi[i].centroid);
+        int dim = cb.maximum_extent();
+        if (cb.mx[dim] == cb.mn[dim]) { make_leaf(); continue; }
+        size_t mid = size / 2;
+        if (size <= 2) {
+            // select_nth_unstable_by(mid, total_cmp) on two elements
+            if (pi[0].centroid[dim] > pi[1].centroid[dim]) std::swap(pi[0], pi[1]);
+        } else {
+            auto bucket_of = [&](const PrimInfo& p) {
+                float off = cb.offset(p.centroid)[dim];
+                size_t b;
+                if (fixed) {
+                    float f = (float)NB * off;
+                    b = f <= 0.0f ? 0 : (size_t)f;  // `as usize` saturates
+                } else {
+                    size_t o = off >= 1.0f ? 1 : 0;  // `offset as usize` is 0 or 1 on [0,1]
+                    b = (size_t)NB * o;
+                }
+                if (b >= (size_t)NB) b = NB - 1;
+                return b;
+            };
+            float count[NB] = {0};
+            Bounds3 bb[NB];
+            for (size_t i = 0; i < size; ++i) {
+                size_t b = bucket_of(pi[i]);
+                count[b] += 1.0f;
+                bb[b].unite(pi[i].b);
+            }
+            float cost[NB - 1];
+            float sa = bounds.surface_area();
+            for (int i = 0; i < NB - 1; ++i) {
+                Bounds3 b0, b1;
+                float c0 = 0.0f, c1 = 0.0f;
+                for (int j = 0; j <= i; ++j) { b0.unite(bb[j]); c0 += count[j]; }
+                for (int j = i + 1; j < NB; ++j) { b1.unite(bb[j]); c1 += count[j]; }
+                cost[i] = 1.0f + (c0 * b0.surface_area() + c1 * b1.surface_area()) / sa;
+            }
+            float min_cost = cost[0];
+            size_t min_b = 0;
+            for (int i = 1; i < NB - 1; ++i)
+                if (cost[i] < min_cost) { min_cost = cost[i]; min_b = i; }
+            float leaf_cost = (float)size;
+            if (size > 256 || min_cost < leaf_cost) {
+                mid = partition_it(pi, size, [&](const PrimInfo& p) { return bucket_of(p) <= min_b; });
+            } else {
+                make_leaf();
+                continue;
+            }
+        }
+        Scene::Node& nd = s.nodes[node_index];
+        nd.b = bounds;  // union of both children's bounds
+        nd.count = 0;
+        nd.axis = (uint32_t)dim;
+        stack.push_back({task.begin + mid, task.end, (int64_t)node_index});  // second child
+        stack.push_back({task.begin, task.begin + mid, -1});                // first child (next)
+    }
+}
+
+// BVH::intersect (bvh.rs:281-352)
+static bool scene_intersect(const Scene& s, Ray& ray, Interaction* it, Counters* cnt) {
+    if (s.nodes.empty()) return false;
+    bool hit = false;
+    V3 inv(1.0f / ray.d.x, 1.0f / ray.d.y, 1.0f / ray.d.z);
+    int neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+    std::vector<uint32_t> todo;
+    todo.reserve(64);
+    uint32_t cur = 0;
+    for (;;) {
+        const Scene::Node& nd = s.nodes[cur];
+        if (cnt) cnt->ext_visits++;
+        if (nd.b.intersect_p(ray, inv, neg)) {
+            if (nd.count > 0) {
+                for (uint32_t i = 0; i < nd.count; ++i) {
+                    if (cnt) cnt->ext_tests++;
+                    if (prim_intersect(s, s.order[nd.offset + i], ray, it)) hit = true;
+                }
+                if (todo.empty()) break;
+                cur = todo.back();
+                todo.pop_back();
+            } else {
+                if (neg[nd.axis]) { todo.push_back(cur + 1); cur = nd.offset; }
+                else { todo.push_back(nd.offset); cur = cur + 1; }
+            }
+        } else {
+            if (todo.empty()) break;
+            cur = todo.back();
+            todo.pop_back();
+        }
+    }
+    return hit;
+}
+// BVH::intersect_test (bvh.rs:354-423)
+static bool scene_intersect_test(const Scene& s, const Ray& ray, Counters* cnt) {
+    if (s.nodes.empty()) return false;
+    V3 inv(1.0f / ray.d.x, 1.0f / ray.d.y, 1.0f / ray.d.z);
+    int neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+    std::vector<uint32_t> todo;
+    todo.reserve(64);
+    uint32_t cur = 0;
+    for (;;) {
+        const Scene::Node& nd = s.nodes[cur];
+        if (cnt) cnt->sh_visits++;
+        if (nd.b.intersect_p(ray, inv, neg)) {
+            if (nd.count > 0) {
+                for (uint32_t i = 0; i < nd.count; ++i) {
+                    if (cnt) cnt->sh_tests++;
+                    if (prim_intersect_test(s, s.order[nd.offset + i], ray)) return true;
+                }
+                if (todo.empty()) break;
+                cur = todo.back();
+                todo.pop_back();
+            } else {
+                if (neg[nd.axis]) { todo.push_back(cur + 1); cur = nd.offset; }
+                else { todo.push_back(nd.offset); cur = cur + 1; }
+            }
+        } else {
+            if (todo.empty()) break;
+            cur = todo.back();
+            todo.pop_back();
+        }
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- BxDFs (src/base/bxdf.rs ...)
+enum : uint8_t { BSDF_REFLECTION = 1, BSDF_TRANSMISSION = 2, BSDF_DIFFUSE = 4, BSDF_GLOSSY = 8, BSDF_SPECULAR = 16,
+                 BSDF_ALL = 31 };
+inline float cos_theta(V3 w) { return w.z; }
+inline float cos2_theta(V3 w) { return w.z * w.z; }
+inline float abs_cos_theta(V3 w) { return std::fabs(w.z); }
+inline float sin2_theta(V3 w) { return rmax(0.0f, 1.0f - cos2_theta(w)); }
+inline float sin_theta(V3 w) { return std::sqrt(sin2_theta(w)); }
+inline float tan_theta(V3 w) { return sin_theta(w) / cos_theta(w); }
+inline float tan2_theta(V3 w) { return sin2_theta(w) / cos2_theta(w); }
+inline float cos_phi(V3 w) { float v = sin_theta(w); return v == 0.0f ? 1.0f : rclamp(w.x / v, -1.0f, 1.0f); }
+inline float sin_phi(V3 w) { float v = sin_theta(w); return v == 0.0f ? 0.0f : rclamp(w.y / v, -1.0f, 1.0f); }
+inline float cos2_phi(V3 w) { return cos_phi(w) * cos_phi(w); }
+inline float sin2_phi(V3 w) { return sin_phi(w) * sin_phi(w); }
+inline bool same_hemisphere(V3 a, V3 b) { return a.z * b.z > 0.0f; }
+inline V3 reflect(V3 wo, V3 n) { return -wo + 2.0f * dot(wo, n) * n; }  // bxdf.rs:142-144
+static bool refract(V3 wi, V3 n, float eta, V3* wt) {  // bxdf.rs:146-159
+    float cos_i = dot(n, wi);
+    float sin2_i = rmax(0.0f, 1.0f - cos_i * cos_i);
+    float sin2_t = eta * eta * sin2_i;
+    if (sin2_t >= 1.0f) return false;
+    float cos_t = std::sqrt(1.0f - sin2_t);
+    *wt = eta * -wi + (eta * cos_i - cos_t) * n;
+    return true;
+}
+// bxdf.rs:165-188 (F14: REF keeps a negative cos after swapping the indices; PBRT takes |cos|)
+static float fresnel_dielectric(float cos_i, float eta_i, float eta_t, Mode mode) {
+    cos_i = rclamp(cos_i, -1.0f, 1.0f);
+    if (!(cos_i > 0.0f)) {
+        std::swap(eta_i, eta_t);
+        if (mode == PBRT) cos_i = std::fabs(cos_i);
+    }
+    float sin_i = std::sqrt(rmax(0.0f, 1.0f - cos_i * cos_i));
+    float sin_t = eta_i / eta_t * sin_i;
+    if (sin_t >= 1.0f) return 1.0f;
+    float cos_t = std::sqrt(rmax(0.0f, 1.0f - sin_t * sin_t));
+    float rpar = ((eta_t * cos_i) - (eta_i * cos_t)) / ((eta_t * cos_i) + (eta_i * cos_t));
+    float rperp = ((eta_i * cos_i) - (eta_t * cos_t)) / ((eta_i * cos_i) + (eta_t * cos_t));
+    return (rpar * rpar + rperp * rperp) / 2.0f;
+}
+static RGB fresnel_conductor(float cos_i_in, RGB eta_i, RGB eta_t, RGB k) {  // bxdf.rs:190-217
+    RGB cos_i(rclamp(cos_i_in, -1.0f, 1.0f));
+    RGB eta = eta_t / eta_i;
+    RGB eta_k = k / eta_i;
+    RGB cos_i2 = cos_i * cos_i;
+    RGB sin_i2 = RGB(1.0f) - cos_i2;
+    RGB eta2 = eta * eta;
+    RGB eta_k2 = eta_k * eta_k;
+    RGB t0 = eta2 - eta_k2 - sin_i2;
+    RGB a2b2 = rgb_sqrt(t0 * t0 + eta2 * eta_k2 * 4.0f);
+    RGB t1 = a2b2 + cos_i2;
+    RGB a = rgb_sqrt((a2b2 + t0) * 0.5f);
+    RGB t2 = cos_i * a * 2.0f;
+    RGB rs = (t1 - t2) / (t1 + t2);
+    RGB t3 = cos_i2 * a2b2 + sin_i2 * sin_i2;
+    RGB t4 = t2 * sin_i2;
+    RGB rp = rs * (t3 - t4) / (t3 + t4);
+    return (rp + rs) * 0.5f;
+}
+// Trowbridge-Reitz (src/base/microfacet.rs)
+struct TR {
+    float ax, ay;
+    float D(V3 wh) const {  // :116-128
+        float t2 = tan2_theta(wh);
+        if (std::isinf(t2)) return 0.0f;
+        float cos4 = cos2_theta(wh) * cos2_theta(wh);
+        float e = (cos2_phi(wh) / (ax * ax) + sin2_phi(wh) / (ay * ay)) * t2;
+        return 1.0f / (PI * ax * ay * cos4 * (1.0f + e) * (1.0f + e));
+    }
+    float lambda(V3 w) const {  // :130-142
+        float at = std::fabs(tan_theta(w));
+        if (std::isinf(at)) return 0.0f;
+        float alpha = std::sqrt(cos2_phi(w) * ax * ax + sin2_phi(w) * ay * ay);
+        float a2t2 = (alpha * at) * (alpha * at);
+        return (-1.0f + std::sqrt(1.0f + a2t2)) / 2.0f;
+    }
+    // F4: REF G1 = 1/(1/lambda) (microfacet.rs:17-19); PBRT G1 = 1/(1+lambda)
+    float G1(V3 w, Mode mode) const { return mode == REF ? 1.0f / (1.0f / lambda(w)) : 1.0f / (1.0f + lambda(w)); }
+    float G(V3 wo, V3 wi) const { return 1.0f / (1.0f + lambda(wo) + lambda(wi)); }
+    float pdf(V3 wo, V3 wh, Mode mode) const { return D(wh) * G1(wo, mode) * abs_dot(wo, wh) / abs_cos_theta(wo); }
+    static void sample11(float cos_t, float u1, float u2, Mode mode, float* sx_out, float* sy_out) {  // :55-97
+        if (cos_t > 0.9999f) {
+            float r = std::sqrt(u1 / (1.0f - u1));
+            float phi = 6.28318530718f * u2;
+            *sx_out = r * std::cos(phi);
+            *sy_out = r * std::sin(phi);
+            return;
+        }
+        float sin_t = std::sqrt(rmax(1.0f - cos_t * cos_t, 0.0f));
+        float tan_t = sin_t / cos_t;
+        float a = 1.0f / tan_t;
+        float g1 = 2.0f / (1.0f + std::sqrt(1.0f + 1.0f / (a * a)));
+        float A = 2.0f * u1 / g1 - 1.0f;
+        float tmp = 1.0f / (A * A - 1.0f);
+        if (tmp > 1e10f) tmp = 1e10f;
+        float B = tan_t;
+        float D = std::sqrt(rmax(B * B * tmp * tmp - (A * A - B * B) * tmp, 0.0f));
+        float sx1 = B * tmp - D;
+        float sx2 = B * tmp + D;
+        // F5: REF always takes slope_x_1; PBRT takes slope_x_2 unless A < 0 or it is too steep
+        float sx = (mode == REF) ? sx1 : ((A < 0.0f || sx2 > 1.0f / tan_t) ? sx1 : sx2);
+        float S;
+        if (u2 > 0.5f) { S = 1.0f; u2 = 2.0f * (u2 - 0.5f); }
+        else { S = -1.0f; u2 = 2.0f * (0.5f - u2); }
+        float z = (u2 * (u2 * (u2 * 0.27385f - 0.73369f) + 0.46341f)) /
+                  (u2 * (u2 * (u2 * 0.093073f + 0.309420f) - 1.000000f) + 0.597999f);
+        *sx_out = sx;
+        *sy_out = S * z * std::sqrt(1.0f + sx * sx);
+    }
+    V3 sample_vis(V3 wi, float u1, float u2, Mode mode) const {  // :99-112
+        V3 ws = normalize(V3(ax * wi.x, ay * wi.y, wi.z));
+        float sx, sy;
+        sample11(cos_theta(ws), u1, u2, mode, &sx, &sy);
+        float tmp = cos_phi(ws) * sx - sin_phi(ws) * sy;
+        sy = sin_phi(ws) * sx + cos_phi(ws) * sy;
+        sx = tmp;
+        sx = ax * sx;
+        sy = ay * sy;
+        return normalize(V3(-sx, -sy, 1.0f));
+    }
+    V3 sample_wh(V3 wo, float u0, float u1, Mode mode) const {  // :144-153
+        bool flip = wo.z < 0.0f;
+        V3 w = flip ? -wo : wo;
+        V3 wh = sample_vis(w, u0, u1, mode);
+        return flip ? -wh : wh;
+    }
+};
+static float roughness_to_alpha(float r) {  // microfacet.rs:45-53
+    r = rmax(r, 1e-3f);
+    float x = std::log(r);
+    return 1.62142f + 0.819955f * x + 0.1734f * x * x + 0.0171201f * x * x * x + 0.000640711f * x * x * x * x;
+}
+
+enum BxKind { LAMBERT, MF_REFL, FRESNEL_SPEC };
+struct Bxdf {
+    BxKind kind;
+    uint8_t type;
+    RGB r, t;
+    TR dist{1, 1};
+    bool conductor = false;  // fresnel kind for MF_REFL
+    RGB c_eta_i, c_eta_t, c_k;
+    float d_eta_i = 1, d_eta_t = 1;
+    float eta_a = 1, eta_b = 1;
+    bool matches(uint8_t f) const { return (type & f) == type; }
+};
+struct BxSample {
+    V3 wi;
+    RGB f;
+    float pdf = 0;
+    int sampled_type = -1;
+};
+static RGB bx_f(const Bxdf& b, V3 wo, V3 wi, Mode mode) {
+    switch (b.kind) {
+        case LAMBERT: return b.r * (1.0f / PI);  // lambertian.rs:42-45
+        case MF_REFL: {                          // bxdfs/microfacet.rs:69-94
+            float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
+            V3 wh = wi + wo;
+            if (ci == 0.0f || co == 0.0f) return RGB();
+            if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return RGB();
+            wh = normalize(wh);
+            float c = dot(wi, face_forward(wh, V3(0, 0, 1)));
+            RGB F = b.conductor ? fresnel_conductor(std::fabs(c), b.c_eta_i, b.c_eta_t, b.c_k)
+                                : RGB(fresnel_dielectric(c, b.d_eta_i, b.d_eta_t, mode));
+            return b.r * b.dist.D(wh) * b.dist.G(wo, wi) * F / (4.0f * ci * co);
+        }
+        default: return RGB();
+    }
+}
+static float bx_pdf(const Bxdf& b, V3 wo, V3 wi, Mode mode) {
+    switch (b.kind) {
+        case LAMBERT: return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;  // bxdf.rs:72-78
+        case MF_REFL: {  // bxdfs/microfacet.rs:142-147
+            if (!same_hemisphere(wo, wi)) return 0.0f;
+            V3 wh = normalize(wo + wi);
+            return b.dist.pdf(wo, wh, mode) / (4.0f * dot(wo, wh));
+        }
+        default: return 0.0f;
+    }
+}
+static V3 concentric_sample_disk(float u0, float u1, float* dy) {  // sampling.rs:181-198
+    float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+    if (ox == 0.0f && oy == 0.0f) { *dy = 0.0f; return V3(); }
+    float theta, r;
+    if (std::fabs(ox) > std::fabs(oy)) { theta = (PI / 4.0f) * (oy / ox); r = ox; }
+    else { theta = PI_OVER_TWO - (PI / 4.0f) * (ox / oy); r = oy; }
+    *dy = r * std::sin(theta);
+    return V3(r * std::cos(theta), 0, 0);
+}
+static V3 cosine_sample_hemisphere(float u0, float u1) {  // sampling.rs:238-242
+    float dy;
+    float dx = concentric_sample_disk(u0, u1, &dy).x;
+    float z = std::sqrt(rmax(0.0f, 1.0f - dx * dx - dy * dy));
+    return V3(dx, dy, z);
+}
+static BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1, Mode mode) {
+    BxSample s;
+    switch (b.kind) {
+        case LAMBERT: {  // default BxDF::sample (bxdf.rs:33-45)
+            V3 wi = cosine_sample_hemisphere(u0, u1);
+            if (wo.z < 0.0f) wi.z *= -1.0f;
+            s.wi = wi;
+            s.f = bx_f(b, wo, wi, mode);
+            s.pdf = bx_pdf(b, wo, wi, mode);
+            return s;
+        }
+        case MF_REFL: {  // bxdfs/microfacet.rs:96-140
+            if (wo.z == 0.0f) return s;
+            V3 wh = b.dist.sample_wh(wo, u0, u1, mode);
+            if (dot(wo, wh) < 0.0f) return s;
+            V3 wi = reflect(wo, wh);
+            if (!same_hemisphere(wo, wi)) return s;
+            s.wi = wi;
+            s.f = bx_f(b, wo, wi, mode);
+            s.pdf = b.dist.pdf(wo, wh, mode) / (4.0f * dot(wo, wh));
+            return s;
+        }
+        case FRESNEL_SPEC: {  // bxdfs/fresnel.rs:76-122
+            float F = fresnel_dielectric(cos_theta(wo), b.eta_a, b.eta_b, mode);
+            if (u0 < F) {
+                V3 wi(-wo.x, -wo.y, wo.z);
+                s.wi = wi;
+                s.pdf = F;
+                s.f = RGB(F) * b.r / abs_cos_theta(wi);
+                s.sampled_type = BSDF_SPECULAR | BSDF_REFLECTION;
+                return s;
+            }
+            bool entering = cos_theta(wo) > 0.0f;
+            float ei = entering ? b.eta_a : b.eta_b, et = entering ? b.eta_b : b.eta_a;
+            V3 wi;
+            if (!refract(wo, face_forward(V3(0, 0, 1), wo), ei / et, &wi)) return s;
+            RGB ft = b.t * (1.0f - F);
+            ft = ft * ((ei * ei) / (et * et));
+            s.wi = wi;
+            s.f = ft / abs_cos_theta(wi);
+            s.pdf = 1.0f - F;
+            s.sampled_type = BSDF_SPECULAR | BSDF_TRANSMISSION;
+            return s;
+        }
+    }
+    return s;
+}
+
+struct BSDF {  // src/base/bsdf.rs
+    float eta = 1.0f;
+    V3 ns, ng, ss, ts;
+    Bxdf bx[2];
+    int n = 0;
+    int num_components(uint8_t f) const {
+        int k = 0;
+        for (int i = 0; i < n; ++i) k += bx[i].matches(f);
+        return k;
+    }
+    V3 to_local(V3 v) const { return V3(dot(v, ss), dot(v, ts), dot(v, ns)); }
+    V3 to_world(V3 v) const {
+        return V3(ss.x * v.x + ts.x * v.y + ns.x * v.z, ss.y * v.x + ts.y * v.y + ns.y * v.z,
+                  ss.z * v.x + ts.z * v.y + ns.z * v.z);
+    }
+    RGB f(V3 wo_w, V3 wi_w, uint8_t flags, Mode mode) const {  // bsdf.rs:84-105
+        V3 wo = to_local(wo_w), wi = to_local(wi_w);
+        if (wo.z == 0.0f) return RGB();
+        bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
+        RGB r;
+        for (int i = 0; i < n; ++i)
+            if (bx[i].matches(flags) && ((refl && (bx[i].type & BSDF_REFLECTION)) ||
+                                         (!refl && (bx[i].type & BSDF_TRANSMISSION))))
+                r = r + bx_f(bx[i], wo, wi, mode);
+        return r;
+    }
+    float pdf(V3 wo_w, V3 wi_w, uint8_t flags, Mode mode) const {  // bsdf.rs:234-259
+        if (n == 0) return 0.0f;
+        V3 wo = to_local(wo_w), wi = to_local(wi_w);
+        if (wo.z == 0.0f) return 0.0f;
+        float ret = 0.0f, comps = 0.0f;
+        for (int i = 0; i < n; ++i)
+            if (bx[i].matches(flags)) { comps += 1.0f; ret += bx_pdf(bx[i], wo, wi, mode); }
+        return comps > 0.0f ? ret / comps : 0.0f;
+    }
+    BxSample sample(V3 wo_w, float u0, float u1, uint8_t type, Mode mode) const {  // bsdf.rs:140-232
+        BxSample zero;
+        zero.sampled_type = 0;
+        int matches = num_components(type);
+        if (matches == 0) return zero;
+        uint32_t comp = std::min((uint32_t)std::floor(u0 * (float)matches), (uint32_t)matches - 1);
+        // F8: REF decrements the counter for every BxDF (u32), PBRT only for matching ones
+        uint32_t count = comp;
+        int pick = -1;
+        for (int i = 0; i < n; ++i) {
+            if (bx[i].matches(type) && count == 0) { pick = i; break; }
+            if (mode == REF || bx[i].matches(type)) count -= 1;
+        }
+        if (pick < 0) return zero;  // the reference panics here (bsdf.rs:162)
+        const Bxdf& b = bx[pick];
+        float ur0 = rmin(u0 * (float)matches - (float)comp, ONE_MINUS_EPSILON);
+        V3 wo = to_local(wo_w);
+        if (wo.z == 0.0f) return zero;
+        BxSample s = bx_sample(b, wo, ur0, u1, mode);
+        int stype = s.sampled_type >= 0 ? s.sampled_type : b.type;
+        if (s.pdf == 0.0f) return zero;
+        V3 wi_w = to_world(s.wi);
+        if (!(b.type & BSDF_SPECULAR) && matches > 1)
+            for (int i = 0; i < n; ++i)
+                if (i != pick && bx[i].matches(type)) s.pdf += bx_pdf(bx[i], wo, s.wi, mode);
+        if (matches > 1) s.pdf /= (float)matches;
+        if (!(b.type & BSDF_SPECULAR)) {
+            bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
+            s.f = RGB();
+            for (int i = 0; i < n; ++i)
+                if (bx[i].matches(type) && ((refl && (bx[i].type & BSDF_REFLECTION)) ||
+                                            (!refl && (bx[i].type & BSDF_TRANSMISSION))))
+                    s.f = s.f + bx_f(bx[i], wo, s.wi, mode);
+        }
+        s.wi = wi_w;
+        s.sampled_type = stype;
+        return s;
+    }
+};
+// Material::compute_scattering_functions (materials/matte.rs:19-41, plastic.rs:65-95 and the
+// composed conductor / dielectric)
+static BSDF make_bsdf(const Scene& s, const Interaction& it) {
+    const bg_material& m = s.mats[it.prim < s.ntri ? s.tri_mat[it.prim] : s.sph[it.prim - s.ntri].mat];
+    BSDF b;
+    b.ns = it.shading_n;
+    b.ng = it.n;
+    b.ss = normalize(it.shading_dpdu);
+    b.ts = cross(b.ns, b.ss);
+    auto clamp0 = [](const float* c) {
+        return RGB(rclamp(c[0], 0.0f, INFINITY), rclamp(c[1], 0.0f, INFINITY), rclamp(c[2], 0.0f, INFINITY));
+    };
+    if (m.type == BG_MAT_MATTE || m.type == BG_MAT_PLASTIC) {
+        RGB kd = clamp0(m.kd);
+        if (!kd.is_black()) {
+            Bxdf l;
+            l.kind = LAMBERT;
+            l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
+            l.r = kd;
+            b.bx[b.n++] = l;
+        }
+        if (m.type == BG_MAT_PLASTIC) {
+            RGB ks = clamp0(m.ks);
+            if (!ks.is_black()) {
+                float rough = m.roughness;
+                if (m.remap_roughness) rough = roughness_to_alpha(rough);
+                Bxdf g;
+                g.kind = MF_REFL;
+                g.type = BSDF_REFLECTION | BSDF_GLOSSY;
+                g.r = ks;
+                g.dist = TR{rmax(rough, 0.001f), rmax(rough, 0.001f)};
+                g.conductor = false;
+                g.d_eta_i = 1.5f;
+                g.d_eta_t = 1.0f;
+                b.bx[b.n++] = g;
+            }
+        }
+    } else if (m.type == BG_MAT_CONDUCTOR) {
+        Bxdf g;
+        g.kind = MF_REFL;
+        g.type = BSDF_REFLECTION | BSDF_GLOSSY;
+        g.r = RGB(1.0f);
+        g.dist = TR{rmax(m.roughness, 0.001f), rmax(m.roughness, 0.001f)};
+        g.conductor = true;
+        g.c_eta_i = RGB(1.0f);
+        g.c_eta_t = RGB(m.eta[0], m.eta[1], m.eta[2]);
+        g.c_k = RGB(m.k[0], m.k[1], m.k[2]);
+        b.bx[b.n++] = g;
+    } else {  // dielectric
+        b.eta = m.ior;
+        Bxdf d;
+        d.kind = FRESNEL_SPEC;
+        d.type = BSDF_REFLECTION | BSDF_TRANSMISSION | BSDF_SPECULAR;
+        d.r = RGB(1.0f);
+        d.t = RGB(1.0f);
+        d.eta_a = 1.0f;
+        d.eta_b = m.ior;
+        b.bx[b.n++] = d;
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------- lights (src/lights/diffuse.rs)
+static RGB emission(const bg_area_light& l, V3 n, V3 dir) {  // diffuse.rs:163-169
+    if (l.two_sided || dot(n, dir) > 0.0f) return RGB(l.intensity[0], l.intensity[1], l.intensity[2]);
+    return RGB();
+}
+static RGB emitted_radiance(const Scene& s, const Interaction& it, V3 w) {  // interaction.rs:257-266
+    if (it.prim < 0) return RGB();
+    int32_t e = s.prim_emission[it.prim];
+    if (e < 0) return RGB();
+    return emission(s.emis[e], it.n, w);
+}
+struct LightSample {
+    RGB radiance;
+    V3 wi;
+    float pdf = 0.0f;
+    Interaction p0, p1;
+    bool vis = false;
+};
+static LightSample light_sample_point(const Scene& s, int64_t prim, const Interaction& it, float u0, float u1,
+                                      Mode mode) {  // diffuse.rs:54-87 + shape.rs:17-34
+    LightSample ls;
+    float pdf_area;
+    Interaction pit = tri_sample(s, prim, u0, u1, &pdf_area);
+    V3 wi = pit.p - it.p;
+    float pdf;
+    if (length_squared(wi) == 0.0f) pdf = 0.0f;
+    else {
+        wi = normalize(wi);
+        // F13: REF overwrites the area pdf with dist^2/|cos| (shape.rs:31-32); PBRT multiplies
+        float conv = distance_squared(it.p, pit.p) / abs_dot(pit.n, -wi);
+        pdf = mode == REF ? conv : pdf_area * conv;
+        if (std::isinf(pdf)) pdf = 0.0f;
+    }
+    if (pdf == 0.0f || length_squared(pit.p - it.p) == 0.0f) return ls;
+    ls.wi = normalize(pit.p - it.p);
+    // F12: REF evaluates the emission toward +wi (diffuse.rs:67); PBRT toward -wi
+    ls.radiance = emission(s.emis[s.prim_emission[prim]], pit.n, mode == REF ? ls.wi : -ls.wi);
+    ls.pdf = pdf;
+    ls.p0 = it;
+    ls.p0.surface = false;
+    ls.p1 = pit;
+    ls.vis = true;
+    return ls;
+}
+static float light_point_pdf(const Scene& s, int64_t prim, const Interaction& it, V3 wi, Mode mode) {  // shape.rs:40-57
+    Ray ray = spawn_ray(it, wi, mode);
+    float t;
+    Interaction iit;
+    if (!tri_intersect(s, prim, ray, &t, &iit, false)) return 0.0f;
+    float pdf = distance_squared(it.p, iit.p) / (abs_dot(iit.n, -wi) * tri_area(s, prim));
+    if (std::isinf(pdf)) pdf = 0.0f;
+    return pdf;
+}
+static float power_heuristic(float nf, float fpdf, float ng, float gpdf) {  // sampling.rs:248-252
+    float f = nf * fpdf, g = ng * gpdf;
+    return (f * f) / (f * f + g * g);
+}
+
+// estimate_direct (src/base/integrator.rs:330-437)
+static RGB estimate_direct(const Scene& s, const Interaction& it, const BSDF& bsdf, int64_t light_prim, float us0,
+                           float us1, float ul0, float ul1, Mode mode, Counters* cnt) {
+    const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
+    RGB out;
+    LightSample ls = light_sample_point(s, light_prim, it, ul0, ul1, mode);
+    float scattering_pdf = 0.0f;
+    if (ls.pdf > 0.0f && !ls.radiance.is_black()) {
+        RGB f = bsdf.f(it.wo, ls.wi, flags, mode) * abs_dot(ls.wi, it.shading_n);
+        scattering_pdf = bsdf.pdf(it.wo, ls.wi, flags, mode);
+        if (!f.is_black()) {
+            if (cnt) cnt->shadow_rays++;
+            if (scene_intersect_test(s, spawn_ray_to_it(ls.p0, ls.p1), cnt)) ls.radiance = RGB();
+            if (!ls.radiance.is_black()) {
+                float w = power_heuristic(1.0f, ls.pdf, 1.0f, scattering_pdf);
+                out = out + f * ls.radiance * w / ls.pdf;
+            }
+        }
+    }
+    // BSDF sampling half
+    BxSample bs = bsdf.sample(it.wo, us0, us1, flags, mode);
+    RGB f = bs.f * abs_dot(bs.wi, it.shading_n);
+    bool sampled_specular = (bs.sampled_type & BSDF_SPECULAR) != 0;
+    if (mode == REF) {
+        // F2: ray along the LIGHT sample direction, pdf and weight from the light half, any emitter
+        if (!f.is_black() && scattering_pdf > 0.0f) {
+            float w = 1.0f;
+            if (!sampled_specular) {
+                float lpdf = light_point_pdf(s, light_prim, it, ls.wi, mode);
+                if (lpdf == 0.0f) return out;
+                w = power_heuristic(1.0f, scattering_pdf, 1.0f, lpdf);
+            }
+            Interaction lit;
+            Ray ray = spawn_ray(it, ls.wi, mode);
+            if (cnt) cnt->ext_rays++;
+            RGB rad;
+            if (scene_intersect(s, ray, &lit, cnt)) {
+                if (s.prim_emission[lit.prim] >= 0) rad = emitted_radiance(s, lit, -ls.wi);
+            }
+            if (!rad.is_black()) out = out + f * rad * w / scattering_pdf;
+        }
+    } else {
+        float spdf = bs.pdf;
+        if (!f.is_black() && spdf > 0.0f) {
+            float w = 1.0f;
+            if (!sampled_specular) {
+                float lpdf = light_point_pdf(s, light_prim, it, bs.wi, mode);
+                if (lpdf == 0.0f) return out;
+                w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
+            }
+            Interaction lit;
+            Ray ray = spawn_ray(it, bs.wi, mode);
+            if (cnt) cnt->ext_rays++;
+            RGB li;
+            if (scene_intersect(s, ray, &lit, cnt)) {
+                if (lit.prim == light_prim) li = emitted_radiance(s, lit, -bs.wi);
+            }
+            if (!li.is_black()) out = out + f * li * w / spdf;
+        }
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------- camera (perspective.rs)
+struct Camera {
+    Transform raster_to_camera, camera_to_world;
+    int w, h;
+    explicit Camera(const bg_camera& c) {  // perspective.rs:49-113
+        w = (int)c.width;
+        h = (int)c.height;
+        float rx = (float)c.width, ry = (float)c.height;
+        Transform c2s = t_perspective(c.fov_deg, c.near_plane, c.far_plane);
+        float sminx, smaxx, sminy, smaxy;
+        float frame = rx / ry;
+        if (frame > 1.0f) { sminx = -frame; smaxx = frame; sminy = -1.0f; smaxy = 1.0f; }
+        else { sminx = -1.0f; smaxx = 1.0f; sminy = -1.0f / frame; smaxy = 1.0f / frame; }
+        Transform s2r = t_mul(t_mul(t_scale(rx, ry, 1.0f),
+                                    t_scale(1.0f / (smaxx - sminx), 1.0f / (sminy - smaxy), 1.0f)),
+                              t_translate(V3(-sminx, -smaxy, 0.0f)));
+        Transform r2s = t_inverse(s2r);
+        raster_to_camera = t_mul(t_inverse(c2s), r2s);
+        camera_to_world = t_look_at(V3(c.position[0], c.position[1], c.position[2]),
+                                    V3(c.look_at[0], c.look_at[1], c.look_at[2]), V3(c.up[0], c.up[1], c.up[2]));
+    }
+    Ray generate_ray(float fx, float fy, float tu) const {  // perspective.rs:117-175 (pinhole)
+        V3 cp = xf_point(raster_to_camera, V3(fx, fy, 0.0f));
+        Ray r{V3(0, 0, 0), normalize(cp), INFINITY, 0.0f};
+        r.time = (1.0f - tu) * 0.0f + tu * 1.0f;  // lerp(time, 0, 1), math.rs:7-9
+        return xf_ray(camera_to_world, r);
+    }
+};
+
+// ---------------------------------------------------------------- PathIntegrator::radiance
+// src/integrators/path.rs:51-146
+static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max_depth, float rr_threshold,
+                    Mode mode, Counters* cnt) {
+    RGB out, beta(1.0f);
+    bool specular_bounce = false;
+    float eta_scale = 1.0f;
+    uint32_t bounces = 0;
+    for (;;) {
+        Interaction it;
+        if (cnt) cnt->ext_rays++;
+        bool hit = scene_intersect(s, ray, &it, cnt);
+        if (bounces == 0 || specular_bounce) {
+            if (hit) out = out + beta * emitted_radiance(s, it, -ray.d);
+            // lights' radiance(ray) is zero for area lights (light.rs:31-33)
+        }
+        if (!hit || bounces >= max_depth) break;
+        BSDF bsdf = make_bsdf(s, it);
+        const uint32_t base = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounces;
+        if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && !s.light_prims.empty()) {
+            // uniform_sample_one_light (integrator.rs:309-328)
+            float count = (float)s.light_prims.size();
+            size_t li = (size_t)rmin(rng.u(base + BD_LIGHT) * count, count - 1.0f);
+            float light_pdf = 1.0f / count;
+            RGB ld = estimate_direct(s, it, bsdf, s.light_prims[li], rng.u(base + BD_USCAT),
+                                     rng.u(base + BD_USCAT + 1), rng.u(base + BD_ULIGHT),
+                                     rng.u(base + BD_ULIGHT + 1), mode, cnt);
+            out = out + beta * (ld / light_pdf);
+        }
+        V3 wo = -ray.d;
+        BxSample bs = bsdf.sample(wo, rng.u(base + BD_BSDF), rng.u(base + BD_BSDF + 1), BSDF_ALL, mode);
+        if (bs.f.is_black() || bs.pdf == 0.0f) break;
+        beta = beta * (bs.f * abs_dot(bs.wi, it.shading_n) / bs.pdf);
+        specular_bounce = (bs.sampled_type & BSDF_SPECULAR) != 0;
+        if ((bs.sampled_type & BSDF_SPECULAR) && (bs.sampled_type & BSDF_TRANSMISSION)) {
+            float eta = bsdf.eta;
+            eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
+        }
+        // F1: REF keeps re-intersecting the same camera ray (t_max already at the hit);
+        // PBRT spawns the next ray along the sampled direction.
+        if (mode == PBRT) ray = spawn_ray(it, bs.wi, mode);
+        RGB rr_beta = beta * eta_scale;
+        if (rr_beta.max_component_value() < rr_threshold && bounces > 3) {
+            float q = rmax(1.0f - rr_beta.max_component_value(), 0.5f);
+            if (rng.u(base + BD_RR) < q) break;
+            beta = beta / (1.0f - q);
+        }
+        bounces += 1;
+    }
+    return out;
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+// ================================================================= C API (ctypes)
+extern "C" {
+
+void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_mat, const int32_t* tri_light,
+                       const bg_sphere* sph, int64_t nsph, const bg_material* mats, int32_t nmat,
+                       const bg_area_light* emis, int32_t nemis, int32_t bvh_fixed) {
+    Scene* s = new Scene();
+    s->ntri = ntri;
+    s->nsph = nsph;
+    s->pos.resize(3 * ntri);
+    for (int64_t i = 0; i < 3 * ntri; ++i) s->pos[i] = V3(tri_xyz[3 * i], tri_xyz[3 * i + 1], tri_xyz[3 * i + 2]);
+    s->tri_mat.assign(tri_mat, tri_mat + ntri);
+    s->mats.assign(mats, mats + nmat);
+    s->emis.assign(emis, emis + nemis);
+    s->prim_emission.assign(ntri + nsph, -1);
+    s->prim_light.assign(ntri + nsph, -1);
+    for (int64_t i = 0; i < ntri; ++i) {
+        if (tri_light && tri_light[i] >= 0) {
+            s->prim_emission[i] = tri_light[i];
+            s->prim_light[i] = (int32_t)s->light_prims.size();
+            s->light_prims.push_back(i);
+        }
+    }
+    for (int64_t i = 0; i < nsph; ++i) {
+        Sphere sp;
+        V3 c(sph[i].center[0], sph[i].center[1], sph[i].center[2]);
+        sp.o2w = t_translate(c);
+        sp.w2o = is_identity(sp.o2w) ? sp.o2w : t_inverse(sp.o2w);
+        float r = sph[i].radius;
+        sp.radius = r;
+        sp.z_min = rclamp(rmin(-r, r), -r, r);
+        sp.z_max = rclamp(rmax(-r, r), -r, r);
+        sp.theta_min = std::acos(rclamp(rmin(-r, r) / r, -1.0f, 1.0f));
+        sp.theta_max = std::acos(rclamp(rmax(-r, r) / r, -1.0f, 1.0f));
+        sp.phi_max = rclamp(360.0f, 0.0f, 360.0f) * (PI / 180.0f);
+        sp.mat = sph[i].material_id;
+        s->sph.push_back(sp);
+    }
+    build_bvh(*s, bvh_fixed != 0);
+    return s;
+}
+
+void orc_scene_destroy(void* p) { delete (Scene*)p; }
+int64_t orc_bvh_nodes(void* p) { return (int64_t)((Scene*)p)->nodes.size(); }
+int64_t orc_num_lights(void* p) { return (int64_t)((Scene*)p)->light_prims.size(); }
+
+static void parallel_for(int64_t n, int threads, const std::function<void(int64_t, int)>& fn) {
+    if (threads <= 1 || n <= 1) {
+        for (int64_t i = 0; i < n; ++i) fn(i, 0);
+        return;
+    }
+    std::atomic<int64_t> next(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&, t]() {
+            for (;;) {
+                int64_t i = next.fetch_add(1);
+                if (i >= n) break;
+                fn(i, t);
+            }
+        });
+    for (auto& th : pool) th.join();
+}
+
+// Closest-hit / any-hit over a ray set; counters[0..1] = node visits, primitive tests.
+void orc_trace(void* p, const bg_ray* rays, int64_t n, int32_t any_only, bg_hit* hits, uint8_t* occluded,
+               int64_t* counters, int32_t threads) {
+    const Scene& s = *(const Scene*)p;
+    const int64_t chunk = 4096;
+    int64_t nchunks = (n + chunk - 1) / chunk;
+    int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    std::vector<Counters> cs(nt);
+    parallel_for(nchunks, nt, [&](int64_t c, int t) {
+        Counters* cnt = counters ? &cs[t] : nullptr;
+        for (int64_t i = c * chunk; i < std::min(n, (c + 1) * chunk); ++i) {
+            Ray r{V3(rays[i].org[0], rays[i].org[1], rays[i].org[2]),
+                  V3(rays[i].dir[0], rays[i].dir[1], rays[i].dir[2]), rays[i].tmax, 0.0f};
+            if (any_only) {
+                occluded[i] = scene_intersect_test(s, r, cnt) ? 1 : 0;
+            } else {
+                Interaction it;
+                if (scene_intersect(s, r, &it, cnt)) { hits[i].prim = it.prim; hits[i].t = r.t_max; }
+                else { hits[i].prim = -1; hits[i].t = INFINITY; }
+            }
+        }
+    });
+    if (counters) {
+        Counters tot;
+        for (auto& c : cs) tot.add(c);
+        counters[0] = any_only ? tot.sh_visits : tot.ext_visits;
+        counters[1] = any_only ? tot.sh_tests : tot.ext_tests;
+    }
+}
+
+// Renders rows [y0, y1) with stride ystep (all columns), tile rows of 16 as parallel tasks
+// (src/base/integrator.rs:35-133).  Outputs (each may be NULL): rgb (w*h*3, Film::write_image
+// values for the rendered rows), sum / sumsq (w*h*3 doubles of the sanitized sample radiance).
+// counters[0..6] = extension rays, shadow rays, ext visits, ext tests, shadow visits, shadow tests,
+// zeroed samples (counted only when counters != NULL and count_traversal != 0 for 2..5).
+int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_t y0, int32_t y1, int32_t ystep,
+               int32_t threads, int32_t count_traversal, float* rgb, double* sum, double* sumsq, int64_t* counters) {
+    const Scene& s = *(const Scene*)p;
+    Camera camera(*cam);
+    const int W = camera.w, H = camera.h;
+    if (y0 < 0) y0 = 0;
+    if (y1 > H) y1 = H;
+    if (ystep < 1) ystep = 1;
+    Mode mode = opts->mode == BG_MODE_PBRT ? PBRT : REF;
+    int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    const int TILE = 16;
+    int ntx = (W + TILE - 1) / TILE, nty = (H + TILE - 1) / TILE;
+    std::vector<Counters> cs(nt);
+    parallel_for(nty, nt, [&](int64_t ty, int t) {
+        Counters* cnt = (counters && count_traversal) ? &cs[t] : nullptr;
+        Counters& cbase = cs[t];
+        for (int tx = 0; tx < ntx; ++tx) {
+            for (int y = (int)ty * TILE; y < std::min(H, (int)(ty + 1) * TILE); ++y) {
+                if (y < y0 || y >= y1 || ((y - y0) % ystep) != 0) continue;
+                for (int x = tx * TILE; x < std::min(W, (tx + 1) * TILE); ++x) {
+                    RGB tile_sum;  // FilmTilePixel::contribution_sum (f32)
+                    float wsum = 0.0f;
+                    double s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+                    CounterRng rng;
+                    rng.pixel = (uint32_t)(y * W + x);
+                    rng.seed = opts->seed;
+                    for (uint32_t si = 0; si < opts->spp; ++si) {
+                        rng.sample = opts->first_sample + si;
+                        float fx = (float)x + rng.u(DIM_FILM), fy = (float)y + rng.u(DIM_FILM + 1);
+                        Ray ray = camera.generate_ray(fx, fy, rng.u(DIM_TIME));
+                        Counters local;
+                        RGB L = radiance(s, ray, rng, opts->max_depth, opts->rr_threshold, mode,
+                                         cnt ? cnt : (counters ? &local : nullptr));
+                        if (!cnt && counters) { cbase.ext_rays += local.ext_rays; cbase.shadow_rays += local.shadow_rays; }
+                        // sanity checks (integrator.rs:91-117)
+                        if (L.is_nan() || L.y() < -1e-5f || std::isinf(L.y())) {
+                            L = RGB();
+                            cbase.nan_samples++;
+                        }
+                        // FilmTile::add_sample with BoxFilter r=0.5: weight 1 to the sample's pixel
+                        tile_sum = tile_sum + L * 1.0f * 1.0f;
+                        wsum += 1.0f;
+                        for (int c = 0; c < 3; ++c) { s1[c] += L.c[c]; s2[c] += (double)L.c[c] * L.c[c]; }
+                    }
+                    size_t pix = (size_t)y * W + x;
+                    if (sum) for (int c = 0; c < 3; ++c) sum[3 * pix + c] = s1[c];
+                    if (sumsq) for (int c = 0; c < 3; ++c) sumsq[3 * pix + c] = s2[c];
+                    if (rgb) {
+                        // merge_film_tile (rgb_to_xyz, film.rs:138-154) + write_image (film.rs:156-202)
+                        float X = 0.412453f * tile_sum.c[0] + 0.357580f * tile_sum.c[1] + 0.180423f * tile_sum.c[2];
+                        float Y = 0.212671f * tile_sum.c[0] + 0.715160f * tile_sum.c[1] + 0.072169f * tile_sum.c[2];
+                        float Z = 0.019334f * tile_sum.c[0] + 0.119193f * tile_sum.c[1] + 0.950227f * tile_sum.c[2];
+                        float r = 3.240479f * X - 1.537150f * Y - 0.498535f * Z;
+                        float g = -0.969256f * X + 1.875991f * Y + 0.041556f * Z;
+                        float b = 0.055648f * X - 0.204043f * Y + 1.057311f * Z;
+                        if (wsum != 0.0f) {
+                            float inv = 1.0f / wsum;
+                            r = rmax(r * inv, 0.0f);
+                            g = rmax(g * inv, 0.0f);
+                            b = rmax(b * inv, 0.0f);
+                        }
+                        rgb[3 * pix] = r;
+                        rgb[3 * pix + 1] = g;
+                        rgb[3 * pix + 2] = b;
+                    }
+                }
+            }
+        }
+    });
+    if (counters) {
+        Counters tot;
+        for (auto& c : cs) tot.add(c);
+        counters[0] = tot.ext_rays;
+        counters[1] = tot.shadow_rays;
+        counters[2] = tot.ext_visits;
+        counters[3] = tot.ext_tests;
+        counters[4] = tot.sh_visits;
+        counters[5] = tot.sh_tests;
+        counters[6] = tot.nan_samples;
+    }
+    return 0;
+}
+
+// Unit probes used by the tests: one BSDF sample / eval for a material at a canonical frame.
+// frame: ns = (0,0,1), ng = ns, ss = (1,0,0).  out[0..2] f, out[3] pdf, out[4..6] wi, out[7] type.
+void orc_bsdf_sample(const bg_material* m, const float* wo, float u0, float u1, int32_t mode, float* out) {
+    Scene s;
+    s.ntri = 1;
+    s.tri_mat.push_back(0);
+    s.mats.push_back(*m);
+    Interaction it;
+    it.prim = 0;
+    it.n = V3(0, 0, 1);
+    it.shading_n = it.n;
+    it.shading_dpdu = V3(1, 0, 0);
+    BSDF b = make_bsdf(s, it);
+    BxSample bs = b.sample(V3(wo[0], wo[1], wo[2]), u0, u1, BSDF_ALL, mode == 1 ? PBRT : REF);
+    out[0] = bs.f.c[0]; out[1] = bs.f.c[1]; out[2] = bs.f.c[2]; out[3] = bs.pdf;
+    out[4] = bs.wi.x; out[5] = bs.wi.y; out[6] = bs.wi.z; out[7] = (float)bs.sampled_type;
+}
+void orc_bsdf_eval(const bg_material* m, const float* wo, const float* wi, int32_t mode, float* out) {
+    Scene s;
+    s.ntri = 1;
+    s.tri_mat.push_back(0);
+    s.mats.push_back(*m);
+    Interaction it;
+    it.prim = 0;
+    it.n = V3(0, 0, 1);
+    it.shading_n = it.n;
+    it.shading_dpdu = V3(1, 0, 0);
+    BSDF b = make_bsdf(s, it);
+    Mode md = mode == 1 ? PBRT : REF;
+    RGB f = b.f(V3(wo[0], wo[1], wo[2]), V3(wi[0], wi[1], wi[2]), BSDF_ALL, md);
+    out[0] = f.c[0]; out[1] = f.c[1]; out[2] = f.c[2];
+    out[3] = b.pdf(V3(wo[0], wo[1], wo[2]), V3(wi[0], wi[1], wi[2]), BSDF_ALL, md);
+}
+float orc_rng_uniform(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
+    CounterRng r;
+    r.seed = seed;
+    r.pixel = pixel;
+    r.sample = sample;
+    return r.u(dim);
+}
+// Camera ray for a film sample (perspective.rs:117-175): out = ox oy oz dx dy dz.
+void orc_camera_ray(const bg_camera* cam, float fx, float fy, float tu, float* out) {
+    Camera c(*cam);
+    Ray r = c.generate_ray(fx, fy, tu);
+    out[0] = r.o.x; out[1] = r.o.y; out[2] = r.o.z; out[3] = r.d.x; out[4] = r.d.y; out[5] = r.d.z;
+}
+
+}  // extern "C"

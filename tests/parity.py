@@ -1,0 +1,38 @@
+"""Shared parity helpers for the GPU-vs-oracle tests (test infrastructure)."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def pixel_stats(sum_, sumsq, n):
+    n = np.maximum(np.asarray(n, np.float64), 1.0)
+    if n.ndim == sum_.ndim - 1:
+        n = n[..., None]
+    mean = sum_ / n
+    var = np.maximum(sumsq / n - mean * mean, 0.0)
+    se = np.sqrt(var / n)
+    return mean, se
+
+
+def compare_renders(g_sum, g_sumsq, g_n, o_sum, o_sumsq, o_n):
+    """Per-pixel, per-channel comparison of two Monte Carlo renders of the same scene and spp.
+
+    Returns dict(frac_z3, max_abs_z, frac_close, rel_mean_diff): frac_z3 is the fraction of
+    pixel channels whose means differ by more than 3 combined standard errors; frac_close the
+    fraction agreeing to 1e-4 relative (identical random numbers make most paths identical).
+    """
+    mg, sg = pixel_stats(g_sum, g_sumsq, g_n)
+    mo, so = pixel_stats(o_sum, o_sumsq, o_n)
+    d = mg - mo
+    se = np.sqrt(sg * sg + so * so)
+    tiny = 1e-6 * (1.0 + np.abs(mo))
+    z = np.where(se > 0, d / np.maximum(se, 1e-30), np.where(np.abs(d) <= tiny, 0.0, np.inf))
+    close = np.abs(d) <= 1e-4 * (1.0 + np.abs(mo))
+    return {
+        "frac_z3": float(np.mean(np.abs(z) > 3.0)),
+        "max_abs_z": float(np.max(np.abs(z))),
+        "frac_close": float(np.mean(close)),
+        "rel_mean_diff": float(abs(mg.mean() - mo.mean()) / max(abs(mo.mean()), 1e-12)),
+        "mean_g": float(mg.mean()),
+        "mean_o": float(mo.mean()),
+    }
