@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
+    p.add_argument("--profile-spp", type=int, default=1)
     return p.parse_args()
 
 
@@ -316,8 +319,28 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """One render of the production scene (full geometry and resolution, few spp): the case the ncu
+    launch list and kernel captures run on (a few GB on the device, BVH larger than L2)."""
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    sd = workload(False)
+    ctx = G.Context(0)
+    scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    pi = G.PathIntegrator(sd.camera, args.profile_spp, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT)
+    r = pi.render(scene, readback=False)
+    print(json.dumps({"profile_case": True, "spp": args.profile_spp, "device_ms": r.stats.device_ms,
+                      "launches": int(r.stats.launches), "extension_rays": int(r.stats.extension_rays),
+                      "shadow_rays": int(r.stats.shadow_rays)}))
+    scene.close()
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
