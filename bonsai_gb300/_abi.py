@@ -39,6 +39,10 @@ BG_RENDER_NO_READBACK = 2
 BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
 
+BG_NOALLOC_MAX_PIXELS = 512 * 512
+BG_NOALLOC_WAVE_PATHS = 65536
+BG_NOALLOC_SCRATCH_BYTES = 27788288
+
 F3 = C.c_float * 3
 
 
@@ -124,6 +128,7 @@ SIGNATURES = {
     "bg_device_free": (ST, [P, P]),
     "bg_memcpy_h2d": (ST, [P, P, P, C.c_size_t]),
     "bg_memcpy_d2h": (ST, [P, P, P, C.c_size_t]),
+    "bg_render_noalloc": (ST, [P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P, P]),
 }
 
 _LIB = None

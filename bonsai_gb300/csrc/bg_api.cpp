@@ -343,6 +343,21 @@ bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
 
 }  // namespace
 
+namespace bg {
+// Scene internals for the allocation-free render entry point (bg_noalloc.cu).
+bool scene_device_view(const bg_scene* s, Scene* dev, uint32_t* kind, int* device) {
+    if (!s || !s->ctx || !s->committed) return false;
+    *dev = s->dev;
+    *kind = s->kind;
+    *device = s->ctx->device;
+    return true;
+}
+void scene_set_error(const bg_scene* s, const std::string& msg) {
+    if (s && s->ctx) s->ctx->err = msg;
+}
+Camera camera_for(const bg_camera& c) { return make_camera(c); }
+}  // namespace bg
+
 extern "C" {
 
 const char* bg_status_string(bg_status s) {

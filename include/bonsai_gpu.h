@@ -220,6 +220,26 @@ bg_status bg_device_free(bg_ctx* ctx, void* d_ptr);
 bg_status bg_memcpy_h2d(bg_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
 bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
 
+/* ---- render without device allocation ------------------------------------------------------
+ * No counterpart in the reference: an addition for callers that must not allocate device memory
+ * while they render, such as a plugin whose host application owns the GPU memory budget and only
+ * allows allocation at load time, or a frame loop that must never block in the allocator.
+ * Same semantics as bg_render, but it calls no cudaMalloc, cudaFree or other allocating routine:
+ * its scratch (film moments, wavefront queues, path state, counters) lives in one static device
+ * array of BG_NOALLOC_SCRATCH_BYTES bytes that every GPU loading the library holds until exit.
+ * Limits: at most BG_NOALLOC_MAX_PIXELS film pixels (larger films return BG_ERR_INVALID with the
+ * limit in bg_last_error of the scene's context); waves of BG_NOALLOC_WAVE_PATHS paths; no
+ * ACCUMULATE / STAGE_TIMING / GRAPH flags.  The caller passes the committed scene, the output
+ * d_rgb_out (device memory, width*height*3 floats) and a CUDA stream (NULL = default stream); the
+ * call synchronizes that stream before returning.  The first call on a device resolves the
+ * array's device address, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+#define BG_NOALLOC_MAX_PIXELS (512u * 512u)
+#define BG_NOALLOC_WAVE_PATHS 65536u
+#define BG_NOALLOC_SCRATCH_BYTES 27788288u
+bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, const bg_render_opts* opts,
+                            float* d_rgb_out, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
