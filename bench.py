@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--profile", action="store_true",
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
+    p.add_argument("--no-autotune", action="store_true")
     return p.parse_args()
 
 
@@ -243,6 +244,12 @@ def run_ours(args):
     upload_build_s = time.time() - t0
     pi = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=0)
     samples = sd.camera.width * sd.camera.height * sd.spp
+    tuning = None
+    if not args.no_autotune:
+        from bonsai_gb300 import autotune
+        tuning = autotune.tune(ctx, scene, pi, spp=2)
+        tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "ms")} | {
+            "cached": bool(tuning.get("cached", False))}
     for _ in range(args.warmup):
         pi.render(scene, readback=False)
     clocks = Clocks(local)
@@ -302,7 +309,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
-        "config": config_of(sd, args.small),
+        "config": config_of(sd, args.small) | {"tuning": tuning},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
                 "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
         "gpu_launches": launches,

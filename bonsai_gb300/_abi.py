@@ -33,6 +33,7 @@ BG_MAT_DIELECTRIC = 3
 BG_BVH_WIDE = 0
 BG_BVH_REFERENCE = 1
 BG_BVH_REFERENCE_FIXED = 2
+BG_BVH_WIDE2 = 3
 
 BG_RENDER_ACCUMULATE = 1
 BG_RENDER_NO_READBACK = 2
@@ -41,7 +42,7 @@ BG_RENDER_STAGE_TIMING = 8
 
 BG_NOALLOC_MAX_PIXELS = 512 * 512
 BG_NOALLOC_WAVE_PATHS = 65536
-BG_NOALLOC_SCRATCH_BYTES = 27788288
+BG_NOALLOC_SCRATCH_BYTES = 29099008
 
 F3 = C.c_float * 3
 
@@ -93,6 +94,11 @@ class bg_device_opts(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class bg_tuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
 class bg_build_stats(C.Structure):
     _fields_ = [("build_ms", C.c_double), ("nodes", C.c_uint64), ("prims", C.c_uint64),
                 ("device_bytes", C.c_uint64)]
@@ -129,6 +135,8 @@ SIGNATURES = {
     "bg_memcpy_h2d": (ST, [P, P, P, C.c_size_t]),
     "bg_memcpy_d2h": (ST, [P, P, P, C.c_size_t]),
     "bg_render_noalloc": (ST, [P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P, P]),
+    "bg_get_tuning": (ST, [P, C.POINTER(bg_tuning)]),
+    "bg_set_tuning": (ST, [P, C.POINTER(bg_tuning)]),
 }
 
 _LIB = None

@@ -1,0 +1,110 @@
+"""Autotuner for the wavefront launch parameters (bg_tuning).
+
+Tunes, by coordinate descent on short renders of the actual scene (device-timed with the
+library's CUDA events, L2 flushed before each trial):
+  refill        - traversal: lanes a warp lets go idle before it fetches new rays (32 = whole warp)
+  blocks_per_sm - persistent grid of the wavefront stages
+  wave_paths    - paths per wave (queue capacity)
+The result is cached as JSON keyed by GPU name, scene signature and render settings
+(default ~/.cache/bonsai_gb300/tuning.json, or $BONSAI_TUNING_CACHE).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from pathlib import Path
+
+from . import _abi as A
+
+REFILL = [32, 16, 8, 4]
+BLOCKS = [4, 8, 16]
+WAVES = [1 << 20, 1 << 21, 1 << 22, 1 << 23]
+
+
+def cache_path() -> Path:
+    p = os.environ.get("BONSAI_TUNING_CACHE")
+    return Path(p) if p else Path.home() / ".cache" / "bonsai_gb300" / "tuning.json"
+
+
+def _gpu_name() -> str:
+    try:
+        import subprocess
+        return subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                              capture_output=True, text=True, timeout=10).stdout.strip() or "unknown"
+    except Exception:
+        return "unknown"
+
+
+def key_of(sd, spp: int) -> str:
+    c = sd.camera
+    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}"
+
+
+def get(ctx) -> A.bg_tuning:
+    t = A.bg_tuning()
+    ctx.check(ctx.lib.bg_get_tuning(ctx.h, C.byref(t)))
+    return t
+
+
+def set_(ctx, refill: int, blocks: int, wave: int):
+    t = A.bg_tuning()
+    t.refill, t.blocks_per_sm, t.wave_paths = refill, blocks, wave
+    ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
+
+
+def _trial(ctx, scene, integrator, spp: int, reps: int = 2) -> float:
+    best = float("inf")
+    for _ in range(reps):
+        ctx.flush_l2()
+        r = integrator.render(scene, readback=False, spp=spp)
+        best = min(best, r.stats.device_ms)
+    return best
+
+
+def tune(ctx, scene, integrator, spp: int = 2, use_cache: bool = True, verbose: bool = False) -> dict:
+    """Returns {"refill", "blocks_per_sm", "wave_paths", "ms", "trials"} and applies it to ctx."""
+    sd = scene.sd
+    key = key_of(sd, spp)
+    path = cache_path()
+    cache = {}
+    if use_cache and path.exists():
+        try:
+            cache = json.loads(path.read_text())
+        except ValueError:
+            cache = {}
+    if use_cache and key in cache:
+        c = cache[key]
+        set_(ctx, c["refill"], c["blocks_per_sm"], c["wave_paths"])
+        return dict(c, cached=True)
+    cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22}
+    trials = []
+
+    def run(cfg):
+        set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"])
+        integrator.render(scene, readback=False, spp=1)  # allocate / warm
+        ms = _trial(ctx, scene, integrator, spp)
+        trials.append(dict(cfg, ms=ms))
+        if verbose:
+            print("autotune", cfg, f"{ms:.2f} ms")
+        return ms
+
+    best_ms = run(cur)
+    for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES)):
+        for v in values:
+            if v == cur[name]:
+                continue
+            cfg = dict(cur, **{name: v})
+            ms = run(cfg)
+            if ms < best_ms:
+                best_ms, cur = ms, cfg
+    set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"])
+    result = dict(cur, ms=best_ms, trials=trials)
+    if use_cache:
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            cache[key] = {k: result[k] for k in ("refill", "blocks_per_sm", "wave_paths", "ms")}
+            path.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    return result

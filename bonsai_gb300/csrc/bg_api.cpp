@@ -320,6 +320,7 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(sh_ref, 2 * n * sizeof(uint32_t));
     WB(queue[0], n * sizeof(uint32_t));
     WB(queue[1], n * sizeof(uint32_t));
+    WB(cls_queue, 5 * n * sizeof(uint32_t));
     WB(done, n * sizeof(uint32_t));
     WB(counters, 16 * sizeof(uint32_t));
     WB(ray_stats, 4 * sizeof(unsigned long long));
@@ -488,6 +489,26 @@ bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h, const void* d, size_t bytes) {
     return BG_OK;
 }
 
+bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
+    if (!ctx || !out) return BG_ERR_INVALID;
+    out->wave_paths = ctx->max_queue;
+    out->blocks_per_sm = (uint32_t)ctx->shape.blocks_per_sm;
+    out->refill = (uint32_t)ctx->shape.refill;
+    out->reserved = 0;
+    return BG_OK;
+}
+
+bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
+    if (!ctx || !t) return BG_ERR_INVALID;
+    if (t->wave_paths < 1024 || t->wave_paths > (1u << 26)) return fail(ctx, BG_ERR_INVALID, "wave_paths out of range");
+    if (t->blocks_per_sm < 1 || t->blocks_per_sm > 64) return fail(ctx, BG_ERR_INVALID, "blocks_per_sm out of range");
+    if (t->refill < 1 || t->refill > 32) return fail(ctx, BG_ERR_INVALID, "refill must be in 1..32");
+    ctx->max_queue = t->wave_paths;
+    ctx->shape.blocks_per_sm = (int)t->blocks_per_sm;
+    ctx->shape.refill = (int)t->refill;
+    return BG_OK;
+}
+
 // ---------------------------------------------------------------- scene
 bg_status bg_scene_create(bg_ctx* ctx, bg_scene** out) {
     if (!ctx || !out) return BG_ERR_INVALID;
@@ -571,7 +592,7 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if (!s->ctx) return BG_ERR_INVALID;
     bg_ctx* ctx = s->ctx;
     if (s->committed) return fail(ctx, BG_ERR_INVALID, "scene already committed");
-    if (kind > BG_BVH_REFERENCE_FIXED) return fail(ctx, BG_ERR_INVALID, "unknown BVH kind");
+    if (kind > BG_BVH_WIDE2) return fail(ctx, BG_ERR_INVALID, "unknown BVH kind");
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaSetDevice(ctx->device));
     const uint32_t ntri = (uint32_t)s->tri_mat.size(), nsph = (uint32_t)s->sph.size();
@@ -637,6 +658,13 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if ((st = upload(ctx, light_prims, &d.light_prims, &s->allocs)) != BG_OK) return st;
     uint64_t nodes = 0;
     if (kind == BG_BVH_WIDE) {
+        bg::Bvh8 b;
+        bg::build_bvh8(hp, &b);
+        if ((st = upload(ctx, b.nodes, &d.nodes8, &s->allocs)) != BG_OK) return st;
+        if ((st = upload(ctx, b.leaf_prims, &d.leaf_prims, &s->allocs)) != BG_OK) return st;
+        d.n_nodes8 = (uint32_t)b.nodes.size();
+        nodes = b.nodes.size();
+    } else if (kind == BG_BVH_WIDE2) {
         bg::Bvh2 b;
         bg::build_bvh2(hp, &b, 0);
         if ((st = upload(ctx, b.nodes, (const bg::Bvh2Node**)&d.nodes, &s->allocs)) != BG_OK) return st;
@@ -661,8 +689,10 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         stats->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->nodes = nodes;
         stats->prims = (uint64_t)ntri + nsph;
-        uint64_t bytes = tri4.size() * 16 + sph4.size() * 16 + nodes * (kind == BG_BVH_WIDE ? 64 : 32) +
-                ((uint64_t)ntri + nsph) * (kind == BG_BVH_WIDE ? 48 : 4);
+        const bool wide = kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2;
+        uint64_t bytes = tri4.size() * 16 + sph4.size() * 16 +
+                         nodes * (kind == BG_BVH_WIDE ? 80 : (kind == BG_BVH_WIDE2 ? 64 : 32)) +
+                         ((uint64_t)ntri + nsph) * (wide ? 48 : 4);
         stats->device_bytes = bytes;
     }
     return BG_OK;
@@ -679,7 +709,8 @@ static bg_status trace_device(bg_ctx* ctx, const bg_scene* s, const bg_ray* d_ra
         return BG_OK;
     }
     CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
-    bg::launch_trace(s->dev, s->kind != BG_BVH_WIDE, any, d_rays, n, d_hits, d_occ, ctx->d_err, nullptr, ctx->d_head,
+    const bool ref_layout = s->kind == BG_BVH_REFERENCE || s->kind == BG_BVH_REFERENCE_FIXED;
+    bg::launch_trace(s->dev, ref_layout, any, d_rays, n, d_hits, d_occ, ctx->d_err, nullptr, ctx->d_head,
                      ctx->shape, ctx->stream);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev_end, ctx->stream));
@@ -741,7 +772,7 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     if (cam->lens_radius != 0.0f) return fail(ctx, BG_ERR_UNSUPPORTED, "thin-lens cameras are not supported");
     if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) return fail(ctx, BG_ERR_INVALID, "fov out of range");
     if (o->mode > BG_MODE_PBRT) return fail(ctx, BG_ERR_INVALID, "unknown mode");
-    if (o->mode == BG_MODE_REF_COMPAT && s->kind == BG_BVH_WIDE)
+    if (o->mode == BG_MODE_REF_COMPAT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2))
         return fail(ctx, BG_ERR_INVALID, "REF_COMPAT rendering needs a BG_BVH_REFERENCE* scene layout");
     if (o->max_depth > 250) return fail(ctx, BG_ERR_INVALID, "max_depth must be <= 250");
     if (!(o->flags & BG_RENDER_NO_READBACK) && !rgb_out) return BG_ERR_INVALID;
@@ -757,7 +788,7 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     const uint64_t npix = (uint64_t)cam->width * cam->height;
     const uint64_t total = npix * o->spp;
     uint64_t launches = 0;
-    bool wavefront = (o->mode == BG_MODE_PBRT && s->kind == BG_BVH_WIDE);
+    bool wavefront = (o->mode == BG_MODE_PBRT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2));
     uint32_t cap = 0;
     if (wavefront) {
         cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, std::max<uint64_t>(total, 1));

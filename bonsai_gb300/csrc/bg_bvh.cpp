@@ -235,10 +235,9 @@ struct BNode {
     uint32_t first = 0, count = 0;
 };
 constexpr int NBINS = 32;
-constexpr uint32_t MAX_LEAF = 8;
 constexpr float C_TRAV = 1.2f;
 
-std::unique_ptr<BNode> build_rec(Ref2* refs, uint32_t begin, uint32_t end, int depth) {
+std::unique_ptr<BNode> build_rec(Ref2* refs, uint32_t begin, uint32_t end, int depth, uint32_t MAX_LEAF) {
     auto node = std::make_unique<BNode>();
     Box cb;
     for (uint32_t i = begin; i < end; ++i) {
@@ -319,14 +318,35 @@ std::unique_ptr<BNode> build_rec(Ref2* refs, uint32_t begin, uint32_t end, int d
         if (mid == begin || mid == end) mid = begin + n / 2;
     }
     if (n > 65536 && depth < 5) {
-        auto fut = std::async(std::launch::async, build_rec, refs, mid, end, depth + 1);
-        node->l = build_rec(refs, begin, mid, depth + 1);
+        auto fut = std::async(std::launch::async, build_rec, refs, mid, end, depth + 1, MAX_LEAF);
+        node->l = build_rec(refs, begin, mid, depth + 1, MAX_LEAF);
         node->r = fut.get();
     } else {
-        node->l = build_rec(refs, begin, mid, depth + 1);
-        node->r = build_rec(refs, mid, end, depth + 1);
+        node->l = build_rec(refs, begin, mid, depth + 1, MAX_LEAF);
+        node->r = build_rec(refs, mid, end, depth + 1, MAX_LEAF);
     }
     return node;
+}
+
+void emit_prim(const HostPrims& p, uint32_t id, std::vector<float4>* out) {
+    float4 a, b, c;
+    if (id < p.ntri) {
+        const float* v = p.tri + 9 * (size_t)id;
+        a.x = v[0]; a.y = v[1]; a.z = v[2];
+        std::memcpy(&a.w, &id, 4);
+        b.x = v[3]; b.y = v[4]; b.z = v[5]; b.w = 0.0f;
+        c.x = v[6]; c.y = v[7]; c.z = v[8]; c.w = 0.0f;
+    } else {
+        const bg_sphere& s = p.sph[id - p.ntri];
+        a.x = s.center[0]; a.y = s.center[1]; a.z = s.center[2];
+        uint32_t idbits = (id - p.ntri) | SPHERE_BIT;
+        std::memcpy(&a.w, &idbits, 4);
+        b.x = s.radius; b.y = 0.0f; b.z = 0.0f; b.w = 0.0f;
+        c.x = c.y = c.z = c.w = 0.0f;
+    }
+    out->push_back(a);
+    out->push_back(b);
+    out->push_back(c);
 }
 
 struct Flattener {
@@ -405,7 +425,7 @@ void build_bvh2(const HostPrims& p, Bvh2* out, int /*threads*/) {
         }
         refs[i].id = i;
     }
-    std::unique_ptr<BNode> root = build_rec(refs.data(), 0, n, 0);
+    std::unique_ptr<BNode> root = build_rec(refs.data(), 0, n, 0, 8);
     out->nodes.reserve(2 * n / 3 + 2);
     out->leaf_prims.reserve(3 * (size_t)n);
     Flattener fl{p, refs.data(), out};
@@ -423,6 +443,155 @@ void build_bvh2(const HostPrims& p, Bvh2* out, int /*threads*/) {
     } else {
         fl.emit(root.get());
     }
+}
+
+}  // namespace bg
+
+// ================================================================ 8-wide compressed BVH
+namespace bg {
+
+namespace {
+
+struct Wide {
+    const BNode* bin;  // binary node whose subtree this wide node covers
+    uint32_t index;
+};
+
+// Quantisation exponent of one axis: the smallest e with extent / 2^e <= 255.
+int axis_exponent(double extent) {
+    if (!(extent > 0.0)) return -100;
+    int e = (int)std::ceil(std::log2(extent / 255.0));
+    while (extent / std::ldexp(1.0, e) > 255.0) ++e;
+    if (e < -100) e = -100;
+    if (e > 100) e = 100;
+    return e;
+}
+
+}  // namespace
+
+void build_bvh8(const HostPrims& p, Bvh8* out) {
+    out->nodes.clear();
+    out->leaf_prims.clear();
+    const uint32_t n = p.ntri + p.nsph;
+    if (n == 0) return;
+    std::vector<Ref2> refs(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        Box b = prim_box(p, i);
+        for (int k = 0; k < 3; ++k) {
+            refs[i].lo[k] = b.lo[k];
+            refs[i].hi[k] = b.hi[k];
+            refs[i].c[k] = 0.5f * (b.lo[k] + b.hi[k]);
+        }
+        refs[i].id = i;
+    }
+    std::unique_ptr<BNode> root = build_rec(refs.data(), 0, n, 0, 3);
+    out->nodes.reserve(n / 4 + 2);
+    out->leaf_prims.reserve(3 * (size_t)n);
+    out->nodes.push_back(Bvh8Node{});
+    std::vector<Wide> queue{{root.get(), 0}};
+    for (size_t qi = 0; qi < queue.size(); ++qi) {
+        const BNode* b = queue[qi].bin;
+        const uint32_t idx = queue[qi].index;
+        // children: open the largest-area internal child until there are 8
+        std::vector<const BNode*> ch;
+        if (b->count > 0) ch.push_back(b);
+        else {
+            ch.push_back(b->l.get());
+            ch.push_back(b->r.get());
+            while (ch.size() < 8) {
+                int best = -1;
+                float best_area = -1.0f;
+                for (size_t i = 0; i < ch.size(); ++i)
+                    if (ch[i]->count == 0 && ch[i]->box.area() > best_area) {
+                        best_area = ch[i]->box.area();
+                        best = (int)i;
+                    }
+                if (best < 0) break;
+                const BNode* c = ch[best];
+                ch[best] = c->l.get();
+                ch.push_back(c->r.get());
+            }
+        }
+        Box nb;
+        for (const BNode* c : ch) nb.grow(c->box);
+        // octant slot assignment: slot s takes a child that comes first along direction d_s
+        // (components negative where bits 2,1,0 of s are set), greedy on cost = <c - c_parent, d_s>
+        double pc[3];
+        for (int k = 0; k < 3; ++k) pc[k] = 0.5 * ((double)nb.lo[k] + nb.hi[k]);
+        double cost[8][8];
+        for (size_t i = 0; i < ch.size(); ++i) {
+            double cc[3];
+            for (int k = 0; k < 3; ++k) cc[k] = 0.5 * ((double)ch[i]->box.lo[k] + ch[i]->box.hi[k]) - pc[k];
+            for (int sl = 0; sl < 8; ++sl) {
+                double d[3] = {(sl & 4) ? -1.0 : 1.0, (sl & 2) ? -1.0 : 1.0, (sl & 1) ? -1.0 : 1.0};
+                cost[i][sl] = cc[0] * d[0] + cc[1] * d[1] + cc[2] * d[2];
+            }
+        }
+        int slot_child[8];
+        for (int& v : slot_child) v = -1;
+        std::vector<bool> assigned(ch.size(), false);
+        for (size_t round = 0; round < ch.size(); ++round) {
+            double best = 1e300;
+            int bi = -1, bs = -1;
+            for (size_t i = 0; i < ch.size(); ++i) {
+                if (assigned[i]) continue;
+                for (int sl = 0; sl < 8; ++sl)
+                    if (slot_child[sl] < 0 && cost[i][sl] < best) {
+                        best = cost[i][sl];
+                        bi = (int)i;
+                        bs = sl;
+                    }
+            }
+            assigned[bi] = true;
+            slot_child[bs] = bi;
+        }
+        Bvh8Node nd{};
+        int ex[3];
+        for (int k = 0; k < 3; ++k) {
+            nd.p[k] = nb.lo[k];
+            ex[k] = axis_exponent((double)nb.hi[k] - (double)nb.lo[k]);
+            nd.e[k] = (uint8_t)(ex[k] + 127);
+        }
+        // internal children first (contiguous, slot order), then leaf primitives (slot order)
+        uint32_t nint = 0;
+        for (int sl = 0; sl < 8; ++sl)
+            if (slot_child[sl] >= 0 && ch[slot_child[sl]]->count == 0) ++nint;
+        nd.child_base = (uint32_t)(queue.size());
+        nd.tri_base = (uint32_t)(out->leaf_prims.size() / 3);
+        uint32_t tri_off = 0, int_k = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            int ci = slot_child[sl];
+            if (ci < 0) continue;
+            const BNode* c = ch[ci];
+            for (int k = 0; k < 3; ++k) {
+                double sc = std::ldexp(1.0, ex[k]);
+                double lo = std::floor(((double)c->box.lo[k] - (double)nd.p[k]) / sc);
+                double hi = std::ceil(((double)c->box.hi[k] - (double)nd.p[k]) / sc);
+                uint8_t qlo = (uint8_t)std::min(255.0, std::max(0.0, lo));
+                uint8_t qhi = (uint8_t)std::min(255.0, std::max(0.0, hi));
+                uint8_t* dlo = k == 0 ? nd.qlo_x : (k == 1 ? nd.qlo_y : nd.qlo_z);
+                uint8_t* dhi = k == 0 ? nd.qhi_x : (k == 1 ? nd.qhi_y : nd.qhi_z);
+                dlo[sl] = qlo;
+                dhi[sl] = qhi;
+            }
+            if (c->count == 0) {
+                nd.imask |= (uint8_t)(1u << sl);
+                nd.meta[sl] = (uint8_t)((1u << 5) | (24u + (uint32_t)sl));
+                queue.push_back({c, nd.child_base + int_k});
+                ++int_k;
+            } else {
+                uint32_t cnt = c->count;  // 1..3
+                static const uint8_t unary[4] = {0, 1, 3, 7};
+                nd.meta[sl] = (uint8_t)((unary[cnt] << 5) | tri_off);
+                for (uint32_t t = 0; t < cnt; ++t) emit_prim(p, refs[c->first + t].id, &out->leaf_prims);
+                tri_off += cnt;
+            }
+        }
+        (void)nint;
+        if (out->nodes.size() < queue.size()) out->nodes.resize(queue.size());
+        out->nodes[idx] = nd;
+    }
+    out->nodes.resize(queue.size());
 }
 
 }  // namespace bg

@@ -32,4 +32,13 @@ struct Bvh2 {
 };
 void build_bvh2(const HostPrims& p, Bvh2* out, int threads);
 
+// 8-wide compressed BVH: binary SAH BVH with leaves of at most 3 primitives, collapsed greedily
+// (the largest-area internal child is opened until 8 children), child slots assigned by octant,
+// boxes quantised to 8 bits (conservative floor / ceil).
+struct Bvh8 {
+    std::vector<Bvh8Node> nodes;
+    std::vector<float4> leaf_prims;  // 3 per primitive, node-contiguous
+};
+void build_bvh8(const HostPrims& p, Bvh8* out);
+
 }  // namespace bg

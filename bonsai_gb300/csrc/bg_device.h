@@ -49,6 +49,24 @@ struct Bvh2Node {
     int4 child;    // x,y: >=0 inner node; <0: ~first leaf prim; z,w: leaf prim counts
 };
 
+// 8-wide compressed node (Ylitie, Karras, Laine, HPG 2017): 80 B, read as five 128-bit loads.
+// Child boxes are 8-bit offsets on a per-node grid: lo = p + 2^(e-127) * qlo, hi = p + 2^(e-127) * qhi.
+// meta[s]: 0 = empty slot; internal child = 0b001_11sss (24 + s); leaf = unary triangle count in the
+// top 3 bits (001, 011, 111) and the first triangle's offset from tri_base in the low 5 bits.
+// Internal children are stored contiguously from child_base in slot order; slots are assigned so
+// that a ray in direction octant o reaches slot o's child first.
+struct Bvh8Node {
+    float p[3];
+    uint8_t e[3];
+    uint8_t imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
+    uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
+};
+static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node must be 80 bytes");
+
 struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-175)
     float r2c[4][4];  // raster_to_camera.m
     float c2w[4][4];  // camera_to_world.m
@@ -71,7 +89,10 @@ struct Scene {
     uint32_t ref_nnodes;
     uint32_t n_nodes;
     const Bvh2Node* nodes;
-    const float4* leaf_prims;
+    const float4* leaf_prims;   // leaf order of whichever wide layout is built
+    const Bvh8Node* nodes8;
+    uint32_t n_nodes8;
+    uint32_t pad1;
 };
 
 enum : uint32_t {

@@ -64,9 +64,32 @@ BG_D void film_add(const FilmBuffers& f, uint32_t pix, RGB L) {
 }
 
 // ================================================================ ray queries
-template <bool REF_LAYOUT, bool ANY>
+struct TraceSrc {
+    const float4* rays;
+    int2* hits;
+    uint8_t* occ;
+    BG_D Ray load(uint32_t i, int* skip) const {
+        Ray r = load_ray(__ldg(&rays[2 * i]), __ldg(&rays[2 * i + 1]));
+        r.time = 0.0f;
+        *skip = -1;
+        return r;
+    }
+    BG_D void store(uint32_t i, int prim, float t) const {
+        if (occ) occ[i] = prim >= 0 ? 1 : 0;
+        else hits[i] = make_int2(prim, __float_as_int(prim >= 0 ? t : INFINITY));
+    }
+};
+
+// LAYOUT: 1 = reference binary layout, 2 = 2-wide, 8 = 8-wide compressed.
+template <int LAYOUT, bool ANY>
 __global__ void __launch_bounds__(128) k_trace(Scene sc, const float4* rays, uint32_t n, int2* hits, uint8_t* occ,
-                                               uint32_t* err, unsigned long long* counters, uint32_t* head) {
+                                               uint32_t* err, unsigned long long* counters, uint32_t* head, int refill) {
+    if (LAYOUT != 1) {
+        TraceSrc src{rays, hits, ANY ? occ : nullptr};
+        if (LAYOUT == 8) traverse_queue8<ANY>(sc, n, head, src, err, refill);
+        else traverse_queue<ANY>(sc, n, head, src, err, refill);
+        return;
+    }
     for (;;) {
         uint32_t base = warp_fetch(head);
         if (base >= n) break;
@@ -74,7 +97,7 @@ __global__ void __launch_bounds__(128) k_trace(Scene sc, const float4* rays, uin
         if (i < n) {
             Ray ray = load_ray(__ldg(&rays[2 * i]), __ldg(&rays[2 * i + 1]));
             ray.time = 0.0f;
-            int prim = REF_LAYOUT ? ref_traverse<ANY>(sc, ray, err, counters) : bvh2_traverse<ANY>(sc, ray, err);
+            int prim = ref_traverse<ANY>(sc, ray, err, counters);
             if (ANY) occ[i] = prim >= 0 ? 1 : 0;
             else hits[i] = make_int2(prim, __float_as_int(prim >= 0 ? ray.t_max : INFINITY));
         }
@@ -85,17 +108,23 @@ void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays
                   uint8_t* occluded, uint32_t* err, unsigned long long* counters, uint32_t* work_head,
                   const LaunchShape& ls, cudaStream_t s) {
     cudaMemsetAsync(work_head, 0, sizeof(uint32_t), s);
-    dim3 grid(ls.sms * 8), block(128);
+    dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     const float4* r = reinterpret_cast<const float4*>(rays);
     int2* h = reinterpret_cast<int2*>(hits);
     uint32_t nn = (uint32_t)n;
-    if (ref_layout) {
-        if (any) k_trace<true, true><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
-        else k_trace<true, false><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+    const int layout = ref_layout ? 1 : (sc.nodes8 ? 8 : 2);
+#define BG_TRACE(L, A) k_trace<L, A><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head, ls.refill)
+    if (layout == 1) {
+        if (any) BG_TRACE(1, true);
+        else BG_TRACE(1, false);
+    } else if (layout == 2) {
+        if (any) BG_TRACE(2, true);
+        else BG_TRACE(2, false);
     } else {
-        if (any) k_trace<false, true><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
-        else k_trace<false, false><<<grid, block, 0, s>>>(sc, r, nn, h, occluded, err, counters, work_head);
+        if (any) BG_TRACE(8, true);
+        else BG_TRACE(8, false);
     }
+#undef BG_TRACE
 }
 
 // ================================================================ megakernel (reference layout)
@@ -224,7 +253,9 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 
 // ================================================================ wavefront (PBRT, 2-wide BVH)
 enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9 };
-enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5 };
+enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6 };
+constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
+constexpr int CLS_MISS = 4;
 
 __global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
     const uint64_t npix = (uint64_t)rp.width * rp.height;
@@ -256,22 +287,50 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
         wb.counters[C_DONE] = 0;
         wb.counters[C_EXT_HEAD] = 0;
         wb.counters[C_SH_HEAD] = 0;
+        for (int c = 0; c < NCLS; ++c) wb.counters[C_CLS + c] = 0;
     }
 }
 
-__global__ void __launch_bounds__(128) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err) {
+struct ExtendSrc {
+    const uint32_t* q;
+    WaveBuffers wb;
+    BG_D Ray load(uint32_t i, int* skip) const {
+        uint32_t slot = q[i];
+        *skip = -1;
+        return load_ray(wb.ray_o[slot], wb.ray_d[slot]);
+    }
+    BG_D void store(uint32_t i, int prim, float t) const { wb.hit[q[i]] = make_int2(prim, __float_as_int(t)); }
+};
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(128) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err,
+                                                int refill) {
+    const uint32_t n = wb.counters[bounce & 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
+    ExtendSrc src{wb.queue[bounce & 1], wb};
+    if (LAYOUT == 8) traverse_queue8<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
+    else traverse_queue<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
+}
+
+// Material-key binning of this bounce's hits: one queue per material class plus misses, so each
+// shade launch runs one material's code with uniform control flow.
+__global__ void __launch_bounds__(128) k_bin(Scene sc, WaveBuffers wb, uint32_t bounce) {
     const uint32_t n = wb.counters[bounce & 1];
     const uint32_t* q = wb.queue[bounce & 1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
-    for (;;) {
-        uint32_t base = warp_fetch(&wb.counters[C_EXT_HEAD]);
-        if (base >= n) break;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
         uint32_t i = base + lane_id();
+        int cls = -1;
+        uint32_t slot = 0;
         if (i < n) {
-            uint32_t slot = q[i];
-            Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
-            int prim = bvh2_traverse<false>(sc, ray, err);
-            wb.hit[slot] = make_int2(prim, __float_as_int(ray.t_max));
+            slot = q[i];
+            int prim = wb.hit[slot].x;
+            cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
+        }
+#pragma unroll
+        for (int c = 0; c < NCLS; ++c) {
+            uint32_t pos = warp_append(&wb.counters[C_CLS + c], cls == c);
+            if (cls == c) wb.cls_queue[(size_t)c * wb.capacity + pos] = slot;
         }
     }
 }
@@ -289,10 +348,12 @@ BG_D RGB apply_pending(const WaveBuffers& wb, uint32_t slot, RGB L, uint32_t sta
     return L + rgb(nb.x, nb.y, nb.z) * (ld / light_pdf);
 }
 
+// Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
+template <int CLS>
 __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
                                                uint32_t bounce, uint32_t* err) {
-    const uint32_t n = wb.counters[bounce & 1];
-    const uint32_t* q = wb.queue[bounce & 1];
+    const uint32_t n = wb.counters[C_CLS + CLS];
+    const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     uint32_t* qn = wb.queue[(bounce + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
     // warp-uniform loop so the ballots below see all 32 lanes
@@ -316,7 +377,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
             state &= ~ST_PENDING;
             bool specular_bounce = (state & ST_SPECULAR) != 0;
             Isect it;
-            bool hit = prim >= 0 && prim_isect(sc, prim, ray, &it);
+            bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
             if (bounce == 0 || specular_bounce) {
                 if (hit) L = L + beta * emitted_radiance(sc, it, -ray.d);
             }
@@ -327,7 +388,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
                 float u[8];
                 rng.block(ub, u);
                 rng.block(ub + 4, u + 4);
-                BSDF bsdf = make_bsdf(sc, it);
+                BSDF bsdf = make_bsdf<CLS>(sc, it);
                 if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
                     // uniform_sample_one_light + estimate_direct, occlusion deferred to k_shadow
                     const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
@@ -433,24 +494,30 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
     }
 }
 
-__global__ void __launch_bounds__(128) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err) {
+struct ShadowSrc {
+    WaveBuffers wb;
+    BG_D Ray load(uint32_t i, int* skip) const {
+        float4 o = wb.sh_o[i], d = wb.sh_d[i];
+        Ray ray;
+        ray.o = f4xyz(o);
+        ray.t_max = o.w;
+        ray.d = f4xyz(d);
+        ray.time = 0.0f;
+        *skip = __float_as_int(d.w);
+        return ray;
+    }
+    BG_D void store(uint32_t i, int prim, float) const {
+        if (prim < 0) wb.pending[wb.sh_ref[i]].w = 1.0f;
+    }
+};
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(128) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err, int refill) {
     const uint32_t n = min(wb.counters[C_SHADOW], 2 * wb.capacity);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[1], (unsigned long long)n);
-    for (;;) {
-        uint32_t base = warp_fetch(&wb.counters[C_SH_HEAD]);
-        if (base >= n) break;
-        uint32_t i = base + lane_id();
-        if (i < n) {
-            float4 o = wb.sh_o[i], d = wb.sh_d[i];
-            Ray ray;
-            ray.o = f4xyz(o);
-            ray.t_max = o.w;
-            ray.d = f4xyz(d);
-            ray.time = 0.0f;
-            int skip = __float_as_int(d.w);
-            if (bvh2_traverse<true>(sc, ray, err, skip) < 0) wb.pending[wb.sh_ref[i]].w = 1.0f;
-        }
-    }
+    ShadowSrc src{wb};
+    if (LAYOUT == 8) traverse_queue8<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
+    else traverse_queue<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
 }
 
 __global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, WaveBuffers wb) {
@@ -467,20 +534,27 @@ int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, cons
                 const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
                 cudaStream_t s, cudaEvent_t* ev) {
     int launches = 0;
-    dim3 grid(ls.sms * 8), block(128);
+    dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
     ++launches;
     for (uint32_t b = 0; b <= rp.max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 0], s);
-        k_extend<<<grid, block, 0, s>>>(sc, wb, b, err);
+        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill);
+        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill);
+        k_bin<<<grid, block, 0, s>>>(sc, wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        k_shade<<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
-        k_shadow<<<grid, block, 0, s>>>(sc, wb, err);
+        if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
+        else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
         k_finalize<<<grid, block, 0, s>>>(sc, film, wb);
-        launches += 5;
+        launches += 10;
     }
     return launches;
 }

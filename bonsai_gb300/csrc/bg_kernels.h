@@ -41,14 +41,19 @@ struct WaveBuffers {
     float4* sh_d;       // d.xyz, skip prim (int bits)
     uint32_t* sh_ref;   // slot * 2 + kind
     uint32_t* queue[2];
+    uint32_t* cls_queue;  // 5 * capacity: hits binned by material class (matte, plastic, conductor,
+                          // dielectric) and misses, written by extend, read by the class's shade launch
     uint32_t* done;
-    uint32_t* counters; // [0,1] queue sizes, [2] shadow count, [3] done count, [4] extend head, [5] shadow head
+    uint32_t* counters; // [0,1] queue sizes, [2] shadow count, [3] done count, [4] extend head,
+                        // [5] shadow head, [6..10] class queue sizes
     unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
 };
 
 struct LaunchShape {
     int sms;
     int block;
+    int blocks_per_sm = 8;
+    int refill = 32;
 };
 
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,

@@ -61,7 +61,8 @@ constexpr size_t OFF_SH_D = OFF_SH_O + align_up(2 * N * sizeof(float4));
 constexpr size_t OFF_SH_REF = OFF_SH_D + align_up(2 * N * sizeof(float4));
 constexpr size_t OFF_Q0 = OFF_SH_REF + align_up(2 * N * sizeof(uint32_t));
 constexpr size_t OFF_Q1 = OFF_Q0 + align_up(N * sizeof(uint32_t));
-constexpr size_t OFF_DONE = OFF_Q1 + align_up(N * sizeof(uint32_t));
+constexpr size_t OFF_CLS = OFF_Q1 + align_up(N * sizeof(uint32_t));
+constexpr size_t OFF_DONE = OFF_CLS + align_up(5 * N * sizeof(uint32_t));
 constexpr size_t SCRATCH_BYTES = OFF_DONE + align_up(N * sizeof(uint32_t));
 static_assert(SCRATCH_BYTES == BG_NOALLOC_SCRATCH_BYTES, "keep BG_NOALLOC_SCRATCH_BYTES in step");
 
@@ -115,7 +116,7 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     if (cam->lens_radius != 0.0f) return reject(BG_ERR_UNSUPPORTED, "thin-lens cameras are not supported");
     if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) return reject(BG_ERR_INVALID, "fov out of range");
     if (o->mode > BG_MODE_PBRT) return reject(BG_ERR_INVALID, "unknown mode");
-    if (o->mode == BG_MODE_REF_COMPAT && kind == BG_BVH_WIDE)
+    if (o->mode == BG_MODE_REF_COMPAT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2))
         return reject(BG_ERR_INVALID, "REF_COMPAT rendering needs a BG_BVH_REFERENCE* scene layout");
     if (o->max_depth > 250) return reject(BG_ERR_INVALID, "max_depth must be <= 250");
     if (o->flags & (BG_RENDER_ACCUMULATE | BG_RENDER_STAGE_TIMING | BG_RENDER_GRAPH))
@@ -160,6 +161,7 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     w.sh_ref = reinterpret_cast<uint32_t*>(base + OFF_SH_REF);
     w.queue[0] = reinterpret_cast<uint32_t*>(base + OFF_Q0);
     w.queue[1] = reinterpret_cast<uint32_t*>(base + OFF_Q1);
+    w.cls_queue = reinterpret_cast<uint32_t*>(base + OFF_CLS);
     w.done = reinterpret_cast<uint32_t*>(base + OFF_DONE);
     w.counters = reinterpret_cast<uint32_t*>(base + OFF_COUNTERS);
     w.ray_stats = reinterpret_cast<unsigned long long*>(base + OFF_RAYSTATS);
@@ -175,12 +177,12 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
 
     int dev_sms = 0;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
-    LaunchShape shape{dev_sms > 0 ? dev_sms : 1, 128};
+    LaunchShape shape{dev_sms > 0 ? dev_sms : 1, 128, 8, 32};
     Camera dc = camera_for(*cam);
     RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
     const uint64_t total = npix * o->spp;
     if (total > 0) {
-        if (o->mode == BG_MODE_PBRT && kind == BG_BVH_WIDE) {
+        if (o->mode == BG_MODE_PBRT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2)) {
             for (uint64_t item0 = 0; item0 < total; item0 += N) {
                 uint32_t nitems = (uint32_t)((total - item0) < N ? (total - item0) : N);
                 launch_wave(dev, dc, rp, film, w, item0, nitems, d_err, shape, s, nullptr);

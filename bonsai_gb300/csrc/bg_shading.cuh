@@ -276,14 +276,19 @@ BG_D BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1) {
     return s;
 }
 
-struct BSDF {  // src/base/bsdf.rs
+// BSDF (src/base/bsdf.rs) with at most two lobes in fixed slots: slot 0 holds the first BxDF the
+// material adds, slot 1 the second.  Loops run over both slots with compile-time indices (guarded
+// by n) so the lobes stay in registers; the iteration order is the reference's insertion order.
+struct BSDF {
     float eta;
     V3 ns, ng, ss, ts;
     Bxdf bx[2];
     int n;
     BG_D int num_components(uint8_t f) const {
         int k = 0;
-        for (int i = 0; i < n; ++i) k += bx[i].matches(f);
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+            if (i < n) k += bx[i].matches(f);
         return k;
     }
     BG_D V3 to_local(V3 v) const { return v3(dot(v, ss), dot(v, ts), dot(v, ns)); }
@@ -297,8 +302,9 @@ struct BSDF {  // src/base/bsdf.rs
         if (wo.z == 0.0f) return rgb(0.0f);
         bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
         RGB r = rgb(0.0f);
-        for (int i = 0; i < n; ++i)
-            if (bx[i].matches(flags) &&
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+            if (i < n && bx[i].matches(flags) &&
                 ((refl && (bx[i].type & BSDF_REFLECTION)) || (!refl && (bx[i].type & BSDF_TRANSMISSION))))
                 r = r + bx_f<REF>(bx[i], wo, wi);
         return r;
@@ -309,8 +315,9 @@ struct BSDF {  // src/base/bsdf.rs
         V3 wo = to_local(wo_w), wi = to_local(wi_w);
         if (wo.z == 0.0f) return 0.0f;
         float ret = 0.0f, comps = 0.0f;
-        for (int i = 0; i < n; ++i)
-            if (bx[i].matches(flags)) {
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+            if (i < n && bx[i].matches(flags)) {
                 comps += 1.0f;
                 ret += bx_pdf<REF>(bx[i], wo, wi);
             }
@@ -328,15 +335,15 @@ struct BSDF {  // src/base/bsdf.rs
         uint32_t comp = min((uint32_t)floorf(u0 * (float)matches), (uint32_t)matches - 1);
         uint32_t count = comp;
         int pick = -1;
-        for (int i = 0; i < n; ++i) {
-            if (bx[i].matches(type) && count == 0) {
-                pick = i;
-                break;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            if (pick < 0 && i < n) {
+                if (bx[i].matches(type) && count == 0) pick = i;
+                else if (REF || bx[i].matches(type)) count -= 1;  // F8
             }
-            if (REF || bx[i].matches(type)) count -= 1;  // F8
         }
         if (pick < 0) return zero;
-        const Bxdf& b = bx[pick];
+        const Bxdf b = pick == 0 ? bx[0] : bx[1];
         float ur0 = rmin(u0 * (float)matches - (float)comp, ONE_MINUS_EPSILON);
         V3 wo = to_local(wo_w);
         if (wo.z == 0.0f) return zero;
@@ -344,15 +351,18 @@ struct BSDF {  // src/base/bsdf.rs
         int stype = s.stype >= 0 ? s.stype : b.type;
         if (s.pdf == 0.0f) return zero;
         V3 wi_w = to_world(s.wi);
-        if (!(b.type & BSDF_SPECULAR) && matches > 1)
-            for (int i = 0; i < n; ++i)
-                if (i != pick && bx[i].matches(type)) s.pdf += bx_pdf<REF>(bx[i], wo, s.wi);
+        if (!(b.type & BSDF_SPECULAR) && matches > 1) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+                if (i < n && i != pick && bx[i].matches(type)) s.pdf += bx_pdf<REF>(bx[i], wo, s.wi);
+        }
         if (matches > 1) s.pdf /= (float)matches;
         if (!(b.type & BSDF_SPECULAR)) {
             bool refl = dot(wi_w, ng) * dot(wo_w, ng) > 0.0f;
             s.f = rgb(0.0f);
-            for (int i = 0; i < n; ++i)
-                if (bx[i].matches(type) &&
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+                if (i < n && bx[i].matches(type) &&
                     ((refl && (bx[i].type & BSDF_REFLECTION)) || (!refl && (bx[i].type & BSDF_TRANSMISSION))))
                     s.f = s.f + bx_f<REF>(bx[i], wo, s.wi);
         }
@@ -366,9 +376,13 @@ BG_D uint32_t prim_material(const Scene& sc, int prim) {
     return (uint32_t)prim < sc.ntri ? __float_as_uint(sc.tri[3 * prim].w) : sc.sph_mat[prim - sc.ntri];
 }
 
-// Material::compute_scattering_functions for the constant-texture materials.
+// Material::compute_scattering_functions for the constant-texture materials.  CLS is the
+// material type when the caller knows it (the wavefront shades one material class per launch),
+// -1 to read it from the record.
+template <int CLS = -1>
 BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
     const Material& m = sc.mats[prim_material(sc, it.prim)];
+    const uint32_t type = CLS >= 0 ? (uint32_t)CLS : m.type;
     BSDF b;
     b.eta = 1.0f;
     b.n = 0;
@@ -376,7 +390,7 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
     b.ng = it.n;
     b.ss = normalize(it.dpdu);
     b.ts = cross(b.ns, b.ss);
-    if (m.type == 0 || m.type == 1) {  // matte, plastic
+    if (type == 0 || type == 1) {  // matte, plastic
         RGB kd = rgb(rclamp(m.kd[0], 0.0f, INFINITY), rclamp(m.kd[1], 0.0f, INFINITY), rclamp(m.kd[2], 0.0f, INFINITY));
         if (!is_black(kd)) {
             Bxdf& l = b.bx[b.n++];
@@ -385,7 +399,7 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
             l.r = kd;
             l.conductor = false;
         }
-        if (m.type == 1) {
+        if (type == 1) {
             RGB ks = rgb(rclamp(m.ks[0], 0.0f, INFINITY), rclamp(m.ks[1], 0.0f, INFINITY), rclamp(m.ks[2], 0.0f, INFINITY));
             if (!is_black(ks)) {
                 Bxdf& g = b.bx[b.n++];
@@ -398,7 +412,7 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
                 g.et = 1.0f;
             }
         }
-    } else if (m.type == 2) {  // conductor
+    } else if (type == 2) {  // conductor
         Bxdf& g = b.bx[b.n++];
         g.kind = BX_MF_REFL;
         g.type = BSDF_REFLECTION | BSDF_GLOSSY;

@@ -232,4 +232,302 @@ BG_D int bvh2_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) 
     }
 }
 
+// ---------------------------------------------------------------- persistent traversal with ray
+// replacement.  Each warp keeps up to 32 rays in flight; after every traversal step (inner nodes
+// down to one leaf) lanes whose ray finished store the result, and once at least kRefill lanes are
+// idle the warp fetches that many new rays with one atomic (Aila & Laine, HPG 2009, dynamic
+// fetch).  refill = 32 fetches only when the whole warp is idle.  Src supplies rays and takes
+// results: Ray load(uint32_t i, int* skip), void store(uint32_t i, int prim, float t).
+template <bool ANY, class Src>
+BG_D void traverse_queue(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill) {
+    const uint32_t lane = threadIdx.x & 31u;
+    int stack[TRAVERSAL_STACK];
+    Ray ray;
+    FastRay f;
+    TriRay tr;
+    int sp = 0, node = -2, hit = -1, skip = -1, leaf_first = 0, leaf_count = 0;
+    uint32_t idx = 0;
+    bool busy = false, exhausted = false;
+    for (;;) {
+        // refill idle lanes
+        const unsigned idle = __ballot_sync(0xffffffffu, !busy && !exhausted);
+        const int nidle = __popc(idle);
+        if (nidle >= refill || (nidle > 0 && __ballot_sync(0xffffffffu, busy) == 0)) {
+            const uint32_t leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(head, (uint32_t)nidle);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!busy && !exhausted) {
+                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    idx = my;
+                    ray = src.load(my, &skip);
+                    f = make_fast_ray(ray);
+                    tr = make_tri_ray(ray);
+                    sp = 0;
+                    node = sc.n_nodes ? 0 : -2;
+                    hit = -1;
+                    leaf_count = 0;
+                    busy = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, busy) == 0) break;
+        if (busy) {
+            // inner nodes until a leaf is found or this subtree is missed
+            while (node >= 0) {
+                const Bvh2Node* nd = sc.nodes + node;
+                float4 a = __ldg(&nd->c0xy), b = __ldg(&nd->c1xy), c = __ldg(&nd->c01z);
+                int4 ch = __ldg(&nd->child);
+                float t0 = box_enter(a.x, a.y, a.z, a.w, c.x, c.y, f, ray.t_max);
+                float t1 = box_enter(b.x, b.y, b.z, b.w, c.z, c.w, f, ray.t_max);
+                bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+                if (!h0 && !h1) {
+                    node = -2;
+                    break;
+                }
+                int first = h0 ? ch.x : ch.y, cfirst = h0 ? ch.z : ch.w;
+                if (h0 && h1) {
+                    int second = ch.y, csecond = ch.w;
+                    if (t1 < t0) {
+                        first = ch.y;
+                        cfirst = ch.w;
+                        second = ch.x;
+                        csecond = ch.z;
+                    }
+                    if (sp + 2 > TRAVERSAL_STACK) {
+                        atomicOr(err, ERR_STACK_OVERFLOW);
+                        sp = 0;
+                        node = -2;
+                        break;
+                    }
+                    if (second < 0) stack[sp++] = csecond;
+                    stack[sp++] = second;
+                }
+                if (first < 0) {
+                    leaf_first = ~first;
+                    leaf_count = cfirst;
+                    node = -1;
+                } else {
+                    node = first;
+                }
+            }
+            bool done = false;
+            if (node == -1) {
+                for (int i = 0; i < leaf_count; ++i) {
+                    int prim;
+                    if (leaf_prim_hit(sc, (uint32_t)(leaf_first + i), tr, ray, !ANY, &prim)) {
+                        if (ANY && prim == skip) continue;
+                        hit = prim;
+                        if (ANY) {
+                            done = true;
+                            break;
+                        }
+                    }
+                }
+                leaf_count = 0;
+            }
+            if (!done) {
+                if (sp == 0) {
+                    done = true;
+                } else {
+                    int e = stack[--sp];
+                    if (e < 0) {
+                        leaf_first = ~e;
+                        leaf_count = stack[--sp];
+                        node = -1;
+                    } else {
+                        node = e;
+                    }
+                }
+            }
+            if (done) {
+                src.store(idx, hit, ray.t_max);
+                busy = false;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- 8-wide compressed layout
+// Traversal of Bvh8Node trees (Ylitie, Karras, Laine, HPG 2017): a node group (child_base,
+// hit bits) stays in registers; the upper 8 hit bits are internal children in octant order
+// (bit 24 + (slot ^ octinv)), so the highest bit is the nearest child for this ray's direction;
+// the lower 24 bits are leaf primitives relative to tri_base.  The stack holds node groups only.
+constexpr int STACK8 = 32;
+
+BG_D uint32_t sign_extend_bytes(uint32_t x) { return ((x & 0x80808080u) >> 7) * 0xFFu; }
+BG_D float byte_as_float(uint32_t w, int j) { return (float)((w >> (8 * j)) & 0xFFu); }
+
+struct Ray8 {
+    V3 o;
+    V3 idir;
+    uint32_t octinv4;
+    bool negx, negy, negz;
+};
+BG_D Ray8 make_ray8(const Ray& r) {
+    Ray8 q;
+    q.o = r.o;
+    q.idir = v3(1.0f / safe_dir(r.d.x), 1.0f / safe_dir(r.d.y), 1.0f / safe_dir(r.d.z));
+    q.negx = r.d.x < 0.0f;
+    q.negy = r.d.y < 0.0f;
+    q.negz = r.d.z < 0.0f;
+    uint32_t oct = (q.negx ? 4u : 0u) | (q.negy ? 2u : 0u) | (q.negz ? 1u : 0u);
+    q.octinv4 = (7u - oct) * 0x01010101u;
+    return q;
+}
+
+// Intersects the 8 child boxes of node `ni`; returns the node's hit mask in the group layout.
+BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_max, uint2* ngroup, uint2* tgroup) {
+    const float4* raw = reinterpret_cast<const float4*>(sc.nodes8 + ni);
+    const float4 n0 = __ldg(raw + 0), n1 = __ldg(raw + 1), n2 = __ldg(raw + 2), n3 = __ldg(raw + 3),
+                 n4 = __ldg(raw + 4);
+    const uint32_t ebits = __float_as_uint(n0.w);
+    const float sx = __uint_as_float((ebits & 0xFFu) << 23);
+    const float sy = __uint_as_float(((ebits >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((ebits >> 16) & 0xFFu) << 23);
+    const uint32_t imask = ebits >> 24;
+    const V3 aidir = v3(sx * r.idir.x, sy * r.idir.y, sz * r.idir.z);
+    const V3 aorig = v3((n0.x - r.o.x) * r.idir.x, (n0.y - r.o.y) * r.idir.y, (n0.z - r.o.z) * r.idir.z);
+    const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
+    const uint32_t qlx[2] = {__float_as_uint(n2.x), __float_as_uint(n2.y)};
+    const uint32_t qly[2] = {__float_as_uint(n2.z), __float_as_uint(n2.w)};
+    const uint32_t qlz[2] = {__float_as_uint(n3.x), __float_as_uint(n3.y)};
+    const uint32_t qhx[2] = {__float_as_uint(n3.z), __float_as_uint(n3.w)};
+    const uint32_t qhy[2] = {__float_as_uint(n4.x), __float_as_uint(n4.y)};
+    const uint32_t qhz[2] = {__float_as_uint(n4.z), __float_as_uint(n4.w)};
+    const float k = 1.0f + 2.0f * gamma(3.0f);
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const uint32_t m4 = meta[i];
+        const uint32_t is_inner4 = (m4 & (m4 << 1)) & 0x10101010u;
+        const uint32_t inner_mask4 = sign_extend_bytes(is_inner4 << 3);
+        const uint32_t bit_index4 = (m4 ^ (r.octinv4 & inner_mask4)) & 0x1F1F1F1Fu;
+        const uint32_t child_bits4 = (m4 >> 5) & 0x07070707u;
+        // near / far planes per axis by the sign of the direction
+        const uint32_t nx = r.negx ? qhx[i] : qlx[i], fx = r.negx ? qlx[i] : qhx[i];
+        const uint32_t ny = r.negy ? qhy[i] : qly[i], fy = r.negy ? qly[i] : qhy[i];
+        const uint32_t nz = r.negz ? qhz[i] : qlz[i], fz = r.negz ? qlz[i] : qhz[i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float tnx = fmaf(byte_as_float(nx, j), aidir.x, aorig.x);
+            const float tny = fmaf(byte_as_float(ny, j), aidir.y, aorig.y);
+            const float tnz = fmaf(byte_as_float(nz, j), aidir.z, aorig.z);
+            const float tfx = fmaf(byte_as_float(fx, j), aidir.x, aorig.x);
+            const float tfy = fmaf(byte_as_float(fy, j), aidir.y, aorig.y);
+            const float tfz = fmaf(byte_as_float(fz, j), aidir.z, aorig.z);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+            const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * k, t_max);
+            if (tn <= tf) {
+                const uint32_t cb = (child_bits4 >> (8 * j)) & 0xFFu;
+                const uint32_t bi = (bit_index4 >> (8 * j)) & 0xFFu;
+                hitmask |= cb << bi;
+            }
+        }
+    }
+    ngroup->x = __float_as_uint(n1.x);  // child_base
+    ngroup->y = (hitmask & 0xFF000000u) | imask;
+    tgroup->x = __float_as_uint(n1.y);  // tri_base
+    tgroup->y = hitmask & 0x00FFFFFFu;
+}
+
+// Persistent traversal of the 8-wide layout with in-warp ray replacement (see traverse_queue).
+template <bool ANY, class Src>
+BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint2 stack[STACK8];
+    Ray ray;
+    Ray8 r8;
+    TriRay tr;
+    uint2 ngroup = make_uint2(0, 0), tgroup = make_uint2(0, 0);
+    int sp = 0, hit = -1, skip = -1;
+    uint32_t idx = 0;
+    bool busy = false, exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !busy && !exhausted);
+        const int nidle = __popc(idle);
+        if (nidle >= refill || (nidle > 0 && __ballot_sync(0xffffffffu, busy) == 0)) {
+            const uint32_t leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(head, (uint32_t)nidle);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!busy && !exhausted) {
+                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    idx = my;
+                    ray = src.load(my, &skip);
+                    r8 = make_ray8(ray);
+                    tr = make_tri_ray(ray);
+                    sp = 0;
+                    hit = -1;
+                    ngroup = make_uint2(0, sc.n_nodes8 ? 0x80000000u : 0u);
+                    tgroup = make_uint2(0, 0);
+                    busy = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, busy) == 0) break;
+        if (!busy) continue;
+        bool done = false;
+        if (ngroup.y > 0x00FFFFFFu) {
+            const uint32_t hits = ngroup.y;
+            const uint32_t bit = 31u - __clz(hits);
+            ngroup.y &= ~(1u << bit);
+            if (ngroup.y > 0x00FFFFFFu) {
+                if (sp >= STACK8) {
+                    atomicOr(err, ERR_STACK_OVERFLOW);
+                    sp = 0;
+                    ngroup.y = 0;
+                } else {
+                    stack[sp++] = ngroup;
+                }
+            }
+            const uint32_t slot = (bit - 24u) ^ (r8.octinv4 & 0xFFu);
+            const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+            const uint32_t child = ngroup.x + rel;
+            if (child >= sc.n_nodes8) {
+                atomicOr(err, ERR_BAD_NODE);
+                sp = 0;
+                ngroup = make_uint2(0, 0);
+                tgroup = make_uint2(0, 0);
+            } else {
+                bvh8_node_hits(sc, child, r8, ray.t_max, &ngroup, &tgroup);
+            }
+        } else {
+            tgroup = ngroup;
+            ngroup = make_uint2(0, 0);
+        }
+        while (tgroup.y != 0) {
+            const uint32_t bit = 31u - __clz(tgroup.y);
+            tgroup.y &= ~(1u << bit);
+            if (tgroup.x + bit >= sc.ntri + sc.nsph) {
+                atomicOr(err, ERR_BAD_PRIM);
+                continue;
+            }
+            int prim;
+            if (leaf_prim_hit(sc, tgroup.x + bit, tr, ray, !ANY, &prim)) {
+                if (ANY && prim == skip) continue;
+                hit = prim;
+                if (ANY) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (!done && ngroup.y <= 0x00FFFFFFu) {
+            if (sp == 0) done = true;
+            else ngroup = stack[--sp];
+        }
+        if (done) {
+            src.store(idx, hit, ray.t_max);
+            busy = false;
+        }
+    }
+}
+
 }  // namespace bg

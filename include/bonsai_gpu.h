@@ -150,9 +150,10 @@ typedef struct bg_device_opts {
 
 /* BVH layouts the scene builder can produce. */
 typedef enum bg_bvh_kind {
-    BG_BVH_WIDE = 0,          /* 8-wide compressed BVH for the PBRT wavefront path          */
-    BG_BVH_REFERENCE = 1,     /* binary BVH laid out and ordered as the reference's         */
-    BG_BVH_REFERENCE_FIXED = 2 /* same, with the SAH bucket-index precedence bug fixed      */
+    BG_BVH_WIDE = 0,           /* 8-wide compressed BVH (80 B nodes, 8-bit child boxes)      */
+    BG_BVH_REFERENCE = 1,      /* binary BVH laid out and ordered as the reference's         */
+    BG_BVH_REFERENCE_FIXED = 2, /* same, with the SAH bucket-index precedence bug fixed      */
+    BG_BVH_WIDE2 = 3           /* 2-wide BVH, both child boxes in the parent (64 B nodes)    */
 } bg_bvh_kind;
 
 typedef struct bg_build_stats {
@@ -191,6 +192,17 @@ bg_status bg_scene_add_triangles(bg_scene* scene, const float* xyz, size_t ntri,
 bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t n);
 /* Builds the BVH on the host, uploads scene and BVH to the device. */
 bg_status bg_scene_commit(bg_scene* scene, uint32_t bvh_kind, bg_build_stats* stats);
+
+/* ---- launch tuning (chosen by the autotuner in bonsai_gb300/autotune.py) --------------------- */
+typedef struct bg_tuning {
+    uint32_t wave_paths;    /* wavefront capacity: paths per wave                                  */
+    uint32_t blocks_per_sm; /* persistent grid of the wavefront stages = SMs x blocks_per_sm (x128) */
+    uint32_t refill;        /* traversal: a warp fetches new rays once this many lanes are idle
+                               (32 = only when the whole warp is idle)                             */
+    uint32_t reserved;
+} bg_tuning;
+bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
+bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 
 /* ---- render: replaces SamplerIntegrator::render (src/base/integrator.rs:35-133) with
  *      PathIntegrator::radiance (src/integrators/path.rs:51-146).  rgb_out is a host buffer of
@@ -236,7 +248,7 @@ bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t byte
  * calls that overlap on the GPU race and must be serialised by the caller. */
 #define BG_NOALLOC_MAX_PIXELS (512u * 512u)
 #define BG_NOALLOC_WAVE_PATHS 65536u
-#define BG_NOALLOC_SCRATCH_BYTES 27788288u
+#define BG_NOALLOC_SCRATCH_BYTES 29099008u
 bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, const bg_render_opts* opts,
                             float* d_rgb_out, void* cuda_stream);
 

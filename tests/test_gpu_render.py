@@ -41,7 +41,7 @@ def test_cornell_ref_compat(gpu_ctx):
     assert r.stats.error_word == 0
 
 
-@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_REFERENCE_FIXED])
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2, A.BG_BVH_REFERENCE_FIXED])
 def test_cornell_pbrt(gpu_ctx, bvh):
     sd = S.cornell(64, 64)
     r, o, cmp = _render_pair(gpu_ctx, sd, A.BG_MODE_PBRT, bvh, 16)
@@ -51,9 +51,10 @@ def test_cornell_pbrt(gpu_ctx, bvh):
     np.testing.assert_allclose(r.rgb.mean(), o["rgb"].mean(), rtol=1e-3)
 
 
-def test_production_small_pbrt(gpu_ctx):
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2])
+def test_production_small_pbrt(gpu_ctx, bvh):
     sd = S.production(96, 54, spp=4, n_ico=6, ico_level=3, n_spheres=300)
-    r, o, cmp = _render_pair(gpu_ctx, sd, A.BG_MODE_PBRT, A.BG_BVH_WIDE, 4)
+    r, o, cmp = _render_pair(gpu_ctx, sd, A.BG_MODE_PBRT, bvh, 4)
     print(cmp)
     assert cmp["frac_z3"] <= Z3_FRAC
     assert cmp["frac_close"] >= 0.8

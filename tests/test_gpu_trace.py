@@ -54,15 +54,15 @@ def _check_closest(got, ref, exact):
         assert tie.all()
 
 
-@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_REFERENCE_FIXED])
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2, A.BG_BVH_REFERENCE_FIXED])
 def test_closest_soup(gpu_ctx, soup, bvh):
     sd, rays, ref, _ = soup
     assert (ref["prim"] >= 0).mean() > 0.1
     sc = G.Scene(gpu_ctx, sd, bvh)
-    _check_closest(sc.trace(rays), ref, exact=(bvh != A.BG_BVH_WIDE))
+    _check_closest(sc.trace(rays), ref, exact=(bvh == A.BG_BVH_REFERENCE_FIXED))
 
 
-@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_REFERENCE_FIXED])
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2, A.BG_BVH_REFERENCE_FIXED])
 def test_any_soup(gpu_ctx, soup, bvh):
     sd, rays, _, occ = soup
     sc = G.Scene(gpu_ctx, sd, bvh)
@@ -70,18 +70,19 @@ def test_any_soup(gpu_ctx, soup, bvh):
     assert (got != occ).sum() == 0
 
 
-@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_REFERENCE_FIXED])
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2, A.BG_BVH_REFERENCE_FIXED])
 def test_closest_and_any_mixed_spheres(gpu_ctx, mixed, bvh):
     sd, rays, ref, occ = mixed
     assert (ref["prim"] >= sd.ntri).sum() > 100  # spheres are hit
     sc = G.Scene(gpu_ctx, sd, bvh)
-    _check_closest(sc.trace(rays), ref, exact=(bvh != A.BG_BVH_WIDE))
+    _check_closest(sc.trace(rays), ref, exact=(bvh == A.BG_BVH_REFERENCE_FIXED))
     assert (sc.trace(rays, any_hit=True) != occ).sum() == 0
 
 
-def test_finite_tmax_and_empty(gpu_ctx, soup):
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2])
+def test_finite_tmax_and_empty(gpu_ctx, soup, bvh):
     sd, rays, ref, _ = soup
-    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    sc = G.Scene(gpu_ctx, sd, bvh)
     r2 = rays.copy()
     r2["tmax"] = 0.05
     orc = O.OracleScene(sd, fixed_bvh=True)
