@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(128) k_trace(Scene sc, const float4* rays, uin
                                                uint32_t* err, unsigned long long* counters, uint32_t* head, int refill) {
     if (LAYOUT != 1) {
         TraceSrc src{rays, hits, ANY ? occ : nullptr};
-        if (LAYOUT == 8) traverse_queue8<ANY>(sc, n, head, src, err, refill);
+        __shared__ uint2 stack8[STACK8 * 128];
+        if (LAYOUT == 8) traverse_queue8<ANY>(sc, n, head, src, err, refill, stack8);
         else traverse_queue<ANY>(sc, n, head, src, err, refill);
         return;
     }
@@ -308,7 +309,8 @@ __global__ void __launch_bounds__(128) k_extend(Scene sc, WaveBuffers wb, uint32
     const uint32_t n = wb.counters[bounce & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
     ExtendSrc src{wb.queue[bounce & 1], wb};
-    if (LAYOUT == 8) traverse_queue8<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
+    __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
+    if (LAYOUT == 8) traverse_queue8<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
     else traverse_queue<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
 }
 
@@ -516,7 +518,8 @@ __global__ void __launch_bounds__(128) k_shadow(Scene sc, WaveBuffers wb, uint32
     const uint32_t n = min(wb.counters[C_SHADOW], 2 * wb.capacity);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[1], (unsigned long long)n);
     ShadowSrc src{wb};
-    if (LAYOUT == 8) traverse_queue8<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
+    __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
+    if (LAYOUT == 8) traverse_queue8<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill, stack8);
     else traverse_queue<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
 }
 

@@ -359,7 +359,11 @@ BG_D void traverse_queue(const Scene& sc, uint32_t n, uint32_t* head, Src& src, 
 constexpr int STACK8 = 32;
 
 BG_D uint32_t sign_extend_bytes(uint32_t x) { return ((x & 0x80808080u) >> 7) * 0xFFu; }
-BG_D float byte_as_float(uint32_t w, int j) { return (float)((w >> (8 * j)) & 0xFFu); }
+// Byte j of w as a float: one byte permute builds 0x4B0000bb = 2^23 + b, one exact subtraction.
+BG_D float byte_as_float(uint32_t w, int j) {
+    const uint32_t sel = (uint32_t)j | (4u << 4) | (5u << 8) | (7u << 12);
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+}
 
 struct Ray8 {
     V3 o;
@@ -435,10 +439,17 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
 }
 
 // Persistent traversal of the 8-wide layout with in-warp ray replacement (see traverse_queue).
+// The node-group stack lives in shared memory, entry k of thread t at smem[k * blockDim.x + t].
+// Triangle groups are postponed (pushed) while fewer than kPostpone lanes of the warp would test
+// triangles, so leaf work runs with more lanes at once (Ylitie et al. 2017, section 5).
+constexpr int kPostpone = 0;  // 0 disables postponement (measured neutral to slightly slower here)
+
 template <bool ANY, class Src>
-BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill) {
+BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill,
+                          uint2* smem) {
     const uint32_t lane = threadIdx.x & 31u;
-    uint2 stack[STACK8];
+    uint2* stack = smem + threadIdx.x;
+    const uint32_t sstride = blockDim.x;
     Ray ray;
     Ray8 r8;
     TriRay tr;
@@ -484,7 +495,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                     sp = 0;
                     ngroup.y = 0;
                 } else {
-                    stack[sp++] = ngroup;
+                    stack[sstride * sp++] = ngroup;
                 }
             }
             const uint32_t slot = (bit - 24u) ^ (r8.octinv4 & 0xFFu);
@@ -501,6 +512,13 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         } else {
             tgroup = ngroup;
             ngroup = make_uint2(0, 0);
+        }
+        if (tgroup.y != 0) {
+            const unsigned want = __ballot_sync(__activemask(), true);
+            if (__popc(want) < kPostpone && ngroup.y > 0x00FFFFFFu && sp < STACK8) {
+                stack[sstride * sp++] = tgroup;  // upper byte 0: popped back as a triangle group
+                tgroup.y = 0;
+            }
         }
         while (tgroup.y != 0) {
             const uint32_t bit = 31u - __clz(tgroup.y);
@@ -521,7 +539,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         }
         if (!done && ngroup.y <= 0x00FFFFFFu) {
             if (sp == 0) done = true;
-            else ngroup = stack[--sp];
+            else ngroup = stack[sstride * --sp];
         }
         if (done) {
             src.store(idx, hit, ray.t_max);

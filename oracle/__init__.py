@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
         L.orc_rng_uniform.restype = C.c_float
         L.orc_rng_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
         L.orc_camera_ray.argtypes = [C.POINTER(bg_camera), C.c_float, C.c_float, C.c_float, P]
+        L.orc_philox.argtypes = [P, P, P]
         _lib = L
     return _lib
 
@@ -152,6 +153,14 @@ def bsdf_eval(mat: np.ndarray, wo, wi, mode: int) -> np.ndarray:
 
 def rng_uniform(seed: int, pixel: int, sample: int, dim: int) -> float:
     return lib().orc_rng_uniform(seed, pixel, sample, dim)
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.asarray(ctr, np.uint32)
+    k = np.asarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox(_ptr(c), _ptr(k), _ptr(out))
+    return out
 
 
 def camera_ray(cam: S.Camera, fx: float, fy: float, tu: float = 0.0) -> np.ndarray:

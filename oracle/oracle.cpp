@@ -1539,6 +1539,12 @@ void orc_bsdf_eval(const bg_material* m, const float* wo, const float* wi, int32
     out[0] = f.c[0]; out[1] = f.c[1]; out[2] = f.c[2];
     out[3] = b.pdf(V3(wo[0], wo[1], wo[2]), V3(wi[0], wi[1], wi[2]), BSDF_ALL, md);
 }
+// Raw Philox4x32-10 block (known-answer tests).
+void orc_philox(const uint32_t* ctr_in, const uint32_t* key, uint32_t* out) {
+    uint32_t c[4] = {ctr_in[0], ctr_in[1], ctr_in[2], ctr_in[3]};
+    philox4x32_10(c, key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
 float orc_rng_uniform(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
     CounterRng r;
     r.seed = seed;

@@ -1,0 +1,59 @@
+"""Generates the committed golden fixtures of the CPU oracle (tests/golden/*.npz).
+
+The reference has no golden vectors of its own, so these fixtures pin the oracle's behaviour
+against regressions: small seeded ray-set traces (closest hit + any hit, reference-layout BVH
+with and without the bucket bug) and small renders in both estimator modes.
+Run:  python tests/golden/make_golden.py
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+import oracle as O  # noqa: E402
+from bonsai_gb300 import _abi as A  # noqa: E402
+from bonsai_gb300 import scenes as S  # noqa: E402
+
+
+def trace_case():
+    sd, rays = S.ray_soup(3000, 4000)
+    out = {}
+    for fixed in (0, 1):
+        sc = O.OracleScene(sd, fixed_bvh=bool(fixed))
+        h, cnt = sc.trace(rays, count=True, threads=1)
+        occ = sc.trace(rays, any_hit=True, threads=1)
+        out[f"prim_{fixed}"] = h["prim"]
+        out[f"t_{fixed}"] = h["t"]
+        out[f"occ_{fixed}"] = occ
+        out[f"counters_{fixed}"] = cnt
+        out[f"nodes_{fixed}"] = np.array(sc.bvh_nodes)
+    return out
+
+
+def render_case():
+    out = {}
+    sd = S.cornell(16, 16, spp=4)
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=False).render(mode, seed=7, threads=1)
+        out[f"cornell_sum_{mode}"] = r["sum"]
+        out[f"cornell_rgb_{mode}"] = r["rgb"]
+    sd = S.production(24, 16, spp=2, n_ico=2, ico_level=2, n_spheres=20)
+    r = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, seed=1, threads=1)
+    out["production_sum"] = r["sum"]
+    return out
+
+
+def rng_case():
+    idx = np.array([(0, 0, 0, 0), (1, 2, 3, 4), (12345, 999, 7, 41), (2**32 - 1, 2**31, 65535, 1023)], np.uint64)
+    vals = np.array([O.rng_uniform(int(s), int(p), int(n), int(d)) for s, p, n, d in idx], np.float32)
+    return {"rng_index": idx, "rng_value": vals}
+
+
+if __name__ == "__main__":
+    np.savez_compressed(HERE / "oracle_trace.npz", **trace_case())
+    np.savez_compressed(HERE / "oracle_render.npz", **render_case())
+    np.savez_compressed(HERE / "oracle_rng.npz", **rng_case())
+    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))

@@ -1,0 +1,108 @@
+"""Analytic known answers for the CPU oracle (it has no reference outputs to be checked against).
+
+* White furnace: a closed box of albedo rho whose walls all emit L_e = 1 has L = L_e / (1 - rho)
+  everywhere; the PBRT estimator (MIS next-event estimation + BSDF sampling + roulette) must give it.
+* A glass sphere inside an emitting black box transmits or reflects everything: L = 1.
+* BSDF sample / pdf / eval consistency: E[f cos / pdf] over sampled directions equals the
+  quadrature of f cos over the hemisphere (PBRT mode); in REF_COMPAT mode the Trowbridge-Reitz
+  pdf uses G1 = lambda (src/base/microfacet.rs:17-19), which breaks the identity.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from bonsai_gb300 import _abi as A
+from bonsai_gb300 import scenes as S
+
+
+def _closed_box(rho, emit=1.0, two_sided=1):
+    quads = [((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (0, 1, 0)),
+             ((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), (0, -1, 0)),
+             ((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1)),
+             ((-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1), (0, 0, -1)),
+             ((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), (1, 0, 0)),
+             ((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), (-1, 0, 0))]
+    tri = np.concatenate([S._quad(*q) for q in quads])
+    mats = [S.material(S.MATTE, kd=(rho, rho, rho)), S.material(S.DIELECTRIC, ior=1.5)]
+    lights = np.zeros(1, S.LIGHT_DT)
+    lights[0] = ((emit, emit, emit), two_sided)
+    cam = S.Camera((0.0, 0.0, 0.6), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0), 60.0, 12, 12)
+    return S.SceneData(tri, np.zeros(len(tri), np.uint32), np.zeros(len(tri), np.int32), np.zeros(0, S.SPHERE_DT),
+                       np.stack(mats), lights, cam, spp=128, max_depth=60, rr_threshold=1.0)
+
+
+@pytest.mark.parametrize("rho", [0.0, 0.5, 0.8])
+def test_white_furnace(rho):
+    sd = _closed_box(rho)
+    r = O.OracleScene(sd).render(A.BG_MODE_PBRT, seed=11)
+    n = 12 * 12 * sd.spp
+    x = r["sum"].sum(axis=2) / 3.0  # per pixel sum of samples (channel mean)
+    mean = x.sum() / n
+    var = (r["sumsq"].sum(axis=2) / 3.0).sum() / n - mean ** 2
+    se = np.sqrt(max(var, 0.0) / n)
+    expected = 1.0 / (1.0 - rho)
+    assert abs(mean - expected) <= 4 * se + 1e-9, (mean, expected, se)
+
+
+def test_glass_sphere_in_emitting_box():
+    sd = _closed_box(0.0)
+    sph = np.zeros(1, S.SPHERE_DT)
+    sph[0] = ((0.0, 0.0, -0.2), 0.4, 1, -1)
+    sd.spheres = sph
+    r = O.OracleScene(sd).render(A.BG_MODE_PBRT, seed=3)
+    mean = r["sum"].sum() / (3 * 12 * 12 * sd.spp)
+    # paths trapped by total internal reflection past max_depth lose a little energy
+    assert 0.98 <= mean <= 1.0 + 1e-3
+
+
+def _hemisphere_quadrature(mat, wo, mode, n=256):
+    # midpoint rule in (cos theta, phi): dw = d(cos theta) d(phi)
+    ct = (np.arange(n) + 0.5) / n
+    ph = (np.arange(2 * n) + 0.5) * np.pi / n
+    tot = 0.0
+    for c in ct[::4]:
+        s = np.sqrt(1 - c * c)
+        for p in ph[::4]:
+            wi = (s * np.cos(p), s * np.sin(p), c)
+            f = O.bsdf_eval(mat, wo, wi, mode)[:3]
+            tot += f.mean() * c
+    return tot * (1.0 / (n / 4)) * (np.pi / (n / 4))
+
+
+def _sampled_estimate(mat, wo, mode, n=4000, seed=0):
+    rng = np.random.default_rng(seed)
+    acc = 0.0
+    for _ in range(n):
+        out = O.bsdf_sample(mat, wo, float(rng.random()), float(rng.random()), mode)
+        f, pdf, wi = out[:3], out[3], out[4:7]
+        if pdf > 0:
+            acc += f.mean() * abs(wi[2]) / pdf
+    return acc / n
+
+
+@pytest.mark.parametrize("kind", ["matte", "conductor", "plastic"])
+def test_bsdf_sampling_matches_quadrature_pbrt(kind):
+    mat = {"matte": S.material(S.MATTE, kd=(0.6, 0.5, 0.4)),
+           "conductor": S.material(S.CONDUCTOR, roughness=0.3),
+           "plastic": S.material(S.PLASTIC, kd=(0.5, 0.5, 0.5), ks=(0.3, 0.3, 0.3), roughness=0.3)}[kind]
+    wo = np.array([0.3, 0.2, 0.0])
+    wo[2] = np.sqrt(1 - 0.13)
+    q = _hemisphere_quadrature(mat, wo, A.BG_MODE_PBRT)
+    e = _sampled_estimate(mat, wo, A.BG_MODE_PBRT)
+    assert abs(e - q) <= 0.05 * q, (e, q)
+
+
+def test_ref_compat_microfacet_pdf_is_inconsistent():
+    # F4: G1 = lambda makes the reference's pdf disagree with its own sampling
+    mat = S.material(S.CONDUCTOR, roughness=0.3)
+    wo = np.array([0.6, 0.0, 0.8])
+    q = _hemisphere_quadrature(mat, wo, A.BG_MODE_REF_COMPAT)
+    e = _sampled_estimate(mat, wo, A.BG_MODE_REF_COMPAT)
+    assert abs(e - q) > 0.2 * q
+
+
+def test_lambertian_closed_form():
+    mat = S.material(S.MATTE, kd=(0.6, 0.5, 0.4))
+    out = O.bsdf_eval(mat, (0.0, 0.0, 1.0), (0.6, 0.0, 0.8), A.BG_MODE_PBRT)
+    np.testing.assert_allclose(out[:3], np.array([0.6, 0.5, 0.4]) / np.pi, rtol=1e-6)
+    np.testing.assert_allclose(out[3], 0.8 / np.pi, rtol=1e-6)
