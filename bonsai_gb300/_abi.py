@@ -61,6 +61,13 @@ class bg_sphere(C.Structure):
                 ("light_id", C.c_int32)]
 
 
+class bg_quadric(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("reverse_orientation", C.c_uint32), ("object_to_world", C.c_float * 12),
+                ("world_to_object", C.c_float * 12), ("radius", C.c_float), ("inner_radius", C.c_float),
+                ("z_min", C.c_float), ("z_max", C.c_float), ("height", C.c_float), ("phi_max_deg", C.c_float),
+                ("material_id", C.c_uint32), ("light_id", C.c_int32)]
+
+
 class bg_camera(C.Structure):
     _fields_ = [("position", F3), ("look_at", F3), ("up", F3), ("fov_deg", C.c_float),
                 ("near_plane", C.c_float), ("far_plane", C.c_float), ("lens_radius", C.c_float),
@@ -122,6 +129,7 @@ SIGNATURES = {
     "bg_scene_add_area_light": (ST, [P, C.POINTER(bg_area_light), C.POINTER(C.c_uint32)]),
     "bg_scene_add_triangles": (ST, [P, P, C.c_size_t, P, P]),
     "bg_scene_add_spheres": (ST, [P, P, C.c_size_t]),
+    "bg_scene_add_quadrics": (ST, [P, P, C.c_size_t]),
     "bg_scene_commit": (ST, [P, C.c_uint32, C.POINTER(bg_build_stats)]),
     "bg_render": (ST, [P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
                        C.POINTER(bg_render_stats)]),

@@ -61,6 +61,7 @@ struct bg_scene {
     std::vector<uint32_t> tri_mat;
     std::vector<int32_t> tri_light;
     std::vector<bg_sphere> sph;
+    std::vector<bg_quadric> quads;
     std::vector<bg_material> mats;
     std::vector<bg_area_light> lights;
     bool committed = false;
@@ -587,6 +588,26 @@ bg_status bg_scene_add_spheres(bg_scene* s, const bg_sphere* sp, size_t n) {
     return BG_OK;
 }
 
+bg_status bg_scene_add_quadrics(bg_scene* s, const bg_quadric* q, size_t n) {
+    if (!s || (n && !q)) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    for (size_t i = 0; i < n; ++i) {
+        if (q[i].kind > BG_QUADRIC_CONE) return fail(s->ctx, BG_ERR_INVALID, "unknown quadric kind");
+        if (q[i].material_id >= s->mats.size()) return fail(s->ctx, BG_ERR_INVALID, "quadric has an unknown material id");
+        if (q[i].light_id >= 0) return fail(s->ctx, BG_ERR_UNSUPPORTED, "quadric area lights are not supported");
+        if (!(q[i].radius > 0.0f) || !std::isfinite(q[i].radius))
+            return fail(s->ctx, BG_ERR_INVALID, "quadric radius must be finite and > 0");
+        if (q[i].kind == BG_QUADRIC_CONE && !(q[i].height != 0.0f))
+            return fail(s->ctx, BG_ERR_INVALID, "cone height must be non-zero");
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(q[i].object_to_world[k]) || !std::isfinite(q[i].world_to_object[k]))
+                return fail(s->ctx, BG_ERR_INVALID, "quadric transform is not finite");
+    }
+    s->quads.insert(s->quads.end(), q, q + n);
+    return BG_OK;
+}
+
 bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if (!s) return BG_ERR_INVALID;
     if (!s->ctx) return BG_ERR_INVALID;
@@ -596,7 +617,8 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaSetDevice(ctx->device));
     const uint32_t ntri = (uint32_t)s->tri_mat.size(), nsph = (uint32_t)s->sph.size();
-    bg::HostPrims hp{s->tri.data(), ntri, s->sph.data(), nsph};
+    const uint32_t nquad = (uint32_t)s->quads.size();
+    bg::HostPrims hp{s->tri.data(), ntri, s->sph.data(), nsph, s->quads.data(), nquad};
     // triangles as float4 triplets with material / emission / light-index tags
     std::vector<float4> tri4(3 * (size_t)ntri);
     std::vector<uint32_t> light_prims;
@@ -624,6 +646,32 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         sph4[i] = make_float4(s->sph[i].center[0], s->sph[i].center[1], s->sph[i].center[2], s->sph[i].radius);
         sph_mat[i] = s->sph[i].material_id;
     }
+    // quadric records: o2w rows, w2o rows (o2w itself when it is the identity, cylinder.rs:37-41),
+    // (radius, inner, z_min, z_max), (height, phi_max, flags, material)
+    std::vector<float4> quad4((size_t)bg::QUADRIC_F4 * nquad);
+    for (uint32_t i = 0; i < nquad; ++i) {
+        const bg_quadric& q = s->quads[i];
+        float4* r = &quad4[(size_t)bg::QUADRIC_F4 * i];
+        bool ident = true;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 4; ++b) ident &= q.object_to_world[4 * a + b] == ((a == b) ? 1.0f : 0.0f);
+        const float* w2o = ident ? q.object_to_world : q.world_to_object;
+        for (int a = 0; a < 3; ++a) {
+            r[a] = make_float4(q.object_to_world[4 * a], q.object_to_world[4 * a + 1], q.object_to_world[4 * a + 2],
+                               q.object_to_world[4 * a + 3]);
+            r[3 + a] = make_float4(w2o[4 * a], w2o[4 * a + 1], w2o[4 * a + 2], w2o[4 * a + 3]);
+        }
+        const float* m = q.object_to_world;  // Transform::swaps_handedness (transform.rs:212-218)
+        float det = m[0] * (m[5] * m[10] - m[6] * m[9]) - m[1] * (m[4] * m[10] - m[6] * m[8]) +
+                    m[2] * (m[4] * m[9] - m[5] * m[8]);
+        uint32_t flags = q.kind | ((q.reverse_orientation ? 1u : 0u) << 8) | ((det < 0.0f ? 1u : 0u) << 9);
+        float phi_max = std::fmin(std::fmax(q.phi_max_deg, 0.0f), 360.0f) * (3.14159265358979323846f / 180.0f);
+        r[6] = make_float4(q.radius, q.inner_radius, std::fmin(q.z_min, q.z_max), std::fmax(q.z_min, q.z_max));
+        float fbits, mbits;
+        std::memcpy(&fbits, &flags, 4);
+        std::memcpy(&mbits, &q.material_id, 4);
+        r[7] = make_float4(q.height, phi_max, fbits, mbits);
+    }
     std::vector<bg::Material> mats(s->mats.size());
     for (size_t i = 0; i < mats.size(); ++i) {
         const bg_material& m = s->mats[i];
@@ -648,8 +696,10 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     d = bg::Scene{};
     d.ntri = ntri;
     d.nsph = nsph;
+    d.nquad = nquad;
     d.nlights = (uint32_t)light_prims.size();
     bg_status st;
+    if ((st = upload(ctx, quad4, &d.quads, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, tri4, &d.tri, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, sph4, &d.sph, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, sph_mat, &d.sph_mat, &s->allocs)) != BG_OK) return st;
@@ -688,11 +738,11 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if (stats) {
         stats->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->nodes = nodes;
-        stats->prims = (uint64_t)ntri + nsph;
+        stats->prims = (uint64_t)ntri + nsph + nquad;
         const bool wide = kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2;
         uint64_t bytes = tri4.size() * 16 + sph4.size() * 16 +
                          nodes * (kind == BG_BVH_WIDE ? 80 : (kind == BG_BVH_WIDE2 ? 64 : 32)) +
-                         ((uint64_t)ntri + nsph) * (wide ? 48 : 4);
+                         ((uint64_t)ntri + nsph + nquad) * (wide ? 48 : 4) + quad4.size() * 16;
         stats->device_bytes = bytes;
     }
     return BG_OK;

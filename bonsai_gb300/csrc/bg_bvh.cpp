@@ -56,9 +56,34 @@ Box prim_box(const HostPrims& p, uint32_t i) {
         b.grow(v + 6);
         return b;
     }
-    const bg_sphere& s = p.sph[i - p.ntri];
-    const float r = s.radius;
-    const float lo[3] = {-r, -r, std::fmin(-r, r)}, hi[3] = {r, r, std::fmax(-r, r)};
+    float m[3][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+    float lo[3], hi[3];
+    if (i < p.ntri + p.nsph) {
+        const bg_sphere& s = p.sph[i - p.ntri];
+        const float r = s.radius;
+        lo[0] = -r; lo[1] = -r; lo[2] = std::fmin(-r, r);
+        hi[0] = r; hi[1] = r; hi[2] = std::fmax(-r, r);
+        m[0][3] = s.center[0];
+        m[1][3] = s.center[1];
+        m[2][3] = s.center[2];
+    } else {  // cylinder.rs:61-66, disk.rs:57-62, cone.rs:57-62
+        const bg_quadric& q = p.quad[i - p.ntri - p.nsph];
+        const float r = q.radius;
+        float z0 = 0.0f, z1 = 0.0f;
+        if (q.kind == BG_QUADRIC_CYLINDER) {
+            z0 = std::fmin(q.z_min, q.z_max);
+            z1 = std::fmax(q.z_min, q.z_max);
+        } else if (q.kind == BG_QUADRIC_DISK) {
+            z0 = z1 = q.height;
+        } else {
+            z0 = 0.0f;
+            z1 = q.height;
+        }
+        lo[0] = -r; lo[1] = -r; lo[2] = z0;
+        hi[0] = r; hi[1] = r; hi[2] = z1;
+        for (int rr = 0; rr < 3; ++rr)
+            for (int c = 0; c < 4; ++c) m[rr][c] = q.object_to_world[4 * rr + c];
+    }
     bool first = true;
     for (int c = 0; c < 8; ++c) {
         // corner order of transform_bounds; Point3::transform: m00*x + m01*y + m02*z + m03
@@ -66,9 +91,7 @@ Box prim_box(const HostPrims& p, uint32_t i) {
                                         {0, 1, 1}, {1, 1, 0}, {1, 0, 1}, {1, 1, 1}};
         float q[3] = {order[c][0] ? hi[0] : lo[0], order[c][1] ? hi[1] : lo[1], order[c][2] ? hi[2] : lo[2]};
         float w[3];
-        w[0] = 1.0f * q[0] + 0.0f * q[1] + 0.0f * q[2] + s.center[0];
-        w[1] = 0.0f * q[0] + 1.0f * q[1] + 0.0f * q[2] + s.center[1];
-        w[2] = 0.0f * q[0] + 0.0f * q[1] + 1.0f * q[2] + s.center[2];
+        for (int k = 0; k < 3; ++k) w[k] = m[k][0] * q[0] + m[k][1] * q[1] + m[k][2] * q[2] + m[k][3];
         if (first) {
             for (int k = 0; k < 3; ++k) b.lo[k] = b.hi[k] = w[k];
             first = false;
@@ -111,7 +134,7 @@ size_t two_pointer_partition(RefInfo* v, size_t n, F pred) {
 }  // namespace
 
 bool build_reference_bvh(const HostPrims& p, bool faithful, RefBvh* out, uint64_t max_prims_faithful) {
-    const uint64_t n = (uint64_t)p.ntri + p.nsph;
+    const uint64_t n = p.count();
     out->nodes.clear();
     out->order.clear();
     if (n == 0) return true;
@@ -336,12 +359,18 @@ void emit_prim(const HostPrims& p, uint32_t id, std::vector<float4>* out) {
         std::memcpy(&a.w, &id, 4);
         b.x = v[3]; b.y = v[4]; b.z = v[5]; b.w = 0.0f;
         c.x = v[6]; c.y = v[7]; c.z = v[8]; c.w = 0.0f;
-    } else {
+    } else if (id < p.ntri + p.nsph) {
         const bg_sphere& s = p.sph[id - p.ntri];
         a.x = s.center[0]; a.y = s.center[1]; a.z = s.center[2];
         uint32_t idbits = (id - p.ntri) | SPHERE_BIT;
         std::memcpy(&a.w, &idbits, 4);
         b.x = s.radius; b.y = 0.0f; b.z = 0.0f; b.w = 0.0f;
+        c.x = c.y = c.z = c.w = 0.0f;
+    } else {
+        a.x = a.y = a.z = 0.0f;
+        uint32_t idbits = (id - p.ntri - p.nsph) | QUADRIC_BIT;
+        std::memcpy(&a.w, &idbits, 4);
+        b.x = b.y = b.z = b.w = 0.0f;
         c.x = c.y = c.z = c.w = 0.0f;
     }
     out->push_back(a);
@@ -356,32 +385,7 @@ struct Flattener {
     // Emits the leaf's primitives; returns the encoded child reference (~first) and count.
     void emit_leaf(const BNode* n, int* child, int* count) {
         uint32_t first = (uint32_t)(out->leaf_prims.size() / 3);
-        for (uint32_t i = 0; i < n->count; ++i) {
-            uint32_t id = refs[n->first + i].id;
-            if (id < p.ntri) {
-                const float* v = p.tri + 9 * (size_t)id;
-                float4 a, b, c;
-                a.x = v[0]; a.y = v[1]; a.z = v[2];
-                uint32_t idbits = id;
-                std::memcpy(&a.w, &idbits, 4);
-                b.x = v[3]; b.y = v[4]; b.z = v[5]; b.w = 0.0f;
-                c.x = v[6]; c.y = v[7]; c.z = v[8]; c.w = 0.0f;
-                out->leaf_prims.push_back(a);
-                out->leaf_prims.push_back(b);
-                out->leaf_prims.push_back(c);
-            } else {
-                const bg_sphere& s = p.sph[id - p.ntri];
-                float4 a, b, c;
-                a.x = s.center[0]; a.y = s.center[1]; a.z = s.center[2];
-                uint32_t idbits = (id - p.ntri) | SPHERE_BIT;
-                std::memcpy(&a.w, &idbits, 4);
-                b.x = s.radius; b.y = 0.0f; b.z = 0.0f; b.w = 0.0f;
-                c.x = c.y = c.z = c.w = 0.0f;
-                out->leaf_prims.push_back(a);
-                out->leaf_prims.push_back(b);
-                out->leaf_prims.push_back(c);
-            }
-        }
+        for (uint32_t i = 0; i < n->count; ++i) emit_prim(p, refs[n->first + i].id, &out->leaf_prims);
         *child = ~(int)first;
         *count = (int)n->count;
     }
@@ -413,7 +417,7 @@ struct Flattener {
 void build_bvh2(const HostPrims& p, Bvh2* out, int /*threads*/) {
     out->nodes.clear();
     out->leaf_prims.clear();
-    const uint32_t n = p.ntri + p.nsph;
+    const uint32_t n = p.count();
     if (n == 0) return;
     std::vector<Ref2> refs(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -472,7 +476,7 @@ int axis_exponent(double extent) {
 void build_bvh8(const HostPrims& p, Bvh8* out) {
     out->nodes.clear();
     out->leaf_prims.clear();
-    const uint32_t n = p.ntri + p.nsph;
+    const uint32_t n = p.count();
     if (n == 0) return;
     std::vector<Ref2> refs(n);
     for (uint32_t i = 0; i < n; ++i) {

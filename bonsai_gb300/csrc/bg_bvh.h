@@ -13,6 +13,9 @@ struct HostPrims {
     uint32_t ntri;
     const bg_sphere* sph;
     uint32_t nsph;
+    const bg_quadric* quad = nullptr;
+    uint32_t nquad = 0;
+    uint32_t count() const { return ntri + nsph + nquad; }
 };
 
 // BVH::new (src/accelerators/bvh.rs:53-269): 16-bucket SAH, leaves of up to 256 primitives,

@@ -73,10 +73,18 @@ struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-1
     uint32_t width, height;
 };
 
+// Quadric record (8 x float4 = 128 B): rows 0-2 object_to_world (3x4), rows 3-5 world_to_object,
+// row 6 = radius, inner_radius, z_min, z_max; row 7 = height, phi_max (radians),
+// flags (kind | reverse << 8 | swaps_handedness << 9) as bits, material id as bits.
+constexpr int QUADRIC_F4 = 8;
+
 struct Scene {
     const float4* tri;
     uint32_t ntri;
     uint32_t nsph;
+    const float4* quads;  // QUADRIC_F4 per quadric
+    uint32_t nquad;
+    uint32_t pad2;
     const float4* sph;
     const uint32_t* sph_mat;
     const Material* mats;
@@ -103,6 +111,7 @@ enum : uint32_t {
 };
 
 constexpr uint32_t SPHERE_BIT = 0x80000000u;
+constexpr uint32_t QUADRIC_BIT = 0x40000000u;
 constexpr int TRAVERSAL_STACK = 64;
 
 }  // namespace bg

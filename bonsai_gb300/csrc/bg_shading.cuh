@@ -373,7 +373,9 @@ struct BSDF {
 };
 
 BG_D uint32_t prim_material(const Scene& sc, int prim) {
-    return (uint32_t)prim < sc.ntri ? __float_as_uint(sc.tri[3 * prim].w) : sc.sph_mat[prim - sc.ntri];
+    if ((uint32_t)prim < sc.ntri) return __float_as_uint(sc.tri[3 * prim].w);
+    if ((uint32_t)prim < sc.ntri + sc.nsph) return sc.sph_mat[prim - sc.ntri];
+    return __float_as_uint(sc.quads[QUADRIC_F4 * (prim - sc.ntri - sc.nsph) + 7].w);
 }
 
 // Material::compute_scattering_functions for the constant-texture materials.  CLS is the

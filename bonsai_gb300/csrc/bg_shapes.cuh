@@ -255,6 +255,184 @@ BG_D void sphere_isect(float4 s, const SphHit& h, const Ray& rw, Isect* it) {
     it->dpdu = xf_vec_id(dpdu);
 }
 
+// ---------------------------------------------------------------- quadrics (cylinder, disk, cone)
+struct M34 {
+    float m[3][4];
+};
+BG_D M34 load_m34(const float4* r) {
+    M34 x;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float4 v = r[i];
+        x.m[i][0] = v.x;
+        x.m[i][1] = v.y;
+        x.m[i][2] = v.z;
+        x.m[i][3] = v.w;
+    }
+    return x;
+}
+// Point3::transform_with_error / Vec3::transform(_with_error) / Normal::transform with a 3x4 affine
+// matrix (bottom row 0 0 0 1, so the homogeneous w is exactly 1) - point3.rs:71-140, vec3.rs:35-64.
+BG_D V3 m_point_err(const M34& t, V3 p, V3* err) {
+    const auto& m = t.m;
+    float xp = (m[0][0] * p.x + m[0][1] * p.y) + (m[0][2] * p.z + m[0][3]);
+    float yp = (m[1][0] * p.x + m[1][1] * p.y) + (m[1][2] * p.z + m[1][3]);
+    float zp = (m[2][0] * p.x + m[2][1] * p.y) + (m[2][2] * p.z + m[2][3]);
+    float xa = fabsf(m[0][0] * p.x) + fabsf(m[0][1] * p.y) + fabsf(m[0][2] * p.z) + fabsf(m[0][3]);
+    float ya = fabsf(m[1][0] * p.x) + fabsf(m[1][1] * p.y) + fabsf(m[1][2] * p.z) + fabsf(m[1][3]);
+    float za = fabsf(m[2][0] * p.x) + fabsf(m[2][1] * p.y) + fabsf(m[2][2] * p.z) + fabsf(m[2][3]);
+    *err = gamma(3.0f) * v3(xa, ya, za);
+    return v3(xp, yp, zp);
+}
+BG_D V3 m_vec(const M34& t, V3 v) {
+    const auto& m = t.m;
+    return v3(m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+              m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z);
+}
+BG_D V3 m_vec_err(const M34& t, V3 v, V3* e) {
+    const auto& m = t.m;
+    float g3 = gamma(3.0f);
+    e->x = g3 * (fabsf(m[0][0] * v.x) + fabsf(m[0][1] * v.y) + fabsf(m[0][2] * v.z));
+    e->y = g3 * (fabsf(m[1][0] * v.x) + fabsf(m[1][1] * v.y) + fabsf(m[1][2] * v.z));
+    e->z = g3 * (fabsf(m[2][0] * v.x) + fabsf(m[2][1] * v.y) + fabsf(m[2][2] * v.z));
+    return m_vec(t, v);
+}
+BG_D V3 m_normal(const M34& inv, V3 n) {  // uses m_inverse transposed
+    const auto& mi = inv.m;
+    return v3(mi[0][0] * n.x + mi[1][0] * n.y + mi[2][0] * n.z, mi[0][1] * n.x + mi[1][1] * n.y + mi[2][1] * n.z,
+              mi[0][2] * n.x + mi[1][2] * n.y + mi[2][2] * n.z);
+}
+BG_D V3 m_point_perr(const M34& t, V3 p, V3 pe, V3* ae) {
+    const auto& m = t.m;
+    float g3 = gamma(3.0f);
+    V3 r;
+    r.x = (m[0][0] * p.x + m[0][1] * p.y) + (m[0][2] * p.z + m[0][3]);
+    r.y = (m[1][0] * p.x + m[1][1] * p.y) + (m[1][2] * p.z + m[1][3]);
+    r.z = (m[2][0] * p.x + m[2][1] * p.y) + (m[2][2] * p.z + m[2][3]);
+    ae->x = (g3 + 1.0f) * (fabsf(m[0][0]) * pe.x + fabsf(m[0][1]) * pe.y + fabsf(m[0][2]) * pe.z) +
+            g3 * (fabsf(m[0][0] * p.x) + fabsf(m[0][1] * p.y) + fabsf(m[0][2] * p.z) + fabsf(m[0][3]));
+    ae->y = (g3 + 1.0f) * (fabsf(m[1][0]) * pe.x + fabsf(m[1][1]) * pe.y + fabsf(m[1][2]) * pe.z) +
+            g3 * (fabsf(m[1][0] * p.x) + fabsf(m[1][1] * p.y) + fabsf(m[1][2] * p.z) + fabsf(m[1][3]));
+    ae->z = (g3 + 1.0f) * (fabsf(m[2][0]) * pe.x + fabsf(m[2][1]) * pe.y + fabsf(m[2][2]) * pe.z) +
+            g3 * (fabsf(m[2][0] * p.x) + fabsf(m[2][1] * p.y) + fabsf(m[2][2] * p.z) + fabsf(m[2][3]));
+    return r;
+}
+BG_D float ef_abs_err(EF e) { return next_float_up(rmax(fabsf(e.hi - e.v), fabsf(e.v - e.lo))); }
+
+// Cylinder / Disk / Cone ::intersect and ::intersect_test (cylinder.rs:71-288, disk.rs:70-183,
+// cone.rs:67-287).  Fills `it` (world-space interaction) when it is non-null.
+BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out, Isect* it) {
+    const float4 p0 = q[6], p1 = q[7];
+    const uint32_t flags = __float_as_uint(p1.z);
+    const int kind = (int)(flags & 0xFFu);
+    const float radius = p0.x, inner = p0.y, z_min = p0.z, z_max = p0.w, height = p1.x, phi_max = p1.y;
+    const M34 w2o = load_m34(q + 3);
+    V3 oe, de;
+    Ray ray;
+    ray.o = m_point_err(w2o, rw.o, &oe);
+    ray.d = m_vec_err(w2o, rw.d, &de);
+    ray.t_max = t_max;
+    ray.time = rw.time;
+    float ls = length_squared(ray.d);
+    if (ls > 0.0f) {
+        float dt = dot(vabs(ray.d), oe) / ls;
+        ray.o = ray.o + ray.d * dt;
+    }
+    V3 ph, dpdu, dpdv, perr;
+    float tsh_v;
+    if (kind == 1) {  // disk
+        if (ray.d.z == 0.0f) return false;
+        float tsh = (height - ray.o.z) / ray.d.z;
+        if (tsh <= 0.0f || tsh >= ray.t_max) return false;
+        ph = ray.o + ray.d * tsh;
+        float dist = ph.x * ph.x + ph.y * ph.y;
+        if (dist > radius * radius || dist < inner * inner) return false;
+        float phi = atan2f(ph.y, ph.x);
+        if (phi < 0.0f) phi += 2.0f * PI;
+        if (phi > phi_max) return false;
+        if (!it) {
+            *t_out = tsh;
+            return true;
+        }
+        float rh = sqrtf(dist);
+        dpdu = v3(-phi_max * ph.y, phi_max * ph.x, 0.0f);
+        dpdv = v3(ph.x, ph.y, 0.0f) * (inner - radius) / rh;
+        ph.z = height;
+        perr = v3(0.0f, 0.0f, 0.0f);
+        tsh_v = tsh;
+    } else {
+        EF ox = ef(ray.o.x, oe.x), oy = ef(ray.o.y, oe.y), oz = ef(ray.o.z, oe.z);
+        EF dx = ef(ray.d.x, de.x), dy = ef(ray.d.y, de.y), dz = ef(ray.d.z, de.z);
+        EF a, b, c;
+        if (kind == 0) {
+            a = dx * dx + dy * dy;
+            b = ef(2.0f) * (dx * ox + dy * oy);
+            c = ox * ox + oy * oy - ef(radius, 0.0f) * ef(radius, 0.0f);
+        } else {
+            EF k = ef(radius, 0.0f) / ef(height, 0.0f);
+            k = k * k;
+            a = dx * dx + dy * dy - k * dz * dz;
+            b = ef(2.0f) * (dx * ox + dy * oy - k * dz * (oz - ef(height)));
+            c = ox * ox + oy * oy - k * (oz - ef(height)) * (oz - ef(height));
+        }
+        EF t0, t1;
+        if (!quadratic(a, b, c, &t0, &t1)) return false;
+        if (t0.hi > ray.t_max || t1.lo <= 0.0f) return false;
+        EF tsh = t0;
+        if (tsh.lo <= 0.0f) {
+            tsh = t1;
+            if (tsh.hi > ray.t_max) return false;
+        }
+        bool used_t1 = tsh.v == t1.v && tsh.lo == t1.lo && tsh.hi == t1.hi;
+        for (int pass = 0; pass < 2; ++pass) {
+            ph = ray.o + ray.d * tsh.v;
+            if (kind == 0) {
+                float hr = sqrtf(ph.x * ph.x + ph.y * ph.y);
+                ph.x *= radius / hr;
+                ph.y *= radius / hr;
+            }
+            float phi = atan2f(ph.y, ph.x);
+            if (phi < 0.0f) phi += 2.0f * PI;
+            bool clipped = kind == 0 ? (ph.z < z_min || ph.z > z_max || phi > phi_max)
+                                     : (ph.z < 0.0f || ph.z > height || phi > phi_max);
+            if (!clipped) break;
+            if (pass == 1 || used_t1) return false;
+            if (t1.hi > ray.t_max) return false;
+            tsh = t1;
+            used_t1 = true;
+        }
+        if (!it) {
+            *t_out = tsh.v;
+            return true;
+        }
+        dpdu = v3(-phi_max * ph.y, phi_max * ph.x, 0.0f);
+        if (kind == 0) {
+            dpdv = v3(0.0f, 0.0f, z_max - z_min);
+            perr = gamma(3.0f) * vabs(v3(ph.x, ph.y, 0.0f));
+        } else {
+            float v = ph.z / height;
+            dpdv = v3(-ph.x / (1.0f - v), -ph.y / (1.0f - v), height);
+            EF px = ox + tsh * dx, py = oy + tsh * dy, pz = oz + tsh * dz;
+            perr = v3(ef_abs_err(px), ef_abs_err(py), ef_abs_err(pz));
+        }
+        tsh_v = tsh.v;
+    }
+    // Interaction::new + Interaction::transform(object_to_world)
+    const M34 o2w = load_m34(q);
+    V3 n = normalize(cross(dpdu, dpdv));
+    if (((flags >> 8) & 1u) ^ ((flags >> 9) & 1u)) n = n * -1.0f;
+    V3 ae;
+    it->p = m_point_perr(o2w, ph, perr, &ae);
+    it->p_err = ae;
+    it->time = ray.time;
+    it->wo = m_vec(o2w, -ray.d);
+    it->n = normalize(m_normal(w2o, n));
+    it->ns = face_forward(normalize(m_normal(w2o, n)), it->n);
+    it->dpdu = m_vec(o2w, dpdu);
+    *t_out = tsh_v;
+    return true;
+}
+
 // Point3::offset_ray_origin (point3.rs:31-49)
 BG_D V3 offset_ray_origin(V3 p, V3 perr, V3 n, V3 w) {
     V3 offset = dot(vabs(n), perr) * n;
@@ -325,11 +503,14 @@ BG_D bool prim_isect(const Scene& sc, int prim, const Ray& ray, Isect* it) {
         TriHit h;
         if (!tri_test(tr, INFINITY, p0, p1, p2, &h)) return false;
         tri_isect(p0, p1, p2, h, ray, it);
-    } else {
+    } else if ((uint32_t)prim < sc.ntri + sc.nsph) {
         float4 s = sc.sph[prim - sc.ntri];
         SphHit h;
         if (!sphere_test(s, ray, INFINITY, &h)) return false;
         sphere_isect(s, h, ray, it);
+    } else {
+        float t;
+        if (!quadric_hit(sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph), ray, INFINITY, &t, it)) return false;
     }
     it->prim = prim;
     return true;

@@ -52,9 +52,15 @@ BG_D bool prim_hit(const Scene& sc, uint32_t prim, const TriRay& tr, Ray& ray, b
         if (closest) ray.t_max = h.t;
         return true;
     }
-    SphHit h;
-    if (!sphere_test(sc.sph[prim - sc.ntri], ray, ray.t_max, closest ? &h : nullptr)) return false;
-    if (closest) ray.t_max = h.t;
+    if (prim < sc.ntri + sc.nsph) {
+        SphHit h;
+        if (!sphere_test(sc.sph[prim - sc.ntri], ray, ray.t_max, closest ? &h : nullptr)) return false;
+        if (closest) ray.t_max = h.t;
+        return true;
+    }
+    float t;
+    if (!quadric_hit(sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph), ray, ray.t_max, &t, nullptr)) return false;
+    if (closest) ray.t_max = t;
     return true;
 }
 
@@ -141,11 +147,20 @@ BG_D float box_enter(float lox, float hix, float loy, float hiy, float loz, floa
     return (tn <= tf && tn < t_max) ? tn : INFINITY;
 }
 
-// Leaf slot: triangle = (p0, id) (p1, -) (p2, -); sphere = (center, id | SPHERE_BIT) (radius, -, -, -).
+// Leaf slot: triangle = (p0, id) (p1, -) (p2, -); sphere = (center, id | SPHERE_BIT) (radius, -, -, -);
+// quadric = (-, -, -, id | QUADRIC_BIT), the record itself lives in sc.quads.
 BG_D bool leaf_prim_hit(const Scene& sc, uint32_t slot, const TriRay& tr, Ray& ray, bool closest, int* prim) {
     float4 a = __ldg(&sc.leaf_prims[3 * slot]);
     float4 b = __ldg(&sc.leaf_prims[3 * slot + 1]);
     uint32_t id = __float_as_uint(a.w);
+    if (id & QUADRIC_BIT) {
+        uint32_t qi = id & ~QUADRIC_BIT;
+        float t;
+        if (!quadric_hit(sc.quads + QUADRIC_F4 * qi, ray, ray.t_max, &t, nullptr)) return false;
+        if (closest) ray.t_max = t;
+        *prim = (int)(qi + sc.ntri + sc.nsph);
+        return true;
+    }
     if (!(id & SPHERE_BIT)) {
         float4 c = __ldg(&sc.leaf_prims[3 * slot + 2]);
         TriHit h;
@@ -523,7 +538,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         while (tgroup.y != 0) {
             const uint32_t bit = 31u - __clz(tgroup.y);
             tgroup.y &= ~(1u << bit);
-            if (tgroup.x + bit >= sc.ntri + sc.nsph) {
+            if (tgroup.x + bit >= sc.ntri + sc.nsph + sc.nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
                 continue;
             }

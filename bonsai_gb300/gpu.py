@@ -103,6 +103,9 @@ class Scene:
         if sd.nsph:
             sp = np.ascontiguousarray(sd.spheres)
             ctx.check(lib.bg_scene_add_spheres(h, _ptr(sp), sd.nsph))
+        if len(sd.quadrics):
+            qu = np.ascontiguousarray(sd.quadrics)
+            ctx.check(lib.bg_scene_add_quadrics(h, _ptr(qu), len(qu)))
         st = A.bg_build_stats()
         ctx.check(lib.bg_scene_commit(h, bvh, C.byref(st)))
         self.build_ms, self.nodes, self.bvh = st.build_ms, st.nodes, bvh

@@ -22,10 +22,15 @@ MATERIAL_DT = np.dtype([("type", "<u4"), ("kd", "<f4", 3), ("ks", "<f4", 3), ("r
 LIGHT_DT = np.dtype([("intensity", "<f4", 3), ("two_sided", "<u4")])
 SPHERE_DT = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("material_id", "<u4"),
                       ("light_id", "<i4")])
+QUADRIC_DT = np.dtype([("kind", "<u4"), ("reverse_orientation", "<u4"), ("object_to_world", "<f4", 12),
+                       ("world_to_object", "<f4", 12), ("radius", "<f4"), ("inner_radius", "<f4"),
+                       ("z_min", "<f4"), ("z_max", "<f4"), ("height", "<f4"), ("phi_max_deg", "<f4"),
+                       ("material_id", "<u4"), ("light_id", "<i4")])
 RAY_DT = np.dtype([("org", "<f4", 3), ("tmax", "<f4"), ("dir", "<f4", 3), ("pad", "<f4")])
 HIT_DT = np.dtype([("prim", "<i4"), ("t", "<f4")])
 
 MATTE, PLASTIC, CONDUCTOR, DIELECTRIC = 0, 1, 2, 3
+CYLINDER, DISK, CONE = 0, 1, 2
 
 # Conductor constants (copper, RGB): one fixed triple used identically on CPU and GPU.
 COPPER_ETA = (0.200438, 0.924033, 1.10221)
@@ -44,6 +49,40 @@ def material(kind: int, kd=(0, 0, 0), ks=(0, 0, 0), roughness=0.0, remap=False,
     m["k"] = k
     m["ior"] = ior
     return m
+
+
+def rotation(axis, deg: float) -> np.ndarray:
+    """4x4 rotation about `axis` by `deg` degrees (Transform::rotate, src/base/transform.rs:100-116)."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    t = np.radians(deg)
+    c, s_ = np.cos(t), np.sin(t)
+    x, y, z = a
+    m = np.eye(4)
+    m[:3, :3] = [[x * x + (1 - x * x) * c, x * y * (1 - c) - z * s_, x * z * (1 - c) + y * s_],
+                 [x * y * (1 - c) + z * s_, y * y + (1 - y * y) * c, y * z * (1 - c) - x * s_],
+                 [x * z * (1 - c) - y * s_, y * z * (1 - c) + x * s_, z * z + (1 - z * z) * c]]
+    return m
+
+
+def translation(t) -> np.ndarray:
+    m = np.eye(4)
+    m[:3, 3] = t
+    return m
+
+
+def quadric(kind: int, object_to_world: np.ndarray, material_id: int, radius: float = 1.0,
+            inner_radius: float = 0.0, z_min: float = -1.0, z_max: float = 1.0, height: float = 1.0,
+            phi_max_deg: float = 360.0, reverse: bool = False) -> np.ndarray:
+    q = np.zeros((), QUADRIC_DT)
+    q["kind"] = kind
+    q["reverse_orientation"] = int(reverse)
+    m = np.asarray(object_to_world, np.float64)
+    q["object_to_world"] = m[:3, :4].astype(np.float32).ravel()
+    q["world_to_object"] = np.linalg.inv(m)[:3, :4].astype(np.float32).ravel()
+    q["radius"], q["inner_radius"], q["z_min"], q["z_max"] = radius, inner_radius, z_min, z_max
+    q["height"], q["phi_max_deg"], q["material_id"], q["light_id"] = height, phi_max_deg, material_id, -1
+    return q
 
 
 @dataclass
@@ -68,6 +107,7 @@ class SceneData:
     materials: np.ndarray                # (nmat,) MATERIAL_DT
     lights: np.ndarray                   # (nlights,) LIGHT_DT
     camera: Camera | None = None
+    quadrics: np.ndarray = field(default_factory=lambda: np.zeros(0, QUADRIC_DT))
     spp: int = 16
     max_depth: int = 5
     rr_threshold: float = 1.0
@@ -128,6 +168,26 @@ def cornell(width: int = 256, height: int = 256, spp: int = 16, max_depth: int =
     cam = Camera((0.0, 0.0, 3.5), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
     return SceneData(tri, np.asarray(tmat, np.uint32), tri_light, sph, np.stack(mats), lights, cam,
                      spp=spp, max_depth=max_depth, rr_threshold=1.0, name="cornell")
+
+
+def quadric_box(width: int = 64, height: int = 64, spp: int = 8, max_depth: int = 5) -> SceneData:
+    """The Cornell box with a cylinder, a disk and a cone (rotated and partial) in place of the
+    spheres: exercises the quadric shapes (src/shapes/{cylinder,disk,cone}.rs)."""
+    sd = cornell(width, height, spp, max_depth)
+    mats = list(sd.materials) + [material(MATTE, kd=(0.3, 0.6, 0.8)), material(PLASTIC, kd=(0.6, 0.3, 0.2),
+                                                                              ks=(0.4, 0.4, 0.4), roughness=0.2)]
+    m_cyl, m_pl = len(mats) - 2, len(mats) - 1
+    q = [quadric(CYLINDER, translation((-0.45, -0.5, -0.2)) @ rotation((1, 0, 0), -90), m_cyl, radius=0.25,
+                 z_min=-0.5, z_max=0.3, phi_max_deg=300.0),
+         quadric(DISK, translation((0.4, -0.6, 0.2)) @ rotation((1, 0, 0), -70), m_pl, radius=0.3, inner_radius=0.1,
+                 height=0.0, phi_max_deg=360.0),
+         quadric(CONE, translation((0.1, -1.0, -0.5)) @ rotation((1, 0, 0), -90), 3, radius=0.3, height=0.8,
+                 phi_max_deg=330.0)]
+    sd.materials = np.stack(mats)
+    sd.quadrics = np.stack(q)
+    sd.spheres = np.zeros(0, SPHERE_DT)
+    sd.name = "quadric_box"
+    return sd
 
 
 def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:

@@ -81,6 +81,26 @@ typedef struct bg_sphere {
     int32_t light_id; /* must be -1: spherical emitters are not supported */
 } bg_sphere;
 
+/* Quadric shapes (src/shapes/{cylinder,disk,cone}.rs) with an affine object_to_world transform.
+ * Both matrices are given, as the reference's Transform{m, m_inverse}: row-major 3x4 (the bottom
+ * row is 0 0 0 1).  Cylinder: radius, z_min, z_max, phi_max; Disk: height, radius, inner_radius,
+ * phi_max; Cone: radius, height, phi_max (degrees, clamped to [0, 360]). */
+typedef enum bg_quadric_kind { BG_QUADRIC_CYLINDER = 0, BG_QUADRIC_DISK = 1, BG_QUADRIC_CONE = 2 } bg_quadric_kind;
+typedef struct bg_quadric {
+    uint32_t kind;
+    uint32_t reverse_orientation;
+    float object_to_world[12];
+    float world_to_object[12];
+    float radius;
+    float inner_radius;
+    float z_min;
+    float z_max;
+    float height;
+    float phi_max_deg;
+    uint32_t material_id;
+    int32_t light_id; /* must be -1: quadric emitters are not supported */
+} bg_quadric;
+
 /* PerspectiveCamera options (src/cameras/perspective.rs:36-46) with the camera_to_world
  * transform given as Transform::look_at(position, look_at, up) (src/base/transform.rs:152-189),
  * shutter [0,1], and film Film{full_resolution=(width,height), crop [0,1]^2, BoxFilter r=0.5,
@@ -136,7 +156,7 @@ typedef struct bg_ray {
 } bg_ray;
 
 typedef struct bg_hit {
-    int32_t prim; /* triangles 0..ntri-1 in insertion order, then spheres; -1 = miss */
+    int32_t prim; /* triangles 0..ntri-1 in insertion order, then spheres, then quadrics; -1 = miss */
     float t;
 } bg_hit;
 
@@ -190,6 +210,8 @@ bg_status bg_scene_add_area_light(bg_scene* scene, const bg_area_light* l, uint3
 bg_status bg_scene_add_triangles(bg_scene* scene, const float* xyz, size_t ntri,
                                  const uint32_t* material_ids, const int32_t* light_ids);
 bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t n);
+/* Appends n cylinders / disks / cones (GeometricPrimitive{Cylinder|Disk|Cone, material}). */
+bg_status bg_scene_add_quadrics(bg_scene* scene, const bg_quadric* quadrics, size_t n);
 /* Builds the BVH on the host, uploads scene and BVH to the device. */
 bg_status bg_scene_commit(bg_scene* scene, uint32_t bvh_kind, bg_build_stats* stats);
 

@@ -35,7 +35,8 @@ def lib() -> C.CDLL:
         L = C.CDLL(str(LIB))
         P = C.c_void_p
         L.orc_scene_create.restype = P
-        L.orc_scene_create.argtypes = [P, C.c_int64, P, P, P, C.c_int64, P, C.c_int32, P, C.c_int32, C.c_int32]
+        L.orc_scene_create.argtypes = [P, C.c_int64, P, P, P, C.c_int64, P, C.c_int32, P, C.c_int32, C.c_int32,
+                                       P, C.c_int64]
         L.orc_scene_destroy.argtypes = [P]
         L.orc_bvh_nodes.restype = C.c_int64
         L.orc_bvh_nodes.argtypes = [P]
@@ -81,11 +82,12 @@ class OracleScene:
         self.sd = sd
         self._keep = [np.ascontiguousarray(sd.tri, np.float32), np.ascontiguousarray(sd.tri_mat, np.uint32),
                       np.ascontiguousarray(sd.tri_light, np.int32), np.ascontiguousarray(sd.spheres),
-                      np.ascontiguousarray(sd.materials), np.ascontiguousarray(sd.lights)]
-        t, tm, tl, sp, ma, li = self._keep
+                      np.ascontiguousarray(sd.materials), np.ascontiguousarray(sd.lights),
+                      np.ascontiguousarray(sd.quadrics)]
+        t, tm, tl, sp, ma, li, qu = self._keep
         self.h = lib().orc_scene_create(_ptr(t), sd.ntri, _ptr(tm), _ptr(tl), _ptr(sp) if len(sp) else None,
                                         sd.nsph, _ptr(ma), len(ma), _ptr(li) if len(li) else None, len(li),
-                                        int(fixed_bvh))
+                                        int(fixed_bvh), _ptr(qu) if len(qu) else None, len(qu))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -309,9 +309,18 @@ struct Sphere {  // src/shapes/sphere.rs:38-64 (translation-only object_to_world
     float radius, z_min, z_max, theta_min, theta_max, phi_max;
     uint32_t mat;
 };
+// Cylinder / Disk / Cone (src/shapes/{cylinder,disk,cone}.rs) with an affine transform.
+struct Quadric {
+    int kind;  // 0 cylinder, 1 disk, 2 cone
+    Transform o2w, w2o;
+    bool reverse, swaps;
+    float radius, inner, z_min, z_max, height, phi_max;
+    uint32_t mat;
+};
 struct Scene {
     std::vector<V3> pos;  // 3 per triangle (TriangleMesh::position, triangle.rs:17-22)
-    int64_t ntri = 0, nsph = 0;
+    int64_t ntri = 0, nsph = 0, nquad = 0;
+    std::vector<Quadric> quads;
     std::vector<uint32_t> tri_mat;
     std::vector<int32_t> prim_emission;  // emission record per primitive or -1
     std::vector<int32_t> prim_light;     // light-list index per primitive or -1
@@ -328,7 +337,7 @@ struct Scene {
     };
     std::vector<Node> nodes;
     std::vector<uint32_t> order;  // ordered_primitives
-    int64_t nprims() const { return ntri + nsph; }
+    int64_t nprims() const { return ntri + nsph + nquad; }
 };
 
 struct Counters {
@@ -515,11 +524,116 @@ static bool sphere_intersect(const Sphere& sp, const Ray& r_world, float* t_hit,
     return true;
 }
 
+// ---------------------------------------------------------------- quadrics
+inline float absolute_error(const EFloat& e) {  // efloat.rs absolute_error
+    return next_float_up(rmax(std::fabs(e.high - e.v), std::fabs(e.v - e.low)));
+}
+// Interaction::new (interaction.rs:57-100) + Interaction::transform (interaction.rs:268-300)
+static void quadric_interaction(const Quadric& q, V3 ph, V3 perr, const Ray& ray, V3 dpdu, V3 dpdv, Interaction* it) {
+    V3 n = normalize(cross(dpdu, dpdv));
+    if (q.reverse ^ q.swaps) n = n * -1.0f;
+    V3 abs_err;
+    it->p = xf_point_perr(q.o2w, ph, perr, &abs_err);
+    it->p_err = abs_err;
+    it->time = ray.time;
+    it->wo = xf_vec(q.o2w, -ray.d);
+    it->n = normalize(xf_normal(q.o2w, n));
+    it->surface = true;
+    it->dpdu = xf_vec(q.o2w, dpdu);
+    it->shading_n = face_forward(normalize(xf_normal(q.o2w, n)), it->n);
+    it->shading_dpdu = it->dpdu;
+}
+static bool quadric_intersect(const Quadric& q, const Ray& rw, float* t_hit, Interaction* it, bool test_only) {
+    V3 oe, de;
+    Ray ray = xf_ray_err(q.w2o, rw, &oe, &de);
+    if (q.kind == 1) {  // Disk::intersect (disk.rs:70-144)
+        if (ray.d.z == 0.0f) return false;
+        float tsh = (q.height - ray.o.z) / ray.d.z;
+        if (tsh <= 0.0f || tsh >= ray.t_max) return false;
+        V3 ph = ray.o + ray.d * tsh;
+        float dist = ph.x * ph.x + ph.y * ph.y;
+        if (dist > q.radius * q.radius || dist < q.inner * q.inner) return false;
+        float phi = std::atan2(ph.y, ph.x);
+        if (phi < 0.0f) phi += 2.0f * PI;
+        if (phi > q.phi_max) return false;
+        if (test_only) return true;
+        float rh = std::sqrt(dist);
+        V3 dpdu(-q.phi_max * ph.y, q.phi_max * ph.x, 0.0f);
+        V3 dpdv = V3(ph.x, ph.y, 0.0f) * (q.inner - q.radius) / rh;
+        ph.z = q.height;
+        quadric_interaction(q, ph, V3(0, 0, 0), ray, dpdu, dpdv, it);
+        *t_hit = tsh;
+        return true;
+    }
+    EFloat ox(ray.o.x, oe.x), oy(ray.o.y, oe.y), oz(ray.o.z, oe.z);
+    EFloat dx(ray.d.x, de.x), dy(ray.d.y, de.y), dz(ray.d.z, de.z);
+    EFloat a, b, c;
+    if (q.kind == 0) {  // cylinder.rs:71-90
+        a = dx * dx + dy * dy;
+        b = ef(2.0f) * (dx * ox + dy * oy);
+        c = ox * ox + oy * oy - EFloat(q.radius, 0.0f) * EFloat(q.radius, 0.0f);
+    } else {  // cone.rs:67-95
+        EFloat k = EFloat(q.radius, 0.0f) / EFloat(q.height, 0.0f);
+        k = k * k;
+        a = dx * dx + dy * dy - k * dz * dz;
+        b = ef(2.0f) * (dx * ox + dy * oy - k * dz * (oz - ef(q.height)));
+        c = ox * ox + oy * oy - k * (oz - ef(q.height)) * (oz - ef(q.height));
+    }
+    EFloat t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0.high > ray.t_max || t1.low <= 0.0f) return false;
+    EFloat tsh = t0;
+    if (tsh.low <= 0.0f) {
+        tsh = t1;
+        if (tsh.high > ray.t_max) return false;
+    }
+    auto hit_point = [&](const EFloat& t) {
+        V3 ph = ray.o + ray.d * t.v;
+        if (q.kind == 0) {  // refine onto the cylinder
+            float hr = std::sqrt(ph.x * ph.x + ph.y * ph.y);
+            ph.x *= q.radius / hr;
+            ph.y *= q.radius / hr;
+        }
+        return ph;
+    };
+    auto clipped = [&](V3 ph, float phi) {
+        if (q.kind == 0) return ph.z < q.z_min || ph.z > q.z_max || phi > q.phi_max;
+        return ph.z < 0.0f || ph.z > q.height || phi > q.phi_max;
+    };
+    V3 ph = hit_point(tsh);
+    float phi = std::atan2(ph.y, ph.x);
+    if (phi < 0.0f) phi += 2.0f * PI;
+    if (clipped(ph, phi)) {
+        if (tsh.v == t1.v && tsh.low == t1.low && tsh.high == t1.high) return false;
+        if (t1.high > ray.t_max) return false;
+        tsh = t1;
+        ph = hit_point(tsh);
+        phi = std::atan2(ph.y, ph.x);
+        if (phi < 0.0f) phi += 2.0f * PI;
+        if (clipped(ph, phi)) return false;
+    }
+    if (test_only) return true;
+    V3 dpdu(-q.phi_max * ph.y, q.phi_max * ph.x, 0.0f), dpdv, perr;
+    if (q.kind == 0) {
+        dpdv = V3(0.0f, 0.0f, q.z_max - q.z_min);
+        perr = gamma(3.0f) * vabs(V3(ph.x, ph.y, 0.0f));
+    } else {
+        float v = ph.z / q.height;
+        dpdv = V3(-ph.x / (1.0f - v), -ph.y / (1.0f - v), q.height);
+        EFloat px = ox + tsh * dx, py = oy + tsh * dy, pz = oz + tsh * dz;
+        perr = V3(absolute_error(px), absolute_error(py), absolute_error(pz));
+    }
+    quadric_interaction(q, ph, perr, ray, dpdu, dpdv, it);
+    *t_hit = tsh.v;
+    return true;
+}
+
 // ---------------------------------------------------------------- primitives + BVH
 static bool prim_intersect(const Scene& s, int64_t prim, Ray& ray, Interaction* it) {
     float t;  // GeometricPrimitive::intersect (geometric.rs:27-38)
     bool ok = prim < s.ntri ? tri_intersect(s, prim, ray, &t, it, false)
-                            : sphere_intersect(s.sph[prim - s.ntri], ray, &t, it, false);
+              : prim < s.ntri + s.nsph ? sphere_intersect(s.sph[prim - s.ntri], ray, &t, it, false)
+                                       : quadric_intersect(s.quads[prim - s.ntri - s.nsph], ray, &t, it, false);
     if (!ok) return false;
     ray.t_max = t;
     it->prim = (int)prim;
@@ -528,8 +642,9 @@ static bool prim_intersect(const Scene& s, int64_t prim, Ray& ray, Interaction* 
 static bool prim_intersect_test(const Scene& s, int64_t prim, const Ray& ray) {
     float t;
     Interaction dummy;
-    return prim < s.ntri ? tri_intersect(s, prim, ray, &t, &dummy, true)
-                         : sphere_intersect(s.sph[prim - s.ntri], ray, &t, &dummy, true);
+    if (prim < s.ntri) return tri_intersect(s, prim, ray, &t, &dummy, true);
+    if (prim < s.ntri + s.nsph) return sphere_intersect(s.sph[prim - s.ntri], ray, &t, &dummy, true);
+    return quadric_intersect(s.quads[prim - s.ntri - s.nsph], ray, &t, &dummy, true);
 }
 static Bounds3 prim_bounds(const Scene& s, int64_t prim) {
     Bounds3 b;
@@ -542,13 +657,26 @@ static Bounds3 prim_bounds(const Scene& s, int64_t prim) {
         b.unite(p2);
         return b;
     }
-    const Sphere& sp = s.sph[prim - s.ntri];  // sphere.rs:68-78, transform.rs:75-86
-    V3 lo(-sp.radius, -sp.radius, sp.z_min), hi(sp.radius, sp.radius, sp.z_max);
-    V3 c0 = xf_point(sp.o2w, lo);
+    const Transform* o2w;
+    V3 lo, hi;
+    if (prim < s.ntri + s.nsph) {
+        const Sphere& sp = s.sph[prim - s.ntri];  // sphere.rs:68-78
+        o2w = &sp.o2w;
+        lo = V3(-sp.radius, -sp.radius, sp.z_min);
+        hi = V3(sp.radius, sp.radius, sp.z_max);
+    } else {
+        const Quadric& q = s.quads[prim - s.ntri - s.nsph];  // cylinder.rs:61-66, disk.rs:57-62, cone.rs:57-62
+        o2w = &q.o2w;
+        if (q.kind == 0) { lo = V3(-q.radius, -q.radius, q.z_min); hi = V3(q.radius, q.radius, q.z_max); }
+        else if (q.kind == 1) { lo = V3(-q.radius, -q.radius, q.height); hi = V3(q.radius, q.radius, q.height); }
+        else { lo = V3(-q.radius, -q.radius, 0.0f); hi = V3(q.radius, q.radius, q.height); }
+    }
+    // Transform::transform_bounds (transform.rs:75-86)
+    V3 c0 = xf_point(*o2w, lo);
     b.mn = c0; b.mx = c0;
     const V3 corners[7] = {{hi.x, lo.y, lo.z}, {lo.x, hi.y, lo.z}, {lo.x, lo.y, hi.z}, {lo.x, hi.y, hi.z},
                            {hi.x, hi.y, lo.z}, {hi.x, lo.y, hi.z}, {hi.x, hi.y, hi.z}};
-    for (const V3& c : corners) b.unite(xf_point(sp.o2w, c));
+    for (const V3& c : corners) b.unite(xf_point(*o2w, c));
     return b;
 }
 
@@ -1059,7 +1187,9 @@ struct BSDF {  // src/base/bsdf.rs
 // Material::compute_scattering_functions (materials/matte.rs:19-41, plastic.rs:65-95 and the
 // composed conductor / dielectric)
 static BSDF make_bsdf(const Scene& s, const Interaction& it) {
-    const bg_material& m = s.mats[it.prim < s.ntri ? s.tri_mat[it.prim] : s.sph[it.prim - s.ntri].mat];
+    const bg_material& m = s.mats[it.prim < s.ntri ? s.tri_mat[it.prim]
+                                  : it.prim < s.ntri + s.nsph ? s.sph[it.prim - s.ntri].mat
+                                                              : s.quads[it.prim - s.ntri - s.nsph].mat];
     BSDF b;
     b.ns = it.shading_n;
     b.ng = it.n;
@@ -1329,17 +1459,19 @@ extern "C" {
 
 void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_mat, const int32_t* tri_light,
                        const bg_sphere* sph, int64_t nsph, const bg_material* mats, int32_t nmat,
-                       const bg_area_light* emis, int32_t nemis, int32_t bvh_fixed) {
+                       const bg_area_light* emis, int32_t nemis, int32_t bvh_fixed, const bg_quadric* quads,
+                       int64_t nquad) {
     Scene* s = new Scene();
     s->ntri = ntri;
     s->nsph = nsph;
+    s->nquad = nquad;
     s->pos.resize(3 * ntri);
     for (int64_t i = 0; i < 3 * ntri; ++i) s->pos[i] = V3(tri_xyz[3 * i], tri_xyz[3 * i + 1], tri_xyz[3 * i + 2]);
     s->tri_mat.assign(tri_mat, tri_mat + ntri);
     s->mats.assign(mats, mats + nmat);
     s->emis.assign(emis, emis + nemis);
-    s->prim_emission.assign(ntri + nsph, -1);
-    s->prim_light.assign(ntri + nsph, -1);
+    s->prim_emission.assign(ntri + nsph + nquad, -1);
+    s->prim_light.assign(ntri + nsph + nquad, -1);
     for (int64_t i = 0; i < ntri; ++i) {
         if (tri_light && tri_light[i] >= 0) {
             s->prim_emission[i] = tri_light[i];
@@ -1361,6 +1493,34 @@ void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_m
         sp.phi_max = rclamp(360.0f, 0.0f, 360.0f) * (PI / 180.0f);
         sp.mat = sph[i].material_id;
         s->sph.push_back(sp);
+    }
+    for (int64_t i = 0; i < nquad; ++i) {
+        const bg_quadric& g = quads[i];
+        Quadric q;
+        q.kind = (int)g.kind;
+        q.o2w.m = Mat4::identity();
+        q.w2o.m = Mat4::identity();
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 4; ++c) {
+                q.o2w.m.m[r][c] = g.object_to_world[4 * r + c];
+                q.w2o.m.m[r][c] = g.world_to_object[4 * r + c];
+            }
+        q.o2w.mi = q.w2o.m;
+        q.w2o.mi = q.o2w.m;
+        if (is_identity(q.o2w)) q.w2o = q.o2w;  // cylinder.rs:37-41
+        const auto& m = q.o2w.m.m;  // Transform::swaps_handedness (transform.rs:212-218)
+        float det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                    m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        q.swaps = det < 0.0f;
+        q.reverse = g.reverse_orientation != 0;
+        q.radius = g.radius;
+        q.inner = g.inner_radius;
+        q.z_min = rmin(g.z_min, g.z_max);
+        q.z_max = rmax(g.z_min, g.z_max);
+        q.height = g.height;
+        q.phi_max = rclamp(g.phi_max_deg, 0.0f, 360.0f) * (PI / 180.0f);
+        q.mat = g.material_id;
+        s->quads.push_back(q);
     }
     build_bvh(*s, bvh_fixed != 0);
     return s;

@@ -46,6 +46,15 @@ def render_case():
     return out
 
 
+def quadric_case():
+    sd = S.quadric_box(16, 16, spp=4)
+    out = {}
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=False).render(mode, seed=9, threads=1)
+        out[f"sum_{mode}"] = r["sum"]
+    return out
+
+
 def rng_case():
     idx = np.array([(0, 0, 0, 0), (1, 2, 3, 4), (12345, 999, 7, 41), (2**32 - 1, 2**31, 65535, 1023)], np.uint64)
     vals = np.array([O.rng_uniform(int(s), int(p), int(n), int(d)) for s, p, n, d in idx], np.float32)
@@ -56,4 +65,5 @@ if __name__ == "__main__":
     np.savez_compressed(HERE / "oracle_trace.npz", **trace_case())
     np.savez_compressed(HERE / "oracle_render.npz", **render_case())
     np.savez_compressed(HERE / "oracle_rng.npz", **rng_case())
+    np.savez_compressed(HERE / "oracle_quadric.npz", **quadric_case())
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))

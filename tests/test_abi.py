@@ -14,7 +14,7 @@ from .conftest import ROOT
 
 HEADER = ROOT / "include" / "bonsai_gpu.h"
 STRUCTS = ["bg_material", "bg_area_light", "bg_sphere", "bg_camera", "bg_render_opts", "bg_render_stats",
-           "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning"]
+           "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning", "bg_quadric"]
 
 
 def declared_functions():

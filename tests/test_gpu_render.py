@@ -58,3 +58,12 @@ def test_production_small_pbrt(gpu_ctx, bvh):
     print(cmp)
     assert cmp["frac_z3"] <= Z3_FRAC
     assert cmp["frac_close"] >= 0.8
+
+
+@pytest.mark.parametrize("mode,bvh", [(A.BG_MODE_PBRT, A.BG_BVH_WIDE), (A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE)])
+def test_quadric_box(gpu_ctx, mode, bvh):
+    sd = S.quadric_box(48, 48, spp=8)
+    r, o, cmp = _render_pair(gpu_ctx, sd, mode, bvh, 8)
+    print(cmp)
+    assert cmp["frac_z3"] <= Z3_FRAC
+    assert cmp["frac_close"] >= 0.9

@@ -108,3 +108,23 @@ def test_faithful_reference_build_exact(gpu_ctx):
     r2 = rays.copy()
     r2["tmax"] = np.where(ref["prim"] >= 0, ref["t"], np.inf)
     assert (sc.trace(r2)["prim"] != orc.trace(r2)["prim"]).sum() == 0
+
+
+@pytest.mark.parametrize("bvh", [A.BG_BVH_WIDE, A.BG_BVH_WIDE2, A.BG_BVH_REFERENCE_FIXED])
+def test_quadrics_closest_and_any(gpu_ctx, bvh):
+    sd = S.quadric_box(16, 16)
+    rng = np.random.default_rng(5)
+    n = 60_000
+    rays = np.zeros(n, S.RAY_DT)
+    rays["org"] = rng.uniform(-0.95, 0.95, (n, 3)).astype(np.float32)
+    d = rng.standard_normal((n, 3))
+    rays["dir"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rays["tmax"] = np.inf
+    orc = O.OracleScene(sd, fixed_bvh=True)
+    ref, occ = orc.trace(rays), orc.trace(rays, any_hit=True)
+    first_quad = sd.ntri + sd.nsph
+    for k in range(3):  # every quadric is hit
+        assert (ref["prim"] == first_quad + k).sum() > 200
+    sc = G.Scene(gpu_ctx, sd, bvh)
+    _check_closest(sc.trace(rays), ref, exact=(bvh == A.BG_BVH_REFERENCE_FIXED))
+    assert (sc.trace(rays, any_hit=True) != occ).sum() == 0

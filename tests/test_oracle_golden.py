@@ -58,3 +58,11 @@ def test_render_golden():
     sd = S.production(24, 16, spp=2, n_ico=2, ico_level=2, n_spheres=20)
     r = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, seed=1, threads=1)
     np.testing.assert_allclose(r["sum"], g["production_sum"], rtol=RTOL, atol=1e-9)
+
+
+def test_quadric_render_golden():
+    g = np.load(GOLD / "oracle_quadric.npz")
+    sd = S.quadric_box(16, 16, spp=4)
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=False).render(mode, seed=9, threads=1)
+        np.testing.assert_allclose(r["sum"], g[f"sum_{mode}"], rtol=RTOL, atol=1e-9)
