@@ -70,7 +70,7 @@ def config_of(sd, small: bool) -> dict:
                     f"{sd.nsph} spheres, {sd.camera.width}x{sd.camera.height}, {sd.spp} spp, max depth "
                     f"{sd.max_depth}, RR after depth 3, PBRT estimator",
         "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
-        "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "2-wide SAH (binned, 32 bins, <=8 prims/leaf)",
+        "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "8-wide compressed (80 B nodes, 8-bit child boxes, <=3 prims per leaf)", "graph": "wave chain captured as a CUDA graph",
         "l2": "flushed before every step (512 MB device write)",
         "parallelism": "replicas",
     }
@@ -251,7 +251,7 @@ def run_ours(args):
         tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "ms")} | {
             "cached": bool(tuning.get("cached", False))}
     for _ in range(args.warmup):
-        pi.render(scene, readback=False)
+        pi.render(scene, readback=False, graph=True)
     clocks = Clocks(local)
     barrier(dist)
     ctx.synchronize()
@@ -259,7 +259,7 @@ def run_ours(args):
     dev_ms, launches, wall0 = 0.0, 0, time.time()
     for k in range(args.steps):
         ctx.flush_l2()
-        r = pi.render(scene, readback=False, first_sample=k * sd.spp)
+        r = pi.render(scene, readback=False, first_sample=k * sd.spp, graph=True)
         dev_ms += r.stats.device_ms
         launches += r.stats.launches
         if r.stats.error_word:
@@ -275,8 +275,13 @@ def run_ours(args):
     barrier(dist)
     t0 = time.time()
     for k in range(args.steps):
-        pi.render(scene, readback=True, first_sample=k * sd.spp)
+        pi.render(scene, readback=True, first_sample=k * sd.spp, graph=True)
     e2e_s = max_over_ranks(dist, time.time() - t0)
+
+    # the plain wavefront arm (kernel launches, no graph) at the same tuning, one timed frame
+    ctx.flush_l2()
+    plain = pi.render(scene, readback=False)
+    plain_msps = samples / (plain.stats.device_ms / 1e3) / 1e6
     e2e = ws * args.steps * samples / e2e_s / 1e6
 
     # stage timing pass (outside the timed region): dominant-kernel duration and ray counts
@@ -316,7 +321,7 @@ def run_ours(args):
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
-        "extra": {"wall_s_timed_loop": wall, "scene_upload_and_bvh_build_s": upload_build_s,
+        "extra": {"plain_wavefront_msamples_per_s": plain_msps, "wall_s_timed_loop": wall, "scene_upload_and_bvh_build_s": upload_build_s,
                   "bvh_build_ms": scene.build_ms, "bvh_nodes": int(scene.nodes),
                   "extension_rays_per_frame": int(st.extension_rays), "shadow_rays_per_frame": int(st.shadow_rays),
                   "Mrays_per_s": (st.extension_rays + st.shadow_rays) / (st.device_ms / 1e3) / 1e6,

@@ -52,6 +52,10 @@ struct bg_ctx {
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     cudaEvent_t stage_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> timing_ev;
+    // captured wave chain (BG_RENDER_GRAPH) and the launch parameters it was captured with
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<unsigned char> graph_key;
+    int graph_kernels = 0;
     std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
 };
 
@@ -325,6 +329,7 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(done, n * sizeof(uint32_t));
     WB(counters, 16 * sizeof(uint32_t));
     WB(ray_stats, 4 * sizeof(unsigned long long));
+    WB(wavectl, 4 * sizeof(uint32_t));
 #undef WB
     w.capacity = cap;
     return BG_OK;
@@ -443,6 +448,7 @@ void bg_destroy(bg_ctx* ctx) {
     for (auto ev : ctx->stage_ev)
         if (ev) cudaEventDestroy(ev);
     for (auto ev : ctx->timing_ev) cudaEventDestroy(ev);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -856,7 +862,49 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     }
     if (wavefront) CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
     CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
-    if (total > 0) {
+    const bool use_graph = wavefront && !timing && (o->flags & BG_RENDER_GRAPH);
+    if (total > 0 && use_graph) {
+        // key: every launch parameter baked into the graph (first_sample travels in wavectl)
+        bg::RenderParams rk = rp;
+        rk.first_sample = 0;
+        std::vector<unsigned char> key;
+        auto put = [&](const void* p, size_t n) {
+            const unsigned char* b = static_cast<const unsigned char*>(p);
+            key.insert(key.end(), b, b + n);
+        };
+        put(&s->dev, sizeof(s->dev));
+        put(&dc, sizeof(dc));
+        put(&rk, sizeof(rk));
+        put(&ctx->film, sizeof(ctx->film));
+        put(&ctx->wave, sizeof(ctx->wave));
+        put(&ctx->shape, sizeof(ctx->shape));
+        put(&total, sizeof(total));
+        if (!ctx->graph_exec || key != ctx->graph_key) {
+            if (ctx->graph_exec) {
+                cudaGraphExecDestroy(ctx->graph_exec);
+                ctx->graph_exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            int nk = bg::launch_wave_chain(s->dev, dc, rp, ctx->film, ctx->wave, total, ctx->d_err, ctx->shape,
+                                           ctx->stream);
+            cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+            ce = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+            ctx->graph_key = key;
+            ctx->graph_kernels = nk;
+        }
+        uint32_t ctl[4] = {0u, o->first_sample, 0u, 0u};
+        CK(cudaMemcpyAsync(ctx->wave.wavectl, ctl, sizeof(ctl), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));  // ctl is a stack buffer
+        CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+        for (uint64_t w = 0; w < nwaves; ++w) {
+            CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+            launches += (uint64_t)ctx->graph_kernels;
+        }
+    } else if (total > 0) {
         if (wavefront) {
             uint64_t w = 0;
             for (uint64_t item0 = 0; item0 < total; item0 += cap, ++w) {

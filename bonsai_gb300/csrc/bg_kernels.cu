@@ -258,13 +258,14 @@ enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, 
 constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
 constexpr int CLS_MISS = 4;
 
-__global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
+BG_D void generate_paths(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint64_t item0,
+                         uint32_t nitems, uint32_t first_sample) {
     const uint64_t npix = (uint64_t)rp.width * rp.height;
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
         uint64_t item = item0 + i;
         uint32_t pix = (uint32_t)(item % npix);
-        uint32_t s = rp.first_sample + (uint32_t)(item / npix);
+        uint32_t s = first_sample + (uint32_t)(item / npix);
         Rng rng{pix, s, rp.seed};
         float c[4];
         rng.block(0, c);
@@ -279,6 +280,21 @@ __global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t
         wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         wb.queue[0][i] = i;
     }
+}
+
+__global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
+    generate_paths(cam, rp, wb, item0, nitems, rp.first_sample);
+}
+
+// Graph replay: the wave to generate comes from wb.wavectl (advanced by k_wave_advance).
+__global__ void k_generate_ctl(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t total) {
+    const uint64_t item0 = (uint64_t)wb.wavectl[0] * wb.capacity;
+    const uint32_t nitems = item0 >= total ? 0u : (uint32_t)min((uint64_t)wb.capacity, total - item0);
+    generate_paths(cam, rp, wb, item0, nitems, wb.wavectl[1]);
+}
+
+__global__ void k_wave_advance(WaveBuffers wb) {
+    if (threadIdx.x == 0) wb.wavectl[0] += 1;
 }
 
 __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
@@ -533,13 +549,10 @@ __global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, Wa
     }
 }
 
-int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
-                const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
-                cudaStream_t s, cudaEvent_t* ev) {
+static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
+                          uint32_t* err, const LaunchShape& ls, cudaStream_t s, cudaEvent_t* ev) {
     int launches = 0;
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
-    k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
-    ++launches;
     for (uint32_t b = 0; b <= rp.max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 0], s);
@@ -560,6 +573,23 @@ int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, cons
         launches += 10;
     }
     return launches;
+}
+
+int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
+                const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
+                cudaStream_t s, cudaEvent_t* ev) {
+    dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
+    k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
+    return 1 + launch_bounces(sc, rp, film, wb, err, ls, s, ev);
+}
+
+int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
+                      const WaveBuffers& wb, uint64_t total, uint32_t* err, const LaunchShape& ls, cudaStream_t s) {
+    dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
+    k_generate_ctl<<<grid, block, 0, s>>>(cam, rp, wb, total);
+    int n = 1 + launch_bounces(sc, rp, film, wb, err, ls, s, nullptr);
+    k_wave_advance<<<1, 32, 0, s>>>(wb);
+    return n + 1;
 }
 
 // ================================================================ film

@@ -47,6 +47,7 @@ struct WaveBuffers {
     uint32_t* counters; // [0,1] queue sizes, [2] shadow count, [3] done count, [4] extend head,
                         // [5] shadow head, [6..10] class queue sizes
     unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
+    uint32_t* wavectl;              // graph replay: [0] wave index, [1] first sample (device side)
 };
 
 struct LaunchShape {
@@ -67,6 +68,11 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                 const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
                 cudaStream_t s, cudaEvent_t* stage_events);
+// The same stage chain with the wave index and first sample read from wb.wavectl, advanced by the
+// chain itself: a static launch sequence that is captured once into a CUDA graph and replayed
+// for every wave.  Returns the number of kernels in the chain.
+int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
+                      const WaveBuffers& wb, uint64_t total, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
 void launch_resolve(const FilmBuffers& film, cudaStream_t s);
 void launch_clear_film(const FilmBuffers& film, cudaStream_t s);
 

@@ -165,7 +165,7 @@ class PathIntegrator:
         self.rr_threshold, self.mode, self.seed = rr_threshold, mode, seed
 
     def render(self, scene: Scene, first_sample: int = 0, accumulate: bool = False, readback: bool = True,
-               spp: int | None = None) -> RenderResult:
+               spp: int | None = None, graph: bool = False, stage_timing: bool = False) -> RenderResult:
         ctx = scene.ctx
         c = camera_struct(self.camera)
         o = A.bg_render_opts()
@@ -175,7 +175,8 @@ class PathIntegrator:
         o.mode = self.mode
         o.seed = self.seed
         o.first_sample = first_sample
-        o.flags = (A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK)
+        o.flags = ((A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK) |
+                   (A.BG_RENDER_GRAPH if graph else 0) | (A.BG_RENDER_STAGE_TIMING if stage_timing else 0))
         rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
         st = A.bg_render_stats()
         ctx.check(ctx.lib.bg_render(ctx.h, scene.h, C.byref(c), C.byref(o), _ptr(rgb), C.byref(st)))

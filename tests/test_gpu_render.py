@@ -67,3 +67,20 @@ def test_quadric_box(gpu_ctx, mode, bvh):
     print(cmp)
     assert cmp["frac_z3"] <= Z3_FRAC
     assert cmp["frac_close"] >= 0.9
+
+
+def test_graph_replay_matches_launches(gpu_ctx):
+    sd = S.production(96, 54, spp=4, n_ico=6, ico_level=3, n_spheres=300)
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    pi = G.PathIntegrator(sd.camera, 4, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=3)
+    from bonsai_gb300 import autotune
+    autotune.set_(gpu_ctx, 32, 8, 8192)  # several waves per render
+    try:
+        plain = pi.render(sc)
+        for first in (0, 4):  # the captured graph is reused; first_sample travels on the device
+            g = pi.render(sc, graph=True, first_sample=first)
+            ref = plain if first == 0 else pi.render(sc, first_sample=first)
+            np.testing.assert_allclose(g.rgb, ref.rgb, rtol=1e-6, atol=1e-7)
+            assert g.stats.launches > 4 * (sd.max_depth + 1)
+    finally:
+        autotune.set_(gpu_ctx, 32, 8, 1 << 22)
