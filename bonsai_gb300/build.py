@@ -35,8 +35,9 @@ def commands() -> tuple[list[list[str]], list[str]]:
     cmds, objs = [], []
     for src in CU_SOURCES:
         o = str(OBJ / (Path(src).stem + ".o"))
+        defines = os.environ.get("BONSAI_NVCC_DEFINES", "").split()  # -DNAME=VALUE traversal variants
         cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-warn-spills", "-c", str(CSRC / src), "-o", o])
+                     "-Xptxas", "-warn-spills", *defines, "-c", str(CSRC / src), "-o", o])
         objs.append(o)
     for src in CPP_SOURCES:
         o = str(OBJ / (Path(src).stem + ".o"))

@@ -372,12 +372,23 @@ BG_D void traverse_queue(const Scene& sc, uint32_t n, uint32_t* head, Src& src, 
 // (bit 24 + (slot ^ octinv)), so the highest bit is the nearest child for this ray's direction;
 // the lower 24 bits are leaf primitives relative to tri_base.  The stack holds node groups only.
 constexpr int STACK8 = 32;
+#ifndef BG_SMEM_STACK
+#define BG_SMEM_STACK 0
+#endif
 
 BG_D uint32_t sign_extend_bytes(uint32_t x) { return ((x & 0x80808080u) >> 7) * 0xFFu; }
-// Byte j of w as a float: one byte permute builds 0x4B0000bb = 2^23 + b, one exact subtraction.
+// Byte j of w as a float: one byte permute builds 0x4B0000bb = 2^23 + b, one exact subtraction
+// (BG_BYTE_PERM=0: shift, mask and integer conversion instead).
+#ifndef BG_BYTE_PERM
+#define BG_BYTE_PERM 0
+#endif
 BG_D float byte_as_float(uint32_t w, int j) {
+#if BG_BYTE_PERM
     const uint32_t sel = (uint32_t)j | (4u << 4) | (5u << 8) | (7u << 12);
     return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+#else
+    return (float)((w >> (8 * j)) & 0xFFu);
+#endif
 }
 
 struct Ray8 {
@@ -457,14 +468,23 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
 // The node-group stack lives in shared memory, entry k of thread t at smem[k * blockDim.x + t].
 // Triangle groups are postponed (pushed) while fewer than kPostpone lanes of the warp would test
 // triangles, so leaf work runs with more lanes at once (Ylitie et al. 2017, section 5).
-constexpr int kPostpone = 0;  // 0 disables postponement (measured neutral to slightly slower here)
+#ifndef BG_POSTPONE
+#define BG_POSTPONE 0
+#endif
+constexpr int kPostpone = BG_POSTPONE;  // 0 disables postponement
 
 template <bool ANY, class Src>
 BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill,
                           uint2* smem) {
     const uint32_t lane = threadIdx.x & 31u;
+#if BG_SMEM_STACK
     uint2* stack = smem + threadIdx.x;
     const uint32_t sstride = blockDim.x;
+#else
+    uint2 stack[STACK8];
+    const uint32_t sstride = 1;
+    (void)smem;
+#endif
     Ray ray;
     Ray8 r8;
     TriRay tr;
