@@ -299,7 +299,7 @@ def run_ours(args):
         return
     peak, peak_kind = measured_peaks()
     roof = {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
-            "kernel": "k_extend (closest-hit, 2-wide BVH)", "peak_source": peak_kind}
+            "kernel": "k_extend<8> (closest hit, 8-wide compressed BVH)", "peak_source": peak_kind}
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
