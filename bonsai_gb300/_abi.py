@@ -44,6 +44,13 @@ BG_NOALLOC_MAX_PIXELS = 512 * 512
 BG_NOALLOC_WAVE_PATHS = 65536
 BG_NOALLOC_SCRATCH_BYTES = 29099008
 
+BG_GUIDE_PARAMS = 24320
+BG_GUIDE_QUERY_FLOATS = 9
+BG_GUIDE_OUTPUTS = 41
+BG_GUIDE_SAMPLE_FLOATS = 16
+BG_GUIDE_NO_FALLBACK = 1
+BG_GUIDE_NO_TRAIN = 2
+
 F3 = C.c_float * 3
 
 
@@ -111,6 +118,20 @@ class bg_build_stats(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+class bg_guide_opts(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("alpha", C.c_float), ("batch_size", C.c_uint32), ("samples_per_pass", C.c_uint32),
+                ("warmup_passes", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class bg_guide_stats(C.Structure):
+    _fields_ = [("passes", C.c_uint32), ("guided_passes", C.c_uint32), ("fallback", C.c_uint32),
+                ("adam_steps", C.c_uint32), ("render_ms", C.c_double), ("train_ms", C.c_double),
+                ("last_loss", C.c_double), ("relvar_plain", C.c_double), ("relvar_guided", C.c_double),
+                ("ms_plain", C.c_double), ("ms_guided", C.c_double), ("records", C.c_uint64),
+                ("pool_samples", C.c_uint64)]
+
+
 P = C.c_void_p
 PP = C.POINTER(C.c_void_p)
 ST = C.c_int  # bg_status
@@ -145,6 +166,16 @@ SIGNATURES = {
     "bg_render_noalloc": (ST, [P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P, P]),
     "bg_get_tuning": (ST, [P, C.POINTER(bg_tuning)]),
     "bg_set_tuning": (ST, [P, C.POINTER(bg_tuning)]),
+    "bg_guide_create": (ST, [P, C.POINTER(bg_guide_opts), PP]),
+    "bg_guide_destroy": (None, [P]),
+    "bg_guide_get_params": (ST, [P, P]),
+    "bg_guide_set_params": (ST, [P, P]),
+    "bg_guide_forward": (ST, [P, P, C.c_size_t, P]),
+    "bg_guide_gradient": (ST, [P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
+    "bg_guide_train": (ST, [P, P, C.c_size_t, C.POINTER(C.c_float)]),
+    "bg_guide_mixture_eval": (ST, [P, P, P, P, P, C.c_size_t, P]),
+    "bg_render_guided": (ST, [P, P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
+                              C.POINTER(bg_render_stats), C.POINTER(bg_guide_stats)]),
 }
 
 _LIB = None

@@ -17,64 +17,10 @@
 
 #include "../../include/bonsai_gpu.h"
 #include "bg_bvh.h"
+#include "bg_internal.h"
 #include "bg_kernels.h"
 
-namespace {
-
-constexpr uint64_t kFaithfulMaxPrims = 200000;
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-}  // namespace
-
-struct bg_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    uint64_t cap = 0, used = 0;
-    bg::LaunchShape shape{1, 128};
-    uint32_t max_queue = 1u << 22;
-    uint32_t* d_err = nullptr;
-    unsigned long long* d_counters = nullptr;
-    uint32_t* d_head = nullptr;
-    bg::FilmBuffers film{};
-    uint32_t film_w = 0, film_h = 0;
-    bg::WaveBuffers wave{};
-    std::vector<void*> wave_allocs;
-    std::vector<void*> film_allocs;
-    void* flush = nullptr;
-    size_t flush_bytes = 0;
-    std::vector<void*> user;
-    std::unordered_map<void*, size_t> sizes;
-    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
-    cudaEvent_t stage_ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    std::vector<cudaEvent_t> timing_ev;
-    // captured wave chain (BG_RENDER_GRAPH) and the launch parameters it was captured with
-    cudaGraphExec_t graph_exec = nullptr;
-    std::vector<unsigned char> graph_key;
-    int graph_kernels = 0;
-    std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
-};
-
-struct bg_scene {
-    bg_ctx* ctx = nullptr;
-    std::vector<float> tri;
-    std::vector<uint32_t> tri_mat;
-    std::vector<int32_t> tri_light;
-    std::vector<bg_sphere> sph;
-    std::vector<bg_quadric> quads;
-    std::vector<bg_material> mats;
-    std::vector<bg_area_light> lights;
-    bool committed = false;
-    uint32_t kind = BG_BVH_WIDE;
-    bg::Scene dev{};
-    std::vector<void*> allocs;
-};
-
-namespace {
+namespace bgi {
 
 bg_status fail(bg_ctx* c, bg_status s, const std::string& msg) {
     if (c) c->err = msg;
@@ -84,12 +30,6 @@ bg_status cuda_fail(bg_ctx* c, cudaError_t e, const char* what) {
     return fail(c, e == cudaErrorMemoryAllocation ? BG_ERR_OOM : BG_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
-#define CK(call)                                               \
-    do {                                                       \
-        cudaError_t e_ = (call);                               \
-        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-    } while (0)
-
 bg_status dalloc(bg_ctx* ctx, size_t bytes, void** p, std::vector<void*>* owner) {
     if (ctx->cap && ctx->used + bytes > ctx->cap)
         return fail(ctx, BG_ERR_OOM, "device memory cap exceeded (" + std::to_string(ctx->used + bytes) + " > " +
@@ -348,7 +288,9 @@ bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
     return BG_OK;
 }
 
-}  // namespace
+}  // namespace bgi
+
+using namespace bgi;
 
 namespace bg {
 // Scene internals for the allocation-free render entry point (bg_noalloc.cu).
@@ -439,6 +381,7 @@ void bg_destroy(bg_ctx* ctx) {
         s->committed = false;
     }
     ctx->scenes.clear();
+    guide_orphan_all(ctx);
     dfree_all(ctx, ctx->wave_allocs);
     dfree_all(ctx, ctx->film_allocs);
     dfree_all(ctx, ctx->user);
@@ -625,6 +568,21 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     const uint32_t ntri = (uint32_t)s->tri_mat.size(), nsph = (uint32_t)s->sph.size();
     const uint32_t nquad = (uint32_t)s->quads.size();
     bg::HostPrims hp{s->tri.data(), ntri, s->sph.data(), nsph, s->quads.data(), nquad};
+    {
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t i = 0; i < hp.count(); ++i) {
+            float bl[3], bh[3];
+            bg::prim_bounds(hp, i, bl, bh);
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::fmin(lo[k], bl[k]);
+                hi[k] = std::fmax(hi[k], bh[k]);
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            s->bmin[k] = hp.count() ? lo[k] : 0.0f;
+            s->bmax[k] = hp.count() ? hi[k] : 0.0f;
+        }
+    }
     // triangles as float4 triplets with material / emission / light-index tags
     std::vector<float4> tri4(3 * (size_t)ntri);
     std::vector<uint32_t> light_prims;
@@ -819,8 +777,9 @@ bg_status bg_trace_any(bg_ctx* ctx, const bg_scene* s, const bg_ray* rays, size_
 }
 
 // ---------------------------------------------------------------- render
-bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o, float* rgb_out,
-                    bg_render_stats* stats) {
+extern "C++" {
+bg_status bgi::validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o,
+                               const float* rgb_out) {
     if (!ctx || !s || !cam || !o) return BG_ERR_INVALID;
     if (!s->committed || s->ctx != ctx) return fail(ctx, BG_ERR_INVALID, "scene not committed on this context");
     if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height >= (1ull << 31))
@@ -832,8 +791,15 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         return fail(ctx, BG_ERR_INVALID, "REF_COMPAT rendering needs a BG_BVH_REFERENCE* scene layout");
     if (o->max_depth > 250) return fail(ctx, BG_ERR_INVALID, "max_depth must be <= 250");
     if (!(o->flags & BG_RENDER_NO_READBACK) && !rgb_out) return BG_ERR_INVALID;
+    return BG_OK;
+}
+}  // extern "C++"
+
+bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o, float* rgb_out,
+                    bg_render_stats* stats) {
+    bg_status st = validate_render(ctx, s, cam, o, rgb_out);
+    if (st != BG_OK) return st;
     CK(cudaSetDevice(ctx->device));
-    bg_status st;
     if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
     if (!(o->flags & BG_RENDER_ACCUMULATE)) {
         bg::launch_clear_film(ctx->film, ctx->stream);

@@ -133,6 +133,14 @@ size_t two_pointer_partition(RefInfo* v, size_t n, F pred) {
 
 }  // namespace
 
+void prim_bounds(const HostPrims& p, uint32_t i, float lo[3], float hi[3]) {
+    Box b = prim_box(p, i);
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = b.lo[k];
+        hi[k] = b.hi[k];
+    }
+}
+
 bool build_reference_bvh(const HostPrims& p, bool faithful, RefBvh* out, uint64_t max_prims_faithful) {
     const uint64_t n = p.count();
     out->nodes.clear();

@@ -18,6 +18,9 @@ struct HostPrims {
     uint32_t count() const { return ntri + nsph + nquad; }
 };
 
+// World-space bounds of primitive i (the boxes the builders use).
+void prim_bounds(const HostPrims& p, uint32_t i, float lo[3], float hi[3]);
+
 // BVH::new (src/accelerators/bvh.rs:53-269): 16-bucket SAH, leaves of up to 256 primitives,
 // DFS-preorder flattening.  faithful = true keeps the bucket index `16 * (offset as usize)`
 // (bvh.rs:154-155, which only ever yields buckets 0 and 15); false uses floor(16 * offset).

@@ -108,6 +108,7 @@ enum : uint32_t {
     ERR_QUEUE_OVERFLOW = 2u,
     ERR_BAD_PRIM = 4u,
     ERR_BAD_NODE = 8u,
+    ERR_GUIDE_TIMEOUT = 16u,  // a tensor-core wait of the guiding network gave up
 };
 
 constexpr uint32_t SPHERE_BIT = 0x80000000u;

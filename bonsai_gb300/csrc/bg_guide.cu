@@ -1,0 +1,472 @@
+// bg_guide.cu - tensor-core kernels of the guiding network (tcgen05, BF16 operands in shared
+// memory, FP32 accumulators in TMEM) and its optimiser.
+//
+//   k_guide_infer  forward pass for a queue of queries, 128 queries per tile (one per thread /
+//                  TMEM lane); persistent CTAs keep the 48.6 KB weight image in shared memory.
+//   k_guide_train  fused forward + loss gradient + backward for 128 training samples per CTA:
+//                  activations of all layers stay in shared memory, dX = dZ W and
+//                  dW = dZ^T H run as MN-major MMAs on the same tiles, weight gradients are
+//                  reduced into a global FP32 buffer with one atomic add per element and CTA.
+//   k_guide_adam   Adam on the FP32 master weights; rewrites the BF16 core-matrix image.
+//
+// Shared-memory tiles (no swizzle, core matrices of 8 rows x 16 B, see bg_umma.cuh):
+//   weights  W_l[rows][80]  8-row groups 1280 B apart      (48,640 B for all five layers)
+//   act      A[128][80]     8-row groups 1280 B apart      (20,480 B per layer)
+//   dZ       dZ[128][128]   8-row groups 2048 B apart; columns 64..127 stay zero so that
+//            dZ^T can feed an M = 128 MMA for layers with 64 (or 41) output rows.
+#include <cuda_bf16.h>
+
+#include "bg_device.h"
+#include "bg_guide.cuh"
+#include "bg_guide_kernels.h"
+#include "bg_umma.cuh"
+
+namespace bg {
+
+namespace {
+
+constexpr uint32_t ACT_BYTES = 128 * GUIDE_K * 2;         // 20,480
+constexpr uint32_t ACT_RS = GUIDE_ROWGROUP_BYTES;         // 1280
+constexpr uint32_t DZ_RS = 2048;                          // 16 column groups per 8-row group
+constexpr uint32_t DZ_BYTES = 16 * DZ_RS;                 // 32,768
+constexpr uint32_t INFER_SMEM = GUIDE_WPACK_BYTES + 2 * ACT_BYTES;                    // 89,600
+constexpr uint32_t TRAIN_SMEM = GUIDE_WPACK_BYTES + 5 * ACT_BYTES + DZ_BYTES;          // 183,808
+constexpr uint32_t TM_FWD = 0, TM_DX = 64, TM_DW = 160, TM_COLS_TRAIN = 256, TM_COLS_INFER = 64;
+
+BG_D uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+BG_D float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+BG_D float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xFFFF0000u); }
+
+// Writes 8 consecutive columns (c0 a multiple of 8) of one row.
+BG_D void store_row8(uint8_t* tile, uint32_t rs, uint32_t row, uint32_t c0, const float* v) {
+    uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+    *reinterpret_cast<uint4*>(tile + core_off(row, c0, rs)) = q;
+}
+
+BG_D void load_weights(uint8_t* dst, const uint8_t* wpack) {
+    const uint4* s = reinterpret_cast<const uint4*>(wpack);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (uint32_t i = threadIdx.x; i < GUIDE_WPACK_BYTES / 16; i += blockDim.x) d[i] = __ldg(&s[i]);
+}
+
+// Encoded query -> one row of an activation tile (80 columns).
+BG_D void encode_row(uint8_t* act, uint32_t row, const float* q) {
+    float x[GUIDE_K];
+    guide_encode(q, x);
+#pragma unroll
+    for (int g = 0; g < GUIDE_K / 8; ++g) store_row8(act, ACT_RS, row, 8 * g, x + 8 * g);
+}
+
+// D[tm] = act (128 x 80, K-major) * W_l^T (N x 80, K-major); five K = 16 steps.
+BG_D void issue_forward(uint32_t tm, uint32_t act, uint32_t w, int N) {
+#pragma unroll
+    for (int k = 0; k < GUIDE_K / 16; ++k)
+        umma_bf16(tm, umma_desc(act + 256 * k, 128, ACT_RS), umma_desc(w + 256 * k, 128, ACT_RS),
+                  umma_idesc_bf16(128, N, 0, 0), k > 0);
+}
+
+// Forward epilogue of a hidden layer: ReLU of this thread's 64 accumulator columns, BF16, plus
+// the constant bias column 64 and zero columns 65..79.
+BG_D void hidden_epilogue(uint32_t tm_row, uint8_t* dst, uint32_t row) {
+#pragma unroll
+    for (int c = 0; c < GUIDE_HID; c += 16) {
+        float v[16];
+        tmem_ld16(tm_row + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
+        store_row8(dst, ACT_RS, row, c, v);
+        store_row8(dst, ACT_RS, row, c + 8, v + 8);
+    }
+    float tail[16] = {1.0f};
+    store_row8(dst, ACT_RS, row, 64, tail);
+    store_row8(dst, ACT_RS, row, 72, tail + 8);
+}
+
+// Closes an MMA stage: makes this thread's shared-memory writes visible to the tensor core and
+// orders TMEM reads before the next MMA.  Returns true when any thread saw a timeout.
+BG_D bool stage_barrier(bool ok) {
+    fence_async_smem();
+    tc_fence_before();
+    int bad = __syncthreads_or(!ok);
+    tc_fence_after();
+    return bad != 0;
+}
+
+// Bounded clean-up after a timed-out wait: records the error, lets the in-flight MMAs retire
+// (again with a limit) and frees TMEM.
+BG_D void bail_out(uint64_t* bar, uint32_t parity, uint32_t* err, uint32_t tmem, uint32_t ncols) {
+    if (threadIdx.x == 0) atomicOr(err, ERR_GUIDE_TIMEOUT);
+    mbar_wait(bar, parity);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(tmem, ncols);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- inference
+__global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, const float4* query,
+                                                        const uint32_t* count, uint32_t max_n, float* raw,
+                                                        uint32_t* err) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t n = count ? min(*count, max_n) : max_n;
+    const uint32_t ntiles = (n + 127) / 128;
+    if (blockIdx.x >= ntiles) return;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    uint8_t* wsm = sm;
+    uint8_t* act[2] = {sm + GUIDE_WPACK_BYTES, sm + GUIDE_WPACK_BYTES + ACT_BYTES};
+    load_weights(wsm, wpack);
+    if (tid == 0) mbar_init(&bar, 1);
+    if (warp == 0) tmem_alloc(&tslot, TM_COLS_INFER);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t tm_row = tmem + ((warp * 32u) << 16);
+    const uint32_t w_addr = smem_addr(wsm);
+    uint32_t phase = 0;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t qi = tile * 128 + tid;
+        float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
+        if (qi < n) {
+            float4 a = query[3 * (size_t)qi], b = query[3 * (size_t)qi + 1], c = query[3 * (size_t)qi + 2];
+            q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w;
+            q[8] = c.x;
+        }
+        encode_row(act[0], tid, q);
+        if (stage_barrier(true)) return;  // never taken: no wait before the first stage
+        for (int l = 0; l < GUIDE_LAYERS; ++l) {
+            const int N = guide_rows(l);
+            if (tid == 0) {
+                issue_forward(tmem + TM_FWD, smem_addr(act[l & 1]), w_addr + guide_wpack_off(l), N);
+                umma_commit(&bar);
+            }
+            bool ok = mbar_wait(&bar, phase);
+            phase ^= 1;
+            tc_fence_after();
+            if (l < GUIDE_LAYERS - 1) {
+                hidden_epilogue(tm_row + TM_FWD, act[(l + 1) & 1], tid);
+            } else {
+                float* o = raw + (size_t)qi * GUIDE_RAW_STRIDE;
+#pragma unroll
+                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) {
+                    float v[16];
+                    tmem_ld16(tm_row + TM_FWD + c, v);
+                    if (qi < n) {
+#pragma unroll
+                        for (int j = 0; j < 16; j += 4)
+                            *reinterpret_cast<float4*>(o + c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    }
+                }
+            }
+            if (stage_barrier(ok)) {
+                bail_out(&bar, phase ^ 1, err, tmem, TM_COLS_INFER);
+                return;
+            }
+        }
+    }
+    if (warp == 0) tmem_dealloc(tmem, TM_COLS_INFER);
+}
+
+// ---------------------------------------------------------------- training
+__global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (a.step && blockIdx.x == 0 && tid == 0) atomicAdd(a.step, 1u);
+    uint8_t* wsm = sm;
+    uint8_t* act = sm + GUIDE_WPACK_BYTES;  // 5 tiles: X0, H1..H4
+    uint8_t* dz = sm + GUIDE_WPACK_BYTES + 5 * ACT_BYTES;
+    load_weights(wsm, a.wpack);
+    {   // zero dZ (columns 64..127 must read as zero in every dW MMA)
+        uint4* d = reinterpret_cast<uint4*>(dz);
+        for (uint32_t i = tid; i < DZ_BYTES / 16; i += blockDim.x) d[i] = make_uint4(0, 0, 0, 0);
+    }
+    if (tid == 0) mbar_init(&bar, 1);
+    if (warp == 0) tmem_alloc(&tslot, TM_COLS_TRAIN);
+    // this thread's sample
+    const uint32_t si = blockIdx.x * 128 + tid;
+    float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
+    V3 wi = v3(0.0f, 0.0f, 1.0f);
+    float p_b = 0.0f, wn = 0.0f;
+    if (si < a.n) {
+        const float4* s = a.samples + (size_t)GUIDE_SAMPLE_F4 * si;
+        float4 f0 = s[0], f1 = s[1], f2 = s[2], f3 = s[3];
+        q[0] = f0.x; q[1] = f0.y; q[2] = f0.z; q[3] = f0.w; q[4] = f1.x; q[5] = f1.y; q[6] = f1.z; q[7] = f1.w;
+        q[8] = f2.x;
+        wi = v3(f2.y, f2.z, f2.w);
+        p_b = f3.x;
+        const float wsum = *a.wsum;
+        wn = (wsum > 0.0f && f3.y > 0.0f && isfinite(f3.y)) ? f3.y / wsum : 0.0f;
+    }
+    encode_row(act, tid, q);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t tm_row = tmem + ((warp * 32u) << 16);
+    const uint32_t w_addr = smem_addr(wsm), act_addr = smem_addr(act), dz_addr = smem_addr(dz);
+    uint32_t phase = 0;
+    // forward
+    for (int l = 0; l < GUIDE_LAYERS; ++l) {
+        if (tid == 0) {
+            issue_forward(tmem + TM_FWD, act_addr + l * ACT_BYTES, w_addr + guide_wpack_off(l), guide_rows(l));
+            umma_commit(&bar);
+        }
+        bool ok = mbar_wait(&bar, phase);
+        phase ^= 1;
+        tc_fence_after();
+        if (l < GUIDE_LAYERS - 1) {
+            hidden_epilogue(tm_row + TM_FWD, act + (l + 1) * ACT_BYTES, tid);
+        } else {
+            float raw[GUIDE_RAW_STRIDE], g[GUIDE_RAW_STRIDE];
+#pragma unroll
+            for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, raw + c);
+            float loss = guide_loss_grad(raw, wi, p_b, wn, a.alpha, g);
+            // loss gradient -> dZ4 (columns 0..47; 48..63 zero)
+#pragma unroll
+            for (int c = 0; c < GUIDE_OUT_ROWS; c += 8) store_row8(dz, DZ_RS, tid, c, g + c);
+            float zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            store_row8(dz, DZ_RS, tid, 48, zero8);
+            store_row8(dz, DZ_RS, tid, 56, zero8);
+            float cnt = wn > 0.0f ? 1.0f : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                loss += __shfl_xor_sync(0xffffffffu, loss, o);
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&a.stats[0], loss);
+                atomicAdd(&a.stats[1], cnt);
+            }
+        }
+        if (stage_barrier(ok)) {
+            bail_out(&bar, phase ^ 1, a.err, tmem, TM_COLS_TRAIN);
+            return;
+        }
+    }
+    // backward: layer l's dZ is in `dz`; its input activation is act tile l
+    for (int l = GUIDE_LAYERS - 1; l >= 0; --l) {
+        const uint32_t a_l = act_addr + l * ACT_BYTES;
+        const uint32_t w_l = w_addr + guide_wpack_off(l);
+        const int kout = guide_rows(l);  // 48 or 64 dZ columns feed the dX MMA
+        if (tid == 0) {
+            if (l > 0) {
+                // dX = dZ (128 x kout, K-major) * W_l (kout x 80 read MN-major: N = 80 input columns)
+                for (int k = 0; k < kout / 16; ++k)
+                    umma_bf16(tmem + TM_DX, umma_desc(dz_addr + 256 * k, 128, DZ_RS),
+                              umma_desc(w_l + 2 * ACT_RS * k, ACT_RS, 128), umma_idesc_bf16(128, GUIDE_K, 0, 1),
+                              k > 0);
+            }
+            // dW = dZ^T (M = 128 output rows incl. zero rows, K = 128 samples) * act_l (N = 80, K = samples)
+            for (int k = 0; k < 128 / 16; ++k)
+                umma_bf16(tmem + TM_DW, umma_desc(dz_addr + 2 * DZ_RS * k, DZ_RS, 128),
+                          umma_desc(a_l + 2 * ACT_RS * k, ACT_RS, 128), umma_idesc_bf16(128, GUIDE_K, 1, 1), k > 0);
+            umma_commit(&bar);
+        }
+        bool ok = mbar_wait(&bar, phase);
+        phase ^= 1;
+        tc_fence_after();
+        // weight gradient rows (thread = output row)
+        const int used = guide_used_rows(l);
+        if ((int)(warp * 32) < used) {
+            float* gl = a.grad + guide_param_off(l) + tid * GUIDE_K;
+#pragma unroll
+            for (int c = 0; c < GUIDE_K; c += 16) {
+                float v[16];
+                tmem_ld16(tm_row + TM_DW + c, v);
+                if ((int)tid < used) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (v[j] != 0.0f) atomicAdd(gl + c + j, v[j]);
+                }
+            }
+        }
+        if (l > 0) {
+            // dZ_{l-1} = dX[:, 0..63] * relu'(H_l), H_l = act tile l (this thread's row)
+            const uint8_t* hrow = act + l * ACT_BYTES;
+#pragma unroll
+            for (int c = 0; c < GUIDE_HID; c += 16) {
+                float v[16];
+                tmem_ld16(tm_row + TM_DX + c, v);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint4 hv = *reinterpret_cast<const uint4*>(hrow + core_off(tid, c + 8 * h, ACT_RS));
+                    uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (!(bf16_lo(hw[j]) > 0.0f)) v[8 * h + 2 * j] = 0.0f;
+                        if (!(bf16_hi(hw[j]) > 0.0f)) v[8 * h + 2 * j + 1] = 0.0f;
+                    }
+                }
+                store_row8(dz, DZ_RS, tid, c, v);
+                store_row8(dz, DZ_RS, tid, c + 8, v + 8);
+            }
+        }
+        if (stage_barrier(ok)) {
+            bail_out(&bar, phase ^ 1, a.err, tmem, TM_COLS_TRAIN);
+            return;
+        }
+    }
+    if (warp == 0) tmem_dealloc(tmem, TM_COLS_TRAIN);
+}
+
+// ---------------------------------------------------------------- optimiser and helpers
+__device__ __forceinline__ void pack_param(uint8_t* wpack, int i, float p) {
+    int l = min(i / (GUIDE_HID * GUIDE_K), GUIDE_LAYERS - 1);
+    int r = (i - guide_param_off(l)) / GUIDE_K, c = (i - guide_param_off(l)) % GUIDE_K;
+    *reinterpret_cast<__nv_bfloat16*>(wpack + guide_wpack_off(l) + core_off(r, c, ACT_RS)) = __float2bfloat16_rn(p);
+}
+
+__global__ void k_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
+                             GuideAdam h) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= GUIDE_PARAMS) return;
+    float gi = g[i];
+    g[i] = 0.0f;
+    float t = (float)max(*step, 1u);
+    float mi = h.beta1 * m[i] + (1.0f - h.beta1) * gi;
+    float vi = h.beta2 * v[i] + (1.0f - h.beta2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    float mhat = mi / (1.0f - powf(h.beta1, t));
+    float vhat = vi / (1.0f - powf(h.beta2, t));
+    float pi = p[i] - h.lr * mhat / (sqrtf(vhat) + h.eps);
+    p[i] = pi;
+    pack_param(wpack, i, pi);
+}
+
+__global__ void k_guide_pack(const float* p, uint8_t* wpack) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < GUIDE_PARAMS) pack_param(wpack, i, p[i]);
+}
+
+// Sum of the training weights of each batch of the sample pool.
+__global__ void k_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, float* wsum) {
+    __shared__ float red[256];
+    const uint32_t b0 = blockIdx.x * batch, b1 = min(n, b0 + batch);
+    float s = 0.0f;
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        float w = samples[(size_t)GUIDE_SAMPLE_F4 * i + 3].y;
+        if (w > 0.0f && isfinite(w)) s += w;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) wsum[blockIdx.x] = red[0];
+}
+
+__global__ void k_pass_relvar(const double* sum, const uint32_t* count, const float* pass, uint32_t npix, double* out) {
+    double acc = 0.0, cnt = 0.0;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const uint32_t n = count[p];
+        if (n < 2) continue;
+        const double corr = (double)(n - 1) / (double)n;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double x = pass[3 * p + c];
+            const double m = (sum[3 * p + c] - x) / (double)(n - 1);
+            const double d = x - m;
+            acc += d * d / (m * m + 0.01) * corr;
+            cnt += 1.0;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0.0) {
+        atomicAdd(&out[0], acc);
+        atomicAdd(&out[1], cnt);
+    }
+}
+
+// Test entry: mixture parsing, sampling, pdf and loss gradient for given raw outputs.
+// out (48 per item): sampled wi.xyz, pdf(sampled), pdf(w), c, loss, -, grad[40..] -> out[8..48]
+__global__ void k_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
+                                     float alpha, float* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r[GUIDE_RAW_STRIDE];
+    for (int j = 0; j < GUIDE_RAW_STRIDE; ++j) r[j] = j < GUIDE_OUT ? raw[(size_t)GUIDE_OUT * i + j] : 0.0f;
+    VmfMix m = guide_parse(r);
+    V3 ws = guide_sample(m, u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+    V3 wq = v3(w[3 * i], w[3 * i + 1], w[3 * i + 2]);
+    float g[GUIDE_RAW_STRIDE];
+    float loss = guide_loss_grad(r, wq, pb[i], 1.0f, alpha, g);
+    float* o = out + (size_t)48 * i;
+    o[0] = ws.x;
+    o[1] = ws.y;
+    o[2] = ws.z;
+    o[3] = guide_pdf(m, ws);
+    o[4] = guide_pdf(m, wq);
+    o[5] = m.c;
+    o[6] = loss;
+    o[7] = 0.0f;
+    for (int j = 0; j < 40; ++j) o[8 + j] = g[j];
+    // g[40] (selection logit) goes in slot 7
+    o[7] = g[40];
+}
+
+// ---------------------------------------------------------------- launchers
+void guide_set_smem_limits() {
+    static bool done = false;
+    if (done) return;
+    cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+    cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
+    done = true;
+}
+
+void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* raw,
+                        uint32_t* err, int sms, cudaStream_t s) {
+    guide_set_smem_limits();
+    uint32_t tiles = (max_n + 127) / 128;
+    uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms * 2);
+    if (grid == 0) return;
+    k_guide_infer<<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, raw, err);
+}
+
+void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
+    guide_set_smem_limits();
+    uint32_t grid = (a.n + 127) / 128;
+    if (grid == 0) return;
+    k_guide_train<<<grid, 128, TRAIN_SMEM, s>>>(a);
+}
+
+void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
+                       const GuideAdam& h, cudaStream_t s) {
+    k_guide_adam<<<(GUIDE_PARAMS + 255) / 256, 256, 0, s>>>(p, m, v, g, wpack, step, h);
+}
+
+void launch_guide_pack(const float* p, uint8_t* wpack, cudaStream_t s) {
+    k_guide_pack<<<(GUIDE_PARAMS + 255) / 256, 256, 0, s>>>(p, wpack);
+}
+
+void launch_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, float* wsum, cudaStream_t s) {
+    uint32_t nb = (n + batch - 1) / batch;
+    if (nb) k_guide_wsum<<<nb, 256, 0, s>>>(samples, n, batch, wsum);
+}
+
+void launch_pass_relvar(const FilmBuffers& film, double* out, cudaStream_t s) {
+    if (film.npix && film.pass) k_pass_relvar<<<1216, 256, 0, s>>>(film.sum, film.count, film.pass, film.npix, out);
+}
+
+void launch_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
+                               float alpha, float* out, cudaStream_t s) {
+    if (n) k_guide_mixture_eval<<<(n + 127) / 128, 128, 0, s>>>(raw, u, w, pb, n, alpha, out);
+}
+
+}  // namespace bg

@@ -1,0 +1,204 @@
+// bg_guide.cuh - neural path guiding: network layout, input encoding, the von Mises-Fisher
+// mixture it outputs, and the per-sample loss gradient.  No counterpart in the reference (its
+// PathIntegrator samples the BSDF only); the estimator stays unbiased because every guided
+// direction is weighted by the pdf of the one-sample mixture it was drawn from.
+//
+// Network: 78 inputs -> 4 hidden layers of 64 (ReLU) -> 41 outputs.
+//   inputs  x[0..71]  position: each scene-normalised coordinate p in [0,1] through 12 octaves,
+//                     x[24c + 2k] = sin(pi 2^k p_c), x[24c + 2k + 1] = cos(pi 2^k p_c)
+//           x[72..74] shading normal, x[75..77] outgoing direction wo
+//   outputs raw[5i .. 5i+2] lobe i mean direction (normalised), raw[5i+3] log kappa,
+//           raw[5i+4] lobe weight logit (8 lobes), raw[40] logit of the guide selection probability.
+// The parameter layout (biases folded into a constant-1 input column) is in bg_guide_layout.h.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "bg_guide_layout.h"
+#include "bg_math.cuh"
+
+namespace bg {
+
+// Encoded input of one query (80 values, see above).  q: p.xyz (in [0,1]), n.xyz, wo.xyz.
+BG_D void guide_encode(const float* q, float* x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int k = 0; k < GUIDE_OCTAVES; ++k) {
+            float s, co;
+            sincospif(q[c] * (float)(1 << k), &s, &co);
+            x[c * 2 * GUIDE_OCTAVES + 2 * k] = s;
+            x[c * 2 * GUIDE_OCTAVES + 2 * k + 1] = co;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) x[72 + i] = q[3 + i];
+    x[78] = 1.0f;
+    x[79] = 0.0f;
+}
+
+// ---------------------------------------------------------------- vMF mixture
+constexpr float GUIDE_C_MAX = 0.95f;   // the BSDF keeps >= 5% of the proposal
+constexpr float GUIDE_LOGK_MIN = -2.0f, GUIDE_LOGK_MAX = 8.0f;
+constexpr float LOG_2PI = 1.8378770664093453f;
+
+struct VmfMix {
+    V3 mu[GUIDE_LOBES];
+    float kappa[GUIDE_LOBES];
+    float logc[GUIDE_LOBES];   // log of the lobe's normalisation kappa / (2 pi (1 - e^{-2 kappa}))
+    float w[GUIDE_LOBES];      // softmax lobe weights
+    float c;                   // probability of sampling the guide instead of the BSDF
+};
+
+// log(1 - e^{-2 kappa}) without cancellation for small kappa
+BG_D float vmf_log_norm(float kappa, float logk) { return logk - LOG_2PI - __logf(-expm1f(-2.0f * kappa)); }
+
+BG_D VmfMix guide_parse(const float* raw) {
+    VmfMix m;
+    float mx = -FLT_BIG;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) mx = fmaxf(mx, raw[5 * i + 4]);
+    float sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        V3 d = v3(raw[5 * i], raw[5 * i + 1], raw[5 * i + 2]);
+        float l = length(d);
+        m.mu[i] = l > 1e-20f ? d / l : v3(0.0f, 0.0f, 1.0f);
+        float lk = rclamp(raw[5 * i + 3], GUIDE_LOGK_MIN, GUIDE_LOGK_MAX);
+        m.kappa[i] = __expf(lk);
+        m.logc[i] = vmf_log_norm(m.kappa[i], lk);
+        m.w[i] = __expf(raw[5 * i + 4] - mx);
+        sum += m.w[i];
+    }
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) m.w[i] = m.w[i] / sum;
+    m.c = GUIDE_C_MAX / (1.0f + __expf(-raw[40]));
+    return m;
+}
+
+BG_D float guide_pdf(const VmfMix& m, V3 w) {
+    float p = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) p += m.w[i] * __expf(m.logc[i] + m.kappa[i] * (dot(m.mu[i], w) - 1.0f));
+    return p;
+}
+
+// Draws a direction from the mixture: u0 picks the lobe, (u1, u2) the direction inside it with
+// cos(theta) = 1 + log(u1 + (1 - u1) e^{-2 kappa}) / kappa (W. Jakob, "Numerically stable sampling
+// of the von Mises-Fisher distribution on S^2", 2012) and phi = 2 pi u2.
+BG_D V3 guide_sample(const VmfMix& m, float u0, float u1, float u2) {
+    int k = GUIDE_LOBES - 1;
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES - 1; ++i) {
+        acc += m.w[i];
+        if (k == GUIDE_LOBES - 1 && u0 < acc) k = i;
+    }
+    float kappa = m.kappa[0];
+    V3 mu = m.mu[0];
+#pragma unroll
+    for (int i = 1; i < GUIDE_LOBES; ++i)
+        if (i == k) {
+            kappa = m.kappa[i];
+            mu = m.mu[i];
+        }
+    float ct = 1.0f + __logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)) / kappa;
+    ct = rclamp(ct, -1.0f, 1.0f);
+    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    // orthonormal basis around mu (T. Duff et al., "Building an orthonormal basis, revisited", JCGT 2017)
+    float sign = copysignf(1.0f, mu.z);
+    float a = -1.0f / (sign + mu.z);
+    float b = mu.x * mu.y * a;
+    V3 t = v3(1.0f + sign * mu.x * mu.x * a, sign * b, -sign * mu.x);
+    V3 bt = v3(b, sign + mu.y * mu.y * a, -mu.y);
+    return normalize(ct * mu + st * (cp * t + sp * bt));
+}
+
+// ---------------------------------------------------------------- training loss
+// Per sample (direction wi drawn from the proposal that rendered it, p_b = BSDF pdf of wi,
+// weight w = f(wo, wi) |cos| Li(wi) / p_proposal(wi) as luminance, wn = w / sum of w over the batch):
+//   loss = -wn [alpha log(c q(wi) + (1 - c) p_b) + (1 - alpha) log q(wi)]
+// a Monte Carlo estimate of the KL divergence from the normalised product f Li cos to the
+// one-sample mixture (first term) and to the guide alone (second term), up to a constant.
+// Writes d loss / d raw (41 values, raw[41..47] = 0) and returns the loss.
+constexpr float GUIDE_ALPHA = 0.5f;
+
+BG_D float guide_loss_grad(const float* raw, V3 wi, float p_b, float wn, float alpha, float* g) {
+#pragma unroll
+    for (int j = 0; j < GUIDE_RAW_STRIDE; ++j) g[j] = 0.0f;
+    if (!(wn > 0.0f)) return 0.0f;
+    float mx = -FLT_BIG;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) mx = fmaxf(mx, raw[5 * i + 4]);
+    float pi_[GUIDE_LOBES], lv[GUIDE_LOBES], kap[GUIDE_LOBES], mw[GUIDE_LOBES], dlen[GUIDE_LOBES];
+    V3 mu[GUIDE_LOBES];
+    bool kfree[GUIDE_LOBES];
+    float psum = 0.0f;
+    float lmax = -FLT_BIG;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        V3 d = v3(raw[5 * i], raw[5 * i + 1], raw[5 * i + 2]);
+        float l = length(d);
+        dlen[i] = fmaxf(l, 1e-20f);
+        mu[i] = l > 1e-20f ? d / l : v3(0.0f, 0.0f, 1.0f);
+        float lk0 = raw[5 * i + 3];
+        kfree[i] = lk0 > GUIDE_LOGK_MIN && lk0 < GUIDE_LOGK_MAX;
+        float lk = rclamp(lk0, GUIDE_LOGK_MIN, GUIDE_LOGK_MAX);
+        kap[i] = __expf(lk);
+        mw[i] = dot(mu[i], wi);
+        lv[i] = vmf_log_norm(kap[i], lk) + kap[i] * (mw[i] - 1.0f);
+        pi_[i] = __expf(raw[5 * i + 4] - mx);
+        psum += pi_[i];
+    }
+    float lq_terms[GUIDE_LOBES];
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        pi_[i] = pi_[i] / psum;
+        lq_terms[i] = __logf(pi_[i]) + lv[i];
+        lmax = fmaxf(lmax, lq_terms[i]);
+    }
+    float se = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) se += __expf(lq_terms[i] - lmax);
+    const float lq = lmax + __logf(se);  // log q(wi)
+    const float sig = 1.0f / (1.0f + __expf(-raw[40]));
+    const float c = GUIDE_C_MAX * sig;
+    // log mix, s = c q / mix, dmix_dc = (q - p_b) / mix, all in log space
+    const float la = __logf(c) + lq;
+    float lmix, s, dmdc;
+    if (p_b > 0.0f) {
+        float lb = __logf((1.0f - c) * p_b);
+        float hi = fmaxf(la, lb);
+        lmix = hi + log1pf(__expf(-fabsf(la - lb)));
+        s = __expf(la - lmix);
+        dmdc = __expf(lq - lmix) - __expf(__logf(p_b) - lmix);
+    } else {
+        lmix = la;
+        s = 1.0f;
+        dmdc = 1.0f / c;
+    }
+    const float loss = -wn * (alpha * lmix + (1.0f - alpha) * lq);
+    const float dlq = -wn * (alpha * s + (1.0f - alpha));  // d loss / d log q
+    const float dc = -wn * alpha * dmdc;                    // d loss / d c
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        float r = __expf(lq_terms[i] - lq);  // responsibility pi_i v_i / q
+        // direction: d log v / d d = kappa (wi - (mu.wi) mu) / |d|
+        float sc = dlq * r * kap[i] / dlen[i];
+        g[5 * i + 0] = sc * (wi.x - mw[i] * mu[i].x);
+        g[5 * i + 1] = sc * (wi.y - mw[i] * mu[i].y);
+        g[5 * i + 2] = sc * (wi.z - mw[i] * mu[i].z);
+        // log kappa: d log v / d log kappa = 1 - 2 kappa / (e^{2 kappa} - 1) + kappa (mu.wi - 1)
+        if (kfree[i]) {
+            float dn = 1.0f - 2.0f * kap[i] / expm1f(2.0f * kap[i]);
+            g[5 * i + 3] = dlq * r * (dn + kap[i] * (mw[i] - 1.0f));
+        }
+        // softmax logits: d log q / d a_i = r_i - pi_i
+        g[5 * i + 4] = dlq * (r - pi_[i]);
+    }
+    g[40] = dc * GUIDE_C_MAX * sig * (1.0f - sig);
+    return loss;
+}
+
+}  // namespace bg

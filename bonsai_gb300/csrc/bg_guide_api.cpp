@@ -1,0 +1,598 @@
+// bg_guide_api.cpp - C ABI of the guiding network and the progressive guided render.
+//
+// bg_render_guided runs opts->spp passes of 1 spp.  Per pass: the wavefront renders the image
+// (guided passes add the network inference and the mixture continuation to every bounce); the
+// paths' training records land in a pool of samples_per_pass samples (subsampled by a keep
+// probability set from the previous pass's record count); one reduction estimates the pass's
+// relative variance against the mean of the earlier passes; then the pool is consumed in
+// batch_size Adam steps.  One host synchronisation per pass reads the counters that steer the
+// next pass (keep probability, fallback decision).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../include/bonsai_gpu.h"
+#include "bg_guide_kernels.h"
+#include "bg_guide_layout.h"
+#include "bg_internal.h"
+
+using namespace bgi;
+
+struct bg_guide {
+    bg_ctx* ctx = nullptr;
+    bg_guide_opts o{};
+    float* params = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    uint8_t* wpack = nullptr;
+    uint32_t* step = nullptr;   // Adam step counter
+    uint32_t* ctr = nullptr;    // [0] positive-weight records, [1] pool appends
+    float* stats = nullptr;     // [0] loss, [1] samples with weight > 0
+    double* relvar = nullptr;   // [0] sum of relative squared deviations, [1] terms
+    float* wsum = nullptr;      // per batch of the pool
+    float4* pool = nullptr;
+    uint32_t pool_cap = 0;
+    float* pass = nullptr;      // this pass's sample per pixel
+    size_t pass_pix = 0;
+    float4* rec = nullptr;
+    float4* query = nullptr;
+    uint32_t* gslot = nullptr;
+    float* raw = nullptr;
+    uint32_t wcap = 0;
+    std::vector<void*> allocs, wave_allocs, pass_allocs;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+bg_guide_opts default_opts() {
+    bg_guide_opts o{};
+    o.learning_rate = 1e-3f;
+    o.beta1 = 0.9f;
+    o.beta2 = 0.999f;
+    o.eps = 1e-8f;
+    o.alpha = 0.5f;
+    o.batch_size = 16384;
+    o.samples_per_pass = 1u << 18;
+    o.warmup_passes = 4;
+    o.flags = 0;
+    o.seed = 0;
+    return o;
+}
+
+void free_guide_device(bg_guide* g) {
+    if (!g->ctx) return;
+    dfree_all(g->ctx, g->allocs);
+    dfree_all(g->ctx, g->wave_allocs);
+    dfree_all(g->ctx, g->pass_allocs);
+    for (auto& e : g->ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+}
+
+// He-uniform hidden layers, a 0.1-scaled output layer (near-uniform initial mixture), zero
+// biases and zero padding.
+std::vector<float> init_params(uint64_t seed) {
+    std::vector<float> p(bg::GUIDE_PARAMS, 0.0f);
+    std::mt19937_64 rng(seed ^ 0x9E3779B97F4A7C15ull);
+    std::uniform_real_distribution<float> u(-1.0f, 1.0f);
+    for (int l = 0; l < bg::GUIDE_LAYERS; ++l) {
+        const int fan_in = l == 0 ? bg::GUIDE_IN_USED : bg::GUIDE_HID;
+        float bound = std::sqrt(6.0f / (float)fan_in);
+        if (l == bg::GUIDE_LAYERS - 1) bound *= 0.1f;
+        for (int r = 0; r < bg::guide_used_rows(l); ++r)
+            for (int c = 0; c < fan_in; ++c) p[bg::guide_param_off(l) + r * bg::GUIDE_K + c] = bound * u(rng);
+    }
+    return p;
+}
+
+// Padding entries the network never uses must stay zero (they would otherwise be trained by
+// nothing and read by nothing, but keep the layout canonical).
+bool padding_is_zero(const float* p) {
+    for (int l = 0; l < bg::GUIDE_LAYERS; ++l) {
+        const int used_in = l == 0 ? bg::GUIDE_IN_USED + 1 : bg::GUIDE_HID + 1;
+        for (int r = 0; r < bg::guide_rows(l); ++r)
+            for (int c = 0; c < bg::GUIDE_K; ++c)
+                if ((r >= bg::guide_used_rows(l) || c >= used_in) && p[bg::guide_param_off(l) + r * bg::GUIDE_K + c] != 0.0f)
+                    return false;
+    }
+    return true;
+}
+
+bg_status upload_params(bg_guide* g, const float* host) {
+    bg_ctx* ctx = g->ctx;
+    CK(cudaMemcpyAsync(g->params, host, bg::GUIDE_PARAMS * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(g->m, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(g->v, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(g->grad, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(g->step, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaMemsetAsync(g->wpack, 0, bg::GUIDE_WPACK_BYTES, ctx->stream));
+    bg::launch_guide_pack(g->params, g->wpack, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));  // host is a caller buffer
+    return BG_OK;
+}
+
+bg_status guide_error(bg_ctx* ctx) {
+    uint32_t word = 0;
+    bg_status st = check_device_error(ctx, &word);
+    if (st != BG_OK && (word & bg::ERR_GUIDE_TIMEOUT))
+        return fail(ctx, BG_ERR_TIMEOUT, "a tensor-core wait of the guiding network timed out");
+    return st;
+}
+
+bg_status ensure_guide_wave(bg_guide* g, uint32_t cap) {
+    if (g->wcap >= cap && g->rec) return BG_OK;
+    bg_ctx* ctx = g->ctx;
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree_all(ctx, g->wave_allocs);
+    g->wcap = 0;
+    void* p;
+    bg_status st;
+    const size_t n = cap;
+    if ((st = dalloc(ctx, (size_t)bg::GUIDE_MAXREC * bg::GUIDE_REC_F4 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK)
+        return st;
+    g->rec = (float4*)p;
+    if ((st = dalloc(ctx, 3 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK) return st;
+    g->query = (float4*)p;
+    if ((st = dalloc(ctx, n * sizeof(uint32_t), &p, &g->wave_allocs)) != BG_OK) return st;
+    g->gslot = (uint32_t*)p;
+    if ((st = dalloc(ctx, n * bg::GUIDE_RAW_STRIDE * sizeof(float), &p, &g->wave_allocs)) != BG_OK) return st;
+    g->raw = (float*)p;
+    g->wcap = cap;
+    return BG_OK;
+}
+
+bg_status ensure_pass(bg_guide* g, size_t npix) {
+    if (g->pass_pix == npix && g->pass) return BG_OK;
+    bg_ctx* ctx = g->ctx;
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree_all(ctx, g->pass_allocs);
+    void* p;
+    bg_status st = dalloc(ctx, npix * 3 * sizeof(float), &p, &g->pass_allocs);
+    if (st != BG_OK) return st;
+    g->pass = (float*)p;
+    g->pass_pix = npix;
+    return BG_OK;
+}
+
+// Uploads n host samples into a temporary device buffer owned by `tmp`.
+bg_status upload_samples(bg_guide* g, const float* samples, size_t n, float4** d, std::vector<void*>* tmp) {
+    bg_ctx* ctx = g->ctx;
+    void* p;
+    bg_status st = dalloc(ctx, n * bg::GUIDE_SAMPLE_F4 * sizeof(float4), &p, tmp);
+    if (st != BG_OK) return st;
+    CK(cudaMemcpyAsync(p, samples, n * bg::GUIDE_SAMPLE_F4 * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    *d = (float4*)p;
+    return BG_OK;
+}
+
+// Batches of the sample buffer -> Adam steps (all asynchronous).  Returns the number of steps.
+int train_batches(bg_guide* g, const float4* samples, uint32_t n) {
+    bg_ctx* ctx = g->ctx;
+    const uint32_t B = g->o.batch_size;
+    const uint32_t nb = (n + B - 1) / B;
+    bg::launch_guide_wsum(samples, n, B, g->wsum, ctx->stream);
+    cudaMemsetAsync(g->stats, 0, 2 * sizeof(float), ctx->stream);
+    bg::GuideAdam h{g->o.learning_rate, g->o.beta1, g->o.beta2, g->o.eps};
+    for (uint32_t b = 0; b < nb; ++b) {
+        bg::GuideTrainArgs a{};
+        a.wpack = g->wpack;
+        a.samples = samples + (size_t)b * B * bg::GUIDE_SAMPLE_F4;
+        a.n = std::min(B, n - b * B);
+        a.wsum = g->wsum + b;
+        a.alpha = g->o.alpha;
+        a.grad = g->grad;
+        a.stats = g->stats;
+        a.step = g->step;
+        a.err = ctx->d_err;
+        bg::launch_guide_train(a, ctx->stream);
+        bg::launch_guide_adam(g->params, g->m, g->v, g->grad, g->wpack, g->step, h, ctx->stream);
+    }
+    return (int)nb;
+}
+
+}  // namespace
+
+namespace bgi {
+// Called by bg_destroy: guides outliving their context keep only host state.
+void guide_orphan_all(bg_ctx* ctx) {
+    for (bg_guide* g : ctx->guides) {
+        free_guide_device(g);
+        g->ctx = nullptr;
+    }
+    ctx->guides.clear();
+}
+}  // namespace bgi
+
+extern "C" {
+
+bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out) {
+    if (!ctx || !out) return BG_ERR_INVALID;
+    *out = nullptr;
+    bg_guide_opts o = opts ? *opts : default_opts();
+    if (o.batch_size == 0 || o.batch_size % 128 != 0) return fail(ctx, BG_ERR_INVALID, "batch_size must be a positive multiple of 128");
+    if (o.samples_per_pass < 128 || o.samples_per_pass > (1u << 24))
+        return fail(ctx, BG_ERR_INVALID, "samples_per_pass must be in [128, 2^24]");
+    if (!(o.learning_rate > 0.0f) || !(o.alpha >= 0.0f && o.alpha <= 1.0f) || !(o.beta1 >= 0.0f && o.beta1 < 1.0f) ||
+        !(o.beta2 >= 0.0f && o.beta2 < 1.0f) || !(o.eps > 0.0f))
+        return fail(ctx, BG_ERR_INVALID, "bad optimiser settings");
+    CK(cudaSetDevice(ctx->device));
+    bg_guide* g = new bg_guide();
+    g->ctx = ctx;
+    g->o = o;
+    auto bail = [&](bg_status s) {
+        free_guide_device(g);
+        delete g;
+        return s;
+    };
+    void* p;
+    bg_status st;
+    const size_t pb = bg::GUIDE_PARAMS * sizeof(float);
+    if ((st = dalloc(ctx, 4 * pb, &p, &g->allocs)) != BG_OK) return bail(st);
+    g->params = (float*)p;
+    g->m = g->params + bg::GUIDE_PARAMS;
+    g->v = g->m + bg::GUIDE_PARAMS;
+    g->grad = g->v + bg::GUIDE_PARAMS;
+    if ((st = dalloc(ctx, bg::GUIDE_WPACK_BYTES, &p, &g->allocs)) != BG_OK) return bail(st);
+    g->wpack = (uint8_t*)p;
+    if ((st = dalloc(ctx, 64, &p, &g->allocs)) != BG_OK) return bail(st);
+    g->step = (uint32_t*)p;
+    g->ctr = (uint32_t*)((char*)p + 4);
+    g->stats = (float*)((char*)p + 16);
+    g->relvar = (double*)((char*)p + 32);
+    g->pool_cap = o.samples_per_pass;
+    if ((st = dalloc(ctx, (size_t)g->pool_cap * bg::GUIDE_SAMPLE_F4 * sizeof(float4), &p, &g->allocs)) != BG_OK)
+        return bail(st);
+    g->pool = (float4*)p;
+    if ((st = dalloc(ctx, ((size_t)g->pool_cap / 128 + 1) * sizeof(float), &p, &g->allocs)) != BG_OK) return bail(st);
+    g->wsum = (float*)p;
+    for (auto& e : g->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(ctx, BG_ERR_CUDA, "cudaEventCreate"));
+    if (cudaMemsetAsync(g->step, 0, 64, ctx->stream) != cudaSuccess) return bail(BG_ERR_CUDA);
+    std::vector<float> init = init_params(o.seed);
+    if ((st = upload_params(g, init.data())) != BG_OK) return bail(st);
+    ctx->guides.insert(g);
+    *out = g;
+    return BG_OK;
+}
+
+void bg_guide_destroy(bg_guide* g) {
+    if (!g) return;
+    if (g->ctx) {
+        cudaSetDevice(g->ctx->device);
+        cudaStreamSynchronize(g->ctx->stream);
+        g->ctx->guides.erase(g);
+        free_guide_device(g);
+    }
+    delete g;
+}
+
+bg_status bg_guide_get_params(bg_guide* g, float* params) {
+    if (!g || !g->ctx || !params) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(params, g->params, bg::GUIDE_PARAMS * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BG_OK;
+}
+
+bg_status bg_guide_set_params(bg_guide* g, const float* params) {
+    if (!g || !g->ctx || !params) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    for (uint32_t i = 0; i < bg::GUIDE_PARAMS; ++i)
+        if (!std::isfinite(params[i])) return fail(ctx, BG_ERR_INVALID, "non-finite parameter");
+    if (!padding_is_zero(params)) return fail(ctx, BG_ERR_INVALID, "padding entries of the parameter layout must be zero");
+    CK(cudaSetDevice(ctx->device));
+    return upload_params(g, params);
+}
+
+bg_status bg_guide_forward(bg_guide* g, const float* queries, size_t n, float* out) {
+    if (!g || !g->ctx || (n && (!queries || !out))) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    if (n == 0) return BG_OK;
+    if (n >= (1u << 28)) return fail(ctx, BG_ERR_INVALID, "too many queries");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float4> q(3 * n);
+    for (size_t i = 0; i < n; ++i) {
+        const float* s = queries + 9 * i;
+        q[3 * i] = make_float4(s[0], s[1], s[2], s[3]);
+        q[3 * i + 1] = make_float4(s[4], s[5], s[6], s[7]);
+        q[3 * i + 2] = make_float4(s[8], 0.0f, 0.0f, 0.0f);
+    }
+    std::vector<void*> tmp;
+    void *dq = nullptr, *dr = nullptr;
+    bg_status st = dalloc(ctx, q.size() * sizeof(float4), &dq, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * bg::GUIDE_RAW_STRIDE * sizeof(float), &dr, &tmp);
+    std::vector<float> raw;
+    if (st == BG_OK) {
+        cudaMemcpyAsync(dq, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
+        bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)n, (float*)dr, ctx->d_err, ctx->shape.sms,
+                               ctx->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_infer");
+    }
+    if (st == BG_OK) st = guide_error(ctx);
+    if (st == BG_OK) {
+        raw.resize(n * bg::GUIDE_RAW_STRIDE);
+        cudaError_t e = cudaMemcpyAsync(raw.data(), dr, raw.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMemcpyAsync");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    if (st != BG_OK) return st;
+    for (size_t i = 0; i < n; ++i) std::memcpy(out + bg::GUIDE_OUT * i, raw.data() + bg::GUIDE_RAW_STRIDE * i, bg::GUIDE_OUT * sizeof(float));
+    return BG_OK;
+}
+
+bg_status bg_guide_gradient(bg_guide* g, const float* samples, size_t n, float* grad, float* loss) {
+    if (!g || !g->ctx || !samples || n == 0 || !grad) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    if (n >= (1u << 24)) return fail(ctx, BG_ERR_INVALID, "too many samples");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<void*> tmp;
+    float4* ds = nullptr;
+    bg_status st = upload_samples(g, samples, n, &ds, &tmp);
+    if (st == BG_OK) {
+        cudaMemsetAsync(g->grad, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream);
+        cudaMemsetAsync(g->stats, 0, 2 * sizeof(float), ctx->stream);
+        bg::launch_guide_wsum(ds, (uint32_t)n, (uint32_t)n, g->wsum, ctx->stream);
+        bg::GuideTrainArgs a{};
+        a.wpack = g->wpack;
+        a.samples = ds;
+        a.n = (uint32_t)n;
+        a.wsum = g->wsum;
+        a.alpha = g->o.alpha;
+        a.grad = g->grad;
+        a.stats = g->stats;
+        a.step = nullptr;
+        a.err = ctx->d_err;
+        bg::launch_guide_train(a, ctx->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_train");
+    }
+    if (st == BG_OK) st = guide_error(ctx);
+    float stats[2] = {0, 0};
+    if (st == BG_OK) {
+        cudaError_t e = cudaMemcpyAsync(grad, g->grad, bg::GUIDE_PARAMS * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(stats, g->stats, sizeof(stats), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(g->grad, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "gradient readback");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    if (st == BG_OK && loss) *loss = stats[0];
+    return st;
+}
+
+bg_status bg_guide_train(bg_guide* g, const float* samples, size_t n, float* loss) {
+    if (!g || !g->ctx || (n && !samples)) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    if (n == 0) return BG_OK;
+    if (n >= (1u << 24)) return fail(ctx, BG_ERR_INVALID, "too many samples");
+    if ((n + g->o.batch_size - 1) / g->o.batch_size > (size_t)g->pool_cap / 128 + 1)
+        return fail(ctx, BG_ERR_INVALID, "too many batches for this network's batch-sum buffer");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<void*> tmp;
+    float4* ds = nullptr;
+    bg_status st = upload_samples(g, samples, n, &ds, &tmp);
+    int nb = 0;
+    if (st == BG_OK) {
+        nb = train_batches(g, ds, (uint32_t)n);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "guide training");
+    }
+    if (st == BG_OK) st = guide_error(ctx);
+    float stats[2] = {0, 0};
+    if (st == BG_OK) {
+        cudaError_t e = cudaMemcpyAsync(stats, g->stats, sizeof(stats), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "loss readback");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    if (st == BG_OK && loss) *loss = nb ? stats[0] / (float)nb : 0.0f;
+    return st;
+}
+
+bg_status bg_guide_mixture_eval(bg_guide* g, const float* raw, const float* u, const float* w, const float* p_bsdf,
+                                size_t n, float* out) {
+    if (!g || !g->ctx || (n && (!raw || !u || !w || !p_bsdf || !out))) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    if (n == 0) return BG_OK;
+    if (n >= (1u << 24)) return fail(ctx, BG_ERR_INVALID, "too many items");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<void*> tmp;
+    void *dr, *du, *dw, *dp, *dout;
+    bg_status st = dalloc(ctx, n * bg::GUIDE_OUT * sizeof(float), &dr, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * 3 * sizeof(float), &du, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * 3 * sizeof(float), &dw, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * sizeof(float), &dp, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, n * 48 * sizeof(float), &dout, &tmp);
+    if (st == BG_OK) {
+        cudaMemcpyAsync(dr, raw, n * bg::GUIDE_OUT * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(du, u, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(dw, w, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(dp, p_bsdf, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        bg::launch_guide_mixture_eval((const float*)dr, (const float*)du, (const float*)dw, (const float*)dp,
+                                      (uint32_t)n, g->o.alpha, (float*)dout, ctx->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, n * 48 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_mixture_eval");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    return st;
+}
+
+bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg_camera* cam, const bg_render_opts* o,
+                           float* rgb_out, bg_render_stats* stats, bg_guide_stats* gstats) {
+    bg_status st = validate_render(ctx, s, cam, o, rgb_out);
+    if (st != BG_OK) return st;
+    if (!g || g->ctx != ctx) return fail(ctx, BG_ERR_INVALID, "guide does not belong to this context");
+    if (o->mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering needs BG_MODE_PBRT");
+    if (s->kind != BG_BVH_WIDE && s->kind != BG_BVH_WIDE2)
+        return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering needs a wide BVH layout");
+    if (o->flags & (BG_RENDER_GRAPH | BG_RENDER_STAGE_TIMING))
+        return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering takes no GRAPH or STAGE_TIMING flag");
+    CK(cudaSetDevice(ctx->device));
+    if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
+    if (!(o->flags & BG_RENDER_ACCUMULATE)) {
+        bg::launch_clear_film(ctx->film, ctx->stream);
+        CK(cudaMemsetAsync(ctx->film.nan_count, 0, sizeof(unsigned long long), ctx->stream));
+    }
+    const uint64_t npix = (uint64_t)cam->width * cam->height;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, npix);
+    if ((st = ensure_wave(ctx, cap)) != BG_OK) return st;
+    if ((st = ensure_guide_wave(g, cap)) != BG_OK) return st;
+    if ((st = ensure_pass(g, npix)) != BG_OK) return st;
+    bg::FilmBuffers film = ctx->film;
+    film.pass = g->pass;
+    const bg::Camera dc = make_camera(*cam);
+    bg::GuideWave gw{};
+    gw.pool_cap = g->pool_cap;
+    gw.cap = g->wcap;  // >= cap, the paths of one wave
+    float lo[3], inv[3];
+    for (int k = 0; k < 3; ++k) {
+        float ext = std::fmax(s->bmax[k] - s->bmin[k], 1e-6f) * 1.002f;
+        lo[k] = s->bmin[k] - 0.001f * ext;
+        inv[k] = 1.0f / ext;
+    }
+    gw.bmin = make_float4(lo[0], lo[1], lo[2], 0.0f);
+    gw.binv = make_float4(inv[0], inv[1], inv[2], 0.0f);
+    gw.rec = g->rec;
+    gw.query = g->query;
+    gw.gslot = g->gslot;
+    gw.raw = g->raw;
+    gw.pool = g->pool;
+    gw.ctr = g->ctr;
+    gw.wpack = g->wpack;
+    const bool train = !(g->o.flags & BG_GUIDE_NO_TRAIN);
+    const bool allow_fallback = !(g->o.flags & BG_GUIDE_NO_FALLBACK);
+    bg_guide_stats gs{};
+    double rv_plain_sum = 0, ms_plain_sum = 0, rv_guided_recent[4] = {0, 0, 0, 0}, ms_guided_recent[4] = {0, 0, 0, 0};
+    uint32_t n_plain = 0, n_guided_eval = 0;
+    bool fallback = false;
+    float keep = 1.0f;
+    uint64_t launches = 0;
+    CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+    for (uint32_t p = 0; p < o->spp; ++p) {
+        const bool guided = p >= g->o.warmup_passes && !fallback;
+        const bool record = train && !fallback;
+        gw.flags = (record ? bg::GW_RECORD : 0u) | (guided ? bg::GW_GUIDED : 0u);
+        gw.keep_prob = keep;
+        CK(cudaMemsetAsync(g->ctr, 0, 2 * sizeof(uint32_t), ctx->stream));
+        CK(cudaMemsetAsync(g->relvar, 0, 2 * sizeof(double), ctx->stream));
+        CK(cudaEventRecord(g->ev[0], ctx->stream));
+        bg::RenderParams rp{cam->width, cam->height, 1u, o->max_depth, o->first_sample + p, o->rr_threshold, o->seed};
+        for (uint64_t item0 = 0; item0 < npix; item0 += cap) {
+            uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, npix - item0);
+            launches += (uint64_t)bg::launch_wave(s->dev, dc, rp, film, ctx->wave, item0, nitems, ctx->d_err, ctx->shape,
+                                                  ctx->stream, nullptr, &gw);
+        }
+        bg::launch_pass_relvar(film, g->relvar, ctx->stream);
+        launches += 1;
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(g->ev[1], ctx->stream));
+        uint32_t ctr[2] = {0, 0};
+        double rv[2] = {0, 0};
+        CK(cudaMemcpyAsync(ctr, g->ctr, sizeof(ctr), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(rv, g->relvar, sizeof(rv), cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = guide_error(ctx)) != BG_OK) return st;  // synchronises the stream
+        float pass_ms = 0.0f;
+        CK(cudaEventElapsedTime(&pass_ms, g->ev[0], g->ev[1]));
+        gs.render_ms += pass_ms;
+        gs.passes += 1;
+        gs.guided_passes += guided ? 1 : 0;
+        gs.records += ctr[0];
+        const uint32_t pool_n = std::min(ctr[1], g->pool_cap);
+        gs.pool_samples += pool_n;
+        keep = ctr[0] > 0 ? std::min(1.0f, (float)g->pool_cap / (float)ctr[0]) : 1.0f;
+        float train_ms = 0.0f;
+        if (record && pool_n >= 128) {
+            int nb = train_batches(g, g->pool, pool_n);
+            launches += 1 + 2 * (uint64_t)nb;
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(g->ev[2], ctx->stream));
+            float ls[2] = {0, 0};
+            CK(cudaMemcpyAsync(ls, g->stats, sizeof(ls), cudaMemcpyDeviceToHost, ctx->stream));
+            if ((st = guide_error(ctx)) != BG_OK) return st;
+            CK(cudaEventElapsedTime(&train_ms, g->ev[1], g->ev[2]));
+            gs.train_ms += train_ms;
+            gs.adam_steps += (uint32_t)nb;
+            gs.last_loss = ls[0] / (double)nb;
+        }
+        // variance bookkeeping (relative variance per sample of this pass, see k_pass_relvar)
+        if (rv[1] > 0.0) {
+            const double relvar = rv[0] / rv[1];
+            if (guided) {
+                rv_guided_recent[n_guided_eval % 4] = relvar;
+                ms_guided_recent[n_guided_eval % 4] = pass_ms + train_ms;
+                n_guided_eval += 1;
+            } else if (!fallback) {
+                rv_plain_sum += relvar;
+                ms_plain_sum += pass_ms;
+                n_plain += 1;
+            }
+        }
+        if (n_plain) {
+            gs.relvar_plain = rv_plain_sum / n_plain;
+            gs.ms_plain = ms_plain_sum / n_plain;
+        }
+        if (n_guided_eval) {
+            uint32_t k = std::min(n_guided_eval, 4u);
+            double a = 0, b = 0;
+            for (uint32_t i = 0; i < k; ++i) {
+                a += rv_guided_recent[i];
+                b += ms_guided_recent[i];
+            }
+            gs.relvar_guided = a / k;
+            gs.ms_guided = b / k;
+        }
+        if (guided && allow_fallback && n_plain >= 1 && n_guided_eval >= 2 &&
+            gs.relvar_guided * gs.ms_guided >= gs.relvar_plain * gs.ms_plain)
+            fallback = true;
+    }
+    gs.fallback = fallback ? 1u : 0u;
+    bg::launch_resolve(ctx->film, ctx->stream);
+    launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    uint32_t word = 0;
+    st = check_device_error(ctx, &word);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev_begin, ctx->ev_end);
+        stats->device_ms = ms;
+        stats->samples = npix * o->spp;
+        stats->launches = launches;
+        stats->error_word = word;
+        unsigned long long nan = 0, rs[2] = {0, 0};
+        cudaMemcpy(&nan, ctx->film.nan_count, sizeof(nan), cudaMemcpyDeviceToHost);
+        cudaMemcpy(rs, ctx->wave.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
+        stats->nan_samples = nan;
+        stats->extension_rays = rs[0];
+        stats->shadow_rays = rs[1];
+    }
+    if (gstats) *gstats = gs;
+    if (st != BG_OK) return st;
+    if (!(o->flags & BG_RENDER_NO_READBACK)) {
+        CK(cudaMemcpyAsync(rgb_out, ctx->film.rgb, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return BG_OK;
+}
+
+}  // extern "C"

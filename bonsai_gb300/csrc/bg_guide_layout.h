@@ -1,0 +1,41 @@
+// bg_guide_layout.h - layout constants of the guiding network, shared by host and device code.
+//
+// Biases are folded into the weights: every layer reads 80 input columns, one of which is a
+// constant 1 (column 78 of the encoded input, column 64 of a hidden activation) whose weight is
+// the bias.  Parameter layout (FP32 master copy, row-major W[out][80]):
+//   layer 0..3: 64 rows at offset 5120 l; layer 4: 48 rows (41 used) at 20480; 24,320 floats.
+// The tensor-core kernels read a BF16 image of the same weights, each layer tiled into 8x8
+// core matrices (8-row groups 1280 B apart): 10,240 B per 64-row layer, 48,640 B in total.
+#pragma once
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define BG_LAYOUT_FN constexpr __host__ __device__
+#else
+#define BG_LAYOUT_FN constexpr
+#endif
+
+namespace bg {
+
+constexpr int GUIDE_LAYERS = 5;
+constexpr int GUIDE_K = 80;          // padded input width of every layer (incl. the bias column)
+constexpr int GUIDE_HID = 64;
+constexpr int GUIDE_OUT = 41;
+constexpr int GUIDE_OUT_ROWS = 48;   // output rows padded to a multiple of 16
+constexpr int GUIDE_LOBES = 8;
+constexpr int GUIDE_OCTAVES = 12;
+constexpr int GUIDE_IN_USED = 78;
+constexpr int GUIDE_PARAMS = 4 * GUIDE_HID * GUIDE_K + GUIDE_OUT_ROWS * GUIDE_K;  // 24,320
+constexpr uint32_t GUIDE_ROWGROUP_BYTES = 8 * GUIDE_K * 2;                      // 1280
+constexpr uint32_t GUIDE_WPACK_BYTES = (4 * GUIDE_HID + GUIDE_OUT_ROWS) * GUIDE_K * 2;  // 48,640
+constexpr int GUIDE_RAW_STRIDE = 48;  // floats per query in the raw output buffer
+constexpr int GUIDE_QUERY_F4 = 3;     // query = 3 float4: p.xyz n.x | n.yz wo.xy | wo.z - - -
+constexpr int GUIDE_SAMPLE_F4 = 4;    // training sample = query + wi.xyz (f2.yzw) + p_bsdf, weight (f3.xy)
+
+BG_LAYOUT_FN int guide_rows(int l) { return l == GUIDE_LAYERS - 1 ? GUIDE_OUT_ROWS : GUIDE_HID; }
+BG_LAYOUT_FN int guide_used_rows(int l) { return l == GUIDE_LAYERS - 1 ? GUIDE_OUT : GUIDE_HID; }
+BG_LAYOUT_FN int guide_param_off(int l) { return l * GUIDE_HID * GUIDE_K; }
+BG_LAYOUT_FN uint32_t guide_wpack_off(int l) { return (uint32_t)l * GUIDE_HID * GUIDE_K * 2; }
+BG_LAYOUT_FN int guide_bias_col(int l) { return l == 0 ? GUIDE_IN_USED : GUIDE_HID; }
+
+}  // namespace bg

@@ -1,0 +1,87 @@
+// bg_internal.h - library-internal state behind the C ABI (shared by bg_api.cpp and
+// bg_guide_api.cpp): the context, the scene, and the device-memory / film / wave helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/bonsai_gpu.h"
+#include "bg_kernels.h"
+
+struct bg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t cap = 0, used = 0;
+    bg::LaunchShape shape{1, 128};
+    uint32_t max_queue = 1u << 22;
+    uint32_t* d_err = nullptr;
+    unsigned long long* d_counters = nullptr;
+    uint32_t* d_head = nullptr;
+    bg::FilmBuffers film{};
+    uint32_t film_w = 0, film_h = 0;
+    bg::WaveBuffers wave{};
+    std::vector<void*> wave_allocs;
+    std::vector<void*> film_allocs;
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    std::vector<void*> user;
+    std::unordered_map<void*, size_t> sizes;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    cudaEvent_t stage_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> timing_ev;
+    // captured wave chain (BG_RENDER_GRAPH) and the launch parameters it was captured with
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<unsigned char> graph_key;
+    int graph_kernels = 0;
+    std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
+    std::unordered_set<bg_guide*> guides;  // live guiding networks; orphaned the same way
+};
+
+struct bg_scene {
+    bg_ctx* ctx = nullptr;
+    std::vector<float> tri;
+    std::vector<uint32_t> tri_mat;
+    std::vector<int32_t> tri_light;
+    std::vector<bg_sphere> sph;
+    std::vector<bg_quadric> quads;
+    std::vector<bg_material> mats;
+    std::vector<bg_area_light> lights;
+    bool committed = false;
+    uint32_t kind = BG_BVH_WIDE;
+    bg::Scene dev{};
+    float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};  // bounds of all primitives
+    std::vector<void*> allocs;
+};
+
+
+namespace bgi {
+
+constexpr uint64_t kFaithfulMaxPrims = 200000;
+
+bg_status fail(bg_ctx* c, bg_status s, const std::string& msg);
+bg_status cuda_fail(bg_ctx* c, cudaError_t e, const char* what);
+bg_status dalloc(bg_ctx* ctx, size_t bytes, void** p, std::vector<void*>* owner);
+void dfree(bg_ctx* ctx, void* p);
+void dfree_all(bg_ctx* ctx, std::vector<void*>& v);
+bg::Camera make_camera(const bg_camera& c);
+bg_status ensure_film(bg_ctx* ctx, uint32_t w, uint32_t h);
+bg_status ensure_wave(bg_ctx* ctx, uint32_t cap);
+bg_status check_device_error(bg_ctx* ctx, uint32_t* word);
+// Shared argument checks of bg_render / bg_render_guided.
+bg_status validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o,
+                          const float* rgb_out);
+
+// Frees the device state of the context's guiding networks (bg_destroy); they keep host state only.
+void guide_orphan_all(bg_ctx* ctx);
+
+}  // namespace bgi
+
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return bgi::cuda_fail(ctx, e_, #call); \
+    } while (0)

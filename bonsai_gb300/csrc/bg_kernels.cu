@@ -10,6 +10,8 @@
 // Megakernel (both modes, reference-layout BVH): one thread per (pixel, sample) runs
 // PathIntegrator::radiance end to end; it is the REF_COMPAT path and a cross-check of the
 // wavefront in PBRT mode.
+#include "bg_guide.cuh"
+#include "bg_guide_kernels.h"
 #include "bg_kernels.h"
 #include "bg_shading.cuh"
 #include "bg_traverse.cuh"
@@ -61,6 +63,11 @@ BG_D void film_add(const FilmBuffers& f, uint32_t pix, RGB L) {
     atomicAdd(&f.sumsq[3 * pix + 1], g * g);
     atomicAdd(&f.sumsq[3 * pix + 2], b * b);
     atomicAdd(&f.count[pix], 1u);
+    if (f.pass) {
+        f.pass[3 * pix + 0] = L.r;
+        f.pass[3 * pix + 1] = L.g;
+        f.pass[3 * pix + 2] = L.b;
+    }
 }
 
 // ================================================================ ray queries
@@ -263,8 +270,13 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 }
 
 // ================================================================ wavefront (PBRT)
-enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9 };
-enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6 };
+// Path state word: bits 0-7 bounce, 8 specular bounce, 9 pending NEE contribution, 10 open
+// training record, 12-15 training records written.
+enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10 };
+constexpr uint32_t ST_REC_SHIFT = 12, ST_REC_MASK = 0xFu << ST_REC_SHIFT;
+enum : uint32_t {
+    C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6, C_GUIDE = 11
+};
 constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
 constexpr int CLS_MISS = 4;
 
@@ -315,6 +327,7 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
         wb.counters[C_EXT_HEAD] = 0;
         wb.counters[C_SH_HEAD] = 0;
         for (int c = 0; c < NCLS; ++c) wb.counters[C_CLS + c] = 0;
+        wb.counters[C_GUIDE] = 0;
     }
 }
 
@@ -380,22 +393,114 @@ BG_D RGB apply_pending(const WaveBuffers& wb, uint32_t slot, RGB L, uint32_t sta
     return L + rgb(nb.x, nb.y, nb.z) * (ld / light_pdf);
 }
 
+// ---- guiding: training records and network queries
+BG_D float4* rec_ptr(const GuideWave& gw, uint32_t k, uint32_t f, uint32_t slot) {
+    return gw.rec + ((size_t)(k * GUIDE_REC_F4 + f) * gw.cap + slot);
+}
+BG_D uint32_t rec_count(uint32_t state) { return (state & ST_REC_MASK) >> ST_REC_SHIFT; }
+
+// Closes the open record with the radiance the path has gathered before this vertex adds its own
+// emission: what arrived along the recorded direction is everything added after this point.
+BG_D uint32_t close_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state, RGB L) {
+    if (!(state & ST_REC_OPEN) || slot >= gw.cap) return state;
+    uint32_t k = rec_count(state) - 1;
+    *rec_ptr(gw, k, 4, slot) = make_float4(L.r, L.g, L.b, 0.0f);
+    return state & ~ST_REC_OPEN;
+}
+
+struct GuideQuery {  // p_norm.xyz n.x | n.yz wo.xy | wo.z
+    float4 a, b, c;
+};
+BG_D GuideQuery make_query(const GuideWave& gw, const Isect& it, V3 wo) {
+    V3 pn = v3(rclamp((it.p.x - gw.bmin.x) * gw.binv.x, 0.0f, 1.0f), rclamp((it.p.y - gw.bmin.y) * gw.binv.y, 0.0f, 1.0f),
+               rclamp((it.p.z - gw.bmin.z) * gw.binv.z, 0.0f, 1.0f));
+    V3 n = face_forward(it.ns, wo);
+    return {make_float4(pn.x, pn.y, pn.z, n.x), make_float4(n.y, n.z, wo.x, wo.y), make_float4(wo.z, 0.0f, 0.0f, 0.0f)};
+}
+
+// Opens a training record for a sampled continuation wi (p_b = BSDF pdf of wi, beta = throughput
+// before the vertex).
+BG_D uint32_t open_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state,
+                          const GuideQuery& q, V3 wi, float p_b, RGB beta) {
+    uint32_t k = rec_count(state);
+    if (k >= (uint32_t)GUIDE_MAXREC || slot >= gw.cap) return state;
+    *rec_ptr(gw, k, 0, slot) = q.a;
+    *rec_ptr(gw, k, 1, slot) = q.b;
+    *rec_ptr(gw, k, 2, slot) = make_float4(q.c.x, wi.x, wi.y, wi.z);
+    *rec_ptr(gw, k, 3, slot) = make_float4(p_b, beta.r, beta.g, beta.b);
+    return (state & ~ST_REC_MASK) | ((k + 1) << ST_REC_SHIFT) | ST_REC_OPEN;
+}
+
+// Integer hash in [0, 1) for subsampling records into the training pool (not part of the estimator).
+BG_D float hash_unit(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return (float)(h >> 8) * 0x1p-24f;
+}
+
+// Turns the records of finished paths into training samples.  Warp-collective: every lane calls
+// it, lanes without a finished path pass nrec = 0.
+BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t nrec, RGB L_end) {
+    uint32_t positive = 0;
+    for (uint32_t k = 0; k < (uint32_t)GUIDE_MAXREC; ++k) {
+        const bool has = k < nrec;
+        if (!__any_sync(FULL, has)) break;
+        bool keep = false;
+        float w = 0.0f;
+        float4 r3 = make_float4(0, 0, 0, 0);
+        if (has) {
+            r3 = *rec_ptr(gw, k, 3, slot);
+            float4 r4 = *rec_ptr(gw, k, 4, slot);
+            RGB d = L_end - rgb(r4.x, r4.y, r4.z);
+            // (L_end - L_after) / beta = f |cos| Li / p of the recorded direction
+            RGB li = rgb(r3.y > 0.0f ? d.r / r3.y : 0.0f, r3.z > 0.0f ? d.g / r3.z : 0.0f,
+                         r3.w > 0.0f ? d.b / r3.w : 0.0f);
+            w = luminance(li);
+            if (w > 0.0f && isfinite(w)) {
+                ++positive;
+                keep = hash_unit(wb.pixel[slot], wb.sample[slot], k) < gw.keep_prob;
+            }
+        }
+        uint32_t pos = warp_append(&gw.ctr[1], keep);
+        if (keep && pos < gw.pool_cap) {
+            float4* o = gw.pool + (size_t)GUIDE_SAMPLE_F4 * pos;
+            o[0] = *rec_ptr(gw, k, 0, slot);
+            o[1] = *rec_ptr(gw, k, 1, slot);
+            o[2] = *rec_ptr(gw, k, 2, slot);
+            o[3] = make_float4(r3.x, w, 0.0f, 0.0f);
+        }
+    }
+    uint32_t tot = __reduce_add_sync(FULL, positive);
+    if (lane_id() == 0 && tot) atomicAdd(&gw.ctr[0], tot);
+}
+
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
+// In guided waves the matte / plastic / conductor classes stop after next-event estimation and
+// queue a network query; k_guide_continue samples their continuation.
 template <int CLS>
 __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
-                                               uint32_t bounce, uint32_t* err) {
+                                               GuideWave gw, uint32_t bounce, uint32_t* err) {
+    constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     uint32_t* qn = wb.queue[(bounce + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
+    const bool record = (gw.flags & GW_RECORD) != 0;
     // warp-uniform loop so the ballots below see all 32 lanes
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
         uint32_t i = base + lane_id();
         bool active = i < n;
         uint32_t slot = active ? q[i] : 0;
-        bool cont = false, done_pending = false;
+        bool cont = false, done_pending = false, push_guide = false;
         bool push_sh[2] = {false, false};
         float4 sh_o[2], sh_d[2];
+        GuideQuery gq;
+        uint32_t emit_n = 0;
+        RGB L_emit = rgb(0.0f);
         if (active) {
             float4 ro = wb.ray_o[slot], rd = wb.ray_d[slot];
             Ray ray = load_ray(ro, rd);
@@ -407,6 +512,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
             float4 l4 = wb.L[slot];
             RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
             state &= ~ST_PENDING;
+            if (record) state = close_record(gw, wb, slot, state, L);
             bool specular_bounce = (state & ST_SPECULAR) != 0;
             Isect it;
             bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
@@ -470,31 +576,39 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
                     state |= ST_PENDING;
                 }
                 V3 wo = -ray.d;
-                BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
-                if (is_black(bs.f) || bs.pdf == 0.0f) {
-                    finished = true;
+                if (GUIDABLE && (gw.flags & GW_GUIDED)) {
+                    gq = make_query(gw, it, wo);
+                    push_guide = true;
                 } else {
-                    beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
-                    bool spec = (bs.stype & BSDF_SPECULAR) != 0;
-                    if (spec && (bs.stype & BSDF_TRANSMISSION)) {
-                        float eta = bsdf.eta;
-                        eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
-                    }
-                    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
-                    RGB rr_beta = beta * eta_scale;
-                    bool killed = false;
-                    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
-                        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
-                        if (u[BD_RR] < qq) killed = true;
-                        else beta = beta / (1.0f - qq);
-                    }
-                    if (killed) {
+                    BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+                    if (is_black(bs.f) || bs.pdf == 0.0f) {
                         finished = true;
                     } else {
-                        wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
-                        wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
-                        state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-                        cont = true;
+                        RGB beta0 = beta;
+                        beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
+                        bool spec = (bs.stype & BSDF_SPECULAR) != 0;
+                        if (spec && (bs.stype & BSDF_TRANSMISSION)) {
+                            float eta = bsdf.eta;
+                            eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
+                        }
+                        Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
+                        RGB rr_beta = beta * eta_scale;
+                        bool killed = false;
+                        if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
+                            float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
+                            if (u[BD_RR] < qq) killed = true;
+                            else beta = beta / (1.0f - qq);
+                        }
+                        if (killed) {
+                            finished = true;
+                        } else {
+                            wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
+                            wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
+                            state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
+                            if (GUIDABLE && record)
+                                state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
+                            cont = true;
+                        }
                     }
                 }
             }
@@ -502,8 +616,13 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
             wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
             wb.L[slot] = make_float4(L.r, L.g, L.b, 0.0f);
             if (finished) {
-                if (state & ST_PENDING) done_pending = true;
-                else film_add(film, wb.pixel[slot], L);
+                if (state & ST_PENDING) {
+                    done_pending = true;
+                } else {
+                    film_add(film, wb.pixel[slot], L);
+                    emit_n = rec_count(state);
+                    L_emit = L;
+                }
             }
         }
         // compaction (convergent)
@@ -523,6 +642,126 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
                 }
             }
         }
+        if (GUIDABLE && (gw.flags & GW_GUIDED)) {
+            pos = warp_append(&wb.counters[C_GUIDE], push_guide);
+            if (push_guide && pos >= gw.cap) {
+                atomicOr(err, ERR_QUEUE_OVERFLOW);  // cannot happen: one query per path of the wave
+                push_guide = false;
+            }
+            if (push_guide) {
+                gw.query[3 * (size_t)pos] = gq.a;
+                gw.query[3 * (size_t)pos + 1] = gq.b;
+                gw.query[3 * (size_t)pos + 2] = gq.c;
+                gw.gslot[pos] = slot;
+            }
+        }
+        if (record) emit_records(gw, wb, slot, emit_n, L_emit);
+    }
+}
+
+// Continuation of guided vertices: one-sample MIS between the network's vMF mixture (probability
+// c) and the BSDF (1 - c); the throughput is weighted by the mixture pdf
+//   p(wi) = c q(wi) + (1 - c) p_bsdf(wi),
+// so the estimator stays unbiased whatever the network outputs.  Uniforms: BSDF and roulette dims
+// of the bounce (shared with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce.
+__global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
+                                                        GuideWave gw, uint32_t bounce, uint32_t* err) {
+    const uint32_t n = min(wb.counters[C_GUIDE], gw.cap);
+    uint32_t* qn = wb.queue[(bounce + 1) & 1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const bool record = (gw.flags & GW_RECORD) != 0;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
+        uint32_t i = base + lane_id();
+        bool active = i < n;
+        uint32_t slot = active ? gw.gslot[i] : 0;
+        bool cont = false, done_pending = false;
+        uint32_t emit_n = 0;
+        RGB L_emit = rgb(0.0f);
+        if (active) {
+            Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
+            int prim = wb.hit[slot].x;
+            uint32_t state = wb.state[slot];
+            float4 b4 = wb.beta[slot];
+            RGB beta = rgb(b4.x, b4.y, b4.z);
+            const float eta_scale = b4.w;
+            float4 l4 = wb.L[slot];
+            RGB L = rgb(l4.x, l4.y, l4.z);
+            bool finished = true;
+            Isect it;
+            if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
+                BSDF bsdf = make_bsdf<-1>(sc, it);
+                Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
+                float u[4], ug[4];
+                rng.block(DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce + 4, u);  // u[1..2] BSDF, u[3] roulette
+                rng.block(DIM_GUIDE0 + 4 * bounce, ug);
+                float raw[GUIDE_RAW_STRIDE];
+                const float4* r4 = reinterpret_cast<const float4*>(gw.raw + (size_t)GUIDE_RAW_STRIDE * i);
+#pragma unroll
+                for (int j = 0; j < GUIDE_RAW_STRIDE / 4; ++j) {
+                    float4 v = r4[j];
+                    raw[4 * j] = v.x;
+                    raw[4 * j + 1] = v.y;
+                    raw[4 * j + 2] = v.z;
+                    raw[4 * j + 3] = v.w;
+                }
+                VmfMix mix = guide_parse(raw);
+                V3 wo = -ray.d;
+                V3 wi;
+                RGB f;
+                float p_b;
+                if (ug[0] < mix.c) {
+                    wi = guide_sample(mix, ug[1], ug[2], ug[3]);
+                    f = bsdf.f<false>(wo, wi, BSDF_ALL);
+                    p_b = bsdf.pdf<false>(wo, wi, BSDF_ALL);
+                } else {
+                    BxSample bs = bsdf.sample<false>(wo, u[1], u[2], BSDF_ALL);
+                    wi = bs.wi;
+                    f = bs.pdf > 0.0f ? bs.f : rgb(0.0f);
+                    p_b = bs.pdf;
+                }
+                float pdf = mix.c * guide_pdf(mix, wi) + (1.0f - mix.c) * p_b;
+                if (!is_black(f) && pdf > 0.0f && isfinite(pdf)) {
+                    RGB beta0 = beta;
+                    beta = beta * (f * abs_dot(wi, it.ns) / pdf);
+                    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
+                    RGB rr_beta = beta * eta_scale;
+                    bool killed = false;
+                    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
+                        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
+                        if (u[3] < qq) killed = true;
+                        else beta = beta / (1.0f - qq);
+                    }
+                    if (!killed) {
+                        wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
+                        wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
+                        state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu);
+                        if (record) {
+                            GuideQuery gq{gw.query[3 * (size_t)i], gw.query[3 * (size_t)i + 1],
+                                          gw.query[3 * (size_t)i + 2]};
+                            state = open_record(gw, wb, slot, state, gq, wi, p_b, beta0);
+                        }
+                        cont = true;
+                        finished = false;
+                    }
+                }
+            }
+            wb.state[slot] = state;
+            wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
+            if (finished) {
+                if (state & ST_PENDING) {
+                    done_pending = true;
+                } else {
+                    film_add(film, wb.pixel[slot], L);
+                    emit_n = rec_count(state);
+                    L_emit = L;
+                }
+            }
+        }
+        uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
+        if (cont) qn[pos] = slot;
+        pos = warp_append(&wb.counters[C_DONE], done_pending);
+        if (done_pending) wb.done[pos] = slot;
+        if (record) emit_records(gw, wb, slot, emit_n, L_emit);
     }
 }
 
@@ -557,20 +796,31 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuff
     else traverse_queue<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
 }
 
-__global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, WaveBuffers wb) {
+__global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, WaveBuffers wb, GuideWave gw) {
     const uint32_t n = wb.counters[C_DONE];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t slot = wb.done[i];
-        float4 l4 = wb.L[slot];
-        RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), wb.state[slot], sc.nlights);
-        film_add(film, wb.pixel[slot], L);
+    const bool record = (gw.flags & GW_RECORD) != 0;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + lane_id();
+        uint32_t slot = 0, nrec = 0;
+        RGB L = rgb(0.0f);
+        if (i < n) {
+            slot = wb.done[i];
+            float4 l4 = wb.L[slot];
+            uint32_t state = wb.state[slot];
+            L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
+            film_add(film, wb.pixel[slot], L);
+            nrec = rec_count(state);
+        }
+        if (record) emit_records(gw, wb, slot, nrec, L);
     }
 }
 
 static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                          uint32_t* err, const LaunchShape& ls, cudaStream_t s, cudaEvent_t* ev) {
+                          uint32_t* err, const LaunchShape& ls, cudaStream_t s, cudaEvent_t* ev, const GuideWave* gwp) {
     int launches = 0;
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
+    const GuideWave gw = gwp ? *gwp : GuideWave{};
+    const bool guided = (gw.flags & GW_GUIDED) != 0;
     for (uint32_t b = 0; b <= rp.max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 0], s);
@@ -578,34 +828,40 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill);
         k_bin<<<grid, block, 0, s>>>(sc, wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
-        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
-        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
-        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
-        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, b, err);
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        launches += 5;
+        if (guided && b < rp.max_depth) {
+            launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GUIDE], gw.cap, gw.raw, err, ls.sms, s);
+            k_guide_continue<<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+            launches += 2;
+        }
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
         else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
-        k_finalize<<<grid, block, 0, s>>>(sc, film, wb);
-        launches += 10;
+        k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw);
+        launches += 5;
     }
     return launches;
 }
 
 int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                 const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
-                cudaStream_t s, cudaEvent_t* ev) {
+                cudaStream_t s, cudaEvent_t* ev, const GuideWave* gw) {
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
-    return 1 + launch_bounces(sc, rp, film, wb, err, ls, s, ev);
+    return 1 + launch_bounces(sc, rp, film, wb, err, ls, s, ev, gw);
 }
 
 int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                       const WaveBuffers& wb, uint64_t total, uint32_t* err, const LaunchShape& ls, cudaStream_t s) {
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     k_generate_ctl<<<grid, block, 0, s>>>(cam, rp, wb, total);
-    int n = 1 + launch_bounces(sc, rp, film, wb, err, ls, s, nullptr);
+    int n = 1 + launch_bounces(sc, rp, film, wb, err, ls, s, nullptr, nullptr);
     k_wave_advance<<<1, 32, 0, s>>>(wb);
     return n + 1;
 }

@@ -20,6 +20,7 @@ struct FilmBuffers {
     double* sumsq;   // 3 per pixel
     uint32_t* count; // per pixel
     float* rgb;      // resolved, 3 per pixel
+    float* pass;     // optional: this pass's sample per pixel (3 floats), for per-pass variance
     unsigned long long* nan_count;
     uint32_t npix;
 };
@@ -45,9 +46,36 @@ struct WaveBuffers {
                           // dielectric) and misses, written by extend, read by the class's shade launch
     uint32_t* done;
     uint32_t* counters; // [0,1] queue sizes, [2] shadow count, [3] done count, [4] extend head,
-                        // [5] shadow head, [6..10] class queue sizes
+                        // [5] shadow head, [6..10] class queue sizes, [11] guided queries
     unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
     uint32_t* wavectl;              // graph replay: [0] wave index, [1] first sample (device side)
+};
+
+// Guiding state of one wavefront (all null / zero for unguided renders).
+//   record: every non-specular vertex whose continuation was sampled opens a training record
+//           (query, wi, BSDF pdf, throughput before the vertex); the next shade of the path closes
+//           it with the radiance accumulated so far, and at the end of the path each record becomes
+//           a training sample with weight lum((L_end - L_after) / beta) = f |cos| Li / p.
+//   guided: matte / plastic / conductor vertices queue a network query instead of sampling the
+//           BSDF; k_guide_continue samples the one-sample mixture c * guide + (1 - c) * BSDF.
+enum : uint32_t { GW_RECORD = 1u, GW_GUIDED = 2u };
+constexpr int GUIDE_MAXREC = 6;      // training records kept per path
+constexpr int GUIDE_REC_F4 = 5;      // float4 per record
+constexpr uint32_t DIM_GUIDE0 = 4096;  // guided sampling uniforms: 4 per bounce from here
+
+struct GuideWave {
+    uint32_t flags;
+    uint32_t pool_cap;   // training samples the pool holds
+    float keep_prob;     // probability that a positive-weight record enters the pool
+    uint32_t cap;        // path slots the record / query buffers below hold (>= the wave's paths)
+    float4 bmin, binv;   // position encoding: p_norm = (p - bmin) * binv
+    float4* rec;         // GUIDE_MAXREC * GUIDE_REC_F4 * cap, [k][field][slot]
+    float4* query;       // 3 float4 per guided query (cap queries)
+    uint32_t* gslot;     // guided query -> path slot
+    float* raw;          // GUIDE_RAW_STRIDE floats per guided query (network output)
+    float4* pool;        // 4 float4 per training sample
+    uint32_t* ctr;       // [0] positive-weight records, [1] pool appends (kept)
+    const uint8_t* wpack;  // BF16 weight image
 };
 
 struct LaunchShape {
@@ -65,9 +93,11 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 // One wave of the PBRT wavefront: items [item0, item0 + nitems) of the pixel x sample space.
 // Returns the number of kernels launched.  stage_events (optional): 4 events per bounce, recorded
 // before extend, before shade, before shadow and before finalize.
+// gw (optional): guiding state; guided waves add the network inference and k_guide_continue
+// after the material shades of every bounce.
 int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                 const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
-                cudaStream_t s, cudaEvent_t* stage_events);
+                cudaStream_t s, cudaEvent_t* stage_events, const GuideWave* gw = nullptr);
 // The same stage chain with the wave index and first sample read from wb.wavectl, advanced by the
 // chain itself: a static launch sequence that is captured once into a CUDA graph and replayed
 // for every wave.  Returns the number of kernels in the chain.

@@ -43,6 +43,7 @@ class Context:
             raise BonsaiError(st, "bg_create failed")
         self.h = h
         self._scenes: weakref.WeakSet = weakref.WeakSet()
+        self._guides: weakref.WeakSet = weakref.WeakSet()
 
     def check(self, st: int):
         if st != A.BG_OK:
@@ -52,6 +53,8 @@ class Context:
         if getattr(self, "h", None):
             for sc in list(getattr(self, "_scenes", [])):
                 sc.close()
+            for g in list(getattr(self, "_guides", [])):
+                g.close()
             self.lib.bg_destroy(self.h)
             self.h = None
 
@@ -182,6 +185,26 @@ class PathIntegrator:
         ctx.check(ctx.lib.bg_render(ctx.h, scene.h, C.byref(c), C.byref(o), _ptr(rgb), C.byref(st)))
         return RenderResult(rgb, st)
 
+    def render_guided(self, scene: Scene, guide: "Guide", first_sample: int = 0, accumulate: bool = False,
+                      readback: bool = True, spp: int | None = None) -> "GuidedResult":
+        """Progressive guided render (bg_render_guided): spp passes of 1 spp, online training."""
+        ctx = scene.ctx
+        c = camera_struct(self.camera)
+        o = A.bg_render_opts()
+        o.spp = self.spp if spp is None else spp
+        o.max_depth = self.max_depth
+        o.rr_threshold = self.rr_threshold
+        o.mode = self.mode
+        o.seed = self.seed
+        o.first_sample = first_sample
+        o.flags = (A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK)
+        rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
+        st = A.bg_render_stats()
+        gs = A.bg_guide_stats()
+        ctx.check(ctx.lib.bg_render_guided(ctx.h, scene.h, guide.h, C.byref(c), C.byref(o), _ptr(rgb), C.byref(st),
+                                           C.byref(gs)))
+        return GuidedResult(rgb, st, gs)
+
     @staticmethod
     def moments(ctx: Context, width: int, height: int):
         s1 = np.zeros((height, width, 3), np.float64)
@@ -189,3 +212,78 @@ class PathIntegrator:
         n = np.zeros((height, width), np.uint32)
         ctx.check(ctx.lib.bg_film_moments(ctx.h, _ptr(s1), _ptr(s2), _ptr(n)))
         return s1, s2, n
+
+
+@dataclass
+class GuidedResult:
+    rgb: np.ndarray
+    stats: A.bg_render_stats
+    guide: A.bg_guide_stats
+
+
+class Guide:
+    """Guiding network (bg_guide): 78 -> 4 x 64 -> 41 MLP producing an 8-lobe vMF mixture."""
+
+    def __init__(self, ctx: Context, learning_rate: float = 1e-3, batch_size: int = 16384,
+                 samples_per_pass: int = 1 << 18, warmup_passes: int = 4, alpha: float = 0.5, seed: int = 0,
+                 no_fallback: bool = False, no_train: bool = False):
+        self.ctx = ctx
+        o = A.bg_guide_opts()
+        o.learning_rate, o.beta1, o.beta2, o.eps, o.alpha = learning_rate, 0.9, 0.999, 1e-8, alpha
+        o.batch_size, o.samples_per_pass, o.warmup_passes = batch_size, samples_per_pass, warmup_passes
+        o.flags = (A.BG_GUIDE_NO_FALLBACK if no_fallback else 0) | (A.BG_GUIDE_NO_TRAIN if no_train else 0)
+        o.seed = seed
+        self.opts = o
+        h = C.c_void_p()
+        ctx.check(ctx.lib.bg_guide_create(ctx.h, C.byref(o), C.byref(h)))
+        self.h = h
+        ctx._guides.add(self)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.bg_guide_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.zeros(A.BG_GUIDE_PARAMS, np.float32)
+        self.ctx.check(self.ctx.lib.bg_guide_get_params(self.h, _ptr(p)))
+        return p
+
+    @params.setter
+    def params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == A.BG_GUIDE_PARAMS
+        self.ctx.check(self.ctx.lib.bg_guide_set_params(self.h, _ptr(p)))
+
+    def forward(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, A.BG_GUIDE_QUERY_FLOATS)
+        out = np.zeros((len(q), A.BG_GUIDE_OUTPUTS), np.float32)
+        self.ctx.check(self.ctx.lib.bg_guide_forward(self.h, _ptr(q), len(q), _ptr(out)))
+        return out
+
+    def gradient(self, samples: np.ndarray) -> tuple[np.ndarray, float]:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, A.BG_GUIDE_SAMPLE_FLOATS)
+        g = np.zeros(A.BG_GUIDE_PARAMS, np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.bg_guide_gradient(self.h, _ptr(s), len(s), _ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, samples: np.ndarray) -> float:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, A.BG_GUIDE_SAMPLE_FLOATS)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.bg_guide_train(self.h, _ptr(s), len(s), C.byref(loss)))
+        return loss.value
+
+    def mixture_eval(self, raw: np.ndarray, u: np.ndarray, w: np.ndarray, p_bsdf: np.ndarray) -> np.ndarray:
+        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, A.BG_GUIDE_OUTPUTS)
+        n = len(raw)
+        u = np.ascontiguousarray(u, np.float32).reshape(n, 3)
+        w = np.ascontiguousarray(w, np.float32).reshape(n, 3)
+        pb = np.ascontiguousarray(p_bsdf, np.float32).reshape(n)
+        out = np.zeros((n, 48), np.float32)
+        self.ctx.check(self.ctx.lib.bg_guide_mixture_eval(self.h, _ptr(raw), _ptr(u), _ptr(w), _ptr(pb), n, _ptr(out)))
+        return out

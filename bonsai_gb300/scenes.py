@@ -371,3 +371,71 @@ def production(width: int = 1920, height: int = 1080, spp: int = 64, max_depth: 
     return SceneData(tri, tri_mat, tri_light, sph, np.stack(mats), lights, cam, spp=spp,
                      max_depth=max_depth, rr_threshold=1.0, name="production",
                      meta={"n_ico": n_ico, "ico_level": ico_level, "n_spheres": n_spheres})
+
+
+def slit_room(width: int = 1280, height: int = 720, spp: int = 64, max_depth: int = 10, n_ico: int = 10,
+              ico_level: int = 5, n_spheres: int = 200, light_intensity: float = 60.0, seed: int = 4) -> SceneData:
+    """Indirect-dominated scene for learned path guiding (defaults are the full size).
+
+    A closed 10 x 4 x 10 room (x, z in [-5, 5], y in [0, 4]), diffuse 0.7, with a 0.2-wide vertical
+    slit (z in [-0.1, 0.1], full height) in the x = +5 wall; a closed room with a slit needs 14
+    triangles (the slit wall is two quads).  The only light is a one-sided 3 x 3 quad outside the
+    slit at x = 6, facing the room.  Inside: `n_ico` fBm-displaced icospheres (level 5: 20480
+    triangles each, 204,800 in total) and `n_spheres` spheres with lognormal radii; materials per
+    object (seed 4) 50% matte, 25% plastic, 25% Trowbridge-Reitz conductor.
+    """
+    rng = np.random.default_rng(seed)
+    mats = [material(MATTE, kd=(0.7, 0.7, 0.7)), material(MATTE, kd=(0, 0, 0))]  # walls, light
+
+    def random_material():
+        r = rng.random()
+        if r < 0.5:
+            return material(MATTE, kd=tuple(rng.uniform(0.2, 0.9, 3)))
+        if r < 0.75:
+            return material(PLASTIC, kd=tuple(rng.uniform(0.2, 0.8, 3)), ks=(0.3, 0.3, 0.3),
+                            roughness=float(rng.uniform(0.05, 0.4)))
+        return material(CONDUCTOR, roughness=float(rng.uniform(0.05, 0.5)))
+
+    X, Y, Z, S = 5.0, 4.0, 5.0, 0.1
+    walls = [
+        _quad((-X, 0, -Z), (X, 0, -Z), (X, 0, Z), (-X, 0, Z), (0, 1, 0)),        # floor
+        _quad((-X, Y, -Z), (X, Y, -Z), (X, Y, Z), (-X, Y, Z), (0, -1, 0)),       # ceiling
+        _quad((-X, 0, -Z), (-X, Y, -Z), (-X, Y, Z), (-X, 0, Z), (1, 0, 0)),      # x = -5
+        _quad((-X, 0, -Z), (X, 0, -Z), (X, Y, -Z), (-X, Y, -Z), (0, 0, 1)),      # z = -5
+        _quad((-X, 0, Z), (X, 0, Z), (X, Y, Z), (-X, Y, Z), (0, 0, -1)),         # z = +5
+        _quad((X, 0, -Z), (X, Y, -Z), (X, Y, -S), (X, 0, -S), (-1, 0, 0)),       # x = +5, z < -0.1
+        _quad((X, 0, S), (X, Y, S), (X, Y, Z), (X, 0, Z), (-1, 0, 0)),           # x = +5, z > 0.1
+    ]
+    tris = [np.concatenate(walls)]
+    tmat = [np.zeros(14, np.uint32)]
+    uv, uf = icosphere(ico_level)
+    for i in range(n_ico):
+        r = rng.uniform(0.35, 0.75)
+        c = np.array([rng.uniform(-4.0, 3.5), r * 1.05, rng.uniform(-4.0, 4.0)])
+        d = 1.0 + 0.1 * fbm(uv * 1.5, seed=seed * 1000 + i)
+        tris.append((c + uv * (r * d)[:, None])[uf].reshape(-1, 9))
+        mats.append(random_material())
+        tmat.append(np.full(len(uf), len(mats) - 1, np.uint32))
+    nonlight = sum(len(t) for t in tris)
+    tris.append(_quad((X + 1, 0.5, -1.5), (X + 1, 3.5, -1.5), (X + 1, 3.5, 1.5), (X + 1, 0.5, 1.5), (-1, 0, 0)))
+    tmat.append(np.ones(2, np.uint32))
+    tri = np.concatenate(tris).astype(np.float32)
+    tri_mat = np.concatenate(tmat).astype(np.uint32)
+    tri_light = np.full(len(tri), -1, np.int32)
+    tri_light[nonlight:] = 0
+    radii = np.clip(np.exp(rng.normal(-2.0, 0.5, n_spheres)), 0.03, 0.6)
+    sph = np.zeros(n_spheres, SPHERE_DT)
+    sph["center"][:, 0] = rng.uniform(-4.5, 4.3, n_spheres)
+    sph["center"][:, 2] = rng.uniform(-4.5, 4.5, n_spheres)
+    sph["center"][:, 1] = radii + rng.uniform(0.0, 2.5, n_spheres)
+    sph["radius"] = radii
+    for i in range(n_spheres):
+        mats.append(random_material())
+        sph["material_id"][i] = len(mats) - 1
+    sph["light_id"] = -1
+    lights = np.zeros(1, LIGHT_DT)
+    lights[0] = ((light_intensity, light_intensity * 0.92, light_intensity * 0.8), 0)
+    cam = Camera((-4.6, 2.2, 4.2), (1.0, 1.0, -1.5), (0.0, 1.0, 0.0), 65.0, width, height)
+    return SceneData(tri, tri_mat, tri_light, sph, np.stack(mats), lights, cam, spp=spp,
+                     max_depth=max_depth, rr_threshold=1.0, name="slit_room",
+                     meta={"n_ico": n_ico, "ico_level": ico_level, "n_spheres": n_spheres})

@@ -274,6 +274,90 @@ bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t byte
 bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, const bg_render_opts* opts,
                             float* d_rgb_out, void* cuda_stream);
 
+/* ---- learned path guiding ------------------------------------------------------------------
+ * No counterpart in the reference (its PathIntegrator samples continuation directions from the
+ * BSDF only, src/integrators/path.rs:110-117).  A small network maps a shading point (position
+ * normalised to the scene bounds and encoded with 12 octaves of sin/cos, shading normal,
+ * outgoing direction) to a mixture of 8 von Mises-Fisher lobes and a selection probability c.
+ * At matte, plastic and conductor vertices bg_render_guided draws the continuation from the
+ * one-sample mixture c * guide + (1 - c) * BSDF and weights it by that mixture's pdf, so the
+ * estimate stays unbiased whatever the network outputs.  The network (78 -> 4 x 64 ReLU -> 41,
+ * BF16 weights and activations, FP32 accumulation on the tensor cores) trains online on the
+ * radiance the render itself measures, with Adam.
+ *
+ * Parameter layout (BG_GUIDE_PARAMS floats): five layers of row-major W[out][80], biases folded
+ * in as the weight of a constant-1 input column (column 78 of layer 0, column 64 of layers 1-4);
+ * layers 0-3 have 64 rows (offset 5120 * l), layer 4 48 rows of which 41 are used (offset
+ * 20480).  Unused rows and columns stay zero.
+ * Query (BG_GUIDE_QUERY_FLOATS): p.xyz in [0,1], shading normal xyz, wo xyz.
+ * Output (BG_GUIDE_OUTPUTS): lobe i: direction xyz (5i..5i+2, normalised on use), log kappa
+ * (5i+3, clamped to [-2, 8]), weight logit (5i+4); selection logit at 40 (c = 0.95 sigmoid).
+ * Training sample (BG_GUIDE_SAMPLE_FLOATS): query (9), wi xyz (3), BSDF pdf of wi, weight
+ * f |cos| Li / p_proposal (luminance), 2 unused. */
+#define BG_GUIDE_PARAMS 24320u
+#define BG_GUIDE_QUERY_FLOATS 9u
+#define BG_GUIDE_OUTPUTS 41u
+#define BG_GUIDE_SAMPLE_FLOATS 16u
+
+typedef struct bg_guide bg_guide;
+
+typedef struct bg_guide_opts {
+    float learning_rate;       /* Adam step size (1e-3)                                        */
+    float beta1, beta2, eps;   /* Adam moment decay and epsilon (0.9, 0.999, 1e-8)             */
+    float alpha;               /* loss blend between the mixture and guide-only KL terms (0.5) */
+    uint32_t batch_size;       /* samples per Adam step, a multiple of 128 (16384)             */
+    uint32_t samples_per_pass; /* training samples gathered per 1-spp render pass (262144)     */
+    uint32_t warmup_passes;    /* leading unguided passes that only gather training data (4)   */
+    uint32_t flags;            /* BG_GUIDE_* bits                                               */
+    uint64_t seed;             /* weight initialisation seed                                    */
+} bg_guide_opts;
+
+#define BG_GUIDE_NO_FALLBACK 1u /* keep guiding even when its variance estimate is not lower  */
+#define BG_GUIDE_NO_TRAIN 2u    /* render with the current weights; no online training         */
+
+typedef struct bg_guide_stats {
+    uint32_t passes;         /* 1-spp passes rendered                                          */
+    uint32_t guided_passes;  /* passes that sampled the guide mixture                          */
+    uint32_t fallback;       /* 1 when plain BSDF sampling took over for the remaining passes  */
+    uint32_t adam_steps;     /* optimiser steps taken by this call                             */
+    double render_ms;        /* device time of the render passes                               */
+    double train_ms;         /* device time of training (sample pool -> Adam)                  */
+    double last_loss;        /* loss of the last training step                                 */
+    double relvar_plain;     /* relative variance per sample of unguided passes (estimate)     */
+    double relvar_guided;    /* the same for guided passes                                     */
+    double ms_plain;         /* mean device time of an unguided pass                           */
+    double ms_guided;        /* mean device time of a guided pass incl. its training           */
+    uint64_t records;        /* positive-weight training records produced                      */
+    uint64_t pool_samples;   /* of which entered the training pool                             */
+} bg_guide_stats;
+
+/* Creates a network with seeded random weights (opts NULL = the defaults above). */
+bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out);
+void bg_guide_destroy(bg_guide* guide);
+bg_status bg_guide_get_params(bg_guide* guide, float* params);
+/* Replaces the weights and resets the Adam state. */
+bg_status bg_guide_set_params(bg_guide* guide, const float* params);
+/* Network outputs for n host-side queries (out: n * BG_GUIDE_OUTPUTS floats). */
+bg_status bg_guide_forward(bg_guide* guide, const float* queries, size_t n, float* out);
+/* Gradient of the batch loss for n host-side samples (one batch, weights normalised by their
+ * sum); grad: BG_GUIDE_PARAMS floats, loss: the batch loss.  No optimiser step. */
+bg_status bg_guide_gradient(bg_guide* guide, const float* samples, size_t n, float* grad, float* loss);
+/* Adam steps over n host-side samples in batches of batch_size; loss: mean batch loss. */
+bg_status bg_guide_train(bg_guide* guide, const float* samples, size_t n, float* loss);
+/* Device evaluation of the mixture for given raw outputs (test entry): per item raw (41), u (3),
+ * w (3), p_bsdf (1) -> out (48): sampled direction xyz, pdf of it, pdf of w, c, loss and its
+ * gradient (out[7] = d/d raw[40], out[8..47] = d/d raw[0..39]) for a unit-weight sample at w. */
+bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* u, const float* w,
+                                const float* p_bsdf, size_t n, float* out);
+/* Progressive guided render: opts->spp passes of 1 spp (PBRT mode, wide BVH layouts).  Passes
+ * before warmup_passes sample the BSDF and gather training data; later passes sample the guide
+ * mixture and keep training after every pass.  Unless BG_GUIDE_NO_FALLBACK is set, guiding stops
+ * (plain BSDF sampling for the rest of the call) once its relative variance times pass time is
+ * not lower than the unguided passes'.  Film, flags and rgb_out as in bg_render. */
+bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* scene, bg_guide* guide, const bg_camera* camera,
+                           const bg_render_opts* opts, float* rgb_out, bg_render_stats* stats,
+                           bg_guide_stats* guide_stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,7 +14,8 @@ from .conftest import ROOT
 
 HEADER = ROOT / "include" / "bonsai_gpu.h"
 STRUCTS = ["bg_material", "bg_area_light", "bg_sphere", "bg_camera", "bg_render_opts", "bg_render_stats",
-           "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning", "bg_quadric"]
+           "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning", "bg_quadric", "bg_guide_opts",
+           "bg_guide_stats"]
 
 
 def declared_functions():
@@ -32,7 +33,8 @@ def _lib_path():
 def test_header_declares_the_entry_points():
     names = declared_functions()
     for required in ["bg_create", "bg_destroy", "bg_scene_commit", "bg_render", "bg_trace_closest", "bg_trace_any",
-                     "bg_render_noalloc", "bg_set_tuning"]:
+                     "bg_render_noalloc", "bg_set_tuning", "bg_guide_create", "bg_guide_forward",
+                     "bg_guide_gradient", "bg_guide_train", "bg_render_guided"]:
         assert required in names
 
 
@@ -81,3 +83,12 @@ def test_status_strings_without_device():
     assert lib.bg_scene_commit(None, 0, None) == A.BG_ERR_INVALID
     assert lib.bg_render_noalloc(None, None, None, None, None) == A.BG_ERR_INVALID
     assert lib.bg_set_tuning(None, None) == A.BG_ERR_INVALID
+
+
+def test_guide_constants_match_header():
+    text = HEADER.read_text()
+    for name in ["BG_GUIDE_PARAMS", "BG_GUIDE_QUERY_FLOATS", "BG_GUIDE_OUTPUTS", "BG_GUIDE_SAMPLE_FLOATS"]:
+        m = re.search(rf"#define {name} (\d+)u", text)
+        assert m and int(m.group(1)) == getattr(A, name), name
+    from oracle import guide as O
+    assert O.PARAMS == A.BG_GUIDE_PARAMS and O.OUT == A.BG_GUIDE_OUTPUTS
