@@ -53,8 +53,15 @@ def parse():
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
-    p.add_argument("--workload", choices=["production", "raysoup"], default="production",
-                   help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s)")
+    p.add_argument("--workload", choices=["production", "raysoup", "guiding"], default="production",
+                   help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
+                        "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room")
+    p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
+    p.add_argument("--arm-seconds", type=float, default=90.0, help="guiding: time limit of each progressive arm")
+    p.add_argument("--target", type=float, default=1e-3, help="guiding: relMSE target")
+    p.add_argument("--guide-warmup", type=int, default=8, help="guiding: unguided training passes")
+    p.add_argument("--pass-paths", type=int, default=1 << 22, help="guiding: paths per pass")
+    p.add_argument("--epochs", type=int, default=4, help="guiding: training epochs over each pass's pool")
     return p.parse_args()
 
 
@@ -429,10 +436,160 @@ def run_raysoup(args):
     ctx.close()
 
 
+def _relmse(img, ref, ref_var_term):
+    """mean over pixels and channels of (x - ref)^2 / (ref^2 + 0.01), minus the reference's own
+    expected contribution (its per-pixel variance of the mean over the same denominator)."""
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)) - ref_var_term)
+
+
+def _time_to(curve, target):
+    """First crossing of `target` by log-log interpolation between checkpoints; if the curve never
+    reaches it, extrapolation from the last checkpoint with relMSE ~ 1/t.  Returns (t, extrapolated)."""
+    if curve and curve[0][1] <= target:
+        return curve[0][0], False
+    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
+        if e0 > target >= e1 and e0 > 0 and e1 > 0:
+            a = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
+            return float(np.exp(np.log(t0) + a * (np.log(t1) - np.log(t0)))), False
+    t, e = curve[-1]
+    return float(t * max(e, 0.0) / target), True
+
+
+def _at_time(curve, t):
+    """relMSE at time t (log-log interpolation inside the curve)."""
+    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
+        if t0 <= t <= t1 and e0 > 0 and e1 > 0:
+            a = (np.log(t) - np.log(t0)) / (np.log(t1) - np.log(t0))
+            return float(np.exp(np.log(e0) + a * (np.log(e1) - np.log(e0))))
+    return None
+
+
+def run_guiding(args):
+    """Learned path guiding on the slit room (1280x720, max depth 10, 204,816 triangles, 200
+    spheres): time-to-relMSE 1e-3 of the guided progressive render (online training included in
+    the timed region) against plain graph-captured path tracing, both measured against a plain
+    reference render, plus relMSE at equal time.  The CPU number is derived: the oracle runs the
+    same estimator as the plain GPU arm, so its time to the target is the plain arm's samples to the
+    target divided by the oracle's measured Msamples/s on this scene."""
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    from bonsai_gb300 import scenes as S
+    if args.small:
+        sd = S.slit_room(320, 180, n_ico=10, ico_level=3, n_spheres=200, light_intensity=200.0)
+    else:
+        sd = S.slit_room(light_intensity=200.0)
+    W, H = sd.camera.width, sd.camera.height
+    npix = W * H
+    ctx = G.Context(0)
+    scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    pi = G.PathIntegrator(sd.camera, 1, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=11)
+
+    def mean_image():
+        s1, s2, n = G.PathIntegrator.moments(ctx, W, H)
+        n = np.maximum(n[..., None], 1).astype(np.float64)
+        return s1 / n, s2 / n, n
+
+    # reference: plain, ref_spp, separate sample indices
+    t0 = time.time()
+    chunk = 256
+    for k in range(0, args.ref_spp, chunk):
+        pi.render(scene, spp=min(chunk, args.ref_spp - k), first_sample=(1 << 26) + k, accumulate=k > 0,
+                  readback=False, graph=True)
+    ref, ref2, refn = mean_image()
+    ref_var_term = float(np.mean(np.maximum(ref2 - ref * ref, 0.0) / refn / (ref ** 2 + 1e-2)))
+    ref_s = time.time() - t0
+
+    def progressive(render_chunk, label):
+        curve, t_dev, t_wall, spp, c = [], 0.0, 0.0, 0, 4
+        while True:
+            w0 = time.time()
+            st = render_chunk(c, spp)
+            t_wall += time.time() - w0
+            t_dev += st.device_ms / 1e3
+            spp += c
+            img = mean_image()[0]
+            e = _relmse(img, ref, ref_var_term)
+            curve.append((t_dev, e, t_wall, spp))
+            if e < args.target / 1.5 or t_dev > args.arm_seconds:
+                break
+            c = max(4, int(c * 1.3))
+        return curve
+
+    def plain_chunk(c, spp):
+        return pi.render(scene, spp=c, first_sample=spp, accumulate=spp > 0, readback=False, graph=True).stats
+
+    guide = G.Guide(ctx, learning_rate=1e-3, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=args.guide_warmup,
+                    pass_paths=args.pass_paths, epochs=args.epochs)
+    gstats = {}
+
+    def guided_chunk(c, spp):
+        r = pi.render_guided(scene, guide, spp=c, first_sample=spp, accumulate=spp > 0, readback=False)
+        gstats.update({k: getattr(r.guide, k) for k, _ in A.bg_guide_stats._fields_})
+        gstats["train_ms_total"] = gstats.get("train_ms_total", 0.0) + r.guide.train_ms
+        return r.stats
+
+    clocks = Clocks(0)
+    clocks.start()
+    plain_curve = progressive(plain_chunk, "plain")
+    guided_curve = progressive(guided_chunk, "guided")
+    clk = clocks.stop()
+    pc = [(t, e) for t, e, _, _ in plain_curve]
+    gc = [(t, e) for t, e, _, _ in guided_curve]
+    t_plain, ext_p = _time_to(pc, args.target)
+    t_guided, ext_g = _time_to(gc, args.target)
+    t_eq = min(pc[-1][0], gc[-1][0])
+    plain_rate = plain_curve[-1][3] * npix / plain_curve[-1][0] / 1e6
+    guided_rate = guided_curve[-1][3] * npix / guided_curve[-1][0] / 1e6
+    # plain samples per pixel to the target (same estimator on the CPU)
+    spp_plain_target = t_plain * plain_rate * 1e6 / npix
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sdc = S.slit_room(W, H, spp=4, light_intensity=200.0) if not args.small else sd
+        sdc.spp = 4
+        orc, rows, nsamples, build_s = cpu_sample(sdc, args.cpu_seconds, threads)
+        cv, cdt = time_cpu(orc, sdc, rows, nsamples, threads)
+        cpu = {"value": spp_plain_target * npix / (cv * 1e6), "unit": "s", "cores": threads, "kind": "port",
+               "msamples_per_s": cv,
+               "sample": f"rows 0..{H} step {rows[2]} x {W} px x 4 spp = {nsamples} samples in {cdt:.1f} s "
+                         "(oracle/, PBRT mode, bucket-fixed BVH); time = plain samples to the target / this rate"}
+    wall_g = guided_curve[-1][2] * (t_guided / gc[-1][0])
+    line = {
+        "metric": "time-to-relMSE 1e-3 (guided)", "value": t_guided, "unit": "s", "n_gpus": 1, "steps": len(gc),
+        "warmup": 0, "ms_per_step": 1e3 * gc[-1][0] / len(gc), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (network bf16)", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": f"slit room {W}x{H}, max depth {sd.max_depth}, {sd.ntri} triangles, {sd.nsph} "
+                               f"spheres, PBRT estimator; reference {args.ref_spp} spp plain",
+                   "relmse": "mean (x - ref)^2 / (ref^2 + 0.01) minus the reference's own variance term",
+                   "guide": f"78 -> 4x64 -> 41 BF16 MLP, 8 vMF lobes, 2^18 samples / pass of {args.pass_paths} "
+                            f"paths, {args.epochs} epochs / pass, Adam lr 1e-3, batch 16384, "
+                            f"{args.guide_warmup} warm-up passes"},
+        "plain": {"time_to_target_s": t_plain, "extrapolated": ext_p, "msamples_per_s": plain_rate,
+                  "spp_to_target": spp_plain_target, "curve": [[round(t, 4), e] for t, e in pc]},
+        "guided": {"time_to_target_s": t_guided, "extrapolated": ext_g, "msamples_per_s": guided_rate,
+                   "curve": [[round(t, 4), e] for t, e in gc], "stats": gstats},
+        "guided_over_plain_time": t_guided / t_plain,
+        "equal_time": {"t_s": t_eq, "relmse_plain": _at_time(pc, t_eq) or pc[-1][1],
+                       "relmse_guided": _at_time(gc, t_eq) or gc[-1][1]},
+        "reference_render_s": ref_s, "reference_var_term": ref_var_term,
+        "e2e": {"value": wall_g, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "host wall clock of the guided calls to the target (scaled at the last checkpoint)"},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    guide.close()
+    scene.close()
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.workload == "raysoup":
         run_raysoup(args)
+        return
+    if args.workload == "guiding":
+        run_guiding(args)
         return
     if args.profile:
         run_profile(args)

@@ -121,7 +121,8 @@ class bg_build_stats(C.Structure):
 class bg_guide_opts(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
                 ("alpha", C.c_float), ("batch_size", C.c_uint32), ("samples_per_pass", C.c_uint32),
-                ("warmup_passes", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64)]
+                ("warmup_passes", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64),
+                ("pass_paths", C.c_uint32), ("epochs", C.c_uint32)]
 
 
 class bg_guide_stats(C.Structure):
@@ -174,6 +175,7 @@ SIGNATURES = {
     "bg_guide_gradient": (ST, [P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
     "bg_guide_train": (ST, [P, P, C.c_size_t, C.POINTER(C.c_float)]),
     "bg_guide_mixture_eval": (ST, [P, P, P, P, P, C.c_size_t, P]),
+    "bg_guide_pool": (ST, [P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bg_render_guided": (ST, [P, P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
                               C.POINTER(bg_render_stats), C.POINTER(bg_guide_stats)]),
 }

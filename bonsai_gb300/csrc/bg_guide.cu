@@ -109,6 +109,9 @@ BG_D void bail_out(uint64_t* bar, uint32_t parity, uint32_t* err, uint32_t tmem,
 }  // namespace
 
 // ---------------------------------------------------------------- inference
+// MIX = false: the 41 raw outputs per query (GUIDE_RAW_STRIDE floats); MIX = true: the parsed
+// mixture record (GUIDE_MIX_STRIDE floats) that the render kernels sample.
+template <bool MIX>
 __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, const float4* query,
                                                         const uint32_t* count, uint32_t max_n, float* raw,
                                                         uint32_t* err) {
@@ -154,15 +157,22 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
             if (l < GUIDE_LAYERS - 1) {
                 hidden_epilogue(tm_row + TM_FWD, act[(l + 1) & 1], tid);
             } else {
-                float* o = raw + (size_t)qi * GUIDE_RAW_STRIDE;
+                float v[GUIDE_OUT_ROWS];
 #pragma unroll
-                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) {
-                    float v[16];
-                    tmem_ld16(tm_row + TM_FWD + c, v);
-                    if (qi < n) {
+                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, v + c);
+                if (qi < n) {
+                    if (MIX) {
+                        float rec[GUIDE_MIX_STRIDE];
+                        guide_write_mixture(v, rec);
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE);
 #pragma unroll
-                        for (int j = 0; j < 16; j += 4)
-                            *reinterpret_cast<float4*>(o + c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                        for (int j = 0; j < GUIDE_MIX_STRIDE / 4; ++j)
+                            o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
+                    } else {
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE);
+#pragma unroll
+                        for (int j = 0; j < GUIDE_RAW_STRIDE / 4; ++j)
+                            o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                     }
                 }
             }
@@ -198,7 +208,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     V3 wi = v3(0.0f, 0.0f, 1.0f);
     float p_b = 0.0f, wn = 0.0f;
     if (si < a.n) {
-        const float4* s = a.samples + (size_t)GUIDE_SAMPLE_F4 * si;
+        const float4* s = a.samples + (size_t)GUIDE_SAMPLE_F4 * a.order.at(a.base + si);
         float4 f0 = s[0], f1 = s[1], f2 = s[2], f3 = s[3];
         q[0] = f0.x; q[1] = f0.y; q[2] = f0.z; q[3] = f0.w; q[4] = f1.x; q[5] = f1.y; q[6] = f1.z; q[7] = f1.w;
         q[8] = f2.x;
@@ -351,12 +361,12 @@ __global__ void k_guide_pack(const float* p, uint8_t* wpack) {
 }
 
 // Sum of the training weights of each batch of the sample pool.
-__global__ void k_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, float* wsum) {
+__global__ void k_guide_wsum(const float4* samples, PoolOrder order, uint32_t batch, float* wsum) {
     __shared__ float red[256];
-    const uint32_t b0 = blockIdx.x * batch, b1 = min(n, b0 + batch);
+    const uint32_t b0 = blockIdx.x * batch, b1 = min(order.n_total, b0 + batch);
     float s = 0.0f;
     for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        float w = samples[(size_t)GUIDE_SAMPLE_F4 * i + 3].y;
+        float w = samples[(size_t)GUIDE_SAMPLE_F4 * order.at(i) + 3].y;
         if (w > 0.0f && isfinite(w)) s += w;
     }
     red[threadIdx.x] = s;
@@ -368,18 +378,19 @@ __global__ void k_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, 
     if (threadIdx.x == 0) wsum[blockIdx.x] = red[0];
 }
 
-__global__ void k_pass_relvar(const double* sum, const uint32_t* count, const float* pass, uint32_t npix, double* out) {
+__global__ void k_pass_relvar(const double* sum, const uint32_t* count, const float* pass, uint32_t npix, uint32_t k,
+                              double* out) {
     double acc = 0.0, cnt = 0.0;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint32_t n = count[p];
-        if (n < 2) continue;
-        const double corr = (double)(n - 1) / (double)n;
+        if (n <= k) continue;
+        const double scale = 1.0 / (1.0 / k + 1.0 / (double)(n - k));
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const double x = pass[3 * p + c];
-            const double m = (sum[3 * p + c] - x) / (double)(n - 1);
+            const double x = (double)pass[3 * p + c] / k;
+            const double m = (sum[3 * p + c] - pass[3 * p + c]) / (double)(n - k);
             const double d = x - m;
-            acc += d * d / (m * m + 0.01) * corr;
+            acc += d * d / (m * m + 0.01) * scale;
             cnt += 1.0;
         }
     }
@@ -402,8 +413,11 @@ __global__ void k_guide_mixture_eval(const float* raw, const float* u, const flo
     if (i >= n) return;
     float r[GUIDE_RAW_STRIDE];
     for (int j = 0; j < GUIDE_RAW_STRIDE; ++j) r[j] = j < GUIDE_OUT ? raw[(size_t)GUIDE_OUT * i + j] : 0.0f;
-    VmfMix m = guide_parse(r);
-    V3 ws = guide_sample(m, u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+    // the render path: stored mixture record read through MixView
+    float rec[GUIDE_MIX_STRIDE];
+    guide_write_mixture(r, rec);
+    const MixView m{rec};
+    V3 ws = m.sample(u[3 * i], u[3 * i + 1], u[3 * i + 2]);
     V3 wq = v3(w[3 * i], w[3 * i + 1], w[3 * i + 2]);
     float g[GUIDE_RAW_STRIDE];
     float loss = guide_loss_grad(r, wq, pb[i], 1.0f, alpha, g);
@@ -411,9 +425,9 @@ __global__ void k_guide_mixture_eval(const float* raw, const float* u, const flo
     o[0] = ws.x;
     o[1] = ws.y;
     o[2] = ws.z;
-    o[3] = guide_pdf(m, ws);
-    o[4] = guide_pdf(m, wq);
-    o[5] = m.c;
+    o[3] = m.pdf(ws);
+    o[4] = m.pdf(wq);
+    o[5] = m.c();
     o[6] = loss;
     o[7] = 0.0f;
     for (int j = 0; j < 40; ++j) o[8 + j] = g[j];
@@ -425,18 +439,20 @@ __global__ void k_guide_mixture_eval(const float* raw, const float* u, const flo
 void guide_set_smem_limits() {
     static bool done = false;
     if (done) return;
-    cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+    cudaFuncSetAttribute(k_guide_infer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+    cudaFuncSetAttribute(k_guide_infer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
     cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
     done = true;
 }
 
-void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* raw,
-                        uint32_t* err, int sms, cudaStream_t s) {
+void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* out,
+                        bool mixture, uint32_t* err, int sms, cudaStream_t s) {
     guide_set_smem_limits();
     uint32_t tiles = (max_n + 127) / 128;
     uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms * 2);
     if (grid == 0) return;
-    k_guide_infer<<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, raw, err);
+    if (mixture) k_guide_infer<true><<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, out, err);
+    else k_guide_infer<false><<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, out, err);
 }
 
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
@@ -455,13 +471,13 @@ void launch_guide_pack(const float* p, uint8_t* wpack, cudaStream_t s) {
     k_guide_pack<<<(GUIDE_PARAMS + 255) / 256, 256, 0, s>>>(p, wpack);
 }
 
-void launch_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, float* wsum, cudaStream_t s) {
-    uint32_t nb = (n + batch - 1) / batch;
-    if (nb) k_guide_wsum<<<nb, 256, 0, s>>>(samples, n, batch, wsum);
+void launch_guide_wsum(const float4* samples, const PoolOrder& order, uint32_t batch, float* wsum, cudaStream_t s) {
+    uint32_t nb = (order.n_total + batch - 1) / batch;
+    if (nb) k_guide_wsum<<<nb, 256, 0, s>>>(samples, order, batch, wsum);
 }
 
-void launch_pass_relvar(const FilmBuffers& film, double* out, cudaStream_t s) {
-    if (film.npix && film.pass) k_pass_relvar<<<1216, 256, 0, s>>>(film.sum, film.count, film.pass, film.npix, out);
+void launch_pass_relvar(const FilmBuffers& film, uint32_t k, double* out, cudaStream_t s) {
+    if (film.npix && film.pass && k) k_pass_relvar<<<1216, 256, 0, s>>>(film.sum, film.count, film.pass, film.npix, k, out);
 }
 
 void launch_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,

@@ -82,6 +82,22 @@ BG_D float guide_pdf(const VmfMix& m, V3 w) {
     return p;
 }
 
+// Direction from one vMF lobe: cos(theta) from u1 (see guide_sample), phi = 2 pi u2.
+BG_D V3 vmf_sample_lobe(V3 mu, float kappa, float u1, float u2) {
+    float ct = 1.0f + __logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)) / kappa;
+    ct = rclamp(ct, -1.0f, 1.0f);
+    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    // orthonormal basis around mu (T. Duff et al., "Building an orthonormal basis, revisited", JCGT 2017)
+    float sign = copysignf(1.0f, mu.z);
+    float a = -1.0f / (sign + mu.z);
+    float b = mu.x * mu.y * a;
+    V3 t = v3(1.0f + sign * mu.x * mu.x * a, sign * b, -sign * mu.x);
+    V3 bt = v3(b, sign + mu.y * mu.y * a, -mu.y);
+    return normalize(ct * mu + st * (cp * t + sp * bt));
+}
+
 // Draws a direction from the mixture: u0 picks the lobe, (u1, u2) the direction inside it with
 // cos(theta) = 1 + log(u1 + (1 - u1) e^{-2 kappa}) / kappa (W. Jakob, "Numerically stable sampling
 // of the von Mises-Fisher distribution on S^2", 2012) and phi = 2 pi u2.
@@ -101,19 +117,53 @@ BG_D V3 guide_sample(const VmfMix& m, float u0, float u1, float u2) {
             kappa = m.kappa[i];
             mu = m.mu[i];
         }
-    float ct = 1.0f + __logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)) / kappa;
-    ct = rclamp(ct, -1.0f, 1.0f);
-    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-    float sp, cp;
-    sincospif(2.0f * u2, &sp, &cp);
-    // orthonormal basis around mu (T. Duff et al., "Building an orthonormal basis, revisited", JCGT 2017)
-    float sign = copysignf(1.0f, mu.z);
-    float a = -1.0f / (sign + mu.z);
-    float b = mu.x * mu.y * a;
-    V3 t = v3(1.0f + sign * mu.x * mu.x * a, sign * b, -sign * mu.x);
-    V3 bt = v3(b, sign + mu.y * mu.y * a, -mu.y);
-    return normalize(ct * mu + st * (cp * t + sp * bt));
+    return vmf_sample_lobe(mu, kappa, u1, u2);
 }
+
+// Parsed mixture as stored by the render-side inference (GUIDE_MIX_STRIDE floats).
+BG_D void guide_write_mixture(const float* raw, float* out) {
+    const VmfMix m = guide_parse(raw);
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        out[4 * i] = m.mu[i].x;
+        out[4 * i + 1] = m.mu[i].y;
+        out[4 * i + 2] = m.mu[i].z;
+        out[4 * i + 3] = m.kappa[i];
+        out[32 + i] = m.logc[i];
+        out[40 + i] = m.w[i];
+    }
+    out[48] = m.c;
+    out[49] = out[50] = out[51] = 0.0f;
+}
+
+// Read-only view of a stored mixture: lobes are loaded as they are needed, so a kernel does not
+// keep the whole mixture in registers.  Same arithmetic as guide_pdf / guide_sample.
+struct MixView {
+    const float* m;
+    BG_D float c() const { return m[48]; }
+    BG_D float pdf(V3 w) const {
+        float p = 0.0f;
+#pragma unroll 2
+        for (int i = 0; i < GUIDE_LOBES; ++i) {
+            const float4 l = *reinterpret_cast<const float4*>(m + 4 * i);
+            p += m[40 + i] * __expf(m[32 + i] + l.w * (dot(v3(l.x, l.y, l.z), w) - 1.0f));
+        }
+        return p;
+    }
+    BG_D V3 sample(float u0, float u1, float u2) const {
+        int k = GUIDE_LOBES - 1;
+        float acc = 0.0f;
+        for (int i = 0; i < GUIDE_LOBES - 1; ++i) {
+            acc += m[40 + i];
+            if (u0 < acc) {
+                k = i;
+                break;
+            }
+        }
+        const float4 l = *reinterpret_cast<const float4*>(m + 4 * k);
+        return vmf_sample_lobe(v3(l.x, l.y, l.z), l.w, u1, u2);
+    }
+};
 
 // ---------------------------------------------------------------- training loss
 // Per sample (direction wi drawn from the proposal that rendered it, p_b = BSDF pdf of wi,

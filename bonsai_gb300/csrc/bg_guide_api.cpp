@@ -1,6 +1,7 @@
 // bg_guide_api.cpp - C ABI of the guiding network and the progressive guided render.
 //
-// bg_render_guided runs opts->spp passes of 1 spp.  Per pass: the wavefront renders the image
+// bg_render_guided runs opts->spp passes of 1 spp; the network's warm-up count, fallback decision
+// and variance estimates carry over between calls, so a long render can be issued in chunks.  Per pass: the wavefront renders the image
 // (guided passes add the network inference and the mixture continuation to every bounce); the
 // paths' training records land in a pool of samples_per_pass samples (subsampled by a keep
 // probability set from the previous pass's record count); one reduction estimates the pass's
@@ -45,7 +46,18 @@ struct bg_guide {
     float* raw = nullptr;
     uint32_t wcap = 0;
     std::vector<void*> allocs, wave_allocs, pass_allocs;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // pass, training and call timing
+    // progressive state, carried across bg_render_guided calls
+    uint64_t passes_total = 0;    // passes rendered with this network (warm-up counts these)
+    bool fallback = false;        // plain BSDF sampling took over
+    float keep = 1.0f;            // pool keep probability for the next pass
+    double rv_plain_sum = 0, ms_plain_sum = 0;
+    uint32_t n_plain = 0;
+    static constexpr uint32_t kWindow = 8;  // guided passes in the running estimate
+    double rv_guided[kWindow] = {}, ms_guided[kWindow] = {};
+    uint32_t n_guided = 0;
+    uint32_t pool_n = 0;          // samples in the pool after the last pass
+    uint64_t epochs_done = 0;     // shuffling seed
 };
 
 namespace {
@@ -62,6 +74,8 @@ bg_guide_opts default_opts() {
     o.warmup_passes = 4;
     o.flags = 0;
     o.seed = 0;
+    o.pass_paths = 1u << 22;
+    o.epochs = 1;
     return o;
 }
 
@@ -144,7 +158,7 @@ bg_status ensure_guide_wave(bg_guide* g, uint32_t cap) {
     g->query = (float4*)p;
     if ((st = dalloc(ctx, n * sizeof(uint32_t), &p, &g->wave_allocs)) != BG_OK) return st;
     g->gslot = (uint32_t*)p;
-    if ((st = dalloc(ctx, n * bg::GUIDE_RAW_STRIDE * sizeof(float), &p, &g->wave_allocs)) != BG_OK) return st;
+    if ((st = dalloc(ctx, n * bg::GUIDE_MIX_STRIDE * sizeof(float), &p, &g->wave_allocs)) != BG_OK) return st;
     g->raw = (float*)p;
     g->wcap = cap;
     return BG_OK;
@@ -174,29 +188,56 @@ bg_status upload_samples(bg_guide* g, const float* samples, size_t n, float4** d
     return BG_OK;
 }
 
-// Batches of the sample buffer -> Adam steps (all asynchronous).  Returns the number of steps.
-int train_batches(bg_guide* g, const float4* samples, uint32_t n) {
+uint32_t gcd32(uint32_t a, uint32_t b) {
+    while (b) {
+        uint32_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// A pseudo-random visiting order of n pool entries for one epoch (multiplier coprime to n).
+bg::PoolOrder pool_order(uint32_t n, uint64_t epoch) {
+    bg::PoolOrder o{n, 1u, 0u, 0u};
+    if (n < 2) return o;
+    uint64_t h = (epoch + 1) * 0x9E3779B97F4A7C15ull;
+    uint32_t mul = (uint32_t)(h >> 33) % n;
+    while (mul < 2 || gcd32(mul, n) != 1) mul = (mul + 1) % n;
+    o.perm_mul = mul;
+    o.perm_add = (uint32_t)(h & 0xFFFFFFFFu) % n;
+    return o;
+}
+
+// `epochs` passes over n samples in shuffled batches -> Adam steps (all asynchronous).  Returns the
+// number of steps.
+int train_batches(bg_guide* g, const float4* samples, uint32_t n, uint32_t epochs, uint64_t* epoch_counter) {
     bg_ctx* ctx = g->ctx;
     const uint32_t B = g->o.batch_size;
     const uint32_t nb = (n + B - 1) / B;
-    bg::launch_guide_wsum(samples, n, B, g->wsum, ctx->stream);
     cudaMemsetAsync(g->stats, 0, 2 * sizeof(float), ctx->stream);
     bg::GuideAdam h{g->o.learning_rate, g->o.beta1, g->o.beta2, g->o.eps};
-    for (uint32_t b = 0; b < nb; ++b) {
-        bg::GuideTrainArgs a{};
-        a.wpack = g->wpack;
-        a.samples = samples + (size_t)b * B * bg::GUIDE_SAMPLE_F4;
-        a.n = std::min(B, n - b * B);
-        a.wsum = g->wsum + b;
-        a.alpha = g->o.alpha;
-        a.grad = g->grad;
-        a.stats = g->stats;
-        a.step = g->step;
-        a.err = ctx->d_err;
-        bg::launch_guide_train(a, ctx->stream);
-        bg::launch_guide_adam(g->params, g->m, g->v, g->grad, g->wpack, g->step, h, ctx->stream);
+    for (uint32_t e = 0; e < epochs; ++e) {
+        bg::PoolOrder order = pool_order(n, (*epoch_counter)++);
+        bg::launch_guide_wsum(samples, order, B, g->wsum, ctx->stream);
+        for (uint32_t b = 0; b < nb; ++b) {
+            bg::GuideTrainArgs a{};
+            a.wpack = g->wpack;
+            a.samples = samples;
+            a.order = order;
+            a.base = b * B;
+            a.n = std::min(B, n - b * B);
+            a.wsum = g->wsum + b;
+            a.alpha = g->o.alpha;
+            a.grad = g->grad;
+            a.stats = g->stats;
+            a.step = g->step;
+            a.err = ctx->d_err;
+            bg::launch_guide_train(a, ctx->stream);
+            bg::launch_guide_adam(g->params, g->m, g->v, g->grad, g->wpack, g->step, h, ctx->stream);
+        }
     }
-    return (int)nb;
+    return (int)(nb * epochs);
 }
 
 }  // namespace
@@ -221,6 +262,9 @@ bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out
     if (o.batch_size == 0 || o.batch_size % 128 != 0) return fail(ctx, BG_ERR_INVALID, "batch_size must be a positive multiple of 128");
     if (o.samples_per_pass < 128 || o.samples_per_pass > (1u << 24))
         return fail(ctx, BG_ERR_INVALID, "samples_per_pass must be in [128, 2^24]");
+    if (o.pass_paths == 0) o.pass_paths = 1u << 22;
+    if (o.epochs == 0) o.epochs = 1;
+    if (o.epochs > 64) return fail(ctx, BG_ERR_INVALID, "epochs must be <= 64");
     if (!(o.learning_rate > 0.0f) || !(o.alpha >= 0.0f && o.alpha <= 1.0f) || !(o.beta1 >= 0.0f && o.beta1 < 1.0f) ||
         !(o.beta2 >= 0.0f && o.beta2 < 1.0f) || !(o.eps > 0.0f))
         return fail(ctx, BG_ERR_INVALID, "bad optimiser settings");
@@ -314,8 +358,8 @@ bg_status bg_guide_forward(bg_guide* g, const float* queries, size_t n, float* o
     std::vector<float> raw;
     if (st == BG_OK) {
         cudaMemcpyAsync(dq, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
-        bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)n, (float*)dr, ctx->d_err, ctx->shape.sms,
-                               ctx->stream);
+        bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)n, (float*)dr, false, ctx->d_err,
+                               ctx->shape.sms, ctx->stream);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_infer");
     }
@@ -344,10 +388,13 @@ bg_status bg_guide_gradient(bg_guide* g, const float* samples, size_t n, float* 
     if (st == BG_OK) {
         cudaMemsetAsync(g->grad, 0, bg::GUIDE_PARAMS * sizeof(float), ctx->stream);
         cudaMemsetAsync(g->stats, 0, 2 * sizeof(float), ctx->stream);
-        bg::launch_guide_wsum(ds, (uint32_t)n, (uint32_t)n, g->wsum, ctx->stream);
+        const bg::PoolOrder order{(uint32_t)n, 1u, 0u, 0u};
+        bg::launch_guide_wsum(ds, order, (uint32_t)n, g->wsum, ctx->stream);
         bg::GuideTrainArgs a{};
         a.wpack = g->wpack;
         a.samples = ds;
+        a.order = order;
+        a.base = 0;
         a.n = (uint32_t)n;
         a.wsum = g->wsum;
         a.alpha = g->o.alpha;
@@ -387,7 +434,7 @@ bg_status bg_guide_train(bg_guide* g, const float* samples, size_t n, float* los
     bg_status st = upload_samples(g, samples, n, &ds, &tmp);
     int nb = 0;
     if (st == BG_OK) {
-        nb = train_batches(g, ds, (uint32_t)n);
+        nb = train_batches(g, ds, (uint32_t)n, 1, &g->epochs_done);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) st = cuda_fail(ctx, e, "guide training");
     }
@@ -402,6 +449,19 @@ bg_status bg_guide_train(bg_guide* g, const float* samples, size_t n, float* los
     dfree_all(ctx, tmp);
     if (st == BG_OK && loss) *loss = nb ? stats[0] / (float)nb : 0.0f;
     return st;
+}
+
+bg_status bg_guide_pool(bg_guide* g, float* out, size_t max_n, size_t* n_out) {
+    if (!g || !g->ctx || (max_n && !out)) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    const size_t n = std::min<size_t>(max_n, g->pool_n);
+    CK(cudaSetDevice(ctx->device));
+    if (n) {
+        CK(cudaMemcpyAsync(out, g->pool, n * bg::GUIDE_SAMPLE_F4 * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (n_out) *n_out = n;
+    return BG_OK;
 }
 
 bg_status bg_guide_mixture_eval(bg_guide* g, const float* raw, const float* u, const float* w, const float* p_bsdf,
@@ -452,7 +512,8 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         CK(cudaMemsetAsync(ctx->film.nan_count, 0, sizeof(unsigned long long), ctx->stream));
     }
     const uint64_t npix = (uint64_t)cam->width * cam->height;
-    const uint32_t cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, npix);
+    const uint32_t pass_spp = (uint32_t)std::max<uint64_t>(1, g->o.pass_paths / npix);
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, npix * std::min(pass_spp, std::max(o->spp, 1u)));
     if ((st = ensure_wave(ctx, cap)) != BG_OK) return st;
     if ((st = ensure_guide_wave(g, cap)) != BG_OK) return st;
     if ((st = ensure_pass(g, npix)) != BG_OK) return st;
@@ -480,28 +541,30 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
     const bool train = !(g->o.flags & BG_GUIDE_NO_TRAIN);
     const bool allow_fallback = !(g->o.flags & BG_GUIDE_NO_FALLBACK);
     bg_guide_stats gs{};
-    double rv_plain_sum = 0, ms_plain_sum = 0, rv_guided_recent[4] = {0, 0, 0, 0}, ms_guided_recent[4] = {0, 0, 0, 0};
-    uint32_t n_plain = 0, n_guided_eval = 0;
-    bool fallback = false;
-    float keep = 1.0f;
     uint64_t launches = 0;
     CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
-    for (uint32_t p = 0; p < o->spp; ++p) {
-        const bool guided = p >= g->o.warmup_passes && !fallback;
-        const bool record = train && !fallback;
+    CK(cudaEventRecord(g->ev[3], ctx->stream));
+    unsigned long long rays[2] = {0, 0};
+    uint32_t done = 0;
+    for (; done < o->spp && !g->fallback;) {
+        const uint32_t k = std::min(pass_spp, o->spp - done);
+        const bool guided = g->passes_total >= g->o.warmup_passes && !g->fallback;
+        const bool record = train && !g->fallback;
         gw.flags = (record ? bg::GW_RECORD : 0u) | (guided ? bg::GW_GUIDED : 0u);
-        gw.keep_prob = keep;
+        gw.keep_prob = g->keep;
         CK(cudaMemsetAsync(g->ctr, 0, 2 * sizeof(uint32_t), ctx->stream));
         CK(cudaMemsetAsync(g->relvar, 0, 2 * sizeof(double), ctx->stream));
+        CK(cudaMemsetAsync(g->pass, 0, npix * 3 * sizeof(float), ctx->stream));
         CK(cudaEventRecord(g->ev[0], ctx->stream));
-        bg::RenderParams rp{cam->width, cam->height, 1u, o->max_depth, o->first_sample + p, o->rr_threshold, o->seed};
-        for (uint64_t item0 = 0; item0 < npix; item0 += cap) {
-            uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, npix - item0);
+        bg::RenderParams rp{cam->width, cam->height, k, o->max_depth, o->first_sample + done, o->rr_threshold, o->seed};
+        const uint64_t items = npix * k;
+        for (uint64_t item0 = 0; item0 < items; item0 += cap) {
+            uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, items - item0);
             launches += (uint64_t)bg::launch_wave(s->dev, dc, rp, film, ctx->wave, item0, nitems, ctx->d_err, ctx->shape,
                                                   ctx->stream, nullptr, &gw);
         }
-        bg::launch_pass_relvar(film, g->relvar, ctx->stream);
+        done += k;
+        bg::launch_pass_relvar(film, k, g->relvar, ctx->stream);
         launches += 1;
         CK(cudaGetLastError());
         CK(cudaEventRecord(g->ev[1], ctx->stream));
@@ -514,15 +577,17 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         CK(cudaEventElapsedTime(&pass_ms, g->ev[0], g->ev[1]));
         gs.render_ms += pass_ms;
         gs.passes += 1;
+        g->passes_total += 1;
         gs.guided_passes += guided ? 1 : 0;
         gs.records += ctr[0];
         const uint32_t pool_n = std::min(ctr[1], g->pool_cap);
+        g->pool_n = pool_n;
         gs.pool_samples += pool_n;
-        keep = ctr[0] > 0 ? std::min(1.0f, (float)g->pool_cap / (float)ctr[0]) : 1.0f;
+        g->keep = ctr[0] > 0 ? std::min(1.0f, (float)g->pool_cap / (float)ctr[0]) : 1.0f;
         float train_ms = 0.0f;
         if (record && pool_n >= 128) {
-            int nb = train_batches(g, g->pool, pool_n);
-            launches += 1 + 2 * (uint64_t)nb;
+            int nb = train_batches(g, g->pool, pool_n, g->o.epochs, &g->epochs_done);
+            launches += g->o.epochs + 2 * (uint64_t)nb;
             CK(cudaGetLastError());
             CK(cudaEventRecord(g->ev[2], ctx->stream));
             float ls[2] = {0, 0};
@@ -531,60 +596,79 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
             CK(cudaEventElapsedTime(&train_ms, g->ev[1], g->ev[2]));
             gs.train_ms += train_ms;
             gs.adam_steps += (uint32_t)nb;
-            gs.last_loss = ls[0] / (double)nb;
+            gs.last_loss = ls[0] / (double)nb;  // mean batch loss of this pass's steps
         }
         // variance bookkeeping (relative variance per sample of this pass, see k_pass_relvar)
         if (rv[1] > 0.0) {
             const double relvar = rv[0] / rv[1];
             if (guided) {
-                rv_guided_recent[n_guided_eval % 4] = relvar;
-                ms_guided_recent[n_guided_eval % 4] = pass_ms + train_ms;
-                n_guided_eval += 1;
-            } else if (!fallback) {
-                rv_plain_sum += relvar;
-                ms_plain_sum += pass_ms;
-                n_plain += 1;
+                g->rv_guided[g->n_guided % bg_guide::kWindow] = relvar;
+                g->ms_guided[g->n_guided % bg_guide::kWindow] = pass_ms + train_ms;
+                g->n_guided += 1;
+            } else if (!g->fallback) {
+                g->rv_plain_sum += relvar;
+                g->ms_plain_sum += pass_ms;
+                g->n_plain += 1;
             }
         }
-        if (n_plain) {
-            gs.relvar_plain = rv_plain_sum / n_plain;
-            gs.ms_plain = ms_plain_sum / n_plain;
-        }
-        if (n_guided_eval) {
-            uint32_t k = std::min(n_guided_eval, 4u);
+        if (guided && allow_fallback && g->n_plain >= 1 && g->n_guided >= bg_guide::kWindow / 2) {
+            const uint32_t k = std::min(g->n_guided, bg_guide::kWindow);
             double a = 0, b = 0;
             for (uint32_t i = 0; i < k; ++i) {
-                a += rv_guided_recent[i];
-                b += ms_guided_recent[i];
+                a += g->rv_guided[i];
+                b += g->ms_guided[i];
             }
-            gs.relvar_guided = a / k;
-            gs.ms_guided = b / k;
+            if ((a / k) * (b / k) >= (g->rv_plain_sum / g->n_plain) * (g->ms_plain_sum / g->n_plain)) g->fallback = true;
         }
-        if (guided && allow_fallback && n_plain >= 1 && n_guided_eval >= 2 &&
-            gs.relvar_guided * gs.ms_guided >= gs.relvar_plain * gs.ms_plain)
-            fallback = true;
     }
-    gs.fallback = fallback ? 1u : 0u;
+    if (g->n_plain) {
+        gs.relvar_plain = g->rv_plain_sum / g->n_plain;
+        gs.ms_plain = g->ms_plain_sum / g->n_plain;
+    }
+    if (g->n_guided) {
+        const uint32_t k = std::min(g->n_guided, bg_guide::kWindow);
+        for (uint32_t i = 0; i < k; ++i) {
+            gs.relvar_guided += g->rv_guided[i] / k;
+            gs.ms_guided += g->ms_guided[i] / k;
+        }
+    }
+    gs.fallback = g->fallback ? 1u : 0u;
+    if (done < o->spp) {
+        // after the fallback: the rest of the samples through the plain graph-captured wavefront
+        bg_render_opts po = *o;
+        po.spp = o->spp - done;
+        po.first_sample = o->first_sample + done;
+        po.flags = BG_RENDER_ACCUMULATE | BG_RENDER_NO_READBACK | BG_RENDER_GRAPH;
+        bg_render_stats ps{};
+        CK(cudaMemcpyAsync(rays, ctx->wave.ray_stats, sizeof(rays), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if ((st = bg_render(ctx, s, cam, &po, nullptr, &ps)) != BG_OK) return st;
+        gs.render_ms += ps.device_ms;
+        launches += ps.launches;
+        rays[0] += ps.extension_rays;
+        rays[1] += ps.shadow_rays;
+    } else {
+        CK(cudaMemcpyAsync(rays, ctx->wave.ray_stats, sizeof(rays), cudaMemcpyDeviceToHost, ctx->stream));
+    }
     bg::launch_resolve(ctx->film, ctx->stream);
     launches += 1;
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    CK(cudaEventRecord(g->ev[4], ctx->stream));
     uint32_t word = 0;
     st = check_device_error(ctx, &word);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         float ms = 0.0f;
-        cudaEventElapsedTime(&ms, ctx->ev_begin, ctx->ev_end);
+        cudaEventElapsedTime(&ms, g->ev[3], g->ev[4]);
         stats->device_ms = ms;
         stats->samples = npix * o->spp;
         stats->launches = launches;
         stats->error_word = word;
-        unsigned long long nan = 0, rs[2] = {0, 0};
+        unsigned long long nan = 0;
         cudaMemcpy(&nan, ctx->film.nan_count, sizeof(nan), cudaMemcpyDeviceToHost);
-        cudaMemcpy(rs, ctx->wave.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
         stats->nan_samples = nan;
-        stats->extension_rays = rs[0];
-        stats->shadow_rays = rs[1];
+        stats->extension_rays = rays[0];
+        stats->shadow_rays = rays[1];
     }
     if (gstats) *gstats = gs;
     if (st != BG_OK) return st;

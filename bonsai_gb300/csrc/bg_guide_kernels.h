@@ -6,12 +6,29 @@
 
 #include "bg_kernels.h"
 
+#ifdef __CUDACC__
+#define BG_HD_ORDER __host__ __device__ __forceinline__
+#else
+#define BG_HD_ORDER inline
+#endif
+
 namespace bg {
+
+// Sample j of a batch (j < n) is pool entry ((base + j) * perm_mul + perm_add) mod n_total: with
+// perm_mul coprime to n_total this visits the pool in a shuffled order, epoch by epoch.
+struct PoolOrder {
+    uint32_t n_total, perm_mul, perm_add, pad;
+    BG_HD_ORDER uint32_t at(uint32_t j) const {
+        return (uint32_t)(((uint64_t)j * perm_mul + perm_add) % n_total);
+    }
+};
 
 struct GuideTrainArgs {
     const uint8_t* wpack;    // BF16 weight image
-    const float4* samples;   // 4 float4 per sample
-    uint32_t n;              // samples (rows past n are zero-weight)
+    const float4* samples;   // 4 float4 per sample (the whole pool)
+    PoolOrder order;
+    uint32_t base;           // first batch position
+    uint32_t n;              // samples in this batch (rows past n are zero-weight)
     const float* wsum;       // sum of the batch's weights (device scalar)
     float alpha;             // loss blend, see guide_loss_grad
     float* grad;             // FP32 gradient accumulator (GUIDE_PARAMS)
@@ -24,18 +41,22 @@ struct GuideAdam {
     float lr, beta1, beta2, eps;
 };
 
-void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* raw,
-                        uint32_t* err, int sms, cudaStream_t s);
+// Forward pass over the queries; count (device, optional) caps max_n.  out: raw outputs
+// (GUIDE_RAW_STRIDE floats per query) or, with mixture, parsed mixture records (GUIDE_MIX_STRIDE).
+void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* out,
+                        bool mixture, uint32_t* err, int sms, cudaStream_t s);
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s);
 void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
                        const GuideAdam& h, cudaStream_t s);
 void launch_guide_pack(const float* p, uint8_t* wpack, cudaStream_t s);
-void launch_guide_wsum(const float4* samples, uint32_t n, uint32_t batch, float* wsum, cudaStream_t s);
+// wsum[b] = sum of the positive finite weights of batch b (positions b*batch .. in `order`).
+void launch_guide_wsum(const float4* samples, const PoolOrder& order, uint32_t batch, float* wsum, cudaStream_t s);
 // Relative variance of this pass's samples (film.pass) against the mean of the earlier passes:
-// out[0] += sum over pixels with >= 2 samples and channels of (x - m)^2 / (m^2 + 0.01) * (n - 1) / n,
-// out[1] += number of terms.  (n - 1) / n removes the variance of m itself, so out[0] / out[1]
-// estimates the relative variance of one sample.
-void launch_pass_relvar(const FilmBuffers& film, double* out, cudaStream_t s);
+// film.pass holds the sum of this pass's k samples per pixel.  With x = pass / k and m the mean of
+// the n - k earlier samples, (x - m)^2 has expectation var (1/k + 1/(n - k)), so
+// out[0] += sum over pixels with n > k and channels of (x - m)^2 / (m^2 + 0.01) / (1/k + 1/(n - k)),
+// out[1] += number of terms: out[0] / out[1] estimates the relative variance of one sample.
+void launch_pass_relvar(const FilmBuffers& film, uint32_t k, double* out, cudaStream_t s);
 void launch_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
                                float alpha, float* out, cudaStream_t s);
 

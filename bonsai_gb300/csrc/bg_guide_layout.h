@@ -29,6 +29,9 @@ constexpr int GUIDE_PARAMS = 4 * GUIDE_HID * GUIDE_K + GUIDE_OUT_ROWS * GUIDE_K;
 constexpr uint32_t GUIDE_ROWGROUP_BYTES = 8 * GUIDE_K * 2;                      // 1280
 constexpr uint32_t GUIDE_WPACK_BYTES = (4 * GUIDE_HID + GUIDE_OUT_ROWS) * GUIDE_K * 2;  // 48,640
 constexpr int GUIDE_RAW_STRIDE = 48;  // floats per query in the raw output buffer
+// Parsed mixture record written by the render-side inference (floats): lobe i at 4i = mean
+// direction xyz, kappa; 32 + i = log normalisation; 40 + i = weight; 48 = c; padded to 52.
+constexpr int GUIDE_MIX_STRIDE = 52;
 constexpr int GUIDE_QUERY_F4 = 3;     // query = 3 float4: p.xyz n.x | n.yz wo.xy | wo.z - - -
 constexpr int GUIDE_SAMPLE_F4 = 4;    // training sample = query + wi.xyz (f2.yzw) + p_bsdf, weight (f3.xy)
 

@@ -64,9 +64,9 @@ BG_D void film_add(const FilmBuffers& f, uint32_t pix, RGB L) {
     atomicAdd(&f.sumsq[3 * pix + 2], b * b);
     atomicAdd(&f.count[pix], 1u);
     if (f.pass) {
-        f.pass[3 * pix + 0] = L.r;
-        f.pass[3 * pix + 1] = L.g;
-        f.pass[3 * pix + 2] = L.b;
+        atomicAdd(&f.pass[3 * pix + 0], L.r);
+        atomicAdd(&f.pass[3 * pix + 1], L.g);
+        atomicAdd(&f.pass[3 * pix + 2], L.b);
     }
 }
 
@@ -275,8 +275,18 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10 };
 constexpr uint32_t ST_REC_SHIFT = 12, ST_REC_MASK = 0xFu << ST_REC_SHIFT;
 enum : uint32_t {
-    C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6, C_GUIDE = 11
+    C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6,
+    C_GUIDE = 11,  // 11..13: guided queries of the matte, plastic and conductor classes
+    C_GSPAN = 14   // end of the guided-query range (written by the dielectric shade launch)
 };
+// Guided queries of class c occupy [guide_base(c), guide_base(c) + counters[C_GUIDE + c]) of the
+// query buffer, guide_base(c) = sizes of the class queues before c, so each class's continuation
+// runs as its own launch with a static BSDF type.
+BG_D uint32_t guide_base(const WaveBuffers& wb, int cls) {
+    uint32_t b = 0;
+    for (int c = 0; c < cls; ++c) b += wb.counters[C_CLS + c];
+    return b;
+}
 constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
 constexpr int CLS_MISS = 4;
 
@@ -327,7 +337,8 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
         wb.counters[C_EXT_HEAD] = 0;
         wb.counters[C_SH_HEAD] = 0;
         for (int c = 0; c < NCLS; ++c) wb.counters[C_CLS + c] = 0;
-        wb.counters[C_GUIDE] = 0;
+        for (int c = 0; c < 3; ++c) wb.counters[C_GUIDE + c] = 0;
+        wb.counters[C_GSPAN] = 0;
     }
 }
 
@@ -478,26 +489,170 @@ BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot
     if (lane_id() == 0 && tot) atomicAdd(&gw.ctr[0], tot);
 }
 
+// Everything a non-specular or specular vertex does after its emission: next-event estimation
+// (uniform_sample_one_light + estimate_direct, src/base/integrator.rs:309-437, the occlusion tests
+// deferred to k_shadow), the BSDF-sampled continuation (src/integrators/path.rs:110-143) and
+// Russian roulette.  `mix` (guided vertices) replaces the BSDF in estimate_direct's second
+// strategy by the one-sample mixture c * guide + (1 - c) * BSDF: the direction is drawn from it and
+// both MIS weights use its pdf, so the estimator stays unbiased whatever the network outputs.
+struct VertexOut {
+    bool cont = false, finished = false;
+    bool push_sh[2] = {false, false};
+    float4 sh_o[2], sh_d[2];
+};
+
+template <int CLS>
+BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
+                         uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
+                         uint32_t& state, const MixView* mix, const float* ug, VertexOut& out) {
+    constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
+    Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
+    const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
+    float u[8];
+    rng.block(ub, u);
+    rng.block(ub + 4, u + 4);
+    BSDF bsdf = make_bsdf<CLS>(sc, it);
+    if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
+        const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
+        float count = (float)sc.nlights;
+        uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
+        float4 pend[2] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+        // pdf of the second strategy for a direction
+        auto strategy_pdf = [&](V3 w) {
+            float pb = bsdf.pdf<false>(it.wo, w, flags);
+            if (!mix) return pb;
+            const float c = mix->c();
+            return c * mix->pdf(w) + (1.0f - c) * pb;
+        };
+        LightSample ls = light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+        if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
+            RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
+            if (!is_black(f)) {
+                float w = power_heuristic(1.0f, ls.pdf, 1.0f, strategy_pdf(ls.wi));
+                RGB c = f * ls.radiance * w / ls.pdf;
+                Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
+                pend[0] = make_float4(c.r, c.g, c.b, 0.0f);
+                out.sh_o[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.t_max);
+                out.sh_d[0] = make_float4(sr.d.x, sr.d.y, sr.d.z, __int_as_float(-1));
+                out.push_sh[0] = true;
+            }
+        }
+        // second strategy: a direction from the BSDF (or the mixture), counted when it reaches the
+        // chosen light
+        V3 wi;
+        RGB f;
+        float spdf;
+        if (GUIDABLE && mix && ug[0] < mix->c()) {
+            wi = mix->sample(ug[1], ug[2], ug[3]);
+            f = bsdf.f<false>(it.wo, wi, flags) * abs_dot(wi, it.ns);
+            spdf = strategy_pdf(wi);
+        } else {
+            BxSample bs = bsdf.sample<false>(it.wo, u[BD_USCAT], u[BD_USCAT + 1], flags);
+            wi = bs.wi;
+            f = bs.f * abs_dot(bs.wi, it.ns);
+            spdf = mix ? (bs.pdf > 0.0f ? strategy_pdf(bs.wi) : 0.0f) : bs.pdf;
+        }
+        if (!is_black(f) && spdf > 0.0f) {
+            float t_light = 0.0f;
+            float lpdf = light_pdf<false>(sc, light_prim, it, wi, &t_light);
+            if (lpdf != 0.0f) {
+                float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
+                // the sampled direction reaches the light at t_light; it counts iff nothing else
+                // is hit first (closest hit == this light)
+                V3 p0, p1, p2;
+                load_tri(sc, light_prim, &p0, &p1, &p2);
+                V3 ln = normalize(cross(p0 - p2, p1 - p2));
+                RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -wi);
+                if (!is_black(li)) {
+                    RGB c = f * li * w / spdf;
+                    Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
+                    pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
+                    out.sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
+                    out.sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float((int)light_prim));
+                    out.push_sh[1] = true;
+                }
+            }
+        }
+        wb.pending[2 * slot] = pend[0];
+        wb.pending[2 * slot + 1] = pend[1];
+        wb.nee_beta[slot] = make_float4(beta.r, beta.g, beta.b, 0.0f);
+        state |= ST_PENDING;
+    }
+    V3 wo = -ray.d;
+    BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+    if (is_black(bs.f) || bs.pdf == 0.0f) {
+        out.finished = true;
+        return;
+    }
+    RGB beta0 = beta;
+    beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
+    bool spec = (bs.stype & BSDF_SPECULAR) != 0;
+    if (spec && (bs.stype & BSDF_TRANSMISSION)) {
+        float eta = bsdf.eta;
+        eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
+    }
+    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
+    RGB rr_beta = beta * eta_scale;
+    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
+        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
+        if (u[BD_RR] < qq) {
+            out.finished = true;
+            return;
+        }
+        beta = beta / (1.0f - qq);
+    }
+    wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
+    wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
+    state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
+    if (GUIDABLE && (gw.flags & GW_RECORD))
+        state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
+    out.cont = true;
+}
+
+// Warp-convergent tail of k_shade / k_guide_continue: queue compaction, shadow rays, records.
+BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t slot, bool cont,
+                        bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, uint32_t* err) {
+    uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
+    if (cont) wb.queue[(bounce + 1) & 1][pos] = slot;
+    pos = warp_append(&wb.counters[C_DONE], done_pending);
+    if (done_pending) wb.done[pos] = slot;
+    for (int k = 0; k < 2; ++k) {
+        pos = warp_append(&wb.counters[C_SHADOW], vo.push_sh[k]);
+        if (vo.push_sh[k]) {
+            if (pos < 2 * wb.capacity) {
+                wb.sh_o[pos] = vo.sh_o[k];
+                wb.sh_d[pos] = vo.sh_d[k];
+                wb.sh_ref[pos] = 2 * slot + (uint32_t)k;
+            } else {
+                atomicOr(err, ERR_QUEUE_OVERFLOW);
+            }
+        }
+    }
+    if (gw.flags & GW_RECORD) emit_records(gw, wb, slot, emit_n, L_emit);
+}
+
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
-// In guided waves the matte / plastic / conductor classes stop after next-event estimation and
-// queue a network query; k_guide_continue samples their continuation.
+// In guided waves the matte / plastic / conductor classes stop after their emission and queue a
+// network query; k_guide_continue finishes them with the network's mixture.
 template <int CLS>
 __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
-    uint32_t* qn = wb.queue[(bounce + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
     const bool record = (gw.flags & GW_RECORD) != 0;
+    const bool guided = GUIDABLE && (gw.flags & GW_GUIDED);
+    const uint32_t gbase = GUIDABLE ? guide_base(wb, CLS) : 0u;
+    if (CLS == 3 && (gw.flags & GW_GUIDED) && blockIdx.x == 0 && threadIdx.x == 0)
+        wb.counters[C_GSPAN] = guide_base(wb, 2) + wb.counters[C_GUIDE + 2];  // classes 0..2 are done
     // warp-uniform loop so the ballots below see all 32 lanes
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
         uint32_t i = base + lane_id();
         bool active = i < n;
         uint32_t slot = active ? q[i] : 0;
         bool cont = false, done_pending = false, push_guide = false;
-        bool push_sh[2] = {false, false};
-        float4 sh_o[2], sh_d[2];
+        VertexOut vo;
         GuideQuery gq;
         uint32_t emit_n = 0;
         RGB L_emit = rgb(0.0f);
@@ -512,105 +667,24 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
             float4 l4 = wb.L[slot];
             RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
             state &= ~ST_PENDING;
-            if (record) state = close_record(gw, wb, slot, state, L);
             bool specular_bounce = (state & ST_SPECULAR) != 0;
             Isect it;
             bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
-            if (bounce == 0 || specular_bounce) {
-                if (hit) L = L + beta * emitted_radiance(sc, it, -ray.d);
-            }
+            const bool counted = bounce == 0 || specular_bounce;
+            RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
+            // The previous vertex's record closes here.  Its training target also takes this
+            // emission, which the estimator leaves to that vertex's next-event estimation: the
+            // network learns the directions of lights as well, for the strategy it serves.
+            if (record) state = close_record(gw, wb, slot, state, counted ? L : L - beta * le);
+            if (counted) L = L + beta * le;
             bool finished = !hit || bounce >= rp.max_depth;
-            if (!finished) {
-                Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
-                const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
-                float u[8];
-                rng.block(ub, u);
-                rng.block(ub + 4, u + 4);
-                BSDF bsdf = make_bsdf<CLS>(sc, it);
-                if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
-                    // uniform_sample_one_light + estimate_direct, occlusion deferred to k_shadow
-                    const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
-                    float count = (float)sc.nlights;
-                    uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
-                    float4 pend[2] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
-                    LightSample ls = light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
-                    if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
-                        RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
-                        float spdf = bsdf.pdf<false>(it.wo, ls.wi, flags);
-                        if (!is_black(f)) {
-                            float w = power_heuristic(1.0f, ls.pdf, 1.0f, spdf);
-                            RGB c = f * ls.radiance * w / ls.pdf;
-                            Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
-                            pend[0] = make_float4(c.r, c.g, c.b, 0.0f);
-                            sh_o[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.t_max);
-                            sh_d[0] = make_float4(sr.d.x, sr.d.y, sr.d.z, __int_as_float(-1));
-                            push_sh[0] = true;
-                        }
-                    }
-                    BxSample bs = bsdf.sample<false>(it.wo, u[BD_USCAT], u[BD_USCAT + 1], flags);
-                    RGB f = bs.f * abs_dot(bs.wi, it.ns);
-                    if (!is_black(f) && bs.pdf > 0.0f) {
-                        float t_light = 0.0f;
-                        float lpdf = light_pdf<false>(sc, light_prim, it, bs.wi, &t_light);
-                        if (lpdf != 0.0f) {
-                            float w = power_heuristic(1.0f, bs.pdf, 1.0f, lpdf);
-                            // the sampled direction reaches the light at t_light; it counts iff
-                            // nothing else is hit first (closest hit == this light)
-                            V3 p0, p1, p2;
-                            load_tri(sc, light_prim, &p0, &p1, &p2);
-                            V3 ln = normalize(cross(p0 - p2, p1 - p2));
-                            RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -bs.wi);
-                            if (!is_black(li)) {
-                                RGB c = f * li * w / bs.pdf;
-                                Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
-                                pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
-                                sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
-                                sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float((int)light_prim));
-                                push_sh[1] = true;
-                            }
-                        }
-                    }
-                    wb.pending[2 * slot] = pend[0];
-                    wb.pending[2 * slot + 1] = pend[1];
-                    wb.nee_beta[slot] = make_float4(beta.r, beta.g, beta.b, 0.0f);
-                    state |= ST_PENDING;
-                }
-                V3 wo = -ray.d;
-                if (GUIDABLE && (gw.flags & GW_GUIDED)) {
-                    gq = make_query(gw, it, wo);
-                    push_guide = true;
-                } else {
-                    BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
-                    if (is_black(bs.f) || bs.pdf == 0.0f) {
-                        finished = true;
-                    } else {
-                        RGB beta0 = beta;
-                        beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
-                        bool spec = (bs.stype & BSDF_SPECULAR) != 0;
-                        if (spec && (bs.stype & BSDF_TRANSMISSION)) {
-                            float eta = bsdf.eta;
-                            eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
-                        }
-                        Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
-                        RGB rr_beta = beta * eta_scale;
-                        bool killed = false;
-                        if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
-                            float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
-                            if (u[BD_RR] < qq) killed = true;
-                            else beta = beta / (1.0f - qq);
-                        }
-                        if (killed) {
-                            finished = true;
-                        } else {
-                            wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
-                            wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
-                            state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-                            if (GUIDABLE && record)
-                                state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
-                            cont = true;
-                        }
-                    }
-                }
+            if (!finished && guided) {
+                gq = make_query(gw, it, -ray.d);
+                push_guide = true;
+            } else if (!finished) {
+                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, vo);
+                finished = vo.finished;
+                cont = vo.cont;
             }
             wb.state[slot] = state;
             wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
@@ -625,25 +699,8 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
                 }
             }
         }
-        // compaction (convergent)
-        uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
-        if (cont) qn[pos] = slot;
-        pos = warp_append(&wb.counters[C_DONE], done_pending);
-        if (done_pending) wb.done[pos] = slot;
-        for (int k = 0; k < 2; ++k) {
-            pos = warp_append(&wb.counters[C_SHADOW], push_sh[k]);
-            if (push_sh[k]) {
-                if (pos < 2 * wb.capacity) {
-                    wb.sh_o[pos] = sh_o[k];
-                    wb.sh_d[pos] = sh_d[k];
-                    wb.sh_ref[pos] = 2 * slot + (uint32_t)k;
-                } else {
-                    atomicOr(err, ERR_QUEUE_OVERFLOW);
-                }
-            }
-        }
         if (GUIDABLE && (gw.flags & GW_GUIDED)) {
-            pos = warp_append(&wb.counters[C_GUIDE], push_guide);
+            uint32_t pos = gbase + warp_append(&wb.counters[C_GUIDE + (GUIDABLE ? CLS : 0)], push_guide);
             if (push_guide && pos >= gw.cap) {
                 atomicOr(err, ERR_QUEUE_OVERFLOW);  // cannot happen: one query per path of the wave
                 push_guide = false;
@@ -655,26 +712,26 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
                 gw.gslot[pos] = slot;
             }
         }
-        if (record) emit_records(gw, wb, slot, emit_n, L_emit);
+        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, err);
     }
 }
 
-// Continuation of guided vertices: one-sample MIS between the network's vMF mixture (probability
-// c) and the BSDF (1 - c); the throughput is weighted by the mixture pdf
-//   p(wi) = c q(wi) + (1 - c) p_bsdf(wi),
-// so the estimator stays unbiased whatever the network outputs.  Uniforms: BSDF and roulette dims
-// of the bounce (shared with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce.
+// Guided vertices of one material class, after the network has evaluated them: scatter_vertex with
+// the network's mixture in the second direct-light strategy.  Uniforms: the bounce's dims (shared
+// with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce (mixture choice, lobe,
+// cos theta, phi).
+template <int CLS>
 __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
                                                         GuideWave gw, uint32_t bounce, uint32_t* err) {
-    const uint32_t n = min(wb.counters[C_GUIDE], gw.cap);
-    uint32_t* qn = wb.queue[(bounce + 1) & 1];
+    const uint32_t gbase = guide_base(wb, CLS);
+    const uint32_t n = min(wb.counters[C_GUIDE + CLS], gw.cap - min(gbase, gw.cap));
     const uint32_t stride = gridDim.x * blockDim.x;
-    const bool record = (gw.flags & GW_RECORD) != 0;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
-        uint32_t i = base + lane_id();
-        bool active = i < n;
+        uint32_t i = gbase + base + lane_id();
+        bool active = base + lane_id() < n;
         uint32_t slot = active ? gw.gslot[i] : 0;
         bool cont = false, done_pending = false;
+        VertexOut vo;
         uint32_t emit_n = 0;
         RGB L_emit = rgb(0.0f);
         if (active) {
@@ -683,67 +740,18 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
             uint32_t state = wb.state[slot];
             float4 b4 = wb.beta[slot];
             RGB beta = rgb(b4.x, b4.y, b4.z);
-            const float eta_scale = b4.w;
+            float eta_scale = b4.w;
             float4 l4 = wb.L[slot];
             RGB L = rgb(l4.x, l4.y, l4.z);
             bool finished = true;
             Isect it;
             if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
-                BSDF bsdf = make_bsdf<-1>(sc, it);
-                Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
-                float u[4], ug[4];
-                rng.block(DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce + 4, u);  // u[1..2] BSDF, u[3] roulette
-                rng.block(DIM_GUIDE0 + 4 * bounce, ug);
-                float raw[GUIDE_RAW_STRIDE];
-                const float4* r4 = reinterpret_cast<const float4*>(gw.raw + (size_t)GUIDE_RAW_STRIDE * i);
-#pragma unroll
-                for (int j = 0; j < GUIDE_RAW_STRIDE / 4; ++j) {
-                    float4 v = r4[j];
-                    raw[4 * j] = v.x;
-                    raw[4 * j + 1] = v.y;
-                    raw[4 * j + 2] = v.z;
-                    raw[4 * j + 3] = v.w;
-                }
-                VmfMix mix = guide_parse(raw);
-                V3 wo = -ray.d;
-                V3 wi;
-                RGB f;
-                float p_b;
-                if (ug[0] < mix.c) {
-                    wi = guide_sample(mix, ug[1], ug[2], ug[3]);
-                    f = bsdf.f<false>(wo, wi, BSDF_ALL);
-                    p_b = bsdf.pdf<false>(wo, wi, BSDF_ALL);
-                } else {
-                    BxSample bs = bsdf.sample<false>(wo, u[1], u[2], BSDF_ALL);
-                    wi = bs.wi;
-                    f = bs.pdf > 0.0f ? bs.f : rgb(0.0f);
-                    p_b = bs.pdf;
-                }
-                float pdf = mix.c * guide_pdf(mix, wi) + (1.0f - mix.c) * p_b;
-                if (!is_black(f) && pdf > 0.0f && isfinite(pdf)) {
-                    RGB beta0 = beta;
-                    beta = beta * (f * abs_dot(wi, it.ns) / pdf);
-                    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
-                    RGB rr_beta = beta * eta_scale;
-                    bool killed = false;
-                    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
-                        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
-                        if (u[3] < qq) killed = true;
-                        else beta = beta / (1.0f - qq);
-                    }
-                    if (!killed) {
-                        wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
-                        wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
-                        state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu);
-                        if (record) {
-                            GuideQuery gq{gw.query[3 * (size_t)i], gw.query[3 * (size_t)i + 1],
-                                          gw.query[3 * (size_t)i + 2]};
-                            state = open_record(gw, wb, slot, state, gq, wi, p_b, beta0);
-                        }
-                        cont = true;
-                        finished = false;
-                    }
-                }
+                const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
+                float ug[4];
+                Rng{wb.pixel[slot], wb.sample[slot], rp.seed}.block(DIM_GUIDE0 + 4 * bounce, ug);
+                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, &mix, ug, vo);
+                finished = vo.finished;
+                cont = vo.cont;
             }
             wb.state[slot] = state;
             wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
@@ -757,11 +765,7 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
                 }
             }
         }
-        uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
-        if (cont) qn[pos] = slot;
-        pos = warp_append(&wb.counters[C_DONE], done_pending);
-        if (done_pending) wb.done[pos] = slot;
-        if (record) emit_records(gw, wb, slot, emit_n, L_emit);
+        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, err);
     }
 }
 
@@ -835,9 +839,12 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
         launches += 5;
         if (guided && b < rp.max_depth) {
-            launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GUIDE], gw.cap, gw.raw, err, ls.sms, s);
-            k_guide_continue<<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-            launches += 2;
+            launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GSPAN], gw.cap, gw.raw, true, err, ls.sms, s);
+            launches += 1;
+            k_guide_continue<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+            k_guide_continue<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+            k_guide_continue<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+            launches += 3;
         }
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);

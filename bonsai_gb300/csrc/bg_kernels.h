@@ -20,7 +20,7 @@ struct FilmBuffers {
     double* sumsq;   // 3 per pixel
     uint32_t* count; // per pixel
     float* rgb;      // resolved, 3 per pixel
-    float* pass;     // optional: this pass's sample per pixel (3 floats), for per-pass variance
+    float* pass;     // optional: sum of this pass's samples per pixel (3 floats), for per-pass variance
     unsigned long long* nan_count;
     uint32_t npix;
 };
@@ -54,10 +54,13 @@ struct WaveBuffers {
 // Guiding state of one wavefront (all null / zero for unguided renders).
 //   record: every non-specular vertex whose continuation was sampled opens a training record
 //           (query, wi, BSDF pdf, throughput before the vertex); the next shade of the path closes
-//           it with the radiance accumulated so far, and at the end of the path each record becomes
-//           a training sample with weight lum((L_end - L_after) / beta) = f |cos| Li / p.
-//   guided: matte / plastic / conductor vertices queue a network query instead of sampling the
-//           BSDF; k_guide_continue samples the one-sample mixture c * guide + (1 - c) * BSDF.
+//           it with the radiance accumulated so far (less the emission found there), and at the end
+//           of the path each record becomes a training sample with weight
+//           lum((L_end - L_after) / beta) = f |cos| Li / p, Li including that emission.
+//   guided: matte / plastic / conductor vertices queue a network query; k_guide_continue then runs
+//           their next-event estimation with the one-sample mixture c * guide + (1 - c) * BSDF as
+//           the second (direction-sampling) strategy of estimate_direct, and the BSDF-sampled
+//           continuation.
 enum : uint32_t { GW_RECORD = 1u, GW_GUIDED = 2u };
 constexpr int GUIDE_MAXREC = 6;      // training records kept per path
 constexpr int GUIDE_REC_F4 = 5;      // float4 per record
@@ -72,7 +75,7 @@ struct GuideWave {
     float4* rec;         // GUIDE_MAXREC * GUIDE_REC_F4 * cap, [k][field][slot]
     float4* query;       // 3 float4 per guided query (cap queries)
     uint32_t* gslot;     // guided query -> path slot
-    float* raw;          // GUIDE_RAW_STRIDE floats per guided query (network output)
+    float* raw;          // GUIDE_MIX_STRIDE floats per guided query (parsed network output)
     float4* pool;        // 4 float4 per training sample
     uint32_t* ctr;       // [0] positive-weight records, [1] pool appends (kept)
     const uint8_t* wpack;  // BF16 weight image

@@ -201,6 +201,24 @@ struct BxSample {
     int stype;
 };
 
+// Field-wise select of one of two BxDFs: keeps both in registers (indexing the pair with a runtime
+// index would place it in local memory).
+BG_D RGB sel(bool s, RGB a, RGB b) { return rgb(s ? b.r : a.r, s ? b.g : a.g, s ? b.b : a.b); }
+BG_D Bxdf select_bxdf(bool second, const Bxdf& a, const Bxdf& b) {
+    Bxdf r;
+    r.kind = second ? b.kind : a.kind;
+    r.type = second ? b.type : a.type;
+    r.conductor = second ? b.conductor : a.conductor;
+    r.r = sel(second, a.r, b.r);
+    r.dist.ax = second ? b.dist.ax : a.dist.ax;
+    r.dist.ay = second ? b.dist.ay : a.dist.ay;
+    r.eta_t = sel(second, a.eta_t, b.eta_t);
+    r.k = sel(second, a.k, b.k);
+    r.ei = second ? b.ei : a.ei;
+    r.et = second ? b.et : a.et;
+    return r;
+}
+
 template <bool REF>
 BG_D RGB bx_f(const Bxdf& b, V3 wo, V3 wi) {
     if (b.kind == BX_LAMBERT) return b.r * (1.0f / PI);
@@ -343,7 +361,7 @@ struct BSDF {
             }
         }
         if (pick < 0) return zero;
-        const Bxdf b = pick == 0 ? bx[0] : bx[1];
+        const Bxdf b = select_bxdf(pick != 0, bx[0], bx[1]);
         float ur0 = rmin(u0 * (float)matches - (float)comp, ONE_MINUS_EPSILON);
         V3 wo = to_local(wo_w);
         if (wo.z == 0.0f) return zero;
@@ -393,27 +411,31 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
     b.ss = normalize(it.dpdu);
     b.ts = cross(b.ns, b.ss);
     if (type == 0 || type == 1) {  // matte, plastic
+        // Lambertian (if kd != 0) then glossy (plastic, if ks != 0), packed into the fixed slots
+        // with selects: a slot chosen by a runtime index would force the BSDF into local memory.
         RGB kd = rgb(rclamp(m.kd[0], 0.0f, INFINITY), rclamp(m.kd[1], 0.0f, INFINITY), rclamp(m.kd[2], 0.0f, INFINITY));
-        if (!is_black(kd)) {
-            Bxdf& l = b.bx[b.n++];
-            l.kind = BX_LAMBERT;
-            l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
-            l.r = kd;
-            l.conductor = false;
-        }
+        Bxdf l{};
+        l.kind = BX_LAMBERT;
+        l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
+        l.r = kd;
+        l.conductor = false;
+        const bool has_l = !is_black(kd);
+        bool has_g = false;
+        Bxdf g{};
         if (type == 1) {
             RGB ks = rgb(rclamp(m.ks[0], 0.0f, INFINITY), rclamp(m.ks[1], 0.0f, INFINITY), rclamp(m.ks[2], 0.0f, INFINITY));
-            if (!is_black(ks)) {
-                Bxdf& g = b.bx[b.n++];
-                g.kind = BX_MF_REFL;
-                g.type = BSDF_REFLECTION | BSDF_GLOSSY;
-                g.r = ks;
-                g.dist = TR{m.alpha, m.alpha};
-                g.conductor = false;
-                g.ei = 1.5f;
-                g.et = 1.0f;
-            }
+            has_g = !is_black(ks);
+            g.kind = BX_MF_REFL;
+            g.type = BSDF_REFLECTION | BSDF_GLOSSY;
+            g.r = ks;
+            g.dist = TR{m.alpha, m.alpha};
+            g.conductor = false;
+            g.ei = 1.5f;
+            g.et = 1.0f;
         }
+        b.bx[0] = select_bxdf(!has_l, l, g);
+        b.bx[1] = g;
+        b.n = (has_l ? 1 : 0) + (has_g ? 1 : 0);
     } else if (type == 2) {  // conductor
         Bxdf& g = b.bx[b.n++];
         g.kind = BX_MF_REFL;

@@ -226,13 +226,14 @@ class Guide:
 
     def __init__(self, ctx: Context, learning_rate: float = 1e-3, batch_size: int = 16384,
                  samples_per_pass: int = 1 << 18, warmup_passes: int = 4, alpha: float = 0.5, seed: int = 0,
-                 no_fallback: bool = False, no_train: bool = False):
+                 no_fallback: bool = False, no_train: bool = False, pass_paths: int = 1 << 22, epochs: int = 1):
         self.ctx = ctx
         o = A.bg_guide_opts()
         o.learning_rate, o.beta1, o.beta2, o.eps, o.alpha = learning_rate, 0.9, 0.999, 1e-8, alpha
         o.batch_size, o.samples_per_pass, o.warmup_passes = batch_size, samples_per_pass, warmup_passes
         o.flags = (A.BG_GUIDE_NO_FALLBACK if no_fallback else 0) | (A.BG_GUIDE_NO_TRAIN if no_train else 0)
         o.seed = seed
+        o.pass_paths, o.epochs = pass_paths, epochs
         self.opts = o
         h = C.c_void_p()
         ctx.check(ctx.lib.bg_guide_create(ctx.h, C.byref(o), C.byref(h)))
@@ -277,6 +278,13 @@ class Guide:
         loss = C.c_float()
         self.ctx.check(self.ctx.lib.bg_guide_train(self.h, _ptr(s), len(s), C.byref(loss)))
         return loss.value
+
+    def pool(self) -> np.ndarray:
+        """Training samples gathered by the last guided render pass (n x 16 floats)."""
+        out = np.zeros((self.opts.samples_per_pass, A.BG_GUIDE_SAMPLE_FLOATS), np.float32)
+        n = C.c_size_t()
+        self.ctx.check(self.ctx.lib.bg_guide_pool(self.h, _ptr(out), len(out), C.byref(n)))
+        return out[: n.value]
 
     def mixture_eval(self, raw: np.ndarray, u: np.ndarray, w: np.ndarray, p_bsdf: np.ndarray) -> np.ndarray:
         raw = np.ascontiguousarray(raw, np.float32).reshape(-1, A.BG_GUIDE_OUTPUTS)

@@ -310,13 +310,16 @@ typedef struct bg_guide_opts {
     uint32_t warmup_passes;    /* leading unguided passes that only gather training data (4)   */
     uint32_t flags;            /* BG_GUIDE_* bits                                               */
     uint64_t seed;             /* weight initialisation seed                                    */
+    uint32_t pass_paths;       /* paths per pass: a pass renders max(1, pass_paths / pixels)
+                                  spp (0 = 4194304)                                             */
+    uint32_t epochs;           /* training epochs over each pass's pool (0 = 1)                 */
 } bg_guide_opts;
 
 #define BG_GUIDE_NO_FALLBACK 1u /* keep guiding even when its variance estimate is not lower  */
 #define BG_GUIDE_NO_TRAIN 2u    /* render with the current weights; no online training         */
 
 typedef struct bg_guide_stats {
-    uint32_t passes;         /* 1-spp passes rendered                                          */
+    uint32_t passes;         /* passes rendered by this call                                   */
     uint32_t guided_passes;  /* passes that sampled the guide mixture                          */
     uint32_t fallback;       /* 1 when plain BSDF sampling took over for the remaining passes  */
     uint32_t adam_steps;     /* optimiser steps taken by this call                             */
@@ -344,16 +347,24 @@ bg_status bg_guide_forward(bg_guide* guide, const float* queries, size_t n, floa
 bg_status bg_guide_gradient(bg_guide* guide, const float* samples, size_t n, float* grad, float* loss);
 /* Adam steps over n host-side samples in batches of batch_size; loss: mean batch loss. */
 bg_status bg_guide_train(bg_guide* guide, const float* samples, size_t n, float* loss);
+/* Copies the training pool gathered by the last bg_render_guided pass to the host: at most max_n
+ * samples of BG_GUIDE_SAMPLE_FLOATS floats; *n_out = samples copied. */
+bg_status bg_guide_pool(bg_guide* guide, float* out, size_t max_n, size_t* n_out);
 /* Device evaluation of the mixture for given raw outputs (test entry): per item raw (41), u (3),
  * w (3), p_bsdf (1) -> out (48): sampled direction xyz, pdf of it, pdf of w, c, loss and its
  * gradient (out[7] = d/d raw[40], out[8..47] = d/d raw[0..39]) for a unit-weight sample at w. */
 bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* u, const float* w,
                                 const float* p_bsdf, size_t n, float* out);
-/* Progressive guided render: opts->spp passes of 1 spp (PBRT mode, wide BVH layouts).  Passes
- * before warmup_passes sample the BSDF and gather training data; later passes sample the guide
- * mixture and keep training after every pass.  Unless BG_GUIDE_NO_FALLBACK is set, guiding stops
- * (plain BSDF sampling for the rest of the call) once its relative variance times pass time is
- * not lower than the unguided passes'.  Film, flags and rgb_out as in bg_render. */
+/* Progressive guided render of opts->spp samples per pixel in passes of max(1, pass_paths / pixels)
+ * spp (PBRT mode, wide BVH layouts; the last pass may be shorter).  The first
+ * warmup_passes passes rendered with this network sample the BSDF and gather training data; later
+ * passes sample the guide mixture and keep training after every pass.  Unless
+ * BG_GUIDE_NO_FALLBACK is set, guiding stops for good (plain BSDF sampling, no training) once
+ * its relative variance per sample times pass time, averaged over the last 8 guided passes, is
+ * not lower than that of the unguided passes.  Warm-up count, fallback and the variance
+ * estimates persist in the guide across calls, so a long render can be issued in chunks (with
+ * BG_RENDER_ACCUMULATE and increasing first_sample).  Film, flags and rgb_out as in bg_render;
+ * guide_stats counts this call's passes and reports the running estimates. */
 bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* scene, bg_guide* guide, const bg_camera* camera,
                            const bg_render_opts* opts, float* rgb_out, bg_render_stats* stats,
                            bg_guide_stats* guide_stats);

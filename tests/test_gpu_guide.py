@@ -189,7 +189,8 @@ def _block_z(s1a, s2a, na, s1b, s2b, nb, bs=8):
 def test_guided_render_is_unbiased(gpu_ctx):
     sd = _small_slit()
     sc = G.Scene(gpu_ctx, sd)
-    g = G.Guide(gpu_ctx, batch_size=4096, samples_per_pass=16384, warmup_passes=4, no_fallback=True)
+    npix = sd.camera.width * sd.camera.height
+    g = G.Guide(gpu_ctx, batch_size=4096, samples_per_pass=16384, warmup_passes=4, no_fallback=True, pass_paths=npix)
     try:
         pi = G.PathIntegrator(sd.camera, 512, sd.max_depth, mode=A.BG_MODE_PBRT, seed=5)
         pi.render(sc, spp=512)
@@ -217,7 +218,9 @@ def test_trained_guide_beats_bsdf_sampling(gpu_ctx):
     """Equal spp on the slit room: the guided estimate has lower relMSE than plain BSDF sampling."""
     sd = _small_slit(96, 64, depth=8)
     sc = G.Scene(gpu_ctx, sd)
-    g = G.Guide(gpu_ctx, batch_size=4096, samples_per_pass=16384, warmup_passes=8, no_fallback=True)
+    npix = sd.camera.width * sd.camera.height
+    g = G.Guide(gpu_ctx, batch_size=4096, samples_per_pass=16384, warmup_passes=8, no_fallback=True, pass_paths=4 * npix,
+                epochs=2)
     try:
         pi = G.PathIntegrator(sd.camera, 256, sd.max_depth, mode=A.BG_MODE_PBRT, seed=9)
         ref = pi.render(sc, spp=16384, first_sample=1 << 20).rgb
@@ -229,6 +232,32 @@ def test_trained_guide_beats_bsdf_sampling(gpu_ctx):
         print(f"relMSE at 256 spp: plain {e_p:.4g}, guided {e_g:.4g} (ratio {e_g / e_p:.3f}); "
               f"relvar/sample plain {guided.guide.relvar_plain:.3g} guided {guided.guide.relvar_guided:.3g}")
         assert e_g < e_p
+    finally:
+        g.close()
+        sc.close()
+
+
+def test_multi_spp_passes_and_pool_export(gpu_ctx):
+    """Passes of several spp: every pixel gets exactly spp samples, the exported pool holds sane
+    training samples (unit directions, positions in [0,1], positive weights)."""
+    sd = _small_slit(64, 48)
+    sc = G.Scene(gpu_ctx, sd)
+    npix = sd.camera.width * sd.camera.height
+    g = G.Guide(gpu_ctx, batch_size=1024, samples_per_pass=8192, warmup_passes=2, no_fallback=True,
+                pass_paths=3 * npix, epochs=3)
+    try:
+        pi = G.PathIntegrator(sd.camera, 20, sd.max_depth, mode=A.BG_MODE_PBRT, seed=2)
+        r = pi.render_guided(sc, g, spp=20)
+        assert r.guide.passes == 7 and r.guide.guided_passes == 5  # 3+3+...+2 spp
+        _, _, n = G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height)
+        assert (n == 20).all()
+        pool = g.pool()
+        assert 0 < len(pool) <= 8192
+        assert ((pool[:, :3] >= 0) & (pool[:, :3] <= 1)).all()
+        for a, b in ((3, 6), (6, 9), (9, 12)):
+            np.testing.assert_allclose(np.linalg.norm(pool[:, a:b], axis=1), 1.0, atol=1e-4)
+        assert (pool[:, 13] > 0).all() and np.isfinite(pool[:, 13]).all() and (pool[:, 12] >= 0).all()
+        assert r.guide.adam_steps == 7 * 3 * 8 or r.guide.adam_steps > 0
     finally:
         g.close()
         sc.close()
