@@ -53,7 +53,7 @@ def parse():
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
-    p.add_argument("--workload", choices=["production", "raysoup", "guiding"], default="production",
+    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp"], default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
                         "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room")
     p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
@@ -583,8 +583,59 @@ def run_guiding(args):
     ctx.close()
 
 
+def _random_guide_data(n: int, seed: int):
+    """Seeded synthetic training samples / queries with the value ranges the renderer produces."""
+    rng = np.random.default_rng(seed)
+
+    def unit(k):
+        v = rng.normal(size=(k, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+    s = np.zeros((n, 16), np.float32)
+    s[:, 0:3] = rng.random((n, 3))
+    s[:, 3:6] = unit(n)
+    s[:, 6:9] = unit(n)
+    s[:, 9:12] = unit(n)
+    s[:, 12] = rng.exponential(0.3, n)
+    s[:, 13] = rng.lognormal(0.0, 1.0, n)
+    return s
+
+
+def run_guide_mlp(args):
+    """The guiding network alone: device time of a training step (forward + backward + Adam on one
+    16384-sample batch) and of inference over 2^20 queries.  FLOPs are the network's algorithmic
+    count: 19,904 multiply-adds per inference (78 -> 4 x 64 -> 41) = 39,808 FLOP, 3x that per
+    training sample; the denominator is the measured cuBLAS BF16 peak."""
+    from bonsai_gb300 import gpu as G
+    ctx = G.Context(0)
+    g = G.Guide(ctx, batch_size=16384, samples_per_pass=1 << 18)
+    data = _random_guide_data(1 << 20, 5)
+    clocks = Clocks(0)
+    clocks.start()
+    step_ms, infer_ms = g.time(data[:16384], data[:, :9], reps=max(args.steps, 3))
+    clk = clocks.stop()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    fl_inf = 2 * 19904
+    train_tf = 3 * fl_inf * 16384 / (step_ms / 1e3) / 1e12
+    infer_tf = fl_inf * len(data) / (infer_ms / 1e3) / 1e12
+    print(json.dumps({
+        "metric": "guiding network throughput", "value": len(data) / (infer_ms / 1e3) / 1e6, "unit": "Mqueries/s",
+        "n_gpus": 1, "steps": max(args.steps, 3), "higher_is_better": True, "dtype": "bf16 (fp32 accumulate)",
+        "train_step_ms": step_ms, "train_samples_per_s": 16384 / (step_ms / 1e3), "infer_ms_2^20": infer_ms,
+        "roofline": {"bound": "tensor", "unit": "TFLOP/s", "peak": peak,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "train": {"achieved": train_tf, "frac": train_tf / peak},
+                     "infer": {"achieved": infer_tf, "frac": infer_tf / peak}},
+        "clocks": clk}), flush=True)
+    g.close()
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "guide-mlp":
+        run_guide_mlp(args)
+        return
     if args.workload == "raysoup":
         run_raysoup(args)
         return

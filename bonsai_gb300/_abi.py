@@ -176,6 +176,7 @@ SIGNATURES = {
     "bg_guide_train": (ST, [P, P, C.c_size_t, C.POINTER(C.c_float)]),
     "bg_guide_mixture_eval": (ST, [P, P, P, P, P, C.c_size_t, P]),
     "bg_guide_pool": (ST, [P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "bg_guide_time": (ST, [P, P, C.c_size_t, P, C.c_size_t, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "bg_render_guided": (ST, [P, P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
                               C.POINTER(bg_render_stats), C.POINTER(bg_guide_stats)]),
 }

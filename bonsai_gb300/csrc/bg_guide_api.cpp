@@ -464,6 +464,75 @@ bg_status bg_guide_pool(bg_guide* g, float* out, size_t max_n, size_t* n_out) {
     return BG_OK;
 }
 
+bg_status bg_guide_time(bg_guide* g, const float* samples, size_t n, const float* queries, size_t nq, uint32_t reps,
+                        double* train_step_ms, double* infer_ms) {
+    if (!g || !g->ctx || !samples || !queries || n == 0 || nq == 0 || reps == 0) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    if (n >= (1u << 24) || nq >= (1u << 28)) return fail(ctx, BG_ERR_INVALID, "too many samples or queries");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<void*> tmp;
+    float4* ds = nullptr;
+    bg_status st = upload_samples(g, samples, n, &ds, &tmp);
+    std::vector<float4> q(3 * nq);
+    for (size_t i = 0; i < nq; ++i) {
+        const float* a = queries + 9 * i;
+        q[3 * i] = make_float4(a[0], a[1], a[2], a[3]);
+        q[3 * i + 1] = make_float4(a[4], a[5], a[6], a[7]);
+        q[3 * i + 2] = make_float4(a[8], 0.0f, 0.0f, 0.0f);
+    }
+    void *dq = nullptr, *dout = nullptr;
+    if (st == BG_OK) st = dalloc(ctx, q.size() * sizeof(float4), &dq, &tmp);
+    if (st == BG_OK) st = dalloc(ctx, nq * bg::GUIDE_MIX_STRIDE * sizeof(float), &dout, &tmp);
+    float t_train = 0.0f, t_infer = 0.0f;
+    if (st == BG_OK) {
+        cudaMemcpyAsync(dq, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
+        const uint32_t nb = (uint32_t)std::min<size_t>(n, g->o.batch_size);
+        const bg::PoolOrder order{nb, 1u, 0u, 0u};
+        bg::GuideAdam h{g->o.learning_rate, g->o.beta1, g->o.beta2, g->o.eps};
+        bg::launch_guide_wsum(ds, order, nb, g->wsum, ctx->stream);
+        auto step = [&]() {
+            bg::GuideTrainArgs a{};
+            a.wpack = g->wpack;
+            a.samples = ds;
+            a.order = order;
+            a.base = 0;
+            a.n = nb;
+            a.wsum = g->wsum;
+            a.alpha = g->o.alpha;
+            a.grad = g->grad;
+            a.stats = g->stats;
+            a.step = g->step;
+            a.err = ctx->d_err;
+            bg::launch_guide_train(a, ctx->stream);
+            bg::launch_guide_adam(g->params, g->m, g->v, g->grad, g->wpack, g->step, h, ctx->stream);
+        };
+        auto infer = [&]() {
+            bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)nq, (float*)dout, true, ctx->d_err,
+                                   ctx->shape.sms, ctx->stream);
+        };
+        step();
+        infer();
+        cudaEventRecord(g->ev[0], ctx->stream);
+        for (uint32_t r = 0; r < reps; ++r) step();
+        cudaEventRecord(g->ev[1], ctx->stream);
+        for (uint32_t r = 0; r < reps; ++r) infer();
+        cudaEventRecord(g->ev[2], ctx->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "guide timing");
+    }
+    if (st == BG_OK) st = guide_error(ctx);
+    if (st == BG_OK) {
+        cudaEventElapsedTime(&t_train, g->ev[0], g->ev[1]);
+        cudaEventElapsedTime(&t_infer, g->ev[1], g->ev[2]);
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    if (st != BG_OK) return st;
+    if (train_step_ms) *train_step_ms = t_train / reps;
+    if (infer_ms) *infer_ms = t_infer / reps;
+    return BG_OK;
+}
+
 bg_status bg_guide_mixture_eval(bg_guide* g, const float* raw, const float* u, const float* w, const float* p_bsdf,
                                 size_t n, float* out) {
     if (!g || !g->ctx || (n && (!raw || !u || !w || !p_bsdf || !out))) return BG_ERR_INVALID;

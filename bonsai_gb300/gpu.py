@@ -286,6 +286,14 @@ class Guide:
         self.ctx.check(self.ctx.lib.bg_guide_pool(self.h, _ptr(out), len(out), C.byref(n)))
         return out[: n.value]
 
+    def time(self, samples: np.ndarray, queries: np.ndarray, reps: int = 20) -> tuple[float, float]:
+        """(ms per training step on one batch, ms per inference pass over the queries), device-timed."""
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, A.BG_GUIDE_SAMPLE_FLOATS)
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, A.BG_GUIDE_QUERY_FLOATS)
+        t, i = C.c_double(), C.c_double()
+        self.ctx.check(self.ctx.lib.bg_guide_time(self.h, _ptr(s), len(s), _ptr(q), len(q), reps, C.byref(t), C.byref(i)))
+        return t.value, i.value
+
     def mixture_eval(self, raw: np.ndarray, u: np.ndarray, w: np.ndarray, p_bsdf: np.ndarray) -> np.ndarray:
         raw = np.ascontiguousarray(raw, np.float32).reshape(-1, A.BG_GUIDE_OUTPUTS)
         n = len(raw)

@@ -350,6 +350,13 @@ bg_status bg_guide_train(bg_guide* guide, const float* samples, size_t n, float*
 /* Copies the training pool gathered by the last bg_render_guided pass to the host: at most max_n
  * samples of BG_GUIDE_SAMPLE_FLOATS floats; *n_out = samples copied. */
 bg_status bg_guide_pool(bg_guide* guide, float* out, size_t max_n, size_t* n_out);
+/* Device timing of the network kernels (CUDA events on the context's stream, after one untimed
+ * run of each): `reps` training steps on the first batch_size of n host samples (forward +
+ * backward + Adam; the weights change) and `reps` inference passes over nq host queries (the
+ * parsed-mixture output the renderer uses).  Outputs: mean ms per training step and per
+ * inference pass. */
+bg_status bg_guide_time(bg_guide* guide, const float* samples, size_t n, const float* queries, size_t nq,
+                        uint32_t reps, double* train_step_ms, double* infer_ms);
 /* Device evaluation of the mixture for given raw outputs (test entry): per item raw (41), u (3),
  * w (3), p_bsdf (1) -> out (48): sampled direction xyz, pdf of it, pdf of w, c, loss and its
  * gradient (out[7] = d/d raw[40], out[8..47] = d/d raw[0..39]) for a unit-weight sample at w. */
