@@ -53,7 +53,8 @@ def parse():
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
-    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp"], default="production",
+    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch"],
+                   default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
                         "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room")
     p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
@@ -631,8 +632,71 @@ def run_guide_mlp(args):
     ctx.close()
 
 
+def run_batch(args):
+    """Uneven multi-scene batch: 256 seeded scenes (1k..500k triangles, 128^2..512^2 / 640x360,
+    4..64 spp, depth 4..10) rendered by bg_render_batch, whose paths of all scenes share one
+    wavefront; value = aggregate Msamples/s of the batch (device time, L2 flushed before every step).
+    Compared with rendering the same scenes one after another through bg_render (graph-captured)."""
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    from bonsai_gb300 import scenes as S
+    nsc = 32 if args.small else 256
+    t0 = time.time()
+    sds = S.uneven_batch(nsc)
+    gen_s = time.time() - t0
+    ctx = G.Context(0)
+    t0 = time.time()
+    scenes = [G.Scene(ctx, sd, A.BG_BVH_WIDE) for sd in sds]
+    build_s = time.time() - t0
+    jobs = [G.BatchJob(sc, sd.camera, sd.spp, sd.max_depth, seed=k) for k, (sc, sd) in enumerate(zip(scenes, sds))]
+    samples = sum(sd.camera.width * sd.camera.height * sd.spp for sd in sds)
+    for _ in range(args.warmup):
+        G.render_batch(ctx, jobs, readback=False)
+    clocks = Clocks(0)
+    clocks.start()
+    dev_ms, launches = 0.0, 0
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        _, st = G.render_batch(ctx, jobs, readback=False)
+        dev_ms += st.device_ms
+        launches += st.launches
+    clk = clocks.stop()
+    value = args.steps * samples / (dev_ms / 1e3) / 1e6
+    t0 = time.time()
+    for _ in range(args.steps):
+        imgs, _ = G.render_batch(ctx, jobs, readback=True)
+    e2e = args.steps * samples / (time.time() - t0) / 1e6
+    d2h = sum(im.nbytes for im in imgs)
+    # the same scenes one render at a time (graph-captured wavefront per scene)
+    seq_ms = 0.0
+    ctx.flush_l2()
+    for j in jobs:
+        pi = G.PathIntegrator(j.camera, j.spp, j.max_depth, mode=A.BG_MODE_PBRT, seed=j.seed)
+        pi.render(j.scene, readback=False, graph=True)  # capture
+        seq_ms += pi.render(j.scene, readback=False, graph=True).stats.device_ms
+    print(json.dumps({
+        "metric": "Msamples/s (uneven batch)", "value": value, "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": f"uneven batch of {nsc} scenes (scenes.uneven_batch(seed 5)): "
+                               f"{sum(sd.ntri for sd in sds)} triangles, {samples} samples per step",
+                   "l2": "flushed before every step"},
+        "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": nsc * 368, "d2h_bytes_per_step": d2h,
+                "note": "h2d = the 368-byte scene table entry per scene uploaded by every call"},
+        "gpu_launches": launches,
+        "sequential_msamples_per_s": samples / (seq_ms / 1e3) / 1e6,
+        "batch_over_sequential": (samples / (dev_ms / args.steps / 1e3)) / (samples / (seq_ms / 1e3)),
+        "scene_generation_s": gen_s, "upload_and_bvh_build_s": build_s, "clocks": clk}), flush=True)
+    for sc in scenes:
+        sc.close()
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.workload == "batch":
+        run_batch(args)
+        return
     if args.workload == "guide-mlp":
         run_guide_mlp(args)
         return

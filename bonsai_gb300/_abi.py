@@ -133,6 +133,10 @@ class bg_guide_stats(C.Structure):
                 ("pool_samples", C.c_uint64)]
 
 
+class bg_batch_item(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", bg_camera), ("opts", bg_render_opts), ("rgb_out", C.c_void_p)]
+
+
 P = C.c_void_p
 PP = C.POINTER(C.c_void_p)
 ST = C.c_int  # bg_status
@@ -177,6 +181,7 @@ SIGNATURES = {
     "bg_guide_mixture_eval": (ST, [P, P, P, P, P, C.c_size_t, P]),
     "bg_guide_pool": (ST, [P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bg_guide_time": (ST, [P, P, C.c_size_t, P, C.c_size_t, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "bg_render_batch": (ST, [P, C.POINTER(bg_batch_item), C.c_size_t, C.POINTER(bg_render_stats)]),
     "bg_render_guided": (ST, [P, P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
                               C.POINTER(bg_render_stats), C.POINTER(bg_guide_stats)]),
 }

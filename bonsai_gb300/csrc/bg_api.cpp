@@ -270,6 +270,7 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(counters, 16 * sizeof(uint32_t));
     WB(ray_stats, 4 * sizeof(unsigned long long));
     WB(wavectl, 4 * sizeof(uint32_t));
+    WB(scene_id, n * sizeof(uint32_t));
 #undef WB
     w.capacity = cap;
     return BG_OK;
@@ -933,6 +934,112 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         CK(cudaStreamSynchronize(ctx->stream));
     }
     return BG_OK;
+}
+
+bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_render_stats* stats) {
+    if (!ctx || !items || n == 0) return BG_ERR_INVALID;
+    if (n > 65536) return fail(ctx, BG_ERR_INVALID, "at most 65536 scenes per batch");
+    uint64_t total_pix = 0, total_items = 0;
+    uint32_t max_depth = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const bg_batch_item& it = items[i];
+        bg_render_opts o = it.opts;
+        o.flags = BG_RENDER_NO_READBACK;  // read-back is per item below
+        bg_status st = validate_render(ctx, it.scene, &it.camera, &o, nullptr);
+        if (st != BG_OK) return st;
+        if (it.scene->kind != BG_BVH_WIDE)
+            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs scenes committed with BG_BVH_WIDE");
+        if (it.opts.mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs BG_MODE_PBRT");
+        total_pix += (uint64_t)it.camera.width * it.camera.height;
+        total_items += (uint64_t)it.camera.width * it.camera.height * it.opts.spp;
+        max_depth = std::max(max_depth, it.opts.max_depth);
+    }
+    if (total_pix >= (1ull << 31)) return fail(ctx, BG_ERR_INVALID, "batch film too large");
+    CK(cudaSetDevice(ctx->device));
+    bg_status st;
+    if ((st = ensure_film(ctx, (uint32_t)total_pix, 1)) != BG_OK) return st;
+    bg::launch_clear_film(ctx->film, ctx->stream);
+    CK(cudaMemsetAsync(ctx->film.nan_count, 0, sizeof(unsigned long long), ctx->stream));
+    std::vector<bg::SceneRender> tab(n);
+    uint64_t pix0 = 0, item0 = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const bg_batch_item& it = items[i];
+        const uint64_t npix = (uint64_t)it.camera.width * it.camera.height;
+        bg::SceneRender& r = tab[i];
+        r.sc = it.scene->dev;
+        r.cam = make_camera(it.camera);
+        r.rp = bg::RenderParams{it.camera.width, it.camera.height, it.opts.spp, it.opts.max_depth, it.opts.first_sample,
+                                it.opts.rr_threshold, it.opts.seed};
+        r.film = ctx->film;
+        r.film.sum += 3 * pix0;
+        r.film.sumsq += 3 * pix0;
+        r.film.count += pix0;
+        r.film.rgb += 3 * pix0;
+        r.film.pass = nullptr;
+        r.film.npix = (uint32_t)npix;
+        r.item0 = item0;
+        pix0 += npix;
+        item0 += npix * it.opts.spp;
+    }
+    std::vector<void*> tmp;
+    const bg::SceneRender* d_tab = nullptr;
+    if ((st = upload(ctx, tab, &d_tab, &tmp)) != BG_OK) return st;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, std::max<uint64_t>(total_items, 1));
+    if ((st = ensure_wave(ctx, cap)) != BG_OK) {
+        dfree_all(ctx, tmp);
+        return st;
+    }
+    CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+    uint64_t launches = 0;
+    for (uint64_t w0 = 0; w0 < total_items; w0 += cap) {
+        const uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, total_items - w0);
+        launches += (uint64_t)bg::launch_wave_batch(d_tab, (uint32_t)n, max_depth, ctx->wave, w0, nitems, ctx->d_err,
+                                                    ctx->shape, ctx->stream);
+    }
+    bg::launch_resolve(ctx->film, ctx->stream);
+    launches += 1;
+    cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+        cudaStreamSynchronize(ctx->stream);
+        dfree_all(ctx, tmp);
+        return cuda_fail(ctx, le, "batch launch");
+    }
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    uint32_t word = 0;
+    st = check_device_error(ctx, &word);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev_begin, ctx->ev_end);
+        stats->device_ms = ms;
+        stats->samples = total_items;
+        stats->launches = launches;
+        stats->error_word = word;
+        unsigned long long nan = 0, rs[2] = {0, 0};
+        cudaMemcpy(&nan, ctx->film.nan_count, sizeof(nan), cudaMemcpyDeviceToHost);
+        cudaMemcpy(rs, ctx->wave.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
+        stats->nan_samples = nan;
+        stats->extension_rays = rs[0];
+        stats->shadow_rays = rs[1];
+    }
+    if (st == BG_OK) {
+        pix0 = 0;
+        for (size_t i = 0; i < n && st == BG_OK; ++i) {
+            const uint64_t npix = (uint64_t)items[i].camera.width * items[i].camera.height;
+            if (items[i].rgb_out) {
+                cudaError_t e = cudaMemcpyAsync(items[i].rgb_out, ctx->film.rgb + 3 * pix0, npix * 3 * sizeof(float),
+                                                cudaMemcpyDeviceToHost, ctx->stream);
+                if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMemcpyAsync");
+            }
+            pix0 += npix;
+        }
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (st == BG_OK && e != cudaSuccess) st = cuda_fail(ctx, e, "cudaStreamSynchronize");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dfree_all(ctx, tmp);
+    return st;
 }
 
 bg_status bg_film_moments(bg_ctx* ctx, double* sum, double* sumsq, uint32_t* count) {

@@ -290,28 +290,60 @@ BG_D uint32_t guide_base(const WaveBuffers& wb, int cls) {
 constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
 constexpr int CLS_MISS = 4;
 
+// Camera ray of (pixel, sample) into path slot i (PerspectiveCamera::generate_ray).
+BG_D void generate_one(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint32_t i, uint32_t pix,
+                       uint32_t s) {
+    Rng rng{pix, s, rp.seed};
+    float c[4];
+    rng.block(0, c);
+    float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
+    Ray r = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+    wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
+    wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
+    wb.pixel[i] = pix;
+    wb.sample[i] = s;
+    wb.state[i] = 0;
+    wb.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    wb.queue[0][i] = i;
+}
+
 BG_D void generate_paths(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint64_t item0,
                          uint32_t nitems, uint32_t first_sample) {
     const uint64_t npix = (uint64_t)rp.width * rp.height;
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
         uint64_t item = item0 + i;
-        uint32_t pix = (uint32_t)(item % npix);
-        uint32_t s = first_sample + (uint32_t)(item / npix);
-        Rng rng{pix, s, rp.seed};
-        float c[4];
-        rng.block(0, c);
-        float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-        Ray r = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
-        wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
-        wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
-        wb.pixel[i] = pix;
-        wb.sample[i] = s;
-        wb.state[i] = 0;
-        wb.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        wb.queue[0][i] = i;
+        generate_one(cam, rp, wb, i, (uint32_t)(item % npix), first_sample + (uint32_t)(item / npix));
     }
+}
+
+// Batch: item -> scene by binary search over the scenes' first items, then as above.
+__global__ void k_generate_batch(const SceneRender* tab, uint32_t nscenes, WaveBuffers wb, uint64_t item0,
+                                 uint32_t nitems) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+        const uint64_t item = item0 + i;
+        uint32_t lo = 0, hi = nscenes - 1;
+        while (lo < hi) {  // last scene with item0 <= item
+            uint32_t mid = (lo + hi + 1) >> 1;
+            if (tab[mid].item0 <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const SceneRender& sr = tab[lo];
+        const uint64_t local = item - sr.item0;
+        const uint64_t npix = (uint64_t)sr.rp.width * sr.rp.height;
+        generate_one(sr.cam, sr.rp, wb, i, (uint32_t)(local % npix), sr.rp.first_sample + (uint32_t)(local / npix));
+        wb.scene_id[i] = lo;
+    }
+}
+
+// The scene / render parameters / film of a path: the kernel's own in a single-scene render, the
+// path's table entry in a batch render.
+template <bool MULTI, class T>
+BG_D const T& pick(const T& single, const T* multi) {
+    if constexpr (MULTI) return *multi;
+    else return single;
 }
 
 __global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
@@ -345,32 +377,35 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
 struct ExtendSrc {
     const uint32_t* q;
     WaveBuffers wb;
+    const SceneRender* tab;
     BG_D Ray load(uint32_t i, int* skip) const {
         uint32_t slot = q[i];
         *skip = -1;
         return load_ray(wb.ray_o[slot], wb.ray_d[slot]);
     }
+    BG_D const Scene* scene(uint32_t i) const { return &tab[wb.scene_id[q[i]]].sc; }
     BG_D void store(uint32_t i, int prim, float t) const { wb.hit[q[i]] = make_int2(prim, __float_as_int(t)); }
 };
 
-template <int LAYOUT>
+template <int LAYOUT, bool MULTI = false>
 __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err,
-                                                int refill) {
+                                                int refill, const SceneRender* tab) {
     const uint32_t n = wb.counters[bounce & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
-    ExtendSrc src{wb.queue[bounce & 1], wb};
+    ExtendSrc src{wb.queue[bounce & 1], wb, tab};
 #if BG_SMEM_STACK
     __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
 #else
     uint2* stack8 = nullptr;
 #endif
-    if (LAYOUT == 8) traverse_queue8<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
+    if (LAYOUT == 8) traverse_queue8<false, ExtendSrc, MULTI>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
     else traverse_queue<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
 }
 
 // Material-key binning of this bounce's hits: one queue per material class plus misses, so each
 // shade launch runs one material's code with uniform control flow.
-__global__ void __launch_bounds__(128) k_bin(Scene sc, WaveBuffers wb, uint32_t bounce) {
+template <bool MULTI = false>
+__global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t bounce, const SceneRender* tab) {
     const uint32_t n = wb.counters[bounce & 1];
     const uint32_t* q = wb.queue[bounce & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -381,6 +416,7 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc, WaveBuffers wb, uint32_t 
         if (i < n) {
             slot = q[i];
             int prim = wb.hit[slot].x;
+            const Scene& sc = pick<MULTI>(sc0, MULTI ? &tab[wb.scene_id[slot]].sc : nullptr);
             cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
         }
 #pragma unroll
@@ -634,9 +670,9 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
 // In guided waves the matte / plastic / conductor classes stop after their emission and queue a
 // network query; k_guide_continue finishes them with the network's mixture.
-template <int CLS>
-__global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
-                                               GuideWave gw, uint32_t bounce, uint32_t* err) {
+template <int CLS, bool MULTI = false>
+__global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
+                                               GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
@@ -657,6 +693,10 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc, RenderParams rp, FilmBu
         uint32_t emit_n = 0;
         RGB L_emit = rgb(0.0f);
         if (active) {
+            const SceneRender* sr = MULTI ? tab + wb.scene_id[slot] : nullptr;
+            const Scene& sc = pick<MULTI>(sc0, MULTI ? &sr->sc : nullptr);
+            const RenderParams& rp = pick<MULTI>(rp0, MULTI ? &sr->rp : nullptr);
+            const FilmBuffers& film = pick<MULTI>(film0, MULTI ? &sr->film : nullptr);
             float4 ro = wb.ray_o[slot], rd = wb.ray_d[slot];
             Ray ray = load_ray(ro, rd);
             int prim = wb.hit[slot].x;
@@ -771,6 +811,8 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
 
 struct ShadowSrc {
     WaveBuffers wb;
+    const SceneRender* tab;
+    BG_D const Scene* scene(uint32_t i) const { return &tab[wb.scene_id[wb.sh_ref[i] >> 1]].sc; }
     BG_D Ray load(uint32_t i, int* skip) const {
         float4 o = wb.sh_o[i], d = wb.sh_d[i];
         Ray ray;
@@ -786,21 +828,24 @@ struct ShadowSrc {
     }
 };
 
-template <int LAYOUT>
-__global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err, int refill) {
+template <int LAYOUT, bool MULTI = false>
+__global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err, int refill,
+                                                              const SceneRender* tab) {
     const uint32_t n = min(wb.counters[C_SHADOW], 2 * wb.capacity);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[1], (unsigned long long)n);
-    ShadowSrc src{wb};
+    ShadowSrc src{wb, tab};
 #if BG_SMEM_STACK
     __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
 #else
     uint2* stack8 = nullptr;
 #endif
-    if (LAYOUT == 8) traverse_queue8<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill, stack8);
+    if (LAYOUT == 8) traverse_queue8<true, ShadowSrc, MULTI>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill, stack8);
     else traverse_queue<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
 }
 
-__global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, WaveBuffers wb, GuideWave gw) {
+template <bool MULTI = false>
+__global__ void __launch_bounds__(128) k_finalize(Scene sc0, FilmBuffers film0, WaveBuffers wb, GuideWave gw,
+                                                  const SceneRender* tab) {
     const uint32_t n = wb.counters[C_DONE];
     const bool record = (gw.flags & GW_RECORD) != 0;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
@@ -809,6 +854,9 @@ __global__ void __launch_bounds__(128) k_finalize(Scene sc, FilmBuffers film, Wa
         RGB L = rgb(0.0f);
         if (i < n) {
             slot = wb.done[i];
+            const SceneRender* sr = MULTI ? tab + wb.scene_id[slot] : nullptr;
+            const Scene& sc = pick<MULTI>(sc0, MULTI ? &sr->sc : nullptr);
+            const FilmBuffers& film = pick<MULTI>(film0, MULTI ? &sr->film : nullptr);
             float4 l4 = wb.L[slot];
             uint32_t state = wb.state[slot];
             L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
@@ -828,15 +876,15 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
     for (uint32_t b = 0; b <= rp.max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 0], s);
-        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill);
-        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill);
-        k_bin<<<grid, block, 0, s>>>(sc, wb, b);
+        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr);
+        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr);
+        k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         launches += 5;
         if (guided && b < rp.max_depth) {
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GSPAN], gw.cap, gw.raw, true, err, ls.sms, s);
@@ -847,10 +895,10 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             launches += 3;
         }
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
-        if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
-        else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill);
+        if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
+        else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
-        k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw);
+        k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
         launches += 5;
     }
     return launches;
@@ -862,6 +910,31 @@ int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, cons
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     k_generate<<<grid, block, 0, s>>>(cam, rp, wb, item0, nitems);
     return 1 + launch_bounces(sc, rp, film, wb, err, ls, s, ev, gw);
+}
+
+int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_depth, const WaveBuffers& wb,
+                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s) {
+    dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
+    const Scene sc{};
+    const RenderParams rp{};
+    const FilmBuffers film{};
+    const GuideWave gw{};
+    k_generate_batch<<<grid, block, 0, s>>>(tab, nscenes, wb, item0, nitems);
+    int launches = 1;
+    for (uint32_t b = 0; b <= max_depth; ++b) {
+        k_prepare<<<1, 32, 0, s>>>(wb, b);
+        k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab);
+        k_bin<true><<<grid, block, 0, s>>>(sc, wb, b, tab);
+        k_shade<CLS_MISS, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<1, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<2, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<3, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shadow<8, true><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, tab);
+        k_finalize<true><<<grid, block, 0, s>>>(sc, film, wb, gw, tab);
+        launches += 10;
+    }
+    return launches;
 }
 
 int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,

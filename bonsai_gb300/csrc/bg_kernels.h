@@ -49,6 +49,16 @@ struct WaveBuffers {
                         // [5] shadow head, [6..10] class queue sizes, [11] guided queries
     unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
     uint32_t* wavectl;              // graph replay: [0] wave index, [1] first sample (device side)
+    uint32_t* scene_id;             // batch renders: scene of each path slot
+};
+
+// One scene of a batch render (a device table of these): what a path of the scene needs.
+struct SceneRender {
+    Scene sc;
+    Camera cam;
+    RenderParams rp;
+    FilmBuffers film;   // this scene's slice of the batch film
+    uint64_t item0;     // first item (pixel x sample) of the scene in the batch's item space
 };
 
 // Guiding state of one wavefront (all null / zero for unguided renders).
@@ -106,6 +116,11 @@ int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, cons
 // for every wave.  Returns the number of kernels in the chain.
 int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                       const WaveBuffers& wb, uint64_t total, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
+// One wave of a batch render: items [item0, item0 + nitems) of the concatenated item spaces of
+// `nscenes` scenes (tab, device); paths of all scenes share the queues of one set of launches
+// (8-wide BVH layouts).  max_depth = the largest of the scenes'.  Returns the kernels launched.
+int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_depth, const WaveBuffers& wb,
+                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
 void launch_resolve(const FilmBuffers& film, cudaStream_t s);
 void launch_clear_film(const FilmBuffers& film, cudaStream_t s);
 

@@ -473,9 +473,15 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
 #endif
 constexpr int kPostpone = BG_POSTPONE;  // 0 disables postponement
 
-template <bool ANY, class Src>
+// MULTI: rays of different scenes share the queue; src.scene(i) gives the scene of ray i.
+template <bool ANY, class Src, bool MULTI = false>
 BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill,
                           uint2* smem) {
+    const Scene* cur = nullptr;  // MULTI: scene of this lane's ray
+    auto S = [&]() -> const Scene& {
+        if constexpr (MULTI) return *cur;
+        else return sc;
+    };
     const uint32_t lane = threadIdx.x & 31u;
 #if BG_SMEM_STACK
     uint2* stack = smem + threadIdx.x;
@@ -505,11 +511,12 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                 if (my < n) {
                     idx = my;
                     ray = src.load(my, &skip);
+                    if constexpr (MULTI) cur = src.scene(my);
                     r8 = make_ray8(ray);
                     tr = make_tri_ray(ray);
                     sp = 0;
                     hit = -1;
-                    ngroup = make_uint2(0, sc.n_nodes8 ? 0x80000000u : 0u);
+                    ngroup = make_uint2(0, S().n_nodes8 ? 0x80000000u : 0u);
                     tgroup = make_uint2(0, 0);
                     busy = true;
                 } else {
@@ -536,13 +543,13 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
             const uint32_t slot = (bit - 24u) ^ (r8.octinv4 & 0xFFu);
             const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
             const uint32_t child = ngroup.x + rel;
-            if (child >= sc.n_nodes8) {
+            if (child >= S().n_nodes8) {
                 atomicOr(err, ERR_BAD_NODE);
                 sp = 0;
                 ngroup = make_uint2(0, 0);
                 tgroup = make_uint2(0, 0);
             } else {
-                bvh8_node_hits(sc, child, r8, ray.t_max, &ngroup, &tgroup);
+                bvh8_node_hits(S(), child, r8, ray.t_max, &ngroup, &tgroup);
             }
         } else {
             tgroup = ngroup;
@@ -558,12 +565,12 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         while (tgroup.y != 0) {
             const uint32_t bit = 31u - __clz(tgroup.y);
             tgroup.y &= ~(1u << bit);
-            if (tgroup.x + bit >= sc.ntri + sc.nsph + sc.nquad) {
+            if (tgroup.x + bit >= S().ntri + S().nsph + S().nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
                 continue;
             }
             int prim;
-            if (leaf_prim_hit(sc, tgroup.x + bit, tr, ray, !ANY, &prim)) {
+            if (leaf_prim_hit(S(), tgroup.x + bit, tr, ray, !ANY, &prim)) {
                 if (ANY && prim == skip) continue;
                 hit = prim;
                 if (ANY) {

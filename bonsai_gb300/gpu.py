@@ -303,3 +303,32 @@ class Guide:
         out = np.zeros((n, 48), np.float32)
         self.ctx.check(self.ctx.lib.bg_guide_mixture_eval(self.h, _ptr(raw), _ptr(u), _ptr(w), _ptr(pb), n, _ptr(out)))
         return out
+
+
+@dataclass
+class BatchJob:
+    scene: "Scene"
+    camera: S.Camera
+    spp: int
+    max_depth: int
+    rr_threshold: float = 1.0
+    seed: int = 0
+    first_sample: int = 0
+
+
+def render_batch(ctx: Context, jobs: list, readback: bool = True):
+    """Renders every job in one batch (bg_render_batch): paths of all scenes share the wavefront.
+    Returns (list of images or None, bg_render_stats)."""
+    items = (A.bg_batch_item * len(jobs))()
+    outs = []
+    for it, j in zip(items, jobs):
+        it.scene = j.scene.h
+        it.camera = camera_struct(j.camera)
+        it.opts.spp, it.opts.max_depth, it.opts.rr_threshold = j.spp, j.max_depth, j.rr_threshold
+        it.opts.mode, it.opts.seed, it.opts.first_sample, it.opts.flags = A.BG_MODE_PBRT, j.seed, j.first_sample, 0
+        img = np.zeros((j.camera.height, j.camera.width, 3), np.float32) if readback else None
+        it.rgb_out = img.ctypes.data if img is not None else None
+        outs.append(img)
+    st = A.bg_render_stats()
+    ctx.check(ctx.lib.bg_render_batch(ctx.h, items, len(jobs), C.byref(st)))
+    return outs, st

@@ -439,3 +439,69 @@ def slit_room(width: int = 1280, height: int = 720, spp: int = 64, max_depth: in
     return SceneData(tri, tri_mat, tri_light, sph, np.stack(mats), lights, cam, spp=spp,
                      max_depth=max_depth, rr_threshold=1.0, name="slit_room",
                      meta={"n_ico": n_ico, "ico_level": ico_level, "n_spheres": n_spheres})
+
+
+def uneven_batch(n: int = 256, seed: int = 5, max_tris: int = 500_000, min_tris: int = 1_000) -> list[SceneData]:
+    """Seeded batch of scenes of uneven size (the multi-scene batch workload).
+
+    Per scene: triangle count log-uniform in [min_tris, max_tris], about 70% from fBm-displaced
+    icospheres (level 2..5) and the rest random triangles; resolution from {128^2, 256^2, 512^2,
+    640x360}; spp uniform in 4..64; max depth uniform in 4..10; materials 50% diffuse / 30%
+    conductor / 20% dielectric; ground quad and 4 quad area lights as in the production scene.
+    """
+    rng = np.random.default_rng(seed)
+    res = [(128, 128), (256, 256), (512, 512), (640, 360)]
+    out = []
+    for k in range(n):
+        target = int(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris))))
+        level = 2 if target < 20_000 else (3 if target < 80_000 else (4 if target < 300_000 else 5))
+        uv, uf = icosphere(level)
+        n_ico = max(1, int(round(0.7 * target / len(uf))))
+        mats = [material(MATTE, kd=(0.5, 0.5, 0.5)), material(MATTE, kd=(0, 0, 0))]
+
+        def random_material():
+            r = rng.random()
+            if r < 0.5:
+                return material(MATTE, kd=tuple(rng.uniform(0.1, 0.9, 3)))
+            if r < 0.8:
+                return material(CONDUCTOR, roughness=float(rng.uniform(0.05, 0.5)))
+            return material(DIELECTRIC, ior=1.5)
+        tris, tmat = [], []
+        g = int(np.ceil(np.sqrt(n_ico)))
+        span = 2.0 * g
+        for i in range(n_ico):
+            r = rng.uniform(0.5, 0.9)
+            c = np.array([(i % g - (g - 1) / 2) * 2.0, r * 1.05, (i // g - (g - 1) / 2) * 2.0])
+            d = 1.0 + 0.1 * fbm(uv * 1.5, seed=seed * 100000 + k * 100 + i)
+            tris.append((c + uv * (r * d)[:, None])[uf].reshape(-1, 9))
+            mats.append(random_material())
+            tmat.append(np.full(len(uf), len(mats) - 1, np.uint32))
+        nrand = max(0, target - n_ico * len(uf))
+        if nrand:
+            rt = random_triangles(nrand, seed=seed * 7919 + k).reshape(-1, 3, 3)
+            rt = (rt - 0.5) * np.array([span, 2.0, span], np.float32) + np.array([0.0, 1.2, 0.0], np.float32)
+            tris.append(rt.reshape(-1, 9))
+            mats.append(random_material())
+            tmat.append(np.full(nrand, len(mats) - 1, np.uint32))
+        e = span / 2 + 2
+        tris.append(_quad((-e, 0, -e), (e, 0, -e), (e, 0, e), (-e, 0, e), (0, 1, 0)))
+        tmat.append(np.zeros(2, np.uint32))
+        nonlight = sum(len(t) for t in tris)
+        for lx in (-0.5 * e, 0.5 * e):
+            for lz in (-0.5 * e, 0.5 * e):
+                tris.append(_quad((lx - 1, 6, lz - 1), (lx + 1, 6, lz - 1), (lx + 1, 6, lz + 1), (lx - 1, 6, lz + 1),
+                                  (0, -1, 0)))
+                tmat.append(np.ones(2, np.uint32))
+        tri = np.concatenate(tris).astype(np.float32)
+        tri_mat = np.concatenate(tmat).astype(np.uint32)
+        tri_light = np.full(len(tri), -1, np.int32)
+        tri_light[nonlight:] = 0
+        lights = np.zeros(1, LIGHT_DT)
+        lights[0] = ((12.0, 12.0, 12.0), 0)
+        w, h = res[int(rng.integers(0, len(res)))]
+        spp = int(rng.integers(4, 65))
+        depth = int(rng.integers(4, 11))
+        cam = Camera((0.0, 0.35 * span + 3.0, 0.7 * span + 4.0), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0), 50.0, w, h)
+        out.append(SceneData(tri, tri_mat, tri_light, np.zeros(0, SPHERE_DT), np.stack(mats), lights, cam, spp=spp,
+                             max_depth=depth, rr_threshold=1.0, name=f"batch{k}", meta={"target_tris": target}))
+    return out

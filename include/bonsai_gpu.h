@@ -254,6 +254,22 @@ bg_status bg_device_free(bg_ctx* ctx, void* d_ptr);
 bg_status bg_memcpy_h2d(bg_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
 bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
 
+/* ---- uneven multi-scene batch ---------------------------------------------------------------
+ * No counterpart in the reference (it renders one scene per process).  Renders every item in one
+ * sequence of persistent launches: the paths of all scenes share the wavefront queues (each path
+ * carries its scene index into a device table of scene, camera, render options and film slice),
+ * so small and large scenes keep the GPU equally busy.  Scenes must be committed with
+ * BG_BVH_WIDE and rendered in BG_MODE_PBRT; each item's film is cleared and, when rgb_out is not
+ * NULL, read back to it (width*height*3 floats).  Afterwards bg_film_moments returns the films of
+ * all items concatenated in item order.  stats: device time and rays of the whole batch. */
+typedef struct bg_batch_item {
+    const bg_scene* scene;
+    bg_camera camera;
+    bg_render_opts opts; /* spp, max_depth, rr_threshold, seed, first_sample; flags unused */
+    float* rgb_out;      /* host, or NULL */
+} bg_batch_item;
+bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_render_stats* stats);
+
 /* ---- render without device allocation ------------------------------------------------------
  * No counterpart in the reference: an addition for callers that must not allocate device memory
  * while they render, such as a plugin whose host application owns the GPU memory budget and only
