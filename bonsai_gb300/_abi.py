@@ -181,6 +181,10 @@ SIGNATURES = {
     "bg_guide_mixture_eval": (ST, [P, P, P, P, P, C.c_size_t, P]),
     "bg_guide_pool": (ST, [P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bg_guide_time": (ST, [P, P, C.c_size_t, P, C.c_size_t, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "bg_obj_read": (ST, [C.c_char_p, P, P, C.c_size_t, C.POINTER(C.c_size_t), C.c_char_p, C.c_size_t]),
+    "bg_scene_add_obj": (ST, [P, C.c_char_p, P, C.c_uint32, C.c_int32, C.POINTER(C.c_size_t)]),
+    "bg_write_exr": (ST, [C.c_char_p, P, C.c_uint32, C.c_uint32]),
+    "bg_film_write_exr": (ST, [P, C.c_char_p]),
     "bg_render_batch": (ST, [P, C.POINTER(bg_batch_item), C.c_size_t, C.POINTER(bg_render_stats)]),
     "bg_render_guided": (ST, [P, P, P, C.POINTER(bg_camera), C.POINTER(bg_render_opts), P,
                               C.POINTER(bg_render_stats), C.POINTER(bg_guide_stats)]),

@@ -21,7 +21,7 @@ CUDA = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["bg_kernels.cu", "bg_noalloc.cu", "bg_guide.cu"]
-CPP_SOURCES = ["bg_api.cpp", "bg_bvh.cpp", "bg_guide_api.cpp"]
+CPP_SOURCES = ["bg_api.cpp", "bg_bvh.cpp", "bg_guide_api.cpp", "bg_io.cpp"]
 
 
 def _nvcc() -> str:

@@ -254,6 +254,25 @@ bg_status bg_device_free(bg_ctx* ctx, void* d_ptr);
 bg_status bg_memcpy_h2d(bg_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
 bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
 
+/* ---- scene and film I/O ----------------------------------------------------------------------
+ * OBJ::read (src/io/obj.rs:16-123): a triangle mesh from a Wavefront OBJ file, positions through
+ * object_to_world (row-major 3x4, NULL = identity).  Triangles are the consecutive triples of all
+ * face indices in file order (as the reference; polygons are not fanned); normals and texture
+ * coordinates are index-checked but not used (device triangles carry geometric normals).  Files
+ * the reference would panic on give BG_ERR_INVALID (message in err / bg_last_error).
+ * bg_obj_read parses into tri_out (9 floats per triangle, up to max_tri; *ntri = all triangles);
+ * bg_scene_add_obj adds the mesh to a scene with one material and light id. */
+bg_status bg_obj_read(const char* path, const float* object_to_world, float* tri_out, size_t max_tri, size_t* ntri,
+                      char* err, size_t err_len);
+bg_status bg_scene_add_obj(bg_scene* scene, const char* path, const float* object_to_world, uint32_t material_id,
+                           int32_t light_id, size_t* ntri);
+/* Film::write_image (src/base/film.rs:156-202, src/io/image.rs:47-53), headless: an uncompressed
+ * single-part scanline OpenEXR file with float B, G, R channels.  bg_write_exr writes a host RGB
+ * buffer (width*height*3 floats, rows top to bottom); bg_film_write_exr the context's resolved
+ * film of the last render. */
+bg_status bg_write_exr(const char* path, const float* rgb, uint32_t width, uint32_t height);
+bg_status bg_film_write_exr(bg_ctx* ctx, const char* path);
+
 /* ---- uneven multi-scene batch ---------------------------------------------------------------
  * No counterpart in the reference (it renders one scene per process).  Renders every item in one
  * sequence of persistent launches: the paths of all scenes share the wavefront queues (each path

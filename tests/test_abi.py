@@ -15,7 +15,7 @@ from .conftest import ROOT
 HEADER = ROOT / "include" / "bonsai_gpu.h"
 STRUCTS = ["bg_material", "bg_area_light", "bg_sphere", "bg_camera", "bg_render_opts", "bg_render_stats",
            "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning", "bg_quadric", "bg_guide_opts",
-           "bg_guide_stats"]
+           "bg_guide_stats", "bg_batch_item"]
 
 
 def declared_functions():
@@ -34,7 +34,8 @@ def test_header_declares_the_entry_points():
     names = declared_functions()
     for required in ["bg_create", "bg_destroy", "bg_scene_commit", "bg_render", "bg_trace_closest", "bg_trace_any",
                      "bg_render_noalloc", "bg_set_tuning", "bg_guide_create", "bg_guide_forward",
-                     "bg_guide_gradient", "bg_guide_train", "bg_render_guided"]:
+                     "bg_guide_gradient", "bg_guide_train", "bg_render_guided", "bg_render_batch", "bg_obj_read",
+                     "bg_scene_add_obj", "bg_write_exr", "bg_film_write_exr"]:
         assert required in names
 
 
