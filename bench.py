@@ -316,6 +316,12 @@ def run_ours(args):
         bpr = 32 + 8 + 32 * counts["V_ext"] + 40 * counts["T_ext"]
         achieved = st.extension_rays * bpr / (st.trace_ms / 1e3) / 1e9
         roof.update({"achieved": achieved, "frac": achieved / peak, "bytes_per_ray": bpr, **counts})
+        tp = ROOT / "profiles" / "k_extend_traffic.json"
+        if tp.exists():  # DRAM bytes of one captured launch (ncu), per ray, against the algorithmic bytes
+            t = json.loads(tp.read_text())
+            roof["traffic"] = t["dram_bytes_read"] + t["dram_bytes_write"]
+            roof["traffic_launch"] = {"rays": t["rays"], "algorithmic_bytes": t["rays"] * bpr,
+                                      "dram_bytes_per_ray": roof["traffic"] / t["rays"], "workload": t["workload"]}
         cv, cdt = time_cpu(orc, sd, rows, nsamples, threads)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"rows 0..{sd.camera.height} step {rows[2]} x {sd.camera.width} px x {sd.spp} spp "
