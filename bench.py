@@ -257,7 +257,7 @@ def run_ours(args):
     tuning = None
     if not args.no_autotune:
         from bonsai_gb300 import autotune
-        tuning = autotune.tune(ctx, scene, pi, spp=2)
+        tuning = autotune.tune(ctx, scene, pi, spp=4)
         tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "ms")} | {
             "cached": bool(tuning.get("cached", False))}
     for _ in range(args.warmup):

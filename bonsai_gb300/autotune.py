@@ -53,7 +53,7 @@ def set_(ctx, refill: int, blocks: int, wave: int):
     ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
 
 
-def _trial(ctx, scene, integrator, spp: int, reps: int = 2) -> float:
+def _trial(ctx, scene, integrator, spp: int, reps: int = 3) -> float:
     best = float("inf")
     for _ in range(reps):
         ctx.flush_l2()
@@ -62,7 +62,7 @@ def _trial(ctx, scene, integrator, spp: int, reps: int = 2) -> float:
     return best
 
 
-def tune(ctx, scene, integrator, spp: int = 2, use_cache: bool = True, verbose: bool = False) -> dict:
+def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: bool = False) -> dict:
     """Returns {"refill", "blocks_per_sm", "wave_paths", "ms", "trials"} and applies it to ctx."""
     sd = scene.sd
     key = key_of(sd, spp)

@@ -540,7 +540,7 @@ struct VertexOut {
 template <int CLS>
 BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
                          uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
-                         uint32_t& state, const MixView* mix, const float* ug, VertexOut& out) {
+                         uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
     const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
@@ -640,14 +640,14 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    if (GUIDABLE && (gw.flags & GW_RECORD))
-        state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
+    if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
     out.cont = true;
 }
 
 // Warp-convergent tail of k_shade / k_guide_continue: queue compaction, shadow rays, records.
 BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t slot, bool cont,
-                        bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, uint32_t* err) {
+                        bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, bool record,
+                        uint32_t* err) {
     uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
     if (cont) wb.queue[(bounce + 1) & 1][pos] = slot;
     pos = warp_append(&wb.counters[C_DONE], done_pending);
@@ -664,23 +664,24 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
             }
         }
     }
-    if (gw.flags & GW_RECORD) emit_records(gw, wb, slot, emit_n, L_emit);
+    if (record) emit_records(gw, wb, slot, emit_n, L_emit);
 }
 
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
 // In guided waves the matte / plastic / conductor classes stop after their emission and queue a
 // network query; k_guide_continue finishes them with the network's mixture.
-template <int CLS, bool MULTI = false>
+// GWK: guiding support compiled in (records, guided queries); the plain wavefront uses GWK = false.
+template <int CLS, bool MULTI = false, bool GWK = false>
 __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const bool record = (gw.flags & GW_RECORD) != 0;
-    const bool guided = GUIDABLE && (gw.flags & GW_GUIDED);
-    const uint32_t gbase = GUIDABLE ? guide_base(wb, CLS) : 0u;
-    if (CLS == 3 && (gw.flags & GW_GUIDED) && blockIdx.x == 0 && threadIdx.x == 0)
+    const bool record = GWK && (gw.flags & GW_RECORD) != 0;
+    const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
+    const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
+    if (CLS == 3 && GWK && (gw.flags & GW_GUIDED) && blockIdx.x == 0 && threadIdx.x == 0)
         wb.counters[C_GSPAN] = guide_base(wb, 2) + wb.counters[C_GUIDE + 2];  // classes 0..2 are done
     // warp-uniform loop so the ballots below see all 32 lanes
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
@@ -722,7 +723,8 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, Film
                 gq = make_query(gw, it, -ray.d);
                 push_guide = true;
             } else if (!finished) {
-                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, vo);
+                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
+                                    vo);
                 finished = vo.finished;
                 cont = vo.cont;
             }
@@ -739,7 +741,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, Film
                 }
             }
         }
-        if (GUIDABLE && (gw.flags & GW_GUIDED)) {
+        if (GUIDABLE && GWK && (gw.flags & GW_GUIDED)) {
             uint32_t pos = gbase + warp_append(&wb.counters[C_GUIDE + (GUIDABLE ? CLS : 0)], push_guide);
             if (push_guide && pos >= gw.cap) {
                 atomicOr(err, ERR_QUEUE_OVERFLOW);  // cannot happen: one query per path of the wave
@@ -752,7 +754,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, Film
                 gw.gslot[pos] = slot;
             }
         }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, err);
+        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, record, err);
     }
 }
 
@@ -789,7 +791,8 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
                 const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
                 float ug[4];
                 Rng{wb.pixel[slot], wb.sample[slot], rp.seed}.block(DIM_GUIDE0 + 4 * bounce, ug);
-                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, &mix, ug, vo);
+                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, &mix, ug,
+                                    (gw.flags & GW_RECORD) != 0, vo);
                 finished = vo.finished;
                 cont = vo.cont;
             }
@@ -805,7 +808,7 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
                 }
             }
         }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, err);
+        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, (gw.flags & GW_RECORD) != 0, err);
     }
 }
 
@@ -843,11 +846,11 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuff
     else traverse_queue<true>(sc, n, &wb.counters[C_SH_HEAD], src, err, refill);
 }
 
-template <bool MULTI = false>
+template <bool MULTI = false, bool GWK = false>
 __global__ void __launch_bounds__(128) k_finalize(Scene sc0, FilmBuffers film0, WaveBuffers wb, GuideWave gw,
                                                   const SceneRender* tab) {
     const uint32_t n = wb.counters[C_DONE];
-    const bool record = (gw.flags & GW_RECORD) != 0;
+    const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + lane_id();
         uint32_t slot = 0, nrec = 0;
@@ -880,11 +883,19 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr);
         k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        if (gw.flags) {
+            k_shade<CLS_MISS, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<0, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        } else {
+            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        }
         launches += 5;
         if (guided && b < rp.max_depth) {
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GSPAN], gw.cap, gw.raw, true, err, ls.sms, s);
@@ -898,7 +909,8 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
-        k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
+        if (gw.flags) k_finalize<false, true><<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
+        else k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
         launches += 5;
     }
     return launches;
