@@ -39,6 +39,7 @@ BG_RENDER_ACCUMULATE = 1
 BG_RENDER_NO_READBACK = 2
 BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
+BG_TUNE_SORT_RAYS = 1
 
 BG_NOALLOC_MAX_PIXELS = 512 * 512
 BG_NOALLOC_WAVE_PATHS = 65536
@@ -110,7 +111,7 @@ class bg_device_opts(C.Structure):
 
 class bg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("flags", C.c_uint32)]
 
 
 class bg_build_stats(C.Structure):

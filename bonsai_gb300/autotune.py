@@ -5,6 +5,7 @@ library's CUDA events, L2 flushed before each trial):
   refill        - traversal: lanes a warp lets go idle before it fetches new rays (32 = whole warp)
   blocks_per_sm - persistent grid of the wavefront stages
   wave_paths    - paths per wave (queue capacity)
+  sort_rays     - bin each bounce's extension rays by direction octant and origin cell
 The result is cached as JSON keyed by GPU name, scene signature and render settings
 (default ~/.cache/bonsai_gb300/tuning.json, or $BONSAI_TUNING_CACHE).
 """
@@ -19,7 +20,8 @@ from . import _abi as A
 
 REFILL = [32, 16, 8, 4]
 BLOCKS = [4, 8, 16]
-WAVES = [1 << 20, 1 << 21, 1 << 22, 1 << 23]
+WAVES = [1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24]
+SORT = [0, 1]
 
 
 def cache_path() -> Path:
@@ -38,7 +40,7 @@ def _gpu_name() -> str:
 
 def key_of(sd, spp: int) -> str:
     c = sd.camera
-    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}"
+    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}|v2"
 
 
 def get(ctx) -> A.bg_tuning:
@@ -47,9 +49,10 @@ def get(ctx) -> A.bg_tuning:
     return t
 
 
-def set_(ctx, refill: int, blocks: int, wave: int):
+def set_(ctx, refill: int, blocks: int, wave: int, sort_rays: int = 0):
     t = A.bg_tuning()
     t.refill, t.blocks_per_sm, t.wave_paths = refill, blocks, wave
+    t.flags = A.BG_TUNE_SORT_RAYS if sort_rays else 0
     ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
 
 
@@ -75,13 +78,13 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
             cache = {}
     if use_cache and key in cache:
         c = cache[key]
-        set_(ctx, c["refill"], c["blocks_per_sm"], c["wave_paths"])
+        set_(ctx, c["refill"], c["blocks_per_sm"], c["wave_paths"], c.get("sort_rays", 0))
         return dict(c, cached=True)
-    cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22}
+    cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22, "sort_rays": 0}
     trials = []
 
     def run(cfg):
-        set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"])
+        set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"], cfg["sort_rays"])
         integrator.render(scene, readback=False, spp=1)  # allocate / warm
         ms = _trial(ctx, scene, integrator, spp)
         trials.append(dict(cfg, ms=ms))
@@ -90,7 +93,7 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
         return ms
 
     best_ms = run(cur)
-    for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES)):
+    for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES), ("sort_rays", SORT)):
         for v in values:
             if v == cur[name]:
                 continue
@@ -98,12 +101,12 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
             ms = run(cfg)
             if ms < best_ms:
                 best_ms, cur = ms, cfg
-    set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"])
+    set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"], cur["sort_rays"])
     result = dict(cur, ms=best_ms, trials=trials)
     if use_cache:
         try:
             path.parent.mkdir(parents=True, exist_ok=True)
-            cache[key] = {k: result[k] for k in ("refill", "blocks_per_sm", "wave_paths", "ms")}
+            cache[key] = {k: result[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "ms")}
             path.write_text(json.dumps(cache, indent=1))
         except OSError:
             pass

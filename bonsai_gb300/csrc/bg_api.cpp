@@ -271,8 +271,12 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(ray_stats, 4 * sizeof(unsigned long long));
     WB(wavectl, 4 * sizeof(uint32_t));
     WB(scene_id, n * sizeof(uint32_t));
+    WB(qsort, n * sizeof(uint32_t));
+    WB(sort_hist, 8192 * sizeof(uint32_t));
 #undef WB
     w.capacity = cap;
+    if (cudaMemsetAsync(w.sort_hist, 0, 8192 * sizeof(uint32_t), ctx->stream) != cudaSuccess)
+        return fail(ctx, BG_ERR_CUDA, "cudaMemsetAsync");
     return BG_OK;
 }
 
@@ -445,7 +449,7 @@ bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
     out->wave_paths = ctx->max_queue;
     out->blocks_per_sm = (uint32_t)ctx->shape.blocks_per_sm;
     out->refill = (uint32_t)ctx->shape.refill;
-    out->reserved = 0;
+    out->flags = ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u;
     return BG_OK;
 }
 
@@ -457,6 +461,7 @@ bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
     ctx->max_queue = t->wave_paths;
     ctx->shape.blocks_per_sm = (int)t->blocks_per_sm;
     ctx->shape.refill = (int)t->refill;
+    ctx->shape.sort_rays = (t->flags & BG_TUNE_SORT_RAYS) ? 1 : 0;
     return BG_OK;
 }
 
@@ -779,6 +784,14 @@ bg_status bg_trace_any(bg_ctx* ctx, const bg_scene* s, const bg_ray* rays, size_
 
 // ---------------------------------------------------------------- render
 extern "C++" {
+void bgi::scene_bounds(const bg_scene* s, float lo[3], float inv[3]) {
+    for (int k = 0; k < 3; ++k) {
+        const float ext = std::fmax(s->bmax[k] - s->bmin[k], 1e-6f) * 1.002f;
+        lo[k] = s->bmin[k] - 0.001f * ext;
+        inv[k] = 1.0f / ext;
+    }
+}
+
 bg_status bgi::validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o,
                                const float* rgb_out) {
     if (!ctx || !s || !cam || !o) return BG_ERR_INVALID;
@@ -807,7 +820,9 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         CK(cudaMemsetAsync(ctx->film.nan_count, 0, sizeof(unsigned long long), ctx->stream));
     }
     bg::Camera dc = make_camera(*cam);
-    bg::RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
+    bg::RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed,
+                        {0, 0, 0}, {0, 0, 0}};
+    scene_bounds(s, rp.bmin, rp.binv);
     const uint64_t npix = (uint64_t)cam->width * cam->height;
     const uint64_t total = npix * o->spp;
     uint64_t launches = 0;

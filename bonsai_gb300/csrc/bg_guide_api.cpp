@@ -593,11 +593,7 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
     gw.pool_cap = g->pool_cap;
     gw.cap = g->wcap;  // >= cap, the paths of one wave
     float lo[3], inv[3];
-    for (int k = 0; k < 3; ++k) {
-        float ext = std::fmax(s->bmax[k] - s->bmin[k], 1e-6f) * 1.002f;
-        lo[k] = s->bmin[k] - 0.001f * ext;
-        inv[k] = 1.0f / ext;
-    }
+    scene_bounds(s, lo, inv);
     gw.bmin = make_float4(lo[0], lo[1], lo[2], 0.0f);
     gw.binv = make_float4(inv[0], inv[1], inv[2], 0.0f);
     gw.rec = g->rec;
@@ -625,7 +621,8 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         CK(cudaMemsetAsync(g->relvar, 0, 2 * sizeof(double), ctx->stream));
         CK(cudaMemsetAsync(g->pass, 0, npix * 3 * sizeof(float), ctx->stream));
         CK(cudaEventRecord(g->ev[0], ctx->stream));
-        bg::RenderParams rp{cam->width, cam->height, k, o->max_depth, o->first_sample + done, o->rr_threshold, o->seed};
+        bg::RenderParams rp{cam->width, cam->height, k, o->max_depth, o->first_sample + done, o->rr_threshold, o->seed,
+                            {lo[0], lo[1], lo[2]}, {inv[0], inv[1], inv[2]}};
         const uint64_t items = npix * k;
         for (uint64_t item0 = 0; item0 < items; item0 += cap) {
             uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, items - item0);

@@ -71,6 +71,8 @@ bg::Camera make_camera(const bg_camera& c);
 bg_status ensure_film(bg_ctx* ctx, uint32_t w, uint32_t h);
 bg_status ensure_wave(bg_ctx* ctx, uint32_t cap);
 bg_status check_device_error(bg_ctx* ctx, uint32_t* word);
+// Scene bounds padded slightly: p_norm = (p - lo) * inv lies in [0, 1) for every primitive.
+void scene_bounds(const bg_scene* s, float lo[3], float inv[3]);
 // Shared argument checks of bg_render / bg_render_guided.
 bg_status validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const bg_render_opts* o,
                           const float* rgb_out);

@@ -389,10 +389,10 @@ struct ExtendSrc {
 
 template <int LAYOUT, bool MULTI = false>
 __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err,
-                                                int refill, const SceneRender* tab) {
+                                                int refill, const SceneRender* tab, bool sorted) {
     const uint32_t n = wb.counters[bounce & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
-    ExtendSrc src{wb.queue[bounce & 1], wb, tab};
+    ExtendSrc src{sorted ? wb.qsort : wb.queue[bounce & 1], wb, tab};
 #if BG_SMEM_STACK
     __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
 #else
@@ -400,6 +400,100 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_extend(Scene sc, WaveBuff
 #endif
     if (LAYOUT == 8) traverse_queue8<false, ExtendSrc, MULTI>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
     else traverse_queue<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
+}
+
+// ---- ray binning (BG_TUNE_SORT_RAYS): the extension queue of a bounce, counting-sorted by
+// key = direction octant (3 bits) x Morton index of the origin's cell in an 8x8x8 grid over the
+// scene bounds (9 bits).  Rays that leave the same region in the same octant then sit in the same
+// warps and walk the same part of the tree.  hist: block-local shared-memory counts added to a
+// global histogram; scan: one block turns it into bin cursors (and clears the histogram);
+// scatter: each block reserves one range per (block, bin) and places its rays by local rank.
+constexpr int SORT_BINS = 4096;
+constexpr int SORT_K = 8;  // rays per thread per scatter chunk
+
+BG_D uint32_t spread3(uint32_t v) {  // 3 bits -> every third bit
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4);
+}
+BG_D uint32_t ray_key(const WaveBuffers& wb, const RenderParams& rp, uint32_t slot) {
+    const float4 o = wb.ray_o[slot], d = wb.ray_d[slot];
+    const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+    const uint32_t cx = (uint32_t)rclamp((o.x - rp.bmin[0]) * rp.binv[0] * 8.0f, 0.0f, 7.0f);
+    const uint32_t cy = (uint32_t)rclamp((o.y - rp.bmin[1]) * rp.binv[1] * 8.0f, 0.0f, 7.0f);
+    const uint32_t cz = (uint32_t)rclamp((o.z - rp.bmin[2]) * rp.binv[2] * 8.0f, 0.0f, 7.0f);
+    return (oct << 9) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(WaveBuffers wb, RenderParams rp, uint32_t bounce) {
+    __shared__ uint32_t h[SORT_BINS];
+    for (int b = threadIdx.x; b < SORT_BINS; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const uint32_t n = wb.counters[bounce & 1];
+    const uint32_t* q = wb.queue[bounce & 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[ray_key(wb, rp, q[i])], 1u);
+    __syncthreads();
+    for (int b = threadIdx.x; b < SORT_BINS; b += blockDim.x)
+        if (h[b]) atomicAdd(&wb.sort_hist[b], h[b]);
+}
+
+__global__ void __launch_bounds__(1024) k_sort_scan(WaveBuffers wb) {
+    __shared__ uint32_t part[1024];
+    constexpr int PER = SORT_BINS / 1024;
+    uint32_t v[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        v[k] = wb.sort_hist[threadIdx.x * PER + k];
+        sum += v[k];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan of the partial sums
+        uint32_t x = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    uint32_t base = part[threadIdx.x] - sum;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        wb.sort_hist[SORT_BINS + threadIdx.x * PER + k] = base;
+        wb.sort_hist[threadIdx.x * PER + k] = 0;  // ready for the next bounce
+        base += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(WaveBuffers wb, RenderParams rp, uint32_t bounce) {
+    __shared__ uint32_t h[SORT_BINS];
+    const uint32_t n = wb.counters[bounce & 1];
+    const uint32_t* q = wb.queue[bounce & 1];
+    uint32_t* cursor = wb.sort_hist + SORT_BINS;
+    const uint32_t chunk = blockDim.x * SORT_K;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        for (int b = threadIdx.x; b < SORT_BINS; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+        uint32_t key[SORT_K], rank[SORT_K], slot[SORT_K];
+#pragma unroll
+        for (int k = 0; k < SORT_K; ++k) {
+            const uint32_t i = c0 + k * blockDim.x + threadIdx.x;
+            key[k] = SORT_BINS;
+            if (i < n) {
+                slot[k] = q[i];
+                key[k] = ray_key(wb, rp, slot[k]);
+                rank[k] = atomicAdd(&h[key[k]], 1u);
+            }
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < SORT_BINS; b += blockDim.x)
+            if (h[b]) h[b] = atomicAdd(&cursor[b], h[b]);  // this block's range of bin b
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SORT_K; ++k)
+            if (key[k] < SORT_BINS) {
+                const uint32_t pos = h[key[k]] + rank[k];
+                if (pos < n) wb.qsort[pos] = slot[k];
+            }
+        __syncthreads();
+    }
 }
 
 // Material-key binning of this bounce's hits: one queue per material class plus misses, so each
@@ -879,8 +973,15 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
     for (uint32_t b = 0; b <= rp.max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         if (ev) cudaEventRecord(ev[4 * b + 0], s);
-        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr);
-        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr);
+        const bool sorted = ls.sort_rays && b > 0 && wb.qsort;
+        if (sorted) {
+            k_sort_hist<<<ls.sms * 4, 256, 0, s>>>(wb, rp, b);
+            k_sort_scan<<<1, 1024, 0, s>>>(wb);
+            k_sort_scatter<<<ls.sms * 4, 256, 0, s>>>(wb, rp, b);
+            launches += 3;
+        }
+        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
+        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
         k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
         if (gw.flags) {
@@ -935,7 +1036,7 @@ int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_dep
     int launches = 1;
     for (uint32_t b = 0; b <= max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
-        k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab);
+        k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab, false);
         k_bin<true><<<grid, block, 0, s>>>(sc, wb, b, tab);
         k_shade<CLS_MISS, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
         k_shade<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);

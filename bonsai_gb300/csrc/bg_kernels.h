@@ -13,6 +13,7 @@ struct RenderParams {
     uint32_t width, height, spp, max_depth, first_sample;
     float rr_threshold;
     uint64_t seed;
+    float bmin[3], binv[3];  // scene bounds, for ray binning: cell = (p - bmin) * binv in [0,1)
 };
 
 struct FilmBuffers {
@@ -50,6 +51,8 @@ struct WaveBuffers {
     unsigned long long* ray_stats;  // [0] closest-hit rays traced, [1] any-hit rays traced
     uint32_t* wavectl;              // graph replay: [0] wave index, [1] first sample (device side)
     uint32_t* scene_id;             // batch renders: scene of each path slot
+    uint32_t* qsort;                // binned extension queue (BG_TUNE_SORT_RAYS)
+    uint32_t* sort_hist;            // [0, 4096) bin counts, [4096, 8192) bin cursors
 };
 
 // One scene of a batch render (a device table of these): what a path of the scene needs.
@@ -96,6 +99,7 @@ struct LaunchShape {
     int block;
     int blocks_per_sm = 8;
     int refill = 32;
+    int sort_rays = 0;
 };
 
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,

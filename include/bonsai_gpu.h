@@ -221,8 +221,10 @@ typedef struct bg_tuning {
     uint32_t blocks_per_sm; /* persistent grid of the wavefront stages = SMs x blocks_per_sm (x128) */
     uint32_t refill;        /* traversal: a warp fetches new rays once this many lanes are idle
                                (32 = only when the whole warp is idle)                             */
-    uint32_t reserved;
+    uint32_t flags;         /* BG_TUNE_* bits                                                      */
 } bg_tuning;
+#define BG_TUNE_SORT_RAYS 1u /* bin each bounce's extension rays by direction octant and origin
+                                cell before traversal (single-scene renders)                      */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 

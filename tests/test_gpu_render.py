@@ -5,6 +5,8 @@ dimension), so most paths are identical; transcendental-function ulps, fma-based
 products (the reference's f64 spots) and the wide BVH's tie order separate a few.  Bar: fraction
 of pixel channels more than 3 combined standard errors apart <= 1% (a Gaussian gives 0.27%).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -84,3 +86,29 @@ def test_graph_replay_matches_launches(gpu_ctx):
             assert g.stats.launches > 4 * (sd.max_depth + 1)
     finally:
         autotune.set_(gpu_ctx, 32, 8, 1 << 22)
+
+
+def test_ray_binning_keeps_every_path(gpu_ctx):
+    """BG_TUNE_SORT_RAYS only reorders the extension queue: every path, and so the film, is the same."""
+    from bonsai_gb300 import autotune
+    sd = S.production(160, 90, spp=4, max_depth=6, n_ico=4, ico_level=3, n_spheres=100)
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    old = autotune.get(gpu_ctx)
+    try:
+        pi = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, mode=A.BG_MODE_PBRT, seed=4)
+        films = []
+        for flags in (0, A.BG_TUNE_SORT_RAYS):
+            t = A.bg_tuning()
+            t.wave_paths, t.blocks_per_sm, t.refill, t.flags = 1 << 14, old.blocks_per_sm, old.refill, flags
+            gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(t)))
+            r = pi.render(sc)
+            assert r.stats.error_word == 0
+            films.append((r.rgb, G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height)))
+        (rgb0, (a1, a2, an)), (rgb1, (b1, b2, bn)) = films
+        np.testing.assert_array_equal(an, bn)
+        np.testing.assert_allclose(a1, b1, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(a2, b2, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(rgb0, rgb1, rtol=1e-6, atol=1e-6)
+    finally:
+        gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(old)))
+        sc.close()
