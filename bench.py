@@ -53,7 +53,7 @@ def parse():
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
-    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch"],
+    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch", "whitted", "direct"],
                    default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
                         "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room")
@@ -162,7 +162,7 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
-def cpu_sample(sd, target_s: float, threads: int):
+def cpu_sample(sd, target_s: float, threads: int, **kw):
     """Times the CPU restatement over every k-th image row, k chosen for ~target_s of work."""
     import oracle as O
     from bonsai_gb300 import _abi as A
@@ -172,7 +172,7 @@ def cpu_sample(sd, target_s: float, threads: int):
     H, W = sd.camera.height, sd.camera.width
     probe_rows = (0, H, max(1, H // 8))
     t0 = time.time()
-    orc.render(A.BG_MODE_PBRT, spp=max(1, sd.spp // 16), rows=probe_rows, threads=threads)
+    orc.render(A.BG_MODE_PBRT, spp=max(1, sd.spp // 16), rows=probe_rows, threads=threads, **kw)
     dt = max(time.time() - t0, 1e-3)
     probe_samples = len(range(*probe_rows)) * W * max(1, sd.spp // 16)
     rate = probe_samples / dt
@@ -183,10 +183,10 @@ def cpu_sample(sd, target_s: float, threads: int):
     return orc, rows, nrows * W * sd.spp, build_s
 
 
-def time_cpu(orc, sd, rows, nsamples, threads):
+def time_cpu(orc, sd, rows, nsamples, threads, **kw):
     from bonsai_gb300 import _abi as A
     t0 = time.time()
-    orc.render(A.BG_MODE_PBRT, rows=rows, threads=threads)
+    orc.render(A.BG_MODE_PBRT, rows=rows, threads=threads, **kw)
     dt = time.time() - t0
     return nsamples / dt / 1e6, dt
 
@@ -343,6 +343,81 @@ def run_ours(args):
                   "Mrays_per_s": (st.extension_rays + st.shadow_rays) / (st.device_ms / 1e3) / 1e6,
                   "stage_ms": {"extend": st.trace_ms, "shade": st.shade_ms, "shadow": st.shadow_ms,
                                "total": st.device_ms}},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_integrators(args):
+    """The Whitted (`--workload whitted`) and direct-lighting (`--workload direct`, UniformSampleAll:
+    every light with MIS) integrators on the production scene: value = device Msamples/s over K
+    frames (L2 flushed), e2e through bg_render with the film read back; CPU restatement of the same
+    integrator (oracle/) on all host cores.  One thread per sample walks its ray tree over the
+    8-wide BVH (bonsai_gb300/csrc/bg_integrators.cu)."""
+    import ctypes as C
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    rank, ws, local, dist = dist_init()
+    sd = workload(args.small)
+    if args.workload == "whitted":
+        kind, strategy, name = A.BG_INTEGRATOR_WHITTED, 0, "WhittedIntegrator"
+        integ = lambda: G.WhittedIntegrator(sd.camera, sd.spp, sd.max_depth, mode=A.BG_MODE_PBRT)  # noqa: E731
+    else:
+        kind, strategy, name = A.BG_INTEGRATOR_DIRECT, A.BG_LIGHT_UNIFORM_ALL, "DirectLightingIntegrator(UniformSampleAll)"
+        integ = lambda: G.DirectLightingIntegrator(sd.camera, sd.spp, sd.max_depth, strategy,  # noqa: E731
+                                                   mode=A.BG_MODE_PBRT)
+    ctx = G.Context(local)
+    scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    pi = integ()
+    samples = sd.camera.width * sd.camera.height * sd.spp
+    for _ in range(args.warmup):
+        pi.render(scene, readback=False)
+    clocks = Clocks(local)
+    barrier(dist)
+    ctx.synchronize()
+    clocks.start()
+    dev_ms, launches = 0.0, 0
+    for k in range(args.steps):
+        ctx.flush_l2()
+        r = pi.render(scene, readback=False, first_sample=k * sd.spp)
+        dev_ms += r.stats.device_ms
+        launches += r.stats.launches
+        if r.stats.error_word:
+            raise RuntimeError(f"device error word {r.stats.error_word}")
+    ctx.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    dev_ms_max = max_over_ranks(dist, dev_ms)
+    value = ws * args.steps * samples / (dev_ms_max / 1e3) / 1e6
+    barrier(dist)
+    t0 = time.time()
+    for k in range(args.steps):
+        pi.render(scene, readback=True, first_sample=k * sd.spp)
+    e2e = ws * args.steps * samples / max_over_ranks(dist, time.time() - t0) / 1e6
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        kw = {"integrator": kind, "light_strategy": strategy}
+        orc, rows, nsamples, _ = cpu_sample(sd, args.cpu_seconds, threads, **kw)
+        cv, cdt = time_cpu(orc, sd, rows, nsamples, threads, **kw)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"rows 0..{sd.camera.height} step {rows[2]} x {sd.camera.width} px x {sd.spp} spp "
+                         f"= {nsamples} samples in {cdt:.1f} s (oracle/, PBRT mode, bucket-fixed BVH)"}
+    peak, peak_kind = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
+        "config": config_of(sd, args.small) | {"integrator": name},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
+                "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
+                     "kernel": "k_tree<false, 8> (one thread per sample)", "peak_source": peak_kind,
+                     "note": "no per-ray counters in the per-sample kernel; the path workload carries the roofline"},
+        "cpu_baseline": cpu,
+        "clocks": clk,
     }
     print(json.dumps(line), flush=True)
 
@@ -711,6 +786,9 @@ def main():
         return
     if args.workload == "guiding":
         run_guiding(args)
+        return
+    if args.workload in ("whitted", "direct"):
+        run_integrators(args)
         return
     if args.profile:
         run_profile(args)

@@ -41,6 +41,23 @@ BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
 BG_TUNE_SORT_RAYS = 1
 
+BG_TEXTURE_IMAGE = 0
+BG_TEXTURE_UV = 1
+BG_WRAP_REPEAT = 0
+BG_WRAP_BLACK = 1
+BG_WRAP_CLAMP = 2
+BG_MAPPING_UV = 0
+BG_MAPPING_SPHERICAL = 1
+BG_MAPPING_CYLINDRICAL = 2
+BG_MAPPING_PLANAR = 3
+BG_INTEGRATOR_PATH = 0
+BG_INTEGRATOR_WHITTED = 1
+BG_INTEGRATOR_DIRECT = 2
+BG_LIGHT_UNIFORM_ALL = 0
+BG_LIGHT_UNIFORM_ONE = 1
+BG_TRI_REVERSE_ORIENTATION = 1
+BG_TRI_SWAPS_HANDEDNESS = 2
+
 BG_NOALLOC_MAX_PIXELS = 512 * 512
 BG_NOALLOC_WAVE_PATHS = 65536
 BG_NOALLOC_SCRATCH_BYTES = 29099008
@@ -57,7 +74,20 @@ F3 = C.c_float * 3
 
 class bg_material(C.Structure):
     _fields_ = [("type", C.c_uint32), ("kd", F3), ("ks", F3), ("roughness", C.c_float),
-                ("remap_roughness", C.c_uint32), ("eta", F3), ("k", F3), ("ior", C.c_float)]
+                ("remap_roughness", C.c_uint32), ("eta", F3), ("k", F3), ("ior", C.c_float),
+                ("sigma", C.c_float), ("kd_texture", C.c_uint32), ("ks_texture", C.c_uint32)]
+
+
+class bg_texture(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("wrap", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("rgb", C.c_void_p), ("mapping", C.c_uint32), ("uv_scale", C.c_float * 2),
+                ("uv_delta", C.c_float * 2), ("world_to_texture", C.c_float * 12), ("vs", F3), ("vt", F3),
+                ("ds", C.c_float), ("dt", C.c_float)]
+
+
+class bg_obj_info(C.Structure):
+    _fields_ = [("ntri", C.c_size_t), ("has_normals", C.c_uint32), ("has_uvs", C.c_uint32),
+                ("flags", C.c_uint32)]
 
 
 class bg_area_light(C.Structure):
@@ -85,7 +115,7 @@ class bg_camera(C.Structure):
 class bg_render_opts(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("rr_threshold", C.c_float),
                 ("mode", C.c_uint32), ("seed", C.c_uint64), ("first_sample", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("integrator", C.c_uint32), ("light_strategy", C.c_uint32)]
 
 
 class bg_render_stats(C.Structure):
@@ -155,6 +185,8 @@ SIGNATURES = {
     "bg_scene_add_material": (ST, [P, C.POINTER(bg_material), C.POINTER(C.c_uint32)]),
     "bg_scene_add_area_light": (ST, [P, C.POINTER(bg_area_light), C.POINTER(C.c_uint32)]),
     "bg_scene_add_triangles": (ST, [P, P, C.c_size_t, P, P]),
+    "bg_scene_add_triangle_mesh": (ST, [P, P, C.c_size_t, P, P, P, P, C.c_uint32]),
+    "bg_scene_add_texture": (ST, [P, C.POINTER(bg_texture), C.POINTER(C.c_uint32)]),
     "bg_scene_add_spheres": (ST, [P, P, C.c_size_t]),
     "bg_scene_add_quadrics": (ST, [P, P, C.c_size_t]),
     "bg_scene_commit": (ST, [P, C.c_uint32, C.POINTER(bg_build_stats)]),
@@ -184,6 +216,8 @@ SIGNATURES = {
     "bg_guide_time": (ST, [P, P, C.c_size_t, P, C.c_size_t, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "bg_obj_read": (ST, [C.c_char_p, P, P, C.c_size_t, C.POINTER(C.c_size_t), C.c_char_p, C.c_size_t]),
     "bg_scene_add_obj": (ST, [P, C.c_char_p, P, C.c_uint32, C.c_int32, C.POINTER(C.c_size_t)]),
+    "bg_obj_read_mesh": (ST, [C.c_char_p, P, P, P, P, C.c_size_t, C.POINTER(bg_obj_info), C.c_char_p,
+                              C.c_size_t]),
     "bg_write_exr": (ST, [C.c_char_p, P, C.c_uint32, C.c_uint32]),
     "bg_film_write_exr": (ST, [P, C.c_char_p]),
     "bg_render_batch": (ST, [P, C.POINTER(bg_batch_item), C.c_size_t, C.POINTER(bg_render_stats)]),

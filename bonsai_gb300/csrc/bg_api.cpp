@@ -157,6 +157,15 @@ F3 crs(F3 a, F3 b) {  // vec3.rs:108-122 (f64 products, rounded once)
     double x = a.x, y = a.y, z = a.z, vx = b.x, vy = b.y, vz = b.z;
     return {(float)(y * vz - z * vy), (float)(z * vx - x * vz), (float)(x * vy - y * vx)};
 }
+F3 xf_point_h(const float (&m)[4][4], float x, float y, float z) {  // Point3::transform (point3.rs:51-69)
+    float xp = m[0][0] * x + m[0][1] * y + m[0][2] * z + m[0][3];
+    float yp = m[1][0] * x + m[1][1] * y + m[1][2] * z + m[1][3];
+    float zp = m[2][0] * x + m[2][1] * y + m[2][2] * z + m[2][3];
+    float wp = m[3][0] * x + m[3][1] * y + m[3][2] * z + m[3][3];
+    if (wp == 1.0f) return {xp, yp, zp};
+    float inv = 1.0f / wp;
+    return {xp * inv, yp * inv, zp * inv};
+}
 bg::Camera make_camera(const bg_camera& c) {
     bg::Camera out{};
     float rx = (float)c.width, ry = (float)c.height;
@@ -200,6 +209,13 @@ bg::Camera make_camera(const bg_camera& c) {
     std::memcpy(out.c2w, cw.m, sizeof(out.c2w));
     out.width = c.width;
     out.height = c.height;
+    // dx_camera / dy_camera (perspective.rs:86-89): Point3::transform of (1,0,0) / (0,1,0) minus
+    // that of the origin
+    const F3 o = xf_point_h(r2c.m.m, 0.0f, 0.0f, 0.0f), px = xf_point_h(r2c.m.m, 1.0f, 0.0f, 0.0f),
+             py = xf_point_h(r2c.m.m, 0.0f, 1.0f, 0.0f);
+    const F3 dx = sub(px, o), dy = sub(py, o);
+    out.dxc[0] = dx.x; out.dxc[1] = dx.y; out.dxc[2] = dx.z;
+    out.dyc[0] = dy.x; out.dyc[1] = dy.y; out.dyc[2] = dy.z;
     return out;
 }
 
@@ -291,6 +307,60 @@ bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
                                             " (1 stack overflow, 2 queue overflow, 4 bad prim, 8 bad node)");
     }
     return BG_OK;
+}
+
+// Inverse of an affine 3x4 transform through the 4x4 Gauss-Jordan inverse (mat4.rs:72-140), as
+// Transform::new(m) computes m_inverse.
+extern "C++" void affine_inverse(const float* xf, float* inv) {
+    M4 m = ident();
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) m.m[r][c] = xf[4 * r + c];
+    M4 mi = inverse(m);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) inv[4 * r + c] = mi.m[r][c];
+}
+
+// Per-triangle bits for next-event estimation (TRI_LFLIP, TRI_SFLIP): whether the surface normal
+// of a hit (triangle.rs:299-307, then face-forwarded to the shading normal by
+// set_shading_geometry) and of a sampled point (triangle.rs:534-545) point against
+// cross(p1 - p0, p2 - p0).  With vertex normals both follow the sign of dot(ng, sum b_i n_i),
+// fixed over the triangle when the three dot(ng, n_i) share a sign; an emitting triangle whose
+// vertex normals straddle its plane is refused (its emission side would change across it).
+extern "C++" bool triangle_light_sides(const bg_scene* s, std::vector<uint8_t>* out, std::string* why) {
+    const size_t ntri = s->tri_mat.size();
+    out->resize(ntri);
+    for (size_t i = 0; i < ntri; ++i) {
+        uint8_t f = s->tri_flags[i];
+        const bool flip = ((f & bg::TRI_REVERSE) != 0) != ((f & bg::TRI_SWAPS) != 0);
+        if (!(f & bg::TRI_NORMALS)) {
+            if (flip) f |= bg::TRI_LFLIP | bg::TRI_SFLIP;
+            (*out)[i] = f;
+            continue;
+        }
+        const float* p = &s->tri[9 * i];
+        const double e1[3] = {(double)p[3] - p[0], (double)p[4] - p[1], (double)p[5] - p[2]};
+        const double e2[3] = {(double)p[6] - p[0], (double)p[7] - p[1], (double)p[8] - p[2]};
+        const double ng[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        int pos = 0, neg = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float* n = &s->tri_n[9 * i + 3 * k];
+            const double d = ng[0] * n[0] + ng[1] * n[1] + ng[2] * n[2];
+            pos += d > 0.0;
+            neg += d < 0.0;
+        }
+        if (pos == 3 || neg == 3) {
+            const bool against = neg == 3;
+            // hit: the shading normal is the interpolated one, negated for reverse_orientation
+            if (against != ((f & bg::TRI_REVERSE) != 0)) f |= bg::TRI_LFLIP;
+            if (against) f |= bg::TRI_SFLIP;
+        } else if (s->tri_light[i] >= 0) {
+            *why = "emitting triangle " + std::to_string(i) +
+                   " has vertex normals on both sides of its plane (its emission side would vary across it)";
+            return false;
+        }
+        (*out)[i] = f;
+    }
+    return true;
 }
 
 }  // namespace bgi
@@ -493,6 +563,7 @@ bg_status bg_scene_add_material(bg_scene* s, const bg_material* m, uint32_t* id)
     if (m->type > BG_MAT_DIELECTRIC) return fail(s->ctx, BG_ERR_INVALID, "unknown material type");
     if (m->type == BG_MAT_DIELECTRIC && !(m->ior > 0.0f))
         return fail(s->ctx, BG_ERR_INVALID, "dielectric ior must be > 0");
+    if (!std::isfinite(m->sigma)) return fail(s->ctx, BG_ERR_INVALID, "matte sigma must be finite");
     s->mats.push_back(*m);
     if (id) *id = (uint32_t)(s->mats.size() - 1);
     return BG_OK;
@@ -507,11 +578,13 @@ bg_status bg_scene_add_area_light(bg_scene* s, const bg_area_light* l, uint32_t*
     return BG_OK;
 }
 
-bg_status bg_scene_add_triangles(bg_scene* s, const float* xyz, size_t ntri, const uint32_t* mat,
-                                 const int32_t* light) {
+bg_status bg_scene_add_triangle_mesh(bg_scene* s, const float* xyz, size_t ntri, const uint32_t* mat,
+                                     const int32_t* light, const float* normals, const float* uvs, uint32_t flags) {
     if (!s || (ntri && (!xyz || !mat))) return BG_ERR_INVALID;
     if (!s->ctx) return BG_ERR_INVALID;
     if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    if (flags & ~(BG_TRI_REVERSE_ORIENTATION | BG_TRI_SWAPS_HANDEDNESS))
+        return fail(s->ctx, BG_ERR_INVALID, "unknown triangle flags");
     if (s->tri_mat.size() + ntri >= (1ull << 31)) return fail(s->ctx, BG_ERR_INVALID, "too many triangles");
     for (size_t i = 0; i < ntri; ++i) {
         if (mat[i] >= s->mats.size())
@@ -521,10 +594,113 @@ bg_status bg_scene_add_triangles(bg_scene* s, const float* xyz, size_t ntri, con
         for (int k = 0; k < 9; ++k)
             if (!std::isfinite(xyz[9 * i + k]))
                 return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has a non-finite vertex");
+        for (int k = 0; normals && k < 9; ++k)
+            if (!std::isfinite(normals[9 * i + k]))
+                return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has a non-finite normal");
+        for (int k = 0; uvs && k < 6; ++k)
+            if (!std::isfinite(uvs[6 * i + k]))
+                return fail(s->ctx, BG_ERR_INVALID, "triangle " + std::to_string(i) + " has a non-finite uv");
     }
     s->tri.insert(s->tri.end(), xyz, xyz + 9 * ntri);
     s->tri_mat.insert(s->tri_mat.end(), mat, mat + ntri);
     for (size_t i = 0; i < ntri; ++i) s->tri_light.push_back(light ? light[i] : -1);
+    if (normals) s->tri_n.insert(s->tri_n.end(), normals, normals + 9 * ntri);
+    else s->tri_n.insert(s->tri_n.end(), 9 * ntri, 0.0f);
+    static const float kDefaultUv[6] = {0.0f, 0.0f, 1.0f, 0.0f, 1.0f, 1.0f};  // Triangle::get_uvs
+    if (uvs) s->tri_uv.insert(s->tri_uv.end(), uvs, uvs + 6 * ntri);
+    else
+        for (size_t i = 0; i < ntri; ++i) s->tri_uv.insert(s->tri_uv.end(), kDefaultUv, kDefaultUv + 6);
+    uint8_t f = (uint8_t)(((flags & BG_TRI_REVERSE_ORIENTATION) ? bg::TRI_REVERSE : 0) |
+                          ((flags & BG_TRI_SWAPS_HANDEDNESS) ? bg::TRI_SWAPS : 0) | (normals ? bg::TRI_NORMALS : 0));
+    s->tri_flags.insert(s->tri_flags.end(), ntri, f);
+    s->any_normals |= normals != nullptr && ntri > 0;
+    s->any_uvs |= uvs != nullptr && ntri > 0;
+    s->any_flags |= f != 0 && ntri > 0;
+    return BG_OK;
+}
+
+bg_status bg_scene_add_triangles(bg_scene* s, const float* xyz, size_t ntri, const uint32_t* mat,
+                                 const int32_t* light) {
+    return bg_scene_add_triangle_mesh(s, xyz, ntri, mat, light, nullptr, nullptr, 0u);
+}
+
+// Image::generate_pyramid (src/io/image.rs:55-114): each level halves the previous one (at least
+// 1 x 1), a texel being the mean of its 2 x 2 parents ((a + b + c + d) * 0.25 in f32).
+bg_status bg_scene_add_texture(bg_scene* s, const bg_texture* t, uint32_t* id) {
+    if (!s || !t) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    if (t->kind > BG_TEXTURE_UV) return fail(s->ctx, BG_ERR_INVALID, "unknown texture kind");
+    if (t->wrap > BG_WRAP_CLAMP) return fail(s->ctx, BG_ERR_INVALID, "unknown wrap mode");
+    if (t->mapping > BG_MAPPING_PLANAR) return fail(s->ctx, BG_ERR_INVALID, "unknown texture mapping");
+    bg::TexInfo ti{};
+    ti.kind = t->kind;
+    ti.wrap = t->wrap;
+    ti.mapping = t->mapping;
+    ti.su = t->uv_scale[0];
+    ti.sv = t->uv_scale[1];
+    ti.du = t->uv_delta[0];
+    ti.dv = t->uv_delta[1];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) ti.m[r][c] = t->world_to_texture[4 * r + c];
+    for (int k = 0; k < 3; ++k) {
+        ti.vs[k] = t->vs[k];
+        ti.vt[k] = t->vt[k];
+    }
+    ti.ds = t->ds;
+    ti.dt = t->dt;
+    if (t->kind == BG_TEXTURE_IMAGE) {
+        const uint32_t w = t->width, h = t->height;
+        if (!t->rgb || w == 0 || h == 0) return fail(s->ctx, BG_ERR_INVALID, "image texture needs texels");
+        if ((w & (w - 1)) || (h & (h - 1)))
+            return fail(s->ctx, BG_ERR_UNSUPPORTED,
+                        "image texture sizes must be powers of two (the reference resamples other sizes with a "
+                        "third-party Lanczos filter)");
+        if ((uint64_t)w * h > (1ull << 28)) return fail(s->ctx, BG_ERR_INVALID, "image texture too large");
+        uint32_t nlev = 1;
+        for (uint32_t m = std::max(w, h); m > 1; m >>= 1) ++nlev;  // 1 + ilog2(max(w, h))
+        if (nlev > (uint32_t)bg::TEX_MAX_LEVELS) return fail(s->ctx, BG_ERR_INVALID, "image texture too large");
+        if (s->texels.size() + 2ull * w * h > 0xFFFFFFFFull) return fail(s->ctx, BG_ERR_INVALID, "too many texels");
+        ti.nlevels = nlev;
+        std::vector<float> cur(t->rgb, t->rgb + (size_t)w * h * 3), next;
+        uint32_t cw = w, chh = h;
+        for (uint32_t l = 0; l < nlev; ++l) {
+            if (l > 0) {
+                const uint32_t nw = std::max(cw / 2, 1u), nh = std::max(chh / 2, 1u);
+                size_t d[4] = {0, 3, 3 * (size_t)cw, 3 * ((size_t)cw + 1)};
+                if (cw == 1) {
+                    d[1] = 0;
+                    d[3] -= 3;
+                }
+                if (chh == 1) {
+                    d[2] = 0;
+                    d[3] -= 3 * (size_t)cw;
+                }
+                next.assign((size_t)nw * nh * 3, 0.0f);
+                for (uint32_t y = 0; y < nh; ++y) {
+                    size_t src = 3 * ((size_t)(2 * y) * cw), dst = 3 * ((size_t)y * nw);
+                    for (uint32_t x = 0; x < nw; ++x) {
+                        for (int c = 0; c < 3; ++c) {
+                            next[dst] = (cur[src] + cur[src + d[1]] + cur[src + d[2]] + cur[src + d[3]]) * 0.25f;
+                            ++src;
+                            ++dst;
+                        }
+                        src += 3;
+                    }
+                }
+                cur.swap(next);
+                cw = nw;
+                chh = nh;
+            }
+            ti.lw[l] = cw;
+            ti.lh[l] = chh;
+            ti.loff[l] = (uint32_t)s->texels.size();
+            for (size_t i = 0; i < (size_t)cw * chh; ++i)
+                s->texels.push_back(make_float4(cur[3 * i], cur[3 * i + 1], cur[3 * i + 2], 0.0f));
+        }
+    }
+    s->tex.push_back(ti);
+    if (id) *id = (uint32_t)(s->tex.size() - 1);
     return BG_OK;
 }
 
@@ -655,6 +831,16 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         std::memcpy(d.eta, m.eta, sizeof(d.eta));
         std::memcpy(d.k, m.k, sizeof(d.k));
         d.ior = m.ior;
+        // MatteMaterial: sigma clamped to [0, 90], OrenNayer::new's A and B (oren_nayer.rs:20-30)
+        d.sigma = m.type == BG_MAT_MATTE ? std::fmin(std::fmax(m.sigma, 0.0f), 90.0f) : 0.0f;
+        const float sr = d.sigma * (3.14159265358979323846f / 180.0f);  // f32::to_radians
+        const float s2 = sr * sr;
+        d.on_a = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
+        d.on_b = 0.45f * s2 / (s2 + 0.09f);
+        d.kd_tex = (m.type == BG_MAT_MATTE || m.type == BG_MAT_PLASTIC) ? m.kd_texture : 0u;
+        d.ks_tex = m.type == BG_MAT_PLASTIC ? m.ks_texture : 0u;
+        if (d.kd_tex > s->tex.size() || d.ks_tex > s->tex.size())
+            return fail(ctx, BG_ERR_INVALID, "material " + std::to_string(i) + " refers to an unknown texture");
         d.pad = 0;
     }
     std::vector<bg::Emission> emis(s->lights.size());
@@ -676,6 +862,28 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if ((st = upload(ctx, mats, &d.mats, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, emis, &d.emis, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, light_prims, &d.light_prims, &s->allocs)) != BG_OK) return st;
+    if (s->any_normals || s->any_flags) {
+        std::vector<uint8_t> flags;
+        std::string why;
+        if (!bgi::triangle_light_sides(s, &flags, &why)) return fail(ctx, BG_ERR_UNSUPPORTED, why);
+        if ((st = upload(ctx, flags, &d.tri_flags, &s->allocs)) != BG_OK) return st;
+    }
+    if (s->any_normals) {
+        std::vector<float4> ns(3 * (size_t)ntri);
+        for (size_t k = 0; k < ns.size(); ++k)
+            ns[k] = make_float4(s->tri_n[3 * k], s->tri_n[3 * k + 1], s->tri_n[3 * k + 2], 0.0f);
+        if ((st = upload(ctx, ns, &d.tri_ns, &s->allocs)) != BG_OK) return st;
+    }
+    if (s->any_uvs) {
+        std::vector<float2> uv(3 * (size_t)ntri);
+        for (size_t k = 0; k < uv.size(); ++k) uv[k] = make_float2(s->tri_uv[2 * k], s->tri_uv[2 * k + 1]);
+        if ((st = upload(ctx, uv, &d.tri_uv, &s->allocs)) != BG_OK) return st;
+    }
+    if (!s->tex.empty()) {
+        if ((st = upload(ctx, s->tex, &d.tex, &s->allocs)) != BG_OK) return st;
+        if ((st = upload(ctx, s->texels, &d.texels, &s->allocs)) != BG_OK) return st;
+        d.ntex = (uint32_t)s->tex.size();
+    }
     uint64_t nodes = 0;
     if (kind == BG_BVH_WIDE) {
         bg::Bvh8 b;
@@ -712,7 +920,10 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         const bool wide = kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2;
         uint64_t bytes = tri4.size() * 16 + sph4.size() * 16 +
                          nodes * (kind == BG_BVH_WIDE ? 80 : (kind == BG_BVH_WIDE2 ? 64 : 32)) +
-                         ((uint64_t)ntri + nsph + nquad) * (wide ? 48 : 4) + quad4.size() * 16;
+                         ((uint64_t)ntri + nsph + nquad) * (wide ? 48 : 4) + quad4.size() * 16 +
+                         ((s->any_normals || s->any_flags) ? (uint64_t)ntri : 0) +
+                         (s->any_normals ? 48ull * ntri : 0) + (s->any_uvs ? 24ull * ntri : 0) +
+                         s->tex.size() * sizeof(bg::TexInfo) + s->texels.size() * 16;
         stats->device_bytes = bytes;
     }
     return BG_OK;
@@ -804,6 +1015,10 @@ bg_status bgi::validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* 
     if (o->mode == BG_MODE_REF_COMPAT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2))
         return fail(ctx, BG_ERR_INVALID, "REF_COMPAT rendering needs a BG_BVH_REFERENCE* scene layout");
     if (o->max_depth > 250) return fail(ctx, BG_ERR_INVALID, "max_depth must be <= 250");
+    if (o->integrator > BG_INTEGRATOR_DIRECT) return fail(ctx, BG_ERR_INVALID, "unknown integrator");
+    if (o->light_strategy > BG_LIGHT_UNIFORM_ONE) return fail(ctx, BG_ERR_INVALID, "unknown light strategy");
+    if (o->integrator != BG_INTEGRATOR_PATH && o->max_depth > bg::TREE_MAX_DEPTH)
+        return fail(ctx, BG_ERR_INVALID, "the Whitted and direct-lighting integrators accept max_depth <= 30");
     if (!(o->flags & BG_RENDER_NO_READBACK) && !rgb_out) return BG_ERR_INVALID;
     return BG_OK;
 }
@@ -823,10 +1038,12 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     bg::RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed,
                         {0, 0, 0}, {0, 0, 0}};
     scene_bounds(s, rp.bmin, rp.binv);
+    rp = bg::with_camera(rp, dc, o->spp);
     const uint64_t npix = (uint64_t)cam->width * cam->height;
     const uint64_t total = npix * o->spp;
     uint64_t launches = 0;
-    bool wavefront = (o->mode == BG_MODE_PBRT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2));
+    const bool tree = o->integrator != BG_INTEGRATOR_PATH;
+    bool wavefront = !tree && (o->mode == BG_MODE_PBRT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2));
     uint32_t cap = 0;
     if (wavefront) {
         cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, std::max<uint64_t>(total, 1));
@@ -895,6 +1112,13 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
                                             ctx->shape, ctx->stream,
                                             timing ? ctx->timing_ev.data() + w * ev_per_wave : nullptr);
             }
+        } else if (tree) {
+            const int kind = o->integrator == BG_INTEGRATOR_WHITTED ? 1
+                             : (o->light_strategy == BG_LIGHT_UNIFORM_ALL ? 2 : 3);
+            const int layout = s->kind == BG_BVH_WIDE ? 8 : (s->kind == BG_BVH_WIDE2 ? 2 : 1);
+            bg::launch_tree_integrator(kind, o->mode == BG_MODE_REF_COMPAT, layout, s->dev, dc, rp, ctx->film,
+                                       ctx->d_err, ctx->shape, ctx->stream);
+            launches += 1;
         } else {
             bg::launch_megakernel(o->mode == BG_MODE_REF_COMPAT, s->dev, dc, rp, ctx->film, ctx->d_err, ctx->shape,
                                   ctx->stream);
@@ -985,6 +1209,7 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         r.cam = make_camera(it.camera);
         r.rp = bg::RenderParams{it.camera.width, it.camera.height, it.opts.spp, it.opts.max_depth, it.opts.first_sample,
                                 it.opts.rr_threshold, it.opts.seed};
+        r.rp = bg::with_camera(r.rp, r.cam, it.opts.spp);
         r.film = ctx->film;
         r.film.sum += 3 * pix0;
         r.film.sumsq += 3 * pix0;

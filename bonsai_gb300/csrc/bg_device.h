@@ -10,6 +10,11 @@
 //   nodes        Bvh2Node : 2-wide BVH, both children's boxes in the parent (64 B/node)
 //   leaf_prims   float4x3 : primitives in leaf order (48 B each; triangle p0 p1 p2, or sphere
 //                           center/radius); w of the first float4 = prim id (bit 31: sphere)
+//   tri_flags    uint8    : per triangle TRI_* bits (null when no triangle has attributes)
+//   tri_ns[3*i+k] float4  : shading normal of triangle i vertex k (TRI_NORMALS triangles only)
+//   tri_uv[3*i+k] float2  : uv of triangle i vertex k (null: the default (0,0) (1,0) (1,1))
+//   tex[t]       TexInfo  : image / uv texture t with its mapping and MIPMap level table
+//   texels       float4   : every texture level, rows top to bottom, rgb + 0
 #pragma once
 #include <cstdint>
 
@@ -27,7 +32,36 @@ struct Material {
     float eta[3];
     float k[3];
     float ior;
+    uint32_t kd_tex;  // 0: constant kd, t: texture t - 1 (matte, plastic)
+    float sigma;      // matte: Oren-Nayar sigma in degrees, clamped to [0, 90] (0: Lambertian)
+    float on_a, on_b; // Oren-Nayar A and B of OrenNayer::new (src/bxdfs/oren_nayer.rs:20-30)
+    uint32_t ks_tex;  // 0: constant ks, t: texture t - 1 (plastic)
     uint32_t pad;
+};
+
+// Triangle attribute bits: TriangleOptions::reverse_orientation, Transform::swaps_handedness of
+// the mesh transform, and per-vertex shading normals (TriangleMesh::normal, triangle.rs:17-90).
+// LFLIP / SFLIP (computed when the scene is committed): the surface normal of a hit
+// (triangle.rs:299-307 and Interaction::set_shading_geometry) / of a sampled point
+// (triangle.rs:534-545) is -normalize(cross(p0 - p2, p1 - p2)).  Both depend only on the
+// triangle as long as its vertex normals lie on one side of it, which the host checks for
+// emitting triangles; next-event estimation reads these bits instead of the vertex normals.
+enum : uint8_t { TRI_REVERSE = 1, TRI_SWAPS = 2, TRI_NORMALS = 4, TRI_LFLIP = 8, TRI_SFLIP = 16 };
+
+// ImageTexture / UVTexture with their TextureMapping2D (src/textures/{image,uv}.rs,
+// src/base/texture.rs) and the MIPMap pyramid (src/base/mipmap.rs, src/io/image.rs:55-114).
+enum : uint32_t { TEX_IMAGE = 0, TEX_UV = 1 };
+enum : uint32_t { WRAP_REPEAT = 0, WRAP_BLACK = 1, WRAP_CLAMP = 2 };
+enum : uint32_t { MAP_UV = 0, MAP_SPHERICAL = 1, MAP_CYLINDRICAL = 2, MAP_PLANAR = 3 };
+constexpr int TEX_MAX_LEVELS = 16;
+struct TexInfo {
+    uint32_t kind, wrap, mapping, nlevels;
+    float su, sv, du, dv;  // UVMapping2D scales and deltas
+    float m[3][4];         // world_to_texture (spherical / cylindrical), affine rows
+    float vs[3], ds;       // PlanarMapping2D
+    float vt[3], dt;
+    uint32_t lw[TEX_MAX_LEVELS], lh[TEX_MAX_LEVELS];
+    uint32_t loff[TEX_MAX_LEVELS];  // first texel of each level in `texels`
 };
 
 struct Emission {
@@ -71,6 +105,7 @@ struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-1
     float r2c[4][4];  // raster_to_camera.m
     float c2w[4][4];  // camera_to_world.m
     uint32_t width, height;
+    float dxc[3], dyc[3];  // dx_camera, dy_camera: raster one-pixel steps in camera space
 };
 
 // Quadric record (8 x float4 = 128 B): rows 0-2 object_to_world (3x4), rows 3-5 world_to_object,
@@ -100,7 +135,12 @@ struct Scene {
     const float4* leaf_prims;   // leaf order of whichever wide layout is built
     const Bvh8Node* nodes8;
     uint32_t n_nodes8;
-    uint32_t pad1;
+    uint32_t ntex;
+    const uint8_t* tri_flags;
+    const float4* tri_ns;
+    const float2* tri_uv;
+    const TexInfo* tex;
+    const float4* texels;
 };
 
 enum : uint32_t {

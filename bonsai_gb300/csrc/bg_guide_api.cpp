@@ -623,6 +623,7 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         CK(cudaEventRecord(g->ev[0], ctx->stream));
         bg::RenderParams rp{cam->width, cam->height, k, o->max_depth, o->first_sample + done, o->rr_threshold, o->seed,
                             {lo[0], lo[1], lo[2]}, {inv[0], inv[1], inv[2]}};
+        rp = bg::with_camera(rp, dc, o->spp);
         const uint64_t items = npix * k;
         for (uint64_t item0 = 0; item0 < items; item0 += cap) {
             uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, items - item0);

@@ -46,6 +46,13 @@ struct bg_scene {
     std::vector<float> tri;
     std::vector<uint32_t> tri_mat;
     std::vector<int32_t> tri_light;
+    // per-triangle mesh attributes (all triangles, filled with defaults for triangles without)
+    std::vector<float> tri_n;         // 9 per triangle: vertex shading normals (TRI_NORMALS only)
+    std::vector<float> tri_uv;        // 6 per triangle: vertex uvs
+    std::vector<uint8_t> tri_flags;   // TRI_REVERSE | TRI_SWAPS | TRI_NORMALS
+    bool any_normals = false, any_uvs = false, any_flags = false;
+    std::vector<bg::TexInfo> tex;     // textures, level offsets into texels
+    std::vector<float4> texels;
     std::vector<bg_sphere> sph;
     std::vector<bg_quadric> quads;
     std::vector<bg_material> mats;
@@ -61,6 +68,9 @@ struct bg_scene {
 namespace bgi {
 
 constexpr uint64_t kFaithfulMaxPrims = 200000;
+
+bool triangle_light_sides(const bg_scene* s, std::vector<uint8_t>* out, std::string* why);
+void affine_inverse(const float* xf, float* inv);
 
 bg_status fail(bg_ctx* c, bg_status s, const std::string& msg);
 bg_status cuda_fail(bg_ctx* c, cudaError_t e, const char* what);

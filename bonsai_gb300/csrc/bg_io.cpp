@@ -6,10 +6,14 @@
 // 'v' appends a texture coordinate / normal / position (the first three values), and the mesh is
 // the consecutive triples of all face indices in file order (polygons with more than three
 // corners are not fanned; a trailing partial triple is dropped).  Positions go through the
-// object-to-world transform (TriangleMesh::new).  Normals and texture coordinates are parsed and
-// index-checked like positions but not kept: the device triangles carry geometric normals only.
+// object-to-world transform and normals through its inverse transpose (TriangleMesh::new,
+// src/shapes/triangle.rs:48-90; both skipped for the identity).  The i-th face vertex takes the
+// i-th normal index and the i-th texture index of the file, as the reference pairs them; a mesh
+// has per-vertex normals / uvs when any face gives them.  The mesh's triangles swap handedness
+// when the inverse transform has a negative determinant (Triangle::new, triangle.rs:94-105).
 // Where the reference panics (unreadable file, bad number, index 0 or past the end, a 'v' line
-// with fewer than three values) this returns BG_ERR_INVALID with the line number.
+// with fewer than three values, fewer normal or texture indices than face vertices) this returns
+// BG_ERR_INVALID with the line number.
 //
 // EXR: a single-part scanline file, uncompressed, channels B G R as 32-bit float, one scanline per
 // block - what Image::write (src/io/image.rs:47-53) stores for an Rgb32F buffer, headless.
@@ -97,15 +101,29 @@ std::string trim(const std::string& s) {
     return s.substr(a, b - a);
 }
 
-// Parses the file into world-space triangles (9 floats each).
-bool read_obj(const char* path, const float* xf, std::vector<float>* tri, std::string* err) {
+struct ObjMesh {
+    std::vector<float> tri;  // 9 per triangle, world space
+    std::vector<float> nrm;  // 9 per triangle, or empty
+    std::vector<float> uv;   // 6 per triangle, or empty
+    uint32_t flags = 0;      // BG_TRI_SWAPS_HANDEDNESS
+};
+
+bool is_identity(const float* xf) {
+    if (!xf) return true;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c)
+            if (xf[4 * r + c] != (r == c ? 1.0f : 0.0f)) return false;
+    return true;
+}
+
+// Parses the file into world-space triangles, with their vertex normals and uvs when `attrs`.
+bool read_obj(const char* path, const float* xf, ObjMesh* mesh, std::string* err, bool attrs = true) {
     FILE* f = std::fopen(path, "rb");
     if (!f) {
         *err = std::string("cannot open ") + path;
         return false;
     }
-    std::vector<float> pos;
-    size_t nnormals = 0, nuvs = 0;
+    std::vector<float> pos, nrm, uvv;
     std::vector<size_t> vi, ni, ti;
     std::vector<size_t> vi_line;  // line of each face index, for messages
     std::string line;
@@ -168,10 +186,10 @@ bool read_obj(const char* path, const float* xf, std::vector<float>* tri, std::s
             if (!ok) break;
             if (t.rfind("vt", 0) == 0) {
                 if (p.size() < 2) fail("texture coordinate needs 2 values");
-                ++nuvs;
+                else uvv.insert(uvv.end(), p.begin(), p.begin() + 2);
             } else if (t.rfind("vn", 0) == 0) {
                 if (p.size() < 3) fail("normal needs 3 values");
-                ++nnormals;
+                else nrm.insert(nrm.end(), p.begin(), p.begin() + 3);
             } else {
                 if (p.size() < 3) fail("position needs 3 values");
                 else pos.insert(pos.end(), p.begin(), p.begin() + 3);
@@ -180,7 +198,7 @@ bool read_obj(const char* path, const float* xf, std::vector<float>* tri, std::s
     }
     std::fclose(f);
     if (!ok) return false;
-    const size_t npos = pos.size() / 3;
+    const size_t npos = pos.size() / 3, nnormals = nrm.size() / 3, nuvs = uvv.size() / 2;
     for (size_t i = 0; i < vi.size(); ++i)
         if (vi[i] == 0 || vi[i] > npos) {
             *err = std::string(path) + ":" + std::to_string(vi_line[i]) + ": position index " + std::to_string(vi[i]) +
@@ -198,17 +216,58 @@ bool read_obj(const char* path, const float* xf, std::vector<float>* tri, std::s
             return false;
         }
     const size_t ntri = vi.size() / 3;
-    tri->resize(ntri * 9);
+    if (!attrs) {
+        ni.clear();
+        ti.clear();
+    }
+    // a triangle reads normal[3t + k] / uv[3t + k]: the lists must cover every used face vertex
+    if (!ni.empty() && ni.size() < 3 * ntri) {
+        *err = std::string(path) + ": " + std::to_string(ni.size()) + " normal indices for " +
+               std::to_string(3 * ntri) + " triangle vertices";
+        return false;
+    }
+    if (!ti.empty() && ti.size() < 3 * ntri) {
+        *err = std::string(path) + ": " + std::to_string(ti.size()) + " texture indices for " +
+               std::to_string(3 * ntri) + " triangle vertices";
+        return false;
+    }
+    const bool ident = is_identity(xf);
+    float inv[12];
+    if (!ident) {
+        bgi::affine_inverse(xf, inv);
+        // Transform::swaps_handedness of world_to_object = the inverse (transform.rs:218-224)
+        float det = inv[0] * (inv[5] * inv[10] - inv[6] * inv[9]) - inv[1] * (inv[4] * inv[10] - inv[6] * inv[8]) +
+                    inv[2] * (inv[4] * inv[9] - inv[5] * inv[8]);
+        if (det < 0.0f) mesh->flags |= BG_TRI_SWAPS_HANDEDNESS;
+    }
+    mesh->tri.resize(ntri * 9);
+    if (!ni.empty()) mesh->nrm.resize(ntri * 9);
+    if (!ti.empty()) mesh->uv.resize(ntri * 6);
     for (size_t k = 0; k < ntri * 3; ++k) {
         const float* p = &pos[3 * (vi[k] - 1)];
-        float* o = &(*tri)[3 * k];
-        if (xf) {  // Transform::transform_point of an affine matrix (w = 1)
+        float* o = &mesh->tri[3 * k];
+        if (!ident) {  // Point3::transform of an affine matrix (w = 1)
             for (int r = 0; r < 3; ++r)
                 o[r] = xf[4 * r] * p[0] + xf[4 * r + 1] * p[1] + xf[4 * r + 2] * p[2] + xf[4 * r + 3];
         } else {
             o[0] = p[0];
             o[1] = p[1];
             o[2] = p[2];
+        }
+        if (!ni.empty()) {
+            const float* n = &nrm[3 * (ni[k] - 1)];
+            float* q = &mesh->nrm[3 * k];
+            if (!ident) {  // Normal::transform: m_inverse transposed (normal.rs:21-30)
+                for (int c = 0; c < 3; ++c) q[c] = inv[c] * n[0] + inv[4 + c] * n[1] + inv[8 + c] * n[2];
+            } else {
+                q[0] = n[0];
+                q[1] = n[1];
+                q[2] = n[2];
+            }
+        }
+        if (!ti.empty()) {
+            mesh->uv[2 * k] = uvv[2 * (ti[k] - 1)];
+            mesh->uv[2 * k + 1] = uvv[2 * (ti[k] - 1) + 1];
         }
     }
     return true;
@@ -295,14 +354,34 @@ extern "C" {
 bg_status bg_obj_read(const char* path, const float* object_to_world, float* tri_out, size_t max_tri, size_t* ntri,
                       char* err, size_t err_len) {
     if (!path || !ntri || (max_tri && !tri_out)) return BG_ERR_INVALID;
-    std::vector<float> tri;
+    ObjMesh m;
     std::string msg;
-    if (!read_obj(path, object_to_world, &tri, &msg)) {
+    if (!read_obj(path, object_to_world, &m, &msg, false)) {
         set_err(err, err_len, msg);
         return BG_ERR_INVALID;
     }
-    *ntri = tri.size() / 9;
-    if (tri_out) std::memcpy(tri_out, tri.data(), std::min(max_tri, *ntri) * 9 * sizeof(float));
+    *ntri = m.tri.size() / 9;
+    if (tri_out) std::memcpy(tri_out, m.tri.data(), std::min(max_tri, *ntri) * 9 * sizeof(float));
+    return BG_OK;
+}
+
+bg_status bg_obj_read_mesh(const char* path, const float* object_to_world, float* tri_out, float* normal_out,
+                           float* uv_out, size_t max_tri, bg_obj_info* info, char* err, size_t err_len) {
+    if (!path || !info || (max_tri && !tri_out)) return BG_ERR_INVALID;
+    ObjMesh m;
+    std::string msg;
+    if (!read_obj(path, object_to_world, &m, &msg)) {
+        set_err(err, err_len, msg);
+        return BG_ERR_INVALID;
+    }
+    const size_t n = m.tri.size() / 9, k = std::min(max_tri, n);
+    info->ntri = n;
+    info->has_normals = m.nrm.empty() ? 0u : 1u;
+    info->has_uvs = m.uv.empty() ? 0u : 1u;
+    info->flags = m.flags;
+    if (tri_out) std::memcpy(tri_out, m.tri.data(), k * 9 * sizeof(float));
+    if (normal_out && !m.nrm.empty()) std::memcpy(normal_out, m.nrm.data(), k * 9 * sizeof(float));
+    if (uv_out && !m.uv.empty()) std::memcpy(uv_out, m.uv.data(), k * 6 * sizeof(float));
     return BG_OK;
 }
 
@@ -310,13 +389,15 @@ bg_status bg_scene_add_obj(bg_scene* s, const char* path, const float* object_to
                            int32_t light_id, size_t* ntri) {
     if (!s || !path) return BG_ERR_INVALID;
     if (!s->ctx) return BG_ERR_INVALID;
-    std::vector<float> tri;
+    ObjMesh m;
     std::string msg;
-    if (!read_obj(path, object_to_world, &tri, &msg)) return bgi::fail(s->ctx, BG_ERR_INVALID, msg);
-    const size_t n = tri.size() / 9;
+    if (!read_obj(path, object_to_world, &m, &msg)) return bgi::fail(s->ctx, BG_ERR_INVALID, msg);
+    const size_t n = m.tri.size() / 9;
     std::vector<uint32_t> mat(n, material_id);
     std::vector<int32_t> light(n, light_id);
-    bg_status st = bg_scene_add_triangles(s, tri.data(), n, mat.data(), light.data());
+    bg_status st = bg_scene_add_triangle_mesh(s, m.tri.data(), n, mat.data(), light.data(),
+                                              m.nrm.empty() ? nullptr : m.nrm.data(),
+                                              m.uv.empty() ? nullptr : m.uv.data(), m.flags);
     if (st == BG_OK && ntri) *ntri = n;
     return st;
 }

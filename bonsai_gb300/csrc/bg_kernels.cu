@@ -15,6 +15,8 @@
 #include "bg_kernels.h"
 #include "bg_shading.cuh"
 #include "bg_traverse.cuh"
+#include "bg_film.cuh"
+#include "bg_estimate.cuh"
 
 namespace bg {
 
@@ -45,29 +47,6 @@ BG_D Ray load_ray(float4 o, float4 d) {
     r.d = f4xyz(d);
     r.time = d.w;
     return r;
-}
-
-// FilmTile::add_sample with the box filter (r = 0.5: weight 1 to the sample's own pixel) after
-// the radiance sanity checks of SamplerIntegrator::render (src/base/integrator.rs:91-120).
-BG_D void film_add(const FilmBuffers& f, uint32_t pix, RGB L) {
-    float y = luminance(L);
-    if (is_nan(L) || y < -1e-5f || isinf(y)) {
-        L = rgb(0.0f);
-        atomicAdd(f.nan_count, 1ull);
-    }
-    double r = L.r, g = L.g, b = L.b;
-    atomicAdd(&f.sum[3 * pix + 0], r);
-    atomicAdd(&f.sum[3 * pix + 1], g);
-    atomicAdd(&f.sum[3 * pix + 2], b);
-    atomicAdd(&f.sumsq[3 * pix + 0], r * r);
-    atomicAdd(&f.sumsq[3 * pix + 1], g * g);
-    atomicAdd(&f.sumsq[3 * pix + 2], b * b);
-    atomicAdd(&f.count[pix], 1u);
-    if (f.pass) {
-        atomicAdd(&f.pass[3 * pix + 0], L.r);
-        atomicAdd(&f.pass[3 * pix + 1], L.g);
-        atomicAdd(&f.pass[3 * pix + 2], L.b);
-    }
 }
 
 // ================================================================ ray queries
@@ -145,57 +124,45 @@ void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays
 #undef BG_TRACE
 }
 
-// ================================================================ megakernel (reference layout)
-// estimate_direct (src/base/integrator.rs:330-437) over the reference BVH.
-template <bool REF>
-BG_D RGB estimate_direct_ref(const Scene& sc, const Isect& it, const BSDF& bsdf, uint32_t light_prim, float us0,
-                             float us1, float ul0, float ul1, uint32_t* err) {
-    const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
-    RGB out = rgb(0.0f);
-    LightSample ls = light_sample<REF>(sc, light_prim, it, ul0, ul1);
-    float scattering_pdf = 0.0f;
-    if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
-        RGB f = bsdf.f<REF>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
-        scattering_pdf = bsdf.pdf<REF>(it.wo, ls.wi, flags);
-        if (!is_black(f)) {
-            Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
-            if (ref_traverse<true>(sc, sr, err, nullptr) >= 0) ls.radiance = rgb(0.0f);
-            if (!is_black(ls.radiance)) {
-                float w = power_heuristic(1.0f, ls.pdf, 1.0f, scattering_pdf);
-                out = out + f * ls.radiance * w / ls.pdf;
-            }
-        }
-    }
-    BxSample bs = bsdf.sample<REF>(it.wo, us0, us1, flags);
-    RGB f = bs.f * abs_dot(bs.wi, it.ns);
-    bool sampled_specular = (bs.stype & BSDF_SPECULAR) != 0;
-    // REF (F2): ray along the light sample's direction with the light half's pdf, any emitter
-    V3 wdir = REF ? ls.wi : bs.wi;
-    float spdf = REF ? scattering_pdf : bs.pdf;
-    if (!is_black(f) && spdf > 0.0f) {
-        float w = 1.0f;
-        if (!sampled_specular) {
-            float lpdf = light_pdf<REF>(sc, light_prim, it, wdir, nullptr);
-            if (lpdf == 0.0f) return out;
-            w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
-        }
-        Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wdir, REF);
-        Ray rr = ray;
-        int prim = ref_traverse<false>(sc, rr, err, nullptr);
-        RGB li = rgb(0.0f);
-        if (prim >= 0 && (REF ? prim_emission(sc, prim) >= 0 : prim == (int)light_prim)) {
-            Isect lit;
-            if (prim_isect(sc, prim, ray, &lit)) li = emitted_radiance(sc, lit, -wdir);
-        }
-        if (!is_black(li)) out = out + f * li * w / spdf;
-    }
-    return out;
+// ================================================================ textures
+// Texture inputs at a hit whose material is textured (nullptr otherwise): the surface geometry
+// re-derived from the hit and the screen-space differentials of ray differentials `rd`.
+BG_D const TexPoint* tex_point(const Scene& sc, const Isect& it, const Ray& ray, const RayDiff* rd, TexPoint* tp) {
+    if (!sc.ntex || !material_textured(sc.mats[prim_material(sc, it.prim)])) return nullptr;
+    Isect tmp;
+    if (!prim_isect(sc, it.prim, ray, &tmp, &tp->g)) tp->g = SurfaceGeom{};
+    tp->p = it.p;
+    tp->n = it.n;
+    tp->d = compute_differentials(it.p, it.n, tp->g, rd);
+    return tp;
+}
+// The camera ray differentials of path (pixel, sample); `cam_ray` is its camera ray.
+BG_D RayDiff path_camera_diff(const RenderParams& rp, uint32_t pix, uint32_t s, const Ray& cam_ray) {
+    Rng rng{pix, s, rp.seed};
+    float c[4];
+    rng.block(0, c);
+    float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
+    return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale);
+}
+// BSDF of a path vertex: textured materials read the camera differentials at the first hit
+// (PathIntegrator spawns later rays without differentials, path.rs:139).
+// TEX: texture support compiled in (it costs the shade kernels about 30 registers).
+template <int CLS, bool TEX>
+BG_D BSDF path_bsdf(const Scene& sc, const RenderParams& rp, uint32_t pix, uint32_t s, uint32_t bounce, const Ray& ray,
+                    const Isect& it) {
+    if (!TEX || !sc.ntex) return make_bsdf<CLS>(sc, it);
+    TexPoint tp;
+    RayDiff rd;
+    if (bounce == 0) rd = path_camera_diff(rp, pix, s, ray);
+    return make_bsdf<CLS>(sc, it, tex_point(sc, it, ray, bounce == 0 ? &rd : nullptr, &tp));
 }
 
-// PathIntegrator::radiance (src/integrators/path.rs:51-146) over the reference BVH.
+// ================================================================ megakernel (reference layout)
+// `rd0`: the camera ray's differentials (textured scenes), which the path keeps in REF mode (the
+// ray never re-spawns, F1) and only has at the first hit in PBRT mode.
 template <bool REF>
 BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_depth, float rr_threshold,
-                      uint32_t* err) {
+                      uint32_t* err, const RayDiff* rd0) {
     RGB out = rgb(0.0f), beta = rgb(1.0f);
     bool specular_bounce = false;
     float eta_scale = 1.0f;
@@ -209,7 +176,8 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
             if (hit) out = out + beta * emitted_radiance(sc, it, -ray.d);
         }
         if (!hit || bounces >= max_depth) break;
-        BSDF bsdf = make_bsdf(sc, it);
+        TexPoint tp;
+        BSDF bsdf = make_bsdf<-1, REF>(sc, it, tex_point(sc, it, traced, (REF || bounces == 0) ? rd0 : nullptr, &tp));
         const uint32_t base = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounces;
         float u[8];
         rng.block(base, u);
@@ -218,7 +186,7 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
             float count = (float)sc.nlights;
             uint32_t li = (uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f);
             float lpdf = 1.0f / count;
-            RGB ld = estimate_direct_ref<REF>(sc, it, bsdf, sc.light_prims[li], u[BD_USCAT], u[BD_USCAT + 1],
+            RGB ld = estimate_direct_mk<REF, 1>(sc, it, bsdf, sc.light_prims[li], u[BD_USCAT], u[BD_USCAT + 1],
                                               u[BD_ULIGHT], u[BD_ULIGHT + 1], err);
             out = out + beta * (ld / lpdf);
         }
@@ -257,7 +225,9 @@ __global__ void __launch_bounds__(128) k_megakernel(Scene sc, Camera cam, Render
         rng.block(0, c);
         float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
         Ray ray = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
-        RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err);
+        RayDiff rd;
+        if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale);
+        RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err, sc.ntex ? &rd : nullptr);
         film_add(film, pix, L);
     }
 }
@@ -631,7 +601,7 @@ struct VertexOut {
     float4 sh_o[2], sh_d[2];
 };
 
-template <int CLS>
+template <int CLS, bool TEX = false>
 BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
                          uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
                          uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out) {
@@ -641,7 +611,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     float u[8];
     rng.block(ub, u);
     rng.block(ub + 4, u + 4);
-    BSDF bsdf = make_bsdf<CLS>(sc, it);
+    BSDF bsdf = path_bsdf<CLS, TEX>(sc, rp, wb.pixel[slot], wb.sample[slot], bounce, ray, it);
     if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
         float count = (float)sc.nlights;
@@ -684,14 +654,12 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         }
         if (!is_black(f) && spdf > 0.0f) {
             float t_light = 0.0f;
-            float lpdf = light_pdf<false>(sc, light_prim, it, wi, &t_light);
+            V3 ln;
+            float lpdf = light_pdf<false>(sc, light_prim, it, wi, &t_light, &ln);
             if (lpdf != 0.0f) {
                 float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
                 // the sampled direction reaches the light at t_light; it counts iff nothing else
                 // is hit first (closest hit == this light)
-                V3 p0, p1, p2;
-                load_tri(sc, light_prim, &p0, &p1, &p2);
-                V3 ln = normalize(cross(p0 - p2, p1 - p2));
                 RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -wi);
                 if (!is_black(li)) {
                     RGB c = f * li * w / spdf;
@@ -765,7 +733,7 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 // In guided waves the matte / plastic / conductor classes stop after their emission and queue a
 // network query; k_guide_continue finishes them with the network's mixture.
 // GWK: guiding support compiled in (records, guided queries); the plain wavefront uses GWK = false.
-template <int CLS, bool MULTI = false, bool GWK = false>
+template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false>
 __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
@@ -817,7 +785,7 @@ __global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, Film
                 gq = make_query(gw, it, -ray.d);
                 push_guide = true;
             } else if (!finished) {
-                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
+                scatter_vertex<CLS, TEX>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
                                     vo);
                 finished = vo.finished;
                 cont = vo.cont;
@@ -990,6 +958,12 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        } else if (sc.ntex) {
+            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         } else {
             k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);

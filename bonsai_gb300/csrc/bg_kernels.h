@@ -1,5 +1,6 @@
 // bg_kernels.h - launch interface between the host driver (bg_api.cpp) and the kernels.
 #pragma once
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -14,7 +15,16 @@ struct RenderParams {
     float rr_threshold;
     uint64_t seed;
     float bmin[3], binv[3];  // scene bounds, for ray binning: cell = (p - bmin) * binv in [0,1)
+    Camera cam;              // for the camera rays' differentials at the first hit (textures)
+    float diff_scale;        // Ray::scale_differentials factor, 1 / sqrt(samples per pixel)
+    uint32_t pad;            // keeps the struct free of tail padding (it is hashed as graph key)
 };
+// RenderParams for a render call: camera and differential scale filled in.
+inline RenderParams with_camera(RenderParams rp, const Camera& cam, uint32_t total_spp) {
+    rp.cam = cam;
+    rp.diff_scale = 1.0f / sqrtf((float)(total_spp ? total_spp : 1u));
+    return rp;
+}
 
 struct FilmBuffers {
     double* sum;     // 3 per pixel
@@ -105,6 +115,15 @@ struct LaunchShape {
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,
                   uint8_t* occluded, uint32_t* err, unsigned long long* counters, uint32_t* work_head,
                   const LaunchShape& ls, cudaStream_t s);
+// Whitted / direct-lighting integrators (bg_integrators.cu): kind 1 Whitted, 2 direct lighting with
+// UniformSampleAll, 3 direct lighting with UniformSampleOne; layout 1 reference, 2 two-wide,
+// 8 eight-wide.  Tree depth is limited to TREE_MAX_DEPTH (a specular ray tree's pending-ray
+// stack holds at most max_depth + 1 entries).
+constexpr uint32_t TREE_MAX_DEPTH = 30;
+constexpr int TREE_STACK = (int)TREE_MAX_DEPTH + 2;
+void launch_tree_integrator(int kind, bool ref_compat, int layout, const Scene& sc, const Camera& cam,
+                            const RenderParams& rp, const FilmBuffers& film, uint32_t* err, const LaunchShape& ls,
+                            cudaStream_t s);
 void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, const RenderParams& rp,
                        const FilmBuffers& film, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
 // One wave of the PBRT wavefront: items [item0, item0 + nitems) of the pixel x sample space.

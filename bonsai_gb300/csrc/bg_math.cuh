@@ -188,9 +188,10 @@ BG_HD void philox4x32_10(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
 struct Rng {
     uint32_t pixel, sample;
     uint64_t seed;
+    uint32_t stream;  // 0 for path integrators; a tree integrator's node (node id - 1)
     // four consecutive dimensions starting at a multiple of 4
     BG_D void block(uint32_t dim4, float out[4]) const {
-        uint32_t c[4] = {sample, dim4 >> 2, (uint32_t)(seed >> 32), 0x626F6E73u};
+        uint32_t c[4] = {sample, dim4 >> 2, (uint32_t)(seed >> 32), 0x626F6E73u ^ stream};
         philox4x32_10(c, pixel, (uint32_t)seed);
 #pragma unroll
         for (int i = 0; i < 4; ++i) out[i] = (float)(c[i] >> 9) * 0x1p-23f;

@@ -180,6 +180,7 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     LaunchShape shape{dev_sms > 0 ? dev_sms : 1, 128, 8, 32};
     Camera dc = camera_for(*cam);
     RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
+    rp = with_camera(rp, dc, o->spp);
     const uint64_t total = npix * o->spp;
     if (total > 0) {
         if (o->mode == BG_MODE_PBRT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2)) {

@@ -9,6 +9,7 @@
 #include "bg_device.h"
 #include "bg_math.cuh"
 #include "bg_shapes.cuh"
+#include "bg_texture.cuh"
 
 namespace bg {
 
@@ -184,14 +185,24 @@ BG_D float power_heuristic(float nf, float fp, float ng, float gp) {
     return (f * f) / (f * f + g * g);
 }
 
-enum BxKind : uint8_t { BX_LAMBERT = 0, BX_MF_REFL = 1, BX_FRESNEL_SPEC = 2 };
+// BX_OREN_NAYAR: src/bxdfs/oren_nayer.rs; BX_SPEC_REFL / BX_SPEC_TRANS: SpecularReflection /
+// SpecularTransmission (src/bxdfs/specular.rs), the dielectric's two lobes when the caller does
+// not allow a multi-lobe BxDF (the Whitted and direct-lighting integrators, PBRT mode).
+enum BxKind : uint8_t {
+    BX_LAMBERT = 0,
+    BX_MF_REFL = 1,
+    BX_FRESNEL_SPEC = 2,
+    BX_OREN_NAYAR = 3,
+    BX_SPEC_REFL = 4,
+    BX_SPEC_TRANS = 5
+};
 struct Bxdf {
     uint8_t kind, type;
     bool conductor;
-    RGB r;             // R (lambert, microfacet, specular R)
+    RGB r;             // R (lambert, Oren-Nayar, microfacet, specular R / T)
     TR dist;
     RGB eta_t, k;      // conductor (eta_i = 1)
-    float ei, et;      // dielectric fresnel / FresnelSpecular eta_a, eta_b
+    float ei, et;      // dielectric fresnel / specular eta_a, eta_b; Oren-Nayar A, B
     BG_D bool matches(uint8_t f) const { return (type & f) == type; }
 };
 struct BxSample {
@@ -219,9 +230,29 @@ BG_D Bxdf select_bxdf(bool second, const Bxdf& a, const Bxdf& b) {
     return r;
 }
 
+// OrenNayer::f (oren_nayer.rs:34-60)
+BG_D RGB oren_nayar_f(const Bxdf& b, V3 wo, V3 wi) {
+    float sti = sin_theta(wi), sto = sin_theta(wo);
+    float max_cos = 0.0f;
+    if (sti > 1e-4f && sto > 1e-4f) {
+        float spi = sin_phi(wi), cpi = cos_phi(wi), spo = sin_phi(wo), cpo = cos_phi(wo);
+        max_cos = rmax(0.0f, cpi * cpo + spi * spo);
+    }
+    float sin_alpha, tan_beta;
+    if (abs_cos_theta(wi) > abs_cos_theta(wo)) {
+        sin_alpha = sto;
+        tan_beta = sti / abs_cos_theta(wi);
+    } else {
+        sin_alpha = sti;
+        tan_beta = sto / abs_cos_theta(wo);
+    }
+    return b.r * (1.0f / PI) * (b.ei + b.et * max_cos * sin_alpha * tan_beta);
+}
+
 template <bool REF>
 BG_D RGB bx_f(const Bxdf& b, V3 wo, V3 wi) {
     if (b.kind == BX_LAMBERT) return b.r * (1.0f / PI);
+    if (b.kind == BX_OREN_NAYAR) return oren_nayar_f(b, wo, wi);
     if (b.kind == BX_MF_REFL) {  // bxdfs/microfacet.rs:69-94
         float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
         V3 wh = wi + wo;
@@ -237,7 +268,8 @@ BG_D RGB bx_f(const Bxdf& b, V3 wo, V3 wi) {
 }
 template <bool REF>
 BG_D float bx_pdf(const Bxdf& b, V3 wo, V3 wi) {
-    if (b.kind == BX_LAMBERT) return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;
+    if (b.kind == BX_LAMBERT || b.kind == BX_OREN_NAYAR)
+        return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;
     if (b.kind == BX_MF_REFL) {
         if (!same_hemisphere(wo, wi)) return 0.0f;
         V3 wh = normalize(wo + wi);
@@ -252,7 +284,7 @@ BG_D BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1) {
     s.f = rgb(0.0f);
     s.pdf = 0.0f;
     s.stype = -1;
-    if (b.kind == BX_LAMBERT) {
+    if (b.kind == BX_LAMBERT || b.kind == BX_OREN_NAYAR) {
         V3 wi = cosine_sample_hemisphere(u0, u1);
         if (wo.z < 0.0f) wi.z *= -1.0f;
         s.wi = wi;
@@ -269,6 +301,25 @@ BG_D BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1) {
         s.wi = wi;
         s.f = bx_f<REF>(b, wo, wi);
         s.pdf = b.dist.pdf<REF>(wo, wh) / (4.0f * dot(wo, wh));
+        return s;
+    }
+    if (b.kind == BX_SPEC_REFL) {  // specular.rs:57-66
+        V3 wi = v3(-wo.x, -wo.y, wo.z);
+        s.wi = wi;
+        s.f = rgb(fresnel_dielectric<REF>(wi.z, b.ei, b.et)) * b.r / abs_cos_theta(wi);
+        s.pdf = 1.0f;
+        return s;
+    }
+    if (b.kind == BX_SPEC_TRANS) {  // specular.rs:82-113
+        bool entering = wo.z > 0.0f;
+        float ei = entering ? b.ei : b.et, et = entering ? b.et : b.ei;
+        V3 wi;
+        if (!refract(wo, face_forward(v3(0.0f, 0.0f, 1.0f), wo), ei / et, &wi)) return s;
+        RGB f = b.r * (rgb(1.0f) - rgb(fresnel_dielectric<REF>(wi.z, b.ei, b.et)));
+        f = f * ((ei * ei) / (et * et));
+        s.wi = wi;
+        s.f = f / abs_cos_theta(wi);
+        s.pdf = 1.0f;
         return s;
     }
     // FresnelSpecular (bxdfs/fresnel.rs:76-122)
@@ -396,11 +447,18 @@ BG_D uint32_t prim_material(const Scene& sc, int prim) {
     return __float_as_uint(sc.quads[QUADRIC_F4 * (prim - sc.ntri - sc.nsph) + 7].w);
 }
 
-// Material::compute_scattering_functions for the constant-texture materials.  CLS is the
-// material type when the caller knows it (the wavefront shades one material class per launch),
-// -1 to read it from the record.
-template <int CLS = -1>
-BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
+BG_D bool material_textured(const Material& m) { return (m.kd_tex | m.ks_tex) != 0u; }
+BG_D RGB clamp_rgb0(RGB c) {  // RGBSpectrum::clamp(0, +inf)
+    return rgb(rclamp(c.r, 0.0f, INFINITY), rclamp(c.g, 0.0f, INFINITY), rclamp(c.b, 0.0f, INFINITY));
+}
+
+// Material::compute_scattering_functions (src/materials/{matte,plastic}.rs and the composed
+// conductor / dielectric).  CLS is the material type when the caller knows it (the wavefront
+// shades one material class per launch), -1 to read it from the record.  `tp` carries the
+// texture inputs (needed when the material is textured); `multi_lobe` = allow_multiple_lobes:
+// false splits the dielectric into SpecularReflection + SpecularTransmission in PBRT mode.
+template <int CLS = -1, bool REF = false>
+BG_D BSDF make_bsdf(const Scene& sc, const Isect& it, const TexPoint* tp = nullptr, bool multi_lobe = true) {
     const Material& m = sc.mats[prim_material(sc, it.prim)];
     const uint32_t type = CLS >= 0 ? (uint32_t)CLS : m.type;
     BSDF b;
@@ -411,19 +469,25 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
     b.ss = normalize(it.dpdu);
     b.ts = cross(b.ns, b.ss);
     if (type == 0 || type == 1) {  // matte, plastic
-        // Lambertian (if kd != 0) then glossy (plastic, if ks != 0), packed into the fixed slots
-        // with selects: a slot chosen by a runtime index would force the BSDF into local memory.
-        RGB kd = rgb(rclamp(m.kd[0], 0.0f, INFINITY), rclamp(m.kd[1], 0.0f, INFINITY), rclamp(m.kd[2], 0.0f, INFINITY));
+        // Lambertian / Oren-Nayar (if kd != 0) then glossy (plastic, if ks != 0), packed into the
+        // fixed slots with selects: a slot chosen by a runtime index would force the BSDF into
+        // local memory.
+        RGB kd = (m.kd_tex && tp) ? tex_eval<REF>(sc, m.kd_tex - 1u, *tp) : rgb(m.kd[0], m.kd[1], m.kd[2]);
+        kd = clamp_rgb0(kd);
         Bxdf l{};
-        l.kind = BX_LAMBERT;
+        const bool oren = type == 0 && m.sigma != 0.0f;
+        l.kind = oren ? BX_OREN_NAYAR : BX_LAMBERT;
         l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
         l.r = kd;
         l.conductor = false;
+        l.ei = m.on_a;
+        l.et = m.on_b;
         const bool has_l = !is_black(kd);
         bool has_g = false;
         Bxdf g{};
         if (type == 1) {
-            RGB ks = rgb(rclamp(m.ks[0], 0.0f, INFINITY), rclamp(m.ks[1], 0.0f, INFINITY), rclamp(m.ks[2], 0.0f, INFINITY));
+            RGB ks = (m.ks_tex && tp) ? tex_eval<REF>(sc, m.ks_tex - 1u, *tp) : rgb(m.ks[0], m.ks[1], m.ks[2]);
+            ks = clamp_rgb0(ks);
             has_g = !is_black(ks);
             g.kind = BX_MF_REFL;
             g.type = BSDF_REFLECTION | BSDF_GLOSSY;
@@ -445,7 +509,7 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
         g.conductor = true;
         g.eta_t = rgb(m.eta[0], m.eta[1], m.eta[2]);
         g.k = rgb(m.k[0], m.k[1], m.k[2]);
-    } else {  // dielectric
+    } else if (REF || multi_lobe) {  // dielectric
         b.eta = m.ior;
         Bxdf& d = b.bx[b.n++];
         d.kind = BX_FRESNEL_SPEC;
@@ -454,6 +518,22 @@ BG_D BSDF make_bsdf(const Scene& sc, const Isect& it) {
         d.conductor = false;
         d.ei = 1.0f;
         d.et = m.ior;
+    } else {  // dielectric as two specular lobes (PBRT-v3 GlassMaterial without multiple lobes)
+        b.eta = m.ior;
+        Bxdf r{}, t{};
+        r.kind = BX_SPEC_REFL;
+        r.type = BSDF_REFLECTION | BSDF_SPECULAR;
+        r.r = rgb(1.0f);
+        r.ei = 1.0f;
+        r.et = m.ior;
+        t.kind = BX_SPEC_TRANS;
+        t.type = BSDF_TRANSMISSION | BSDF_SPECULAR;
+        t.r = rgb(1.0f);
+        t.ei = 1.0f;
+        t.et = m.ior;
+        b.bx[0] = r;
+        b.bx[1] = t;
+        b.n = 2;
     }
     return b;
 }
@@ -488,6 +568,7 @@ BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, f
     V3 p0, p1, p2;
     load_tri(sc, prim, &p0, &p1, &p2);
     ls.pt = tri_sample(p0, p1, p2, u0, u1);
+    if (tri_flag_bits(sc, prim) & TRI_SFLIP) ls.pt.n = ls.pt.n * -1.0f;
     V3 wi = ls.pt.p - it.p;
     float pdf;
     if (length_squared(wi) == 0.0f) pdf = 0.0f;
@@ -503,9 +584,10 @@ BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, f
     ls.pdf = pdf;
     return ls;
 }
-// Shape::pdf_from_it for a triangle light (shape.rs:40-57).  Also returns the hit distance.
+// Shape::pdf_from_it for a triangle light (shape.rs:40-57).  Also returns the hit distance and
+// the light's surface normal there (for its one-sided emission).
 template <bool REF>
-BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, float* t_light) {
+BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, float* t_light, V3* n_light = nullptr) {
     Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wi, REF);
     V3 p0, p1, p2;
     load_tri(sc, prim, &p0, &p1, &p2);
@@ -513,10 +595,12 @@ BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, flo
     TriHit h;
     if (!tri_test(tr, ray.t_max, p0, p1, p2, &h)) return 0.0f;
     Isect li;
-    tri_isect(p0, p1, p2, h, ray, &li);
+    tri_isect_plain(p0, p1, p2, h, ray, &li);
+    if (tri_flag_bits(sc, prim) & TRI_LFLIP) li.n = -li.n;
     float pdf = distance_squared(it.p, li.p) / (abs_dot(li.n, -wi) * tri_area(p0, p1, p2));
     if (isinf(pdf)) pdf = 0.0f;
     if (t_light) *t_light = h.t;
+    if (n_light) *n_light = li.n;
     return pdf;
 }
 

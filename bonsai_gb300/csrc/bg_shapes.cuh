@@ -108,19 +108,32 @@ struct Isect {
     int prim;
 };
 
-// Triangle::intersect's interaction (triangle.rs:241-307) from the barycentrics.
-BG_D void tri_isect(V3 p0, V3 p1, V3 p2, const TriHit& h, const Ray& ray, Isect* it) {
+// The parts of a SurfaceInteraction that only textures and ray differentials read: the (u,v)
+// parameterisation, the geometric partials dpdu / dpdv and the shading normal's partials
+// (interaction.rs:18-55).  Computed on demand (prim_geom) so plain shading does not carry them.
+struct SurfaceGeom {
+    float u, v;
+    V3 dpdu, dpdv;  // geometric (SurfaceInteraction::dpdu / dpdv)
+    V3 dndu, dndv;  // shading (Shading::dndu / dndv)
+};
+
+// Vec3::coordinate_system (vec3.rs:25-33)
+BG_D void coordinate_system(V3 v1, V3* v2, V3* v3o) {
+    if (fabsf(v1.x) > fabsf(v1.y)) *v2 = v3(-v1.z, 0.0f, v1.x) / sqrtf(v1.x * v1.x + v1.z * v1.z);
+    else *v2 = v3(0.0f, v1.z, -v1.y) / sqrtf(v1.y * v1.y + v1.z * v1.z);
+    *v3o = cross(v1, *v2);
+}
+
+// Triangle interaction without vertex attributes (default uvs (0,0),(1,0),(1,1), no shading
+// normals, no orientation flip): triangle.rs:241-307 with the uv deltas folded.
+BG_D void tri_isect_plain(V3 p0, V3 p1, V3 p2, const TriHit& h, const Ray& ray, Isect* it) {
     V3 dp02 = p0 - p2, dp12 = p1 - p2;
     // default uvs (0,0),(1,0),(1,1): duv02=(-1,-1), duv12=(0,-1), determinant 1
     V3 dpdu = (-1.0f * dp02 - -1.0f * dp12) * 1.0f;
     V3 dpdv = (-0.0f * dp02 + -1.0f * dp12) * 1.0f;
     if (length_squared(cross(dpdu, dpdv)) == 0.0f) {
         V3 ng = normalize(cross(p2 - p0, p1 - p0));
-        // Vec3::coordinate_system (vec3.rs:25-33)
-        if (fabsf(ng.x) > fabsf(ng.y))
-            dpdu = v3(-ng.z, 0.0f, ng.x) / sqrtf(ng.x * ng.x + ng.z * ng.z);
-        else
-            dpdu = v3(0.0f, ng.z, -ng.y) / sqrtf(ng.y * ng.y + ng.z * ng.z);
+        coordinate_system(ng, &dpdu, &dpdv);
     }
     float xs = fabsf(h.b0 * p0.x) + fabsf(h.b1 * p1.x) + fabsf(h.b2 * p2.x);
     float ys = fabsf(h.b0 * p0.y) + fabsf(h.b1 * p1.y) + fabsf(h.b2 * p2.y);
@@ -133,6 +146,101 @@ BG_D void tri_isect(V3 p0, V3 p1, V3 p2, const TriHit& h, const Ray& ray, Isect*
     it->n = nn;
     it->ns = nn;
     it->dpdu = dpdu;
+}
+
+BG_D uint8_t tri_flag_bits(const Scene& sc, uint32_t prim) { return sc.tri_flags ? sc.tri_flags[prim] : (uint8_t)0; }
+// Triangle::get_uvs (triangle.rs:107-117)
+BG_D void tri_uvs(const Scene& sc, uint32_t prim, float2 uv[3]) {
+    if (sc.tri_uv) {
+        uv[0] = sc.tri_uv[3 * prim];
+        uv[1] = sc.tri_uv[3 * prim + 1];
+        uv[2] = sc.tri_uv[3 * prim + 2];
+    } else {
+        uv[0] = make_float2(0.0f, 0.0f);
+        uv[1] = make_float2(1.0f, 0.0f);
+        uv[2] = make_float2(1.0f, 1.0f);
+    }
+}
+
+// Triangle::intersect's interaction with the mesh's vertex attributes (triangle.rs:241-400):
+// partials from the vertex uvs, the geometric normal flipped for reverse_orientation ^
+// transform_swaps_handedness, and with vertex normals the shading frame of
+// Interaction::set_shading_geometry (interaction.rs:145-168, orientation authoritative).
+BG_D void tri_isect(const Scene& sc, uint32_t prim, V3 p0, V3 p1, V3 p2, const TriHit& h, const Ray& ray, Isect* it,
+                    SurfaceGeom* g = nullptr) {
+    const uint8_t fl = tri_flag_bits(sc, prim);
+    if (!sc.tri_uv && fl == 0 && !g) {
+        tri_isect_plain(p0, p1, p2, h, ray, it);
+        return;
+    }
+    float2 uv[3];
+    tri_uvs(sc, prim, uv);
+    const float du02 = uv[0].x - uv[2].x, dv02 = uv[0].y - uv[2].y;
+    const float du12 = uv[1].x - uv[2].x, dv12 = uv[1].y - uv[2].y;
+    V3 dp02 = p0 - p2, dp12 = p1 - p2;
+    const float det = du02 * dv12 - dv02 * du12;
+    const bool degenerate_uv = fabsf(det) < 1e-8f;
+    V3 dpdu = v3(0.0f, 0.0f, 0.0f), dpdv = v3(0.0f, 0.0f, 0.0f);
+    if (!degenerate_uv) {
+        float inv = 1.0f / det;
+        dpdu = (dv12 * dp02 - dv02 * dp12) * inv;
+        dpdv = (-du12 * dp02 + du02 * dp12) * inv;
+    }
+    if (degenerate_uv || length_squared(cross(dpdu, dpdv)) == 0.0f) {
+        V3 ng = cross(p2 - p0, p1 - p0);
+        coordinate_system(normalize(ng), &dpdu, &dpdv);
+    }
+    float xs = fabsf(h.b0 * p0.x) + fabsf(h.b1 * p1.x) + fabsf(h.b2 * p2.x);
+    float ys = fabsf(h.b0 * p0.y) + fabsf(h.b1 * p1.y) + fabsf(h.b2 * p2.y);
+    float zs = fabsf(h.b0 * p0.z) + fabsf(h.b1 * p1.z) + fabsf(h.b2 * p2.z);
+    it->p_err = gamma(7.0f) * v3(xs, ys, zs);
+    it->p = h.b0 * p0 + h.b1 * p1 + h.b2 * p2;
+    it->time = ray.time;
+    it->wo = -ray.d;
+    V3 nn = normalize(cross(dp02, dp12));
+    if (((fl & TRI_REVERSE) != 0) != ((fl & TRI_SWAPS) != 0)) nn = -nn;
+    it->n = nn;
+    it->ns = nn;
+    it->dpdu = dpdu;
+    V3 dndu = v3(0.0f, 0.0f, 0.0f), dndv = v3(0.0f, 0.0f, 0.0f);
+    if (fl & TRI_NORMALS) {
+        const V3 n0 = f4xyz(sc.tri_ns[3 * prim]), n1 = f4xyz(sc.tri_ns[3 * prim + 1]),
+                 n2 = f4xyz(sc.tri_ns[3 * prim + 2]);
+        V3 sn = h.b0 * n0 + h.b1 * n1 + h.b2 * n2;
+        sn = length_squared(sn) > 0.0f ? normalize(sn) : it->n;
+        V3 st = normalize(dpdu);
+        V3 sb = cross(st, sn);
+        if (length_squared(sb) > 0.0f) {
+            sb = normalize(sb);
+            st = cross(sb, sn);
+        } else {
+            coordinate_system(sn, &st, &sb);
+        }
+        if (g) {
+            V3 dn1 = n0 - n2, dn2 = n1 - n2;
+            if (degenerate_uv) {
+                V3 dn = cross(n2 - n0, n1 - n0);
+                if (length_squared(dn) != 0.0f) coordinate_system(dn, &dndu, &dndv);
+            } else {
+                float inv = 1.0f / det;
+                dndu = (dv12 * dn1 - dv02 * dn2) * inv;
+                dndv = (-du12 * dn1 + du02 * dn2) * inv;
+            }
+        }
+        if (fl & TRI_REVERSE) sb = -sb;
+        V3 ns = normalize(cross(st, sb));
+        it->n = face_forward(it->n, ns);
+        it->ns = ns;
+        it->dpdu = st;
+    }
+    if (g) {
+        g->u = (h.b0 * uv[0].x + h.b1 * uv[1].x) + h.b2 * uv[2].x;
+        g->v = (h.b0 * uv[0].y + h.b1 * uv[1].y) + h.b2 * uv[2].y;
+        g->dpdu = dpdu;
+        g->dpdv = dpdv;
+        g->dndu = dndu;
+        g->dndv = dndv;
+    }
 }
 
 BG_D float tri_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(p1 - p0, p2 - p0)); }
@@ -170,6 +278,17 @@ BG_D V3 xf_vec_err_id(V3 v, V3* e) {
     e->y = g3 * (fabsf(0.0f * v.x) + fabsf(1.0f * v.y) + fabsf(0.0f * v.z));
     e->z = g3 * (fabsf(0.0f * v.x) + fabsf(0.0f * v.y) + fabsf(1.0f * v.z));
     return xf_vec_id(v);
+}
+
+// Normal partials from the fundamental forms (sphere.rs:191-204, cylinder.rs:161-179,
+// cone.rs:161-179).
+BG_D void weingarten(V3 dpdu, V3 dpdv, V3 d2pduu, V3 d2pduv, V3 d2pdvv, V3* dndu, V3* dndv) {
+    float e1 = dot(dpdu, dpdu), f1 = dot(dpdu, dpdv), g1 = dot(dpdv, dpdv);
+    V3 n = normalize(cross(dpdu, dpdv));
+    float e2 = dot(n, d2pduu), f2 = dot(n, d2pduv), g2 = dot(n, d2pdvv);
+    float inv_egf = 1.0f / (e1 * g1 - f1 * f1);
+    *dndu = (f2 * f1 - e2 * g1) * inv_egf * dpdu + (e2 * f1 - f2 * e1) * inv_egf * dpdv;
+    *dndv = (g2 * f1 - f2 * g1) * inv_egf * dpdu + (f2 * f1 - g2 * e1) * inv_egf * dpdv;
 }
 
 struct SphHit {
@@ -214,7 +333,7 @@ BG_D bool sphere_test(float4 s, const Ray& rw, float t_max, SphHit* out) {
 }
 
 // Sphere interaction (sphere.rs:163-236 + Interaction::transform, interaction.rs:268-300).
-BG_D void sphere_isect(float4 s, const SphHit& h, const Ray& rw, Isect* it) {
+BG_D void sphere_isect(float4 s, const SphHit& h, const Ray& rw, Isect* it, SurfaceGeom* g = nullptr) {
     const float radius = s.w;
     const float phi_max = 360.0f * (PI / 180.0f);
     const float theta_min = acosf(rclamp(-radius / radius, -1.0f, 1.0f));
@@ -253,6 +372,20 @@ BG_D void sphere_isect(float4 s, const SphHit& h, const Ray& rw, Isect* it) {
     it->n = normalize(nt);
     it->ns = face_forward(normalize(nt), it->n);
     it->dpdu = xf_vec_id(dpdu);
+    if (g) {  // sphere.rs:165-204: (u, v) and the Weingarten normal derivatives
+        float phi = atan2f(ph.y, ph.x);
+        if (phi < 0.0f) phi += 2.0f * PI;
+        g->u = phi / phi_max;
+        g->v = (theta - theta_min) / (theta_max - theta_min);
+        V3 d2pduu = -phi_max * phi_max * v3(ph.x, ph.y, 0.0f);
+        V3 d2pduv = (theta_max - theta_min) * ph.z * phi_max * v3(-sin_phi, cos_phi, 0.0f);
+        V3 d2pdvv = -(theta_max - theta_min) * (theta_max - theta_min) * ph;
+        weingarten(dpdu, dpdv, d2pduu, d2pduv, d2pdvv, &g->dndu, &g->dndv);
+        g->dpdu = xf_vec_id(dpdu);
+        g->dpdv = xf_vec_id(dpdv);
+        g->dndu = xf_vec_id(g->dndu);  // Normal::transform with the identity m_inverse
+        g->dndv = xf_vec_id(g->dndv);
+    }
 }
 
 // ---------------------------------------------------------------- quadrics (cylinder, disk, cone)
@@ -321,7 +454,8 @@ BG_D float ef_abs_err(EF e) { return next_float_up(rmax(fabsf(e.hi - e.v), fabsf
 
 // Cylinder / Disk / Cone ::intersect and ::intersect_test (cylinder.rs:71-288, disk.rs:70-183,
 // cone.rs:67-287).  Fills `it` (world-space interaction) when it is non-null.
-BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out, Isect* it) {
+BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out, Isect* it,
+                      SurfaceGeom* g = nullptr) {
     const float4 p0 = q[6], p1 = q[7];
     const uint32_t flags = __float_as_uint(p1.z);
     const int kind = (int)(flags & 0xFFu);
@@ -339,7 +473,8 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
         ray.o = ray.o + ray.d * dt;
     }
     V3 ph, dpdu, dpdv, perr;
-    float tsh_v;
+    V3 d2pduu = v3(0.0f, 0.0f, 0.0f), d2pduv = v3(0.0f, 0.0f, 0.0f);
+    float tsh_v, gu = 0.0f, gv = 0.0f;
     if (kind == 1) {  // disk
         if (ray.d.z == 0.0f) return false;
         float tsh = (height - ray.o.z) / ray.d.z;
@@ -355,6 +490,8 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
             return true;
         }
         float rh = sqrtf(dist);
+        gu = phi / phi_max;  // disk.rs:106-113 (dndu = dndv = 0)
+        gv = (radius - rh) / (radius - inner);
         dpdu = v3(-phi_max * ph.y, phi_max * ph.x, 0.0f);
         dpdv = v3(ph.x, ph.y, 0.0f) * (inner - radius) / rh;
         ph.z = height;
@@ -384,6 +521,7 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
             if (tsh.hi > ray.t_max) return false;
         }
         bool used_t1 = tsh.v == t1.v && tsh.lo == t1.lo && tsh.hi == t1.hi;
+        float phi = 0.0f;
         for (int pass = 0; pass < 2; ++pass) {
             ph = ray.o + ray.d * tsh.v;
             if (kind == 0) {
@@ -391,7 +529,7 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
                 ph.x *= radius / hr;
                 ph.y *= radius / hr;
             }
-            float phi = atan2f(ph.y, ph.x);
+            phi = atan2f(ph.y, ph.x);
             if (phi < 0.0f) phi += 2.0f * PI;
             bool clipped = kind == 0 ? (ph.z < z_min || ph.z > z_max || phi > phi_max)
                                      : (ph.z < 0.0f || ph.z > height || phi > phi_max);
@@ -406,12 +544,17 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
             return true;
         }
         dpdu = v3(-phi_max * ph.y, phi_max * ph.x, 0.0f);
+        gu = phi / phi_max;
+        d2pduu = -phi_max * phi_max * v3(ph.x, ph.y, 0.0f);
         if (kind == 0) {
+            gv = (ph.z - z_min) / (z_max - z_min);
             dpdv = v3(0.0f, 0.0f, z_max - z_min);
             perr = gamma(3.0f) * vabs(v3(ph.x, ph.y, 0.0f));
         } else {
             float v = ph.z / height;
+            gv = v;
             dpdv = v3(-ph.x / (1.0f - v), -ph.y / (1.0f - v), height);
+            d2pduv = phi_max / (1.0f - v) * v3(ph.y, -ph.x, 0.0f);
             EF px = ox + tsh * dx, py = oy + tsh * dy, pz = oz + tsh * dz;
             perr = v3(ef_abs_err(px), ef_abs_err(py), ef_abs_err(pz));
         }
@@ -429,6 +572,16 @@ BG_D bool quadric_hit(const float4* q, const Ray& rw, float t_max, float* t_out,
     it->n = normalize(m_normal(w2o, n));
     it->ns = face_forward(normalize(m_normal(w2o, n)), it->n);
     it->dpdu = m_vec(o2w, dpdu);
+    if (g) {
+        V3 dndu = v3(0.0f, 0.0f, 0.0f), dndv = v3(0.0f, 0.0f, 0.0f);
+        if (kind != 1) weingarten(dpdu, dpdv, d2pduu, d2pduv, v3(0.0f, 0.0f, 0.0f), &dndu, &dndv);
+        g->u = gu;
+        g->v = gv;
+        g->dpdu = m_vec(o2w, dpdu);
+        g->dpdv = m_vec(o2w, dpdv);
+        g->dndu = m_normal(w2o, dndu);
+        g->dndv = m_normal(w2o, dndv);
+    }
     *t_out = tsh_v;
     return true;
 }
@@ -472,6 +625,7 @@ BG_D Ray spawn_ray_to(V3 p, V3 perr, V3 n, float time, V3 q, V3 qerr, V3 qn) {
 struct ShapeSample {
     V3 p, p_err, n;
     float pdf_area;
+    float b0, b1;
 };
 BG_D ShapeSample tri_sample(V3 p0, V3 p1, V3 p2, float u0, float u1) {
     ShapeSample s;
@@ -483,6 +637,8 @@ BG_D ShapeSample tri_sample(V3 p0, V3 p1, V3 p2, float u0, float u1) {
     V3 pabs = vabs(b0 * p0) + vabs(b1 * p1) + vabs(b2 * p2);
     s.p_err = gamma(6.0f) * pabs;
     s.pdf_area = 1.0f / tri_area(p0, p1, p2);
+    s.b0 = b0;
+    s.b1 = b1;
     return s;
 }
 
@@ -495,22 +651,23 @@ BG_D void load_tri(const Scene& sc, uint32_t prim, V3* p0, V3* p1, V3* p2) {
 
 // Full closest-hit interaction for a primitive given the ray (re-runs the shape test with
 // t_max = infinity, which reproduces the traversal's t, barycentrics and hit side).
-BG_D bool prim_isect(const Scene& sc, int prim, const Ray& ray, Isect* it) {
+// With `g`, also the surface parameterisation and partials (SurfaceGeom).
+BG_D bool prim_isect(const Scene& sc, int prim, const Ray& ray, Isect* it, SurfaceGeom* g = nullptr) {
     if ((uint32_t)prim < sc.ntri) {
         V3 p0, p1, p2;
         load_tri(sc, (uint32_t)prim, &p0, &p1, &p2);
         TriRay tr = make_tri_ray(ray);
         TriHit h;
         if (!tri_test(tr, INFINITY, p0, p1, p2, &h)) return false;
-        tri_isect(p0, p1, p2, h, ray, it);
+        tri_isect(sc, (uint32_t)prim, p0, p1, p2, h, ray, it, g);
     } else if ((uint32_t)prim < sc.ntri + sc.nsph) {
         float4 s = sc.sph[prim - sc.ntri];
         SphHit h;
         if (!sphere_test(s, ray, INFINITY, &h)) return false;
-        sphere_isect(s, h, ray, it);
+        sphere_isect(s, h, ray, it, g);
     } else {
         float t;
-        if (!quadric_hit(sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph), ray, INFINITY, &t, it)) return false;
+        if (!quadric_hit(sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph), ray, INFINITY, &t, it, g)) return false;
     }
     it->prim = prim;
     return true;

@@ -464,6 +464,62 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
     tgroup->y = hitmask & 0x00FFFFFFu;
 }
 
+// One ray through the 8-wide layout on one thread (the node-group walk of traverse_queue8 without
+// the warp's ray replacement), for the per-sample megakernels.  Returns the hit prim; closest hit
+// leaves the distance in ray.t_max.  `skip` excludes one primitive (any-hit only).
+template <bool ANY>
+BG_D int bvh8_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) {
+    if (sc.n_nodes8 == 0) return -1;
+    const Ray8 r8 = make_ray8(ray);
+    const TriRay tr = make_tri_ray(ray);
+    uint2 stack[STACK8];
+    int sp = 0, hit = -1;
+    uint2 ngroup = make_uint2(0, 0x80000000u), tgroup = make_uint2(0, 0);
+    for (;;) {
+        if (ngroup.y > 0x00FFFFFFu) {
+            const uint32_t hits = ngroup.y;
+            const uint32_t bit = 31u - __clz(hits);
+            ngroup.y &= ~(1u << bit);
+            if (ngroup.y > 0x00FFFFFFu) {
+                if (sp >= STACK8) {
+                    atomicOr(err, ERR_STACK_OVERFLOW);
+                    return hit;
+                }
+                stack[sp++] = ngroup;
+            }
+            const uint32_t slot = (bit - 24u) ^ (r8.octinv4 & 0xFFu);
+            const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+            const uint32_t child = ngroup.x + rel;
+            if (child >= sc.n_nodes8) {
+                atomicOr(err, ERR_BAD_NODE);
+                return hit;
+            }
+            bvh8_node_hits(sc, child, r8, ray.t_max, &ngroup, &tgroup);
+        } else {
+            tgroup = ngroup;
+            ngroup = make_uint2(0, 0);
+        }
+        while (tgroup.y != 0) {
+            const uint32_t bit = 31u - __clz(tgroup.y);
+            tgroup.y &= ~(1u << bit);
+            if (tgroup.x + bit >= sc.ntri + sc.nsph + sc.nquad) {
+                atomicOr(err, ERR_BAD_PRIM);
+                continue;
+            }
+            int prim;
+            if (leaf_prim_hit(sc, tgroup.x + bit, tr, ray, !ANY, &prim)) {
+                if (ANY && prim == skip) continue;
+                hit = prim;
+                if (ANY) return hit;
+            }
+        }
+        if (ngroup.y <= 0x00FFFFFFu) {
+            if (sp == 0) return hit;
+            ngroup = stack[--sp];
+        }
+    }
+}
+
 // Persistent traversal of the 8-wide layout with in-warp ray replacement (see traverse_queue).
 // The node-group stack lives in shared memory, entry k of thread t at smem[k * blockDim.x + t].
 // Triangle groups are postponed (pushed) while fewer than kPostpone lanes of the warp would test

@@ -99,10 +99,21 @@ class Scene:
         for l in sd.lights:
             ll = A.bg_area_light.from_buffer_copy(np.ascontiguousarray(l).tobytes())
             ctx.check(lib.bg_scene_add_area_light(h, C.byref(ll), None))
+        for t in sd.textures:
+            tt, keep = S.texture_struct(t)
+            ctx.check(lib.bg_scene_add_texture(h, C.byref(tt), None))
         tri = np.ascontiguousarray(sd.tri, np.float32)
         tm = np.ascontiguousarray(sd.tri_mat, np.uint32)
         tl = np.ascontiguousarray(sd.tri_light, np.int32)
-        ctx.check(lib.bg_scene_add_triangles(h, _ptr(tri), sd.ntri, _ptr(tm), _ptr(tl)))
+        if sd.tri_normals is None and sd.tri_uvs is None and sd.tri_flags is None:
+            ctx.check(lib.bg_scene_add_triangles(h, _ptr(tri), sd.ntri, _ptr(tm), _ptr(tl)))
+        else:
+            nrm = None if sd.tri_normals is None else np.ascontiguousarray(sd.tri_normals, np.float32)
+            uvs = None if sd.tri_uvs is None else np.ascontiguousarray(sd.tri_uvs, np.float32)
+            for a, b, has_n, fl in S.triangle_runs(sd):
+                ctx.check(lib.bg_scene_add_triangle_mesh(
+                    h, tri[a:].ctypes.data, b - a, tm[a:].ctypes.data, tl[a:].ctypes.data,
+                    nrm[a:].ctypes.data if has_n else None, uvs[a:].ctypes.data if uvs is not None else None, fl))
         if sd.nsph:
             sp = np.ascontiguousarray(sd.spheres)
             ctx.check(lib.bg_scene_add_spheres(h, _ptr(sp), sd.nsph))
@@ -162,6 +173,9 @@ class RenderResult:
 class PathIntegrator:
     """PathIntegrator::new(camera, sampler, max_depth, rr_threshold) rendering on the GPU."""
 
+    integrator = A.BG_INTEGRATOR_PATH
+    light_strategy = 0
+
     def __init__(self, camera: S.Camera, spp: int, max_depth: int, rr_threshold: float = 1.0,
                  mode: int = A.BG_MODE_PBRT, seed: int = 0):
         self.camera, self.spp, self.max_depth = camera, spp, max_depth
@@ -178,6 +192,7 @@ class PathIntegrator:
         o.mode = self.mode
         o.seed = self.seed
         o.first_sample = first_sample
+        o.integrator, o.light_strategy = self.integrator, self.light_strategy
         o.flags = ((A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK) |
                    (A.BG_RENDER_GRAPH if graph else 0) | (A.BG_RENDER_STAGE_TIMING if stage_timing else 0))
         rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
@@ -212,6 +227,27 @@ class PathIntegrator:
         n = np.zeros((height, width), np.uint32)
         ctx.check(ctx.lib.bg_film_moments(ctx.h, _ptr(s1), _ptr(s2), _ptr(n)))
         return s1, s2, n
+
+
+class WhittedIntegrator(PathIntegrator):
+    """WhittedIntegrator::new(camera, sampler, max_depth) (src/integrators/whitted.rs:128-136)."""
+
+    integrator = A.BG_INTEGRATOR_WHITTED
+
+    def __init__(self, camera: S.Camera, spp: int, max_depth: int, mode: int = A.BG_MODE_PBRT, seed: int = 0):
+        super().__init__(camera, spp, max_depth, 1.0, mode, seed)
+
+
+class DirectLightingIntegrator(PathIntegrator):
+    """DirectLightingIntegrator::new(camera, sampler, scene, max_depth, strategy)
+    (src/integrators/direct.rs:27-53); strategy = A.BG_LIGHT_UNIFORM_ALL or A.BG_LIGHT_UNIFORM_ONE."""
+
+    integrator = A.BG_INTEGRATOR_DIRECT
+
+    def __init__(self, camera: S.Camera, spp: int, max_depth: int, strategy: int = A.BG_LIGHT_UNIFORM_ALL,
+                 mode: int = A.BG_MODE_PBRT, seed: int = 0):
+        super().__init__(camera, spp, max_depth, 1.0, mode, seed)
+        self.light_strategy = strategy
 
 
 @dataclass

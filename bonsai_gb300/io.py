@@ -30,6 +30,27 @@ def read_obj(path: str | os.PathLike, object_to_world: np.ndarray | None = None)
     return tri
 
 
+def read_obj_mesh(path: str | os.PathLike, object_to_world: np.ndarray | None = None):
+    """(triangles (n, 9), vertex normals (n, 9) or None, uvs (n, 6) or None, BG_TRI_* flags) of an OBJ
+    file, as bg_scene_add_obj adds it; raises ValueError with the library's message."""
+    lib = A.load()
+    xf = None if object_to_world is None else np.ascontiguousarray(object_to_world, np.float32).reshape(12)
+    info = A.bg_obj_info()
+    err = C.create_string_buffer(512)
+    p = os.fsencode(str(path))
+    xp = None if xf is None else xf.ctypes.data
+    if lib.bg_obj_read_mesh(p, xp, None, None, None, 0, C.byref(info), err, len(err)) != A.BG_OK:
+        raise ValueError(err.value.decode(errors="replace"))
+    n = info.ntri
+    tri = np.zeros((n, 9), np.float32)
+    nrm = np.zeros((n, 9), np.float32) if info.has_normals else None
+    uv = np.zeros((n, 6), np.float32) if info.has_uvs else None
+    ptr = lambda a: None if a is None or not n else a.ctypes.data  # noqa: E731
+    if lib.bg_obj_read_mesh(p, xp, ptr(tri), ptr(nrm), ptr(uv), n, C.byref(info), err, len(err)) != A.BG_OK:
+        raise ValueError(err.value.decode(errors="replace"))
+    return tri, nrm, uv, int(info.flags)
+
+
 def write_exr(path: str | os.PathLike, rgb: np.ndarray) -> None:
     rgb = np.ascontiguousarray(rgb, np.float32)
     h, w, c = rgb.shape

@@ -18,7 +18,7 @@ import numpy as np
 
 MATERIAL_DT = np.dtype([("type", "<u4"), ("kd", "<f4", 3), ("ks", "<f4", 3), ("roughness", "<f4"),
                         ("remap_roughness", "<u4"), ("eta", "<f4", 3), ("k", "<f4", 3),
-                        ("ior", "<f4")])
+                        ("ior", "<f4"), ("sigma", "<f4"), ("kd_texture", "<u4"), ("ks_texture", "<u4")])
 LIGHT_DT = np.dtype([("intensity", "<f4", 3), ("two_sided", "<u4")])
 SPHERE_DT = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("material_id", "<u4"),
                       ("light_id", "<i4")])
@@ -38,7 +38,8 @@ COPPER_K = (3.91295, 2.45285, 2.14219)
 
 
 def material(kind: int, kd=(0, 0, 0), ks=(0, 0, 0), roughness=0.0, remap=False,
-             eta=COPPER_ETA, k=COPPER_K, ior=1.5) -> np.ndarray:
+             eta=COPPER_ETA, k=COPPER_K, ior=1.5, sigma=0.0, kd_texture=0, ks_texture=0) -> np.ndarray:
+    """A bg_material record; kd_texture / ks_texture are texture indices + 1 (0 = the constant)."""
     m = np.zeros((), MATERIAL_DT)
     m["type"] = kind
     m["kd"] = kd
@@ -48,7 +49,61 @@ def material(kind: int, kd=(0, 0, 0), ks=(0, 0, 0), roughness=0.0, remap=False,
     m["eta"] = eta
     m["k"] = k
     m["ior"] = ior
+    m["sigma"] = sigma
+    m["kd_texture"] = kd_texture
+    m["ks_texture"] = ks_texture
     return m
+
+
+def texture_struct(t: "Texture"):
+    """(bg_texture, keep-alive array) for a Texture."""
+    from ._abi import bg_texture
+    c = bg_texture()
+    c.kind, c.wrap, c.mapping = t.kind, t.wrap, t.mapping
+    keep = None
+    if t.kind == 0:
+        keep = np.ascontiguousarray(t.rgb, np.float32)
+        c.height, c.width = keep.shape[0], keep.shape[1]
+        c.rgb = keep.ctypes.data
+    c.uv_scale[:] = t.uv_scale
+    c.uv_delta[:] = t.uv_delta
+    c.world_to_texture[:] = np.asarray(t.world_to_texture, np.float32).reshape(12)
+    c.vs[:] = t.vs
+    c.vt[:] = t.vt
+    c.ds, c.dt = t.ds, t.dt
+    return c, keep
+
+
+def triangle_runs(sd: "SceneData"):
+    """Consecutive triangle ranges [a, b) sharing (has normals, flags): one mesh call each."""
+    n = sd.ntri
+    has_n = np.zeros(n, bool)
+    if sd.tri_normals is not None:
+        has_n[:] = True if sd.tri_normal_mask is None else np.asarray(sd.tri_normal_mask, bool)
+    fl = np.zeros(n, np.uint32) if sd.tri_flags is None else np.asarray(sd.tri_flags, np.uint32)
+    runs, a = [], 0
+    for i in range(1, n + 1):
+        if i == n or has_n[i] != has_n[a] or fl[i] != fl[a]:
+            runs.append((a, i, bool(has_n[a]), int(fl[a])))
+            a = i
+    return runs
+
+
+@dataclass
+class Texture:
+    """bg_texture: an image (rgb of shape (h, w, 3), power-of-two sizes) or a uv texture, with its
+    mapping (src/base/texture.rs)."""
+    kind: int = 0                     # 0 image, 1 uv
+    rgb: np.ndarray | None = None     # (h, w, 3) float32, row 0 at the top
+    wrap: int = 0                     # 0 repeat, 1 black, 2 clamp
+    mapping: int = 0                  # 0 uv, 1 spherical, 2 cylindrical, 3 planar
+    uv_scale: tuple = (1.0, 1.0)
+    uv_delta: tuple = (0.0, 0.0)
+    world_to_texture: np.ndarray = field(default_factory=lambda: np.eye(3, 4, dtype=np.float32))
+    vs: tuple = (1.0, 0.0, 0.0)
+    vt: tuple = (0.0, 1.0, 0.0)
+    ds: float = 0.0
+    dt: float = 0.0
 
 
 def rotation(axis, deg: float) -> np.ndarray:
@@ -108,6 +163,13 @@ class SceneData:
     lights: np.ndarray                   # (nlights,) LIGHT_DT
     camera: Camera | None = None
     quadrics: np.ndarray = field(default_factory=lambda: np.zeros(0, QUADRIC_DT))
+    # triangle mesh attributes: (ntri, 9) vertex normals with a (ntri,) mask of the triangles that
+    # have them (None = all), (ntri, 6) uvs, (ntri,) BG_TRI_* flags; None = absent
+    tri_normals: np.ndarray | None = None
+    tri_normal_mask: np.ndarray | None = None
+    tri_uvs: np.ndarray | None = None
+    tri_flags: np.ndarray | None = None
+    textures: list = field(default_factory=list)
     spp: int = 16
     max_depth: int = 5
     rr_threshold: float = 1.0
@@ -188,6 +250,87 @@ def quadric_box(width: int = 64, height: int = 64, spp: int = 8, max_depth: int 
     sd.spheres = np.zeros(0, SPHERE_DT)
     sd.name = "quadric_box"
     return sd
+
+
+def checker_image(n: int = 64, tiles: int = 8, seed: int = 0) -> np.ndarray:
+    """(n, n, 3) float32 test image: a two-colour checkerboard with per-texel noise in blue."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:n, 0:n]
+    c = ((x * tiles // n + y * tiles // n) % 2).astype(np.float32)
+    img = np.empty((n, n, 3), np.float32)
+    img[..., 0] = 0.15 + 0.7 * c
+    img[..., 1] = 0.2 + 0.5 * (1.0 - c)
+    img[..., 2] = (0.2 + 0.4 * rng.random((n, n))).astype(np.float32)
+    return img
+
+
+def textured_room(width: int = 64, height: int = 64, spp: int = 16, max_depth: int = 5) -> SceneData:
+    """The Cornell box with every texture and mesh-attribute path of the reference in use:
+    back wall: image texture (64^2, repeat) through UVMapping2D with per-vertex uvs, scaled so the
+    MIPMap filters between levels; floor: UVTexture through PlanarMapping2D on an Oren-Nayar matte
+    (sigma 25); left wall: plastic whose ks is an image through CylindricalMapping2D (black wrap);
+    diffuse sphere: image through SphericalMapping2D (clamp); a smooth-shaded icosphere (vertex
+    normals, Oren-Nayar sigma 40); ceiling triangles marked as mirrored by their transform; a
+    one-sided ceiling light of two triangles wound upward, one turned toward the room by
+    reverse_orientation and one by its vertex normals."""
+    sd = cornell(width, height, spp, max_depth)
+    nwall = 10
+    mats = list(sd.materials)  # 0 grey, 1 red, 2 green, 3 conductor, 4 light (black)
+    m_back = len(mats); mats.append(material(MATTE, kd_texture=1))
+    m_floor = len(mats); mats.append(material(MATTE, kd=(0.7, 0.7, 0.7), kd_texture=2, sigma=25.0))
+    m_sph = len(mats); mats.append(material(MATTE, kd_texture=3))
+    m_left = len(mats); mats.append(material(PLASTIC, kd=(0.35, 0.1, 0.08), ks_texture=4, roughness=0.3))
+    m_ico = len(mats); mats.append(material(MATTE, kd=(0.6, 0.6, 0.5), sigma=40.0))
+    tex = [Texture(kind=0, rgb=checker_image(64, 8, 1), wrap=0, mapping=0, uv_scale=(6.0, 6.0), uv_delta=(0.1, 0.0)),
+           Texture(kind=1, mapping=3, vs=(1.5, 0.0, 0.0), vt=(0.0, 0.0, 1.5), ds=0.25, dt=0.5),
+           Texture(kind=0, rgb=checker_image(32, 4, 2), wrap=2, mapping=1,
+                   world_to_texture=translation((0.4, 0.7, 0.3))[:3].astype(np.float32)),
+           Texture(kind=0, rgb=checker_image(16, 2, 3), wrap=1, mapping=2,
+                   world_to_texture=(rotation((1, 0, 0), 90) @ translation((1.0, 0.0, 0.0)))[:3].astype(np.float32))]
+    tri = sd.tri[:nwall].copy()
+    tmat = sd.tri_mat[:nwall].copy()
+    tmat[0:2] = m_floor
+    tmat[4:6] = m_back
+    tmat[6:8] = m_left
+    uvs = np.tile(np.array([0, 0, 1, 0, 1, 1], np.float32), (nwall, 1))
+    for t in (4, 5):  # back wall: uv = position x, y mapped to [0, 1]
+        p = tri[t].reshape(3, 3)
+        uvs[t] = np.stack([(p[:, 0] + 1) / 2, (p[:, 1] + 1) / 2], axis=1).reshape(6)
+    flags = np.zeros(nwall, np.uint8)
+    flags[2:4] = 2  # ceiling: transform swaps handedness
+    # smooth icosphere (level 2) with vertex normals
+    v, f = icosphere(2)
+    c, r = np.array([0.35, -0.55, -0.35]), 0.3
+    ico = (c + r * v[f]).reshape(-1, 9).astype(np.float32)
+    ico_n = v[f].reshape(-1, 9).astype(np.float32)
+    nico = len(ico)
+    # one-sided light: two triangles with upward winding
+    a, b, cc, d = (-0.25, 0.999, -0.25), (0.25, 0.999, -0.25), (0.25, 0.999, 0.25), (-0.25, 0.999, 0.25)
+    lq = _quad(a, b, cc, d, (0, 1, 0))
+    ln = np.tile(np.array([0.1, -1.0, 0.05], np.float32), 3)
+    all_tri = np.concatenate([tri, ico, lq]).astype(np.float32)
+    n = len(all_tri)
+    normals = np.zeros((n, 9), np.float32)
+    normals[nwall:nwall + nico] = ico_n
+    normals[n - 1] = ln
+    mask = np.zeros(n, bool)
+    mask[nwall:nwall + nico] = True
+    mask[n - 1] = True
+    all_uv = np.tile(np.array([0, 0, 1, 0, 1, 1], np.float32), (n, 1))
+    all_uv[:nwall] = uvs
+    all_flags = np.zeros(n, np.uint8)
+    all_flags[:nwall] = flags
+    all_flags[n - 2] = 1  # reverse_orientation
+    tmat_all = np.concatenate([tmat, np.full(nico, m_ico, np.uint32), np.full(2, 4, np.uint32)]).astype(np.uint32)
+    tl = np.full(n, -1, np.int32)
+    tl[n - 2:] = 0
+    lights = sd.lights.copy()
+    lights[0]["two_sided"] = 0
+    sph = sd.spheres.copy()
+    sph[0]["material_id"] = m_sph
+    return SceneData(all_tri, tmat_all, tl, sph, np.stack(mats), lights, sd.camera, spp=spp, max_depth=max_depth,
+                     rr_threshold=1.0, name="textured_room", tri_normals=normals, tri_normal_mask=mask,
+                     tri_uvs=all_uv, tri_flags=all_flags, textures=tex)
 
 
 def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:

@@ -64,7 +64,44 @@ typedef struct bg_material {
     float eta[3];             /* conductor eta                                             */
     float k[3];               /* conductor absorption k                                    */
     float ior;                /* dielectric index of refraction (outside medium is 1.0)    */
+    float sigma;              /* matte: Oren-Nayar sigma in degrees (0 = Lambertian,
+                                 src/materials/matte.rs:28-37; clamped to [0, 90])         */
+    uint32_t kd_texture;      /* 0: constant kd; t > 0: texture t - 1 (matte, plastic)     */
+    uint32_t ks_texture;      /* 0: constant ks; t > 0: texture t - 1 (plastic)            */
 } bg_material;
+
+/* Textures (Texture<RGBSpectrum>, src/base/texture.rs:10-12).  IMAGE = ImageTexture with its
+ * MIPMap (src/textures/image.rs, src/base/mipmap.rs): `rgb` holds width*height*3 linear floats,
+ * rows top to bottom (Image::pixels); width and height must be powers of two (the reference
+ * resamples other sizes with the image crate's Lanczos3 filter but keeps the original
+ * resolution, src/io/image.rs:28-44).  UV = UVTexture (src/textures/uv.rs): (s - floor s,
+ * t - floor t, 0).  The mapping turns a shading point into (s, t) (src/base/texture.rs:22-144):
+ * UV = UVMapping2D{uv_scale, uv_delta}; SPHERICAL / CYLINDRICAL = {world_to_texture} (row-major
+ * 3x4 affine); PLANAR = PlanarMapping2D{vs, vt, ds, dt}. */
+typedef enum bg_texture_kind { BG_TEXTURE_IMAGE = 0, BG_TEXTURE_UV = 1 } bg_texture_kind;
+typedef enum bg_wrap_mode { BG_WRAP_REPEAT = 0, BG_WRAP_BLACK = 1, BG_WRAP_CLAMP = 2 } bg_wrap_mode;
+typedef enum bg_mapping_kind {
+    BG_MAPPING_UV = 0,
+    BG_MAPPING_SPHERICAL = 1,
+    BG_MAPPING_CYLINDRICAL = 2,
+    BG_MAPPING_PLANAR = 3
+} bg_mapping_kind;
+typedef struct bg_texture {
+    uint32_t kind;            /* bg_texture_kind                                           */
+    uint32_t wrap;            /* bg_wrap_mode (ImageWrapMode, src/io/image.rs:11-16)       */
+    uint32_t width, height;   /* image size (IMAGE)                                        */
+    const float* rgb;         /* IMAGE texels; copied by bg_scene_add_texture              */
+    uint32_t mapping;         /* bg_mapping_kind                                           */
+    float uv_scale[2];        /* UV mapping: u_scale, v_scale                              */
+    float uv_delta[2];        /* UV mapping: u_delta, v_delta                              */
+    float world_to_texture[12];
+    float vs[3], vt[3];       /* PLANAR mapping axes                                       */
+    float ds, dt;             /* PLANAR mapping offsets                                    */
+} bg_texture;
+
+/* Triangle mesh attributes (TriangleMesh, src/shapes/triangle.rs:17-90; TriangleOptions:40-45). */
+#define BG_TRI_REVERSE_ORIENTATION 1u /* TriangleOptions::reverse_orientation                   */
+#define BG_TRI_SWAPS_HANDEDNESS 2u    /* the mesh transform swaps handedness (det < 0)          */
 
 /* DiffuseAreaLight options (src/lights/diffuse.rs:26-30). */
 typedef struct bg_area_light {
@@ -126,7 +163,24 @@ typedef struct bg_render_opts {
     uint64_t seed;         /* counter-RNG key                                             */
     uint32_t first_sample; /* index of the first sample (progressive rendering)           */
     uint32_t flags;        /* BG_RENDER_* bits                                            */
+    uint32_t integrator;   /* bg_integrator (0 = PathIntegrator)                          */
+    uint32_t light_strategy; /* direct lighting: bg_light_strategy                        */
 } bg_render_opts;
+
+/* The SamplerIntegrator behind bg_render.  PATH = PathIntegrator (src/integrators/path.rs);
+ * WHITTED = WhittedIntegrator (src/integrators/whitted.rs): emission, every light sampled once
+ * without MIS, specular reflection / transmission recursion; DIRECT = DirectLightingIntegrator
+ * (src/integrators/direct.rs) with LightStrategy UniformSampleAll (every light, MIS) or
+ * UniformSampleOne, and the same specular recursion.  Whitted and direct lighting evaluate the
+ * BSDF without multiple lobes (the dielectric becomes SpecularReflection + SpecularTransmission
+ * in PBRT mode; the reference's own materials have no specular lobes, so its recursion never
+ * fires) and accept max_depth <= 30. */
+typedef enum bg_integrator {
+    BG_INTEGRATOR_PATH = 0,
+    BG_INTEGRATOR_WHITTED = 1,
+    BG_INTEGRATOR_DIRECT = 2
+} bg_integrator;
+typedef enum bg_light_strategy { BG_LIGHT_UNIFORM_ALL = 0, BG_LIGHT_UNIFORM_ONE = 1 } bg_light_strategy;
 
 #define BG_RENDER_ACCUMULATE 1u  /* add to the film accumulated by earlier calls          */
 #define BG_RENDER_NO_READBACK 2u /* leave the film on the device (rgb_out may be NULL)    */
@@ -209,7 +263,17 @@ bg_status bg_scene_add_area_light(bg_scene* scene, const bg_area_light* l, uint3
  * material, area_light} (src/primitives/geometric.rs:15-20). */
 bg_status bg_scene_add_triangles(bg_scene* scene, const float* xyz, size_t ntri,
                                  const uint32_t* material_ids, const int32_t* light_ids);
+/* As bg_scene_add_triangles with the mesh's per-vertex data: normals (9 floats per triangle:
+ * world-space shading normals of p0 p1 p2, or NULL) and uvs (6 floats per triangle, or NULL for
+ * the default (0,0) (1,0) (1,1)), and BG_TRI_* flags for every triangle of the call.  An emitting
+ * triangle's vertex normals must all lie on one side of it (BG_ERR_UNSUPPORTED at commit). */
+bg_status bg_scene_add_triangle_mesh(bg_scene* scene, const float* xyz, size_t ntri,
+                                     const uint32_t* material_ids, const int32_t* light_ids,
+                                     const float* normals, const float* uvs, uint32_t flags);
 bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t n);
+/* Appends a texture; materials refer to it as *id + 1.  Image texels are copied and their MIPMap
+ * pyramid is built here (Image::generate_pyramid, src/io/image.rs:55-114). */
+bg_status bg_scene_add_texture(bg_scene* scene, const bg_texture* tex, uint32_t* id);
 /* Appends n cylinders / disks / cones (GeometricPrimitive{Cylinder|Disk|Cone, material}). */
 bg_status bg_scene_add_quadrics(bg_scene* scene, const bg_quadric* quadrics, size_t n);
 /* Builds the BVH on the host, uploads scene and BVH to the device. */
@@ -258,14 +322,24 @@ bg_status bg_memcpy_d2h(bg_ctx* ctx, void* h_dst, const void* d_src, size_t byte
 
 /* ---- scene and film I/O ----------------------------------------------------------------------
  * OBJ::read (src/io/obj.rs:16-123): a triangle mesh from a Wavefront OBJ file, positions through
- * object_to_world (row-major 3x4, NULL = identity).  Triangles are the consecutive triples of all
- * face indices in file order (as the reference; polygons are not fanned); normals and texture
- * coordinates are index-checked but not used (device triangles carry geometric normals).  Files
- * the reference would panic on give BG_ERR_INVALID (message in err / bg_last_error).
- * bg_obj_read parses into tri_out (9 floats per triangle, up to max_tri; *ntri = all triangles);
- * bg_scene_add_obj adds the mesh to a scene with one material and light id. */
+ * object_to_world (row-major 3x4, NULL = identity) and vertex normals through its inverse
+ * transpose.  Triangles are the consecutive triples of all face indices in file order (as the
+ * reference; polygons are not fanned); the i-th face vertex takes the i-th normal / texture index
+ * of the file.  Files the reference would panic on give BG_ERR_INVALID (message in err /
+ * bg_last_error).  bg_obj_read parses the positions into tri_out (9 floats per triangle, up to
+ * max_tri; *ntri = all triangles); bg_obj_read_mesh also the vertex normals (9 floats per
+ * triangle) and uvs (6 floats per triangle) when the file has them, and the mesh's BG_TRI_*
+ * flags; bg_scene_add_obj adds the mesh, attributes included, with one material and light id. */
+typedef struct bg_obj_info {
+    size_t ntri;
+    uint32_t has_normals;
+    uint32_t has_uvs;
+    uint32_t flags; /* BG_TRI_SWAPS_HANDEDNESS when the transform mirrors */
+} bg_obj_info;
 bg_status bg_obj_read(const char* path, const float* object_to_world, float* tri_out, size_t max_tri, size_t* ntri,
                       char* err, size_t err_len);
+bg_status bg_obj_read_mesh(const char* path, const float* object_to_world, float* tri_out, float* normal_out,
+                           float* uv_out, size_t max_tri, bg_obj_info* info, char* err, size_t err_len);
 bg_status bg_scene_add_obj(bg_scene* scene, const char* path, const float* object_to_world, uint32_t material_id,
                            int32_t light_id, size_t* ntri);
 /* Film::write_image (src/base/film.rs:156-202, src/io/image.rs:47-53), headless: an uncompressed

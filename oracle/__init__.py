@@ -38,6 +38,9 @@ def lib() -> C.CDLL:
         L.orc_scene_create.argtypes = [P, C.c_int64, P, P, P, C.c_int64, P, C.c_int32, P, C.c_int32, C.c_int32,
                                        P, C.c_int64]
         L.orc_scene_destroy.argtypes = [P]
+        L.orc_scene_set_tri_attrs.argtypes = [P, P, P, P, P]
+        L.orc_scene_add_texture.restype = C.c_int32
+        L.orc_scene_add_texture.argtypes = [P, P]
         L.orc_bvh_nodes.restype = C.c_int64
         L.orc_bvh_nodes.argtypes = [P]
         L.orc_num_lights.restype = C.c_int64
@@ -88,6 +91,16 @@ class OracleScene:
         self.h = lib().orc_scene_create(_ptr(t), sd.ntri, _ptr(tm), _ptr(tl), _ptr(sp) if len(sp) else None,
                                         sd.nsph, _ptr(ma), len(ma), _ptr(li) if len(li) else None, len(li),
                                         int(fixed_bvh), _ptr(qu) if len(qu) else None, len(qu))
+        if sd.tri_normals is not None or sd.tri_uvs is not None or sd.tri_flags is not None:
+            nrm = None if sd.tri_normals is None else np.ascontiguousarray(sd.tri_normals, np.float32)
+            mask = None if sd.tri_normal_mask is None else np.ascontiguousarray(sd.tri_normal_mask, np.uint8)
+            uvs = None if sd.tri_uvs is None else np.ascontiguousarray(sd.tri_uvs, np.float32)
+            fl = None if sd.tri_flags is None else np.ascontiguousarray(sd.tri_flags, np.uint8)
+            self._keep += [nrm, mask, uvs, fl]
+            lib().orc_scene_set_tri_attrs(self.h, _ptr(nrm), _ptr(mask), _ptr(uvs), _ptr(fl))
+        for tex in sd.textures:
+            tt, keep = S.texture_struct(tex)
+            lib().orc_scene_add_texture(self.h, C.byref(tt))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -112,7 +125,8 @@ class OracleScene:
 
     def render(self, mode: int, spp: int | None = None, seed: int = 0, first_sample: int = 0,
                rows: tuple[int, int, int] | None = None, threads: int = 0, count_traversal: bool = False,
-               camera: S.Camera | None = None, max_depth: int | None = None):
+               camera: S.Camera | None = None, max_depth: int | None = None, integrator: int = 0,
+               light_strategy: int = 0):
         """Returns dict(rgb, sum, sumsq, counters).  rows = (y0, y1, ystep) restricts the rendered rows."""
         sd = self.sd
         cam = camera or sd.camera
@@ -125,6 +139,7 @@ class OracleScene:
         o.seed = seed
         o.first_sample = first_sample
         o.flags = 0
+        o.integrator, o.light_strategy = integrator, light_strategy
         W, H = cam.width, cam.height
         rgb = np.zeros((H, W, 3), np.float32)
         s1 = np.zeros((H, W, 3), np.float64)

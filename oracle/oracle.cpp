@@ -279,6 +279,11 @@ struct Interaction {  // src/base/interaction.rs:47-54 (+ the SurfaceInteraction
     bool surface = false;
     V3 dpdu, shading_n, shading_dpdu;
     int prim = -1;
+    // SurfaceInteraction parameterisation (interaction.rs:18-45)
+    float uv[2] = {0.0f, 0.0f};
+    V3 dpdv, dndu, dndv, shading_dndu, shading_dndv;
+    V3 dpdx, dpdy;
+    float dudx = 0.0f, dvdx = 0.0f, dudy = 0.0f, dvdy = 0.0f;
 };
 // src/geometries/point3.rs:31-49
 static V3 offset_ray_origin(V3 p, V3 perr, V3 n, V3 w) {
@@ -317,6 +322,21 @@ struct Quadric {
     float radius, inner, z_min, z_max, height, phi_max;
     uint32_t mat;
 };
+enum : uint8_t { TA_REVERSE = 1, TA_SWAPS = 2, TA_NORMALS = 4 };
+// ImageTexture / UVTexture + TextureMapping2D (src/textures/{image,uv}.rs, src/base/texture.rs)
+// with the MIPMap pyramid (src/base/mipmap.rs, src/io/image.rs:55-159).
+struct Image {
+    int w = 0, h = 0;
+    std::vector<float> px;  // Image::pixels, 3 per texel
+};
+struct Texture {
+    uint32_t kind = 0, wrap = 0, mapping = 0;
+    float su = 1, sv = 1, du = 0, dv = 0;
+    Transform w2t;
+    V3 vs, vt;
+    float ds = 0, dt = 0;
+    std::vector<Image> pyramid;
+};
 struct Scene {
     std::vector<V3> pos;  // 3 per triangle (TriangleMesh::position, triangle.rs:17-22)
     int64_t ntri = 0, nsph = 0, nquad = 0;
@@ -328,6 +348,11 @@ struct Scene {
     std::vector<bg_material> mats;
     std::vector<bg_area_light> emis;
     std::vector<int64_t> light_prims;  // Scene::lights (one DiffuseAreaLight per emitting shape)
+    // TriangleMesh vertex attributes (triangle.rs:17-22) and TriangleOptions flags, per triangle
+    std::vector<V3> tri_n;             // 3 per triangle (meaningful where TA_NORMALS is set)
+    std::vector<float> tri_uv;         // 6 per triangle; empty: Triangle::get_uvs defaults
+    std::vector<uint8_t> tri_flags;    // TA_* bits; empty: none
+    std::vector<struct Texture> tex;
     // BVH (src/accelerators/bvh.rs:20-31)
     struct Node {
         Bounds3 b;
@@ -400,8 +425,13 @@ static bool tri_intersect(const Scene& s, int64_t i, const Ray& ray, float* t_hi
     float delta_t = 3.0f * (gamma(3.0f) * max_e * max_zt + delta_e * max_zt + delta_z * max_e) *
                     std::fabs(inv_det);
     if (t <= delta_t) return false;
-    // partial derivatives with the default uvs (0,0),(1,0),(1,1) (:107-117, :241-268)
-    const float uv[3][2] = {{0.0f, 0.0f}, {1.0f, 0.0f}, {1.0f, 1.0f}};
+    // uvs (Triangle::get_uvs, :107-117) and partial derivatives (:241-268)
+    float uv[3][2] = {{0.0f, 0.0f}, {1.0f, 0.0f}, {1.0f, 1.0f}};
+    if (!s.tri_uv.empty())
+        for (int k = 0; k < 3; ++k) {
+            uv[k][0] = s.tri_uv[6 * i + 2 * k];
+            uv[k][1] = s.tri_uv[6 * i + 2 * k + 1];
+        }
     float duv02[2] = {uv[0][0] - uv[2][0], uv[0][1] - uv[2][1]};
     float duv12[2] = {uv[1][0] - uv[2][0], uv[1][1] - uv[2][1]};
     V3 dp02 = p0 - p2, dp12 = p1 - p2;
@@ -419,23 +449,62 @@ static bool tri_intersect(const Scene& s, int64_t i, const Ray& ray, float* t_hi
         coordinate_system(normalize(ng), &dpdu, &dpdv);
     }
     if (test_only) return true;
-    // error bounds and hit point (:270-278)
+    const uint8_t fl = s.tri_flags.empty() ? 0 : s.tri_flags[i];
+    const bool reverse = (fl & TA_REVERSE) != 0, swaps = (fl & TA_SWAPS) != 0;
+    // error bounds, hit point and uv (:270-278)
     float xs = std::fabs(b0 * p0.x) + std::fabs(b1 * p1.x) + std::fabs(b2 * p2.x);
     float ys = std::fabs(b0 * p0.y) + std::fabs(b1 * p1.y) + std::fabs(b2 * p2.y);
     float zs = std::fabs(b0 * p0.z) + std::fabs(b1 * p1.z) + std::fabs(b2 * p2.z);
     V3 perr = gamma(7.0f) * V3(xs, ys, zs);
     V3 phit = b0 * p0 + b1 * p1 + b2 * p2;
-    // Interaction::new (interaction.rs:57-100), normal overridden (:299-307)
+    // Interaction::new (interaction.rs:57-100): shading geometry starts as the true geometry
     it->p = phit;
     it->p_err = perr;
     it->time = ray.time;
     it->wo = -ray.d;
     it->surface = true;
+    it->uv[0] = b0 * uv[0][0] + b1 * uv[1][0] + b2 * uv[2][0];
+    it->uv[1] = b0 * uv[0][1] + b1 * uv[1][1] + b2 * uv[2][1];
     it->dpdu = dpdu;
+    it->dpdv = dpdv;
+    it->dndu = it->dndv = V3(0, 0, 0);
     it->shading_dpdu = dpdu;
+    it->shading_dndu = it->shading_dndv = V3(0, 0, 0);
+    // the normal is overridden with the winding normal (:299-307)
     V3 nn = normalize(cross(dp02, dp12));
+    if (reverse ^ swaps) nn = -nn;
     it->n = nn;
     it->shading_n = nn;
+    if (fl & TA_NORMALS) {  // shading geometry from the vertex normals (:309-398)
+        const V3 n0 = s.tri_n[3 * i], n1 = s.tri_n[3 * i + 1], n2 = s.tri_n[3 * i + 2];
+        V3 sn = b0 * n0 + b1 * n1 + b2 * n2;
+        sn = length_squared(sn) > 0.0f ? normalize(sn) : it->n;
+        V3 st = normalize(it->dpdu);
+        V3 sb = cross(st, sn);
+        if (length_squared(sb) > 0.0f) {
+            sb = normalize(sb);
+            st = cross(sb, sn);
+        } else {
+            coordinate_system(sn, &st, &sb);
+        }
+        V3 dndu(0, 0, 0), dndv(0, 0, 0);
+        V3 dn1 = n0 - n2, dn2 = n1 - n2;
+        if (degenerate_uv) {
+            V3 dn = cross(n2 - n0, n1 - n0);
+            if (length_squared(dn) != 0.0f) coordinate_system(dn, &dndu, &dndv);
+        } else {
+            float invd = 1.0f / uvdet;
+            dndu = (duv12[1] * dn1 - duv02[1] * dn2) * invd;
+            dndv = (-duv12[0] * dn1 + duv02[0] * dn2) * invd;
+        }
+        if (reverse) sb = -sb;
+        // Interaction::set_shading_geometry(st, sb, dndu, dndv, true) (interaction.rs:145-168)
+        it->shading_n = normalize(cross(st, sb));
+        it->n = face_forward(it->n, it->shading_n);
+        it->shading_dpdu = st;
+        it->shading_dndu = dndu;
+        it->shading_dndv = dndv;
+    }
     *t_hit = t;
     return true;
 }
@@ -453,10 +522,27 @@ static Interaction tri_sample(const Scene& s, int64_t i, float u0, float u1, flo
     Interaction r;
     r.p = b0 * p0 + b1 * p1 + b2 * p2;
     r.n = normalize(cross(p1 - p0, p2 - p0));
+    const uint8_t fl = s.tri_flags.empty() ? 0 : s.tri_flags[i];
+    if (fl & TA_NORMALS) {  // face the interpolated vertex normal (:534-545)
+        V3 shaded = b0 * s.tri_n[3 * i] + b1 * s.tri_n[3 * i + 1] + (1.0f - b0 - b1) * s.tri_n[3 * i + 2];
+        r.n = face_forward(r.n, shaded);
+    } else if (((fl & TA_REVERSE) != 0) ^ ((fl & TA_SWAPS) != 0)) {
+        r.n = r.n * -1.0f;
+    }
     V3 pabs = vabs(b0 * p0) + vabs(b1 * p1) + vabs(b2 * p2);
     r.p_err = gamma(6.0f) * pabs;
     *pdf = 1.0f / tri_area(s, i);
     return r;
+}
+
+// Weingarten equations (sphere.rs:191-204; the same in cylinder.rs and cone.rs)
+static void fundamental_forms(V3 dpdu, V3 dpdv, V3 d2pduu, V3 d2pduv, V3 d2pdvv, V3* dndu, V3* dndv) {
+    float E = dot(dpdu, dpdu), F = dot(dpdu, dpdv), G = dot(dpdv, dpdv);
+    V3 N = normalize(cross(dpdu, dpdv));
+    float e = dot(N, d2pduu), f = dot(N, d2pduv), g = dot(N, d2pdvv);
+    float inv = 1.0f / (E * G - F * F);
+    *dndu = (f * F - e * G) * inv * dpdu + (e * F - f * E) * inv * dpdv;
+    *dndv = (g * F - f * G) * inv * dpdu + (f * F - g * E) * inv * dpdv;
 }
 
 // ---------------------------------------------------------------- Sphere (sphere.rs)
@@ -507,6 +593,12 @@ static bool sphere_intersect(const Sphere& sp, const Ray& r_world, float* t_hit,
     float cos_phi = ph.x * inv_zr, sin_phi = ph.y * inv_zr;
     V3 dpdu(-sp.phi_max * ph.y, sp.phi_max * ph.x, 0.0f);
     V3 dpdv = (sp.theta_max - sp.theta_min) * V3(ph.z * cos_phi, ph.z * sin_phi, -sp.radius * std::sin(theta));
+    // normal derivatives from the fundamental forms (:178-204)
+    V3 d2pduu = -sp.phi_max * sp.phi_max * V3(ph.x, ph.y, 0.0f);
+    V3 d2pduv = (sp.theta_max - sp.theta_min) * ph.z * sp.phi_max * V3(-sin_phi, cos_phi, 0.0f);
+    V3 d2pdvv = -(sp.theta_max - sp.theta_min) * (sp.theta_max - sp.theta_min) * ph;
+    V3 dndu, dndv;
+    fundamental_forms(dpdu, dpdv, d2pduu, d2pduv, d2pdvv, &dndu, &dndv);
     V3 perr = gamma(5.0f) * vabs(ph);  // :209
     // Interaction::new then Interaction::transform(object_to_world) (interaction.rs:268-300)
     V3 n = normalize(cross(dpdu, dpdv));
@@ -517,9 +609,16 @@ static bool sphere_intersect(const Sphere& sp, const Ray& r_world, float* t_hit,
     it->wo = xf_vec(sp.o2w, -ray.d);
     it->n = normalize(xf_normal(sp.o2w, n));
     it->surface = true;
+    it->uv[0] = phi / sp.phi_max;
+    it->uv[1] = (theta - sp.theta_min) / (sp.theta_max - sp.theta_min);
     it->dpdu = xf_vec(sp.o2w, dpdu);
+    it->dpdv = xf_vec(sp.o2w, dpdv);
+    it->dndu = xf_normal(sp.o2w, dndu);
+    it->dndv = xf_normal(sp.o2w, dndv);
     it->shading_n = face_forward(normalize(xf_normal(sp.o2w, n)), it->n);
     it->shading_dpdu = xf_vec(sp.o2w, dpdu);
+    it->shading_dndu = it->dndu;
+    it->shading_dndv = it->dndv;
     *t_hit = tsh.v;
     return true;
 }
@@ -529,7 +628,8 @@ inline float absolute_error(const EFloat& e) {  // efloat.rs absolute_error
     return next_float_up(rmax(std::fabs(e.high - e.v), std::fabs(e.v - e.low)));
 }
 // Interaction::new (interaction.rs:57-100) + Interaction::transform (interaction.rs:268-300)
-static void quadric_interaction(const Quadric& q, V3 ph, V3 perr, const Ray& ray, V3 dpdu, V3 dpdv, Interaction* it) {
+static void quadric_interaction(const Quadric& q, V3 ph, V3 perr, const Ray& ray, V3 dpdu, V3 dpdv, float u,
+                                float v, V3 dndu, V3 dndv, Interaction* it) {
     V3 n = normalize(cross(dpdu, dpdv));
     if (q.reverse ^ q.swaps) n = n * -1.0f;
     V3 abs_err;
@@ -539,9 +639,16 @@ static void quadric_interaction(const Quadric& q, V3 ph, V3 perr, const Ray& ray
     it->wo = xf_vec(q.o2w, -ray.d);
     it->n = normalize(xf_normal(q.o2w, n));
     it->surface = true;
+    it->uv[0] = u;
+    it->uv[1] = v;
     it->dpdu = xf_vec(q.o2w, dpdu);
+    it->dpdv = xf_vec(q.o2w, dpdv);
+    it->dndu = xf_normal(q.o2w, dndu);
+    it->dndv = xf_normal(q.o2w, dndv);
     it->shading_n = face_forward(normalize(xf_normal(q.o2w, n)), it->n);
     it->shading_dpdu = it->dpdu;
+    it->shading_dndu = it->dndu;
+    it->shading_dndv = it->dndv;
 }
 static bool quadric_intersect(const Quadric& q, const Ray& rw, float* t_hit, Interaction* it, bool test_only) {
     V3 oe, de;
@@ -558,10 +665,11 @@ static bool quadric_intersect(const Quadric& q, const Ray& rw, float* t_hit, Int
         if (phi > q.phi_max) return false;
         if (test_only) return true;
         float rh = std::sqrt(dist);
+        float u = phi / q.phi_max, v = (q.radius - rh) / (q.radius - q.inner);  // disk.rs:106-113
         V3 dpdu(-q.phi_max * ph.y, q.phi_max * ph.x, 0.0f);
         V3 dpdv = V3(ph.x, ph.y, 0.0f) * (q.inner - q.radius) / rh;
         ph.z = q.height;
-        quadric_interaction(q, ph, V3(0, 0, 0), ray, dpdu, dpdv, it);
+        quadric_interaction(q, ph, V3(0, 0, 0), ray, dpdu, dpdv, u, v, V3(0, 0, 0), V3(0, 0, 0), it);
         *t_hit = tsh;
         return true;
     }
@@ -613,17 +721,23 @@ static bool quadric_intersect(const Quadric& q, const Ray& rw, float* t_hit, Int
         if (clipped(ph, phi)) return false;
     }
     if (test_only) return true;
-    V3 dpdu(-q.phi_max * ph.y, q.phi_max * ph.x, 0.0f), dpdv, perr;
-    if (q.kind == 0) {
+    V3 dpdu(-q.phi_max * ph.y, q.phi_max * ph.x, 0.0f), dpdv, perr, d2pduv(0, 0, 0);
+    V3 d2pduu = -q.phi_max * q.phi_max * V3(ph.x, ph.y, 0.0f);
+    float u = phi / q.phi_max, v;
+    if (q.kind == 0) {  // cylinder.rs:149-181
+        v = (ph.z - q.z_min) / (q.z_max - q.z_min);
         dpdv = V3(0.0f, 0.0f, q.z_max - q.z_min);
         perr = gamma(3.0f) * vabs(V3(ph.x, ph.y, 0.0f));
-    } else {
-        float v = ph.z / q.height;
+    } else {  // cone.rs:141-194
+        v = ph.z / q.height;
         dpdv = V3(-ph.x / (1.0f - v), -ph.y / (1.0f - v), q.height);
+        d2pduv = q.phi_max / (1.0f - v) * V3(ph.y, -ph.x, 0.0f);
         EFloat px = ox + tsh * dx, py = oy + tsh * dy, pz = oz + tsh * dz;
         perr = V3(absolute_error(px), absolute_error(py), absolute_error(pz));
     }
-    quadric_interaction(q, ph, perr, ray, dpdu, dpdv, it);
+    V3 dndu, dndv;
+    fundamental_forms(dpdu, dpdv, d2pduu, d2pduv, V3(0, 0, 0), &dndu, &dndv);
+    quadric_interaction(q, ph, perr, ray, dpdu, dpdv, u, v, dndu, dndv, it);
     *t_hit = tsh.v;
     return true;
 }
@@ -1001,7 +1115,7 @@ static float roughness_to_alpha(float r) {  // microfacet.rs:45-53
     return 1.62142f + 0.819955f * x + 0.1734f * x * x + 0.0171201f * x * x * x + 0.000640711f * x * x * x * x;
 }
 
-enum BxKind { LAMBERT, MF_REFL, FRESNEL_SPEC };
+enum BxKind { LAMBERT, MF_REFL, FRESNEL_SPEC, OREN_NAYAR, SPEC_REFL, SPEC_TRANS };
 struct Bxdf {
     BxKind kind;
     uint8_t type;
@@ -1011,6 +1125,7 @@ struct Bxdf {
     RGB c_eta_i, c_eta_t, c_k;
     float d_eta_i = 1, d_eta_t = 1;
     float eta_a = 1, eta_b = 1;
+    float on_a = 1, on_b = 0;  // OrenNayer A, B
     bool matches(uint8_t f) const { return (type & f) == type; }
 };
 struct BxSample {
@@ -1022,6 +1137,23 @@ struct BxSample {
 static RGB bx_f(const Bxdf& b, V3 wo, V3 wi, Mode mode) {
     switch (b.kind) {
         case LAMBERT: return b.r * (1.0f / PI);  // lambertian.rs:42-45
+        case OREN_NAYAR: {                       // oren_nayer.rs:34-60
+            float sin_i = sin_theta(wi), sin_o = sin_theta(wo);
+            float max_cos = 0.0f;
+            if (sin_i > 1e-4f && sin_o > 1e-4f) {
+                float d_cos = cos_phi(wi) * cos_phi(wo) + sin_phi(wi) * sin_phi(wo);
+                max_cos = rmax(0.0f, d_cos);
+            }
+            float sin_alpha, tan_beta;
+            if (abs_cos_theta(wi) > abs_cos_theta(wo)) {
+                sin_alpha = sin_o;
+                tan_beta = sin_i / abs_cos_theta(wi);
+            } else {
+                sin_alpha = sin_i;
+                tan_beta = sin_o / abs_cos_theta(wo);
+            }
+            return b.r * (1.0f / PI) * (b.on_a + b.on_b * max_cos * sin_alpha * tan_beta);
+        }
         case MF_REFL: {                          // bxdfs/microfacet.rs:69-94
             float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
             V3 wh = wi + wo;
@@ -1038,7 +1170,8 @@ static RGB bx_f(const Bxdf& b, V3 wo, V3 wi, Mode mode) {
 }
 static float bx_pdf(const Bxdf& b, V3 wo, V3 wi, Mode mode) {
     switch (b.kind) {
-        case LAMBERT: return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;  // bxdf.rs:72-78
+        case LAMBERT:
+        case OREN_NAYAR: return same_hemisphere(wo, wi) ? abs_cos_theta(wi) * (1.0f / PI) : 0.0f;  // bxdf.rs:72-78
         case MF_REFL: {  // bxdfs/microfacet.rs:142-147
             if (!same_hemisphere(wo, wi)) return 0.0f;
             V3 wh = normalize(wo + wi);
@@ -1065,6 +1198,26 @@ static V3 cosine_sample_hemisphere(float u0, float u1) {  // sampling.rs:238-242
 static BxSample bx_sample(const Bxdf& b, V3 wo, float u0, float u1, Mode mode) {
     BxSample s;
     switch (b.kind) {
+        case SPEC_REFL: {  // specular.rs:57-66
+            V3 wi(-wo.x, -wo.y, wo.z);
+            s.wi = wi;
+            s.f = RGB(fresnel_dielectric(cos_theta(wi), b.eta_a, b.eta_b, mode)) * b.r / abs_cos_theta(wi);
+            s.pdf = 1.0f;
+            return s;
+        }
+        case SPEC_TRANS: {  // specular.rs:82-113
+            bool entering = cos_theta(wo) > 0.0f;
+            float ei = entering ? b.eta_a : b.eta_b, et = entering ? b.eta_b : b.eta_a;
+            V3 wi;
+            if (!refract(wo, face_forward(V3(0, 0, 1), wo), ei / et, &wi)) return s;
+            RGB f = b.t * (RGB(1.0f) - RGB(fresnel_dielectric(cos_theta(wi), b.eta_a, b.eta_b, mode)));
+            f = f * ((ei * ei) / (et * et));
+            s.wi = wi;
+            s.f = f / abs_cos_theta(wi);
+            s.pdf = 1.0f;
+            return s;
+        }
+        case OREN_NAYAR:
         case LAMBERT: {  // default BxDF::sample (bxdf.rs:33-45)
             V3 wi = cosine_sample_hemisphere(u0, u1);
             if (wo.z < 0.0f) wi.z *= -1.0f;
@@ -1184,9 +1337,192 @@ struct BSDF {  // src/base/bsdf.rs
         return s;
     }
 };
+// ---------------------------------------------------------------- ray differentials + textures
+struct RayDifferential {  // ray.rs:7-13
+    bool has = false;
+    V3 rxo, ryo, rxd, ryd;
+};
+// solve_linear_system_2x2 (src/base/math.rs:52-68)
+static bool solve_2x2(const float a[2][2], const float b[2], float* x0, float* x1) {
+    float det = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+    if (std::fabs(det) < 1e-10f) return false;
+    *x0 = (a[1][1] * b[0] - a[0][1] * b[1]) / det;
+    *x1 = (a[0][0] * b[1] - a[1][0] * b[0]) / det;
+    if (std::isnan(*x0) || std::isnan(*x1)) return false;
+    return true;
+}
+// Interaction::compute_differentials (interaction.rs:184-250)
+static void compute_differentials(Interaction* it, const RayDifferential& rd) {
+    it->dudx = it->dvdx = it->dudy = it->dvdy = 0.0f;
+    it->dpdx = it->dpdy = V3(0, 0, 0);
+    if (!rd.has) return;
+    float d = dot(it->n, it->p);
+    float tx = -(dot(it->n, rd.rxo) - d) / dot(it->n, rd.rxd);
+    if (std::isinf(tx) || std::isnan(tx)) return;
+    V3 px = rd.rxo + tx * rd.rxd;
+    float ty = -(dot(it->n, rd.ryo) - d) / dot(it->n, rd.ryd);
+    if (std::isinf(ty) || std::isnan(ty)) return;
+    V3 py = rd.ryo + ty * rd.ryd;
+    it->dpdx = px - it->p;
+    it->dpdy = py - it->p;
+    const V3& n = it->n;
+    int dim[2];
+    if (std::fabs(n.x) > std::fabs(n.y) && std::fabs(n.x) > std::fabs(n.z)) { dim[0] = 1; dim[1] = 2; }
+    else if (std::fabs(n.y) > std::fabs(n.z)) { dim[0] = 0; dim[1] = 2; }
+    else { dim[0] = 0; dim[1] = 1; }
+    float a[2][2] = {{it->dpdu[dim[0]], it->dpdv[dim[0]]}, {it->dpdu[dim[1]], it->dpdv[dim[1]]}};
+    float bx[2] = {px[dim[0]] - it->p[dim[0]], px[dim[1]] - it->p[dim[1]]};
+    float by[2] = {py[dim[0]] - it->p[dim[0]], py[dim[1]] - it->p[dim[1]]};
+    if (!solve_2x2(a, bx, &it->dudx, &it->dvdx)) it->dudx = it->dvdx = 0.0f;
+    if (!solve_2x2(a, by, &it->dudy, &it->dvdy)) it->dudy = it->dvdy = 0.0f;
+}
+
+// `as i32` (saturating, NaN -> 0)
+static int32_t to_i32(float f) {
+    if (std::isnan(f)) return 0;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)f;
+}
+static int32_t modulo_i32(int32_t a, int32_t b) {  // math.rs:43-50
+    int32_t r = a - (a / b) * b;
+    return r < 0 ? r + b : r;
+}
+// Image::get_channel with remap_pixel (image.rs:130-159)
+static float image_channel(const Image& im, int32_t x, int32_t y, int c, uint32_t wrap) {
+    int32_t p[2] = {x, y};
+    const int32_t res[2] = {im.w, im.h};
+    for (int k = 0; k < 2; ++k) {
+        if (p[k] >= 0 && p[k] < res[k]) continue;
+        if (wrap == BG_WRAP_REPEAT) p[k] = modulo_i32(p[k], res[k]);
+        else if (wrap == BG_WRAP_CLAMP) p[k] = p[k] < 0 ? 0 : (p[k] > res[k] - 1 ? res[k] - 1 : p[k]);
+        else return 0.0f;
+    }
+    return im.px[3 * ((size_t)p[1] * im.w + p[0]) + c];
+}
+static RGB mip_texel(const Texture& t, size_t level, int32_t x, int32_t y) {  // mipmap.rs:175-182
+    const Image& im = t.pyramid[level];
+    return RGB(image_channel(im, x, y, 0, t.wrap), image_channel(im, x, y, 1, t.wrap),
+               image_channel(im, x, y, 2, t.wrap));
+}
+static RGB mip_triangle(const Texture& t, size_t level, float st0, float st1) {  // mipmap.rs:156-173
+    level = std::min(level, t.pyramid.size() - 1);
+    const Image& im = t.pyramid[level];
+    float sx = st0 * (float)im.w - 0.5f, sy = st1 * (float)im.h - 0.5f;
+    float ds = sx - std::floor(sx), dt = sy - std::floor(sy);
+    int32_t s0 = to_i32(std::floor(sx)), t0 = to_i32(std::floor(sy));
+    int32_t s1 = (int32_t)((uint32_t)s0 + 1u), t1 = (int32_t)((uint32_t)t0 + 1u);
+    return (1.0f - ds) * (1.0f - dt) * mip_texel(t, level, s0, t0) + (1.0f - ds) * dt * mip_texel(t, level, s0, t1) +
+           ds * (1.0f - dt) * mip_texel(t, level, s1, t0) + ds * dt * mip_texel(t, level, s1, t1);
+}
+// MIPMap::filter / trilinear_filter (mipmap.rs:103-128)
+static RGB mip_filter(const Texture& t, float st0, float st1, const float d0[2], const float d1[2]) {
+    float width = rmax(rmax(std::fabs(d0[0]), std::fabs(d0[1])), rmax(std::fabs(d1[0]), std::fabs(d1[1])));
+    const float top = (float)(t.pyramid.size() - 1);
+    float level = top + std::log2(rmax(width, 1e-8f));
+    if (level < 0.0f) return mip_triangle(t, 0, st0, st1);
+    if (level >= top) return mip_texel(t, t.pyramid.size() - 1, 0, 0);
+    size_t il = (size_t)std::floor(level);
+    float f = level - std::floor(level);
+    return (1.0f - f) * mip_triangle(t, il, st0, st1) + f * mip_triangle(t, il + 1, st0, st1);
+}
+// SphericalMapping2D::sphere / CylindricalMapping2D::cylinder (texture.rs:48-62)
+static void map_sphere(const Texture& t, V3 p, Mode mode, float st[2]) {
+    V3 v = normalize(xf_point(t.w2t, p) - V3(0, 0, 0));
+    float theta = std::acos(rclamp(v.z, -1.0f, 1.0f));
+    float phi = std::atan2(v.y, v.x);
+    if (phi < 0.0f) phi = phi + 2.0f * PI;
+    st[0] = theta * (1.0f / PI);
+    st[1] = phi * (mode == REF ? (1.0f / PI) : (1.0f / (2.0f * PI)));  // REF: phi / pi as written
+}
+static void map_cylinder(const Texture& t, V3 p, float st[2]) {
+    V3 v = normalize(xf_point(t.w2t, p) - V3(0, 0, 0));
+    st[0] = (PI + std::atan2(v.y, v.x)) * (1.0f / (2.0f * PI));
+    st[1] = v.z;
+}
+// TextureMapping2D::map (texture.rs:64-144)
+static void tex_map(const Texture& t, const Interaction& it, Mode mode, float st[2], float dx[2], float dy[2]) {
+    if (t.mapping == BG_MAPPING_UV) {
+        dx[0] = t.su * it.dudx;
+        dx[1] = t.sv * it.dvdx;
+        dy[0] = t.su * it.dudy;
+        dy[1] = t.sv * it.dvdy;
+        st[0] = t.su * it.uv[0] + t.du;
+        st[1] = t.sv * it.uv[1] + t.dv;
+        return;
+    }
+    if (t.mapping == BG_MAPPING_PLANAR) {
+        dx[0] = dot(it.dpdx, t.vs);
+        dx[1] = dot(it.dpdx, t.vt);
+        dy[0] = dot(it.dpdy, t.vs);
+        dy[1] = dot(it.dpdy, t.vt);
+        st[0] = t.ds + dot(it.p, t.vs);
+        st[1] = t.dt + dot(it.p, t.vt);
+        return;
+    }
+    const float DELTA = 0.1f;
+    auto at = [&](V3 p, float o[2]) {
+        if (t.mapping == BG_MAPPING_SPHERICAL) map_sphere(t, p, mode, o);
+        else map_cylinder(t, p, o);
+    };
+    float sx[2], sy[2];
+    at(it.p, st);
+    at(it.p + DELTA * it.dpdx, sx);
+    at(it.p + DELTA * it.dpdy, sy);
+    for (int k = 0; k < 2; ++k) {
+        dx[k] = (sx[k] - st[k]) / DELTA;
+        dy[k] = (sy[k] - st[k]) / DELTA;
+    }
+    for (float* d : {dx, dy}) {  // mapping discontinuity of the second coordinate
+        if (d[1] > 0.5f) d[1] = 1.0f - d[1];
+        else if (d[1] < -0.5f) d[1] = -(d[1] + 1.0f);
+    }
+}
+// Texture<RGBSpectrum>::evaluate (image.rs:35-42, uv.rs:8-15)
+static RGB tex_eval(const Scene& s, uint32_t id, const Interaction& it, Mode mode) {
+    const Texture& t = s.tex[id];
+    float st[2], dx[2], dy[2];
+    tex_map(t, it, mode, st, dx, dy);
+    if (t.kind == BG_TEXTURE_UV) return RGB(st[0] - std::floor(st[0]), st[1] - std::floor(st[1]), 0.0f);
+    return mip_filter(t, st[0], st[1], dx, dy);
+}
+// Image::generate_pyramid (image.rs:55-114)
+static std::vector<Image> generate_pyramid(Image img) {
+    size_t levels = 1;
+    for (int m = std::max(img.w, img.h); m > 1; m >>= 1) ++levels;
+    std::vector<Image> pyr;
+    pyr.push_back(std::move(img));
+    for (size_t i = 1; i < levels; ++i) {
+        const Image& last = pyr[i - 1];
+        Image next;
+        next.w = std::max(last.w / 2, 1);
+        next.h = std::max(last.h / 2, 1);
+        next.px.assign((size_t)next.w * next.h * 3, 0.0f);
+        size_t deltas[4] = {0, 3, 3 * (size_t)last.w, 3 * ((size_t)last.w + 1)};
+        if (last.w == 1) { deltas[1] = 0; deltas[3] -= 3; }
+        if (last.h == 1) { deltas[2] = 0; deltas[3] -= 3 * (size_t)last.w; }
+        for (int y = 0; y < next.h; ++y) {
+            size_t src = 3 * ((size_t)(2 * y) * last.w), dst = 3 * ((size_t)y * next.w);
+            for (int x = 0; x < next.w; ++x) {
+                for (int c = 0; c < 3; ++c) {
+                    next.px[dst] = (last.px[src] + last.px[src + deltas[1]] + last.px[src + deltas[2]] +
+                                    last.px[src + deltas[3]]) * 0.25f;
+                    ++src;
+                    ++dst;
+                }
+                src += 3;
+            }
+        }
+        pyr.push_back(std::move(next));
+    }
+    return pyr;
+}
+
 // Material::compute_scattering_functions (materials/matte.rs:19-41, plastic.rs:65-95 and the
 // composed conductor / dielectric)
-static BSDF make_bsdf(const Scene& s, const Interaction& it) {
+// `it` carries the differentials (compute_differentials) that textures read; multi_lobe =
+// allow_multiple_lobes (false for the Whitted and direct-lighting integrators).
+static BSDF make_bsdf(const Scene& s, const Interaction& it, Mode mode = PBRT, bool multi_lobe = true) {
     const bg_material& m = s.mats[it.prim < s.ntri ? s.tri_mat[it.prim]
                                   : it.prim < s.ntri + s.nsph ? s.sph[it.prim - s.ntri].mat
                                                               : s.quads[it.prim - s.ntri - s.nsph].mat];
@@ -1195,20 +1531,31 @@ static BSDF make_bsdf(const Scene& s, const Interaction& it) {
     b.ng = it.n;
     b.ss = normalize(it.shading_dpdu);
     b.ts = cross(b.ns, b.ss);
-    auto clamp0 = [](const float* c) {
-        return RGB(rclamp(c[0], 0.0f, INFINITY), rclamp(c[1], 0.0f, INFINITY), rclamp(c[2], 0.0f, INFINITY));
+    auto clamp0 = [](RGB c) {  // RGBSpectrum::clamp(0, inf)
+        return RGB(rclamp(c.c[0], 0.0f, INFINITY), rclamp(c.c[1], 0.0f, INFINITY), rclamp(c.c[2], 0.0f, INFINITY));
+    };
+    auto texture = [&](uint32_t id, const float* constant) {  // ConstantTexture or textures[id - 1]
+        return id ? tex_eval(s, id - 1, it, mode) : RGB(constant[0], constant[1], constant[2]);
     };
     if (m.type == BG_MAT_MATTE || m.type == BG_MAT_PLASTIC) {
-        RGB kd = clamp0(m.kd);
+        RGB kd = clamp0(texture(m.kd_texture, m.kd));
         if (!kd.is_black()) {
             Bxdf l;
             l.kind = LAMBERT;
             l.type = BSDF_REFLECTION | BSDF_DIFFUSE;
             l.r = kd;
+            float sigma = m.type == BG_MAT_MATTE ? rclamp(m.sigma, 0.0f, 90.0f) : 0.0f;
+            if (sigma != 0.0f) {  // OrenNayer::new (oren_nayer.rs:20-30)
+                l.kind = OREN_NAYAR;
+                float rad = sigma * (PI / 180.0f);
+                float s2 = rad * rad;
+                l.on_a = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
+                l.on_b = 0.45f * s2 / (s2 + 0.09f);
+            }
             b.bx[b.n++] = l;
         }
         if (m.type == BG_MAT_PLASTIC) {
-            RGB ks = clamp0(m.ks);
+            RGB ks = clamp0(texture(m.ks_texture, m.ks));
             if (!ks.is_black()) {
                 float rough = m.roughness;
                 if (m.remap_roughness) rough = roughness_to_alpha(rough);
@@ -1234,7 +1581,7 @@ static BSDF make_bsdf(const Scene& s, const Interaction& it) {
         g.c_eta_t = RGB(m.eta[0], m.eta[1], m.eta[2]);
         g.c_k = RGB(m.k[0], m.k[1], m.k[2]);
         b.bx[b.n++] = g;
-    } else {  // dielectric
+    } else if (mode == REF || multi_lobe) {  // dielectric
         b.eta = m.ior;
         Bxdf d;
         d.kind = FRESNEL_SPEC;
@@ -1244,6 +1591,22 @@ static BSDF make_bsdf(const Scene& s, const Interaction& it) {
         d.eta_a = 1.0f;
         d.eta_b = m.ior;
         b.bx[b.n++] = d;
+    } else {  // dielectric without multiple lobes: SpecularReflection + SpecularTransmission
+        b.eta = m.ior;
+        Bxdf r;
+        r.kind = SPEC_REFL;
+        r.type = BSDF_REFLECTION | BSDF_SPECULAR;
+        r.r = RGB(1.0f);
+        r.eta_a = 1.0f;
+        r.eta_b = m.ior;
+        b.bx[b.n++] = r;
+        Bxdf t;
+        t.kind = SPEC_TRANS;
+        t.type = BSDF_TRANSMISSION | BSDF_SPECULAR;
+        t.t = RGB(1.0f);
+        t.eta_a = 1.0f;
+        t.eta_b = m.ior;
+        b.bx[b.n++] = t;
     }
     return b;
 }
@@ -1396,12 +1759,34 @@ struct Camera {
         r.time = (1.0f - tu) * 0.0f + tu * 1.0f;  // lerp(time, 0, 1), math.rs:7-9
         return xf_ray(camera_to_world, r);
     }
+    // The same ray's differentials (perspective.rs:141-170), moved to world space by Ray::transform
+    // (ray.rs:66-73) and scaled by Ray::scale_differentials (ray.rs:41-48).
+    RayDifferential differentials(float fx, float fy, const Ray& world_ray, float scale) const {
+        V3 origin = xf_point(raster_to_camera, V3(0, 0, 0));
+        V3 dx_camera = xf_point(raster_to_camera, V3(1, 0, 0)) - origin;  // perspective.rs:86-89
+        V3 dy_camera = xf_point(raster_to_camera, V3(0, 1, 0)) - origin;
+        V3 cp = xf_point(raster_to_camera, V3(fx, fy, 0.0f));
+        RayDifferential d;
+        d.has = true;
+        d.rxo = xf_point(camera_to_world, V3(0, 0, 0));
+        d.ryo = d.rxo;
+        d.rxd = xf_vec(camera_to_world, normalize(cp + dx_camera));
+        d.ryd = xf_vec(camera_to_world, normalize(cp + dy_camera));
+        const V3 o = world_ray.o, dd = world_ray.d;
+        d.rxo = o + (d.rxo - o) * scale;
+        d.ryo = o + (d.ryo - o) * scale;
+        d.rxd = dd + (d.rxd - dd) * scale;
+        d.ryd = dd + (d.ryd - dd) * scale;
+        return d;
+    }
 };
 
 // ---------------------------------------------------------------- PathIntegrator::radiance
 // src/integrators/path.rs:51-146
+// rd0: the camera ray's differentials; REF keeps them on every bounce (the ray never re-spawns,
+// F1), PBRT has them at the first hit only (spawn_ray drops them).
 static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max_depth, float rr_threshold,
-                    Mode mode, Counters* cnt) {
+                    Mode mode, Counters* cnt, const RayDifferential& rd0 = RayDifferential()) {
     RGB out, beta(1.0f);
     bool specular_bounce = false;
     float eta_scale = 1.0f;
@@ -1415,7 +1800,8 @@ static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max
             // lights' radiance(ray) is zero for area lights (light.rs:31-33)
         }
         if (!hit || bounces >= max_depth) break;
-        BSDF bsdf = make_bsdf(s, it);
+        compute_differentials(&it, (mode == REF || bounces == 0) ? rd0 : RayDifferential());
+        BSDF bsdf = make_bsdf(s, it, mode);
         const uint32_t base = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounces;
         if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && !s.light_prims.empty()) {
             // uniform_sample_one_light (integrator.rs:309-328)
@@ -1446,6 +1832,97 @@ static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max
             beta = beta / (1.0f - q);
         }
         bounces += 1;
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------- Whitted / DirectLighting
+// WhittedIntegrator::radiance (src/integrators/whitted.rs:147-201), DirectLightingIntegrator::
+// radiance (src/integrators/direct.rs:65-111) with specular_reflect / specular_transmit and
+// uniform_sample_all_lights (src/base/integrator.rs:143-307), recursively as the reference.
+// kind 1 Whitted, 2 direct with UniformSampleAll, 3 direct with UniformSampleOne.  Random numbers:
+// stream = node - 1 of the ray tree (root 1, reflection 2k, transmission 2k + 1); dims 8-9
+// reflection, 10-11 transmission, lights from 12 (Whitted 12 + 2j; all lights 12 + 4j u_light,
+// +2 u_scattering; one light: pick 12, u_light 13-14, u_scattering 15-16).
+static RGB tree_radiance(const Scene& s, Ray ray, const RayDifferential& rd, CounterRng rng, uint32_t node,
+                         uint32_t depth, uint32_t max_depth, int kind, Mode mode, Counters* cnt) {
+    RGB out;
+    Interaction it;
+    if (cnt) cnt->ext_rays++;
+    if (!scene_intersect(s, ray, &it, cnt)) return out;  // area lights: Light::radiance is zero
+    rng.stream = node - 1;
+    compute_differentials(&it, rd);
+    BSDF bsdf = make_bsdf(s, it, mode, false);  // allow_multiple_lobes = false
+    out = out + emitted_radiance(s, it, it.wo);
+    const size_t nl = s.light_prims.size();
+    if (nl > 0) {
+        if (kind == 1) {
+            for (size_t j = 0; j < nl; ++j) {
+                LightSample ls = light_sample_point(s, s.light_prims[j], it, rng.u(12 + 2 * (uint32_t)j),
+                                                    rng.u(13 + 2 * (uint32_t)j), mode);
+                if (ls.radiance.is_black() || ls.pdf == 0.0f) continue;
+                RGB f = bsdf.f(it.wo, ls.wi, BSDF_ALL, mode);
+                if (!ls.vis || f.is_black()) continue;
+                if (cnt) cnt->shadow_rays++;
+                if (scene_intersect_test(s, spawn_ray_to_it(ls.p0, ls.p1), cnt)) continue;
+                out = out + f * ls.radiance * abs_dot(ls.wi, it.shading_n) / ls.pdf;
+            }
+        } else if (kind == 2) {
+            for (size_t j = 0; j < nl; ++j) {
+                const uint32_t b = 12 + 4 * (uint32_t)j;
+                RGB d = estimate_direct(s, it, bsdf, s.light_prims[j], rng.u(b + 2), rng.u(b + 3), rng.u(b), rng.u(b + 1),
+                                        mode, cnt);
+                out = out + d / 1.0f;
+            }
+        } else {
+            float count = (float)nl;
+            size_t li = (size_t)rmin(rng.u(12) * count, count - 1.0f);
+            RGB d = estimate_direct(s, it, bsdf, s.light_prims[li], rng.u(15), rng.u(16), rng.u(13), rng.u(14), mode, cnt);
+            out = out + d / (1.0f / count);
+        }
+    }
+    if (depth + 1 < max_depth) {
+        for (int k = 0; k < 2; ++k) {  // specular_reflect, then specular_transmit
+            const uint8_t type = k == 0 ? (BSDF_REFLECTION | BSDF_SPECULAR) : (BSDF_TRANSMISSION | BSDF_SPECULAR);
+            BxSample bs = bsdf.sample(it.wo, rng.u(8 + 2 * k), rng.u(9 + 2 * k), type, mode);
+            V3 normal = it.shading_n;
+            if (!(bs.pdf > 0.0f) || bs.f.is_black() || abs_dot(bs.wi, normal) == 0.0f) continue;
+            Ray child = spawn_ray(it, bs.wi, mode);
+            RayDifferential crd;
+            if (rd.has) {
+                crd.has = true;
+                crd.rxo = it.p + it.dpdx;
+                crd.ryo = it.p + it.dpdy;
+                V3 dndx = it.shading_dndu * it.dudx + it.shading_dndv * it.dvdx;
+                V3 dndy = it.shading_dndu * it.dudy + it.shading_dndv * it.dvdy;
+                const V3 wo = it.wo;
+                if (k == 0) {
+                    V3 dwodx = -rd.rxd - wo, dwody = -rd.ryd - wo;
+                    float ddndx = dot(dwodx, normal) + dot(wo, dndx);
+                    float ddndy = dot(dwody, normal) + dot(wo, dndy);
+                    crd.rxd = bs.wi - dwodx + 2.0f * (dot(wo, normal) * dndx + ddndx * normal);
+                    crd.ryd = bs.wi - dwody + 2.0f * (dot(wo, normal) * dndy + ddndy * normal);
+                } else {
+                    float eta = 1.0f / bsdf.eta;
+                    if (dot(wo, normal) < 0.0f) {
+                        eta = 1.0f / eta;
+                        normal = -normal;
+                        dndx = -dndx;
+                        dndy = -dndy;
+                    }
+                    V3 dwodx = -rd.rxd - wo, dwody = -rd.ryd - wo;
+                    float ddndx = dot(dwodx, normal) + dot(wo, dndx);
+                    float ddndy = dot(dwody, normal) + dot(wo, dndy);
+                    float mu = eta * dot(wo, normal) - abs_dot(bs.wi, normal);
+                    float dmudx = (eta - (eta * eta * dot(wo, normal)) / abs_dot(bs.wi, normal)) * ddndx;
+                    float dmudy = (eta - (eta * eta * dot(wo, normal)) / abs_dot(bs.wi, normal)) * ddndy;
+                    crd.rxd = bs.wi - eta * dwodx + (mu * dndx + dmudx * normal);
+                    crd.ryd = bs.wi - eta * dwody + (mu * dndy + dmudy * normal);
+                }
+            }
+            RGB li = tree_radiance(s, child, crd, rng, 2 * node + (uint32_t)k, depth + 1, max_depth, kind, mode, cnt);
+            out = out + bs.f * li * abs_dot(bs.wi, normal) / bs.pdf;
+        }
     }
     return out;
 }
@@ -1526,6 +2003,60 @@ void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_m
     return s;
 }
 
+// Triangle mesh attributes (bg_scene_add_triangle_mesh): normals 9 floats per triangle (rows
+// where has_normals[i] == 0 are ignored), uvs 6 floats per triangle or NULL, flags per triangle
+// (BG_TRI_* bits) or NULL.
+void orc_scene_set_tri_attrs(void* p, const float* normals, const uint8_t* has_normals, const float* uvs,
+                             const uint8_t* flags) {
+    Scene& s = *(Scene*)p;
+    s.tri_flags.assign(s.ntri, 0);
+    s.tri_n.assign(3 * s.ntri, V3(0, 0, 0));
+    for (int64_t i = 0; i < s.ntri; ++i) {
+        uint8_t f = 0;
+        if (flags) {
+            if (flags[i] & BG_TRI_REVERSE_ORIENTATION) f |= TA_REVERSE;
+            if (flags[i] & BG_TRI_SWAPS_HANDEDNESS) f |= TA_SWAPS;
+        }
+        if (normals && (!has_normals || has_normals[i])) {
+            f |= TA_NORMALS;
+            for (int k = 0; k < 3; ++k)
+                s.tri_n[3 * i + k] = V3(normals[9 * i + 3 * k], normals[9 * i + 3 * k + 1], normals[9 * i + 3 * k + 2]);
+        }
+        s.tri_flags[i] = f;
+    }
+    if (uvs) s.tri_uv.assign(uvs, uvs + 6 * s.ntri);
+    else s.tri_uv.clear();
+}
+// Appends a texture (bg_texture); materials refer to it as (returned id) + 1.
+int32_t orc_scene_add_texture(void* p, const bg_texture* t) {
+    Scene& s = *(Scene*)p;
+    Texture x;
+    x.kind = t->kind;
+    x.wrap = t->wrap;
+    x.mapping = t->mapping;
+    x.su = t->uv_scale[0];
+    x.sv = t->uv_scale[1];
+    x.du = t->uv_delta[0];
+    x.dv = t->uv_delta[1];
+    x.w2t.m = Mat4::identity();
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) x.w2t.m.m[r][c] = t->world_to_texture[4 * r + c];
+    x.w2t.mi = mat_inverse(x.w2t.m);
+    x.vs = V3(t->vs[0], t->vs[1], t->vs[2]);
+    x.vt = V3(t->vt[0], t->vt[1], t->vt[2]);
+    x.ds = t->ds;
+    x.dt = t->dt;
+    if (t->kind == BG_TEXTURE_IMAGE) {
+        Image img;
+        img.w = (int)t->width;
+        img.h = (int)t->height;
+        img.px.assign(t->rgb, t->rgb + (size_t)t->width * t->height * 3);
+        x.pyramid = generate_pyramid(std::move(img));
+    }
+    s.tex.push_back(std::move(x));
+    return (int32_t)s.tex.size() - 1;
+}
+
 void orc_scene_destroy(void* p) { delete (Scene*)p; }
 int64_t orc_bvh_nodes(void* p) { return (int64_t)((Scene*)p)->nodes.size(); }
 int64_t orc_num_lights(void* p) { return (int64_t)((Scene*)p)->light_prims.size(); }
@@ -1593,6 +2124,9 @@ int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_
     if (ystep < 1) ystep = 1;
     Mode mode = opts->mode == BG_MODE_PBRT ? PBRT : REF;
     int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    const float diff_scale = 1.0f / std::sqrt((float)(opts->spp ? opts->spp : 1u));  // integrator.rs:80-82
+    const int tree_kind = opts->integrator == BG_INTEGRATOR_WHITTED ? 1
+                          : (opts->light_strategy == BG_LIGHT_UNIFORM_ALL ? 2 : 3);
     const int TILE = 16;
     int ntx = (W + TILE - 1) / TILE, nty = (H + TILE - 1) / TILE;
     std::vector<Counters> cs(nt);
@@ -1613,9 +2147,13 @@ int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_
                         rng.sample = opts->first_sample + si;
                         float fx = (float)x + rng.u(DIM_FILM), fy = (float)y + rng.u(DIM_FILM + 1);
                         Ray ray = camera.generate_ray(fx, fy, rng.u(DIM_TIME));
+                        RayDifferential rd;
+                        if (!s.tex.empty()) rd = camera.differentials(fx, fy, ray, diff_scale);
                         Counters local;
-                        RGB L = radiance(s, ray, rng, opts->max_depth, opts->rr_threshold, mode,
-                                         cnt ? cnt : (counters ? &local : nullptr));
+                        Counters* cc = cnt ? cnt : (counters ? &local : nullptr);
+                        RGB L = opts->integrator == BG_INTEGRATOR_PATH
+                                    ? radiance(s, ray, rng, opts->max_depth, opts->rr_threshold, mode, cc, rd)
+                                    : tree_radiance(s, ray, rd, rng, 1, 0, opts->max_depth, tree_kind, mode, cc);
                         if (!cnt && counters) { cbase.ext_rays += local.ext_rays; cbase.shadow_rays += local.shadow_rays; }
                         // sanity checks (integrator.rs:91-117)
                         if (L.is_nan() || L.y() < -1e-5f || std::isinf(L.y())) {
@@ -1678,7 +2216,7 @@ void orc_bsdf_sample(const bg_material* m, const float* wo, float u0, float u1, 
     it.n = V3(0, 0, 1);
     it.shading_n = it.n;
     it.shading_dpdu = V3(1, 0, 0);
-    BSDF b = make_bsdf(s, it);
+    BSDF b = make_bsdf(s, it, mode == 1 ? PBRT : REF);
     BxSample bs = b.sample(V3(wo[0], wo[1], wo[2]), u0, u1, BSDF_ALL, mode == 1 ? PBRT : REF);
     out[0] = bs.f.c[0]; out[1] = bs.f.c[1]; out[2] = bs.f.c[2]; out[3] = bs.pdf;
     out[4] = bs.wi.x; out[5] = bs.wi.y; out[6] = bs.wi.z; out[7] = (float)bs.sampled_type;
@@ -1693,8 +2231,8 @@ void orc_bsdf_eval(const bg_material* m, const float* wo, const float* wi, int32
     it.n = V3(0, 0, 1);
     it.shading_n = it.n;
     it.shading_dpdu = V3(1, 0, 0);
-    BSDF b = make_bsdf(s, it);
     Mode md = mode == 1 ? PBRT : REF;
+    BSDF b = make_bsdf(s, it, md);
     RGB f = b.f(V3(wo[0], wo[1], wo[2]), V3(wi[0], wi[1], wi[2]), BSDF_ALL, md);
     out[0] = f.c[0]; out[1] = f.c[1]; out[2] = f.c[2];
     out[3] = b.pdf(V3(wo[0], wo[1], wo[2]), V3(wi[0], wi[1], wi[2]), BSDF_ALL, md);

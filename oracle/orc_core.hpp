@@ -179,8 +179,9 @@ inline void philox4x32_10(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
 struct CounterRng {
     uint32_t pixel = 0, sample = 0;
     uint64_t seed = 0;
+    uint32_t stream = 0;  // the Whitted / direct-lighting integrators: node id - 1 of the ray tree
     float u(uint32_t dim) const {
-        uint32_t ctr[4] = {sample, dim >> 2, (uint32_t)(seed >> 32), 0x626F6E73u};
+        uint32_t ctr[4] = {sample, dim >> 2, (uint32_t)(seed >> 32), 0x626F6E73u ^ stream};
         philox4x32_10(ctr, pixel, (uint32_t)seed);
         uint32_t x = ctr[dim & 3];
         return (float)(x >> 9) * 0x1p-23f;

@@ -65,6 +65,51 @@ def test_obj_errors(tmp_path, text):
         bio.read_obj(p)
 
 
+MESH_TEXT = """v 0 0 0
+v 1 0 0
+v 1 1 0
+v 0 1 0
+vt 0 0
+vt 1 0
+vt 1 1
+vt 0 1
+vn 0 0 1
+vn 0.1 0 0.9
+vn 0 0.2 0.8
+f 1/1/1 2/2/2 3/3/3
+f 1/1/1 3/3/3 4/4/2
+"""
+
+
+@pytest.mark.parametrize("xf", [None, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32),
+                                np.array([[0.5, 0.1, 0, 1], [0, 2, 0.3, -1], [0.25, 0, 1, 3]], np.float32),
+                                np.array([[-1, 0, 0, 0.3], [0, 1, 0, 0.1], [0, 0, 1, -0.7]], np.float32)])
+def test_obj_mesh_attributes_match_reference_rules(tmp_path, xf):
+    p = _write(tmp_path, MESH_TEXT)
+    tri, nrm, uv, flags = bio.read_obj_mesh(p, xf)
+    wt, wn, wuv, wswap = OO.read_obj_mesh(p, xf)
+    np.testing.assert_array_equal(tri, wt)
+    np.testing.assert_array_equal(nrm, wn)
+    np.testing.assert_array_equal(uv, wuv)
+    assert uv[1].tolist() == [0, 0, 1, 1, 0, 1]
+    assert bool(flags & 2) == wswap == (xf is not None and np.linalg.det(xf[:, :3]) < 0)
+
+
+def test_obj_mesh_positions_only(tmp_path):
+    p = _write(tmp_path, "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    tri, nrm, uv, flags = bio.read_obj_mesh(p)
+    assert tri.shape == (1, 9) and nrm is None and uv is None and flags == 0
+
+
+def test_obj_mesh_rejects_partial_normals(tmp_path):
+    # the second face has no normals: the reference would index past its normal list
+    p = _write(tmp_path, "v 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//1 3//1\nf 1 2 3\n")
+    with pytest.raises(ValueError):
+        OO.read_obj_mesh(p)
+    with pytest.raises(ValueError, match="normal indices"):
+        bio.read_obj_mesh(p)
+
+
 def test_obj_missing_file(tmp_path):
     with pytest.raises(ValueError, match="cannot open"):
         bio.read_obj(tmp_path / "nope.obj")
