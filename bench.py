@@ -351,8 +351,8 @@ def run_integrators(args):
     """The Whitted (`--workload whitted`) and direct-lighting (`--workload direct`, UniformSampleAll:
     every light with MIS) integrators on the production scene: value = device Msamples/s over K
     frames (L2 flushed), e2e through bg_render with the film read back; CPU restatement of the same
-    integrator (oracle/) on all host cores.  One thread per sample walks its ray tree over the
-    8-wide BVH (bonsai_gb300/csrc/bg_integrators.cu)."""
+    integrator (oracle/) on all host cores.  The ray trees run as a breadth-first wavefront over
+    the 8-wide BVH (bonsai_gb300/csrc/bg_tree_wave.cu)."""
     import ctypes as C
     from bonsai_gb300 import _abi as A
     from bonsai_gb300 import gpu as G
@@ -375,12 +375,13 @@ def run_integrators(args):
     barrier(dist)
     ctx.synchronize()
     clocks.start()
-    dev_ms, launches = 0.0, 0
+    dev_ms, launches, rays = 0.0, 0, 0
     for k in range(args.steps):
         ctx.flush_l2()
         r = pi.render(scene, readback=False, first_sample=k * sd.spp)
         dev_ms += r.stats.device_ms
         launches += r.stats.launches
+        rays += r.stats.extension_rays + r.stats.shadow_rays
         if r.stats.error_word:
             raise RuntimeError(f"device error word {r.stats.error_word}")
     ctx.synchronize()
@@ -409,15 +410,17 @@ def run_integrators(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
-        "config": config_of(sd, args.small) | {"integrator": name},
+        "config": config_of(sd, args.small) | {"integrator": name, "graph": "no (a host check per wave)",
+                                               "waves": "breadth-first ray-tree wavefront, <= 2M samples per wave"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
                 "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
-                     "kernel": "k_tree<false, 8> (one thread per sample)", "peak_source": peak_kind,
-                     "note": "no per-ray counters in the per-sample kernel; the path workload carries the roofline"},
+                     "kernel": "k_tw_extend<8> / k_tw_shadow<8> (tree wavefront)", "peak_source": peak_kind,
+                     "note": "the traversal kernels are those of the path workload, which carries the roofline"},
         "cpu_baseline": cpu,
         "clocks": clk,
+        "extra": {"rays_per_frame": rays // args.steps, "Mrays_per_s": rays / (dev_ms / 1e3) / 1e6},
     }
     print(json.dumps(line), flush=True)
 

@@ -296,6 +296,46 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     return BG_OK;
 }
 
+// Tree wavefront buffers for `samples` camera samples per wave: two level queues of 2 x samples
+// nodes each (node differentials only for textured scenes), `sh_cap` shadow rays, one
+// accumulator per sample.
+bg_status ensure_tree_wave(bg_ctx* ctx, uint32_t samples, uint32_t sh_cap, bool textured) {
+    bg::TreeWave& t = ctx->tree;
+    const uint32_t cap = 2 * samples;
+    if (t.counters && t.samp_cap >= samples && t.cap >= cap && t.sh_cap >= sh_cap && (t.textured || !textured))
+        return BG_OK;
+    dfree_all(ctx, ctx->tree_allocs);
+    t = bg::TreeWave{};
+    auto get = [&](size_t bytes, void** p) { return dalloc(ctx, bytes, p, &ctx->tree_allocs); };
+    bg_status s;
+#define TW(field, bytes)                                   \
+    do {                                                   \
+        void* p_;                                          \
+        if ((s = get((bytes), &p_)) != BG_OK) return s;    \
+        t.field = (decltype(t.field))p_;                   \
+    } while (0)
+    for (int b = 0; b < 2; ++b) {
+        TW(ray_o[b], (size_t)cap * sizeof(float4));
+        TW(ray_d[b], (size_t)cap * sizeof(float4));
+        TW(beta[b], (size_t)cap * sizeof(float4));
+        TW(meta[b], (size_t)cap * sizeof(uint4));
+        if (textured) TW(rd[b], 4 * (size_t)cap * sizeof(float4));
+    }
+    TW(hit, (size_t)cap * sizeof(int2));
+    TW(sh_o, (size_t)sh_cap * sizeof(float4));
+    TW(sh_d, (size_t)sh_cap * sizeof(float4));
+    TW(sh_c, (size_t)sh_cap * sizeof(float4));
+    TW(L, (size_t)samples * sizeof(float4));
+    TW(counters, 8 * sizeof(uint32_t));
+    TW(ray_stats, 2 * sizeof(unsigned long long));
+#undef TW
+    t.cap = cap;
+    t.sh_cap = sh_cap;
+    t.samp_cap = samples;
+    t.textured = textured ? 1u : 0u;
+    return BG_OK;
+}
+
 bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
     uint32_t e = 0;
     CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -458,6 +498,7 @@ void bg_destroy(bg_ctx* ctx) {
     ctx->scenes.clear();
     guide_orphan_all(ctx);
     dfree_all(ctx, ctx->wave_allocs);
+    dfree_all(ctx, ctx->tree_allocs);
     dfree_all(ctx, ctx->film_allocs);
     dfree_all(ctx, ctx->user);
     if (ctx->flush) cudaFree(ctx->flush);
@@ -1115,10 +1156,45 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         } else if (tree) {
             const int kind = o->integrator == BG_INTEGRATOR_WHITTED ? 1
                              : (o->light_strategy == BG_LIGHT_UNIFORM_ALL ? 2 : 3);
-            const int layout = s->kind == BG_BVH_WIDE ? 8 : (s->kind == BG_BVH_WIDE2 ? 2 : 1);
-            bg::launch_tree_integrator(kind, o->mode == BG_MODE_REF_COMPAT, layout, s->dev, dc, rp, ctx->film,
-                                       ctx->d_err, ctx->shape, ctx->stream);
-            launches += 1;
+            const bool wide = s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2;
+            if (o->mode == BG_MODE_PBRT && wide) {
+                // breadth-first wavefront over the trees of up to W samples per wave
+                const uint64_t nl = std::max<uint64_t>(s->dev.nlights, 1);
+                const uint64_t per_node = kind == 1 ? nl : (kind == 2 ? 2 * nl : 2);
+                const uint64_t sh_budget = 1ull << 25;  // shadow rays per level
+                uint64_t W = std::min<uint64_t>({(uint64_t)kTreeWaveSamples, (uint64_t)ctx->max_queue, total,
+                                                 std::max<uint64_t>(1, sh_budget / (2 * per_node))});
+                W = std::max<uint64_t>(W, 1);
+                const bool textured = s->dev.ntex > 0;
+                if ((st = ensure_tree_wave(ctx, (uint32_t)W, (uint32_t)std::min<uint64_t>(sh_budget, 2 * W * per_node),
+                                           textured)) != BG_OK)
+                    return st;
+                CK(cudaMemsetAsync(ctx->tree.ray_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+                uint64_t n_wave = W;
+                for (uint64_t item0 = 0; item0 < total;) {
+                    const uint32_t n = (uint32_t)std::min<uint64_t>(n_wave, total - item0);
+                    launches += bg::launch_tree_wave(kind, s->dev, dc, rp, ctx->tree, item0, n, ctx->d_err, ctx->shape,
+                                                     ctx->stream);
+                    uint32_t overflow = 0;
+                    CK(cudaMemcpyAsync(&overflow, ctx->tree.counters + 5, sizeof(overflow), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+                    CK(cudaStreamSynchronize(ctx->stream));
+                    if (overflow) {  // nothing reached the film: render these samples in smaller waves
+                        if (n == 1)
+                            return fail(ctx, BG_ERR_UNSUPPORTED, "one sample's ray tree outgrew the tree wavefront");
+                        n_wave = std::max<uint64_t>(1, n / 2);
+                        continue;
+                    }
+                    bg::launch_tree_final(rp, ctx->film, ctx->tree, item0, n, ctx->shape, ctx->stream);
+                    launches += 1;
+                    item0 += n;
+                }
+            } else {
+                const int layout = s->kind == BG_BVH_WIDE ? 8 : (s->kind == BG_BVH_WIDE2 ? 2 : 1);
+                bg::launch_tree_integrator(kind, o->mode == BG_MODE_REF_COMPAT, layout, s->dev, dc, rp, ctx->film,
+                                           ctx->d_err, ctx->shape, ctx->stream);
+                launches += 1;
+            }
         } else {
             bg::launch_megakernel(o->mode == BG_MODE_REF_COMPAT, s->dev, dc, rp, ctx->film, ctx->d_err, ctx->shape,
                                   ctx->stream);
@@ -1142,9 +1218,9 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         unsigned long long nan = 0;
         cudaMemcpy(&nan, ctx->film.nan_count, sizeof(nan), cudaMemcpyDeviceToHost);
         stats->nan_samples = nan;
-        if (wavefront) {
+        if (wavefront || (tree && ctx->tree.ray_stats)) {
             unsigned long long rs[2] = {0, 0};
-            cudaMemcpy(rs, ctx->wave.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
+            cudaMemcpy(rs, wavefront ? ctx->wave.ray_stats : ctx->tree.ray_stats, sizeof(rs), cudaMemcpyDeviceToHost);
             stats->extension_rays = rs[0];
             stats->shadow_rays = rs[1];
         }

@@ -25,6 +25,8 @@ struct bg_ctx {
     uint32_t film_w = 0, film_h = 0;
     bg::WaveBuffers wave{};
     std::vector<void*> wave_allocs;
+    bg::TreeWave tree{};  // Whitted / direct-lighting wavefront (allocated on first use)
+    std::vector<void*> tree_allocs;
     std::vector<void*> film_allocs;
     void* flush = nullptr;
     size_t flush_bytes = 0;
@@ -68,8 +70,10 @@ struct bg_scene {
 namespace bgi {
 
 constexpr uint64_t kFaithfulMaxPrims = 200000;
+constexpr uint32_t kTreeWaveSamples = 1u << 21;  // camera samples per Whitted / direct-lighting wave
 
 bool triangle_light_sides(const bg_scene* s, std::vector<uint8_t>* out, std::string* why);
+bg_status ensure_tree_wave(bg_ctx* ctx, uint32_t samples, uint32_t sh_cap, bool textured);
 void affine_inverse(const float* xf, float* inv);
 
 bg_status fail(bg_ctx* c, bg_status s, const std::string& msg);

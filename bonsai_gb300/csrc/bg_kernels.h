@@ -115,6 +115,37 @@ struct LaunchShape {
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,
                   uint8_t* occluded, uint32_t* err, unsigned long long* counters, uint32_t* work_head,
                   const LaunchShape& ls, cudaStream_t s);
+// Breadth-first wavefront of the Whitted / direct-lighting ray trees (bg_tree_wave.cu).  One wave
+// = up to `nsamp` camera samples; level d of every sample's tree is one queue of tree nodes (depth
+// d), ping-ponged between two buffers; light-sampling rays of a level go to one shadow queue.
+// Contributions add into per-sample accumulators, which reach the film once the wave's trees are
+// done.  counters: [0,1] level sizes, [2] shadow rays, [3] extension head, [4] shadow head,
+// [5] overflow (a level or the shadow queue outgrew its capacity: the wave is redone smaller).
+struct TreeWave {
+    uint32_t cap, sh_cap, samp_cap;
+    uint32_t textured;
+    float4* ray_o[2];   // o.xyz, t_max
+    float4* ray_d[2];   // d.xyz, time
+    float4* beta[2];    // rgb
+    uint4* meta[2];     // sample slot, node id, depth, has differentials
+    float4* rd[2];      // 4 per node: rx origin, ry origin, rx direction, ry direction (textured scenes)
+    int2* hit;          // closest hit of the current level's nodes
+    float4* sh_o;       // shadow ray origin, t_max
+    float4* sh_d;       // direction, prim to skip (int bits)
+    float4* sh_c;       // contribution rgb, sample slot (uint bits)
+    float4* L;          // per sample slot: radiance accumulated so far
+    uint32_t* counters;
+    unsigned long long* ray_stats;  // [0] closest-hit rays, [1] any-hit rays
+};
+// Traces and shades the trees of samples [item0, item0 + n) (item = sample * npix + pixel, as the
+// path wavefront) into the wave's accumulators; returns the kernel launches.  kind as below.  The
+// host then reads counters[5]: zero -> launch_tree_final adds the samples to the film; set -> the
+// wave outgrew a queue and is rendered again in smaller waves (nothing reached the film).
+int launch_tree_wave(int kind, const Scene& sc, const Camera& cam, const RenderParams& rp, const TreeWave& tw,
+                     uint64_t item0, uint32_t n, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
+void launch_tree_final(const RenderParams& rp, const FilmBuffers& film, const TreeWave& tw, uint64_t item0,
+                       uint32_t n, const LaunchShape& ls, cudaStream_t s);
+
 // Whitted / direct-lighting integrators (bg_integrators.cu): kind 1 Whitted, 2 direct lighting with
 // UniformSampleAll, 3 direct lighting with UniformSampleOne; layout 1 reference, 2 two-wide,
 // 8 eight-wide.  Tree depth is limited to TREE_MAX_DEPTH (a specular ray tree's pending-ray

@@ -228,4 +228,41 @@ BG_D RGB tex_eval(const Scene& sc, uint32_t tid, const TexPoint& tp) {
     return mip_filter(sc, t, st, dx, dy);
 }
 
+// Differentials of a specular child ray (integrator.rs:164-190 reflection, 225-262 transmission).
+BG_D RayDiff specular_diff(const Isect& it, const TexPoint& tp, const RayDiff& rd, V3 wi, float bsdf_eta,
+                           bool transmit) {
+    const SurfDiff& d = tp.d;
+    RayDiff o;
+    o.rxo = it.p + d.dpdx;
+    o.ryo = it.p + d.dpdy;
+    V3 n = it.ns;
+    V3 dndx = tp.g.dndu * d.dudx + tp.g.dndv * d.dvdx;
+    V3 dndy = tp.g.dndu * d.dudy + tp.g.dndv * d.dvdy;
+    const V3 wo = it.wo;
+    if (!transmit) {
+        V3 dwodx = -rd.rxd - wo, dwody = -rd.ryd - wo;
+        float ddndx = dot(dwodx, n) + dot(wo, dndx);
+        float ddndy = dot(dwody, n) + dot(wo, dndy);
+        o.rxd = wi - dwodx + 2.0f * (dot(wo, n) * dndx + ddndx * n);
+        o.ryd = wi - dwody + 2.0f * (dot(wo, n) * dndy + ddndy * n);
+        return o;
+    }
+    float eta = 1.0f / bsdf_eta;
+    if (dot(wo, n) < 0.0f) {
+        eta = 1.0f / eta;
+        n = -n;
+        dndx = -dndx;
+        dndy = -dndy;
+    }
+    V3 dwodx = -rd.rxd - wo, dwody = -rd.ryd - wo;
+    float ddndx = dot(dwodx, n) + dot(wo, dndx);
+    float ddndy = dot(dwody, n) + dot(wo, dndy);
+    float mu = eta * dot(wo, n) - abs_dot(wi, n);
+    float dmudx = (eta - (eta * eta * dot(wo, n)) / abs_dot(wi, n)) * ddndx;
+    float dmudy = (eta - (eta * eta * dot(wo, n)) / abs_dot(wi, n)) * ddndy;
+    o.rxd = wi - eta * dwodx + (mu * dndx + dmudx * n);
+    o.ryd = wi - eta * dwody + (mu * dndy + dmudy * n);
+    return o;
+}
+
 }  // namespace bg

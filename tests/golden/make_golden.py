@@ -55,15 +55,40 @@ def quadric_case():
     return out
 
 
+def texture_case():
+    """The textured room (image / uv textures, the four mappings, MIPMap filtering, Oren-Nayar,
+    vertex normals, orientation flags), both estimator modes, and the Whitted / direct-lighting
+    integrators on the same room with its conductor sphere turned to glass."""
+    out = {}
+    sd = S.textured_room(16, 16, spp=4)
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=True).render(mode, seed=3, threads=1)
+        out[f"textured_sum_{mode}"] = r["sum"]
+    mats = list(sd.materials) + [S.material(S.DIELECTRIC, ior=1.5)]
+    sd.materials = np.stack(mats)
+    sd.spheres = sd.spheres.copy()
+    sd.spheres[1]["material_id"] = len(mats) - 1
+    for name, kind, strategy in (("whitted", A.BG_INTEGRATOR_WHITTED, 0),
+                                 ("direct_all", A.BG_INTEGRATOR_DIRECT, A.BG_LIGHT_UNIFORM_ALL),
+                                 ("direct_one", A.BG_INTEGRATOR_DIRECT, A.BG_LIGHT_UNIFORM_ONE)):
+        r = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, seed=5, threads=1, integrator=kind,
+                                                     light_strategy=strategy)
+        out[f"{name}_sum"] = r["sum"]
+    return out
+
+
 def rng_case():
     idx = np.array([(0, 0, 0, 0), (1, 2, 3, 4), (12345, 999, 7, 41), (2**32 - 1, 2**31, 65535, 1023)], np.uint64)
     vals = np.array([O.rng_uniform(int(s), int(p), int(n), int(d)) for s, p, n, d in idx], np.float32)
     return {"rng_index": idx, "rng_value": vals}
 
 
+CASES = {"oracle_trace.npz": trace_case, "oracle_render.npz": render_case, "oracle_rng.npz": rng_case,
+         "oracle_quadric.npz": quadric_case, "oracle_texture.npz": texture_case}
+
 if __name__ == "__main__":
-    np.savez_compressed(HERE / "oracle_trace.npz", **trace_case())
-    np.savez_compressed(HERE / "oracle_render.npz", **render_case())
-    np.savez_compressed(HERE / "oracle_rng.npz", **rng_case())
-    np.savez_compressed(HERE / "oracle_quadric.npz", **quadric_case())
-    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+    # writes the fixtures named on the command line (all of them without arguments)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        np.savez_compressed(HERE / name, **CASES[name]())
+    print("wrote", names)

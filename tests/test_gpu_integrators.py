@@ -2,6 +2,8 @@
 against the CPU oracle's recursive restatement (same random numbers per ray-tree node), in both
 estimator modes, over the three BVH layouts, on a room with a glass sphere (the specular
 recursion) and textured walls (ray differentials carried through specular bounces)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -116,3 +118,31 @@ def test_depth_limits(gpu_ctx):
         assert r.stats.samples == 64 and o.integrator == 0
     finally:
         sc.close()
+
+
+def test_small_tree_waves_match_large_ones(gpu_ctx):
+    """The tree wavefront renders in waves of at most bg_tuning.wave_paths samples; a wave whose
+    ray trees outgrow a level queue is discarded and rendered again in halves.  Tiny waves over
+    deep glass trees (reached only through the halving when a wave overflows) give the film of one
+    large wave up to float summation order."""
+    sd = glass_room(48, 48, spp=8, max_depth=12, textured=False)
+    sd.spheres = sd.spheres.copy()
+    sd.spheres[0]["material_id"] = sd.spheres[1]["material_id"]  # both spheres glass
+    out = []
+    saved = A.bg_tuning()
+    gpu_ctx.check(gpu_ctx.lib.bg_get_tuning(gpu_ctx.h, C.byref(saved)))
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    try:
+        for wave in (1 << 20, 1024):
+            t = A.bg_tuning.from_buffer_copy(bytes(saved))
+            t.wave_paths = wave
+            gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(t)))
+            r = G.WhittedIntegrator(sd.camera, 8, 12).render(sc)
+            assert r.stats.error_word == 0
+            out.append((r.rgb, r.stats.launches))
+    finally:
+        gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(saved)))
+        sc.close()
+    (a, la), (b, lb) = out
+    assert lb > la  # many more waves
+    np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-5)

@@ -66,3 +66,21 @@ def test_quadric_render_golden():
     for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
         r = O.OracleScene(sd, fixed_bvh=False).render(mode, seed=9, threads=1)
         np.testing.assert_allclose(r["sum"], g[f"sum_{mode}"], rtol=RTOL, atol=1e-9)
+
+
+def test_texture_and_integrator_golden():
+    g = np.load(GOLD / "oracle_texture.npz")
+    sd = S.textured_room(16, 16, spp=4)
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=True).render(mode, seed=3, threads=1)
+        np.testing.assert_allclose(r["sum"], g[f"textured_sum_{mode}"], rtol=RTOL, atol=1e-9)
+    mats = list(sd.materials) + [S.material(S.DIELECTRIC, ior=1.5)]
+    sd.materials = np.stack(mats)
+    sd.spheres = sd.spheres.copy()
+    sd.spheres[1]["material_id"] = len(mats) - 1
+    for name, kind, strategy in (("whitted", A.BG_INTEGRATOR_WHITTED, 0),
+                                 ("direct_all", A.BG_INTEGRATOR_DIRECT, A.BG_LIGHT_UNIFORM_ALL),
+                                 ("direct_one", A.BG_INTEGRATOR_DIRECT, A.BG_LIGHT_UNIFORM_ONE)):
+        r = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, seed=5, threads=1, integrator=kind,
+                                                     light_strategy=strategy)
+        np.testing.assert_allclose(r["sum"], g[f"{name}_sum"], rtol=RTOL, atol=1e-9)
