@@ -1265,6 +1265,10 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         if (it.scene->kind != BG_BVH_WIDE)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs scenes committed with BG_BVH_WIDE");
         if (it.opts.mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs BG_MODE_PBRT");
+        if (it.opts.integrator != BG_INTEGRATOR_PATH)
+            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering runs the path integrator only");
+        if (it.scene->dev.ntex)
+            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering does not support textured scenes");
         total_pix += (uint64_t)it.camera.width * it.camera.height;
         total_items += (uint64_t)it.camera.width * it.camera.height * it.opts.spp;
         max_depth = std::max(max_depth, it.opts.max_depth);

@@ -574,6 +574,9 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering needs a wide BVH layout");
     if (o->flags & (BG_RENDER_GRAPH | BG_RENDER_STAGE_TIMING))
         return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering takes no GRAPH or STAGE_TIMING flag");
+    if (o->integrator != BG_INTEGRATOR_PATH)
+        return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering runs the path integrator only");
+    if (s->dev.ntex) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering does not support textured scenes");
     CK(cudaSetDevice(ctx->device));
     if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
     if (!(o->flags & BG_RENDER_ACCUMULATE)) {

@@ -121,6 +121,8 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     if (o->max_depth > 250) return reject(BG_ERR_INVALID, "max_depth must be <= 250");
     if (o->flags & (BG_RENDER_ACCUMULATE | BG_RENDER_STAGE_TIMING | BG_RENDER_GRAPH))
         return reject(BG_ERR_UNSUPPORTED, "accumulate / stage timing / graph flags need bg_render");
+    if (o->integrator != BG_INTEGRATOR_PATH)
+        return reject(BG_ERR_UNSUPPORTED, "the Whitted and direct-lighting integrators need bg_render");
 
     int prev = -1;
     cudaGetDevice(&prev);

@@ -354,7 +354,7 @@ bg_status bg_film_write_exr(bg_ctx* ctx, const char* path);
  * sequence of persistent launches: the paths of all scenes share the wavefront queues (each path
  * carries its scene index into a device table of scene, camera, render options and film slice),
  * so small and large scenes keep the GPU equally busy.  Scenes must be committed with
- * BG_BVH_WIDE and rendered in BG_MODE_PBRT; each item's film is cleared and, when rgb_out is not
+ * BG_BVH_WIDE and rendered in BG_MODE_PBRT with the path integrator (untextured scenes); each item's film is cleared and, when rgb_out is not
  * NULL, read back to it (width*height*3 floats).  Afterwards bg_film_moments returns the films of
  * all items concatenated in item order.  stats: device time and rays of the whole batch. */
 typedef struct bg_batch_item {
@@ -372,7 +372,7 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
  * Same semantics as bg_render, but it calls no cudaMalloc, cudaFree or other allocating routine:
  * its scratch (film moments, wavefront queues, path state, counters) lives in one static device
  * array of BG_NOALLOC_SCRATCH_BYTES bytes that every GPU loading the library holds until exit.
- * Limits: at most BG_NOALLOC_MAX_PIXELS film pixels (larger films return BG_ERR_INVALID with the
+ * Limits: the path integrator only; at most BG_NOALLOC_MAX_PIXELS film pixels (larger films return BG_ERR_INVALID with the
  * limit in bg_last_error of the scene's context); waves of BG_NOALLOC_WAVE_PATHS paths; no
  * ACCUMULATE / STAGE_TIMING / GRAPH flags.  The caller passes the committed scene, the output
  * d_rgb_out (device memory, width*height*3 floats) and a CUDA stream (NULL = default stream); the
@@ -482,7 +482,8 @@ bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* 
  * not lower than that of the unguided passes.  Warm-up count, fallback and the variance
  * estimates persist in the guide across calls, so a long render can be issued in chunks (with
  * BG_RENDER_ACCUMULATE and increasing first_sample).  Film, flags and rgb_out as in bg_render;
- * guide_stats counts this call's passes and reports the running estimates. */
+ * guide_stats counts this call's passes and reports the running estimates.  The path integrator
+ * only, on untextured scenes (BG_ERR_UNSUPPORTED otherwise). */
 bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* scene, bg_guide* guide, const bg_camera* camera,
                            const bg_render_opts* opts, float* rgb_out, bg_render_stats* stats,
                            bg_guide_stats* guide_stats);
