@@ -706,8 +706,14 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 // In guided waves the matte / plastic / conductor classes stop after their emission and queue a
 // network query; k_guide_continue finishes them with the network's mixture.
 // GWK: guiding support compiled in (records, guided queries); the plain wavefront uses GWK = false.
+// Minimum resident CTAs per SM the shade kernels are compiled for: 4 caps them at 128 registers
+// (the plastic and conductor classes would use 148 / 159).  Measured on the production scene at
+// 4 spp: shade 7.1 ms against 7.7 ms unconstrained; 5 and 6 CTAs gave 7.3 and 7.1 ms.
+#ifndef BG_SHADE_MINBLOCKS
+#define BG_SHADE_MINBLOCKS 4
+#endif
 template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false>
-__global__ void __launch_bounds__(128) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
+__global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
