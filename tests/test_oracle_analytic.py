@@ -80,11 +80,12 @@ def _sampled_estimate(mat, wo, mode, n=4000, seed=0):
     return acc / n
 
 
-@pytest.mark.parametrize("kind", ["matte", "conductor", "plastic"])
+@pytest.mark.parametrize("kind", ["matte", "conductor", "plastic", "oren_nayar"])
 def test_bsdf_sampling_matches_quadrature_pbrt(kind):
     mat = {"matte": S.material(S.MATTE, kd=(0.6, 0.5, 0.4)),
            "conductor": S.material(S.CONDUCTOR, roughness=0.3),
-           "plastic": S.material(S.PLASTIC, kd=(0.5, 0.5, 0.5), ks=(0.3, 0.3, 0.3), roughness=0.3)}[kind]
+           "plastic": S.material(S.PLASTIC, kd=(0.5, 0.5, 0.5), ks=(0.3, 0.3, 0.3), roughness=0.3),
+           "oren_nayar": S.material(S.MATTE, kd=(0.6, 0.5, 0.4), sigma=25.0)}[kind]
     wo = np.array([0.3, 0.2, 0.0])
     wo[2] = np.sqrt(1 - 0.13)
     q = _hemisphere_quadrature(mat, wo, A.BG_MODE_PBRT)
@@ -106,3 +107,30 @@ def test_lambertian_closed_form():
     out = O.bsdf_eval(mat, (0.0, 0.0, 1.0), (0.6, 0.0, 0.8), A.BG_MODE_PBRT)
     np.testing.assert_allclose(out[:3], np.array([0.6, 0.5, 0.4]) / np.pi, rtol=1e-6)
     np.testing.assert_allclose(out[3], 0.8 / np.pi, rtol=1e-6)
+
+
+def test_oren_nayar_closed_form():
+    """The Oren-Nayar qualitative model (Oren & Nayar 1994, as in PBRT-v3):
+    f = R/pi (A + B max(0, cos(phi_i - phi_o)) sin(alpha) tan(beta)), A = 1 - s^2 / (2 (s^2 + 0.33)),
+    B = 0.45 s^2 / (s^2 + 0.09), s = sigma in radians, alpha / beta the larger / smaller of the angles."""
+    sigma = 30.0
+    mat = S.material(S.MATTE, kd=(0.6, 0.5, 0.4), sigma=sigma)
+    s2 = np.radians(sigma) ** 2
+    a, b = 1 - s2 / (2 * (s2 + 0.33)), 0.45 * s2 / (s2 + 0.09)
+    for wo, wi in [((0.3, 0.1, 0.0), (-0.5, 0.2, 0.0)), ((0.0, 0.6, 0.0), (0.1, 0.45, 0.0))]:
+        wo, wi = np.array(wo), np.array(wi)
+        wo[2], wi[2] = np.sqrt(1 - wo @ wo), np.sqrt(1 - wi @ wi)
+        ti, to = np.arccos(wi[2]), np.arccos(wo[2])
+        dphi = np.arctan2(wi[1], wi[0]) - np.arctan2(wo[1], wo[0])
+        want = np.array([0.6, 0.5, 0.4]) / np.pi * (a + b * max(0.0, np.cos(dphi)) * np.sin(max(ti, to))
+                                                     * np.tan(min(ti, to)))
+        out = O.bsdf_eval(mat, wo, wi, A.BG_MODE_PBRT)
+        np.testing.assert_allclose(out[:3], want, rtol=2e-5)
+        np.testing.assert_allclose(out[3], wi[2] / np.pi, rtol=1e-5)
+
+
+def test_oren_nayar_sigma_zero_is_lambertian():
+    wo, wi = (0.3, 0.1, np.sqrt(0.9)), (-0.5, 0.2, np.sqrt(0.71))
+    a = O.bsdf_eval(S.material(S.MATTE, kd=(0.6, 0.5, 0.4), sigma=0.0), wo, wi, A.BG_MODE_PBRT)
+    b = O.bsdf_eval(S.material(S.MATTE, kd=(0.6, 0.5, 0.4)), wo, wi, A.BG_MODE_PBRT)
+    np.testing.assert_array_equal(a, b)
