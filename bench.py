@@ -76,7 +76,8 @@ def workload(small: bool):
 def config_of(sd, small: bool) -> dict:
     return {
         "workload": ("production-small" if small else "production 1080p") +
-                    f": {sd.ntri} triangles (64 fBm icospheres L5 + ground + 4 quad lights), "
+                    f": {sd.ntri} triangles ({sd.meta.get('n_ico', 64)} fBm icospheres "
+                    f"L{sd.meta.get('ico_level', 5)} + ground + 4 quad lights), "
                     f"{sd.nsph} spheres, {sd.camera.width}x{sd.camera.height}, {sd.spp} spp, max depth "
                     f"{sd.max_depth}, RR after depth 3, PBRT estimator",
         "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
