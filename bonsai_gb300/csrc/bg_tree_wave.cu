@@ -173,8 +173,11 @@ BG_D void direct_rays(const Scene& sc, const TreeWave& tw, bool valid, const Ise
 // Shades level d: emission, light sampling (kind 1 Whitted, 2 all lights, 3 one light) and the
 // specular children of level d + 1 (PBRT mode: the dielectric as SpecularReflection +
 // SpecularTransmission).
+#ifndef BG_TREE_SHADE_MINBLOCKS
+#define BG_TREE_SHADE_MINBLOCKS 1
+#endif
 template <bool TEX>
-__global__ void __launch_bounds__(128) k_tw_shade(Scene sc, RenderParams rp, TreeWave tw, uint32_t d, int kind,
+__global__ void __launch_bounds__(128, BG_TREE_SHADE_MINBLOCKS) k_tw_shade(Scene sc, RenderParams rp, TreeWave tw, uint32_t d, int kind,
                                                   uint64_t item0, uint32_t* err) {
     const uint32_t b = d & 1u, nb = b ^ 1u;
     const uint32_t n = min(tw.counters[b], tw.cap);

@@ -213,3 +213,26 @@ def test_paths_without_texture_support_refuse_textured_scenes(gpu_ctx):
             g.close()
     finally:
         sc.close()
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 64), (64, 2), (8, 8)])
+@pytest.mark.parametrize("wrap", [A.BG_WRAP_REPEAT, A.BG_WRAP_BLACK, A.BG_WRAP_CLAMP])
+def test_texture_shapes_and_wrap_modes(gpu_ctx, shape, wrap):
+    """Degenerate pyramids (a 1 x 1 image has a single level; 2 x 64 and 64 x 2 reach 1 texel in one
+    axis long before the other) under every wrap mode, on the back wall through a UV mapping that
+    runs past [0, 1], against the oracle."""
+    h, w = shape
+    rng = np.random.default_rng(h * 100 + w)
+    img = rng.random((h, w, 3)).astype(np.float32)
+    sd = S.cornell(32, 32, spp=8, max_depth=3)
+    mats = list(sd.materials) + [S.material(S.MATTE, kd_texture=1)]
+    sd.materials = np.stack(mats)
+    sd.tri_mat = sd.tri_mat.copy()
+    sd.tri_mat[4:6] = len(mats) - 1
+    sd.tri_uvs = np.tile(np.array([0, 0, 1, 0, 1, 1], np.float32), (sd.ntri, 1))
+    sd.textures = [S.Texture(kind=0, rgb=img, wrap=wrap, mapping=A.BG_MAPPING_UV, uv_scale=(2.5, 1.5),
+                             uv_delta=(-0.7, 0.3))]
+    r, o, cmp = _pair(gpu_ctx, sd, A.BG_MODE_PBRT, A.BG_BVH_WIDE, 8)
+    assert r.stats.error_word == 0
+    assert cmp["frac_z3"] <= Z3_FRAC
+    assert cmp["frac_close"] >= 0.9
