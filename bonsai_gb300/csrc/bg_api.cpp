@@ -296,6 +296,39 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     return BG_OK;
 }
 
+// L2 access-policy window over the scene's 8-wide traversal range (nodes + leaf primitives): its
+// lines persist in the L2 set-aside while the wave state streams past them.  The set-aside is
+// requested for the render and given back after it (limit 0, persisting lines reset), so nothing
+// outlasts the call.
+void l2_window(bg_ctx* ctx, const bg_scene* s, bool on) {
+    if (!ctx->shape.l2_persist) return;
+    if (ctx->l2_window_max == 0 && ctx->l2_persist_max == 0) {
+        int persist = 0, window = 0;
+        cudaDeviceGetAttribute(&persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device);
+        cudaDeviceGetAttribute(&window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device);
+        ctx->l2_persist_max = (size_t)std::max(persist, 0);
+        ctx->l2_window_max = (size_t)std::max(window, 0);
+    }
+    cudaStreamAttrValue a;
+    std::memset(&a, 0, sizeof(a));
+    const bool use = on && s && s->hot && ctx->l2_persist_max && ctx->l2_window_max;
+    if (use) {
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, ctx->l2_persist_max);
+        const size_t n = std::min(s->hot_bytes, ctx->l2_window_max);
+        a.accessPolicyWindow.base_ptr = s->hot;
+        a.accessPolicyWindow.num_bytes = n;
+        a.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)ctx->l2_persist_max / (double)n);
+        a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    }
+    cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &a);
+    if (!use) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
+}
+
 // Tree wavefront buffers for `samples` camera samples per wave: two level queues of 2 x samples
 // nodes each (node differentials only for textured scenes), `sh_cap` shadow rays, one
 // accumulator per sample.
@@ -560,7 +593,7 @@ bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
     out->wave_paths = ctx->max_queue;
     out->blocks_per_sm = (uint32_t)ctx->shape.blocks_per_sm;
     out->refill = (uint32_t)ctx->shape.refill;
-    out->flags = ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u;
+    out->flags = (ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u) | (ctx->shape.l2_persist ? BG_TUNE_L2_PERSIST : 0u);
     return BG_OK;
 }
 
@@ -573,6 +606,7 @@ bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
     ctx->shape.blocks_per_sm = (int)t->blocks_per_sm;
     ctx->shape.refill = (int)t->refill;
     ctx->shape.sort_rays = (t->flags & BG_TUNE_SORT_RAYS) ? 1 : 0;
+    ctx->shape.l2_persist = (t->flags & BG_TUNE_L2_PERSIST) ? 1 : 0;
     return BG_OK;
 }
 
@@ -929,8 +963,20 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if (kind == BG_BVH_WIDE) {
         bg::Bvh8 b;
         bg::build_bvh8(hp, &b);
-        if ((st = upload(ctx, b.nodes, &d.nodes8, &s->allocs)) != BG_OK) return st;
-        if ((st = upload(ctx, b.leaf_prims, &d.leaf_prims, &s->allocs)) != BG_OK) return st;
+        // nodes and leaf primitives in one allocation: the range traversal reads, which an L2
+        // access-policy window can keep resident (BG_TUNE_L2_PERSIST)
+        const size_t nb = (b.nodes.size() * sizeof(bg::Bvh8Node) + 255) & ~(size_t)255;
+        const size_t lb = b.leaf_prims.size() * sizeof(float4);
+        void* hot = nullptr;
+        if ((st = dalloc(ctx, nb + lb, &hot, &s->allocs)) != BG_OK) return st;
+        if (!b.nodes.empty())
+            CK(cudaMemcpyAsync(hot, b.nodes.data(), b.nodes.size() * sizeof(bg::Bvh8Node), cudaMemcpyHostToDevice,
+                               ctx->stream));
+        if (lb) CK(cudaMemcpyAsync((char*)hot + nb, b.leaf_prims.data(), lb, cudaMemcpyHostToDevice, ctx->stream));
+        d.nodes8 = (const bg::Bvh8Node*)hot;
+        d.leaf_prims = (const float4*)((char*)hot + nb);
+        s->hot = hot;
+        s->hot_bytes = nb + lb;
         d.n_nodes8 = (uint32_t)b.nodes.size();
         nodes = b.nodes.size();
     } else if (kind == BG_BVH_WIDE2) {
@@ -1101,6 +1147,7 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
         }
     }
     if (wavefront) CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    l2_window(ctx, s, true);
     CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
     const bool use_graph = wavefront && !timing && (o->flags & BG_RENDER_GRAPH);
     if (total > 0 && use_graph) {
@@ -1205,6 +1252,7 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     launches += 1;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev_end, ctx->stream));
+    l2_window(ctx, s, false);
     uint32_t word = 0;
     st = check_device_error(ctx, &word);
     if (stats) {

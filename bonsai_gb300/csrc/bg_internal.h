@@ -41,6 +41,8 @@ struct bg_ctx {
     int graph_kernels = 0;
     std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
     std::unordered_set<bg_guide*> guides;  // live guiding networks; orphaned the same way
+    size_t l2_persist_max = 0, l2_window_max = 0;  // device limits for L2 access-policy windows
+    bool l2_limit_set = false;
 };
 
 struct bg_scene {
@@ -63,6 +65,8 @@ struct bg_scene {
     uint32_t kind = BG_BVH_WIDE;
     bg::Scene dev{};
     float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};  // bounds of all primitives
+    void* hot = nullptr;   // 8-wide layout: nodes + leaf primitives, one range
+    size_t hot_bytes = 0;
     std::vector<void*> allocs;
 };
 
@@ -74,6 +78,9 @@ constexpr uint32_t kTreeWaveSamples = 1u << 21;  // camera samples per Whitted /
 
 bool triangle_light_sides(const bg_scene* s, std::vector<uint8_t>* out, std::string* why);
 bg_status ensure_tree_wave(bg_ctx* ctx, uint32_t samples, uint32_t sh_cap, bool textured);
+// With BG_TUNE_L2_PERSIST: marks the scene's traversal range as persisting in L2 for the launches
+// that follow on the context's stream (on = false clears the window and the persisting lines).
+void l2_window(bg_ctx* ctx, const bg_scene* s, bool on);
 void affine_inverse(const float* xf, float* inv);
 
 bg_status fail(bg_ctx* c, bg_status s, const std::string& msg);

@@ -110,6 +110,7 @@ struct LaunchShape {
     int blocks_per_sm = 8;
     int refill = 32;
     int sort_rays = 0;
+    int l2_persist = 0;  // BG_TUNE_L2_PERSIST (part of the captured graph's key)
 };
 
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,

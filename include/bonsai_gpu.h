@@ -289,6 +289,9 @@ typedef struct bg_tuning {
 } bg_tuning;
 #define BG_TUNE_SORT_RAYS 1u /* bin each bounce's extension rays by direction octant and origin
                                 cell before traversal (single-scene renders)                      */
+#define BG_TUNE_L2_PERSIST 2u /* keep the 8-wide BVH (nodes + leaf primitives) resident in L2 with a
+                                 persisting access-policy window during renders; the set-aside
+                                 belongs to the context and ends with it                        */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 
