@@ -53,10 +53,12 @@ def parse():
                    help="profiling case for ncu: one render of the full-size scene at --profile-spp spp")
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
-    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch", "whitted", "direct"],
+    p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch", "whitted", "direct",
+                                          "example"],
                    default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
-                        "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room")
+                        "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room; "
+                        "example: the reference's example scene (UV-textured sphere under an environment map)")
     p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
     p.add_argument("--arm-seconds", type=float, default=90.0, help="guiding: time limit of each progressive arm")
     p.add_argument("--target", type=float, default=1e-3, help="guiding: relMSE target")
@@ -84,6 +86,20 @@ def config_of(sd, small: bool) -> dict:
         "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "8-wide compressed (80 B nodes, 8-bit child boxes, <=3 prims per leaf)", "graph": "wave chain captured as a CUDA graph",
         "l2": "flushed before every step (512 MB device write)",
         "parallelism": "replicas",
+    }
+
+
+def example_config(sd, small: bool) -> dict:
+    e = sd.env.rgb.shape
+    return {
+        "workload": f"reference example scene (src/main.rs){' small' if small else ''}: unit sphere, matte with a "
+                    f"UVTexture, InfiniteAreaLight with a {e[1]}x{e[0]} synthetic environment map, "
+                    f"{sd.camera.width}x{sd.camera.height}, {sd.spp} spp, max depth {sd.max_depth}, "
+                    f"RR threshold {sd.rr_threshold}, PBRT estimator",
+        "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
+        "integrator": "PathIntegrator", "env_map": [int(e[1]), int(e[0])],
+        "bvh": "8-wide compressed", "graph": "wave chain captured as a CUDA graph",
+        "l2": "flushed before every step (512 MB device write)", "parallelism": "replicas",
     }
 
 
@@ -348,18 +364,35 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def example_workload(small: bool):
+    """The reference's example program (src/main.rs): a unit sphere, matte with a UVTexture, under an
+    InfiniteAreaLight of identity transform, 1024x1024, 16 spp (its 4x4 stratified sampler), path
+    depth 5, roulette threshold 1; the environment map is a seeded synthetic 2048x1024 sky."""
+    from bonsai_gb300 import scenes as S
+    if small:
+        return S.env_sphere(256, 256, spp=16, max_depth=5, env_w=512, env_h=256)
+    return S.env_sphere(1024, 1024, spp=16, max_depth=5, env_w=2048, env_h=1024)
+
+
 def run_integrators(args):
     """The Whitted (`--workload whitted`) and direct-lighting (`--workload direct`, UniformSampleAll:
-    every light with MIS) integrators on the production scene: value = device Msamples/s over K
-    frames (L2 flushed), e2e through bg_render with the film read back; CPU restatement of the same
+    every light with MIS) integrators on the production scene, or the path integrator on the
+    reference's example scene (`--workload example`): value = device Msamples/s over K frames (L2
+    flushed), e2e through bg_render with the film read back; CPU restatement of the same
     integrator (oracle/) on all host cores.  The ray trees run as a breadth-first wavefront over
     the 8-wide BVH (bonsai_gb300/csrc/bg_tree_wave.cu)."""
     import ctypes as C
     from bonsai_gb300 import _abi as A
     from bonsai_gb300 import gpu as G
     rank, ws, local, dist = dist_init()
-    sd = workload(args.small)
-    if args.workload == "whitted":
+    sd = example_workload(args.small) if args.workload == "example" else workload(args.small)
+    graph = False
+    if args.workload == "example":
+        kind, strategy, name = A.BG_INTEGRATOR_PATH, 0, "PathIntegrator"
+        integ = lambda: G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, sd.rr_threshold,  # noqa: E731
+                                         mode=A.BG_MODE_PBRT)
+        graph = True
+    elif args.workload == "whitted":
         kind, strategy, name = A.BG_INTEGRATOR_WHITTED, 0, "WhittedIntegrator"
         integ = lambda: G.WhittedIntegrator(sd.camera, sd.spp, sd.max_depth, mode=A.BG_MODE_PBRT)  # noqa: E731
     else:
@@ -370,8 +403,9 @@ def run_integrators(args):
     scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
     pi = integ()
     samples = sd.camera.width * sd.camera.height * sd.spp
+    gkw = {"graph": True} if graph else {}
     for _ in range(args.warmup):
-        pi.render(scene, readback=False)
+        pi.render(scene, readback=False, **gkw)
     clocks = Clocks(local)
     barrier(dist)
     ctx.synchronize()
@@ -379,7 +413,7 @@ def run_integrators(args):
     dev_ms, launches, rays = 0.0, 0, 0
     for k in range(args.steps):
         ctx.flush_l2()
-        r = pi.render(scene, readback=False, first_sample=k * sd.spp)
+        r = pi.render(scene, readback=False, first_sample=k * sd.spp, **gkw)
         dev_ms += r.stats.device_ms
         launches += r.stats.launches
         rays += r.stats.extension_rays + r.stats.shadow_rays
@@ -393,7 +427,7 @@ def run_integrators(args):
     barrier(dist)
     t0 = time.time()
     for k in range(args.steps):
-        pi.render(scene, readback=True, first_sample=k * sd.spp)
+        pi.render(scene, readback=True, first_sample=k * sd.spp, **gkw)
     e2e = ws * args.steps * samples / max_over_ranks(dist, time.time() - t0) / 1e6
     if rank != 0:
         return
@@ -411,14 +445,17 @@ def run_integrators(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
-        "config": config_of(sd, args.small) | {"integrator": name, "graph": "no (a host check per wave)",
-                                               "waves": "breadth-first ray-tree wavefront, <= 2M samples per wave"},
+        "config": (example_config(sd, args.small) if args.workload == "example" else
+                   config_of(sd, args.small) | {"integrator": name, "graph": "no (a host check per wave)",
+                                                "waves": "breadth-first ray-tree wavefront, <= 2M samples per wave"}),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
                 "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
-                     "kernel": "k_tw_extend<8> / k_tw_shadow<8> (tree wavefront)", "peak_source": peak_kind,
-                     "note": "the traversal kernels are those of the path workload, which carries the roofline"},
+                     "kernel": ("k_extend<8> / k_shadow<8> (path wavefront)" if graph else
+                                "k_tw_extend<8> / k_tw_shadow<8> (tree wavefront)"), "peak_source": peak_kind,
+                     "note": "the traversal kernels are those of the production path workload, which carries "
+                             "the roofline"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "extra": {"rays_per_frame": rays // args.steps, "Mrays_per_s": rays / (dev_ms / 1e3) / 1e6},
@@ -791,7 +828,7 @@ def main():
     if args.workload == "guiding":
         run_guiding(args)
         return
-    if args.workload in ("whitted", "direct"):
+    if args.workload in ("whitted", "direct", "example"):
         run_integrators(args)
         return
     if args.profile:

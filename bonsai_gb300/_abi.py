@@ -40,6 +40,7 @@ BG_RENDER_NO_READBACK = 2
 BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
 BG_TUNE_SORT_RAYS = 1
+BG_TUNE_L2_PERSIST = 2
 
 BG_TEXTURE_IMAGE = 0
 BG_TEXTURE_UV = 1
@@ -83,6 +84,11 @@ class bg_texture(C.Structure):
                 ("rgb", C.c_void_p), ("mapping", C.c_uint32), ("uv_scale", C.c_float * 2),
                 ("uv_delta", C.c_float * 2), ("world_to_texture", C.c_float * 12), ("vs", F3), ("vt", F3),
                 ("ds", C.c_float), ("dt", C.c_float)]
+
+
+class bg_infinite_light(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.c_void_p), ("intensity", F3),
+                ("light_to_world", C.c_float * 12)]
 
 
 class bg_obj_info(C.Structure):
@@ -187,6 +193,7 @@ SIGNATURES = {
     "bg_scene_add_triangles": (ST, [P, P, C.c_size_t, P, P]),
     "bg_scene_add_triangle_mesh": (ST, [P, P, C.c_size_t, P, P, P, P, C.c_uint32]),
     "bg_scene_add_texture": (ST, [P, C.POINTER(bg_texture), C.POINTER(C.c_uint32)]),
+    "bg_scene_add_infinite_light": (ST, [P, C.POINTER(bg_infinite_light)]),
     "bg_scene_add_spheres": (ST, [P, P, C.c_size_t]),
     "bg_scene_add_quadrics": (ST, [P, P, C.c_size_t]),
     "bg_scene_commit": (ST, [P, C.c_uint32, C.POINTER(bg_build_stats)]),

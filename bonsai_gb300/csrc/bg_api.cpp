@@ -700,7 +700,64 @@ bg_status bg_scene_add_triangles(bg_scene* s, const float* xyz, size_t ntri, con
 }
 
 // Image::generate_pyramid (src/io/image.rs:55-114): each level halves the previous one (at least
-// 1 x 1), a texel being the mean of its 2 x 2 parents ((a + b + c + d) * 0.25 in f32).
+// 1 x 1), a texel being the mean of its 2 x 2 parents ((a + b + c + d) * 0.25 in f32).  Appends the
+// levels to the scene's texels and fills ti's level table; `scale` multiplies the base image's
+// channels first (Image::scale, image.rs:116-128).
+static bg_status append_pyramid(bg_scene* s, const float* rgb, uint32_t w, uint32_t h, const float* scale,
+                                bg::TexInfo* ti, const char* what) {
+    const std::string name(what);
+    if (!rgb || w == 0 || h == 0) return fail(s->ctx, BG_ERR_INVALID, name + " needs texels");
+    if ((w & (w - 1)) || (h & (h - 1)))
+        return fail(s->ctx, BG_ERR_UNSUPPORTED,
+                    name + " sizes must be powers of two (the reference resamples other sizes with a "
+                           "third-party Lanczos filter)");
+    if ((uint64_t)w * h > (1ull << 28)) return fail(s->ctx, BG_ERR_INVALID, name + " too large");
+    uint32_t nlev = 1;
+    for (uint32_t m = std::max(w, h); m > 1; m >>= 1) ++nlev;  // 1 + ilog2(max(w, h))
+    if (nlev > (uint32_t)bg::TEX_MAX_LEVELS) return fail(s->ctx, BG_ERR_INVALID, name + " too large");
+    if (s->texels.size() + 2ull * w * h > 0xFFFFFFFFull) return fail(s->ctx, BG_ERR_INVALID, "too many texels");
+    ti->nlevels = nlev;
+    std::vector<float> cur(rgb, rgb + (size_t)w * h * 3), next;
+    if (scale)
+        for (size_t i = 0; i < cur.size(); ++i) cur[i] *= scale[i % 3];
+    uint32_t cw = w, chh = h;
+    for (uint32_t l = 0; l < nlev; ++l) {
+        if (l > 0) {
+            const uint32_t nw = std::max(cw / 2, 1u), nh = std::max(chh / 2, 1u);
+            size_t d[4] = {0, 3, 3 * (size_t)cw, 3 * ((size_t)cw + 1)};
+            if (cw == 1) {
+                d[1] = 0;
+                d[3] -= 3;
+            }
+            if (chh == 1) {
+                d[2] = 0;
+                d[3] -= 3 * (size_t)cw;
+            }
+            next.assign((size_t)nw * nh * 3, 0.0f);
+            for (uint32_t y = 0; y < nh; ++y) {
+                size_t src = 3 * ((size_t)(2 * y) * cw), dst = 3 * ((size_t)y * nw);
+                for (uint32_t x = 0; x < nw; ++x) {
+                    for (int c = 0; c < 3; ++c) {
+                        next[dst] = (cur[src] + cur[src + d[1]] + cur[src + d[2]] + cur[src + d[3]]) * 0.25f;
+                        ++src;
+                        ++dst;
+                    }
+                    src += 3;
+                }
+            }
+            cur.swap(next);
+            cw = nw;
+            chh = nh;
+        }
+        ti->lw[l] = cw;
+        ti->lh[l] = chh;
+        ti->loff[l] = (uint32_t)s->texels.size();
+        for (size_t i = 0; i < (size_t)cw * chh; ++i)
+            s->texels.push_back(make_float4(cur[3 * i], cur[3 * i + 1], cur[3 * i + 2], 0.0f));
+    }
+    return BG_OK;
+}
+
 bg_status bg_scene_add_texture(bg_scene* s, const bg_texture* t, uint32_t* id) {
     if (!s || !t) return BG_ERR_INVALID;
     if (!s->ctx) return BG_ERR_INVALID;
@@ -725,57 +782,45 @@ bg_status bg_scene_add_texture(bg_scene* s, const bg_texture* t, uint32_t* id) {
     ti.ds = t->ds;
     ti.dt = t->dt;
     if (t->kind == BG_TEXTURE_IMAGE) {
-        const uint32_t w = t->width, h = t->height;
-        if (!t->rgb || w == 0 || h == 0) return fail(s->ctx, BG_ERR_INVALID, "image texture needs texels");
-        if ((w & (w - 1)) || (h & (h - 1)))
-            return fail(s->ctx, BG_ERR_UNSUPPORTED,
-                        "image texture sizes must be powers of two (the reference resamples other sizes with a "
-                        "third-party Lanczos filter)");
-        if ((uint64_t)w * h > (1ull << 28)) return fail(s->ctx, BG_ERR_INVALID, "image texture too large");
-        uint32_t nlev = 1;
-        for (uint32_t m = std::max(w, h); m > 1; m >>= 1) ++nlev;  // 1 + ilog2(max(w, h))
-        if (nlev > (uint32_t)bg::TEX_MAX_LEVELS) return fail(s->ctx, BG_ERR_INVALID, "image texture too large");
-        if (s->texels.size() + 2ull * w * h > 0xFFFFFFFFull) return fail(s->ctx, BG_ERR_INVALID, "too many texels");
-        ti.nlevels = nlev;
-        std::vector<float> cur(t->rgb, t->rgb + (size_t)w * h * 3), next;
-        uint32_t cw = w, chh = h;
-        for (uint32_t l = 0; l < nlev; ++l) {
-            if (l > 0) {
-                const uint32_t nw = std::max(cw / 2, 1u), nh = std::max(chh / 2, 1u);
-                size_t d[4] = {0, 3, 3 * (size_t)cw, 3 * ((size_t)cw + 1)};
-                if (cw == 1) {
-                    d[1] = 0;
-                    d[3] -= 3;
-                }
-                if (chh == 1) {
-                    d[2] = 0;
-                    d[3] -= 3 * (size_t)cw;
-                }
-                next.assign((size_t)nw * nh * 3, 0.0f);
-                for (uint32_t y = 0; y < nh; ++y) {
-                    size_t src = 3 * ((size_t)(2 * y) * cw), dst = 3 * ((size_t)y * nw);
-                    for (uint32_t x = 0; x < nw; ++x) {
-                        for (int c = 0; c < 3; ++c) {
-                            next[dst] = (cur[src] + cur[src + d[1]] + cur[src + d[2]] + cur[src + d[3]]) * 0.25f;
-                            ++src;
-                            ++dst;
-                        }
-                        src += 3;
-                    }
-                }
-                cur.swap(next);
-                cw = nw;
-                chh = nh;
-            }
-            ti.lw[l] = cw;
-            ti.lh[l] = chh;
-            ti.loff[l] = (uint32_t)s->texels.size();
-            for (size_t i = 0; i < (size_t)cw * chh; ++i)
-                s->texels.push_back(make_float4(cur[3 * i], cur[3 * i + 1], cur[3 * i + 2], 0.0f));
-        }
+        bg_status st = append_pyramid(s, t->rgb, t->width, t->height, nullptr, &ti, "image texture");
+        if (st != BG_OK) return st;
     }
     s->tex.push_back(ti);
     if (id) *id = (uint32_t)(s->tex.size() - 1);
+    return BG_OK;
+}
+
+// InfiniteAreaLight::new (src/lights/infinite.rs:38-80), the image part: the environment map scaled
+// by the intensity, as a MIPMap with repeat wrapping.  The sampling distribution and the world's
+// bounding sphere wait for the commit, which knows the scene's bounds.
+bg_status bg_scene_add_infinite_light(bg_scene* s, const bg_infinite_light* l) {
+    if (!s || !l) return BG_ERR_INVALID;
+    if (!s->ctx) return BG_ERR_INVALID;
+    if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
+    if (s->has_inf) return fail(s->ctx, BG_ERR_UNSUPPORTED, "a scene holds at most one infinite light");
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(l->intensity[k])) return fail(s->ctx, BG_ERR_INVALID, "infinite light intensity is not finite");
+    for (int k = 0; k < 12; ++k)
+        if (!std::isfinite(l->light_to_world[k]))
+            return fail(s->ctx, BG_ERR_INVALID, "infinite light transform is not finite");
+    const float* m = l->light_to_world;
+    const float det = m[0] * (m[5] * m[10] - m[6] * m[9]) - m[1] * (m[4] * m[10] - m[6] * m[8]) +
+                      m[2] * (m[4] * m[9] - m[5] * m[8]);
+    if (!(det != 0.0f) || !std::isfinite(det))
+        return fail(s->ctx, BG_ERR_INVALID, "infinite light transform is singular");
+    bg::TexInfo ti{};
+    ti.kind = BG_TEXTURE_IMAGE;
+    ti.wrap = BG_WRAP_REPEAT;
+    const size_t texels0 = s->texels.size();
+    bg_status st = append_pyramid(s, l->rgb, l->width, l->height, l->intensity, &ti, "environment map");
+    if (st != BG_OK) {
+        s->texels.resize(texels0);
+        return st;
+    }
+    s->inf_map = ti;
+    std::memcpy(s->inf_l2w, l->light_to_world, sizeof(s->inf_l2w));
+    bgi::affine_inverse(l->light_to_world, s->inf_w2l);
+    s->has_inf = true;
     return BG_OK;
 }
 
@@ -811,6 +856,125 @@ bg_status bg_scene_add_quadrics(bg_scene* s, const bg_quadric* q, size_t n) {
                 return fail(s->ctx, BG_ERR_INVALID, "quadric transform is not finite");
     }
     s->quads.insert(s->quads.end(), q, q + n);
+    return BG_OK;
+}
+
+// ---- the infinite light's sampling distribution, built on the host at commit
+namespace {
+int32_t sat_i32(float f) {  // `as i32`: saturating, NaN to 0
+    if (std::isnan(f)) return 0;
+    if (f >= 2147483648.0f) return 2147483647;
+    if (f <= -2147483648.0f) return (-2147483647 - 1);
+    return (int32_t)f;
+}
+int32_t imod(int32_t a, int32_t b) {  // math::modulo (math.rs:43-50)
+    int32_t r = a - (a / b) * b;
+    return r < 0 ? r + b : r;
+}
+// Image::get_channel with repeat wrapping (image.rs:130-159), the three channels.
+void env_texel(const bg_scene* s, const bg::TexInfo& t, int level, int32_t x, int32_t y, float out[3]) {
+    const int32_t w = (int32_t)t.lw[level], h = (int32_t)t.lh[level];
+    x = imod(x, w);
+    y = imod(y, h);
+    const float4 v = s->texels[t.loff[level] + (size_t)y * (size_t)w + (size_t)x];
+    out[0] = v.x;
+    out[1] = v.y;
+    out[2] = v.z;
+}
+// MIPMap::triangle (mipmap.rs:156-173)
+void env_bilerp(const bg_scene* s, const bg::TexInfo& t, int level, float s0, float t0, float out[3]) {
+    const float fs = s0 * (float)t.lw[level] - 0.5f, ft = t0 * (float)t.lh[level] - 0.5f;
+    const float ds = fs - std::floor(fs), dt = ft - std::floor(ft);
+    const int32_t x = sat_i32(std::floor(fs)), y = sat_i32(std::floor(ft));
+    const int32_t x1 = (int32_t)((uint32_t)x + 1u), y1 = (int32_t)((uint32_t)y + 1u);
+    float a[3], b[3], c[3], d[3];
+    env_texel(s, t, level, x, y, a);
+    env_texel(s, t, level, x, y1, b);
+    env_texel(s, t, level, x1, y, c);
+    env_texel(s, t, level, x1, y1, d);
+    const float wa = (1.0f - ds) * (1.0f - dt), wb = (1.0f - ds) * dt, wc = ds * (1.0f - dt), wd = ds * dt;
+    for (int k = 0; k < 3; ++k) out[k] = wa * a[k] + wb * b[k] + wc * c[k] + wd * d[k];
+}
+// MIPMap::trilinear_filter (mipmap.rs:46-63)
+void env_trilinear(const bg_scene* s, const bg::TexInfo& t, float s0, float t0, float width, float out[3]) {
+    const float top = (float)(t.nlevels - 1);
+    const float level = top + std::log2(std::fmax(width, 1e-8f));
+    if (level < 0.0f) return env_bilerp(s, t, 0, s0, t0, out);
+    if (level >= top) return env_texel(s, t, (int)t.nlevels - 1, 0, 0, out);
+    const int il = (int)std::floor(level);
+    const float f = level - std::floor(level);
+    float a[3], b[3];
+    env_bilerp(s, t, il, s0, t0, a);
+    env_bilerp(s, t, il + 1, s0, t0, b);
+    for (int k = 0; k < 3; ++k) out[k] = (1.0f - f) * a[k] + f * b[k];
+}
+// Distribution1D::new (sampling.rs:22-47) over func[0..n): cdf has n + 1 entries.
+float dist1d_build(const float* func, uint32_t n, float* cdf) {
+    cdf[0] = 0.0f;
+    for (uint32_t i = 1; i <= n; ++i) cdf[i] = cdf[i - 1] + func[i - 1] / (float)n;
+    const float func_int = cdf[n];
+    if (func_int == 0.0f) {
+        for (uint32_t i = 1; i <= n; ++i) cdf[i] = (float)i / (float)n;
+    } else {
+        for (uint32_t i = 1; i <= n; ++i) cdf[i] /= func_int;
+    }
+    return func_int;
+}
+}  // namespace
+
+// InfiniteAreaLight::new (infinite.rs:38-80), the part that needs the scene: the luminance of the
+// map over a 2w x 2h grid weighted by sin(theta), its Distribution2D (sampling.rs:79-97) and the
+// world's bounding sphere (Bounds3::bounding_sphere, bounds3.rs:208-215).
+static bg_status commit_infinite_light(bg_scene* s, bg::InfLight* L) {
+    bg_ctx* ctx = s->ctx;
+    const bg::TexInfo& map = s->inf_map;
+    const uint32_t nu = 2 * map.lw[0], nv = 2 * map.lh[0];
+    const float PI = 3.14159265358979323846f;
+    const float fwidth = 0.5f / (float)std::min(nu, nv);
+    std::vector<float> func((size_t)nu * nv), cond_cdf((size_t)nv * (nu + 1)), cond_int(nv), marg_cdf(nv + 1);
+    for (uint32_t v = 0; v < nv; ++v) {
+        const float vp = ((float)v + 0.5f) / (float)nv;
+        const float sin_theta = std::sin(PI * ((float)v + 0.5f) / (float)nv);
+        for (uint32_t u = 0; u < nu; ++u) {
+            const float up = ((float)u + 0.5f) / (float)nu;
+            float c[3];
+            env_trilinear(s, map, up, vp, fwidth, c);
+            const float y = 0.212671f * c[0] + 0.715160f * c[1] + 0.072169f * c[2];  // RGBSpectrum::y
+            func[(size_t)v * nu + u] = y * sin_theta;
+        }
+    }
+    for (uint32_t v = 0; v < nv; ++v)
+        cond_int[v] = dist1d_build(&func[(size_t)v * nu], nu, &cond_cdf[(size_t)v * (nu + 1)]);
+    const float marg_int = dist1d_build(cond_int.data(), nv, marg_cdf.data());
+    *L = bg::InfLight{};
+    L->map = map;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) {
+            L->l2w[r][c] = s->inf_l2w[4 * r + c];
+            L->w2l[r][c] = s->inf_w2l[4 * r + c];
+        }
+    float center[3], radius = 0.0f;
+    bool inside = true;
+    for (int k = 0; k < 3; ++k) {
+        center[k] = (s->bmin[k] + s->bmax[k]) * (1.0f / 2.0f);
+        inside = inside && center[k] >= s->bmin[k] && center[k] <= s->bmax[k];
+    }
+    if (inside) {
+        const float dx = center[0] - s->bmax[0], dy = center[1] - s->bmax[1], dz = center[2] - s->bmax[2];
+        radius = std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    std::memcpy(L->center, center, sizeof(center));
+    L->radius = radius;
+    L->nu = nu;
+    L->nv = nv;
+    L->marg_int = marg_int;
+    bg_status st;
+    if ((st = upload(ctx, cond_cdf, &L->cond_cdf, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, func, &L->cond_func, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, cond_int, &L->cond_int, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, marg_cdf, &L->marg_cdf, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, cond_int, &L->marg_func, &s->allocs)) != BG_OK) return st;
+    CK(cudaStreamSynchronize(ctx->stream));  // the host vectors end here
     return BG_OK;
 }
 
@@ -923,6 +1087,8 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         std::memcpy(emis[i].intensity, s->lights[i].intensity, sizeof(emis[i].intensity));
         emis[i].two_sided = s->lights[i].two_sided;
     }
+    // the light list: emitting triangles in order, then the infinite light
+    if (s->has_inf) light_prims.push_back(bg::LIGHT_INFINITE);
     bg::Scene& d = s->dev;
     d = bg::Scene{};
     d.ntri = ntri;
@@ -956,8 +1122,17 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     }
     if (!s->tex.empty()) {
         if ((st = upload(ctx, s->tex, &d.tex, &s->allocs)) != BG_OK) return st;
-        if ((st = upload(ctx, s->texels, &d.texels, &s->allocs)) != BG_OK) return st;
         d.ntex = (uint32_t)s->tex.size();
+    }
+    if (!s->texels.empty())
+        if ((st = upload(ctx, s->texels, &d.texels, &s->allocs)) != BG_OK) return st;
+    uint64_t inf_bytes = 0;
+    if (s->has_inf) {
+        std::vector<bg::InfLight> inf(1);
+        if ((st = commit_infinite_light(s, &inf[0])) != BG_OK) return st;
+        if ((st = upload(ctx, inf, &d.inf, &s->allocs)) != BG_OK) return st;
+        const uint64_t nu = inf[0].nu, nv = inf[0].nv;
+        inf_bytes = sizeof(bg::InfLight) + 4 * (nv * (nu + 1) + nu * nv + 2 * nv + nv + 1);
     }
     uint64_t nodes = 0;
     if (kind == BG_BVH_WIDE) {
@@ -1010,7 +1185,7 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
                          ((uint64_t)ntri + nsph + nquad) * (wide ? 48 : 4) + quad4.size() * 16 +
                          ((s->any_normals || s->any_flags) ? (uint64_t)ntri : 0) +
                          (s->any_normals ? 48ull * ntri : 0) + (s->any_uvs ? 24ull * ntri : 0) +
-                         s->tex.size() * sizeof(bg::TexInfo) + s->texels.size() * 16;
+                         s->tex.size() * sizeof(bg::TexInfo) + s->texels.size() * 16 + inf_bytes;
         stats->device_bytes = bytes;
     }
     return BG_OK;
@@ -1315,8 +1490,8 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         if (it.opts.mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs BG_MODE_PBRT");
         if (it.opts.integrator != BG_INTEGRATOR_PATH)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering runs the path integrator only");
-        if (it.scene->dev.ntex)
-            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering does not support textured scenes");
+        if (it.scene->dev.ntex || it.scene->has_inf)
+            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering does not support textured scenes or infinite lights");
         total_pix += (uint64_t)it.camera.width * it.camera.height;
         total_items += (uint64_t)it.camera.width * it.camera.height * it.opts.spp;
         max_depth = std::max(max_depth, it.opts.max_depth);

@@ -101,6 +101,27 @@ struct Bvh8Node {
 };
 static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node must be 80 bytes");
 
+// InfiniteAreaLight (src/lights/infinite.rs): the environment map's MIPMap (a TexInfo over the
+// shared texel array, repeat wrap), its transforms, the scene's bounding sphere and the
+// Distribution2D over a (2w x 2h) luminance * sin(theta) image (src/base/sampling.rs:10-118):
+// row v's conditional cdf at cond_cdf[v * (nu + 1)], its function values at cond_func[v * nu],
+// its integral in cond_int[v]; the marginal over rows in marg_cdf / marg_func / marg_int.
+struct InfLight {
+    TexInfo map;
+    float l2w[3][4], w2l[3][4];
+    float center[3], radius;
+    uint32_t nu, nv;
+    const float* cond_cdf;
+    const float* cond_func;
+    const float* cond_int;
+    const float* marg_cdf;
+    const float* marg_func;
+    float marg_int;
+    uint32_t pad;
+};
+// Light-list entry of the infinite light in Scene::light_prims (area lights hold their triangle).
+constexpr uint32_t LIGHT_INFINITE = 0xFFFFFFFFu;
+
 struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-175)
     float r2c[4][4];  // raster_to_camera.m
     float c2w[4][4];  // camera_to_world.m
@@ -141,6 +162,7 @@ struct Scene {
     const float2* tri_uv;
     const TexInfo* tex;
     const float4* texels;
+    const InfLight* inf;  // the infinite light, or null
 };
 
 enum : uint32_t {

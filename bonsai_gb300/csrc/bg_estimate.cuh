@@ -23,7 +23,7 @@ BG_D RGB estimate_direct_mk(const Scene& sc, const Isect& it, const BSDF& bsdf, 
                              float us1, float ul0, float ul1, uint32_t* err) {
     const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
     RGB out = rgb(0.0f);
-    LightSample ls = light_sample<REF>(sc, light_prim, it, ul0, ul1);
+    LightSample ls = light_sample_any<REF>(sc, light_prim, it, ul0, ul1);
     float scattering_pdf = 0.0f;
     if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
         RGB f = bsdf.f<REF>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
@@ -46,7 +46,7 @@ BG_D RGB estimate_direct_mk(const Scene& sc, const Isect& it, const BSDF& bsdf, 
     if (!is_black(f) && spdf > 0.0f) {
         float w = 1.0f;
         if (!sampled_specular) {
-            float lpdf = light_pdf<REF>(sc, light_prim, it, wdir, nullptr);
+            float lpdf = light_pdf_any<REF>(sc, light_prim, it, wdir, nullptr);
             if (lpdf == 0.0f) return out;
             w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
         }
@@ -54,7 +54,10 @@ BG_D RGB estimate_direct_mk(const Scene& sc, const Isect& it, const BSDF& bsdf, 
         Ray rr = ray;
         int prim = trace_one<LAYOUT, false>(sc, rr, err);
         RGB li = rgb(0.0f);
-        if (prim >= 0 && (REF ? prim_emission(sc, prim) >= 0 : prim == (int)light_prim)) {
+        if (prim < 0) {
+            // an escaping ray sees Light::radiance: the environment map of an infinite light
+            if (light_prim == LIGHT_INFINITE) li = inf_radiance(sc, wdir);
+        } else if (REF ? prim_emission(sc, prim) >= 0 : prim == (int)light_prim) {
             Isect lit;
             if (prim_isect(sc, prim, ray, &lit)) li = emitted_radiance(sc, lit, -wdir);
         }

@@ -52,7 +52,10 @@ BG_D RGB tree_radiance(const Scene& sc, const RenderParams& rp, int kind, Ray ca
         const TreeRay nd = st[--sp];
         Ray r = nd.ray;
         const int prim = trace_one<LAYOUT, false>(sc, r, err);
-        if (prim < 0) continue;  // area lights add no radiance to escaping rays (light.rs:31-33)
+        if (prim < 0) {  // background radiance (whitted.rs:45-51, direct.rs:75-81); area lights add none
+            if (sc.inf) L = L + nd.beta * inf_radiance(sc, nd.ray.d);
+            continue;
+        }
         Isect it;
         if (!prim_isect(sc, prim, nd.ray, &it)) continue;
         const Rng rng{pix, s, rp.seed, nd.node - 1u};
@@ -74,7 +77,7 @@ BG_D RGB tree_radiance(const Scene& sc, const RenderParams& rp, int kind, Ray ca
             if (kind == 1) {  // whitted.rs:176-192
                 for (uint32_t j = 0; j < sc.nlights; ++j) {
                     const uint32_t lp = sc.light_prims[j];
-                    LightSample ls = light_sample<REF>(sc, lp, it, rng.u(DIM_LIGHTS + 2 * j), rng.u(DIM_LIGHTS + 2 * j + 1));
+                    LightSample ls = light_sample_any<REF>(sc, lp, it, rng.u(DIM_LIGHTS + 2 * j), rng.u(DIM_LIGHTS + 2 * j + 1));
                     if (is_black(ls.radiance) || ls.pdf == 0.0f) continue;
                     RGB f = bsdf.f<REF>(it.wo, ls.wi, BSDF_ALL);
                     if (is_black(f)) continue;

@@ -57,6 +57,10 @@ struct bg_scene {
     bool any_normals = false, any_uvs = false, any_flags = false;
     std::vector<bg::TexInfo> tex;     // textures, level offsets into texels
     std::vector<float4> texels;
+    // the infinite area light: its environment map's pyramid (in texels) and transforms
+    bool has_inf = false;
+    bg::TexInfo inf_map{};
+    float inf_l2w[12] = {}, inf_w2l[12] = {};
     std::vector<bg_sphere> sph;
     std::vector<bg_quadric> quads;
     std::vector<bg_material> mats;

@@ -147,6 +147,7 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
         if (hit) hit = prim_isect(sc, prim, traced, &it);
         if (bounces == 0 || specular_bounce) {
             if (hit) out = out + beta * emitted_radiance(sc, it, -ray.d);
+            else if (prim < 0) out = out + beta * escaped_radiance(sc, ray.d);
         }
         if (!hit || bounces >= max_depth) break;
         TexPoint tp;
@@ -597,7 +598,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
             const float c = mix->c();
             return c * mix->pdf(w) + (1.0f - c) * pb;
         };
-        LightSample ls = light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+        LightSample ls = light_sample_any<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
         if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
             RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
             if (!is_black(f)) {
@@ -628,18 +629,20 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         if (!is_black(f) && spdf > 0.0f) {
             float t_light = 0.0f;
             V3 ln;
-            float lpdf = light_pdf<false>(sc, light_prim, it, wi, &t_light, &ln);
+            float lpdf = light_pdf_any<false>(sc, light_prim, it, wi, &t_light, &ln);
             if (lpdf != 0.0f) {
                 float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
                 // the sampled direction reaches the light at t_light; it counts iff nothing else
-                // is hit first (closest hit == this light)
-                RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -wi);
+                // is hit first (closest hit == this light; for the infinite light t_light is
+                // infinite and nothing may be hit)
+                RGB li = light_radiance_along(sc, light_prim, wi, ln);
                 if (!is_black(li)) {
                     RGB c = f * li * w / spdf;
                     Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
                     pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
                     out.sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
-                    out.sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float((int)light_prim));
+                    const int skip = light_prim == LIGHT_INFINITE ? -1 : (int)light_prim;
+                    out.sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float(skip));
                     out.push_sh[1] = true;
                 }
             }
@@ -754,6 +757,8 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
             const bool counted = bounce == 0 || specular_bounce;
             RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
+            // an escaped ray gathers the infinite light's radiance (path.rs:78-85)
+            if (CLS == CLS_MISS && prim < 0 && counted && sc.inf) le = inf_radiance(sc, ray.d);
             // The previous vertex's record closes here.  Its training target also takes this
             // emission, which the estimator leaves to that vertex's next-event estimation: the
             // network learns the directions of lights as well, for the strategy it serves.

@@ -604,6 +604,143 @@ BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, flo
     return pdf;
 }
 
+// ---- InfiniteAreaLight (src/lights/infinite.rs) and Distribution2D (src/base/sampling.rs:10-118)
+BG_D V3 m34_vec(const float m[3][4], V3 v) {  // Vec3::transform with an affine 3x4
+    return v3(m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+              m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z);
+}
+// find_interval (src/base/math.rs:70-87) over a cdf of `size` entries
+BG_D uint32_t find_interval(const float* cdf, uint32_t size, float u) {
+    uint32_t first = 0, len = size;
+    while (len > 0) {
+        uint32_t half = len >> 1, middle = first + half;
+        if (cdf[middle] <= u) {
+            first = middle + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    int32_t r = (int32_t)first - 1;
+    return (uint32_t)(r < 0 ? 0 : (r > (int32_t)size - 2 ? (int32_t)size - 2 : r));
+}
+// Distribution1D::sample_continuous (sampling.rs:53-76); `count` is the divisor of the result
+BG_D float dist1d_sample(const float* cdf, const float* func, float func_int, uint32_t n, uint32_t count, float u,
+                         float* pdf, uint32_t* off) {
+    uint32_t o = find_interval(cdf, n + 1, u);
+    if (off) *off = o;
+    float du = u - cdf[o];
+    if (cdf[o + 1] - cdf[o] > 0.0f) du /= cdf[o + 1] - cdf[o];
+    *pdf = func_int > 0.0f ? func[o] / func_int : 0.0f;
+    return ((float)o + du) / (float)count;
+}
+// Distribution2D::sample_continuous (sampling.rs:99-111).  REF (F18): a conditional row keeps the
+// whole tail of the function (sampling.rs:84), so its count() is (nv - v) * nu.
+template <bool REF>
+BG_D float2 dist2d_sample(const InfLight& L, float u0, float u1, float* pdf) {
+    float p0, p1;
+    uint32_t v = 0;
+    const float d1 = dist1d_sample(L.marg_cdf, L.marg_func, L.marg_int, L.nv, L.nv, u1, &p1, &v);
+    const uint32_t count = REF ? (L.nv - v) * L.nu : L.nu;
+    const float d0 = dist1d_sample(L.cond_cdf + (size_t)v * (L.nu + 1), L.cond_func + (size_t)v * L.nu,
+                                   L.cond_int[v], L.nu, count, u0, &p0, nullptr);
+    *pdf = p0 * p1;
+    return make_float2(d0, d1);
+}
+// Distribution2D::pdf (sampling.rs:113-117).  REF (F19): p is cast to an integer before the scaling,
+// so the cell is (0, 0) unless a coordinate reaches 1; the column bound is row 0's count, the whole
+// function (F18).  Row v's tail is the function from v * nu on; an index past its end (where the
+// reference panics) reads the last entry.
+template <bool REF>
+BG_D float dist2d_pdf(const InfLight& L, float p0, float p1) {
+    size_t idx;
+    if (REF) {
+        const size_t v = p1 >= 1.0f ? L.nv - 1 : 0;
+        const size_t u = p0 >= 1.0f ? (size_t)L.nv * L.nu - 1 : 0;
+        idx = v * L.nu + u;
+        if (idx > (size_t)L.nv * L.nu - 1) idx = (size_t)L.nv * L.nu - 1;
+    } else {
+        int iu = (int)(p0 * (float)L.nu), iv = (int)(p1 * (float)L.nv);
+        iu = iu < 0 ? 0 : (iu > (int)L.nu - 1 ? (int)L.nu - 1 : iu);
+        iv = iv < 0 ? 0 : (iv > (int)L.nv - 1 ? (int)L.nv - 1 : iv);
+        idx = (size_t)iv * L.nu + (size_t)iu;
+    }
+    return L.cond_func[idx] / L.marg_int;
+}
+// InfiniteAreaLight::radiance (infinite.rs:88-96): the map at the ray direction, level 0.
+BG_D RGB inf_radiance(const Scene& sc, V3 dir) {
+    const InfLight& L = *sc.inf;
+    V3 w = normalize(m34_vec(L.w2l, dir));
+    float phi = atan2f(w.y, w.x);
+    if (phi < 0.0f) phi = phi + 2.0f * PI;
+    float theta = acosf(rclamp(w.z, -1.0f, 1.0f));
+    float2 st = make_float2(phi * (1.0f / (2.0f * PI)), theta * (1.0f / PI));
+    return mip_filter(sc, L.map, st, make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f));
+}
+// InfiniteAreaLight::sample_point (infinite.rs:98-153); the visibility target is 2 world radii
+// along wi with no error bound and no normal.
+template <bool REF>
+BG_D LightSample inf_sample(const Scene& sc, const Isect& it, float u0, float u1) {
+    const InfLight& L = *sc.inf;
+    LightSample ls;
+    ls.radiance = rgb(0.0f);
+    ls.wi = v3(0, 0, 0);
+    ls.pdf = 0.0f;
+    float map_pdf;
+    float2 uv = dist2d_sample<REF>(L, u0, u1, &map_pdf);
+    if (map_pdf == 0.0f) return ls;
+    float theta = uv.y * PI, phi = uv.x * 2.0f * PI;
+    float st = sinf(theta), ct = cosf(theta), sp = sinf(phi), cp = cosf(phi);
+    V3 wi = m34_vec(L.l2w, v3(st * cp, st * sp, ct));
+    float pdf = map_pdf / (2.0f * PI * PI * st);
+    if (st == 0.0f) pdf = 0.0f;
+    ls.wi = wi;
+    ls.pdf = pdf;
+    ls.radiance = mip_filter(sc, L.map, uv, make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f));
+    ls.pt.p = it.p + wi * (2.0f * L.radius);
+    ls.pt.p_err = v3(0.0f, 0.0f, 0.0f);
+    ls.pt.n = v3(0.0f, 0.0f, 0.0f);
+    ls.pt.pdf_area = 0.0f;
+    return ls;
+}
+// InfiniteAreaLight::point_pdf (infinite.rs:155-169)
+template <bool REF>
+BG_D float inf_pdf(const Scene& sc, V3 w) {
+    const InfLight& L = *sc.inf;
+    V3 wi = m34_vec(L.w2l, w);
+    float theta = acosf(rclamp(wi.z, -1.0f, 1.0f));
+    float phi = atan2f(wi.y, wi.x);
+    if (phi < 0.0f) phi = phi + 2.0f * PI;
+    float s = sinf(theta);
+    if (s == 0.0f) return 0.0f;
+    return dist2d_pdf<REF>(L, phi * (1.0f / (2.0f * PI)), theta * (1.0f / PI)) / (2.0f * PI * PI * s);
+}
+// Light::sample_point for an entry of the light list (a triangle or the infinite light).
+template <bool REF>
+BG_D LightSample light_sample_any(const Scene& sc, uint32_t light, const Isect& it, float u0, float u1) {
+    if (light == LIGHT_INFINITE) return inf_sample<REF>(sc, it, u0, u1);
+    return light_sample<REF>(sc, light, it, u0, u1);
+}
+// Light::point_pdf for an entry of the light list.  t_light: the hit distance on an area light,
+// infinity for the infinite light; n_light: the area light's normal there.
+template <bool REF>
+BG_D float light_pdf_any(const Scene& sc, uint32_t light, const Isect& it, V3 wi, float* t_light,
+                         V3* n_light = nullptr) {
+    if (light == LIGHT_INFINITE) {
+        if (t_light) *t_light = INFINITY;
+        return inf_pdf<REF>(sc, wi);
+    }
+    return light_pdf<REF>(sc, light, it, wi, t_light, n_light);
+}
+// Radiance arriving along a BSDF-sampled direction wi that reaches light `light` unoccluded:
+// the area light's one-sided emission at its surface, or the environment map.
+BG_D RGB light_radiance_along(const Scene& sc, uint32_t light, V3 wi, V3 n_light) {
+    if (light == LIGHT_INFINITE) return inf_radiance(sc, wi);
+    return emission(sc.emis[prim_emission(sc, (int)light)], n_light, -wi);
+}
+// Light::radiance of every light for a ray that escapes the scene (only infinite lights emit).
+BG_D RGB escaped_radiance(const Scene& sc, V3 dir) { return sc.inf ? inf_radiance(sc, dir) : rgb(0.0f); }
+
 // ---- camera
 BG_D V3 xf_point(const float m[4][4], V3 p) {  // point3.rs:51-69
     float xp = m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3];

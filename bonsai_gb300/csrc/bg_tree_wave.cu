@@ -136,7 +136,7 @@ BG_D void direct_rays(const Scene& sc, const TreeWave& tw, bool valid, const Ise
     Ray r0, r1;
     RGB c0 = rgb(0.0f), c1 = rgb(0.0f);
     if (valid) {
-        LightSample ls = light_sample<false>(sc, light_prim, it, ul0, ul1);
+        LightSample ls = light_sample_any<false>(sc, light_prim, it, ul0, ul1);
         float scattering_pdf = 0.0f;
         if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
             RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
@@ -153,10 +153,10 @@ BG_D void direct_rays(const Scene& sc, const TreeWave& tw, bool valid, const Ise
         if (!is_black(f) && bs.pdf > 0.0f) {
             float t_light = 0.0f;
             V3 ln;
-            float lpdf = light_pdf<false>(sc, light_prim, it, bs.wi, &t_light, &ln);
+            float lpdf = light_pdf_any<false>(sc, light_prim, it, bs.wi, &t_light, &ln);
             if (lpdf != 0.0f) {
                 float w = power_heuristic(1.0f, bs.pdf, 1.0f, lpdf);
-                RGB li = emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -bs.wi);
+                RGB li = light_radiance_along(sc, light_prim, bs.wi, ln);
                 if (!is_black(li)) {
                     c1 = scale * (f * li * w / bs.pdf);
                     r1 = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
@@ -167,16 +167,17 @@ BG_D void direct_rays(const Scene& sc, const TreeWave& tw, bool valid, const Ise
         }
     }
     push_shadow(tw, h0, r0, -1, c0, slot);
-    push_shadow(tw, h1, r1, (int)light_prim, c1, slot);
+    push_shadow(tw, h1, r1, light_prim == LIGHT_INFINITE ? -1 : (int)light_prim, c1, slot);
 }
 
 // Shades level d: emission, light sampling (kind 1 Whitted, 2 all lights, 3 one light) and the
 // specular children of level d + 1 (PBRT mode: the dielectric as SpecularReflection +
 // SpecularTransmission).
-// Compiled for 4 resident CTAs per SM (at most 128 registers): production 1080p, 64 spp, Whitted
-// 71.7 and direct lighting 33.7 Msamples/s, against 67.2 / 30.6 unconstrained (196 registers).
+// Compiled for 6 resident CTAs per SM (at most 80 registers): production 1080p, 64 spp, Whitted
+// 72.6 and direct lighting 36.8 Msamples/s, against 71.7 / 33.7 with 4 CTAs, 72.0 / 35.0 with 5
+// and 67.2 / 30.6 unconstrained (196 registers).
 #ifndef BG_TREE_SHADE_MINBLOCKS
-#define BG_TREE_SHADE_MINBLOCKS 4
+#define BG_TREE_SHADE_MINBLOCKS 6
 #endif
 template <bool TEX>
 __global__ void __launch_bounds__(128, BG_TREE_SHADE_MINBLOCKS) k_tw_shade(Scene sc, RenderParams rp, TreeWave tw, uint32_t d, int kind,
@@ -200,6 +201,8 @@ __global__ void __launch_bounds__(128, BG_TREE_SHADE_MINBLOCKS) k_tw_shade(Scene
             beta = rgb(b4.x, b4.y, b4.z);
             ray = load_ray(tw.ray_o[b][i], tw.ray_d[b][i]);
             prim = tw.hit[i].x;
+            // background radiance of an escaped ray (whitted.rs:45-51, direct.rs:75-81)
+            if (prim < 0 && sc.inf) add_L(tw, meta.x, beta * inf_radiance(sc, ray.d));
             valid = prim >= 0 && prim_isect(sc, prim, ray, &it);
         }
         const uint32_t slot = meta.x, node = meta.y;
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(128, BG_TREE_SHADE_MINBLOCKS) k_tw_shade(Scene
                     Ray sr;
                     RGB c = rgb(0.0f);
                     if (valid) {
-                        LightSample ls = light_sample<false>(sc, sc.light_prims[j], it, rng.u(TW_DIM_LIGHTS + 2 * j),
+                        LightSample ls = light_sample_any<false>(sc, sc.light_prims[j], it, rng.u(TW_DIM_LIGHTS + 2 * j),
                                                              rng.u(TW_DIM_LIGHTS + 2 * j + 1));
                         if (!is_black(ls.radiance) && ls.pdf != 0.0f) {
                             RGB f = bsdf.f<false>(it.wo, ls.wi, BSDF_ALL);

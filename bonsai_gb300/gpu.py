@@ -102,6 +102,9 @@ class Scene:
         for t in sd.textures:
             tt, keep = S.texture_struct(t)
             ctx.check(lib.bg_scene_add_texture(h, C.byref(tt), None))
+        if sd.env is not None:
+            el, keep = S.env_struct(sd.env)
+            ctx.check(lib.bg_scene_add_infinite_light(h, C.byref(el)))
         tri = np.ascontiguousarray(sd.tri, np.float32)
         tm = np.ascontiguousarray(sd.tri_mat, np.uint32)
         tl = np.ascontiguousarray(sd.tri_light, np.int32)

@@ -74,6 +74,27 @@ def texture_struct(t: "Texture"):
     return c, keep
 
 
+@dataclass
+class EnvMap:
+    """bg_infinite_light: an environment map (rgb of shape (h, w, 3), power-of-two sizes, row 0 at
+    theta = 0) scaled by `intensity`, oriented by a 3x4 light_to_world (src/lights/infinite.rs)."""
+    rgb: np.ndarray
+    intensity: tuple = (1.0, 1.0, 1.0)
+    light_to_world: np.ndarray = field(default_factory=lambda: np.eye(3, 4, dtype=np.float32))
+
+
+def env_struct(e: EnvMap):
+    """(bg_infinite_light, keep-alive array) for an EnvMap."""
+    from ._abi import bg_infinite_light
+    c = bg_infinite_light()
+    keep = np.ascontiguousarray(e.rgb, np.float32)
+    c.height, c.width = keep.shape[0], keep.shape[1]
+    c.rgb = keep.ctypes.data
+    c.intensity[:] = e.intensity
+    c.light_to_world[:] = np.asarray(e.light_to_world, np.float32).reshape(12)
+    return c, keep
+
+
 def triangle_runs(sd: "SceneData"):
     """Consecutive triangle ranges [a, b) sharing (has normals, flags): one mesh call each."""
     n = sd.ntri
@@ -170,6 +191,7 @@ class SceneData:
     tri_uvs: np.ndarray | None = None
     tri_flags: np.ndarray | None = None
     textures: list = field(default_factory=list)
+    env: EnvMap | None = None            # the infinite area light, last in the light list
     spp: int = 16
     max_depth: int = 5
     rr_threshold: float = 1.0
@@ -331,6 +353,61 @@ def textured_room(width: int = 64, height: int = 64, spp: int = 16, max_depth: i
     return SceneData(all_tri, tmat_all, tl, sph, np.stack(mats), lights, sd.camera, spp=spp, max_depth=max_depth,
                      rr_threshold=1.0, name="textured_room", tri_normals=normals, tri_normal_mask=mask,
                      tri_uvs=all_uv, tri_flags=all_flags, textures=tex)
+
+
+def environment_image(w: int = 64, h: int = 32, seed: int = 0, sun=(0.25, 0.3), sun_radius: float = 0.12,
+                      sun_radiance: float = 40.0) -> np.ndarray:
+    """(h, w, 3) float32 synthetic environment map over (phi, theta) = (2 pi (x + .5) / w,
+    pi (y + .5) / h): a blue sky above the horizon (theta < pi / 2), a brown ground below, a small
+    bright sun at (theta, phi) = pi * sun[0], 2 pi * sun[1], and seeded per-texel noise."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float32)
+    theta = np.pi * (y + 0.5) / h
+    phi = 2 * np.pi * (x + 0.5) / w
+    up = np.cos(theta)[..., None]
+    sky = np.array([0.25, 0.45, 0.9], np.float32) * (0.4 + 0.6 * np.clip(up, 0, 1)) + 0.15
+    ground = np.array([0.3, 0.24, 0.18], np.float32) * (0.6 + 0.4 * np.clip(-up, 0, 1))
+    img = np.where(up > 0, sky, ground)
+    ts, ps = np.pi * sun[0], 2 * np.pi * sun[1]
+    cosang = np.sin(theta) * np.sin(ts) * np.cos(phi - ps) + np.cos(theta) * np.cos(ts)
+    sun_mask = np.arccos(np.clip(cosang, -1, 1)) < sun_radius
+    img = img + sun_mask[..., None] * (sun_radiance * np.array([1.0, 0.9, 0.7], np.float32))
+    img = img * (0.9 + 0.2 * rng.random((h, w, 1)))
+    return img.astype(np.float32)
+
+
+def env_sphere(width: int = 64, height: int = 64, spp: int = 16, max_depth: int = 5, env_w: int = 64,
+               env_h: int = 32, seed: int = 0, extra: bool = False) -> SceneData:
+    """The reference's example scene (src/main.rs): a unit sphere at the origin, matte with a
+    UVTexture through the default UVMapping2D, lit only by an InfiniteAreaLight of identity
+    transform; camera at (5, 0, 0) looking at the origin, up (0, 0, 1), fov 45.  The environment map
+    is synthetic (environment_image).  extra = True adds a glass and a plastic sphere and a small
+    one-sided emitting quad, so the light list mixes area lights with the infinite light."""
+    mats = [material(MATTE, kd_texture=1, sigma=0.0)]
+    tex = [Texture(kind=1, mapping=0)]
+    spheres = [((0.0, 0.0, 0.0), 1.0, 0)]
+    tri = np.zeros((0, 9), np.float32)
+    tri_light = np.zeros(0, np.int32)
+    lights = np.zeros(0, LIGHT_DT)
+    if extra:
+        mats.append(material(DIELECTRIC, ior=1.5))
+        mats.append(material(PLASTIC, kd=(0.1, 0.3, 0.6), ks=(0.4, 0.4, 0.4), roughness=0.2))
+        mats.append(material(MATTE, kd=(0.0, 0.0, 0.0)))
+        spheres += [((1.2, 1.6, 0.3), 0.5, 1), ((0.8, -1.5, -0.6), 0.45, 2)]
+        tri = _quad((1.5, -0.4, 1.6), (1.5, 0.4, 1.6), (1.5, 0.4, 2.2), (1.5, -0.4, 2.2), (-1, 0, 0))
+        tri_light = np.zeros(2, np.int32)
+        lights = np.zeros(1, LIGHT_DT)
+        lights[0]["intensity"] = (6.0, 5.0, 4.0)
+        lights[0]["two_sided"] = 0
+    sph = np.zeros(len(spheres), SPHERE_DT)
+    for i, (c, r, m) in enumerate(spheres):
+        sph[i]["center"], sph[i]["radius"], sph[i]["material_id"], sph[i]["light_id"] = c, r, m, -1
+    tri_mat = np.full(len(tri), len(mats) - 1, np.uint32)
+    cam = Camera((5.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 45.0, width, height)
+    env = EnvMap(environment_image(env_w, env_h, seed))
+    return SceneData(tri.astype(np.float32), tri_mat, tri_light, sph, np.stack(mats), lights, cam, spp=spp,
+                     max_depth=max_depth, rr_threshold=1.0, name="env_sphere" + ("_extra" if extra else ""),
+                     textures=tex, env=env)
 
 
 def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:

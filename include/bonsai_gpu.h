@@ -99,6 +99,19 @@ typedef struct bg_texture {
     float ds, dt;             /* PLANAR mapping offsets                                    */
 } bg_texture;
 
+/* InfiniteAreaLight (src/lights/infinite.rs:21-79): an environment map seen from every escaping
+ * ray and sampled by its luminance.  rgb: width*height*3 linear floats, rows top to bottom (row 0
+ * at theta = 0), powers of two (as image textures); texels are multiplied by intensity
+ * (Image::scale); light_to_world is the light's transform (row-major 3x4 affine, all zeros =
+ * identity).  The scene's light list is its emitting triangles in insertion order, then the
+ * infinite light. */
+typedef struct bg_infinite_light {
+    uint32_t width, height;
+    const float* rgb;
+    float intensity[3];
+    float light_to_world[12];
+} bg_infinite_light;
+
 /* Triangle mesh attributes (TriangleMesh, src/shapes/triangle.rs:17-90; TriangleOptions:40-45). */
 #define BG_TRI_REVERSE_ORIENTATION 1u /* TriangleOptions::reverse_orientation                   */
 #define BG_TRI_SWAPS_HANDEDNESS 2u    /* the mesh transform swaps handedness (det < 0)          */
@@ -274,6 +287,10 @@ bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t
 /* Appends a texture; materials refer to it as *id + 1.  Image texels are copied and their MIPMap
  * pyramid is built here (Image::generate_pyramid, src/io/image.rs:55-114). */
 bg_status bg_scene_add_texture(bg_scene* scene, const bg_texture* tex, uint32_t* id);
+/* Sets the scene's InfiniteAreaLight (at most one); texels are copied.  Its MIPMap and the 2D
+ * sampling distribution (InfiniteAreaLight::new) are built at commit, from the committed scene's
+ * bounds (the light's world radius). */
+bg_status bg_scene_add_infinite_light(bg_scene* scene, const bg_infinite_light* light);
 /* Appends n cylinders / disks / cones (GeometricPrimitive{Cylinder|Disk|Cone, material}). */
 bg_status bg_scene_add_quadrics(bg_scene* scene, const bg_quadric* quadrics, size_t n);
 /* Builds the BVH on the host, uploads scene and BVH to the device. */
@@ -291,7 +308,8 @@ typedef struct bg_tuning {
                                 cell before traversal (single-scene renders)                      */
 #define BG_TUNE_L2_PERSIST 2u /* keep the 8-wide BVH (nodes + leaf primitives) resident in L2 with a
                                  persisting access-policy window during renders; the set-aside
-                                 belongs to the context and ends with it                        */
+                                 belongs to the context and ends with it.  Off by default: on the
+                                 production frame it slows shading more than it helps traversal */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 

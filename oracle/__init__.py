@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         L.orc_scene_set_tri_attrs.argtypes = [P, P, P, P, P]
         L.orc_scene_add_texture.restype = C.c_int32
         L.orc_scene_add_texture.argtypes = [P, P]
+        L.orc_scene_add_infinite_light.restype = C.c_int32
+        L.orc_scene_add_infinite_light.argtypes = [P, P]
         L.orc_bvh_nodes.restype = C.c_int64
         L.orc_bvh_nodes.argtypes = [P]
         L.orc_num_lights.restype = C.c_int64
@@ -101,6 +103,10 @@ class OracleScene:
         for tex in sd.textures:
             tt, keep = S.texture_struct(tex)
             lib().orc_scene_add_texture(self.h, C.byref(tt))
+        if sd.env is not None:
+            el, keep = S.env_struct(sd.env)
+            if lib().orc_scene_add_infinite_light(self.h, C.byref(el)) != 0:
+                raise ValueError("a scene holds at most one infinite light")
 
     def __del__(self):
         if getattr(self, "h", None):

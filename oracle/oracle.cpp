@@ -337,6 +337,20 @@ struct Texture {
     float ds = 0, dt = 0;
     std::vector<Image> pyramid;
 };
+// InfiniteAreaLight (src/lights/infinite.rs:21-29) and its Distribution2D (sampling.rs:16-19)
+struct InfiniteLight {
+    Texture map;  // MIPMap of the scaled image, repeat wrap
+    Transform l2w, w2l;
+    V3 center;
+    float radius = 0.0f;
+    uint32_t nu = 0, nv = 0;
+    std::vector<float> func;      // nv rows of nu; conditional v's function is the tail from v * nu
+    std::vector<float> cond_cdf;  // nv rows of nu + 1
+    std::vector<float> cond_int;  // per-row integrals: the marginal's function
+    std::vector<float> marg_cdf;  // nv + 1
+    float marg_int = 0.0f;
+};
+constexpr int64_t LIGHT_INF = -1;  // the infinite light's entry in Scene::light_prims
 struct Scene {
     std::vector<V3> pos;  // 3 per triangle (TriangleMesh::position, triangle.rs:17-22)
     int64_t ntri = 0, nsph = 0, nquad = 0;
@@ -353,6 +367,8 @@ struct Scene {
     std::vector<float> tri_uv;         // 6 per triangle; empty: Triangle::get_uvs defaults
     std::vector<uint8_t> tri_flags;    // TA_* bits; empty: none
     std::vector<struct Texture> tex;
+    bool has_inf = false;
+    InfiniteLight inf;
     // BVH (src/accelerators/bvh.rs:20-31)
     struct Node {
         Bounds3 b;
@@ -1416,8 +1432,7 @@ static RGB mip_triangle(const Texture& t, size_t level, float st0, float st1) { 
            ds * (1.0f - dt) * mip_texel(t, level, s1, t0) + ds * dt * mip_texel(t, level, s1, t1);
 }
 // MIPMap::filter / trilinear_filter (mipmap.rs:103-128)
-static RGB mip_filter(const Texture& t, float st0, float st1, const float d0[2], const float d1[2]) {
-    float width = rmax(rmax(std::fabs(d0[0]), std::fabs(d0[1])), rmax(std::fabs(d1[0]), std::fabs(d1[1])));
+static RGB mip_trilinear(const Texture& t, float st0, float st1, float width) {
     const float top = (float)(t.pyramid.size() - 1);
     float level = top + std::log2(rmax(width, 1e-8f));
     if (level < 0.0f) return mip_triangle(t, 0, st0, st1);
@@ -1425,6 +1440,10 @@ static RGB mip_filter(const Texture& t, float st0, float st1, const float d0[2],
     size_t il = (size_t)std::floor(level);
     float f = level - std::floor(level);
     return (1.0f - f) * mip_triangle(t, il, st0, st1) + f * mip_triangle(t, il + 1, st0, st1);
+}
+static RGB mip_filter(const Texture& t, float st0, float st1, const float d0[2], const float d1[2]) {
+    float width = rmax(rmax(std::fabs(d0[0]), std::fabs(d0[1])), rmax(std::fabs(d1[0]), std::fabs(d1[1])));
+    return mip_trilinear(t, st0, st1, width);
 }
 // SphericalMapping2D::sphere / CylindricalMapping2D::cylinder (texture.rs:48-62)
 static void map_sphere(const Texture& t, V3 p, Mode mode, float st[2]) {
@@ -1629,9 +1648,96 @@ struct LightSample {
     Interaction p0, p1;
     bool vis = false;
 };
+// ---- InfiniteAreaLight (src/lights/infinite.rs) over Distribution2D (src/base/sampling.rs)
+// find_interval (math.rs:70-87): the last index i < size - 1 with cdf[i] <= u
+static size_t cdf_interval(const float* cdf, size_t size, float u) {
+    size_t lo = 0, len = size;
+    while (len > 0) {
+        size_t half = len / 2;
+        if (cdf[lo + half] <= u) {
+            lo = lo + half + 1;
+            len = len - half - 1;
+        } else {
+            len = half;
+        }
+    }
+    size_t r = lo == 0 ? 0 : lo - 1;  // cdf[0] = 0 <= u, so lo >= 1 for u >= 0
+    return r > size - 2 ? size - 2 : r;
+}
+// Distribution1D::sample_continuous (sampling.rs:53-76); count = Distribution1D::count
+static float d1_sample(const float* cdf, const float* func, float func_int, size_t n, size_t count, float u,
+                       float* pdf, size_t* off) {
+    size_t o = cdf_interval(cdf, n + 1, u);
+    if (off) *off = o;
+    float du = u - cdf[o];
+    if (cdf[o + 1] - cdf[o] > 0.0f) du /= cdf[o + 1] - cdf[o];
+    *pdf = func_int > 0.0f ? func[o] / func_int : 0.0f;
+    return ((float)o + du) / (float)count;
+}
+// Distribution2D::sample_continuous (sampling.rs:99-111).  F18 (REF): conditional v holds the
+// function's whole tail (func[v * nu..], sampling.rs:84), so its count is (nv - v) * nu.
+static void d2_sample(const InfiniteLight& L, float u0, float u1, Mode mode, float uv[2], float* pdf) {
+    float p1, p0;
+    size_t v = 0;
+    uv[1] = d1_sample(L.marg_cdf.data(), L.cond_int.data(), L.marg_int, L.nv, L.nv, u1, &p1, &v);
+    size_t count = mode == REF ? (size_t)(L.nv - v) * L.nu : L.nu;
+    uv[0] = d1_sample(&L.cond_cdf[v * (L.nu + 1)], &L.func[v * L.nu], L.cond_int[v], L.nu, count, u0, &p0, nullptr);
+    *pdf = p0 * p1;
+}
+// Distribution2D::pdf (sampling.rs:113-117).  F19 (REF): `p[0] as usize * count` truncates p
+// before scaling: the cell is 0 unless a coordinate is >= 1, and the column bound is conditional
+// 0's count (nv * nu under F18).  An index past row v's tail (a panic in the reference) reads the
+// function's last entry.
+static float d2_pdf(const InfiniteLight& L, float p0, float p1, Mode mode) {
+    size_t idx;
+    if (mode == REF) {
+        auto trunc = [](float x) -> size_t { return x >= 1.0f ? (size_t)x : 0; };
+        size_t cu = (size_t)L.nv * L.nu, cv = L.nv;
+        size_t u = std::min(trunc(p0) * cu, cu - 1), v = std::min(trunc(p1) * cv, cv - 1);
+        idx = std::min(v * L.nu + u, (size_t)L.nv * L.nu - 1);
+    } else {
+        int64_t u = (int64_t)(p0 * (float)L.nu), v = (int64_t)(p1 * (float)L.nv);
+        u = std::max<int64_t>(0, std::min<int64_t>(u, L.nu - 1));
+        v = std::max<int64_t>(0, std::min<int64_t>(v, L.nv - 1));
+        idx = (size_t)v * L.nu + (size_t)u;
+    }
+    return L.func[idx] / L.marg_int;
+}
+static float sph_theta(V3 v) { return std::acos(rclamp(v.z, -1.0f, 1.0f)); }  // geometry.rs:6-8
+static float sph_phi(V3 v) {                                                     // geometry.rs:10-17
+    float p = std::atan2(v.y, v.x);
+    return p < 0.0f ? p + 2.0f * PI : p;
+}
+// InfiniteAreaLight::radiance (infinite.rs:88-96)
+static RGB inf_radiance(const Scene& s, V3 dir) {
+    V3 w = normalize(xf_vec(s.inf.w2l, dir));
+    return mip_trilinear(s.inf.map, sph_phi(w) * (1.0f / (2.0f * PI)), sph_theta(w) * (1.0f / PI), 0.0f);
+}
+// Light::radiance summed over the scene's lights for an escaping ray: only the infinite light's
+// is non-zero (area lights return zero, light.rs:31-33).
+static RGB escaped_radiance(const Scene& s, V3 dir) { return s.has_inf ? inf_radiance(s, dir) : RGB(); }
+
 static LightSample light_sample_point(const Scene& s, int64_t prim, const Interaction& it, float u0, float u1,
                                       Mode mode) {  // diffuse.rs:54-87 + shape.rs:17-34
     LightSample ls;
+    if (prim == LIGHT_INF) {  // InfiniteAreaLight::sample_point (infinite.rs:98-153)
+        const InfiniteLight& L = s.inf;
+        float uv[2], map_pdf;
+        d2_sample(L, u0, u1, mode, uv, &map_pdf);
+        if (map_pdf == 0.0f) return ls;
+        float theta = uv[1] * PI, phi = uv[0] * 2.0f * PI;
+        float st = std::sin(theta), ct = std::cos(theta), sp = std::sin(phi), cp = std::cos(phi);
+        ls.wi = xf_vec(L.l2w, V3(st * cp, st * sp, ct));
+        ls.pdf = st == 0.0f ? 0.0f : map_pdf / (2.0f * PI * PI * st);
+        ls.radiance = mip_trilinear(L.map, uv[0], uv[1], 0.0f);
+        ls.p0 = it;
+        ls.p0.surface = false;
+        ls.p1 = Interaction();
+        ls.p1.p = it.p + ls.wi * (2.0f * L.radius);
+        ls.p1.time = it.time;
+        ls.vis = true;
+        return ls;
+    }
     float pdf_area;
     Interaction pit = tri_sample(s, prim, u0, u1, &pdf_area);
     V3 wi = pit.p - it.p;
@@ -1656,6 +1762,13 @@ static LightSample light_sample_point(const Scene& s, int64_t prim, const Intera
     return ls;
 }
 static float light_point_pdf(const Scene& s, int64_t prim, const Interaction& it, V3 wi, Mode mode) {  // shape.rs:40-57
+    if (prim == LIGHT_INF) {  // InfiniteAreaLight::point_pdf (infinite.rs:155-169)
+        V3 w = xf_vec(s.inf.w2l, wi);
+        float theta = sph_theta(w), phi = sph_phi(w);
+        float st = std::sin(theta);
+        if (st == 0.0f) return 0.0f;
+        return d2_pdf(s.inf, phi * (1.0f / (2.0f * PI)), theta * (1.0f / PI), mode) / (2.0f * PI * PI * st);
+    }
     Ray ray = spawn_ray(it, wi, mode);
     float t;
     Interaction iit;
@@ -1707,6 +1820,8 @@ static RGB estimate_direct(const Scene& s, const Interaction& it, const BSDF& bs
             RGB rad;
             if (scene_intersect(s, ray, &lit, cnt)) {
                 if (s.prim_emission[lit.prim] >= 0) rad = emitted_radiance(s, lit, -ls.wi);
+            } else if (light_prim == LIGHT_INF) {
+                rad = inf_radiance(s, ray.d);  // light.radiance(&ray)
             }
             if (!rad.is_black()) out = out + f * rad * w / scattering_pdf;
         }
@@ -1725,6 +1840,8 @@ static RGB estimate_direct(const Scene& s, const Interaction& it, const BSDF& bs
             RGB li;
             if (scene_intersect(s, ray, &lit, cnt)) {
                 if (lit.prim == light_prim) li = emitted_radiance(s, lit, -bs.wi);
+            } else if (light_prim == LIGHT_INF) {
+                li = inf_radiance(s, ray.d);
             }
             if (!li.is_black()) out = out + f * li * w / spdf;
         }
@@ -1797,7 +1914,7 @@ static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max
         bool hit = scene_intersect(s, ray, &it, cnt);
         if (bounces == 0 || specular_bounce) {
             if (hit) out = out + beta * emitted_radiance(s, it, -ray.d);
-            // lights' radiance(ray) is zero for area lights (light.rs:31-33)
+            else out = out + beta * escaped_radiance(s, ray.d);  // path.rs:81-83
         }
         if (!hit || bounces >= max_depth) break;
         compute_differentials(&it, (mode == REF || bounces == 0) ? rd0 : RayDifferential());
@@ -1849,7 +1966,7 @@ static RGB tree_radiance(const Scene& s, Ray ray, const RayDifferential& rd, Cou
     RGB out;
     Interaction it;
     if (cnt) cnt->ext_rays++;
-    if (!scene_intersect(s, ray, &it, cnt)) return out;  // area lights: Light::radiance is zero
+    if (!scene_intersect(s, ray, &it, cnt)) return escaped_radiance(s, ray.d);  // whitted.rs:45-51
     rng.stream = node - 1;
     compute_differentials(&it, rd);
     BSDF bsdf = make_bsdf(s, it, mode, false);  // allow_multiple_lobes = false
@@ -2055,6 +2172,63 @@ int32_t orc_scene_add_texture(void* p, const bg_texture* t) {
     }
     s.tex.push_back(std::move(x));
     return (int32_t)s.tex.size() - 1;
+}
+
+// InfiniteAreaLight::new (infinite.rs:38-80) with the scene's BVH bounds as the world bounds; the
+// light joins the end of the light list.
+int32_t orc_scene_add_infinite_light(void* p, const bg_infinite_light* l) {
+    Scene& s = *(Scene*)p;
+    if (s.has_inf) return -1;
+    InfiniteLight& L = s.inf;
+    L.map.kind = BG_TEXTURE_IMAGE;
+    L.map.wrap = BG_WRAP_REPEAT;
+    Image img;
+    img.w = (int)l->width;
+    img.h = (int)l->height;
+    img.px.assign(l->rgb, l->rgb + (size_t)l->width * l->height * 3);
+    for (size_t i = 0; i < img.px.size(); ++i) img.px[i] *= l->intensity[i % 3];  // Image::scale
+    L.map.pyramid = generate_pyramid(std::move(img));
+    L.nu = 2 * l->width;
+    L.nv = 2 * l->height;
+    const float fwidth = 0.5f / (float)std::min(L.nu, L.nv);
+    L.func.assign((size_t)L.nu * L.nv, 0.0f);
+    for (uint32_t v = 0; v < L.nv; ++v) {
+        float vp = ((float)v + 0.5f) / (float)L.nv;
+        float sin_theta = std::sin(PI * ((float)v + 0.5f) / (float)L.nv);
+        for (uint32_t u = 0; u < L.nu; ++u) {
+            float up = ((float)u + 0.5f) / (float)L.nu;
+            RGB c = mip_trilinear(L.map, up, vp, fwidth);
+            L.func[(size_t)v * L.nu + u] = c.y() * sin_theta;  // RGBSpectrum::y
+        }
+    }
+    // Distribution1D::new (sampling.rs:22-47) for each row, then the marginal
+    auto build = [](const float* f, uint32_t n, float* cdf) {
+        cdf[0] = 0.0f;
+        for (uint32_t i = 1; i <= n; ++i) cdf[i] = cdf[i - 1] + f[i - 1] / (float)n;
+        float integral = cdf[n];
+        for (uint32_t i = 1; i <= n; ++i) cdf[i] = integral == 0.0f ? (float)i / (float)n : cdf[i] / integral;
+        return integral;
+    };
+    L.cond_cdf.assign((size_t)L.nv * (L.nu + 1), 0.0f);
+    L.cond_int.assign(L.nv, 0.0f);
+    for (uint32_t v = 0; v < L.nv; ++v)
+        L.cond_int[v] = build(&L.func[(size_t)v * L.nu], L.nu, &L.cond_cdf[(size_t)v * (L.nu + 1)]);
+    L.marg_cdf.assign(L.nv + 1, 0.0f);
+    L.marg_int = build(L.cond_int.data(), L.nv, L.marg_cdf.data());
+    L.l2w.m = Mat4::identity();
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) L.l2w.m.m[r][c] = l->light_to_world[4 * r + c];
+    L.l2w.mi = mat_inverse(L.l2w.m);
+    L.w2l = t_inverse(L.l2w);
+    // Bounds3::bounding_sphere (bounds3.rs:208-215) of the BVH's root bounds
+    Bounds3 b = s.nodes.empty() ? Bounds3() : s.nodes[0].b;
+    V3 c = (b.mn + b.mx) * (1.0f / 2.0f);
+    bool inside = c.x >= b.mn.x && c.x <= b.mx.x && c.y >= b.mn.y && c.y <= b.mx.y && c.z >= b.mn.z && c.z <= b.mx.z;
+    L.center = c;
+    L.radius = inside ? length(c - b.mx) : 0.0f;
+    s.has_inf = true;
+    s.light_prims.push_back(LIGHT_INF);
+    return 0;
 }
 
 void orc_scene_destroy(void* p) { delete (Scene*)p; }

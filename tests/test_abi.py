@@ -15,7 +15,7 @@ from .conftest import ROOT
 HEADER = ROOT / "include" / "bonsai_gpu.h"
 STRUCTS = ["bg_material", "bg_area_light", "bg_sphere", "bg_camera", "bg_render_opts", "bg_render_stats",
            "bg_ray", "bg_hit", "bg_device_opts", "bg_build_stats", "bg_tuning", "bg_quadric", "bg_guide_opts",
-           "bg_guide_stats", "bg_batch_item", "bg_texture", "bg_obj_info"]
+           "bg_guide_stats", "bg_batch_item", "bg_texture", "bg_obj_info", "bg_infinite_light"]
 
 
 def declared_functions():
