@@ -160,3 +160,29 @@ def test_batch_and_guided_refuse_infinite_lights(gpu_ctx):
             g.close()
     finally:
         sc.close()
+
+
+@pytest.mark.parametrize("mode,bvh", [(A.BG_MODE_PBRT, A.BG_BVH_WIDE),
+                                      (A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE_FIXED)])
+def test_rotated_and_tinted_environment(gpu_ctx, mode, bvh):
+    """A light_to_world rotation (the map's pole tilted 35 degrees about x, then turned 70 degrees
+    about z) and a per-channel intensity, against the oracle."""
+    sd = S.env_sphere(40, 40, spp=16, max_depth=4, extra=True, seed=5)
+    rot = S.rotation((0, 0, 1), 70.0) @ S.rotation((1, 0, 0), 35.0)
+    sd.env.light_to_world = rot[:3].astype(np.float32)
+    sd.env.intensity = (1.5, 1.0, 0.6)
+    r, o, cmp = _pair(gpu_ctx, sd, A.BG_INTEGRATOR_PATH, 0, mode, bvh, 16)
+    print(cmp)
+    assert cmp["frac_z3"] <= Z3_FRAC
+    assert cmp["frac_close"] >= 0.85
+
+
+def test_environment_map_shapes(gpu_ctx):
+    """Degenerate maps: 1 x 1 (a single level, a 2 x 2 distribution), 1 x 64 and 64 x 1."""
+    for h, w in ((1, 1), (1, 64), (64, 1), (2, 4)):
+        sd = S.env_sphere(24, 24, spp=8, max_depth=3)
+        rng = np.random.default_rng(h * 100 + w)
+        sd.env.rgb = (0.2 + rng.random((h, w, 3))).astype(np.float32)
+        r, o, cmp = _pair(gpu_ctx, sd, A.BG_INTEGRATOR_PATH, 0, A.BG_MODE_PBRT, A.BG_BVH_WIDE, 8)
+        assert cmp["frac_z3"] <= Z3_FRAC, (h, w, cmp)
+        assert cmp["frac_close"] >= 0.85, (h, w, cmp)
