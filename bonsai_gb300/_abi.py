@@ -41,6 +41,7 @@ BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
 BG_TUNE_SORT_RAYS = 1
 BG_TUNE_L2_PERSIST = 2
+BG_SAMPLER_INDEPENDENT, BG_SAMPLER_STRATIFIED = 0, 1
 
 BG_TEXTURE_IMAGE = 0
 BG_TEXTURE_UV = 1
@@ -121,7 +122,9 @@ class bg_camera(C.Structure):
 class bg_render_opts(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("rr_threshold", C.c_float),
                 ("mode", C.c_uint32), ("seed", C.c_uint64), ("first_sample", C.c_uint32),
-                ("flags", C.c_uint32), ("integrator", C.c_uint32), ("light_strategy", C.c_uint32)]
+                ("flags", C.c_uint32), ("integrator", C.c_uint32), ("light_strategy", C.c_uint32),
+                ("sampler", C.c_uint32), ("x_pixel_samples", C.c_uint32), ("y_pixel_samples", C.c_uint32),
+                ("sampled_dimensions", C.c_uint32), ("jitter_samples", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class bg_render_stats(C.Structure):

@@ -1281,6 +1281,14 @@ bg_status bgi::validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* 
     if (o->light_strategy > BG_LIGHT_UNIFORM_ONE) return fail(ctx, BG_ERR_INVALID, "unknown light strategy");
     if (o->integrator != BG_INTEGRATOR_PATH && o->max_depth > bg::TREE_MAX_DEPTH)
         return fail(ctx, BG_ERR_INVALID, "the Whitted and direct-lighting integrators accept max_depth <= 30");
+    bg::StratParams sp;
+    if (const char* why = bg::strat_params(o->sampler, o->spp, o->x_pixel_samples, o->y_pixel_samples,
+                                           o->sampled_dimensions, o->jitter_samples, &sp))
+        return fail(ctx, BG_ERR_INVALID, why);
+    if (o->integrator != BG_INTEGRATOR_PATH && sp.dims > 1)
+        return fail(ctx, BG_ERR_UNSUPPORTED,
+                    "the Whitted and direct-lighting integrators take sampled_dimensions <= 1 (the camera sample): "
+                    "the reference's later calls follow its depth-first recursion");
     if (!(o->flags & BG_RENDER_NO_READBACK) && !rgb_out) return BG_ERR_INVALID;
     return BG_OK;
 }
@@ -1301,6 +1309,8 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
                         {0, 0, 0}, {0, 0, 0}};
     scene_bounds(s, rp.bmin, rp.binv);
     rp = bg::with_camera(rp, dc, o->spp);
+    bg::strat_params(o->sampler, o->spp, o->x_pixel_samples, o->y_pixel_samples, o->sampled_dimensions,
+                     o->jitter_samples, &rp.strat);  // checked by validate_render
     const uint64_t npix = (uint64_t)cam->width * cam->height;
     const uint64_t total = npix * o->spp;
     uint64_t launches = 0;
@@ -1490,6 +1500,8 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         if (it.opts.mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs BG_MODE_PBRT");
         if (it.opts.integrator != BG_INTEGRATOR_PATH)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering runs the path integrator only");
+        if (it.opts.sampler != BG_SAMPLER_INDEPENDENT)
+            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering takes the independent sampler only");
         if (it.scene->dev.ntex || it.scene->has_inf)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering does not support textured scenes or infinite lights");
         total_pix += (uint64_t)it.camera.width * it.camera.height;

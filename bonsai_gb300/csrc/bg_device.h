@@ -122,6 +122,13 @@ struct InfLight {
 // Light-list entry of the infinite light in Scene::light_prims (area lights hold their triangle).
 constexpr uint32_t LIGHT_INFINITE = 0xFFFFFFFFu;
 
+// StratifiedSampler options of a render (src/samplers/stratified.rs:32-37).
+struct StratParams {
+    uint32_t dims;    // sampled_dimensions (0: every call draws from the counter RNG)
+    uint32_t nx, ny;  // x_pixel_samples, y_pixel_samples
+    uint32_t jitter;  // jitter_samples
+};
+
 struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-175)
     float r2c[4][4];  // raster_to_camera.m
     float c2w[4][4];  // camera_to_world.m

@@ -578,6 +578,8 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering runs the path integrator only");
     if (s->dev.ntex) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering does not support textured scenes");
     if (s->has_inf) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering does not support infinite lights");
+    if (o->sampler != BG_SAMPLER_INDEPENDENT)
+        return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering takes the independent sampler only");
     CK(cudaSetDevice(ctx->device));
     if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
     if (!(o->flags & BG_RENDER_ACCUMULATE)) {

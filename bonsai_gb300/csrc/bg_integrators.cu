@@ -137,10 +137,9 @@ __global__ void __launch_bounds__(128) k_tree(Scene sc, Camera cam, RenderParams
         const uint32_t pix = (uint32_t)(item % npix);
         const uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, 0u};
-        float c[4];
-        rng.block(0, c);
-        const float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-        const Ray ray = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+        const CameraUs cu = camera_us(rp.strat, REF, rng);  // sampled_dimensions <= 1: camera only
+        const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
+        const Ray ray = camera_ray(cam, fx, fy, cu.time);
         RayDiff rd;
         if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale);
         RGB L = tree_radiance<REF, LAYOUT>(sc, rp, kind, ray, sc.ntex ? &rd : nullptr, pix, s, err);

@@ -135,7 +135,8 @@ BG_D BSDF path_bsdf(const Scene& sc, const RenderParams& rp, uint32_t pix, uint3
 // ray never re-spawns, F1) and only has at the first hit in PBRT mode.
 template <bool REF>
 BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_depth, float rr_threshold,
-                      uint32_t* err, const RayDiff* rd0) {
+                      uint32_t* err, const RayDiff* rd0, const StratParams& sp) {
+    SamplerCalls calls{sp, REF, rng.pixel, rng.sample, rng.seed, 1u, 2u};  // after the camera sample
     RGB out = rgb(0.0f), beta = rgb(1.0f);
     bool specular_bounce = false;
     float eta_scale = 1.0f;
@@ -157,6 +158,9 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
         rng.block(base, u);
         rng.block(base + 4, u + 4);
         if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
+            calls.get_1d(u[BD_LIGHT]);
+            calls.get_2d(u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+            calls.get_2d(u[BD_USCAT], u[BD_USCAT + 1]);
             float count = (float)sc.nlights;
             uint32_t li = (uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f);
             float lpdf = 1.0f / count;
@@ -165,6 +169,7 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
             out = out + beta * (ld / lpdf);
         }
         V3 wo = -ray.d;
+        calls.get_2d(u[BD_BSDF], u[BD_BSDF + 1]);
         BxSample bs = bsdf.sample<REF>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
         if (is_black(bs.f) || bs.pdf == 0.0f) break;
         beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
@@ -177,6 +182,7 @@ BG_D RGB radiance_ref(const Scene& sc, Ray ray, const Rng& rng, uint32_t max_dep
         if (!REF) ray = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
         RGB rr_beta = beta * eta_scale;
         if (max_value(rr_beta) < rr_threshold && bounces > 3) {
+            calls.get_1d(u[BD_RR]);
             float q = rmax(1.0f - max_value(rr_beta), 0.5f);
             if (u[BD_RR] < q) break;
             beta = beta / (1.0f - q);
@@ -195,13 +201,13 @@ __global__ void __launch_bounds__(128) k_megakernel(Scene sc, Camera cam, Render
         uint32_t pix = (uint32_t)(item % npix);
         uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         Rng rng{pix, s, rp.seed};
-        float c[4];
-        rng.block(0, c);
-        float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-        Ray ray = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+        const CameraUs cu = camera_us(rp.strat, REF, rng);
+        float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
+        Ray ray = camera_ray(cam, fx, fy, cu.time);
         RayDiff rd;
         if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale);
-        RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err, sc.ntex ? &rd : nullptr);
+        RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err, sc.ntex ? &rd : nullptr,
+                                  rp.strat);
         film_add(film, pix, L);
     }
 }
@@ -215,9 +221,15 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 
 // ================================================================ wavefront (PBRT)
 // Path state word: bits 0-7 bounce, 8 specular bounce, 9 pending NEE contribution, 10 open
-// training record, 12-15 training records written.
+// training record, 12-15 training records written, 16-23 / 24-31 the sampler's get_1d / get_2d
+// calls so far (saturating at 255; calls below sampled_dimensions take stratified values).
 enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10 };
 constexpr uint32_t ST_REC_SHIFT = 12, ST_REC_MASK = 0xFu << ST_REC_SHIFT;
+BG_D uint32_t st_k1(uint32_t st) { return (st >> 16) & 0xFFu; }
+BG_D uint32_t st_k2(uint32_t st) { return st >> 24; }
+BG_D uint32_t st_set_k(uint32_t st, uint32_t k1, uint32_t k2) {
+    return (st & 0xFFFFu) | (min(k1, 255u) << 16) | (min(k2, 255u) << 24);
+}
 enum : uint32_t {
     C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6,
     C_GUIDE = 11,  // 11..13: guided queries of the matte, plastic and conductor classes
@@ -238,15 +250,14 @@ constexpr int CLS_MISS = 4;
 BG_D void generate_one(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint32_t i, uint32_t pix,
                        uint32_t s) {
     Rng rng{pix, s, rp.seed};
-    float c[4];
-    rng.block(0, c);
-    float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-    Ray r = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+    const CameraUs cu = camera_us(rp.strat, false, rng);
+    float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
+    Ray r = camera_ray(cam, fx, fy, cu.time);
     wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
     wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
     wb.pixel[i] = pix;
     wb.sample[i] = s;
-    wb.state[i] = 0;
+    wb.state[i] = st_set_k(0u, 1u, 2u);  // the camera sample made one get_1d and two get_2d calls
     wb.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
     wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     wb.queue[0][i] = i;
@@ -586,7 +597,11 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     rng.block(ub, u);
     rng.block(ub + 4, u + 4);
     BSDF bsdf = path_bsdf<CLS, TEX>(sc, rp, wb.pixel[slot], wb.sample[slot], bounce, ray, it);
+    SamplerCalls calls{rp.strat, false, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state)};
     if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
+        calls.get_1d(u[BD_LIGHT]);
+        calls.get_2d(u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+        calls.get_2d(u[BD_USCAT], u[BD_USCAT + 1]);
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
         float count = (float)sc.nlights;
         uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
@@ -653,6 +668,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         state |= ST_PENDING;
     }
     V3 wo = -ray.d;
+    calls.get_2d(u[BD_BSDF], u[BD_BSDF + 1]);
     BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
     if (is_black(bs.f) || bs.pdf == 0.0f) {
         out.finished = true;
@@ -668,6 +684,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
     RGB rr_beta = beta * eta_scale;
     if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
+        calls.get_1d(u[BD_RR]);
         float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
         if (u[BD_RR] < qq) {
             out.finished = true;
@@ -678,6 +695,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
+    state = st_set_k(state, calls.k1, calls.k2);
     if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
     out.cont = true;
 }

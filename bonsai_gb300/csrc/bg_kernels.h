@@ -17,8 +17,23 @@ struct RenderParams {
     float bmin[3], binv[3];  // scene bounds, for ray binning: cell = (p - bmin) * binv in [0,1)
     Camera cam;              // for the camera rays' differentials at the first hit (textures)
     float diff_scale;        // Ray::scale_differentials factor, 1 / sqrt(samples per pixel)
+    StratParams strat;       // StratifiedSampler (dims = 0: the counter RNG alone)
     uint32_t pad;            // keeps the struct free of tail padding (it is hashed as graph key)
 };
+// StratParams of a render's sampler options (sampler 0 independent, 1 stratified): nullptr when
+// they are valid, otherwise why not.
+inline const char* strat_params(uint32_t sampler, uint32_t spp, uint32_t nx, uint32_t ny, uint32_t dims,
+                                uint32_t jitter, StratParams* sp) {
+    *sp = StratParams{0u, 1u, 1u, 0u};
+    if (sampler > 1) return "unknown sampler";
+    if (sampler == 0) return nullptr;
+    if (nx == 0 || ny == 0 || (uint64_t)nx * ny != spp)
+        return "the stratified sampler needs spp == x_pixel_samples * y_pixel_samples";
+    if (dims > 64) return "the stratified sampler accepts sampled_dimensions <= 64";
+    if (jitter > 1) return "jitter_samples must be 0 or 1";
+    *sp = StratParams{dims, nx, ny, jitter};
+    return nullptr;
+}
 // RenderParams for a render call: camera and differential scale filled in.
 inline RenderParams with_camera(RenderParams rp, const Camera& cam, uint32_t total_spp) {
     rp.cam = cam;

@@ -8,6 +8,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bg_device.h"
+
 #define BG_HD __host__ __device__ __forceinline__
 #define BG_D __device__ __forceinline__
 
@@ -201,10 +203,113 @@ struct Rng {
         block(dim & ~3u, b);
         return b[dim & 3];
     }
+    BG_D uint32_t bits(uint32_t dim) const {  // the raw 32 bits behind u(dim)
+        uint32_t c[4] = {sample, dim >> 2, (uint32_t)(seed >> 32), 0x626F6E73u ^ stream};
+        philox4x32_10(c, pixel, (uint32_t)seed);
+        return c[dim & 3];
+    }
 };
+
 // Dimension schedule shared with the CPU oracle: camera film.xy 0-1, lens 2-3, time 4;
 // bounce b: base 8+8b: light pick +0, u_light +1..2, u_scattering +3..4, BSDF +5..6, roulette +7.
 constexpr uint32_t DIM_FILM = 0, DIM_TIME = 4, DIM_BOUNCE0 = 8, DIMS_PER_BOUNCE = 8;
 constexpr uint32_t BD_LIGHT = 0, BD_ULIGHT = 1, BD_USCAT = 3, BD_BSDF = 5, BD_RR = 7;
+
+// ---- StratifiedSampler (src/samplers/stratified.rs:75-137, src/base/sampling.rs:120-179) without
+// per-pixel arrays.  The samples of a pixel form passes of spp = nx * ny (pass = sample / spp); in
+// each pass, stratified dimension k of sample s takes stratum perm_k(s % spp), jittered inside the
+// stratum (1D: spp strata of [0, 1); 2D: an nx x ny grid).  perm_k is the identity in REF_COMPAT
+// mode (F6: shuffle never swaps, so every dimension walks the strata in the same order) and a
+// keyed permutation in PBRT mode.  Random numbers come from the counter RNG on stream
+// 0x80000000 | 2k | is_2d: dimension 0 keys the permutation, 4 + 2j and 5 + 2j jitter stratum j.
+// A bijection of [0, n) keyed by `key`: a keyed bijection of [0, 2^b) (xor, odd multiply, xorshift,
+// add; each invertible modulo 2^b) iterated until it lands below n (cycle walking: the cycle through
+// i < n returns to [0, n) within 2^b steps).
+BG_HD uint32_t strat_permute(uint32_t i, uint32_t n, uint32_t key) {
+    if (n <= 1) return 0;
+    uint32_t b = 0;
+    while ((1u << b) < n) ++b;
+    const uint32_t mask = b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u;
+    const uint32_t sh = (b + 1) / 2;
+    uint32_t x = i;
+    for (uint32_t it = 0; it <= mask; ++it) {
+        x = (x ^ key) & mask;
+        x = (x * 0x2F5A6B1Du) & mask;
+        x ^= x >> sh;
+        x = (x + (key >> 7)) & mask;
+        x = (x * 0x6C8E9CF5u) & mask;
+        x ^= x >> sh;
+        x = (x ^ (key >> 13) ^ 0x5BD1E995u) & mask;
+        x = (x * 0x1B873593u) & mask;
+        x ^= x >> sh;
+        if (x < n) return x;
+    }
+    return i;  // not reached
+}
+BG_D uint32_t strat_stratum(const StratParams& sp, bool ref, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k,
+                            uint32_t is2d, Rng* jr) {
+    const uint32_t n = sp.nx * sp.ny;
+    const uint32_t s = sample % n;
+    *jr = Rng{pix, sample / n, seed, 0x80000000u | (k << 1) | is2d};
+    return ref ? s : strat_permute(s, n, jr->bits(0));
+}
+// get_1d / get_2d for stratified dimension k (k < sp.dims).
+BG_D float strat_1d(const StratParams& sp, bool ref, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k) {
+    Rng jr;
+    const uint32_t j = strat_stratum(sp, ref, pix, sample, seed, k, 0u, &jr);
+    const float delta = sp.jitter ? jr.u(4 + 2 * j) : 0.5f;
+    const float inv = 1.0f / (float)(sp.nx * sp.ny);
+    return rmin(((float)j + delta) * inv, ONE_MINUS_EPSILON);
+}
+BG_D float2 strat_2d(const StratParams& sp, bool ref, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k) {
+    Rng jr;
+    const uint32_t j = strat_stratum(sp, ref, pix, sample, seed, k, 1u, &jr);
+    const float jx = sp.jitter ? jr.u(4 + 2 * j) : 0.5f, jy = sp.jitter ? jr.u(5 + 2 * j) : 0.5f;
+    const float dx = 1.0f / (float)sp.nx, dy = 1.0f / (float)sp.ny;
+    return make_float2(rmin(((float)(j % sp.nx) + jx) * dx, ONE_MINUS_EPSILON),
+                       rmin(((float)(j / sp.nx) + jy) * dy, ONE_MINUS_EPSILON));
+}
+// A sample's sampler calls in the reference's order: get_1d / get_2d number k1 / k2 take stratified
+// values while below sp.dims and otherwise keep the counter RNG's value already in place.
+struct SamplerCalls {
+    const StratParams& sp;
+    bool ref;
+    uint32_t pix, sample;
+    uint64_t seed;
+    uint32_t k1, k2;
+    BG_D void get_1d(float& v) {
+        if (k1 < sp.dims) v = strat_1d(sp, ref, pix, sample, seed, k1);
+        ++k1;
+    }
+    BG_D void get_2d(float& a, float& b) {
+        if (k2 < sp.dims) {
+            const float2 t = strat_2d(sp, ref, pix, sample, seed, k2);
+            a = t.x;
+            b = t.y;
+        }
+        ++k2;
+    }
+};
+// The sampler calls a camera sample makes (Sampler::get_camera_sample: film get_2d, lens get_2d,
+// time get_1d): the film offset and the time, from the stratified sampler or the counter RNG.
+struct CameraUs {
+    float fx, fy, time;
+};
+BG_D CameraUs camera_us(const StratParams& sp, bool ref, const Rng& rng) {
+    CameraUs c;
+    if (sp.dims > 0) {
+        float2 f = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
+        c.fx = f.x;
+        c.fy = f.y;
+        c.time = strat_1d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
+    } else {
+        float b[4];
+        rng.block(0, b);
+        c.fx = b[0];
+        c.fy = b[1];
+        c.time = rng.u(DIM_TIME);
+    }
+    return c;
+}
 
 }  // namespace bg

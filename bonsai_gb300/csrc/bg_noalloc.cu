@@ -123,6 +123,10 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
         return reject(BG_ERR_UNSUPPORTED, "accumulate / stage timing / graph flags need bg_render");
     if (o->integrator != BG_INTEGRATOR_PATH)
         return reject(BG_ERR_UNSUPPORTED, "the Whitted and direct-lighting integrators need bg_render");
+    StratParams strat;
+    if (const char* why = strat_params(o->sampler, o->spp, o->x_pixel_samples, o->y_pixel_samples,
+                                       o->sampled_dimensions, o->jitter_samples, &strat))
+        return reject(BG_ERR_INVALID, why);
 
     int prev = -1;
     cudaGetDevice(&prev);
@@ -183,6 +187,7 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     Camera dc = camera_for(*cam);
     RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
     rp = with_camera(rp, dc, o->spp);
+    rp.strat = strat;
     const uint64_t total = npix * o->spp;
     if (total > 0) {
         if (o->mode == BG_MODE_PBRT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2)) {

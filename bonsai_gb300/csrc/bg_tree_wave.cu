@@ -67,10 +67,9 @@ __global__ void k_tw_gen(Camera cam, RenderParams rp, TreeWave tw, uint64_t item
         const uint64_t item = item0 + i;
         const uint32_t pix = (uint32_t)(item % npix), s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, 0u};
-        float c[4];
-        rng.block(0, c);
-        const float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-        const Ray r = camera_ray(cam, fx, fy, rng.u(DIM_TIME));
+        const CameraUs cu = camera_us(rp.strat, false, rng);  // sampled_dimensions <= 1: camera only
+        const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
+        const Ray r = camera_ray(cam, fx, fy, cu.time);
         tw.ray_o[0][i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
         tw.ray_d[0][i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
         tw.beta[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);

@@ -180,9 +180,10 @@ class PathIntegrator:
     light_strategy = 0
 
     def __init__(self, camera: S.Camera, spp: int, max_depth: int, rr_threshold: float = 1.0,
-                 mode: int = A.BG_MODE_PBRT, seed: int = 0):
+                 mode: int = A.BG_MODE_PBRT, seed: int = 0, sampler: S.StratifiedSampler | None = None):
         self.camera, self.spp, self.max_depth = camera, spp, max_depth
         self.rr_threshold, self.mode, self.seed = rr_threshold, mode, seed
+        self.sampler = sampler
 
     def render(self, scene: Scene, first_sample: int = 0, accumulate: bool = False, readback: bool = True,
                spp: int | None = None, graph: bool = False, stage_timing: bool = False) -> RenderResult:
@@ -196,6 +197,7 @@ class PathIntegrator:
         o.seed = self.seed
         o.first_sample = first_sample
         o.integrator, o.light_strategy = self.integrator, self.light_strategy
+        S.set_sampler(o, self.sampler)
         o.flags = ((A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK) |
                    (A.BG_RENDER_GRAPH if graph else 0) | (A.BG_RENDER_STAGE_TIMING if stage_timing else 0))
         rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
@@ -215,6 +217,7 @@ class PathIntegrator:
         o.mode = self.mode
         o.seed = self.seed
         o.first_sample = first_sample
+        S.set_sampler(o, self.sampler)
         o.flags = (A.BG_RENDER_ACCUMULATE if accumulate else 0) | (0 if readback else A.BG_RENDER_NO_READBACK)
         rgb = np.zeros((self.camera.height, self.camera.width, 3), np.float32) if readback else None
         st = A.bg_render_stats()
@@ -237,8 +240,9 @@ class WhittedIntegrator(PathIntegrator):
 
     integrator = A.BG_INTEGRATOR_WHITTED
 
-    def __init__(self, camera: S.Camera, spp: int, max_depth: int, mode: int = A.BG_MODE_PBRT, seed: int = 0):
-        super().__init__(camera, spp, max_depth, 1.0, mode, seed)
+    def __init__(self, camera: S.Camera, spp: int, max_depth: int, mode: int = A.BG_MODE_PBRT, seed: int = 0,
+                 sampler: S.StratifiedSampler | None = None):
+        super().__init__(camera, spp, max_depth, 1.0, mode, seed, sampler)
 
 
 class DirectLightingIntegrator(PathIntegrator):
@@ -248,8 +252,8 @@ class DirectLightingIntegrator(PathIntegrator):
     integrator = A.BG_INTEGRATOR_DIRECT
 
     def __init__(self, camera: S.Camera, spp: int, max_depth: int, strategy: int = A.BG_LIGHT_UNIFORM_ALL,
-                 mode: int = A.BG_MODE_PBRT, seed: int = 0):
-        super().__init__(camera, spp, max_depth, 1.0, mode, seed)
+                 mode: int = A.BG_MODE_PBRT, seed: int = 0, sampler: S.StratifiedSampler | None = None):
+        super().__init__(camera, spp, max_depth, 1.0, mode, seed, sampler)
         self.light_strategy = strategy
 
 
@@ -353,6 +357,7 @@ class BatchJob:
     rr_threshold: float = 1.0
     seed: int = 0
     first_sample: int = 0
+    sampler: S.StratifiedSampler | None = None
 
 
 def render_batch(ctx: Context, jobs: list, readback: bool = True):
@@ -365,6 +370,7 @@ def render_batch(ctx: Context, jobs: list, readback: bool = True):
         it.camera = camera_struct(j.camera)
         it.opts.spp, it.opts.max_depth, it.opts.rr_threshold = j.spp, j.max_depth, j.rr_threshold
         it.opts.mode, it.opts.seed, it.opts.first_sample, it.opts.flags = A.BG_MODE_PBRT, j.seed, j.first_sample, 0
+        S.set_sampler(it.opts, j.sampler)
         img = np.zeros((j.camera.height, j.camera.width, 3), np.float32) if readback else None
         it.rgb_out = img.ctypes.data if img is not None else None
         outs.append(img)

@@ -75,6 +75,29 @@ def texture_struct(t: "Texture"):
 
 
 @dataclass
+class StratifiedSampler:
+    """StratifiedSamplerOptions (src/samplers/stratified.rs:32-37); spp = x * y."""
+    x_pixel_samples: int
+    y_pixel_samples: int
+    sampled_dimensions: int
+    jitter_samples: bool = True
+
+    @property
+    def spp(self) -> int:
+        return self.x_pixel_samples * self.y_pixel_samples
+
+
+def set_sampler(o, sampler: "StratifiedSampler | None"):
+    """Fills a bg_render_opts' sampler fields (None: the independent counter-RNG sampler)."""
+    if sampler is None:
+        o.sampler = 0
+        return
+    o.sampler = 1
+    o.x_pixel_samples, o.y_pixel_samples = sampler.x_pixel_samples, sampler.y_pixel_samples
+    o.sampled_dimensions, o.jitter_samples = sampler.sampled_dimensions, int(bool(sampler.jitter_samples))
+
+
+@dataclass
 class EnvMap:
     """bg_infinite_light: an environment map (rgb of shape (h, w, 3), power-of-two sizes, row 0 at
     theta = 0) scaled by `intensity`, oriented by a 3x4 light_to_world (src/lights/infinite.rs)."""

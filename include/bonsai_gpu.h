@@ -178,7 +178,24 @@ typedef struct bg_render_opts {
     uint32_t flags;        /* BG_RENDER_* bits                                            */
     uint32_t integrator;   /* bg_integrator (0 = PathIntegrator)                          */
     uint32_t light_strategy; /* direct lighting: bg_light_strategy                        */
+    uint32_t sampler;      /* bg_sampler                                                  */
+    uint32_t x_pixel_samples, y_pixel_samples; /* StratifiedSampler: spp = x * y             */
+    uint32_t sampled_dimensions; /* StratifiedSampler: stratified get_1d / get_2d calls     */
+    uint32_t jitter_samples;     /* StratifiedSampler: jitter inside the strata (0 / 1)     */
+    uint32_t reserved;
 } bg_render_opts;
+
+/* The sampler (src/base/sampler.rs).  INDEPENDENT: every get_1d / get_2d call of a sample draws
+ * from the counter-based RNG keyed by (pixel, sample, dimension).  STRATIFIED: StratifiedSampler
+ * (src/samplers/stratified.rs): the first sampled_dimensions get_1d calls and get_2d calls of each
+ * sample (camera film, lens and time first, then the path's calls in the reference's order) take
+ * stratified values over the pixel's spp = x_pixel_samples * y_pixel_samples samples; later calls
+ * draw from the counter RNG.  In REF_COMPAT mode every dimension visits the strata in the same
+ * order (the reference's shuffle never swaps); in PBRT mode each dimension is permuted.  Strata are
+ * defined per aligned block of spp samples (first_sample a multiple of spp starts a new block).
+ * Whitted and direct lighting accept sampled_dimensions <= 1 (the camera sample's calls); guided
+ * and batch renders take the independent sampler only. */
+typedef enum bg_sampler { BG_SAMPLER_INDEPENDENT = 0, BG_SAMPLER_STRATIFIED = 1 } bg_sampler;
 
 /* The SamplerIntegrator behind bg_render.  PATH = PathIntegrator (src/integrators/path.rs);
  * WHITTED = WhittedIntegrator (src/integrators/whitted.rs): emission, every light sampled once

@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         L.orc_scene_set_tri_attrs.argtypes = [P, P, P, P, P]
         L.orc_scene_add_texture.restype = C.c_int32
         L.orc_scene_add_texture.argtypes = [P, P]
+        L.orc_strat_sample.restype = C.c_int32
+        L.orc_strat_sample.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, P]
         L.orc_scene_add_infinite_light.restype = C.c_int32
         L.orc_scene_add_infinite_light.argtypes = [P, P]
         L.orc_bvh_nodes.restype = C.c_int64
@@ -132,7 +134,7 @@ class OracleScene:
     def render(self, mode: int, spp: int | None = None, seed: int = 0, first_sample: int = 0,
                rows: tuple[int, int, int] | None = None, threads: int = 0, count_traversal: bool = False,
                camera: S.Camera | None = None, max_depth: int | None = None, integrator: int = 0,
-               light_strategy: int = 0):
+               light_strategy: int = 0, sampler: S.StratifiedSampler | None = None):
         """Returns dict(rgb, sum, sumsq, counters).  rows = (y0, y1, ystep) restricts the rendered rows."""
         sd = self.sd
         cam = camera or sd.camera
@@ -146,14 +148,16 @@ class OracleScene:
         o.first_sample = first_sample
         o.flags = 0
         o.integrator, o.light_strategy = integrator, light_strategy
+        S.set_sampler(o, sampler)
         W, H = cam.width, cam.height
         rgb = np.zeros((H, W, 3), np.float32)
         s1 = np.zeros((H, W, 3), np.float64)
         s2 = np.zeros((H, W, 3), np.float64)
         cnt = np.zeros(7, np.int64)
         y0, y1, ys = rows if rows else (0, H, 1)
-        lib().orc_render(self.h, C.byref(c), C.byref(o), y0, y1, ys, threads, int(count_traversal),
-                         _ptr(rgb), _ptr(s1), _ptr(s2), _ptr(cnt))
+        if lib().orc_render(self.h, C.byref(c), C.byref(o), y0, y1, ys, threads, int(count_traversal),
+                            _ptr(rgb), _ptr(s1), _ptr(s2), _ptr(cnt)) != 0:
+            raise ValueError("the stratified sampler needs spp == x_pixel_samples * y_pixel_samples")
         return {"rgb": rgb, "sum": s1, "sumsq": s2, "counters": cnt, "spp": o.spp}
 
 
@@ -195,3 +199,15 @@ def camera_ray(cam: S.Camera, fx: float, fy: float, tu: float = 0.0) -> np.ndarr
 
 def threads_available() -> int:
     return os.cpu_count() or 1
+
+
+def strat_sample(sampler: S.StratifiedSampler, mode: int, pixel: int, sample: int, k: int, is2d: bool,
+                 seed: int = 0) -> np.ndarray:
+    """The stratified sampler's value of stratified dimension k for (pixel, sample): (2,) floats."""
+    o = bg_render_opts()
+    o.spp, o.mode, o.seed = sampler.spp, mode, seed
+    S.set_sampler(o, sampler)
+    out = np.zeros(2, np.float32)
+    if lib().orc_strat_sample(C.byref(o), pixel, sample, k, int(is2d), _ptr(out)) != 0:
+        raise ValueError("not a stratified sampler")
+    return out

@@ -1903,7 +1903,9 @@ struct Camera {
 // rd0: the camera ray's differentials; REF keeps them on every bounce (the ray never re-spawns,
 // F1), PBRT has them at the first hit only (spawn_ray drops them).
 static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max_depth, float rr_threshold,
-                    Mode mode, Counters* cnt, const RayDifferential& rd0 = RayDifferential()) {
+                    Mode mode, Counters* cnt, const RayDifferential& rd0 = RayDifferential(),
+                    const Strat& sp = Strat()) {
+    SamplerCalls calls{sp, mode == REF, rng, 1u, 2u};  // after the camera sample's calls
     RGB out, beta(1.0f);
     bool specular_bounce = false;
     float eta_scale = 1.0f;
@@ -1923,15 +1925,20 @@ static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max
         if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && !s.light_prims.empty()) {
             // uniform_sample_one_light (integrator.rs:309-328)
             float count = (float)s.light_prims.size();
-            size_t li = (size_t)rmin(rng.u(base + BD_LIGHT) * count, count - 1.0f);
+            const float upick = calls.get_1d(rng.u(base + BD_LIGHT));
+            float ul0 = rng.u(base + BD_ULIGHT), ul1 = rng.u(base + BD_ULIGHT + 1);
+            calls.get_2d(&ul0, &ul1);
+            float us0 = rng.u(base + BD_USCAT), us1 = rng.u(base + BD_USCAT + 1);
+            calls.get_2d(&us0, &us1);
+            size_t li = (size_t)rmin(upick * count, count - 1.0f);
             float light_pdf = 1.0f / count;
-            RGB ld = estimate_direct(s, it, bsdf, s.light_prims[li], rng.u(base + BD_USCAT),
-                                     rng.u(base + BD_USCAT + 1), rng.u(base + BD_ULIGHT),
-                                     rng.u(base + BD_ULIGHT + 1), mode, cnt);
+            RGB ld = estimate_direct(s, it, bsdf, s.light_prims[li], us0, us1, ul0, ul1, mode, cnt);
             out = out + beta * (ld / light_pdf);
         }
         V3 wo = -ray.d;
-        BxSample bs = bsdf.sample(wo, rng.u(base + BD_BSDF), rng.u(base + BD_BSDF + 1), BSDF_ALL, mode);
+        float ub0 = rng.u(base + BD_BSDF), ub1 = rng.u(base + BD_BSDF + 1);
+        calls.get_2d(&ub0, &ub1);
+        BxSample bs = bsdf.sample(wo, ub0, ub1, BSDF_ALL, mode);
         if (bs.f.is_black() || bs.pdf == 0.0f) break;
         beta = beta * (bs.f * abs_dot(bs.wi, it.shading_n) / bs.pdf);
         specular_bounce = (bs.sampled_type & BSDF_SPECULAR) != 0;
@@ -1945,7 +1952,7 @@ static RGB radiance(const Scene& s, Ray ray, const CounterRng& rng, uint32_t max
         RGB rr_beta = beta * eta_scale;
         if (rr_beta.max_component_value() < rr_threshold && bounces > 3) {
             float q = rmax(1.0f - rr_beta.max_component_value(), 0.5f);
-            if (rng.u(base + BD_RR) < q) break;
+            if (calls.get_1d(rng.u(base + BD_RR)) < q) break;
             beta = beta / (1.0f - q);
         }
         bounces += 1;
@@ -2231,6 +2238,31 @@ int32_t orc_scene_add_infinite_light(void* p, const bg_infinite_light* l) {
     return 0;
 }
 
+// The stratified sampler's value for stratified dimension k (is2d: get_2d, else get_1d) of
+// (pixel, sample) under the render options; out[1] = 0 for get_1d.  -1 when the options are not
+// a stratified sampler.
+int32_t orc_strat_sample(const bg_render_opts* o, uint32_t pixel, uint32_t sample, uint32_t k, int32_t is2d,
+                         float* out) {
+    if (o->sampler != BG_SAMPLER_STRATIFIED || o->x_pixel_samples * o->y_pixel_samples == 0) return -1;
+    Strat sp;
+    sp.dims = o->sampled_dimensions;
+    sp.nx = o->x_pixel_samples;
+    sp.ny = o->y_pixel_samples;
+    sp.jitter = o->jitter_samples;
+    CounterRng rng;
+    rng.pixel = pixel;
+    rng.sample = sample;
+    rng.seed = o->seed;
+    const bool ref = o->mode == BG_MODE_REF_COMPAT;
+    if (is2d) {
+        strat_2d(sp, ref, rng, k, &out[0], &out[1]);
+    } else {
+        out[0] = strat_1d(sp, ref, rng, k);
+        out[1] = 0.0f;
+    }
+    return 0;
+}
+
 void orc_scene_destroy(void* p) { delete (Scene*)p; }
 int64_t orc_bvh_nodes(void* p) { return (int64_t)((Scene*)p)->nodes.size(); }
 int64_t orc_num_lights(void* p) { return (int64_t)((Scene*)p)->light_prims.size(); }
@@ -2301,6 +2333,14 @@ int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_
     const float diff_scale = 1.0f / std::sqrt((float)(opts->spp ? opts->spp : 1u));  // integrator.rs:80-82
     const int tree_kind = opts->integrator == BG_INTEGRATOR_WHITTED ? 1
                           : (opts->light_strategy == BG_LIGHT_UNIFORM_ALL ? 2 : 3);
+    Strat sp;
+    if (opts->sampler == BG_SAMPLER_STRATIFIED) {
+        sp.dims = opts->sampled_dimensions;
+        sp.nx = opts->x_pixel_samples;
+        sp.ny = opts->y_pixel_samples;
+        sp.jitter = opts->jitter_samples;
+        if (sp.nx * sp.ny != opts->spp || sp.nx == 0) return -1;
+    }
     const int TILE = 16;
     int ntx = (W + TILE - 1) / TILE, nty = (H + TILE - 1) / TILE;
     std::vector<Counters> cs(nt);
@@ -2319,14 +2359,21 @@ int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_
                     rng.seed = opts->seed;
                     for (uint32_t si = 0; si < opts->spp; ++si) {
                         rng.sample = opts->first_sample + si;
-                        float fx = (float)x + rng.u(DIM_FILM), fy = (float)y + rng.u(DIM_FILM + 1);
-                        Ray ray = camera.generate_ray(fx, fy, rng.u(DIM_TIME));
+                        // Sampler::get_camera_sample: film get_2d, lens get_2d, time get_1d
+                        float ux = rng.u(DIM_FILM), uy = rng.u(DIM_FILM + 1);
+                        float ut = rng.u(DIM_TIME);
+                        if (sp.dims > 0) {
+                            strat_2d(sp, mode == REF, rng, 0, &ux, &uy);
+                            ut = strat_1d(sp, mode == REF, rng, 0);
+                        }
+                        float fx = (float)x + ux, fy = (float)y + uy;
+                        Ray ray = camera.generate_ray(fx, fy, ut);
                         RayDifferential rd;
                         if (!s.tex.empty()) rd = camera.differentials(fx, fy, ray, diff_scale);
                         Counters local;
                         Counters* cc = cnt ? cnt : (counters ? &local : nullptr);
                         RGB L = opts->integrator == BG_INTEGRATOR_PATH
-                                    ? radiance(s, ray, rng, opts->max_depth, opts->rr_threshold, mode, cc, rd)
+                                    ? radiance(s, ray, rng, opts->max_depth, opts->rr_threshold, mode, cc, rd, sp)
                                     : tree_radiance(s, ray, rd, rng, 1, 0, opts->max_depth, tree_kind, mode, cc);
                         if (!cnt && counters) { cbase.ext_rays += local.ext_rays; cbase.shadow_rays += local.shadow_rays; }
                         // sanity checks (integrator.rs:91-117)

@@ -186,6 +186,85 @@ struct CounterRng {
         uint32_t x = ctr[dim & 3];
         return (float)(x >> 9) * 0x1p-23f;
     }
+    uint32_t bits(uint32_t dim) const {
+        uint32_t ctr[4] = {sample, dim >> 2, (uint32_t)(seed >> 32), 0x626F6E73u ^ stream};
+        philox4x32_10(ctr, pixel, (uint32_t)seed);
+        return ctr[dim & 3];
+    }
+};
+
+// StratifiedSampler (src/samplers/stratified.rs:75-137, src/base/sampling.rs:120-179) as the
+// device draws it: a pixel's samples form passes of spp = nx * ny; stratified dimension k of sample
+// s takes stratum perm_k(s % spp) (the identity under REF, F6: shuffle never swaps; a keyed
+// permutation under PBRT), jittered by the counter RNG on stream 0x80000000 | 2k | is_2d (dimension
+// 0 keys the permutation, 4 + 2j and 5 + 2j jitter stratum j).
+struct Strat {
+    uint32_t dims = 0, nx = 1, ny = 1, jitter = 0;
+};
+// The keyed bijection of [0, n) the device uses (cycle walking over a bijection of [0, 2^b)).
+inline uint32_t strat_permute(uint32_t i, uint32_t n, uint32_t key) {
+    if (n <= 1) return 0;
+    uint32_t b = 0;
+    while ((1u << b) < n) ++b;
+    const uint32_t mask = b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u;
+    const uint32_t sh = (b + 1) / 2;
+    uint32_t x = i;
+    for (uint32_t it = 0; it <= mask; ++it) {
+        x = (x ^ key) & mask;
+        x = (x * 0x2F5A6B1Du) & mask;
+        x ^= x >> sh;
+        x = (x + (key >> 7)) & mask;
+        x = (x * 0x6C8E9CF5u) & mask;
+        x ^= x >> sh;
+        x = (x ^ (key >> 13) ^ 0x5BD1E995u) & mask;
+        x = (x * 0x1B873593u) & mask;
+        x ^= x >> sh;
+        if (x < n) return x;
+    }
+    return i;
+}
+inline uint32_t strat_stratum(const Strat& sp, bool ref, const CounterRng& rng, uint32_t k, uint32_t is2d,
+                              CounterRng* jr) {
+    const uint32_t n = sp.nx * sp.ny;
+    *jr = CounterRng();
+    jr->pixel = rng.pixel;
+    jr->sample = rng.sample / n;
+    jr->seed = rng.seed;
+    jr->stream = 0x80000000u | (k << 1) | is2d;
+    const uint32_t s = rng.sample % n;
+    return ref ? s : strat_permute(s, n, jr->bits(0));
+}
+inline float strat_1d(const Strat& sp, bool ref, const CounterRng& rng, uint32_t k) {  // stratified_sample_1d
+    CounterRng jr;
+    const uint32_t j = strat_stratum(sp, ref, rng, k, 0u, &jr);
+    const float delta = sp.jitter ? jr.u(4 + 2 * j) : 0.5f;
+    const float inv = 1.0f / (float)(sp.nx * sp.ny);
+    return std::fmin(((float)j + delta) * inv, ONE_MINUS_EPSILON);
+}
+inline void strat_2d(const Strat& sp, bool ref, const CounterRng& rng, uint32_t k, float* a, float* b) {
+    CounterRng jr;
+    const uint32_t j = strat_stratum(sp, ref, rng, k, 1u, &jr);
+    const float jx = sp.jitter ? jr.u(4 + 2 * j) : 0.5f, jy = sp.jitter ? jr.u(5 + 2 * j) : 0.5f;
+    const float dx = 1.0f / (float)sp.nx, dy = 1.0f / (float)sp.ny;
+    *a = std::fmin(((float)(j % sp.nx) + jx) * dx, ONE_MINUS_EPSILON);
+    *b = std::fmin(((float)(j / sp.nx) + jy) * dy, ONE_MINUS_EPSILON);
+}
+// Sampler::get_1d / get_2d of one sample in call order: stratified below sp.dims, else `v` (the
+// counter RNG's value for the call's fixed dimension).
+struct SamplerCalls {
+    const Strat& sp;
+    bool ref;
+    const CounterRng& rng;
+    uint32_t k1 = 0, k2 = 0;
+    float get_1d(float v) {
+        if (k1 < sp.dims) v = strat_1d(sp, ref, rng, k1);
+        ++k1;
+        return v;
+    }
+    void get_2d(float* a, float* b) {
+        if (k2 < sp.dims) strat_2d(sp, ref, rng, k2, a, b);
+        ++k2;
+    }
 };
 // Dimension schedule (identical on the device): camera film.xy 0-1, lens 2-3, time 4;
 // bounce b uses 8+8b: light pick, +1..2 u_light, +3..4 u_scattering, +5..6 BSDF, +7 roulette.
