@@ -597,11 +597,22 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     rng.block(ub, u);
     rng.block(ub + 4, u + 4);
     BSDF bsdf = path_bsdf<CLS, TEX>(sc, rp, wb.pixel[slot], wb.sample[slot], bounce, ray, it);
-    SamplerCalls calls{rp.strat, false, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state)};
-    if (bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0) {
-        calls.get_1d(u[BD_LIGHT]);
-        calls.get_2d(u[BD_ULIGHT], u[BD_ULIGHT + 1]);
-        calls.get_2d(u[BD_USCAT], u[BD_USCAT + 1]);
+    const bool nee = bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0;
+    // the bounce's sampler calls: [get_1d light, get_2d u_light, get_2d u_scattering,] get_2d BSDF,
+    // get_1d roulette (made only when the roulette test runs; its value is drawn here regardless)
+    if (rp.strat.dims > 0) {
+        SamplerCalls calls{rp.strat, false, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state)};
+        if (nee) {
+            calls.get_1d(u[BD_LIGHT]);
+            calls.get_2d(u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+            calls.get_2d(u[BD_USCAT], u[BD_USCAT + 1]);
+        }
+        calls.get_2d(u[BD_BSDF], u[BD_BSDF + 1]);
+        calls.get_1d(u[BD_RR]);
+    }
+    // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
+    state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
+    if (nee) {
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
         float count = (float)sc.nlights;
         uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
@@ -668,7 +679,6 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         state |= ST_PENDING;
     }
     V3 wo = -ray.d;
-    calls.get_2d(u[BD_BSDF], u[BD_BSDF + 1]);
     BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
     if (is_black(bs.f) || bs.pdf == 0.0f) {
         out.finished = true;
@@ -684,7 +694,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
     RGB rr_beta = beta * eta_scale;
     if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
-        calls.get_1d(u[BD_RR]);
+        state = st_set_k(state, st_k1(state) + 1u, st_k2(state));
         float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
         if (u[BD_RR] < qq) {
             out.finished = true;
@@ -695,7 +705,6 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    state = st_set_k(state, calls.k1, calls.k2);
     if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
     out.cont = true;
 }
