@@ -98,6 +98,7 @@ def example_config(sd, small: bool) -> dict:
                     f"RR threshold {sd.rr_threshold}, PBRT estimator",
         "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
         "integrator": "PathIntegrator", "env_map": [int(e[1]), int(e[0])],
+        "sampler": "StratifiedSampler 4x4, 4 sampled dimensions, jitter",
         "bvh": "8-wide compressed", "graph": "wave chain captured as a CUDA graph",
         "l2": "flushed before every step (512 MB device write)", "parallelism": "replicas",
     }
@@ -189,9 +190,10 @@ def cpu_sample(sd, target_s: float, threads: int, **kw):
     H, W = sd.camera.height, sd.camera.width
     probe_rows = (0, H, max(1, H // 8))
     t0 = time.time()
-    orc.render(A.BG_MODE_PBRT, spp=max(1, sd.spp // 16), rows=probe_rows, threads=threads, **kw)
+    probe_spp = sd.spp if kw.get("sampler") is not None else max(1, sd.spp // 16)  # a stratified pass is whole
+    orc.render(A.BG_MODE_PBRT, spp=probe_spp, rows=probe_rows, threads=threads, **kw)
     dt = max(time.time() - t0, 1e-3)
-    probe_samples = len(range(*probe_rows)) * W * max(1, sd.spp // 16)
+    probe_samples = len(range(*probe_rows)) * W * probe_spp
     rate = probe_samples / dt
     want_rows = max(1, int(target_s * rate / (W * sd.spp)))
     step = max(1, H // want_rows)
@@ -387,10 +389,14 @@ def run_integrators(args):
     rank, ws, local, dist = dist_init()
     sd = example_workload(args.small) if args.workload == "example" else workload(args.small)
     graph = False
+    extra_kw = {}
     if args.workload == "example":
+        from bonsai_gb300 import scenes as S
         kind, strategy, name = A.BG_INTEGRATOR_PATH, 0, "PathIntegrator"
+        smp = S.StratifiedSampler(4, 4, 4, True)  # src/main.rs: StratifiedSampler 4 x 4, 4 dimensions, jitter
         integ = lambda: G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, sd.rr_threshold,  # noqa: E731
-                                         mode=A.BG_MODE_PBRT)
+                                         mode=A.BG_MODE_PBRT, sampler=smp)
+        extra_kw = {"sampler": smp}
         graph = True
     elif args.workload == "whitted":
         kind, strategy, name = A.BG_INTEGRATOR_WHITTED, 0, "WhittedIntegrator"
@@ -434,7 +440,7 @@ def run_integrators(args):
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        kw = {"integrator": kind, "light_strategy": strategy}
+        kw = {"integrator": kind, "light_strategy": strategy} | extra_kw
         orc, rows, nsamples, _ = cpu_sample(sd, args.cpu_seconds, threads, **kw)
         cv, cdt = time_cpu(orc, sd, rows, nsamples, threads, **kw)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",

@@ -586,10 +586,50 @@ struct VertexOut {
     float4 sh_o[2], sh_d[2];
 };
 
-template <int CLS, bool TEX = false>
+// The stratified values a bounce may take (get_1d calls k1 and k1 + 1, get_2d calls k2 .. k2 + 2:
+// with light sampling the bounce makes 1D k1, 2D k2, k2 + 1, the BSDF's 2D k2 + 2 and the roulette's
+// 1D k1 + 1; without, the BSDF's 2D k2 and the roulette's 1D k1), -1 where the call falls through to
+// the counter RNG.  A shade thread computes them when it picks up a path, where few registers are
+// live, into its column of shared memory (8 rows, stride SU_STRIDE).
+constexpr uint32_t SU_STRIDE = 128;
+BG_D void strat_prefetch(const StratParams& sp, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k1,
+                         uint32_t k2, float* col) {
+    col[0] = k1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1) : -1.0f;
+    col[SU_STRIDE] = k1 + 1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1 + 1) : -1.0f;
+    for (uint32_t j = 0; j < 3; ++j) {
+        const float2 v = k2 + j < sp.dims ? strat_2d(sp, false, pix, sample, seed, k2 + j) : make_float2(-1.0f, -1.0f);
+        col[(2 + 2 * j) * SU_STRIDE] = v.x;
+        col[(3 + 2 * j) * SU_STRIDE] = v.y;
+    }
+}
+BG_D void strat_apply(const float* su, bool nee, float u[8]) {
+    const float a = su[0], b = su[SU_STRIDE];
+    auto pair = [&](int row, int slot) {
+        const float x = su[row * SU_STRIDE];
+        if (x >= 0.0f) {
+            u[slot] = x;
+            u[slot + 1] = su[(row + 1) * SU_STRIDE];
+        }
+    };
+    if (nee) {
+        if (a >= 0.0f) u[BD_LIGHT] = a;
+        pair(2, BD_ULIGHT);
+        pair(4, BD_USCAT);
+        pair(6, BD_BSDF);
+        if (b >= 0.0f) u[BD_RR] = b;
+    } else {
+        pair(2, BD_BSDF);
+        if (a >= 0.0f) u[BD_RR] = a;
+    }
+}
+
+// INF: the scene's light list may hold the infinite light (variants launched only for such scenes,
+// so that the others carry none of its code).
+template <int CLS, bool TEX = false, bool INF = false>
 BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
                          uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
-                         uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out) {
+                         uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out,
+                         const float* su = nullptr) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
     const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
@@ -600,16 +640,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     const bool nee = bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0;
     // the bounce's sampler calls: [get_1d light, get_2d u_light, get_2d u_scattering,] get_2d BSDF,
     // get_1d roulette (made only when the roulette test runs; its value is drawn here regardless)
-    if (rp.strat.dims > 0) {
-        SamplerCalls calls{rp.strat, false, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state)};
-        if (nee) {
-            calls.get_1d(u[BD_LIGHT]);
-            calls.get_2d(u[BD_ULIGHT], u[BD_ULIGHT + 1]);
-            calls.get_2d(u[BD_USCAT], u[BD_USCAT + 1]);
-        }
-        calls.get_2d(u[BD_BSDF], u[BD_BSDF + 1]);
-        calls.get_1d(u[BD_RR]);
-    }
+    if (su) strat_apply(su, nee, u);  // the stratified sampler's values, prefetched by the shade thread
     // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
     state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
     if (nee) {
@@ -624,7 +655,8 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
             const float c = mix->c();
             return c * mix->pdf(w) + (1.0f - c) * pb;
         };
-        LightSample ls = light_sample_any<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+        LightSample ls = INF ? light_sample_any<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1])
+                             : light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
         if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
             RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
             if (!is_black(f)) {
@@ -655,19 +687,21 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         if (!is_black(f) && spdf > 0.0f) {
             float t_light = 0.0f;
             V3 ln;
-            float lpdf = light_pdf_any<false>(sc, light_prim, it, wi, &t_light, &ln);
+            float lpdf = INF ? light_pdf_any<false>(sc, light_prim, it, wi, &t_light, &ln)
+                             : light_pdf<false>(sc, light_prim, it, wi, &t_light, &ln);
             if (lpdf != 0.0f) {
                 float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
                 // the sampled direction reaches the light at t_light; it counts iff nothing else
                 // is hit first (closest hit == this light; for the infinite light t_light is
                 // infinite and nothing may be hit)
-                RGB li = light_radiance_along(sc, light_prim, wi, ln);
+                RGB li = INF ? light_radiance_along(sc, light_prim, wi, ln)
+                             : emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -wi);
                 if (!is_black(li)) {
                     RGB c = f * li * w / spdf;
                     Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
                     pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
                     out.sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
-                    const int skip = light_prim == LIGHT_INFINITE ? -1 : (int)light_prim;
+                    const int skip = INF && light_prim == LIGHT_INFINITE ? -1 : (int)light_prim;
                     out.sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float(skip));
                     out.push_sh[1] = true;
                 }
@@ -742,13 +776,14 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 #ifndef BG_SHADE_MINBLOCKS
 #define BG_SHADE_MINBLOCKS 4
 #endif
-template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false>
+template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false>
 __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     const uint32_t stride = gridDim.x * blockDim.x;
+    __shared__ float strat_su[(!MULTI && !GWK && CLS != CLS_MISS) ? 8 * SU_STRIDE : 1];
     const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
     const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
@@ -776,6 +811,12 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             float4 b4 = wb.beta[slot];
             RGB beta = rgb(b4.x, b4.y, b4.z);
             float eta_scale = b4.w;
+            const float* su = nullptr;
+            if (!MULTI && !GWK && CLS != CLS_MISS && rp.strat.dims > 0) {
+                float* col = strat_su + threadIdx.x;
+                strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
+                su = col;
+            }
             float4 l4 = wb.L[slot];
             RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
             state &= ~ST_PENDING;
@@ -796,8 +837,8 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
                 gq = make_query(gw, it, -ray.d);
                 push_guide = true;
             } else if (!finished) {
-                scatter_vertex<CLS, TEX>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
-                                    vo);
+                scatter_vertex<CLS, TEX, INF>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
+                                    vo, su);
                 finished = vo.finished;
                 cont = vo.cont;
             }
@@ -969,6 +1010,17 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        } else if (sc.inf) {  // the light list holds the infinite light
+            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            if (sc.ntex) {
+                k_shade<0, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+                k_shade<1, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            } else {
+                k_shade<0, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+                k_shade<1, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            }
+            k_shade<2, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<3, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         } else if (sc.ntex) {
             k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
             k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
