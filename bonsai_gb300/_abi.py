@@ -41,6 +41,7 @@ BG_RENDER_GRAPH = 4
 BG_RENDER_STAGE_TIMING = 8
 BG_TUNE_SORT_RAYS = 1
 BG_TUNE_L2_PERSIST = 2
+BG_TUNE_TILE_PIXELS = 4
 BG_SAMPLER_INDEPENDENT, BG_SAMPLER_STRATIFIED = 0, 1
 
 BG_TEXTURE_IMAGE = 0

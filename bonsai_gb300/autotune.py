@@ -52,7 +52,7 @@ def get(ctx) -> A.bg_tuning:
 def set_(ctx, refill: int, blocks: int, wave: int, sort_rays: int = 0):
     t = A.bg_tuning()
     t.refill, t.blocks_per_sm, t.wave_paths = refill, blocks, wave
-    t.flags = A.BG_TUNE_SORT_RAYS if sort_rays else 0
+    t.flags = (A.BG_TUNE_SORT_RAYS if sort_rays else 0) | A.BG_TUNE_TILE_PIXELS
     ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
 
 

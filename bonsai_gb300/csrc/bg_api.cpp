@@ -593,7 +593,8 @@ bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
     out->wave_paths = ctx->max_queue;
     out->blocks_per_sm = (uint32_t)ctx->shape.blocks_per_sm;
     out->refill = (uint32_t)ctx->shape.refill;
-    out->flags = (ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u) | (ctx->shape.l2_persist ? BG_TUNE_L2_PERSIST : 0u);
+    out->flags = (ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u) | (ctx->shape.l2_persist ? BG_TUNE_L2_PERSIST : 0u) |
+                 (ctx->shape.tile_pixels ? BG_TUNE_TILE_PIXELS : 0u);
     return BG_OK;
 }
 
@@ -607,6 +608,7 @@ bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
     ctx->shape.refill = (int)t->refill;
     ctx->shape.sort_rays = (t->flags & BG_TUNE_SORT_RAYS) ? 1 : 0;
     ctx->shape.l2_persist = (t->flags & BG_TUNE_L2_PERSIST) ? 1 : 0;
+    ctx->shape.tile_pixels = (t->flags & BG_TUNE_TILE_PIXELS) ? 1 : 0;
     return BG_OK;
 }
 
@@ -1311,6 +1313,7 @@ bg_status bg_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* cam, const 
     rp = bg::with_camera(rp, dc, o->spp);
     bg::strat_params(o->sampler, o->spp, o->x_pixel_samples, o->y_pixel_samples, o->sampled_dimensions,
                      o->jitter_samples, &rp.strat);  // checked by validate_render
+    rp.pixel_tiles = ctx->shape.tile_pixels ? 1u : 0u;
     const uint64_t npix = (uint64_t)cam->width * cam->height;
     const uint64_t total = npix * o->spp;
     uint64_t launches = 0;

@@ -269,7 +269,8 @@ BG_D void generate_paths(const Camera& cam, const RenderParams& rp, const WaveBu
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
         uint64_t item = item0 + i;
-        generate_one(cam, rp, wb, i, (uint32_t)(item % npix), first_sample + (uint32_t)(item / npix));
+        generate_one(cam, rp, wb, i, pixel_of((uint32_t)(item % npix), rp.width, rp.height, rp.pixel_tiles),
+                     first_sample + (uint32_t)(item / npix));
     }
 }
 

@@ -210,6 +210,29 @@ struct Rng {
     }
 };
 
+// The pixel of a render's linear pixel index t in [0, w * h): scanline order, or (tiles != 0)
+// bands of 4 rows walked in 8 x 4 tiles, so that the 32 camera rays of a warp cover a compact block;
+// the ragged right column of tiles (w % 8) and bottom band (h % 4) keep narrower / shorter tiles.
+BG_HD uint32_t pixel_of(uint32_t t, uint32_t w, uint32_t h, uint32_t tiles) {
+    if (!tiles) return t;
+    const uint32_t full_band = 4u * w, nfull = h / 4u;
+    const uint32_t band = t / full_band < nfull ? t / full_band : nfull;
+    const uint32_t y0 = band * 4u, bh = band < nfull ? 4u : h - y0;
+    const uint32_t o = t - band * full_band;
+    const uint32_t wt = w / 8u, tile = 8u * bh;
+    uint32_t x, y;
+    if (o < wt * tile) {
+        const uint32_t c = o / tile, k = o - c * tile;
+        x = c * 8u + (k & 7u);
+        y = y0 + (k >> 3);
+    } else {
+        const uint32_t r = o - wt * tile, wr = w - wt * 8u;
+        x = wt * 8u + r % wr;
+        y = y0 + r / wr;
+    }
+    return y * w + x;
+}
+
 // Dimension schedule shared with the CPU oracle: camera film.xy 0-1, lens 2-3, time 4;
 // bounce b: base 8+8b: light pick +0, u_light +1..2, u_scattering +3..4, BSDF +5..6, roulette +7.
 constexpr uint32_t DIM_FILM = 0, DIM_TIME = 4, DIM_BOUNCE0 = 8, DIMS_PER_BOUNCE = 8;

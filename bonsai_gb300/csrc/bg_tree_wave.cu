@@ -65,7 +65,8 @@ __global__ void k_tw_gen(Camera cam, RenderParams rp, TreeWave tw, uint64_t item
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint64_t item = item0 + i;
-        const uint32_t pix = (uint32_t)(item % npix), s = rp.first_sample + (uint32_t)(item / npix);
+        const uint32_t pix = pixel_of((uint32_t)(item % npix), rp.width, rp.height, rp.pixel_tiles);
+        const uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, 0u};
         const CameraUs cu = camera_us(rp.strat, false, rng);  // sampled_dimensions <= 1: camera only
         const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
@@ -206,7 +207,8 @@ __global__ void __launch_bounds__(128, BG_TREE_SHADE_MINBLOCKS) k_tw_shade(Scene
         }
         const uint32_t slot = meta.x, node = meta.y;
         const uint64_t item = item0 + slot;
-        const uint32_t pix = (uint32_t)(item % npix), s = rp.first_sample + (uint32_t)(item / npix);
+        const uint32_t pix = pixel_of((uint32_t)(item % npix), rp.width, rp.height, rp.pixel_tiles);
+        const uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, node - 1u};
         TexPoint tp;
         bool have_tp = false;
@@ -331,7 +333,8 @@ __global__ void k_tw_final(RenderParams rp, FilmBuffers film, TreeWave tw, uint6
     const uint64_t npix = (uint64_t)rp.width * rp.height;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 l = tw.L[i];
-        film_add(film, (uint32_t)((item0 + i) % npix), rgb(l.x, l.y, l.z));
+        film_add(film, pixel_of((uint32_t)((item0 + i) % npix), rp.width, rp.height, rp.pixel_tiles),
+                 rgb(l.x, l.y, l.z));
     }
 }
 

@@ -327,6 +327,9 @@ typedef struct bg_tuning {
                                  persisting access-policy window during renders; the set-aside
                                  belongs to the context and ends with it.  Off by default: on the
                                  production frame it slows shading more than it helps traversal */
+#define BG_TUNE_TILE_PIXELS 4u /* generate the wavefront's camera rays in 8 x 4 pixel tiles instead of
+                                  scanline order (more coherent first-bounce traversal); on by
+                                  default                                                        */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 

@@ -112,3 +112,31 @@ def test_ray_binning_keeps_every_path(gpu_ctx):
     finally:
         gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(old)))
         sc.close()
+
+
+def _with_flags(ctx, flags, fn):
+    saved = A.bg_tuning()
+    ctx.check(ctx.lib.bg_get_tuning(ctx.h, C.byref(saved)))
+    t = A.bg_tuning.from_buffer_copy(bytes(saved))
+    t.flags = flags
+    ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
+    try:
+        return fn()
+    finally:
+        ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(saved)))
+
+
+@pytest.mark.parametrize("w,h", [(48, 40), (37, 23)])
+def test_tiled_pixel_order_changes_only_the_summation_order(gpu_ctx, w, h):
+    """BG_TUNE_TILE_PIXELS hands the wavefront's camera rays out in 8 x 4 pixel tiles (ragged edges
+    included): every pixel keeps its own samples, so the path and Whitted films equal the scanline
+    order's up to the order of the film sums."""
+    sd = S.env_sphere(w, h, spp=8, max_depth=5, extra=True)
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    try:
+        for it in (G.PathIntegrator(sd.camera, 8, 5), G.WhittedIntegrator(sd.camera, 8, 5)):
+            a = _with_flags(gpu_ctx, 0, lambda: it.render(sc).rgb)
+            b = _with_flags(gpu_ctx, A.BG_TUNE_TILE_PIXELS, lambda: it.render(sc).rgb)
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+    finally:
+        sc.close()
