@@ -18,6 +18,7 @@
 #include "bg_film.cuh"
 #include "bg_estimate.cuh"
 #include "bg_warp.cuh"
+#include "bg_wave.cuh"
 
 namespace bg {
 
@@ -95,39 +96,6 @@ void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays
         else BG_TRACE(8, false);
     }
 #undef BG_TRACE
-}
-
-// ================================================================ textures
-// Texture inputs at a hit whose material is textured (nullptr otherwise): the surface geometry
-// re-derived from the hit and the screen-space differentials of ray differentials `rd`.
-BG_D const TexPoint* tex_point(const Scene& sc, const Isect& it, const Ray& ray, const RayDiff* rd, TexPoint* tp) {
-    if (!sc.ntex || !material_textured(sc.mats[prim_material(sc, it.prim)])) return nullptr;
-    Isect tmp;
-    if (!prim_isect(sc, it.prim, ray, &tmp, &tp->g)) tp->g = SurfaceGeom{};
-    tp->p = it.p;
-    tp->n = it.n;
-    tp->d = compute_differentials(it.p, it.n, tp->g, rd);
-    return tp;
-}
-// The camera ray differentials of path (pixel, sample); `cam_ray` is its camera ray.
-BG_D RayDiff path_camera_diff(const RenderParams& rp, uint32_t pix, uint32_t s, const Ray& cam_ray) {
-    Rng rng{pix, s, rp.seed};
-    float c[4];
-    rng.block(0, c);
-    float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
-    return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale);
-}
-// BSDF of a path vertex: textured materials read the camera differentials at the first hit
-// (PathIntegrator spawns later rays without differentials, path.rs:139).
-// TEX: texture support compiled in (it costs the shade kernels about 30 registers).
-template <int CLS, bool TEX>
-BG_D BSDF path_bsdf(const Scene& sc, const RenderParams& rp, uint32_t pix, uint32_t s, uint32_t bounce, const Ray& ray,
-                    const Isect& it) {
-    if (!TEX || !sc.ntex) return make_bsdf<CLS>(sc, it);
-    TexPoint tp;
-    RayDiff rd;
-    if (bounce == 0) rd = path_camera_diff(rp, pix, s, ray);
-    return make_bsdf<CLS>(sc, it, tex_point(sc, it, ray, bounce == 0 ? &rd : nullptr, &tp));
 }
 
 // ================================================================ megakernel (reference layout)
@@ -219,61 +187,6 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
     else k_megakernel<false><<<grid, block, 0, s>>>(sc, cam, rp, film, err);
 }
 
-// ================================================================ wavefront (PBRT)
-// Path state word: bits 0-7 bounce, 8 specular bounce, 9 pending NEE contribution, 10 open
-// training record, 12-15 training records written, 16-23 / 24-31 the sampler's get_1d / get_2d
-// calls so far (saturating at 255; calls below sampled_dimensions take stratified values).
-enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10 };
-constexpr uint32_t ST_REC_SHIFT = 12, ST_REC_MASK = 0xFu << ST_REC_SHIFT;
-BG_D uint32_t st_k1(uint32_t st) { return (st >> 16) & 0xFFu; }
-BG_D uint32_t st_k2(uint32_t st) { return st >> 24; }
-BG_D uint32_t st_set_k(uint32_t st, uint32_t k1, uint32_t k2) {
-    return (st & 0xFFFFu) | (min(k1, 255u) << 16) | (min(k2, 255u) << 24);
-}
-enum : uint32_t {
-    C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6,
-    C_GUIDE = 11,  // 11..13: guided queries of the matte, plastic and conductor classes
-    C_GSPAN = 14   // end of the guided-query range (written by the dielectric shade launch)
-};
-// Guided queries of class c occupy [guide_base(c), guide_base(c) + counters[C_GUIDE + c]) of the
-// query buffer, guide_base(c) = sizes of the class queues before c, so each class's continuation
-// runs as its own launch with a static BSDF type.
-BG_D uint32_t guide_base(const WaveBuffers& wb, int cls) {
-    uint32_t b = 0;
-    for (int c = 0; c < cls; ++c) b += wb.counters[C_CLS + c];
-    return b;
-}
-constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
-constexpr int CLS_MISS = 4;
-
-// Camera ray of (pixel, sample) into path slot i (PerspectiveCamera::generate_ray).
-BG_D void generate_one(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint32_t i, uint32_t pix,
-                       uint32_t s) {
-    Rng rng{pix, s, rp.seed};
-    const CameraUs cu = camera_us(rp.strat, false, rng);
-    float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-    Ray r = camera_ray(cam, fx, fy, cu.time);
-    wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
-    wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
-    wb.pixel[i] = pix;
-    wb.sample[i] = s;
-    wb.state[i] = st_set_k(0u, 1u, 2u);  // the camera sample made one get_1d and two get_2d calls
-    wb.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    wb.queue[0][i] = i;
-}
-
-BG_D void generate_paths(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint64_t item0,
-                         uint32_t nitems, uint32_t first_sample) {
-    const uint64_t npix = (uint64_t)rp.width * rp.height;
-    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[C_Q0] = nitems;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
-        uint64_t item = item0 + i;
-        generate_one(cam, rp, wb, i, pixel_of((uint32_t)(item % npix), rp.width, rp.height, rp.pixel_tiles),
-                     first_sample + (uint32_t)(item / npix));
-    }
-}
-
 // Batch: item -> scene by binary search over the scenes' first items, then as above.
 __global__ void k_generate_batch(const SceneRender* tab, uint32_t nscenes, WaveBuffers wb, uint64_t item0,
                                  uint32_t nitems) {
@@ -294,13 +207,6 @@ __global__ void k_generate_batch(const SceneRender* tab, uint32_t nscenes, WaveB
     }
 }
 
-// The scene / render parameters / film of a path: the kernel's own in a single-scene render, the
-// path's table entry in a batch render.
-template <bool MULTI, class T>
-BG_D const T& pick(const T& single, const T* multi) {
-    if constexpr (MULTI) return *multi;
-    else return single;
-}
 
 __global__ void k_generate(Camera cam, RenderParams rp, WaveBuffers wb, uint64_t item0, uint32_t nitems) {
     generate_paths(cam, rp, wb, item0, nitems, rp.first_sample);
@@ -477,456 +383,6 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
     }
 }
 
-// Adds the pending next-event contribution of the previous vertex:
-// L += beta_nee * ((part0 + part1) / light_pdf)  (path.rs:107-109, integrator.rs:327).
-BG_D RGB apply_pending(const WaveBuffers& wb, uint32_t slot, RGB L, uint32_t state, uint32_t nlights) {
-    if (!(state & ST_PENDING)) return L;
-    float4 p0 = wb.pending[2 * slot], p1 = wb.pending[2 * slot + 1];
-    RGB ld = rgb(0.0f);
-    if (p0.w != 0.0f) ld = ld + rgb(p0.x, p0.y, p0.z);
-    if (p1.w != 0.0f) ld = ld + rgb(p1.x, p1.y, p1.z);
-    float4 nb = wb.nee_beta[slot];
-    float light_pdf = 1.0f / (float)nlights;
-    return L + rgb(nb.x, nb.y, nb.z) * (ld / light_pdf);
-}
-
-// ---- guiding: training records and network queries
-BG_D float4* rec_ptr(const GuideWave& gw, uint32_t k, uint32_t f, uint32_t slot) {
-    return gw.rec + ((size_t)(k * GUIDE_REC_F4 + f) * gw.cap + slot);
-}
-BG_D uint32_t rec_count(uint32_t state) { return (state & ST_REC_MASK) >> ST_REC_SHIFT; }
-
-// Closes the open record with the radiance the path has gathered before this vertex adds its own
-// emission: what arrived along the recorded direction is everything added after this point.
-BG_D uint32_t close_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state, RGB L) {
-    if (!(state & ST_REC_OPEN) || slot >= gw.cap) return state;
-    uint32_t k = rec_count(state) - 1;
-    *rec_ptr(gw, k, 4, slot) = make_float4(L.r, L.g, L.b, 0.0f);
-    return state & ~ST_REC_OPEN;
-}
-
-struct GuideQuery {  // p_norm.xyz n.x | n.yz wo.xy | wo.z
-    float4 a, b, c;
-};
-BG_D GuideQuery make_query(const GuideWave& gw, const Isect& it, V3 wo) {
-    V3 pn = v3(rclamp((it.p.x - gw.bmin.x) * gw.binv.x, 0.0f, 1.0f), rclamp((it.p.y - gw.bmin.y) * gw.binv.y, 0.0f, 1.0f),
-               rclamp((it.p.z - gw.bmin.z) * gw.binv.z, 0.0f, 1.0f));
-    V3 n = face_forward(it.ns, wo);
-    return {make_float4(pn.x, pn.y, pn.z, n.x), make_float4(n.y, n.z, wo.x, wo.y), make_float4(wo.z, 0.0f, 0.0f, 0.0f)};
-}
-
-// Opens a training record for a sampled continuation wi (p_b = BSDF pdf of wi, beta = throughput
-// before the vertex).
-BG_D uint32_t open_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state,
-                          const GuideQuery& q, V3 wi, float p_b, RGB beta) {
-    uint32_t k = rec_count(state);
-    if (k >= (uint32_t)GUIDE_MAXREC || slot >= gw.cap) return state;
-    *rec_ptr(gw, k, 0, slot) = q.a;
-    *rec_ptr(gw, k, 1, slot) = q.b;
-    *rec_ptr(gw, k, 2, slot) = make_float4(q.c.x, wi.x, wi.y, wi.z);
-    *rec_ptr(gw, k, 3, slot) = make_float4(p_b, beta.r, beta.g, beta.b);
-    return (state & ~ST_REC_MASK) | ((k + 1) << ST_REC_SHIFT) | ST_REC_OPEN;
-}
-
-// Integer hash in [0, 1) for subsampling records into the training pool (not part of the estimator).
-BG_D float hash_unit(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
-    h ^= h >> 15;
-    h *= 0x2C1B3C6Du;
-    h ^= h >> 12;
-    h *= 0x297A2D39u;
-    h ^= h >> 15;
-    return (float)(h >> 8) * 0x1p-24f;
-}
-
-// Turns the records of finished paths into training samples.  Warp-collective: every lane calls
-// it, lanes without a finished path pass nrec = 0.
-BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t nrec, RGB L_end) {
-    uint32_t positive = 0;
-    for (uint32_t k = 0; k < (uint32_t)GUIDE_MAXREC; ++k) {
-        const bool has = k < nrec;
-        if (!__any_sync(FULL, has)) break;
-        bool keep = false;
-        float w = 0.0f;
-        float4 r3 = make_float4(0, 0, 0, 0);
-        if (has) {
-            r3 = *rec_ptr(gw, k, 3, slot);
-            float4 r4 = *rec_ptr(gw, k, 4, slot);
-            RGB d = L_end - rgb(r4.x, r4.y, r4.z);
-            // (L_end - L_after) / beta = f |cos| Li / p of the recorded direction
-            RGB li = rgb(r3.y > 0.0f ? d.r / r3.y : 0.0f, r3.z > 0.0f ? d.g / r3.z : 0.0f,
-                         r3.w > 0.0f ? d.b / r3.w : 0.0f);
-            w = luminance(li);
-            if (w > 0.0f && isfinite(w)) {
-                ++positive;
-                keep = hash_unit(wb.pixel[slot], wb.sample[slot], k) < gw.keep_prob;
-            }
-        }
-        uint32_t pos = warp_append(&gw.ctr[1], keep);
-        if (keep && pos < gw.pool_cap) {
-            float4* o = gw.pool + (size_t)GUIDE_SAMPLE_F4 * pos;
-            o[0] = *rec_ptr(gw, k, 0, slot);
-            o[1] = *rec_ptr(gw, k, 1, slot);
-            o[2] = *rec_ptr(gw, k, 2, slot);
-            o[3] = make_float4(r3.x, w, 0.0f, 0.0f);
-        }
-    }
-    uint32_t tot = __reduce_add_sync(FULL, positive);
-    if (lane_id() == 0 && tot) atomicAdd(&gw.ctr[0], tot);
-}
-
-// Everything a non-specular or specular vertex does after its emission: next-event estimation
-// (uniform_sample_one_light + estimate_direct, src/base/integrator.rs:309-437, the occlusion tests
-// deferred to k_shadow), the BSDF-sampled continuation (src/integrators/path.rs:110-143) and
-// Russian roulette.  `mix` (guided vertices) replaces the BSDF in estimate_direct's second
-// strategy by the one-sample mixture c * guide + (1 - c) * BSDF: the direction is drawn from it and
-// both MIS weights use its pdf, so the estimator stays unbiased whatever the network outputs.
-struct VertexOut {
-    bool cont = false, finished = false;
-    bool push_sh[2] = {false, false};
-    float4 sh_o[2], sh_d[2];
-};
-
-// The stratified values a bounce may take (get_1d calls k1 and k1 + 1, get_2d calls k2 .. k2 + 2:
-// with light sampling the bounce makes 1D k1, 2D k2, k2 + 1, the BSDF's 2D k2 + 2 and the roulette's
-// 1D k1 + 1; without, the BSDF's 2D k2 and the roulette's 1D k1), -1 where the call falls through to
-// the counter RNG.  A shade thread computes them when it picks up a path, where few registers are
-// live, into its column of shared memory (8 rows, stride SU_STRIDE).
-constexpr uint32_t SU_STRIDE = 128;
-BG_D void strat_prefetch(const StratParams& sp, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k1,
-                         uint32_t k2, float* col) {
-    col[0] = k1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1) : -1.0f;
-    col[SU_STRIDE] = k1 + 1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1 + 1) : -1.0f;
-    for (uint32_t j = 0; j < 3; ++j) {
-        const float2 v = k2 + j < sp.dims ? strat_2d(sp, false, pix, sample, seed, k2 + j) : make_float2(-1.0f, -1.0f);
-        col[(2 + 2 * j) * SU_STRIDE] = v.x;
-        col[(3 + 2 * j) * SU_STRIDE] = v.y;
-    }
-}
-BG_D void strat_apply(const float* su, bool nee, float u[8]) {
-    const float a = su[0], b = su[SU_STRIDE];
-    auto pair = [&](int row, int slot) {
-        const float x = su[row * SU_STRIDE];
-        if (x >= 0.0f) {
-            u[slot] = x;
-            u[slot + 1] = su[(row + 1) * SU_STRIDE];
-        }
-    };
-    if (nee) {
-        if (a >= 0.0f) u[BD_LIGHT] = a;
-        pair(2, BD_ULIGHT);
-        pair(4, BD_USCAT);
-        pair(6, BD_BSDF);
-        if (b >= 0.0f) u[BD_RR] = b;
-    } else {
-        pair(2, BD_BSDF);
-        if (a >= 0.0f) u[BD_RR] = a;
-    }
-}
-
-// INF: the scene's light list may hold the infinite light (variants launched only for such scenes,
-// so that the others carry none of its code).
-template <int CLS, bool TEX = false, bool INF = false>
-BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
-                         uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
-                         uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out,
-                         const float* su = nullptr) {
-    constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
-    Rng rng{wb.pixel[slot], wb.sample[slot], rp.seed};
-    const uint32_t ub = DIM_BOUNCE0 + DIMS_PER_BOUNCE * bounce;
-    float u[8];
-    rng.block(ub, u);
-    rng.block(ub + 4, u + 4);
-    BSDF bsdf = path_bsdf<CLS, TEX>(sc, rp, wb.pixel[slot], wb.sample[slot], bounce, ray, it);
-    const bool nee = bsdf.num_components(BSDF_ALL & ~BSDF_SPECULAR) > 0 && sc.nlights > 0;
-    // the bounce's sampler calls: [get_1d light, get_2d u_light, get_2d u_scattering,] get_2d BSDF,
-    // get_1d roulette (made only when the roulette test runs; its value is drawn here regardless)
-    if (su) strat_apply(su, nee, u);  // the stratified sampler's values, prefetched by the shade thread
-    // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
-    state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
-    if (nee) {
-        const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
-        float count = (float)sc.nlights;
-        uint32_t light_prim = sc.light_prims[(uint32_t)rmin(u[BD_LIGHT] * count, count - 1.0f)];
-        float4 pend[2] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
-        // pdf of the second strategy for a direction
-        auto strategy_pdf = [&](V3 w) {
-            float pb = bsdf.pdf<false>(it.wo, w, flags);
-            if (!mix) return pb;
-            const float c = mix->c();
-            return c * mix->pdf(w) + (1.0f - c) * pb;
-        };
-        LightSample ls = INF ? light_sample_any<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1])
-                             : light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
-        if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
-            RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
-            if (!is_black(f)) {
-                float w = power_heuristic(1.0f, ls.pdf, 1.0f, strategy_pdf(ls.wi));
-                RGB c = f * ls.radiance * w / ls.pdf;
-                Ray sr = spawn_ray_to(it.p, it.p_err, it.n, it.time, ls.pt.p, ls.pt.p_err, ls.pt.n);
-                pend[0] = make_float4(c.r, c.g, c.b, 0.0f);
-                out.sh_o[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.t_max);
-                out.sh_d[0] = make_float4(sr.d.x, sr.d.y, sr.d.z, __int_as_float(-1));
-                out.push_sh[0] = true;
-            }
-        }
-        // second strategy: a direction from the BSDF (or the mixture), counted when it reaches the
-        // chosen light
-        V3 wi;
-        RGB f;
-        float spdf;
-        if (GUIDABLE && mix && ug[0] < mix->c()) {
-            wi = mix->sample(ug[1], ug[2], ug[3]);
-            f = bsdf.f<false>(it.wo, wi, flags) * abs_dot(wi, it.ns);
-            spdf = strategy_pdf(wi);
-        } else {
-            BxSample bs = bsdf.sample<false>(it.wo, u[BD_USCAT], u[BD_USCAT + 1], flags);
-            wi = bs.wi;
-            f = bs.f * abs_dot(bs.wi, it.ns);
-            spdf = mix ? (bs.pdf > 0.0f ? strategy_pdf(bs.wi) : 0.0f) : bs.pdf;
-        }
-        if (!is_black(f) && spdf > 0.0f) {
-            float t_light = 0.0f;
-            V3 ln;
-            float lpdf = INF ? light_pdf_any<false>(sc, light_prim, it, wi, &t_light, &ln)
-                             : light_pdf<false>(sc, light_prim, it, wi, &t_light, &ln);
-            if (lpdf != 0.0f) {
-                float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
-                // the sampled direction reaches the light at t_light; it counts iff nothing else
-                // is hit first (closest hit == this light; for the infinite light t_light is
-                // infinite and nothing may be hit)
-                RGB li = INF ? light_radiance_along(sc, light_prim, wi, ln)
-                             : emission(sc.emis[prim_emission(sc, (int)light_prim)], ln, -wi);
-                if (!is_black(li)) {
-                    RGB c = f * li * w / spdf;
-                    Ray br = spawn_ray(it.p, it.p_err, it.n, it.time, wi, false);
-                    pend[1] = make_float4(c.r, c.g, c.b, 0.0f);
-                    out.sh_o[1] = make_float4(br.o.x, br.o.y, br.o.z, t_light);
-                    const int skip = INF && light_prim == LIGHT_INFINITE ? -1 : (int)light_prim;
-                    out.sh_d[1] = make_float4(br.d.x, br.d.y, br.d.z, __int_as_float(skip));
-                    out.push_sh[1] = true;
-                }
-            }
-        }
-        wb.pending[2 * slot] = pend[0];
-        wb.pending[2 * slot + 1] = pend[1];
-        wb.nee_beta[slot] = make_float4(beta.r, beta.g, beta.b, 0.0f);
-        state |= ST_PENDING;
-    }
-    V3 wo = -ray.d;
-    BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
-    if (is_black(bs.f) || bs.pdf == 0.0f) {
-        out.finished = true;
-        return;
-    }
-    RGB beta0 = beta;
-    beta = beta * (bs.f * abs_dot(bs.wi, it.ns) / bs.pdf);
-    bool spec = (bs.stype & BSDF_SPECULAR) != 0;
-    if (spec && (bs.stype & BSDF_TRANSMISSION)) {
-        float eta = bsdf.eta;
-        eta_scale *= dot(wo, it.n) > 0.0f ? eta * eta : 1.0f / (eta * eta);
-    }
-    Ray nr = spawn_ray(it.p, it.p_err, it.n, it.time, bs.wi, false);
-    RGB rr_beta = beta * eta_scale;
-    if (max_value(rr_beta) < rp.rr_threshold && bounce > 3) {
-        state = st_set_k(state, st_k1(state) + 1u, st_k2(state));
-        float qq = rmax(1.0f - max_value(rr_beta), 0.5f);
-        if (u[BD_RR] < qq) {
-            out.finished = true;
-            return;
-        }
-        beta = beta / (1.0f - qq);
-    }
-    wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
-    wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
-    state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
-    out.cont = true;
-}
-
-// Warp-convergent tail of k_shade / k_guide_continue: queue compaction, shadow rays, records.
-BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t slot, bool cont,
-                        bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, bool record,
-                        uint32_t* err) {
-    uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
-    if (cont) wb.queue[(bounce + 1) & 1][pos] = slot;
-    pos = warp_append(&wb.counters[C_DONE], done_pending);
-    if (done_pending) wb.done[pos] = slot;
-    for (int k = 0; k < 2; ++k) {
-        pos = warp_append(&wb.counters[C_SHADOW], vo.push_sh[k]);
-        if (vo.push_sh[k]) {
-            if (pos < 2 * wb.capacity) {
-                wb.sh_o[pos] = vo.sh_o[k];
-                wb.sh_d[pos] = vo.sh_d[k];
-                wb.sh_ref[pos] = 2 * slot + (uint32_t)k;
-            } else {
-                atomicOr(err, ERR_QUEUE_OVERFLOW);
-            }
-        }
-    }
-    if (record) emit_records(gw, wb, slot, emit_n, L_emit);
-}
-
-// Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
-// In guided waves the matte / plastic / conductor classes stop after their emission and queue a
-// network query; k_guide_continue finishes them with the network's mixture.
-// GWK: guiding support compiled in (records, guided queries); the plain wavefront uses GWK = false.
-// Minimum resident CTAs per SM the shade kernels are compiled for: 4 caps them at 128 registers
-// (the plastic and conductor classes would use 148 / 159).  Measured on the production scene at
-// 4 spp: shade 7.1 ms against 7.7 ms unconstrained; 5 and 6 CTAs gave 7.3 and 7.1 ms.
-#ifndef BG_SHADE_MINBLOCKS
-#define BG_SHADE_MINBLOCKS 4
-#endif
-template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false>
-__global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
-                                               GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
-    constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
-    const uint32_t n = wb.counters[C_CLS + CLS];
-    const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ float strat_su[(!MULTI && !GWK && CLS != CLS_MISS) ? 8 * SU_STRIDE : 1];
-    const bool record = GWK && (gw.flags & GW_RECORD) != 0;
-    const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
-    const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
-    if (CLS == 3 && GWK && (gw.flags & GW_GUIDED) && blockIdx.x == 0 && threadIdx.x == 0)
-        wb.counters[C_GSPAN] = guide_base(wb, 2) + wb.counters[C_GUIDE + 2];  // classes 0..2 are done
-    // warp-uniform loop so the ballots below see all 32 lanes
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
-        uint32_t i = base + lane_id();
-        bool active = i < n;
-        uint32_t slot = active ? q[i] : 0;
-        bool cont = false, done_pending = false, push_guide = false;
-        VertexOut vo;
-        GuideQuery gq;
-        uint32_t emit_n = 0;
-        RGB L_emit = rgb(0.0f);
-        if (active) {
-            const SceneRender* sr = MULTI ? tab + wb.scene_id[slot] : nullptr;
-            const Scene& sc = pick<MULTI>(sc0, MULTI ? &sr->sc : nullptr);
-            const RenderParams& rp = pick<MULTI>(rp0, MULTI ? &sr->rp : nullptr);
-            const FilmBuffers& film = pick<MULTI>(film0, MULTI ? &sr->film : nullptr);
-            float4 ro = wb.ray_o[slot], rd = wb.ray_d[slot];
-            Ray ray = load_ray(ro, rd);
-            int prim = wb.hit[slot].x;
-            uint32_t state = wb.state[slot];
-            float4 b4 = wb.beta[slot];
-            RGB beta = rgb(b4.x, b4.y, b4.z);
-            float eta_scale = b4.w;
-            const float* su = nullptr;
-            if (!MULTI && !GWK && CLS != CLS_MISS && rp.strat.dims > 0) {
-                float* col = strat_su + threadIdx.x;
-                strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
-                su = col;
-            }
-            float4 l4 = wb.L[slot];
-            RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
-            state &= ~ST_PENDING;
-            bool specular_bounce = (state & ST_SPECULAR) != 0;
-            Isect it;
-            bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
-            const bool counted = bounce == 0 || specular_bounce;
-            RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
-            // an escaped ray gathers the infinite light's radiance (path.rs:78-85)
-            if (CLS == CLS_MISS && prim < 0 && counted && sc.inf) le = inf_radiance(sc, ray.d);
-            // The previous vertex's record closes here.  Its training target also takes this
-            // emission, which the estimator leaves to that vertex's next-event estimation: the
-            // network learns the directions of lights as well, for the strategy it serves.
-            if (record) state = close_record(gw, wb, slot, state, counted ? L : L - beta * le);
-            if (counted) L = L + beta * le;
-            bool finished = !hit || bounce >= rp.max_depth;
-            if (!finished && guided) {
-                gq = make_query(gw, it, -ray.d);
-                push_guide = true;
-            } else if (!finished) {
-                scatter_vertex<CLS, TEX, INF>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
-                                    vo, su);
-                finished = vo.finished;
-                cont = vo.cont;
-            }
-            wb.state[slot] = state;
-            wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
-            wb.L[slot] = make_float4(L.r, L.g, L.b, 0.0f);
-            if (finished) {
-                if (state & ST_PENDING) {
-                    done_pending = true;
-                } else {
-                    film_add(film, wb.pixel[slot], L);
-                    emit_n = rec_count(state);
-                    L_emit = L;
-                }
-            }
-        }
-        if (GUIDABLE && GWK && (gw.flags & GW_GUIDED)) {
-            uint32_t pos = gbase + warp_append(&wb.counters[C_GUIDE + (GUIDABLE ? CLS : 0)], push_guide);
-            if (push_guide && pos >= gw.cap) {
-                atomicOr(err, ERR_QUEUE_OVERFLOW);  // cannot happen: one query per path of the wave
-                push_guide = false;
-            }
-            if (push_guide) {
-                gw.query[3 * (size_t)pos] = gq.a;
-                gw.query[3 * (size_t)pos + 1] = gq.b;
-                gw.query[3 * (size_t)pos + 2] = gq.c;
-                gw.gslot[pos] = slot;
-            }
-        }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, record, err);
-    }
-}
-
-// Guided vertices of one material class, after the network has evaluated them: scatter_vertex with
-// the network's mixture in the second direct-light strategy.  Uniforms: the bounce's dims (shared
-// with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce (mixture choice, lobe,
-// cos theta, phi).
-template <int CLS>
-__global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
-                                                        GuideWave gw, uint32_t bounce, uint32_t* err) {
-    const uint32_t gbase = guide_base(wb, CLS);
-    const uint32_t n = min(wb.counters[C_GUIDE + CLS], gw.cap - min(gbase, gw.cap));
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
-        uint32_t i = gbase + base + lane_id();
-        bool active = base + lane_id() < n;
-        uint32_t slot = active ? gw.gslot[i] : 0;
-        bool cont = false, done_pending = false;
-        VertexOut vo;
-        uint32_t emit_n = 0;
-        RGB L_emit = rgb(0.0f);
-        if (active) {
-            Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
-            int prim = wb.hit[slot].x;
-            uint32_t state = wb.state[slot];
-            float4 b4 = wb.beta[slot];
-            RGB beta = rgb(b4.x, b4.y, b4.z);
-            float eta_scale = b4.w;
-            float4 l4 = wb.L[slot];
-            RGB L = rgb(l4.x, l4.y, l4.z);
-            bool finished = true;
-            Isect it;
-            if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
-                const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
-                float ug[4];
-                Rng{wb.pixel[slot], wb.sample[slot], rp.seed}.block(DIM_GUIDE0 + 4 * bounce, ug);
-                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, &mix, ug,
-                                    (gw.flags & GW_RECORD) != 0, vo);
-                finished = vo.finished;
-                cont = vo.cont;
-            }
-            wb.state[slot] = state;
-            wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
-            if (finished) {
-                if (state & ST_PENDING) {
-                    done_pending = true;
-                } else {
-                    film_add(film, wb.pixel[slot], L);
-                    emit_n = rec_count(state);
-                    L_emit = L;
-                }
-            }
-        }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, (gw.flags & GW_RECORD) != 0, err);
-    }
-}
-
 struct ShadowSrc {
     WaveBuffers wb;
     const SceneRender* tab;
@@ -1005,44 +461,12 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
         k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        if (gw.flags) {
-            k_shade<CLS_MISS, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<0, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        } else if (sc.inf) {  // the light list holds the infinite light
-            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            if (sc.ntex) {
-                k_shade<0, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-                k_shade<1, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            } else {
-                k_shade<0, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-                k_shade<1, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            }
-            k_shade<2, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<3, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        } else if (sc.ntex) {
-            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        } else {
-            k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        }
-        launches += 5;
+        if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s);
+        else launches += launch_shade_plain(sc, rp, film, wb, b, err, grid, block, s);
         if (guided && b < rp.max_depth) {
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GSPAN], gw.cap, gw.raw, true, err, ls.sms, s);
             launches += 1;
-            k_guide_continue<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-            k_guide_continue<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-            k_guide_continue<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-            launches += 3;
+            launches += launch_guide_continue(sc, rp, film, wb, gw, b, err, grid, block, s);
         }
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
@@ -1076,11 +500,7 @@ int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_dep
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab, false);
         k_bin<true><<<grid, block, 0, s>>>(sc, wb, b, tab);
-        k_shade<CLS_MISS, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-        k_shade<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-        k_shade<1, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-        k_shade<2, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-        k_shade<3, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        launch_shade_batch(tab, wb, b, err, grid, block, s);
         k_shadow<8, true><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, tab);
         k_finalize<true><<<grid, block, 0, s>>>(sc, film, wb, gw, tab);
         launches += 10;

@@ -1,0 +1,38 @@
+// bg_shade_plain.cu - the shade launches of single-scene wavefront renders: one kernel per
+// material class (misses included), in the variants for textured scenes and for scenes whose
+// light list holds the infinite light.
+#include "bg_wave.cuh"
+
+namespace bg {
+
+int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
+                       uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
+    const GuideWave gw{};
+    if (sc.inf) {  // the light list holds the infinite light
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        if (sc.ntex) {
+            k_shade<0, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        } else {
+            k_shade<0, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        }
+        k_shade<2, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    } else if (sc.ntex) {
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<1, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    } else {
+        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    }
+    return 5;
+}
+
+}  // namespace bg
