@@ -1492,6 +1492,7 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
     if (n > 65536) return fail(ctx, BG_ERR_INVALID, "at most 65536 scenes per batch");
     uint64_t total_pix = 0, total_items = 0;
     uint32_t max_depth = 0;
+    uint32_t variants = 0;  // bit 0: some scene is textured, bit 1: some scene holds an infinite light
     for (size_t i = 0; i < n; ++i) {
         const bg_batch_item& it = items[i];
         bg_render_opts o = it.opts;
@@ -1503,10 +1504,8 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         if (it.opts.mode != BG_MODE_PBRT) return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering needs BG_MODE_PBRT");
         if (it.opts.integrator != BG_INTEGRATOR_PATH)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering runs the path integrator only");
-        if (it.opts.sampler != BG_SAMPLER_INDEPENDENT)
-            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering takes the independent sampler only");
-        if (it.scene->dev.ntex || it.scene->has_inf)
-            return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering does not support textured scenes or infinite lights");
+        if (it.scene->dev.ntex) variants |= 1u;
+        if (it.scene->has_inf) variants |= 2u;
         total_pix += (uint64_t)it.camera.width * it.camera.height;
         total_items += (uint64_t)it.camera.width * it.camera.height * it.opts.spp;
         max_depth = std::max(max_depth, it.opts.max_depth);
@@ -1528,6 +1527,8 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         r.rp = bg::RenderParams{it.camera.width, it.camera.height, it.opts.spp, it.opts.max_depth, it.opts.first_sample,
                                 it.opts.rr_threshold, it.opts.seed};
         r.rp = bg::with_camera(r.rp, r.cam, it.opts.spp);
+        bg::strat_params(it.opts.sampler, it.opts.spp, it.opts.x_pixel_samples, it.opts.y_pixel_samples,
+                         it.opts.sampled_dimensions, it.opts.jitter_samples, &r.rp.strat);  // validated above
         r.film = ctx->film;
         r.film.sum += 3 * pix0;
         r.film.sumsq += 3 * pix0;
@@ -1553,7 +1554,7 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
     for (uint64_t w0 = 0; w0 < total_items; w0 += cap) {
         const uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, total_items - w0);
         launches += (uint64_t)bg::launch_wave_batch(d_tab, (uint32_t)n, max_depth, ctx->wave, w0, nitems, ctx->d_err,
-                                                    ctx->shape, ctx->stream);
+                                                    ctx->shape, ctx->stream, variants);
     }
     bg::launch_resolve(ctx->film, ctx->stream);
     launches += 1;

@@ -488,7 +488,8 @@ int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, cons
 }
 
 int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_depth, const WaveBuffers& wb,
-                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s) {
+                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s,
+                      uint32_t variants) {
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     const Scene sc{};
     const RenderParams rp{};
@@ -500,7 +501,7 @@ int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_dep
         k_prepare<<<1, 32, 0, s>>>(wb, b);
         k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab, false);
         k_bin<true><<<grid, block, 0, s>>>(sc, wb, b, tab);
-        launch_shade_batch(tab, wb, b, err, grid, block, s);
+        launch_shade_batch(tab, wb, b, err, grid, block, s, variants != 0);
         k_shadow<8, true><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, tab);
         k_finalize<true><<<grid, block, 0, s>>>(sc, film, wb, gw, tab);
         launches += 10;

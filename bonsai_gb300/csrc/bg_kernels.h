@@ -192,8 +192,11 @@ int launch_wave_chain(const Scene& sc, const Camera& cam, const RenderParams& rp
 // One wave of a batch render: items [item0, item0 + nitems) of the concatenated item spaces of
 // `nscenes` scenes (tab, device); paths of all scenes share the queues of one set of launches
 // (8-wide BVH layouts).  max_depth = the largest of the scenes'.  Returns the kernels launched.
+// variants: bit 0 some scene is textured, bit 1 some scene holds an infinite light (the shade
+// launches then take the variants that handle both per scene).
 int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_depth, const WaveBuffers& wb,
-                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s);
+                      uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls, cudaStream_t s,
+                      uint32_t variants = 0);
 void launch_resolve(const FilmBuffers& film, cudaStream_t s);
 void launch_clear_film(const FilmBuffers& film, cudaStream_t s);
 

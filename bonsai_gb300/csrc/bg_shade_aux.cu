@@ -23,16 +23,23 @@ int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuf
 }
 
 int launch_shade_batch(const SceneRender* tab, const WaveBuffers& wb, uint32_t b, uint32_t* err, dim3 grid, dim3 block,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool full) {
     const Scene sc{};
     const RenderParams rp{};
     const FilmBuffers film{};
     const GuideWave gw{};
     k_shade<CLS_MISS, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-    k_shade<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-    k_shade<1, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-    k_shade<2, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
-    k_shade<3, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+    if (full) {  // textures (matte, plastic) and the infinite light's next-event estimation, per scene
+        k_shade<0, true, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<1, true, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<2, true, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<3, true, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+    } else {
+        k_shade<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<1, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<2, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+        k_shade<3, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, tab);
+    }
     return 5;
 }
 

@@ -27,12 +27,11 @@ BG_D const TexPoint* tex_point(const Scene& sc, const Isect& it, const Ray& ray,
     tp->d = compute_differentials(it.p, it.n, tp->g, rd);
     return tp;
 }
-// The camera ray differentials of path (pixel, sample); `cam_ray` is its camera ray.
+// The camera ray differentials of path (pixel, sample) at its camera sample's film position (the
+// same sampler values as the ray's generation); `cam_ray` is its camera ray.
 BG_D RayDiff path_camera_diff(const RenderParams& rp, uint32_t pix, uint32_t s, const Ray& cam_ray) {
-    Rng rng{pix, s, rp.seed};
-    float c[4];
-    rng.block(0, c);
-    float fx = (float)(pix % rp.width) + c[0], fy = (float)(pix / rp.width) + c[1];
+    const CameraUs cu = camera_us(rp.strat, false, Rng{pix, s, rp.seed});
+    const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
     return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale);
 }
 // BSDF of a path vertex: textured materials read the camera differentials at the first hit
@@ -418,7 +417,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ float strat_su[(!MULTI && !GWK && CLS != CLS_MISS) ? 8 * SU_STRIDE : 1];
+    __shared__ float strat_su[(!GWK && CLS != CLS_MISS) ? 8 * SU_STRIDE : 1];
     const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
     const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
@@ -447,7 +446,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             RGB beta = rgb(b4.x, b4.y, b4.z);
             float eta_scale = b4.w;
             const float* su = nullptr;
-            if (!MULTI && !GWK && CLS != CLS_MISS && rp.strat.dims > 0) {
+            if (!GWK && CLS != CLS_MISS && rp.strat.dims > 0) {
                 float* col = strat_su + threadIdx.x;
                 strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
                 su = col;
@@ -570,7 +569,8 @@ int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffe
 int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                           const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,
                           cudaStream_t s);
+// full: the variants that handle textured scenes and infinite lights (checked per path's scene).
 int launch_shade_batch(const SceneRender* tab, const WaveBuffers& wb, uint32_t bounce, uint32_t* err, dim3 grid,
-                       dim3 block, cudaStream_t s);
+                       dim3 block, cudaStream_t s, bool full);
 
 }  // namespace bg

@@ -55,3 +55,25 @@ def test_batch_rejects_non_wide_scenes(gpu_ctx):
             G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 2, 3)])
     finally:
         sc.close()
+
+
+def test_batch_mixes_textures_infinite_lights_and_samplers(gpu_ctx):
+    """A batch of the reference's example scene (UV texture, infinite light, two emitting triangles;
+    4x4 stratified sampler), the textured room (image textures filtered with ray differentials)
+    and the Cornell box (independent sampler): each film equals its single-scene render."""
+    sds = [S.env_sphere(40, 32, spp=16, max_depth=5, extra=True), S.textured_room(24, 24, spp=4, max_depth=5),
+           S.cornell(16, 24, spp=4, max_depth=4)]
+    samplers = [S.StratifiedSampler(4, 4, 4, True), S.StratifiedSampler(2, 2, 2, False), None]
+    scenes = [G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE) for sd in sds]
+    try:
+        jobs = [G.BatchJob(sc, sd.camera, sd.spp, sd.max_depth, seed=5, sampler=smp)
+                for sc, sd, smp in zip(scenes, sds, samplers)]
+        imgs, st = G.render_batch(gpu_ctx, jobs)
+        assert st.error_word == 0
+        for sc, sd, smp, img in zip(scenes, sds, samplers, imgs):
+            r = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, seed=5, sampler=smp).render(sc)
+            np.testing.assert_allclose(img, r.rgb, rtol=1e-5, atol=1e-6)
+            assert img.mean() > 0.0
+    finally:
+        for sc in scenes:
+            sc.close()

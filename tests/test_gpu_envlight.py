@@ -144,14 +144,12 @@ def test_infinite_light_arguments(gpu_ctx):
         lib.bg_scene_destroy(h)
 
 
-def test_batch_and_guided_refuse_infinite_lights(gpu_ctx):
+def test_guided_refuses_infinite_lights(gpu_ctx):
     sd = S.env_sphere(16, 16, spp=1)
     sd.textures = []
     sd.materials = np.stack([S.material(S.MATTE, kd=(0.5, 0.5, 0.5))])
     sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
     try:
-        with pytest.raises(RuntimeError, match="infinite"):
-            G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 1, 2)])
         g = G.Guide(gpu_ctx)
         try:
             with pytest.raises(RuntimeError, match="infinite"):

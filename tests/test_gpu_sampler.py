@@ -37,9 +37,16 @@ def _pair(ctx, sd, mode, bvh, sampler, integrator=A.BG_INTEGRATOR_PATH, first_sa
 
 @pytest.mark.parametrize("mode,bvh", [(A.BG_MODE_PBRT, A.BG_BVH_WIDE), (A.BG_MODE_PBRT, A.BG_BVH_REFERENCE_FIXED),
                                       (A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE_FIXED)])
-@pytest.mark.parametrize("scene", ["example", "cornell"])
+@pytest.mark.parametrize("scene", ["example", "cornell", "textured"])
 def test_stratified_path_matches_oracle(gpu_ctx, mode, bvh, scene):
-    sd = S.env_sphere(40, 40, spp=16, max_depth=5, extra=True) if scene == "example" else S.cornell(40, 40, 16, 6)
+    """"textured": image textures filtered with the camera ray's differentials at the stratified
+    film position."""
+    if scene == "example":
+        sd = S.env_sphere(40, 40, spp=16, max_depth=5, extra=True)
+    elif scene == "cornell":
+        sd = S.cornell(40, 40, 16, 6)
+    else:
+        sd = S.textured_room(40, 40, spp=16, max_depth=5)
     r, o, cmp = _pair(gpu_ctx, sd, mode, bvh, MAIN)
     print(scene, cmp)
     assert r.stats.error_word == 0
@@ -113,8 +120,8 @@ def test_sampler_arguments(gpu_ctx):
             G.WhittedIntegrator(sd.camera, 4, 3, sampler=S.StratifiedSampler(2, 2, 2)).render(sc)
         it = G.PathIntegrator(sd.camera, 4, 3)
         it.sampler = S.StratifiedSampler(2, 2, 1)
-        with pytest.raises(RuntimeError, match="independent sampler"):
-            G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 4, 3, sampler=it.sampler)])
+        with pytest.raises(RuntimeError, match="x_pixel_samples"):  # batch items are checked alike
+            G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 4, 3, sampler=S.StratifiedSampler(4, 2, 1))])
         g = G.Guide(gpu_ctx)
         try:
             with pytest.raises(RuntimeError, match="independent sampler"):

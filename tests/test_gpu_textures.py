@@ -197,14 +197,12 @@ def test_texture_arguments(gpu_ctx):
         lib.bg_scene_destroy(h)
 
 
-def test_paths_without_texture_support_refuse_textured_scenes(gpu_ctx):
-    """Batch and guided renders use shade kernels without texture support: they refuse textured
-    scenes instead of rendering them untextured."""
+def test_guided_render_refuses_textured_scenes(gpu_ctx):
+    """Guided renders use shade kernels without texture support: they refuse textured scenes
+    instead of rendering them untextured (batch renders support textures)."""
     sd = S.textured_room(16, 16, spp=1)
     sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
     try:
-        with pytest.raises(RuntimeError, match="textured"):
-            G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 1, 2)])
         g = G.Guide(gpu_ctx)
         try:
             with pytest.raises(RuntimeError, match="textured"):
