@@ -194,7 +194,7 @@ typedef struct bg_render_opts {
  * order (the reference's shuffle never swaps); in PBRT mode each dimension is permuted.  Strata are
  * defined per aligned block of spp samples (first_sample a multiple of spp starts a new block).
  * Whitted and direct lighting accept sampled_dimensions <= 1 (the camera sample's calls); guided
- * and batch renders take the independent sampler only. */
+ * renders take the independent sampler only. */
 typedef enum bg_sampler { BG_SAMPLER_INDEPENDENT = 0, BG_SAMPLER_STRATIFIED = 1 } bg_sampler;
 
 /* The SamplerIntegrator behind bg_render.  PATH = PathIntegrator (src/integrators/path.rs);
@@ -395,7 +395,8 @@ bg_status bg_film_write_exr(bg_ctx* ctx, const char* path);
  * sequence of persistent launches: the paths of all scenes share the wavefront queues (each path
  * carries its scene index into a device table of scene, camera, render options and film slice),
  * so small and large scenes keep the GPU equally busy.  Scenes must be committed with
- * BG_BVH_WIDE and rendered in BG_MODE_PBRT with the path integrator (untextured scenes); each item's film is cleared and, when rgb_out is not
+ * BG_BVH_WIDE and rendered in BG_MODE_PBRT with the path integrator (textures, infinite lights and
+ * either sampler allowed, per item); each item's film is cleared and, when rgb_out is not
  * NULL, read back to it (width*height*3 floats).  Afterwards bg_film_moments returns the films of
  * all items concatenated in item order.  stats: device time and rays of the whole batch. */
 typedef struct bg_batch_item {
