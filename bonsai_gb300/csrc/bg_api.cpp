@@ -810,6 +810,13 @@ bg_status bg_scene_add_infinite_light(bg_scene* s, const bg_infinite_light* l) {
                       m[2] * (m[4] * m[9] - m[5] * m[8]);
     if (!(det != 0.0f) || !std::isfinite(det))
         return fail(s->ctx, BG_ERR_INVALID, "infinite light transform is singular");
+    if (l->rgb && l->width && l->height && (uint64_t)l->width * l->height <= (1ull << 28)) {
+        const size_t nf = 3 * (size_t)l->width * l->height;
+        for (size_t i = 0; i < nf; ++i)
+            if (!(l->rgb[i] >= 0.0f) || !std::isfinite(l->rgb[i]))
+                return fail(s->ctx, BG_ERR_INVALID,
+                            "environment map texels must be finite and >= 0 (its sampling distribution is a CDF)");
+    }
     bg::TexInfo ti{};
     ti.kind = BG_TEXTURE_IMAGE;
     ti.wrap = BG_WRAP_REPEAT;
@@ -910,6 +917,31 @@ void env_trilinear(const bg_scene* s, const bg::TexInfo& t, float s0, float t0, 
     env_bilerp(s, t, il + 1, s0, t0, b);
     for (int k = 0; k < 3; ++k) out[k] = (1.0f - f) * a[k] + f * b[k];
 }
+// find_interval (math.rs:70-87) over a cdf of `size` entries.
+uint32_t cdf_find_interval(const float* cdf, uint32_t size, float u) {
+    uint32_t first = 0, len = size;
+    while (len > 0) {
+        const uint32_t half = len >> 1, middle = first + half;
+        if (cdf[middle] <= u) {
+            first = middle + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    const int64_t r = (int64_t)first - 1;
+    return (uint32_t)(r < 0 ? 0 : (r > (int64_t)size - 2 ? (int64_t)size - 2 : r));
+}
+// Guide table of a cdf of n + 1 entries: g + 1 entries, entry k = find_interval at u = k / g.
+void cdf_guide(const float* cdf, uint32_t n, uint32_t g, uint32_t* out) {
+    for (uint32_t k = 0; k <= g; ++k) out[k] = cdf_find_interval(cdf, n + 1, (float)k / (float)g);
+}
+// Buckets for n intervals: a power of two near n / 8, at least 1.
+uint32_t guide_buckets(uint32_t n) {
+    uint32_t g = 1;
+    while (g * 16 <= n) g *= 2;
+    return g;
+}
 // Distribution1D::new (sampling.rs:22-47) over func[0..n): cdf has n + 1 entries.
 float dist1d_build(const float* func, uint32_t n, float* cdf) {
     cdf[0] = 0.0f;
@@ -970,12 +1002,20 @@ static bg_status commit_infinite_light(bg_scene* s, bg::InfLight* L) {
     L->nu = nu;
     L->nv = nv;
     L->marg_int = marg_int;
+    L->gu = guide_buckets(nu);
+    L->gv = guide_buckets(nv);
+    std::vector<uint32_t> cond_guide((size_t)nv * (L->gu + 1)), marg_guide(L->gv + 1);
+    for (uint32_t v = 0; v < nv; ++v)
+        cdf_guide(&cond_cdf[(size_t)v * (nu + 1)], nu, L->gu, &cond_guide[(size_t)v * (L->gu + 1)]);
+    cdf_guide(marg_cdf.data(), nv, L->gv, marg_guide.data());
     bg_status st;
     if ((st = upload(ctx, cond_cdf, &L->cond_cdf, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, func, &L->cond_func, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, cond_int, &L->cond_int, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, marg_cdf, &L->marg_cdf, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, cond_int, &L->marg_func, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, cond_guide, &L->cond_guide, &s->allocs)) != BG_OK) return st;
+    if ((st = upload(ctx, marg_guide, &L->marg_guide, &s->allocs)) != BG_OK) return st;
     CK(cudaStreamSynchronize(ctx->stream));  // the host vectors end here
     return BG_OK;
 }
@@ -1134,7 +1174,8 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         if ((st = commit_infinite_light(s, &inf[0])) != BG_OK) return st;
         if ((st = upload(ctx, inf, &d.inf, &s->allocs)) != BG_OK) return st;
         const uint64_t nu = inf[0].nu, nv = inf[0].nv;
-        inf_bytes = sizeof(bg::InfLight) + 4 * (nv * (nu + 1) + nu * nv + 2 * nv + nv + 1);
+        inf_bytes = sizeof(bg::InfLight) + 4 * (nv * (nu + 1) + nu * nv + 2 * nv + nv + 1) +
+                    4 * (nv * ((uint64_t)inf[0].gu + 1) + inf[0].gv + 1);
     }
     uint64_t nodes = 0;
     if (kind == BG_BVH_WIDE) {

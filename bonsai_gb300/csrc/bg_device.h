@@ -117,7 +117,12 @@ struct InfLight {
     const float* marg_cdf;
     const float* marg_func;
     float marg_int;
-    uint32_t pad;
+    // Guide tables (power-of-two bucket counts gu, gv): entry k of a CDF's table is its
+    // find_interval at u = k / g, so a search for u starts within [table[k], table[k + 1]],
+    // k = floor(u * g).  Row v's conditional table at cond_guide[v * (gu + 1)].
+    uint32_t gu, gv;
+    const uint32_t* cond_guide;
+    const uint32_t* marg_guide;
 };
 // Light-list entry of the infinite light in Scene::light_prims (area lights hold their triangle).
 constexpr uint32_t LIGHT_INFINITE = 0xFFFFFFFFu;

@@ -624,10 +624,25 @@ BG_D uint32_t find_interval(const float* cdf, uint32_t size, float u) {
     int32_t r = (int32_t)first - 1;
     return (uint32_t)(r < 0 ? 0 : (r > (int32_t)size - 2 ? (int32_t)size - 2 : r));
 }
-// Distribution1D::sample_continuous (sampling.rs:53-76); `count` is the divisor of the result
+// find_interval through a guide table of g (a power of two) buckets: the same index, since the
+// answer is monotone in u and k / g <= u < (k + 1) / g for k = floor(u * g) (exact in f32); every
+// index up to the answer has cdf <= u, so the last such index in [guide[k], guide[k + 1]] is it.
+BG_D uint32_t find_interval_guided(const float* cdf, float u, const uint32_t* guide, uint32_t g) {
+    const float x = u * (float)g;
+    uint32_t k = x >= (float)g ? g - 1 : (x > 0.0f ? (uint32_t)x : 0u);
+    uint32_t lo = guide[k], hi = guide[k + 1];
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (cdf[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+// Distribution1D::sample_continuous (sampling.rs:53-76); `count` is the divisor of the result;
+// `guide` (g buckets) accelerates the interval search.
 BG_D float dist1d_sample(const float* cdf, const float* func, float func_int, uint32_t n, uint32_t count, float u,
-                         float* pdf, uint32_t* off) {
-    uint32_t o = find_interval(cdf, n + 1, u);
+                         float* pdf, uint32_t* off, const uint32_t* guide = nullptr, uint32_t g = 0) {
+    uint32_t o = guide ? find_interval_guided(cdf, u, guide, g) : find_interval(cdf, n + 1, u);
     if (off) *off = o;
     float du = u - cdf[o];
     if (cdf[o + 1] - cdf[o] > 0.0f) du /= cdf[o + 1] - cdf[o];
@@ -640,10 +655,11 @@ template <bool REF>
 BG_D float2 dist2d_sample(const InfLight& L, float u0, float u1, float* pdf) {
     float p0, p1;
     uint32_t v = 0;
-    const float d1 = dist1d_sample(L.marg_cdf, L.marg_func, L.marg_int, L.nv, L.nv, u1, &p1, &v);
+    const float d1 = dist1d_sample(L.marg_cdf, L.marg_func, L.marg_int, L.nv, L.nv, u1, &p1, &v, L.marg_guide, L.gv);
     const uint32_t count = REF ? (L.nv - v) * L.nu : L.nu;
     const float d0 = dist1d_sample(L.cond_cdf + (size_t)v * (L.nu + 1), L.cond_func + (size_t)v * L.nu,
-                                   L.cond_int[v], L.nu, count, u0, &p0, nullptr);
+                                   L.cond_int[v], L.nu, count, u0, &p0, nullptr, L.cond_guide + (size_t)v * (L.gu + 1),
+                                   L.gu);
     *pdf = p0 * p1;
     return make_float2(d0, d1);
 }

@@ -304,9 +304,10 @@ bg_status bg_scene_add_spheres(bg_scene* scene, const bg_sphere* spheres, size_t
 /* Appends a texture; materials refer to it as *id + 1.  Image texels are copied and their MIPMap
  * pyramid is built here (Image::generate_pyramid, src/io/image.rs:55-114). */
 bg_status bg_scene_add_texture(bg_scene* scene, const bg_texture* tex, uint32_t* id);
-/* Sets the scene's InfiniteAreaLight (at most one); texels are copied.  Its MIPMap and the 2D
- * sampling distribution (InfiniteAreaLight::new) are built at commit, from the committed scene's
- * bounds (the light's world radius). */
+/* Sets the scene's InfiniteAreaLight (at most one); texels (finite, >= 0, power-of-two sizes) are
+ * copied and scaled by the intensity.  Its MIPMap is built here; the 2D sampling distribution
+ * (InfiniteAreaLight::new) and the search tables over its CDFs are built at commit, from the
+ * committed scene's bounds (the light's world radius). */
 bg_status bg_scene_add_infinite_light(bg_scene* scene, const bg_infinite_light* light);
 /* Appends n cylinders / disks / cones (GeometricPrimitive{Cylinder|Disk|Cone, material}). */
 bg_status bg_scene_add_quadrics(bg_scene* scene, const bg_quadric* quadrics, size_t n);

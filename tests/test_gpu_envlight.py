@@ -135,6 +135,13 @@ def test_infinite_light_arguments(gpu_ctx):
         sing = S.EnvMap(np.ones((8, 16, 3), np.float32), light_to_world=np.zeros((3, 4), np.float32))
         el, keep = S.env_struct(sing)
         assert lib.bg_scene_add_infinite_light(h, C.byref(el)) == A.BG_ERR_INVALID
+        bad = np.ones((8, 16, 3), np.float32)
+        bad[3, 4, 1] = -0.5
+        el, keep = S.env_struct(S.EnvMap(bad))
+        assert lib.bg_scene_add_infinite_light(h, C.byref(el)) == A.BG_ERR_INVALID
+        bad[3, 4, 1] = np.inf
+        el, keep = S.env_struct(S.EnvMap(bad))
+        assert lib.bg_scene_add_infinite_light(h, C.byref(el)) == A.BG_ERR_INVALID
         ok = S.EnvMap(np.ones((8, 16, 3), np.float32))
         el, keep = S.env_struct(ok)
         ctx.check(lib.bg_scene_add_infinite_light(h, C.byref(el)))
