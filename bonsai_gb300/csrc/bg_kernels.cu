@@ -50,7 +50,7 @@ struct TraceSrc {
 template <int LAYOUT, bool ANY>
 __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_trace(Scene sc, const float4* rays, uint32_t n, int2* hits, uint8_t* occ,
                                                uint32_t* err, unsigned long long* counters, uint32_t* head, int refill) {
-    if (LAYOUT != 1) {
+    if constexpr (LAYOUT != 1) {
         TraceSrc src{rays, hits, ANY ? occ : nullptr};
 #if BG_SMEM_STACK
         __shared__ uint2 stack8[STACK8 * 128];
@@ -60,17 +60,18 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_trace(Scene sc, const flo
         if (LAYOUT == 8) traverse_queue8<ANY>(sc, n, head, src, err, refill, stack8);
         else traverse_queue<ANY>(sc, n, head, src, err, refill);
         return;
-    }
-    for (;;) {
-        uint32_t base = warp_fetch(head);
-        if (base >= n) break;
-        uint32_t i = base + lane_id();
-        if (i < n) {
-            Ray ray = load_ray(__ldg(&rays[2 * i]), __ldg(&rays[2 * i + 1]));
-            ray.time = 0.0f;
-            int prim = ref_traverse<ANY>(sc, ray, err, counters);
-            if (ANY) occ[i] = prim >= 0 ? 1 : 0;
-            else hits[i] = make_int2(prim, __float_as_int(prim >= 0 ? ray.t_max : INFINITY));
+    } else {
+        for (;;) {
+            uint32_t base = warp_fetch(head);
+            if (base >= n) break;
+            uint32_t i = base + lane_id();
+            if (i < n) {
+                Ray ray = load_ray(__ldg(&rays[2 * i]), __ldg(&rays[2 * i + 1]));
+                ray.time = 0.0f;
+                int prim = ref_traverse<ANY>(sc, ray, err, counters);
+                if (ANY) occ[i] = prim >= 0 ? 1 : 0;
+                else hits[i] = make_int2(prim, __float_as_int(prim >= 0 ? ray.t_max : INFINITY));
+            }
         }
     }
 }
@@ -492,7 +493,6 @@ int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_dep
                       uint32_t variants) {
     dim3 grid(ls.sms * ls.blocks_per_sm), block(128);
     const Scene sc{};
-    const RenderParams rp{};
     const FilmBuffers film{};
     const GuideWave gw{};
     k_generate_batch<<<grid, block, 0, s>>>(tab, nscenes, wb, item0, nitems);
