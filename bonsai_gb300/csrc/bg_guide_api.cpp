@@ -576,10 +576,6 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering takes no GRAPH or STAGE_TIMING flag");
     if (o->integrator != BG_INTEGRATOR_PATH)
         return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering runs the path integrator only");
-    if (s->dev.ntex) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering does not support textured scenes");
-    if (s->has_inf) return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering does not support infinite lights");
-    if (o->sampler != BG_SAMPLER_INDEPENDENT)
-        return fail(ctx, BG_ERR_UNSUPPORTED, "guided rendering takes the independent sampler only");
     CK(cudaSetDevice(ctx->device));
     if ((st = ensure_film(ctx, cam->width, cam->height)) != BG_OK) return st;
     if (!(o->flags & BG_RENDER_ACCUMULATE)) {
@@ -630,6 +626,10 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         bg::RenderParams rp{cam->width, cam->height, k, o->max_depth, o->first_sample + done, o->rr_threshold, o->seed,
                             {lo[0], lo[1], lo[2]}, {inv[0], inv[1], inv[2]}};
         rp = bg::with_camera(rp, dc, o->spp);
+        // the stratified sampler's strata follow the global sample index (blocks of x * y samples),
+        // so passes of k samples keep them
+        bg::strat_params(o->sampler, o->spp, o->x_pixel_samples, o->y_pixel_samples, o->sampled_dimensions,
+                         o->jitter_samples, &rp.strat);
         const uint64_t items = npix * k;
         for (uint64_t item0 = 0; item0 < items; item0 += cap) {
             uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, items - item0);

@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
     const uint32_t n = wb.counters[C_CLS + CLS];
     const uint32_t* q = wb.cls_queue + (size_t)CLS * wb.capacity;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ float strat_su[(!GWK && CLS != CLS_MISS) ? 8 * SU_STRIDE : 1];
+    __shared__ float strat_su[CLS != CLS_MISS ? 8 * SU_STRIDE : 1];
     const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
     const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             RGB beta = rgb(b4.x, b4.y, b4.z);
             float eta_scale = b4.w;
             const float* su = nullptr;
-            if (!GWK && CLS != CLS_MISS && rp.strat.dims > 0) {
+            if (CLS != CLS_MISS && rp.strat.dims > 0) {
                 float* col = strat_su + threadIdx.x;
                 strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
                 su = col;
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             const bool counted = bounce == 0 || specular_bounce;
             RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
             // an escaped ray gathers the infinite light's radiance (path.rs:78-85)
-            if (CLS == CLS_MISS && prim < 0 && counted && sc.inf) le = inf_radiance(sc, ray.d);
+            if (CLS == CLS_MISS && prim < 0 && (counted || record) && sc.inf) le = inf_radiance(sc, ray.d);
             // The previous vertex's record closes here.  Its training target also takes this
             // emission, which the estimator leaves to that vertex's next-event estimation: the
             // network learns the directions of lights as well, for the strategy it serves.
@@ -510,9 +510,12 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
 // the network's mixture in the second direct-light strategy.  Uniforms: the bounce's dims (shared
 // with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce (mixture choice, lobe,
 // cos theta, phi).
-template <int CLS>
+// FULL: textures (matte, plastic) and the infinite light's next-event estimation compiled in (the
+// variants launched for scenes that have either).
+template <int CLS, bool FULL = false>
 __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
                                                         GuideWave gw, uint32_t bounce, uint32_t* err) {
+    __shared__ float strat_su[8 * SU_STRIDE];
     const uint32_t gbase = guide_base(wb, CLS);
     const uint32_t n = min(wb.counters[C_GUIDE + CLS], gw.cap - min(gbase, gw.cap));
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -535,12 +538,18 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
             RGB L = rgb(l4.x, l4.y, l4.z);
             bool finished = true;
             Isect it;
+            const float* su = nullptr;
+            if (rp.strat.dims > 0) {
+                float* col = strat_su + threadIdx.x;
+                strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
+                su = col;
+            }
             if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
                 const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
                 float ug[4];
                 Rng{wb.pixel[slot], wb.sample[slot], rp.seed}.block(DIM_GUIDE0 + 4 * bounce, ug);
-                scatter_vertex<CLS>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, &mix, ug,
-                                    (gw.flags & GW_RECORD) != 0, vo);
+                scatter_vertex<CLS, FULL && CLS <= 1, FULL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state,
+                                                            &mix, ug, (gw.flags & GW_RECORD) != 0, vo, su);
                 finished = vo.finished;
                 cont = vo.cont;
             }
@@ -565,6 +574,13 @@ int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffer
                        uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
 int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                         const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
+// The guided launches of scenes with textures or an infinite light (bg_shade_guided_full.cu).
+int launch_shade_guided_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
+                             const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,
+                             cudaStream_t s);
+int launch_guide_continue_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film,
+                               const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid,
+                               dim3 block, cudaStream_t s);
 // The guided vertices' continuation after the network inference (matte, plastic, conductor).
 int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                           const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,

@@ -151,22 +151,6 @@ def test_infinite_light_arguments(gpu_ctx):
         lib.bg_scene_destroy(h)
 
 
-def test_guided_refuses_infinite_lights(gpu_ctx):
-    sd = S.env_sphere(16, 16, spp=1)
-    sd.textures = []
-    sd.materials = np.stack([S.material(S.MATTE, kd=(0.5, 0.5, 0.5))])
-    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
-    try:
-        g = G.Guide(gpu_ctx)
-        try:
-            with pytest.raises(RuntimeError, match="infinite"):
-                G.PathIntegrator(sd.camera, 1, 2).render_guided(sc, g)
-        finally:
-            g.close()
-    finally:
-        sc.close()
-
-
 @pytest.mark.parametrize("mode,bvh", [(A.BG_MODE_PBRT, A.BG_BVH_WIDE),
                                       (A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE_FIXED)])
 def test_rotated_and_tinted_environment(gpu_ctx, mode, bvh):

@@ -122,11 +122,5 @@ def test_sampler_arguments(gpu_ctx):
         it.sampler = S.StratifiedSampler(2, 2, 1)
         with pytest.raises(RuntimeError, match="x_pixel_samples"):  # batch items are checked alike
             G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 4, 3, sampler=S.StratifiedSampler(4, 2, 1))])
-        g = G.Guide(gpu_ctx)
-        try:
-            with pytest.raises(RuntimeError, match="independent sampler"):
-                it.render_guided(sc, g)
-        finally:
-            g.close()
     finally:
         sc.close()

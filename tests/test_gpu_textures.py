@@ -197,22 +197,6 @@ def test_texture_arguments(gpu_ctx):
         lib.bg_scene_destroy(h)
 
 
-def test_guided_render_refuses_textured_scenes(gpu_ctx):
-    """Guided renders use shade kernels without texture support: they refuse textured scenes
-    instead of rendering them untextured (batch renders support textures)."""
-    sd = S.textured_room(16, 16, spp=1)
-    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
-    try:
-        g = G.Guide(gpu_ctx)
-        try:
-            with pytest.raises(RuntimeError, match="textured"):
-                G.PathIntegrator(sd.camera, 1, 2).render_guided(sc, g)
-        finally:
-            g.close()
-    finally:
-        sc.close()
-
-
 @pytest.mark.parametrize("shape", [(1, 1), (2, 64), (64, 2), (8, 8)])
 @pytest.mark.parametrize("wrap", [A.BG_WRAP_REPEAT, A.BG_WRAP_BLACK, A.BG_WRAP_CLAMP])
 def test_texture_shapes_and_wrap_modes(gpu_ctx, shape, wrap):
