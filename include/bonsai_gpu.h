@@ -193,8 +193,7 @@ typedef struct bg_render_opts {
  * draw from the counter RNG.  In REF_COMPAT mode every dimension visits the strata in the same
  * order (the reference's shuffle never swaps); in PBRT mode each dimension is permuted.  Strata are
  * defined per aligned block of spp samples (first_sample a multiple of spp starts a new block).
- * Whitted and direct lighting accept sampled_dimensions <= 1 (the camera sample's calls); guided
- * renders take the independent sampler only. */
+ * Whitted and direct lighting accept sampled_dimensions <= 1 (the camera sample's calls). */
 typedef enum bg_sampler { BG_SAMPLER_INDEPENDENT = 0, BG_SAMPLER_STRATIFIED = 1 } bg_sampler;
 
 /* The SamplerIntegrator behind bg_render.  PATH = PathIntegrator (src/integrators/path.rs);
