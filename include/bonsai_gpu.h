@@ -525,7 +525,8 @@ bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* 
  * estimates persist in the guide across calls, so a long render can be issued in chunks (with
  * BG_RENDER_ACCUMULATE and increasing first_sample).  Film, flags and rgb_out as in bg_render;
  * guide_stats counts this call's passes and reports the running estimates.  The path integrator
- * only, on untextured scenes (BG_ERR_UNSUPPORTED otherwise). */
+ * only (BG_ERR_UNSUPPORTED otherwise); textured scenes, infinite lights and the stratified sampler
+ * (strata follow the global sample index, so passes keep them) are supported. */
 bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* scene, bg_guide* guide, const bg_camera* camera,
                            const bg_render_opts* opts, float* rgb_out, bg_render_stats* stats,
                            bg_guide_stats* guide_stats);
