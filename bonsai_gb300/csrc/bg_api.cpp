@@ -216,6 +216,8 @@ bg::Camera make_camera(const bg_camera& c) {
     const F3 dx = sub(px, o), dy = sub(py, o);
     out.dxc[0] = dx.x; out.dxc[1] = dx.y; out.dxc[2] = dx.z;
     out.dyc[0] = dy.x; out.dyc[1] = dy.y; out.dyc[2] = dy.z;
+    out.lens_radius = c.lens_radius;
+    out.focal_distance = c.focal_distance;
     return out;
 }
 
@@ -1314,7 +1316,10 @@ bg_status bgi::validate_render(bg_ctx* ctx, const bg_scene* s, const bg_camera* 
     if (!s->committed || s->ctx != ctx) return fail(ctx, BG_ERR_INVALID, "scene not committed on this context");
     if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height >= (1ull << 31))
         return fail(ctx, BG_ERR_INVALID, "bad film resolution");
-    if (cam->lens_radius != 0.0f) return fail(ctx, BG_ERR_UNSUPPORTED, "thin-lens cameras are not supported");
+    if (!(cam->lens_radius >= 0.0f) || !std::isfinite(cam->lens_radius))
+        return fail(ctx, BG_ERR_INVALID, "lens_radius must be finite and >= 0");
+    if (cam->lens_radius > 0.0f && (!(cam->focal_distance > 0.0f) || !std::isfinite(cam->focal_distance)))
+        return fail(ctx, BG_ERR_INVALID, "a thin-lens camera needs a finite focal_distance > 0");
     if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) return fail(ctx, BG_ERR_INVALID, "fov out of range");
     if (o->mode > BG_MODE_PBRT) return fail(ctx, BG_ERR_INVALID, "unknown mode");
     if (o->mode == BG_MODE_REF_COMPAT && (s->kind == BG_BVH_WIDE || s->kind == BG_BVH_WIDE2))

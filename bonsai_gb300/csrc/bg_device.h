@@ -134,11 +134,12 @@ struct StratParams {
     uint32_t jitter;  // jitter_samples
 };
 
-struct Camera {   // PerspectiveCamera pinhole (src/cameras/perspective.rs:117-175)
+struct Camera {   // PerspectiveCamera (src/cameras/perspective.rs:117-175)
     float r2c[4][4];  // raster_to_camera.m
     float c2w[4][4];  // camera_to_world.m
     uint32_t width, height;
     float dxc[3], dyc[3];  // dx_camera, dy_camera: raster one-pixel steps in camera space
+    float lens_radius, focal_distance;  // thin lens (lens_radius 0: pinhole)
 };
 
 // Quadric record (8 x float4 = 128 B): rows 0-2 object_to_world (3x4), rows 3-5 world_to_object,

@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(128) k_megakernel(Scene sc, Camera cam, Render
         Rng rng{pix, s, rp.seed};
         const CameraUs cu = camera_us(rp.strat, REF, rng);
         float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-        Ray ray = camera_ray(cam, fx, fy, cu.time);
+        Ray ray = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         RayDiff rd;
-        if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale);
+        if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale, cu.lx, cu.ly);
         RGB L = radiance_ref<REF>(sc, ray, rng, rp.max_depth, rp.rr_threshold, err, sc.ntex ? &rd : nullptr,
                                   rp.strat);
         film_add(film, pix, L);

@@ -317,22 +317,54 @@ struct SamplerCalls {
 // time get_1d): the film offset and the time, from the stratified sampler or the counter RNG.
 struct CameraUs {
     float fx, fy, time;
+    float lx, ly;  // lens sample
 };
 BG_D CameraUs camera_us(const StratParams& sp, bool ref, const Rng& rng) {
     CameraUs c;
+    float b[4];
+    rng.block(0, b);  // film 0-1, lens 2-3
+    c.fx = b[0];
+    c.fy = b[1];
+    c.lx = b[2];
+    c.ly = b[3];
+    c.time = rng.u(DIM_TIME);
     if (sp.dims > 0) {
         float2 f = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
         c.fx = f.x;
         c.fy = f.y;
         c.time = strat_1d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
-    } else {
-        float b[4];
-        rng.block(0, b);
-        c.fx = b[0];
-        c.fy = b[1];
-        c.time = rng.u(DIM_TIME);
+        if (sp.dims > 1) {
+            const float2 l = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 1);
+            c.lx = l.x;
+            c.ly = l.y;
+        }
     }
     return c;
 }
 
+// concentric_sample_disk (sampling.rs:181-198)
+BG_D float2 concentric_sample_disk(float u0, float u1) {
+    const float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+    if (ox == 0.0f && oy == 0.0f) return make_float2(0.0f, 0.0f);
+    float theta, r;
+    if (fabsf(ox) > fabsf(oy)) {
+        theta = (PI / 4.0f) * (oy / ox);
+        r = ox;
+    } else {
+        theta = PI_OVER_TWO - (PI / 4.0f) * (ox / oy);
+        r = oy;
+    }
+    return make_float2(r * cosf(theta), r * sinf(theta));
+}
+// The camera-space origin and direction of a thin-lens camera ray (perspective.rs:127-139): the
+// lens point lens_radius * concentric_sample_disk(u) and the point where the pinhole direction d
+// meets the plane of focus.
+BG_D void thin_lens(const Camera& c, V3 d, float lu0, float lu1, V3* o, V3* dir) {
+    const float2 l = concentric_sample_disk(lu0, lu1);
+    const float lx = c.lens_radius * l.x, ly = c.lens_radius * l.y;
+    const float t = c.focal_distance / d.z;
+    const V3 focus = v3(0.0f + d.x * t, 0.0f + d.y * t, 0.0f + d.z * t);  // Ray::at from the origin
+    *o = v3(lx, ly, 0.0f);
+    *dir = normalize(focus - *o);
+}
 }  // namespace bg

@@ -113,7 +113,10 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
         return reject(BG_ERR_INVALID, std::to_string(cam->width) + "x" + std::to_string(cam->height) +
                                           " film exceeds the scratch limit of " +
                                           std::to_string(BG_NOALLOC_MAX_PIXELS) + " pixels");
-    if (cam->lens_radius != 0.0f) return reject(BG_ERR_UNSUPPORTED, "thin-lens cameras are not supported");
+    if (!(cam->lens_radius >= 0.0f) || !std::isfinite(cam->lens_radius))
+        return reject(BG_ERR_INVALID, "lens_radius must be finite and >= 0");
+    if (cam->lens_radius > 0.0f && (!(cam->focal_distance > 0.0f) || !std::isfinite(cam->focal_distance)))
+        return reject(BG_ERR_INVALID, "a thin-lens camera needs a finite focal_distance > 0");
     if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f)) return reject(BG_ERR_INVALID, "fov out of range");
     if (o->mode > BG_MODE_PBRT) return reject(BG_ERR_INVALID, "unknown mode");
     if (o->mode == BG_MODE_REF_COMPAT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2))

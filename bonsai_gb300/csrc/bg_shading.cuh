@@ -767,11 +767,14 @@ BG_D V3 xf_point(const float m[4][4], V3 p) {  // point3.rs:51-69
     return v3(xp, yp, zp) / wp;
 }
 // PerspectiveCamera::generate_ray, pinhole (perspective.rs:117-175) + Ray::transform (ray.rs:50-76)
-BG_D Ray camera_ray(const Camera& c, float fx, float fy, float tu) {
+// lu0, lu1: the lens sample (used when c.lens_radius > 0).
+BG_D Ray camera_ray(const Camera& c, float fx, float fy, float tu, float lu0 = 0.5f, float lu1 = 0.5f) {
     V3 cp = xf_point(c.r2c, v3(fx, fy, 0.0f));
     V3 d = normalize(cp);
+    V3 oc = v3(0.0f, 0.0f, 0.0f);
+    if (c.lens_radius > 0.0f) thin_lens(c, d, lu0, lu1, &oc, &d);
     const auto& m = c.c2w;
-    float x = 0.0f, y = 0.0f, z = 0.0f;
+    float x = oc.x, y = oc.y, z = oc.z;
     float xp = (m[0][0] * x + m[0][1] * y) + (m[0][2] * z + m[0][3]);
     float yp = (m[1][0] * x + m[1][1] * y) + (m[1][2] * z + m[1][3]);
     float zp = (m[2][0] * x + m[2][1] * y) + (m[2][2] * z + m[2][3]);

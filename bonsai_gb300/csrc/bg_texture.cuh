@@ -46,14 +46,19 @@ BG_D V3 xf_vec_h(const float m[4][4], V3 v) {  // Vec3::transform (vec3.rs:35-44
 // The camera ray's differentials for film point (fx, fy), moved to world space by
 // Ray::transform and scaled by Ray::scale_differentials(1 / sqrt(spp))
 // (src/base/integrator.rs:76-82).  `r` is the camera ray of the same sample (camera_ray).
-BG_D RayDiff camera_diff(const Camera& c, float fx, float fy, const Ray& r, float scale) {
+BG_D RayDiff camera_diff(const Camera& c, float fx, float fy, const Ray& r, float scale, float lu0 = 0.5f,
+                         float lu1 = 0.5f) {
     V3 cp = xf_point_h(c.r2c, v3(fx, fy, 0.0f));
     V3 dx = normalize(cp + v3(c.dxc[0], c.dxc[1], c.dxc[2]));
     V3 dy = normalize(cp + v3(c.dyc[0], c.dyc[1], c.dyc[2]));
-    V3 o = xf_point_h(c.c2w, v3(0.0f, 0.0f, 0.0f));
+    V3 oxc = v3(0.0f, 0.0f, 0.0f), oyc = oxc;
+    if (c.lens_radius > 0.0f) {  // perspective.rs:141-157: both offset rays through the same lens point
+        thin_lens(c, dx, lu0, lu1, &oxc, &dx);
+        thin_lens(c, dy, lu0, lu1, &oyc, &dy);
+    }
     RayDiff d;
-    d.rxo = o;
-    d.ryo = o;
+    d.rxo = xf_point_h(c.c2w, oxc);
+    d.ryo = xf_point_h(c.c2w, oyc);
     d.rxd = xf_vec_h(c.c2w, dx);
     d.ryd = xf_vec_h(c.c2w, dy);
     d.rxo = r.o + (d.rxo - r.o) * scale;

@@ -140,9 +140,9 @@ __global__ void __launch_bounds__(128) k_tree(Scene sc, Camera cam, RenderParams
         const Rng rng{pix, s, rp.seed, 0u};
         const CameraUs cu = camera_us(rp.strat, REF, rng);  // sampled_dimensions <= 1: camera only
         const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-        const Ray ray = camera_ray(cam, fx, fy, cu.time);
+        const Ray ray = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         RayDiff rd;
-        if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale);
+        if (sc.ntex) rd = camera_diff(cam, fx, fy, ray, rp.diff_scale, cu.lx, cu.ly);
         RGB L = tree_radiance<REF, LAYOUT>(sc, rp, kind, ray, sc.ntex ? &rd : nullptr, pix, s, err);
         film_add(film, pix, L);
     }

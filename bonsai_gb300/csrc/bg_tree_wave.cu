@@ -41,12 +41,12 @@ __global__ void k_tw_gen(Camera cam, RenderParams rp, TreeWave tw, uint64_t item
         const Rng rng{pix, s, rp.seed, 0u};
         const CameraUs cu = camera_us(rp.strat, false, rng);  // sampled_dimensions <= 1: camera only
         const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-        const Ray r = camera_ray(cam, fx, fy, cu.time);
+        const Ray r = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         tw.ray_o[0][i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
         tw.ray_d[0][i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
         tw.beta[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         tw.meta[0][i] = make_uint4(i, 1u, 0u, tw.textured);
-        if (tw.textured) store_rd(tw.rd[0], i, camera_diff(cam, fx, fy, r, rp.diff_scale));
+        if (tw.textured) store_rd(tw.rd[0], i, camera_diff(cam, fx, fy, r, rp.diff_scale, cu.lx, cu.ly));
         tw.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }

@@ -32,7 +32,7 @@ BG_D const TexPoint* tex_point(const Scene& sc, const Isect& it, const Ray& ray,
 BG_D RayDiff path_camera_diff(const RenderParams& rp, uint32_t pix, uint32_t s, const Ray& cam_ray) {
     const CameraUs cu = camera_us(rp.strat, false, Rng{pix, s, rp.seed});
     const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-    return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale);
+    return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale, cu.lx, cu.ly);
 }
 // BSDF of a path vertex: textured materials read the camera differentials at the first hit
 // (PathIntegrator spawns later rays without differentials, path.rs:139).
@@ -80,7 +80,7 @@ BG_D void generate_one(const Camera& cam, const RenderParams& rp, const WaveBuff
     Rng rng{pix, s, rp.seed};
     const CameraUs cu = camera_us(rp.strat, false, rng);
     float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
-    Ray r = camera_ray(cam, fx, fy, cu.time);
+    Ray r = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
     wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
     wb.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, r.time);
     wb.pixel[i] = pix;

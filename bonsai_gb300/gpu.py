@@ -160,8 +160,8 @@ def camera_struct(cam: S.Camera) -> A.bg_camera:
     c.fov_deg = cam.fov_deg
     c.near_plane = cam.near_plane
     c.far_plane = cam.far_plane
-    c.lens_radius = 0.0
-    c.focal_distance = 1e6
+    c.lens_radius = cam.lens_radius
+    c.focal_distance = cam.focal_distance
     c.width = cam.width
     c.height = cam.height
     return c

@@ -194,6 +194,8 @@ class Camera:
     height: int
     near_plane: float = 0.01
     far_plane: float = 1000.0
+    lens_radius: float = 0.0        # thin lens (0: pinhole)
+    focal_distance: float = 1e6
 
 
 @dataclass

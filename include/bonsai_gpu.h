@@ -162,7 +162,7 @@ typedef struct bg_camera {
     float fov_deg;
     float near_plane;
     float far_plane;
-    float lens_radius;    /* must be 0: thin-lens depth of field is not supported */
+    float lens_radius;    /* thin-lens depth of field (0: pinhole), perspective.rs:127-139 */
     float focal_distance;
     uint32_t width;
     uint32_t height;

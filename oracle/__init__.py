@@ -57,7 +57,7 @@ def lib() -> C.CDLL:
         L.orc_bsdf_eval.argtypes = [P, P, P, C.c_int32, P]
         L.orc_rng_uniform.restype = C.c_float
         L.orc_rng_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
-        L.orc_camera_ray.argtypes = [C.POINTER(bg_camera), C.c_float, C.c_float, C.c_float, P]
+        L.orc_camera_ray.argtypes = [C.POINTER(bg_camera), C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P]
         L.orc_philox.argtypes = [P, P, P]
         _lib = L
     return _lib
@@ -75,8 +75,8 @@ def camera_struct(cam: S.Camera) -> bg_camera:
     c.fov_deg = cam.fov_deg
     c.near_plane = cam.near_plane
     c.far_plane = cam.far_plane
-    c.lens_radius = 0.0
-    c.focal_distance = 1e6
+    c.lens_radius = cam.lens_radius
+    c.focal_distance = cam.focal_distance
     c.width = cam.width
     c.height = cam.height
     return c
@@ -190,10 +190,11 @@ def philox(ctr, key) -> np.ndarray:
     return out
 
 
-def camera_ray(cam: S.Camera, fx: float, fy: float, tu: float = 0.0) -> np.ndarray:
+def camera_ray(cam: S.Camera, fx: float, fy: float, tu: float = 0.0, lens=(0.5, 0.5)) -> np.ndarray:
+    """(origin, direction) of PerspectiveCamera::generate_ray; `lens` is the lens sample (thin lens)."""
     c = camera_struct(cam)
     out = np.zeros(6, np.float32)
-    lib().orc_camera_ray(C.byref(c), fx, fy, tu, _ptr(out))
+    lib().orc_camera_ray(C.byref(c), fx, fy, tu, lens[0], lens[1], _ptr(out))
     return out
 
 

@@ -1853,9 +1853,12 @@ static RGB estimate_direct(const Scene& s, const Interaction& it, const BSDF& bs
 struct Camera {
     Transform raster_to_camera, camera_to_world;
     int w, h;
+    float lens_radius = 0.0f, focal_distance = 1e6f;
     explicit Camera(const bg_camera& c) {  // perspective.rs:49-113
         w = (int)c.width;
         h = (int)c.height;
+        lens_radius = c.lens_radius;
+        focal_distance = c.focal_distance;
         float rx = (float)c.width, ry = (float)c.height;
         Transform c2s = t_perspective(c.fov_deg, c.near_plane, c.far_plane);
         float sminx, smaxx, sminy, smaxy;
@@ -1870,25 +1873,44 @@ struct Camera {
         camera_to_world = t_look_at(V3(c.position[0], c.position[1], c.position[2]),
                                     V3(c.look_at[0], c.look_at[1], c.look_at[2]), V3(c.up[0], c.up[1], c.up[2]));
     }
-    Ray generate_ray(float fx, float fy, float tu) const {  // perspective.rs:117-175 (pinhole)
+    // The lens point and the direction through the plane of focus (perspective.rs:127-139).
+    void thin_lens(V3 d, float lu0, float lu1, V3* o, V3* dir) const {
+        float ly;
+        float lx = concentric_sample_disk(lu0, lu1, &ly).x;
+        lx = lens_radius * lx;
+        ly = lens_radius * ly;
+        float t = focal_distance / d.z;
+        V3 focus(0.0f + d.x * t, 0.0f + d.y * t, 0.0f + d.z * t);  // Ray::at from the origin
+        *o = V3(lx, ly, 0.0f);
+        *dir = normalize(focus - *o);
+    }
+    Ray generate_ray(float fx, float fy, float tu, float lu0 = 0.5f, float lu1 = 0.5f) const {  // perspective.rs:117-175
         V3 cp = xf_point(raster_to_camera, V3(fx, fy, 0.0f));
         Ray r{V3(0, 0, 0), normalize(cp), INFINITY, 0.0f};
+        if (lens_radius > 0.0f) thin_lens(r.d, lu0, lu1, &r.o, &r.d);
         r.time = (1.0f - tu) * 0.0f + tu * 1.0f;  // lerp(time, 0, 1), math.rs:7-9
         return xf_ray(camera_to_world, r);
     }
     // The same ray's differentials (perspective.rs:141-170), moved to world space by Ray::transform
     // (ray.rs:66-73) and scaled by Ray::scale_differentials (ray.rs:41-48).
-    RayDifferential differentials(float fx, float fy, const Ray& world_ray, float scale) const {
+    RayDifferential differentials(float fx, float fy, const Ray& world_ray, float scale, float lu0 = 0.5f,
+                                  float lu1 = 0.5f) const {
         V3 origin = xf_point(raster_to_camera, V3(0, 0, 0));
         V3 dx_camera = xf_point(raster_to_camera, V3(1, 0, 0)) - origin;  // perspective.rs:86-89
         V3 dy_camera = xf_point(raster_to_camera, V3(0, 1, 0)) - origin;
         V3 cp = xf_point(raster_to_camera, V3(fx, fy, 0.0f));
+        V3 dx = normalize(cp + dx_camera), dy = normalize(cp + dy_camera);
+        V3 ox(0, 0, 0), oy(0, 0, 0);
+        if (lens_radius > 0.0f) {  // perspective.rs:141-157
+            thin_lens(dx, lu0, lu1, &ox, &dx);
+            thin_lens(dy, lu0, lu1, &oy, &dy);
+        }
         RayDifferential d;
         d.has = true;
-        d.rxo = xf_point(camera_to_world, V3(0, 0, 0));
-        d.ryo = d.rxo;
-        d.rxd = xf_vec(camera_to_world, normalize(cp + dx_camera));
-        d.ryd = xf_vec(camera_to_world, normalize(cp + dy_camera));
+        d.rxo = xf_point(camera_to_world, ox);
+        d.ryo = xf_point(camera_to_world, oy);
+        d.rxd = xf_vec(camera_to_world, dx);
+        d.ryd = xf_vec(camera_to_world, dy);
         const V3 o = world_ray.o, dd = world_ray.d;
         d.rxo = o + (d.rxo - o) * scale;
         d.ryo = o + (d.ryo - o) * scale;
@@ -2361,15 +2383,17 @@ int orc_render(void* p, const bg_camera* cam, const bg_render_opts* opts, int32_
                         rng.sample = opts->first_sample + si;
                         // Sampler::get_camera_sample: film get_2d, lens get_2d, time get_1d
                         float ux = rng.u(DIM_FILM), uy = rng.u(DIM_FILM + 1);
+                        float lx = rng.u(DIM_LENS), ly = rng.u(DIM_LENS + 1);
                         float ut = rng.u(DIM_TIME);
                         if (sp.dims > 0) {
                             strat_2d(sp, mode == REF, rng, 0, &ux, &uy);
                             ut = strat_1d(sp, mode == REF, rng, 0);
+                            if (sp.dims > 1) strat_2d(sp, mode == REF, rng, 1, &lx, &ly);
                         }
                         float fx = (float)x + ux, fy = (float)y + uy;
-                        Ray ray = camera.generate_ray(fx, fy, ut);
+                        Ray ray = camera.generate_ray(fx, fy, ut, lx, ly);
                         RayDifferential rd;
-                        if (!s.tex.empty()) rd = camera.differentials(fx, fy, ray, diff_scale);
+                        if (!s.tex.empty()) rd = camera.differentials(fx, fy, ray, diff_scale, lx, ly);
                         Counters local;
                         Counters* cc = cnt ? cnt : (counters ? &local : nullptr);
                         RGB L = opts->integrator == BG_INTEGRATOR_PATH
@@ -2472,9 +2496,9 @@ float orc_rng_uniform(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t d
     return r.u(dim);
 }
 // Camera ray for a film sample (perspective.rs:117-175): out = ox oy oz dx dy dz.
-void orc_camera_ray(const bg_camera* cam, float fx, float fy, float tu, float* out) {
+void orc_camera_ray(const bg_camera* cam, float fx, float fy, float tu, float lu0, float lu1, float* out) {
     Camera c(*cam);
-    Ray r = c.generate_ray(fx, fy, tu);
+    Ray r = c.generate_ray(fx, fy, tu, lu0, lu1);
     out[0] = r.o.x; out[1] = r.o.y; out[2] = r.o.z; out[3] = r.d.x; out[4] = r.d.y; out[5] = r.d.z;
 }
 

@@ -140,3 +140,45 @@ def test_tiled_pixel_order_changes_only_the_summation_order(gpu_ctx, w, h):
             np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
     finally:
         sc.close()
+
+
+@pytest.mark.parametrize("mode,bvh,integrator", [(A.BG_MODE_PBRT, A.BG_BVH_WIDE, A.BG_INTEGRATOR_PATH),
+                                                 (A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE_FIXED, A.BG_INTEGRATOR_PATH),
+                                                 (A.BG_MODE_PBRT, A.BG_BVH_WIDE, A.BG_INTEGRATOR_WHITTED)])
+@pytest.mark.parametrize("scene", ["example", "textured"])
+def test_thin_lens_camera_matches_oracle(gpu_ctx, mode, bvh, integrator, scene):
+    """PerspectiveCamera with a lens (perspective.rs:127-157): depth of field through the counter
+    RNG's lens dimensions, and the ray differentials of a thin lens for texture filtering."""
+    if scene == "example":
+        sd = S.env_sphere(40, 32, spp=16, max_depth=5, extra=True)
+        sd.camera.lens_radius, sd.camera.focal_distance = 0.3, 4.0
+    else:
+        sd = S.textured_room(40, 32, spp=16, max_depth=5)
+        sd.camera.lens_radius, sd.camera.focal_distance = 0.15, 3.0
+    o = O.OracleScene(sd, fixed_bvh=True).render(mode, spp=16, integrator=integrator)
+    sc = G.Scene(gpu_ctx, sd, bvh)
+    try:
+        it = (G.PathIntegrator(sd.camera, 16, 5, mode=mode) if integrator == A.BG_INTEGRATOR_PATH
+              else G.WhittedIntegrator(sd.camera, 16, 5, mode=mode))
+        r = it.render(sc)
+    finally:
+        sc.close()
+    s1, s2, n = G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height)
+    cmp = compare_renders(s1, s2, n, o["sum"], o["sumsq"], np.full(n.shape, 16))
+    print(scene, cmp)
+    assert r.stats.error_word == 0
+    assert cmp["frac_z3"] <= 0.01
+    assert cmp["frac_close"] >= 0.85
+
+
+def test_camera_lens_arguments(gpu_ctx):
+    sd = S.cornell(8, 8, spp=1)
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    try:
+        for lr, fd in ((-0.1, 1.0), (0.1, 0.0), (float("nan"), 1.0)):
+            cam = S.Camera(sd.camera.position, sd.camera.look_at, sd.camera.up, sd.camera.fov_deg, 8, 8,
+                           lens_radius=lr, focal_distance=fd)
+            with pytest.raises(RuntimeError, match="lens|focal"):
+                G.PathIntegrator(cam, 1, 2).render(sc)
+    finally:
+        sc.close()

@@ -134,3 +134,31 @@ def test_oren_nayar_sigma_zero_is_lambertian():
     a = O.bsdf_eval(S.material(S.MATTE, kd=(0.6, 0.5, 0.4), sigma=0.0), wo, wi, A.BG_MODE_PBRT)
     b = O.bsdf_eval(S.material(S.MATTE, kd=(0.6, 0.5, 0.4)), wo, wi, A.BG_MODE_PBRT)
     np.testing.assert_array_equal(a, b)
+
+
+def test_thin_lens_rays_meet_on_the_plane_of_focus():
+    """PerspectiveCamera with a lens (perspective.rs:127-139): the rays of one film point through
+    different lens points cross the plane at focal_distance along the view axis in one point, and
+    their origins lie on the lens disk of radius lens_radius."""
+    cam = S.Camera((0.0, 1.0, 6.0), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0), 40.0, 64, 48, lens_radius=0.25,
+                   focal_distance=4.0)
+    pos = np.array(cam.position, np.float64)
+    fwd = np.array(cam.look_at, np.float64) - pos
+    fwd /= np.linalg.norm(fwd)
+    rng = np.random.default_rng(3)
+    for fx, fy in ((10.5, 7.25), (32.0, 24.0), (60.0, 40.0)):
+        pts = []
+        for lu in rng.random((12, 2)):
+            r = O.camera_ray(cam, fx, fy, 0.0, lens=tuple(lu)).astype(np.float64)
+            o, d = r[:3], r[3:]
+            assert np.linalg.norm(o - pos) <= 0.25 * (1 + 1e-5) + 1e-5
+            assert abs(np.dot(o - pos, fwd)) < 1e-4  # the lens plane is perpendicular to the view axis
+            t = (4.0 - np.dot(o - pos, fwd)) / np.dot(d, fwd)
+            pts.append(o + t * d)
+        pts = np.array(pts)
+        assert np.abs(pts - pts.mean(axis=0)).max() < 2e-4
+        # the pinhole ray of the film point passes through the same focus point
+        pin = S.Camera(cam.position, cam.look_at, cam.up, 40.0, 64, 48)
+        r = O.camera_ray(pin, fx, fy).astype(np.float64)
+        t = (4.0 - np.dot(r[:3] - pos, fwd)) / np.dot(r[3:], fwd)
+        assert np.abs(r[:3] + t * r[3:] - pts.mean(axis=0)).max() < 1e-3
