@@ -124,3 +124,11 @@ def test_sampler_arguments(gpu_ctx):
             G.render_batch(gpu_ctx, [G.BatchJob(sc, sd.camera, 4, 3, sampler=S.StratifiedSampler(4, 2, 1))])
     finally:
         sc.close()
+
+
+def test_stratified_lens_samples(gpu_ctx):
+    """sampled_dimensions >= 2: the thin lens takes the sampler's second get_2d call."""
+    sd = S.env_sphere(40, 32, spp=16, max_depth=5, extra=True)
+    sd.camera.lens_radius, sd.camera.focal_distance = 0.3, 4.0
+    r, o, cmp = _pair(gpu_ctx, sd, A.BG_MODE_PBRT, A.BG_BVH_WIDE, MAIN)
+    assert cmp["frac_z3"] <= 0.01 and cmp["frac_close"] >= 0.85, cmp
