@@ -841,8 +841,8 @@ bg_status bg_scene_add_spheres(bg_scene* s, const bg_sphere* sp, size_t n) {
     if (s->committed) return fail(s->ctx, BG_ERR_INVALID, "scene already committed");
     for (size_t i = 0; i < n; ++i) {
         if (sp[i].material_id >= s->mats.size()) return fail(s->ctx, BG_ERR_INVALID, "sphere has an unknown material id");
-        if (sp[i].light_id >= 0)
-            return fail(s->ctx, BG_ERR_UNSUPPORTED, "spherical area lights are not supported");
+        if (sp[i].light_id >= (int32_t)s->lights.size())
+            return fail(s->ctx, BG_ERR_INVALID, "sphere has an unknown area light id");
         if (!(sp[i].radius > 0.0f) || !std::isfinite(sp[i].radius))
             return fail(s->ctx, BG_ERR_INVALID, "sphere radius must be finite and > 0");
     }
@@ -857,7 +857,10 @@ bg_status bg_scene_add_quadrics(bg_scene* s, const bg_quadric* q, size_t n) {
     for (size_t i = 0; i < n; ++i) {
         if (q[i].kind > BG_QUADRIC_CONE) return fail(s->ctx, BG_ERR_INVALID, "unknown quadric kind");
         if (q[i].material_id >= s->mats.size()) return fail(s->ctx, BG_ERR_INVALID, "quadric has an unknown material id");
-        if (q[i].light_id >= 0) return fail(s->ctx, BG_ERR_UNSUPPORTED, "quadric area lights are not supported");
+        if (q[i].light_id >= (int32_t)s->lights.size())
+            return fail(s->ctx, BG_ERR_INVALID, "quadric has an unknown area light id");
+        if (q[i].light_id >= 0 && q[i].kind == BG_QUADRIC_CONE)
+            return fail(s->ctx, BG_ERR_UNSUPPORTED, "cones cannot be area lights (the reference's Cone has no sample())");
         if (!(q[i].radius > 0.0f) || !std::isfinite(q[i].radius))
             return fail(s->ctx, BG_ERR_INVALID, "quadric radius must be finite and > 0");
         if (q[i].kind == BG_QUADRIC_CONE && !(q[i].height != 0.0f))
@@ -1131,7 +1134,21 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
         std::memcpy(emis[i].intensity, s->lights[i].intensity, sizeof(emis[i].intensity));
         emis[i].two_sided = s->lights[i].two_sided;
     }
-    // the light list: emitting triangles in order, then the infinite light
+    // the light list: emitting triangles, spheres and quadrics in order, then the infinite light
+    std::vector<int32_t> sph_emis(nsph, -1), quad_emis(nquad, -1);
+    bool any_sph_light = false, any_quad_light = false;
+    for (uint32_t i = 0; i < nsph; ++i)
+        if (s->sph[i].light_id >= 0) {
+            sph_emis[i] = s->sph[i].light_id;
+            light_prims.push_back(ntri + i);
+            any_sph_light = true;
+        }
+    for (uint32_t i = 0; i < nquad; ++i)
+        if (s->quads[i].light_id >= 0) {
+            quad_emis[i] = s->quads[i].light_id;
+            light_prims.push_back(ntri + nsph + i);
+            any_quad_light = true;
+        }
     if (s->has_inf) light_prims.push_back(bg::LIGHT_INFINITE);
     bg::Scene& d = s->dev;
     d = bg::Scene{};
@@ -1147,6 +1164,8 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if ((st = upload(ctx, mats, &d.mats, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, emis, &d.emis, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, light_prims, &d.light_prims, &s->allocs)) != BG_OK) return st;
+    if (any_sph_light && (st = upload(ctx, sph_emis, &d.sph_emis, &s->allocs)) != BG_OK) return st;
+    if (any_quad_light && (st = upload(ctx, quad_emis, &d.quad_emis, &s->allocs)) != BG_OK) return st;
     if (s->any_normals || s->any_flags) {
         std::vector<uint8_t> flags;
         std::string why;

@@ -156,6 +156,8 @@ struct Scene {
     uint32_t pad2;
     const float4* sph;
     const uint32_t* sph_mat;
+    const int32_t* sph_emis;   // emission record per sphere (-1 none); null: no emitting sphere
+    const int32_t* quad_emis;  // the same per quadric
     const Material* mats;
     const Emission* emis;
     const uint32_t* light_prims;  // Scene::lights order: one DiffuseAreaLight per emitting triangle

@@ -544,7 +544,10 @@ BG_D RGB emission(const Emission& e, V3 n, V3 dir) {
     return rgb(0.0f);
 }
 BG_D int prim_emission(const Scene& sc, int prim) {
-    return (uint32_t)prim < sc.ntri ? __float_as_int(sc.tri[3 * prim + 1].w) : -1;
+    if (prim < 0) return -1;
+    if ((uint32_t)prim < sc.ntri) return __float_as_int(sc.tri[3 * prim + 1].w);
+    if ((uint32_t)prim < sc.ntri + sc.nsph) return sc.sph_emis ? sc.sph_emis[prim - sc.ntri] : -1;
+    return sc.quad_emis ? sc.quad_emis[prim - sc.ntri - sc.nsph] : -1;
 }
 BG_D RGB emitted_radiance(const Scene& sc, const Isect& it, V3 w) {  // interaction.rs:257-266
     int e = prim_emission(sc, it.prim);
@@ -558,17 +561,101 @@ struct LightSample {
     float pdf;
     ShapeSample pt;
 };
-// DiffuseAreaLight::sample_point + Shape::sample_from_it (diffuse.rs:54-87, shape.rs:17-34)
+
+// ---- shapes as area lights: Shape::sample (sphere.rs:328-355, disk.rs:184-214, cylinder.rs:289-321)
+// and area (sphere.rs:375-377, disk.rs:216-218, cylinder.rs:323-325).  Spheres are full with a
+// translation-only transform; quadrics carry their affine transform (rows 0-2 object-to-world,
+// rows 3-5 world-to-object).
+BG_D float sphere_area(float r) { return (360.0f * (PI / 180.0f)) * r * (r - (-r)); }
+BG_D float quadric_area(const float4* q) {
+    const float4 p0 = q[6], p1 = q[7];
+    const int kind = (int)(__float_as_uint(p1.z) & 0xFFu);
+    if (kind == 1) return p1.y * 0.5f * (p0.x * p0.x - p0.y * p0.y);  // disk
+    return (p0.w - p0.z) * p0.x * p1.y;                                // cylinder
+}
+// Sphere::sample.  REF (F21): the normal is the object-space point itself, not normalised (length
+// radius), so Shape::sample_from_it's |cos| and pdf carry a factor radius.
+template <bool REF>
+BG_D ShapeSample sphere_light_sample(float4 s, float u0, float u1) {
+    const float r = s.w;
+    const float z = 1.0f - 2.0f * u0;  // uniform_sample_sphere (sampling.rs:211-216)
+    const float rr = sqrtf(rmax(1.0f - z * z, 0.0f));
+    const float phi = 2.0f * PI * u1;
+    V3 obj = v3(0.0f + r * (rr * cosf(phi)), 0.0f + r * (rr * sinf(phi)), 0.0f + r * z);
+    ShapeSample ss;
+    ss.n = REF ? obj : normalize(obj);
+    const float k = r / length(obj);  // reprojection onto the surface
+    obj = v3(obj.x * k, obj.y * k, obj.z * k);
+    const V3 oerr = gamma(5.0f) * vabs(obj);
+    M34 t;
+    t.m[0][0] = 1.0f; t.m[0][1] = 0.0f; t.m[0][2] = 0.0f; t.m[0][3] = s.x;
+    t.m[1][0] = 0.0f; t.m[1][1] = 1.0f; t.m[1][2] = 0.0f; t.m[1][3] = s.y;
+    t.m[2][0] = 0.0f; t.m[2][1] = 0.0f; t.m[2][2] = 1.0f; t.m[2][3] = s.z;
+    ss.p = m_point_perr(t, obj, oerr, &ss.p_err);
+    ss.pdf_area = 1.0f / sphere_area(r);
+    ss.b0 = ss.b1 = 0.0f;
+    return ss;
+}
+// Disk::sample / Cylinder::sample.  REF (F22): the disk draws from the whole disk of the outer
+// radius whatever inner_radius and phi_max (the intersection-based pdf is 0 in the hole), and the
+// cylinder's normal is not normalised (F21).  PBRT draws the annulus sector uniformly and
+// normalises.
+template <bool REF>
+BG_D ShapeSample quadric_light_sample(const float4* q, float u0, float u1) {
+    const float4 p0 = q[6], p1 = q[7];
+    const uint32_t flags = __float_as_uint(p1.z);
+    const int kind = (int)(flags & 0xFFu);
+    const bool reverse = (flags >> 8) & 1u;
+    const float radius = p0.x, inner = p0.y, z_min = p0.z, z_max = p0.w, height = p1.x, phi_max = p1.y;
+    const M34 o2w = load_m34(q), w2o = load_m34(q + 3);
+    ShapeSample ss;
+    V3 obj, oerr = v3(0.0f, 0.0f, 0.0f);
+    if (kind == 1) {
+        if (REF) {
+            const float2 d = concentric_sample_disk(u0, u1);
+            obj = v3(d.x * radius, d.y * radius, height);
+        } else {
+            const float rad = sqrtf((1.0f - u0) * (inner * inner) + u0 * (radius * radius));
+            const float ph = u1 * phi_max;
+            obj = v3(rad * cosf(ph), rad * sinf(ph), height);
+        }
+        ss.n = normalize(m_normal(w2o, v3(0.0f, 0.0f, 1.0f)));
+    } else {
+        const float z = (1.0f - u0) * z_min + u0 * z_max;  // lerp (math.rs:7-9)
+        const float phi = u1 * phi_max;
+        obj = v3(radius * cosf(phi), radius * sinf(phi), z);
+        const V3 n = m_normal(w2o, v3(obj.x, obj.y, 0.0f));
+        ss.n = REF ? n : normalize(n);
+        const float hr = sqrtf(obj.x * obj.x + obj.y * obj.y);
+        obj.x *= radius / hr;
+        obj.y *= radius / hr;
+        oerr = gamma(3.0f) * vabs(v3(obj.x, obj.y, 0.0f));
+    }
+    if (reverse) ss.n = ss.n * -1.0f;
+    ss.p = m_point_perr(o2w, obj, oerr, &ss.p_err);
+    ss.pdf_area = 1.0f / quadric_area(q);
+    ss.b0 = ss.b1 = 0.0f;
+    return ss;
+}
+
+// DiffuseAreaLight::sample_point + Shape::sample_from_it (diffuse.rs:54-87, shape.rs:17-34) for a
+// triangle, sphere, disk or cylinder light.
 template <bool REF>
 BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, float u0, float u1) {
     LightSample ls;
     ls.radiance = rgb(0.0f);
     ls.wi = v3(0, 0, 0);
     ls.pdf = 0.0f;
-    V3 p0, p1, p2;
-    load_tri(sc, prim, &p0, &p1, &p2);
-    ls.pt = tri_sample(p0, p1, p2, u0, u1);
-    if (tri_flag_bits(sc, prim) & TRI_SFLIP) ls.pt.n = ls.pt.n * -1.0f;
+    if (prim < sc.ntri) {
+        V3 p0, p1, p2;
+        load_tri(sc, prim, &p0, &p1, &p2);
+        ls.pt = tri_sample(p0, p1, p2, u0, u1);
+        if (tri_flag_bits(sc, prim) & TRI_SFLIP) ls.pt.n = ls.pt.n * -1.0f;
+    } else if (prim < sc.ntri + sc.nsph) {
+        ls.pt = sphere_light_sample<REF>(sc.sph[prim - sc.ntri], u0, u1);
+    } else {
+        ls.pt = quadric_light_sample<REF>(sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph), u0, u1);
+    }
     V3 wi = ls.pt.p - it.p;
     float pdf;
     if (length_squared(wi) == 0.0f) pdf = 0.0f;
@@ -584,22 +671,50 @@ BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, f
     ls.pdf = pdf;
     return ls;
 }
-// Shape::pdf_from_it for a triangle light (shape.rs:40-57).  Also returns the hit distance and
-// the light's surface normal there (for its one-sided emission).
+// Shape::pdf_from_it (shape.rs:40-57) of a triangle, sphere, disk or cylinder light.  Also returns
+// the hit distance and the light's surface normal there (for its one-sided emission).  REF (F20):
+// a sphere seen from outside reports the pdf of uniform cone sampling (sphere.rs:357-373),
+// although Sphere::sample draws uniformly by area.
 template <bool REF>
 BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, float* t_light, V3* n_light = nullptr) {
     Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wi, REF);
-    V3 p0, p1, p2;
-    load_tri(sc, prim, &p0, &p1, &p2);
-    TriRay tr = make_tri_ray(ray);
-    TriHit h;
-    if (!tri_test(tr, ray.t_max, p0, p1, p2, &h)) return 0.0f;
     Isect li;
-    tri_isect_plain(p0, p1, p2, h, ray, &li);
-    if (tri_flag_bits(sc, prim) & TRI_LFLIP) li.n = -li.n;
-    float pdf = distance_squared(it.p, li.p) / (abs_dot(li.n, -wi) * tri_area(p0, p1, p2));
+    float area, t;
+    if (prim < sc.ntri) {
+        V3 p0, p1, p2;
+        load_tri(sc, prim, &p0, &p1, &p2);
+        TriRay tr = make_tri_ray(ray);
+        TriHit h;
+        if (!tri_test(tr, ray.t_max, p0, p1, p2, &h)) return 0.0f;
+        tri_isect_plain(p0, p1, p2, h, ray, &li);
+        if (tri_flag_bits(sc, prim) & TRI_LFLIP) li.n = -li.n;
+        area = tri_area(p0, p1, p2);
+        t = h.t;
+    } else if (prim < sc.ntri + sc.nsph) {
+        const float4 s = sc.sph[prim - sc.ntri];
+        if (REF) {
+            const V3 center = v3(s.x, s.y, s.z);
+            const V3 o = offset_ray_origin(it.p, it.p_err, it.n, center - it.p);
+            if (!(distance_squared(o, center) <= s.w * s.w)) {
+                const float sin2 = s.w * s.w / distance_squared(it.p, center);
+                const float cos_max = sqrtf(rmax(0.0f, 1.0f - sin2));
+                if (t_light) *t_light = INFINITY;
+                return 1.0f / (2.0f * PI * (1.0f - cos_max));  // uniform_cone_pdf
+            }
+        }
+        SphHit h;
+        if (!sphere_test(s, ray, ray.t_max, &h)) return 0.0f;
+        sphere_isect(s, h, ray, &li);
+        area = sphere_area(s.w);
+        t = h.t;
+    } else {
+        const float4* q = sc.quads + QUADRIC_F4 * (prim - sc.ntri - sc.nsph);
+        if (!quadric_hit(q, ray, ray.t_max, &t, &li)) return 0.0f;
+        area = quadric_area(q);
+    }
+    float pdf = distance_squared(it.p, li.p) / (abs_dot(li.n, -wi) * area);
     if (isinf(pdf)) pdf = 0.0f;
-    if (t_light) *t_light = h.t;
+    if (t_light) *t_light = t;
     if (n_light) *n_light = li.n;
     return pdf;
 }

@@ -299,6 +299,36 @@ def quadric_box(width: int = 64, height: int = 64, spp: int = 8, max_depth: int 
     return sd
 
 
+def shape_lights(width: int = 64, height: int = 64, spp: int = 8, max_depth: int = 5,
+                 triangle_light: bool = True) -> SceneData:
+    """The Cornell box lit by DiffuseAreaLights on a sphere (r 0.12, two-sided), a full disk facing
+    down from the ceiling, a partial annulus (inner radius, 270 degrees) and a cylinder (one-sided,
+    outward), with or without the box's own triangle light."""
+    sd = cornell(width, height, spp, max_depth)
+    lights = list(sd.lights)
+    for inten, two in (((6.0, 5.0, 4.0), 1), ((3.0, 4.0, 6.0), 0), ((5.0, 2.0, 2.0), 0), ((2.0, 5.0, 3.0), 0)):
+        l = np.zeros((), LIGHT_DT)
+        l["intensity"], l["two_sided"] = inten, two
+        lights.append(l)
+    mats = list(sd.materials) + [material(MATTE, kd=(0.0, 0.0, 0.0))]
+    m_black = len(mats) - 1
+    sph = list(sd.spheres) + [np.zeros((), SPHERE_DT)]
+    sph[-1]["center"], sph[-1]["radius"], sph[-1]["material_id"], sph[-1]["light_id"] = (0.0, 0.55, -0.2), 0.12, m_black, 1
+    q = [quadric(DISK, translation((0.45, 0.985, 0.25)) @ rotation((1, 0, 0), 90), m_black, radius=0.2, height=0.0),
+         quadric(DISK, translation((-0.45, 0.985, 0.3)) @ rotation((1, 0, 0), 90), m_black, radius=0.2,
+                 inner_radius=0.08, height=0.0, phi_max_deg=270.0),
+         quadric(CYLINDER, translation((-0.55, 0.3, -0.4)), m_black, radius=0.06, z_min=-0.2, z_max=0.2)]
+    q[0]["light_id"], q[1]["light_id"], q[2]["light_id"] = 2, 3, 4
+    tri, tm, tl = sd.tri, sd.tri_mat, sd.tri_light
+    if not triangle_light:
+        keep = tl < 0
+        tri, tm, tl = tri[keep], tm[keep], tl[keep]
+    out = SceneData(tri.copy(), tm.copy(), tl.copy(), np.stack(sph), np.stack(mats), np.stack(lights), sd.camera,
+                    quadrics=np.stack(q), spp=spp, max_depth=max_depth, rr_threshold=1.0,
+                    name="shape_lights" + ("" if triangle_light else "_only"))
+    return out
+
+
 def checker_image(n: int = 64, tiles: int = 8, seed: int = 0) -> np.ndarray:
     """(n, n, 3) float32 test image: a two-colour checkerboard with per-texel noise in blue."""
     rng = np.random.default_rng(seed)

@@ -128,7 +128,7 @@ typedef struct bg_sphere {
     float center[3];
     float radius;
     uint32_t material_id;
-    int32_t light_id; /* must be -1: spherical emitters are not supported */
+    int32_t light_id; /* area light record (DiffuseAreaLight on the sphere) or -1 */
 } bg_sphere;
 
 /* Quadric shapes (src/shapes/{cylinder,disk,cone}.rs) with an affine object_to_world transform.
@@ -148,7 +148,7 @@ typedef struct bg_quadric {
     float height;
     float phi_max_deg;
     uint32_t material_id;
-    int32_t light_id; /* must be -1: quadric emitters are not supported */
+    int32_t light_id; /* area light record or -1 (cylinders and disks; cones cannot emit) */
 } bg_quadric;
 
 /* PerspectiveCamera options (src/cameras/perspective.rs:36-46) with the camera_to_world

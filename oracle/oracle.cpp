@@ -1648,6 +1648,61 @@ struct LightSample {
     Interaction p0, p1;
     bool vis = false;
 };
+// ---- shapes as area lights: Shape::sample (sphere.rs:328-355, disk.rs:184-214,
+// cylinder.rs:289-321) and area (sphere.rs:375-377, disk.rs:216-218, cylinder.rs:323-325).
+// F21 (REF): sphere and cylinder sample normals are not normalised.  F22 (REF): the disk draws
+// from the whole disk of the outer radius; PBRT draws the annulus sector uniformly.
+static float sphere_area(const Sphere& sp) { return sp.phi_max * sp.radius * (sp.z_max - sp.z_min); }
+static float quadric_area(const Quadric& q) {
+    if (q.kind == 1) return q.phi_max * 0.5f * (q.radius * q.radius - q.inner * q.inner);
+    return (q.z_max - q.z_min) * q.radius * q.phi_max;
+}
+static Interaction sphere_sample(const Sphere& sp, float u0, float u1, Mode mode, float* pdf) {
+    float z = 1.0f - 2.0f * u0;  // uniform_sample_sphere (sampling.rs:211-216)
+    float rr = std::sqrt(rmax(1.0f - z * z, 0.0f));
+    float phi = 2.0f * PI * u1;
+    V3 obj(0.0f + sp.radius * (rr * std::cos(phi)), 0.0f + sp.radius * (rr * std::sin(phi)), 0.0f + sp.radius * z);
+    Interaction r;
+    r.n = xf_normal(sp.o2w, obj);
+    if (mode == PBRT) r.n = normalize(r.n);
+    float k = sp.radius / length(obj);
+    obj = V3(obj.x * k, obj.y * k, obj.z * k);
+    V3 oerr = gamma(5.0f) * vabs(obj);
+    r.p = xf_point_perr(sp.o2w, obj, oerr, &r.p_err);
+    *pdf = 1.0f / sphere_area(sp);
+    return r;
+}
+static Interaction quadric_sample(const Quadric& q, float u0, float u1, Mode mode, float* pdf) {
+    Interaction r;
+    V3 obj, oerr(0.0f, 0.0f, 0.0f);
+    if (q.kind == 1) {  // disk
+        if (mode == REF) {
+            float dy;
+            float dx = concentric_sample_disk(u0, u1, &dy).x;
+            obj = V3(dx * q.radius, dy * q.radius, q.height);
+        } else {
+            float rad = std::sqrt((1.0f - u0) * (q.inner * q.inner) + u0 * (q.radius * q.radius));
+            float ph = u1 * q.phi_max;
+            obj = V3(rad * std::cos(ph), rad * std::sin(ph), q.height);
+        }
+        r.n = normalize(xf_normal(q.o2w, V3(0.0f, 0.0f, 1.0f)));
+    } else {  // cylinder
+        float z = (1.0f - u0) * q.z_min + u0 * q.z_max;
+        float phi = u1 * q.phi_max;
+        obj = V3(q.radius * std::cos(phi), q.radius * std::sin(phi), z);
+        r.n = xf_normal(q.o2w, V3(obj.x, obj.y, 0.0f));
+        if (mode == PBRT) r.n = normalize(r.n);
+        float hr = std::sqrt(obj.x * obj.x + obj.y * obj.y);
+        obj.x *= q.radius / hr;
+        obj.y *= q.radius / hr;
+        oerr = gamma(3.0f) * vabs(V3(obj.x, obj.y, 0.0f));
+    }
+    if (q.reverse) r.n = r.n * -1.0f;
+    r.p = xf_point_perr(q.o2w, obj, oerr, &r.p_err);
+    *pdf = 1.0f / quadric_area(q);
+    return r;
+}
+
 // ---- InfiniteAreaLight (src/lights/infinite.rs) over Distribution2D (src/base/sampling.rs)
 // find_interval (math.rs:70-87): the last index i < size - 1 with cdf[i] <= u
 static size_t cdf_interval(const float* cdf, size_t size, float u) {
@@ -1739,7 +1794,9 @@ static LightSample light_sample_point(const Scene& s, int64_t prim, const Intera
         return ls;
     }
     float pdf_area;
-    Interaction pit = tri_sample(s, prim, u0, u1, &pdf_area);
+    Interaction pit = prim < s.ntri ? tri_sample(s, prim, u0, u1, &pdf_area)
+                      : prim < s.ntri + s.nsph ? sphere_sample(s.sph[prim - s.ntri], u0, u1, mode, &pdf_area)
+                                               : quadric_sample(s.quads[prim - s.ntri - s.nsph], u0, u1, mode, &pdf_area);
     V3 wi = pit.p - it.p;
     float pdf;
     if (length_squared(wi) == 0.0f) pdf = 0.0f;
@@ -1772,8 +1829,29 @@ static float light_point_pdf(const Scene& s, int64_t prim, const Interaction& it
     Ray ray = spawn_ray(it, wi, mode);
     float t;
     Interaction iit;
-    if (!tri_intersect(s, prim, ray, &t, &iit, false)) return 0.0f;
-    float pdf = distance_squared(it.p, iit.p) / (abs_dot(iit.n, -wi) * tri_area(s, prim));
+    float area;
+    if (prim < s.ntri) {
+        if (!tri_intersect(s, prim, ray, &t, &iit, false)) return 0.0f;
+        area = tri_area(s, prim);
+    } else if (prim < s.ntri + s.nsph) {
+        const Sphere& sp = s.sph[prim - s.ntri];
+        if (mode == REF) {  // F20: Sphere::pdf_from_it (sphere.rs:357-373)
+            V3 center = xf_point(sp.o2w, V3(0.0f, 0.0f, 0.0f));
+            V3 origin = offset_ray_origin(it.p, it.p_err, it.n, center - it.p);
+            if (!(distance_squared(origin, center) <= sp.radius * sp.radius)) {
+                float sin2 = sp.radius * sp.radius / distance_squared(it.p, center);
+                float cos_max = std::sqrt(rmax(0.0f, 1.0f - sin2));
+                return 1.0f / (2.0f * PI * (1.0f - cos_max));  // uniform_cone_pdf
+            }
+        }
+        if (!sphere_intersect(sp, ray, &t, &iit, false)) return 0.0f;
+        area = sphere_area(sp);
+    } else {
+        const Quadric& q = s.quads[prim - s.ntri - s.nsph];
+        if (!quadric_intersect(q, ray, &t, &iit, false)) return 0.0f;
+        area = quadric_area(q);
+    }
+    float pdf = distance_squared(it.p, iit.p) / (abs_dot(iit.n, -wi) * area);
     if (std::isinf(pdf)) pdf = 0.0f;
     return pdf;
 }
@@ -2116,6 +2194,11 @@ void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_m
         sp.phi_max = rclamp(360.0f, 0.0f, 360.0f) * (PI / 180.0f);
         sp.mat = sph[i].material_id;
         s->sph.push_back(sp);
+        if (sph[i].light_id >= 0) {  // DiffuseAreaLight on the sphere
+            s->prim_emission[ntri + i] = sph[i].light_id;
+            s->prim_light[ntri + i] = (int32_t)s->light_prims.size();
+            s->light_prims.push_back(ntri + i);
+        }
     }
     for (int64_t i = 0; i < nquad; ++i) {
         const bg_quadric& g = quads[i];
@@ -2144,6 +2227,11 @@ void* orc_scene_create(const float* tri_xyz, int64_t ntri, const uint32_t* tri_m
         q.phi_max = rclamp(g.phi_max_deg, 0.0f, 360.0f) * (PI / 180.0f);
         q.mat = g.material_id;
         s->quads.push_back(q);
+        if (g.light_id >= 0) {
+            s->prim_emission[ntri + nsph + i] = g.light_id;
+            s->prim_light[ntri + nsph + i] = (int32_t)s->light_prims.size();
+            s->light_prims.push_back(ntri + nsph + i);
+        }
     }
     build_bvh(*s, bvh_fixed != 0);
     return s;

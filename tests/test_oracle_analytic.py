@@ -162,3 +162,69 @@ def test_thin_lens_rays_meet_on_the_plane_of_focus():
         r = O.camera_ray(pin, fx, fy).astype(np.float64)
         t = (4.0 - np.dot(r[:3] - pos, fwd)) / np.dot(r[3:], fwd)
         assert np.abs(r[:3] + t * r[3:] - pts.mean(axis=0)).max() < 1e-3
+
+
+def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5):
+    """A matte floor (y = 0, 20 x 20) lit only by one shape light of unit radiance: `sphere` =
+    (center, radius), `disk` = (center, radius) facing down."""
+    tri = S._quad((-10, 0, -10), (10, 0, -10), (10, 0, 10), (-10, 0, 10), (0, 1, 0))
+    mats = np.stack([S.material(S.MATTE, kd=(albedo,) * 3), S.material(S.MATTE)])
+    lights = np.zeros(1, S.LIGHT_DT)
+    lights[0]["intensity"], lights[0]["two_sided"] = (1.0, 1.0, 1.0), 0
+    sph = np.zeros(0, S.SPHERE_DT)
+    quads = np.zeros(0, S.QUADRIC_DT)
+    if sphere is not None:
+        sph = np.zeros(1, S.SPHERE_DT)
+        sph[0]["center"], sph[0]["radius"], sph[0]["material_id"], sph[0]["light_id"] = sphere[0], sphere[1], 1, 0
+    if disk is not None:
+        q = S.quadric(S.DISK, S.translation(disk[0]) @ S.rotation((1, 0, 0), 90), 1, radius=disk[1], height=0.0)
+        q["light_id"] = 0
+        quads = np.stack([q])
+    return S.SceneData(tri.astype(np.float32), np.zeros(2, np.uint32), np.full(2, -1, np.int32), sph, mats, lights,
+                       cam, quadrics=quads, spp=16, max_depth=1, rr_threshold=1.0)
+
+
+def test_sphere_light_direct_lighting_known_answer():
+    """Irradiance from a sphere of radiance L fully above the horizon: pi L (r / d)^2 cos(theta);
+    a matte floor of albedo rho shows rho L (r / d)^2 cos(theta) (PBRT, direct lighting only)."""
+    c, r = np.array([1.2, 1.0, 0.0]), 0.4
+    cam = S.Camera((0.0, 2.0, 0.01), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 30.0, 33, 33)
+    sd = _floor_scene(33, 33, cam, sphere=(tuple(c), r))
+    spp = 1024
+    o = O.OracleScene(sd).render(A.BG_MODE_PBRT, spp=spp, rows=(12, 21, 4), threads=4)
+    var = o["sumsq"] / spp - (o["sum"] / spp) ** 2
+    for y in (12, 16, 20):
+        for x in (12, 16, 20):
+            ray = O.camera_ray(cam, x + 0.5, y + 0.5).astype(np.float64)
+            t = -ray[1] / ray[4]
+            p = ray[:3] + t * ray[3:]
+            d = c - p
+            dist2 = d @ d
+            expect = 0.5 * (r * r / dist2) * (d[1] / np.sqrt(dist2))
+            se = np.sqrt(var[y, x, 0] / spp) + 2e-3 * expect
+            assert abs(o["rgb"][y, x, 0] - expect) < 5 * se, (x, y, o["rgb"][y, x, 0], expect)
+
+
+def test_disk_light_on_axis_known_answer():
+    """A disk of radius R and radiance L at height h facing down: irradiance on its axis
+    pi L R^2 / (h^2 + R^2); both the PBRT annulus sampling and the intersection pdf are exercised."""
+    h, R = 1.5, 0.6
+    cam = S.Camera((0.0, 0.8, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 10.0, 33, 33)
+    sd = _floor_scene(33, 33, cam, disk=((0.0, h, 0.0), R))
+    spp = 4096
+    o = O.OracleScene(sd).render(A.BG_MODE_PBRT, spp=spp, rows=(16, 17, 1), threads=4)
+    expect = 0.5 * R * R / (h * h + R * R)
+    v = o["rgb"][16, 16, 0]
+    se = np.sqrt(max(o["sumsq"][16, 16, 0] / spp - (o["sum"][16, 16, 0] / spp) ** 2, 0) / spp)
+    assert abs(v - expect) < 5 * se + 1e-3 * expect, (v, expect)
+
+
+def test_ref_compat_shape_light_defects_change_the_estimate():
+    """REF_COMPAT: the sphere's sample normal of length r (F21) and its cone pdf against area
+    sampling (F20) move the estimate away from the PBRT value."""
+    c, r = (1.2, 1.0, 0.0), 0.4
+    cam = S.Camera((0.0, 2.0, 0.01), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 30.0, 17, 17)
+    sd = _floor_scene(17, 17, cam, sphere=(c, r))
+    pb = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, spp=256, threads=4)["rgb"].mean()
+    rf = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_REF_COMPAT, spp=256, threads=4)["rgb"].mean()
+    assert abs(rf - pb) > 0.1 * pb, (rf, pb)
