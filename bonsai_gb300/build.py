@@ -20,7 +20,8 @@ LIB = PKG / "lib" / "libbonsai_gpu.so"
 CUDA = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["bg_kernels.cu", "bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade_guided_full.cu", "bg_noalloc.cu",
+CU_SOURCES = ["bg_kernels.cu", "bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade_guided_full.cu", "bg_shade_shapes.cu",
+              "bg_noalloc.cu",
               "bg_guide.cu",
               "bg_integrators.cu", "bg_integrators_pbrt.cu", "bg_tree_wave.cu",
               "bg_tree_shade_w.cu", "bg_tree_shade_d.cu"]

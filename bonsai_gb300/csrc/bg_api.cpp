@@ -1570,7 +1570,7 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         if (it.opts.integrator != BG_INTEGRATOR_PATH)
             return fail(ctx, BG_ERR_UNSUPPORTED, "batch rendering runs the path integrator only");
         if (it.scene->dev.ntex) variants |= 1u;
-        if (it.scene->has_inf) variants |= 2u;
+        if (it.scene->has_inf || it.scene->dev.sph_emis || it.scene->dev.quad_emis) variants |= 2u;
         total_pix += (uint64_t)it.camera.width * it.camera.height;
         total_items += (uint64_t)it.camera.width * it.camera.height * it.opts.spp;
         max_depth = std::max(max_depth, it.opts.max_depth);

@@ -6,7 +6,7 @@ namespace bg {
 
 int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                         const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
-    if (sc.ntex || sc.inf) return launch_shade_guided_full(sc, rp, film, wb, gw, b, err, grid, block, s);
+    if (sc.ntex || general_lights(sc)) return launch_shade_guided_full(sc, rp, film, wb, gw, b, err, grid, block, s);
     k_shade<CLS_MISS, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     k_shade<0, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
@@ -17,7 +17,7 @@ int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffe
 
 int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                           const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
-    if (sc.ntex || sc.inf) return launch_guide_continue_full(sc, rp, film, wb, gw, b, err, grid, block, s);
+    if (sc.ntex || general_lights(sc)) return launch_guide_continue_full(sc, rp, film, wb, gw, b, err, grid, block, s);
     k_guide_continue<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
     k_guide_continue<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
     k_guide_continue<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);

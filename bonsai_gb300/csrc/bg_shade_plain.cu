@@ -8,17 +8,18 @@ namespace bg {
 int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                        uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
     const GuideWave gw{};
+    if (sc.sph_emis || sc.quad_emis) return launch_shade_shapes(sc, rp, film, wb, b, err, grid, block, s);
     if (sc.inf) {  // the light list holds the infinite light
         k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         if (sc.ntex) {
-            k_shade<0, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, false, true, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<0, false, false, true, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, true, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         } else {
-            k_shade<0, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<0, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         }
-        k_shade<2, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<3, false, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     } else if (sc.ntex) {
         k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
         k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);

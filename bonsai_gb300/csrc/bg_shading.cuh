@@ -639,14 +639,15 @@ BG_D ShapeSample quadric_light_sample(const float4* q, float u0, float u1) {
 }
 
 // DiffuseAreaLight::sample_point + Shape::sample_from_it (diffuse.rs:54-87, shape.rs:17-34) for a
-// triangle, sphere, disk or cylinder light.
-template <bool REF>
+// triangle, sphere, disk or cylinder light (SHAPES = false: triangles only, for light lists that
+// hold nothing else).
+template <bool REF, bool SHAPES = true>
 BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, float u0, float u1) {
     LightSample ls;
     ls.radiance = rgb(0.0f);
     ls.wi = v3(0, 0, 0);
     ls.pdf = 0.0f;
-    if (prim < sc.ntri) {
+    if (!SHAPES || prim < sc.ntri) {
         V3 p0, p1, p2;
         load_tri(sc, prim, &p0, &p1, &p2);
         ls.pt = tri_sample(p0, p1, p2, u0, u1);
@@ -675,12 +676,12 @@ BG_D LightSample light_sample(const Scene& sc, uint32_t prim, const Isect& it, f
 // the hit distance and the light's surface normal there (for its one-sided emission).  REF (F20):
 // a sphere seen from outside reports the pdf of uniform cone sampling (sphere.rs:357-373),
 // although Sphere::sample draws uniformly by area.
-template <bool REF>
+template <bool REF, bool SHAPES = true>
 BG_D float light_pdf(const Scene& sc, uint32_t prim, const Isect& it, V3 wi, float* t_light, V3* n_light = nullptr) {
     Ray ray = spawn_ray(it.p, it.p_err, it.n, it.time, wi, REF);
     Isect li;
     float area, t;
-    if (prim < sc.ntri) {
+    if (!SHAPES || prim < sc.ntri) {
         V3 p0, p1, p2;
         load_tri(sc, prim, &p0, &p1, &p2);
         TriRay tr = make_tri_ray(ray);
@@ -847,21 +848,21 @@ BG_D float inf_pdf(const Scene& sc, V3 w) {
     return dist2d_pdf<REF>(L, phi * (1.0f / (2.0f * PI)), theta * (1.0f / PI)) / (2.0f * PI * PI * s);
 }
 // Light::sample_point for an entry of the light list (a triangle or the infinite light).
-template <bool REF>
+template <bool REF, bool SHAPES = true>
 BG_D LightSample light_sample_any(const Scene& sc, uint32_t light, const Isect& it, float u0, float u1) {
     if (light == LIGHT_INFINITE) return inf_sample<REF>(sc, it, u0, u1);
-    return light_sample<REF>(sc, light, it, u0, u1);
+    return light_sample<REF, SHAPES>(sc, light, it, u0, u1);
 }
 // Light::point_pdf for an entry of the light list.  t_light: the hit distance on an area light,
 // infinity for the infinite light; n_light: the area light's normal there.
-template <bool REF>
+template <bool REF, bool SHAPES = true>
 BG_D float light_pdf_any(const Scene& sc, uint32_t light, const Isect& it, V3 wi, float* t_light,
                          V3* n_light = nullptr) {
     if (light == LIGHT_INFINITE) {
         if (t_light) *t_light = INFINITY;
         return inf_pdf<REF>(sc, wi);
     }
-    return light_pdf<REF>(sc, light, it, wi, t_light, n_light);
+    return light_pdf<REF, SHAPES>(sc, light, it, wi, t_light, n_light);
 }
 // Radiance arriving along a BSDF-sampled direction wi that reaches light `light` unoccluded:
 // the area light's one-sided emission at its surface, or the environment map.
@@ -869,6 +870,9 @@ BG_D RGB light_radiance_along(const Scene& sc, uint32_t light, V3 wi, V3 n_light
     if (light == LIGHT_INFINITE) return inf_radiance(sc, wi);
     return emission(sc.emis[prim_emission(sc, (int)light)], n_light, -wi);
 }
+// Whether a scene's light list holds more than triangles (the infinite light, emitting spheres or
+// quadrics): such scenes run the shade variants with the general light code.
+BG_HD bool general_lights(const Scene& sc) { return sc.inf || sc.sph_emis || sc.quad_emis; }
 // Light::radiance of every light for a ray that escapes the scene (only infinite lights emit).
 BG_D RGB escaped_radiance(const Scene& sc, V3 dir) { return sc.inf ? inf_radiance(sc, dir) : rgb(0.0f); }
 

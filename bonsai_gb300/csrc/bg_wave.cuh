@@ -257,9 +257,11 @@ BG_D void strat_apply(const float* su, bool nee, float u[8]) {
     }
 }
 
-// INF: the scene's light list may hold the infinite light (variants launched only for such scenes,
-// so that the others carry none of its code).
-template <int CLS, bool TEX = false, bool INF = false>
+// INF: the scene's light list may hold more than triangles - the infinite light, emitting spheres
+// or quadrics (variants launched only for such scenes, general_lights, so that the others carry
+// none of that code).
+// SHL: emitting spheres / quadrics may be in the light list (with INF).
+template <int CLS, bool TEX = false, bool INF = false, bool SHL = INF>
 BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuffers& wb, const GuideWave& gw,
                          uint32_t slot, uint32_t bounce, const Ray& ray, const Isect& it, RGB& beta, float& eta_scale,
                          uint32_t& state, const MixView* mix, const float* ug, bool record, VertexOut& out,
@@ -289,8 +291,8 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
             const float c = mix->c();
             return c * mix->pdf(w) + (1.0f - c) * pb;
         };
-        LightSample ls = INF ? light_sample_any<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1])
-                             : light_sample<false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
+        LightSample ls = INF ? light_sample_any<false, SHL>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1])
+                             : light_sample<false, false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
         if (ls.pdf > 0.0f && !is_black(ls.radiance)) {
             RGB f = bsdf.f<false>(it.wo, ls.wi, flags) * abs_dot(ls.wi, it.ns);
             if (!is_black(f)) {
@@ -321,8 +323,8 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         if (!is_black(f) && spdf > 0.0f) {
             float t_light = 0.0f;
             V3 ln;
-            float lpdf = INF ? light_pdf_any<false>(sc, light_prim, it, wi, &t_light, &ln)
-                             : light_pdf<false>(sc, light_prim, it, wi, &t_light, &ln);
+            float lpdf = INF ? light_pdf_any<false, SHL>(sc, light_prim, it, wi, &t_light, &ln)
+                             : light_pdf<false, false>(sc, light_prim, it, wi, &t_light, &ln);
             if (lpdf != 0.0f) {
                 float w = power_heuristic(1.0f, spdf, 1.0f, lpdf);
                 // the sampled direction reaches the light at t_light; it counts iff nothing else
@@ -410,7 +412,7 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 #ifndef BG_SHADE_MINBLOCKS
 #define BG_SHADE_MINBLOCKS 4
 #endif
-template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false>
+template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false, bool SHL = INF>
 __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
                 gq = make_query(gw, it, -ray.d);
                 push_guide = true;
             } else if (!finished) {
-                scatter_vertex<CLS, TEX, INF>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
+                scatter_vertex<CLS, TEX, INF, SHL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
                                     vo, su);
                 finished = vo.finished;
                 cont = vo.cont;
@@ -569,6 +571,9 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
     }
 }
 
+// Single-scene shade launches for scenes with emitting spheres or quadrics (bg_shade_shapes.cu).
+int launch_shade_shapes(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
+                        uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
 // Shade launches of one bounce (the five material classes, misses included).
 int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                        uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
