@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(128) k_megakernel(Scene sc, Camera cam, Render
         uint32_t pix = (uint32_t)(item % npix);
         uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         Rng rng{pix, s, rp.seed};
-        const CameraUs cu = camera_us(rp.strat, REF, rng);
+        const CameraUs cu = camera_us(rp.strat, REF, rng, cam.lens_radius > 0.0f);
         float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
         Ray ray = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         RayDiff rd;

@@ -319,24 +319,37 @@ struct CameraUs {
     float fx, fy, time;
     float lx, ly;  // lens sample
 };
-BG_D CameraUs camera_us(const StratParams& sp, bool ref, const Rng& rng) {
+// lens / time: whether the caller needs the lens sample (a thin-lens camera) and the time.
+BG_D CameraUs camera_us(const StratParams& sp, bool ref, const Rng& rng, bool lens, bool time = true) {
     CameraUs c;
-    float b[4];
-    rng.block(0, b);  // film 0-1, lens 2-3
-    c.fx = b[0];
-    c.fy = b[1];
-    c.lx = b[2];
-    c.ly = b[3];
-    c.time = rng.u(DIM_TIME);
-    if (sp.dims > 0) {
-        float2 f = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
-        c.fx = f.x;
-        c.fy = f.y;
-        c.time = strat_1d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
+    c.lx = c.ly = 0.5f;
+    c.time = 0.0f;
+    if (sp.dims == 0) {
+        float b[4];
+        rng.block(0, b);  // film 0-1, lens 2-3
+        c.fx = b[0];
+        c.fy = b[1];
+        if (lens) {
+            c.lx = b[2];
+            c.ly = b[3];
+        }
+        if (time) c.time = rng.u(DIM_TIME);
+        return c;
+    }
+    const float2 f = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
+    c.fx = f.x;
+    c.fy = f.y;
+    if (time) c.time = strat_1d(sp, ref, rng.pixel, rng.sample, rng.seed, 0);
+    if (lens) {
         if (sp.dims > 1) {
             const float2 l = strat_2d(sp, ref, rng.pixel, rng.sample, rng.seed, 1);
             c.lx = l.x;
             c.ly = l.y;
+        } else {
+            float b[4];
+            rng.block(0, b);
+            c.lx = b[2];
+            c.ly = b[3];
         }
     }
     return c;

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128) k_tree(Scene sc, Camera cam, RenderParams
         const uint32_t pix = (uint32_t)(item % npix);
         const uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, 0u};
-        const CameraUs cu = camera_us(rp.strat, REF, rng);  // sampled_dimensions <= 1: camera only
+        const CameraUs cu = camera_us(rp.strat, REF, rng, cam.lens_radius > 0.0f);  // sampled_dimensions <= 1: camera only
         const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
         const Ray ray = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         RayDiff rd;

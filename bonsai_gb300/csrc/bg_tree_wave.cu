@@ -39,7 +39,7 @@ __global__ void k_tw_gen(Camera cam, RenderParams rp, TreeWave tw, uint64_t item
         const uint32_t pix = pixel_of((uint32_t)(item % npix), rp.width, rp.height, rp.pixel_tiles);
         const uint32_t s = rp.first_sample + (uint32_t)(item / npix);
         const Rng rng{pix, s, rp.seed, 0u};
-        const CameraUs cu = camera_us(rp.strat, false, rng);  // sampled_dimensions <= 1: camera only
+        const CameraUs cu = camera_us(rp.strat, false, rng, cam.lens_radius > 0.0f);  // sampled_dimensions <= 1: camera only
         const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
         const Ray r = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
         tw.ray_o[0][i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);

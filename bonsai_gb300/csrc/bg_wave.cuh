@@ -30,7 +30,7 @@ BG_D const TexPoint* tex_point(const Scene& sc, const Isect& it, const Ray& ray,
 // The camera ray differentials of path (pixel, sample) at its camera sample's film position (the
 // same sampler values as the ray's generation); `cam_ray` is its camera ray.
 BG_D RayDiff path_camera_diff(const RenderParams& rp, uint32_t pix, uint32_t s, const Ray& cam_ray) {
-    const CameraUs cu = camera_us(rp.strat, false, Rng{pix, s, rp.seed});
+    const CameraUs cu = camera_us(rp.strat, false, Rng{pix, s, rp.seed}, rp.cam.lens_radius > 0.0f, false);
     const float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
     return camera_diff(rp.cam, fx, fy, cam_ray, rp.diff_scale, cu.lx, cu.ly);
 }
@@ -78,7 +78,7 @@ constexpr int CLS_MISS = 4;
 BG_D void generate_one(const Camera& cam, const RenderParams& rp, const WaveBuffers& wb, uint32_t i, uint32_t pix,
                        uint32_t s) {
     Rng rng{pix, s, rp.seed};
-    const CameraUs cu = camera_us(rp.strat, false, rng);
+    const CameraUs cu = camera_us(rp.strat, false, rng, cam.lens_radius > 0.0f);
     float fx = (float)(pix % rp.width) + cu.fx, fy = (float)(pix / rp.width) + cu.fy;
     Ray r = camera_ray(cam, fx, fy, cu.time, cu.lx, cu.ly);
     wb.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, r.t_max);
