@@ -164,7 +164,7 @@ def test_thin_lens_rays_meet_on_the_plane_of_focus():
         assert np.abs(r[:3] + t * r[3:] - pts.mean(axis=0)).max() < 1e-3
 
 
-def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5):
+def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5, inner=0.0):
     """A matte floor (y = 0, 20 x 20) lit only by one shape light of unit radiance: `sphere` =
     (center, radius), `disk` = (center, radius) facing down."""
     tri = S._quad((-10, 0, -10), (10, 0, -10), (10, 0, 10), (-10, 0, 10), (0, 1, 0))
@@ -177,7 +177,8 @@ def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5):
         sph = np.zeros(1, S.SPHERE_DT)
         sph[0]["center"], sph[0]["radius"], sph[0]["material_id"], sph[0]["light_id"] = sphere[0], sphere[1], 1, 0
     if disk is not None:
-        q = S.quadric(S.DISK, S.translation(disk[0]) @ S.rotation((1, 0, 0), 90), 1, radius=disk[1], height=0.0)
+        q = S.quadric(S.DISK, S.translation(disk[0]) @ S.rotation((1, 0, 0), 90), 1, radius=disk[1], height=0.0,
+                      inner_radius=inner)
         q["light_id"] = 0
         quads = np.stack([q])
     return S.SceneData(tri.astype(np.float32), np.zeros(2, np.uint32), np.full(2, -1, np.int32), sph, mats, lights,
@@ -228,3 +229,20 @@ def test_ref_compat_shape_light_defects_change_the_estimate():
     pb = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, spp=256, threads=4)["rgb"].mean()
     rf = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_REF_COMPAT, spp=256, threads=4)["rgb"].mean()
     assert abs(rf - pb) > 0.1 * pb, (rf, pb)
+
+
+def test_annulus_light_on_axis_known_answer_and_ref_defect():
+    """An annulus (radii Ri < R) at height h facing down: irradiance on its axis
+    pi L (R^2 / (h^2 + R^2) - Ri^2 / (h^2 + Ri^2)).  PBRT draws the annulus and meets it; REF_COMPAT
+    draws the whole disk (F22), and samples in the hole find no surface behind them."""
+    h, R, Ri = 1.5, 0.6, 0.35
+    cam = S.Camera((0.0, 0.8, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 10.0, 33, 33)
+    sd = _floor_scene(33, 33, cam, disk=((0.0, h, 0.0), R), inner=Ri)
+    spp = 4096
+    expect = 0.5 * (R * R / (h * h + R * R) - Ri * Ri / (h * h + Ri * Ri))
+    o = O.OracleScene(sd).render(A.BG_MODE_PBRT, spp=spp, rows=(16, 17, 1), threads=4)
+    v = o["rgb"][16, 16, 0]
+    se = np.sqrt(max(o["sumsq"][16, 16, 0] / spp - (o["sum"][16, 16, 0] / spp) ** 2, 0) / spp)
+    assert abs(v - expect) < 5 * se + 1e-3 * expect, (v, expect)
+    rf = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_REF_COMPAT, spp=spp, rows=(16, 17, 1), threads=4)
+    assert abs(rf["rgb"][16, 16, 0] - expect) > 0.05 * expect
