@@ -1,7 +1,7 @@
 """CPU oracle for the path-tracing hot path - TEST INFRASTRUCTURE ONLY.
 
 A C++ restatement of kazijawad/bonsai's PathIntegrator path (see oracle.cpp) behind ctypes.
-Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may use it, as the checker.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may use it, as the test oracle.
 Parity unpinned: the reference ships no tests or golden vectors and cannot be built here (no Rust
 toolchain), so this restatement is pinned only by analytic known answers and by its own fixtures.
 """

@@ -1,6 +1,6 @@
 """FP64 host evaluation of the guiding network - TEST INFRASTRUCTURE ONLY.
 
-The checker for the tensor-core kernels of bonsai_gb300 (k_guide_infer, k_guide_train,
+The test oracle for the tensor-core kernels of bonsai_gb300 (k_guide_infer, k_guide_train,
 k_guide_adam) and for the mixture device functions (guide_parse / guide_pdf / guide_sample /
 guide_loss_grad).  The reference has no learned component, so there is nothing of it to follow
 here: this module restates the network, the von Mises-Fisher mixture and the loss as defined in

@@ -1,4 +1,4 @@
-// CPU ORACLE - TEST INFRASTRUCTURE ONLY (the checker, never the product path).
+// CPU ORACLE - TEST INFRASTRUCTURE ONLY (the oracle of the tests, never the product path).
 //
 // C++17 restatement of the path-tracing hot path of kazijawad/bonsai (Rust, f32 build).
 // Parity unpinned: the reference has no tests, golden vectors or fixtures for this path and its

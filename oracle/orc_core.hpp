@@ -1,7 +1,7 @@
 // CPU ORACLE - TEST INFRASTRUCTURE ONLY.
 //
 // Plain C++17 restatement of the arithmetic helpers of kazijawad/bonsai (Rust, f32 build).
-// Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this code, as the checker.
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this code, as the test oracle.
 // Parity unpinned: the reference ships no tests, golden vectors or fixtures for this path, and
 // its Rust toolchain is absent, so this restatement cannot be checked against reference output.
 //
