@@ -77,6 +77,26 @@ def texture_case():
     return out
 
 
+def lights_case():
+    """The lights and samplers beyond the box's triangle light: the reference's example scene with its
+    infinite light (two area lights besides), rotated; area lights on spheres, disks and cylinders;
+    the stratified sampler; a thin-lens camera; both estimator modes."""
+    out = {}
+    sd = S.env_sphere(16, 16, spp=4, max_depth=4, extra=True, env_w=16, env_h=8)
+    sd.env.light_to_world = (S.rotation((0, 0, 1), 40.0) @ S.rotation((1, 0, 0), 20.0))[:3].astype(np.float32)
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=True).render(mode, seed=11, threads=1)
+        out[f"env_sum_{mode}"] = r["sum"]
+        r = O.OracleScene(sd, fixed_bvh=True).render(mode, seed=11, threads=1, sampler=S.StratifiedSampler(2, 2, 4))
+        out[f"env_strat_sum_{mode}"] = r["sum"]
+    sd = S.shape_lights(16, 16, spp=4, max_depth=4)
+    sd.camera.lens_radius, sd.camera.focal_distance = 0.1, 3.0
+    for mode in (A.BG_MODE_REF_COMPAT, A.BG_MODE_PBRT):
+        r = O.OracleScene(sd, fixed_bvh=True).render(mode, seed=13, threads=1)
+        out[f"shapes_sum_{mode}"] = r["sum"]
+    return out
+
+
 def rng_case():
     idx = np.array([(0, 0, 0, 0), (1, 2, 3, 4), (12345, 999, 7, 41), (2**32 - 1, 2**31, 65535, 1023)], np.uint64)
     vals = np.array([O.rng_uniform(int(s), int(p), int(n), int(d)) for s, p, n, d in idx], np.float32)
@@ -84,7 +104,7 @@ def rng_case():
 
 
 CASES = {"oracle_trace.npz": trace_case, "oracle_render.npz": render_case, "oracle_rng.npz": rng_case,
-         "oracle_quadric.npz": quadric_case, "oracle_texture.npz": texture_case}
+         "oracle_quadric.npz": quadric_case, "oracle_texture.npz": texture_case, "oracle_lights.npz": lights_case}
 
 if __name__ == "__main__":
     # writes the fixtures named on the command line (all of them without arguments)

@@ -84,3 +84,18 @@ def test_texture_and_integrator_golden():
         r = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_PBRT, seed=5, threads=1, integrator=kind,
                                                      light_strategy=strategy)
         np.testing.assert_allclose(r["sum"], g[f"{name}_sum"], rtol=RTOL, atol=1e-9)
+
+
+def test_lights_and_samplers_golden():
+    """The infinite light (rotated, with area lights besides), the stratified sampler, area lights on
+    spheres, disks and cylinders and a thin-lens camera, both modes, against the committed fixture
+    (the same renders as tests/golden/make_golden.py's lights_case)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLD / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(GOLD / "oracle_lights.npz")
+    got = mg.lights_case()
+    assert sorted(got) == sorted(g.files)
+    for k in g.files:
+        np.testing.assert_allclose(got[k], g[k], rtol=RTOL, atol=1e-9, err_msg=k)
