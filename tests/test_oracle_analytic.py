@@ -164,7 +164,7 @@ def test_thin_lens_rays_meet_on_the_plane_of_focus():
         assert np.abs(r[:3] + t * r[3:] - pts.mean(axis=0)).max() < 1e-3
 
 
-def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5, inner=0.0):
+def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5, inner=0.0, cylinder=None):
     """A matte floor (y = 0, 20 x 20) lit only by one shape light of unit radiance: `sphere` =
     (center, radius), `disk` = (center, radius) facing down."""
     tri = S._quad((-10, 0, -10), (10, 0, -10), (10, 0, 10), (-10, 0, 10), (0, 1, 0))
@@ -179,6 +179,11 @@ def _floor_scene(w, h, cam, sphere=None, disk=None, albedo=0.5, inner=0.0):
     if disk is not None:
         q = S.quadric(S.DISK, S.translation(disk[0]) @ S.rotation((1, 0, 0), 90), 1, radius=disk[1], height=0.0,
                       inner_radius=inner)
+        q["light_id"] = 0
+        quads = np.stack([q])
+    if cylinder is not None:  # (center, radius, half length): axis along world z
+        q = S.quadric(S.CYLINDER, S.translation(cylinder[0]), 1, radius=cylinder[1], z_min=-cylinder[2],
+                      z_max=cylinder[2])
         q["light_id"] = 0
         quads = np.stack([q])
     return S.SceneData(tri.astype(np.float32), np.zeros(2, np.uint32), np.full(2, -1, np.int32), sph, mats, lights,
@@ -246,3 +251,33 @@ def test_annulus_light_on_axis_known_answer_and_ref_defect():
     assert abs(v - expect) < 5 * se + 1e-3 * expect, (v, expect)
     rf = O.OracleScene(sd, fixed_bvh=True).render(A.BG_MODE_REF_COMPAT, spp=spp, rows=(16, 17, 1), threads=4)
     assert abs(rf["rgb"][16, 16, 0] - expect) > 0.05 * expect
+
+
+def test_cylinder_light_direct_lighting_matches_quadrature():
+    """A one-sided (outward) tube light of unit radiance above a matte floor: the floor shows
+    rho / pi * integral of cos_p cos_l / d^2 over the tube's surface facing the point (the tube is
+    convex, so that part is unoccluded), integrated here with a midpoint rule (PBRT)."""
+    c, rad, half = np.array([0.0, 0.8, 0.0]), 0.25, 0.6
+    cam = S.Camera((0.3, 0.3, 0.0), (0.3, 0.0, 0.0), (0.0, 0.0, -1.0), 10.0, 33, 33)
+    sd = _floor_scene(33, 33, cam, cylinder=(tuple(c), rad, half))
+    spp = 4096
+    o = O.OracleScene(sd).render(A.BG_MODE_PBRT, spp=spp, rows=(16, 17, 1), threads=4)
+    ray = O.camera_ray(cam, 16.5, 16.5).astype(np.float64)
+    p = ray[:3] + (-ray[1] / ray[4]) * ray[3:]
+    nz, nphi = 400, 800
+    z = -half + (np.arange(nz) + 0.5) * (2 * half / nz)
+    phi = (np.arange(nphi) + 0.5) * (2 * np.pi / nphi)
+    Z, PH = np.meshgrid(z, phi, indexing="ij")
+    nrm = np.stack([np.cos(PH), np.sin(PH), np.zeros_like(PH)], -1)
+    x = c + rad * nrm + np.stack([np.zeros_like(Z), np.zeros_like(Z), Z], -1)
+    d = p - x
+    dist2 = np.sum(d * d, -1)
+    dn = d / np.sqrt(dist2)[..., None]
+    cos_l = np.sum(nrm * dn, -1)
+    cos_p = -dn[..., 1]  # the floor's normal is +y; d points from the tube to p
+    dA = rad * (2 * np.pi / nphi) * (2 * half / nz)
+    E = np.sum(np.where((cos_l > 0) & (cos_p > 0), cos_l * cos_p / dist2, 0.0) * dA)
+    expect = 0.5 / np.pi * E
+    v = o["rgb"][16, 16, 0]
+    se = np.sqrt(max(o["sumsq"][16, 16, 0] / spp - (o["sum"][16, 16, 0] / spp) ** 2, 0) / spp)
+    assert abs(v - expect) < 5 * se + 2e-3 * expect, (v, expect, se)
