@@ -54,11 +54,13 @@ def parse():
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch", "whitted", "direct",
-                                          "example"],
+                                          "example", "relmse"],
                    default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
                         "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room; "
-                        "example: the reference's example scene (UV-textured sphere under an environment map)")
+                        "example: the reference's example scene (UV-textured sphere under an environment map); "
+                        "relmse: relMSE of the Cornell (256^2, 16 spp) and 1080p (64 spp) renders against "
+                        "--ref-spp renders of the same scene and mode")
     p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
     p.add_argument("--arm-seconds", type=float, default=90.0, help="guiding: time limit of each progressive arm")
     p.add_argument("--target", type=float, default=1e-3, help="guiding: relMSE target")
@@ -712,6 +714,50 @@ def run_guiding(args):
     ctx.close()
 
 
+def run_relmse(args):
+    """relMSE of the stated renders against --ref-spp (default 16384) renders of the same scene and
+    estimator mode: the Cornell box (256 x 256, 16 spp, depth 5) in REF_COMPAT (the reference's
+    estimator over its own BVH) and PBRT mode, and the 1080p production scene (64 spp, depth 8) in
+    PBRT mode.  relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 0.01), minus the
+    reference's own expected contribution; the reference render draws disjoint sample indices."""
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    from bonsai_gb300 import scenes as S
+    ctx = G.Context(0)
+    out = {}
+    cases = [("cornell_256_16spp_ref_compat", S.cornell(256, 256, spp=16), A.BG_MODE_REF_COMPAT, A.BG_BVH_REFERENCE),
+             ("cornell_256_16spp_pbrt", S.cornell(256, 256, spp=16), A.BG_MODE_PBRT, A.BG_BVH_WIDE)]
+    if not args.small:
+        cases.append(("production_1080p_64spp_pbrt", S.production(), A.BG_MODE_PBRT, A.BG_BVH_WIDE))
+    for name, sd, mode, bvh in cases:
+        W, H = sd.camera.width, sd.camera.height
+        scene = G.Scene(ctx, sd, bvh)
+        pi = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, sd.rr_threshold, mode=mode, seed=0)
+        graph = mode == A.BG_MODE_PBRT
+        t0 = time.time()
+        chunk = max(1, min(args.ref_spp, (1 << 30) // (W * H)))
+        for k in range(0, args.ref_spp, chunk):
+            pi.render(scene, spp=min(chunk, args.ref_spp - k), first_sample=(1 << 26) + k, accumulate=k > 0,
+                      readback=False, graph=graph)
+        s1, s2, n = G.PathIntegrator.moments(ctx, W, H)
+        nn = np.maximum(n[..., None], 1).astype(np.float64)
+        ref, ref2 = s1 / nn, s2 / nn
+        ref_var_term = float(np.mean(np.maximum(ref2 - ref * ref, 0.0) / nn / (ref ** 2 + 1e-2)))
+        ref_s = time.time() - t0
+        r = pi.render(scene, graph=graph)
+        s1, s2, n = G.PathIntegrator.moments(ctx, W, H)
+        img = s1 / np.maximum(n[..., None], 1)
+        out[name] = {"relmse": _relmse(img, ref, ref_var_term), "relmse_uncorrected": _relmse(img, ref, 0.0),
+                     "reference_var_term": ref_var_term, "spp": sd.spp, "reference_spp": args.ref_spp,
+                     "size": [W, H], "reference_render_s": ref_s, "error_word": int(r.stats.error_word)}
+        print(name, json.dumps(out[name]), flush=True)
+        scene.close()
+    print(json.dumps({"metric": "relMSE vs a high-spp render", "unit": "relMSE", "results": out,
+                      "relmse": "mean (x - ref)^2 / (ref^2 + 0.01) minus the reference's own variance term"}),
+          flush=True)
+    ctx.close()
+
+
 def _random_guide_data(n: int, seed: int):
     """Seeded synthetic training samples / queries with the value ranges the renderer produces."""
     rng = np.random.default_rng(seed)
@@ -833,6 +879,9 @@ def main():
         return
     if args.workload == "guiding":
         run_guiding(args)
+        return
+    if args.workload == "relmse":
+        run_relmse(args)
         return
     if args.workload in ("whitted", "direct", "example"):
         run_integrators(args)

@@ -42,6 +42,7 @@ BG_RENDER_STAGE_TIMING = 8
 BG_TUNE_SORT_RAYS = 1
 BG_TUNE_L2_PERSIST = 2
 BG_TUNE_TILE_PIXELS = 4
+BG_TUNE_SHADOW_QUEUE_HALF = 8
 BG_SAMPLER_INDEPENDENT, BG_SAMPLER_STRATIFIED = 0, 1
 
 BG_TEXTURE_IMAGE = 0
@@ -219,6 +220,7 @@ SIGNATURES = {
     "bg_guide_destroy": (None, [P]),
     "bg_guide_get_params": (ST, [P, P]),
     "bg_guide_set_params": (ST, [P, P]),
+    "bg_guide_set_wait_limit": (ST, [P, C.c_uint64]),
     "bg_guide_forward": (ST, [P, P, C.c_size_t, P]),
     "bg_guide_gradient": (ST, [P, P, C.c_size_t, P, C.POINTER(C.c_float)]),
     "bg_guide_train": (ST, [P, P, C.c_size_t, C.POINTER(C.c_float)]),

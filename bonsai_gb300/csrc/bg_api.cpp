@@ -255,7 +255,9 @@ bg_status ensure_film(bg_ctx* ctx, uint32_t w, uint32_t h) {
 }
 
 bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
-    if (ctx->wave.capacity >= cap && ctx->wave.ray_o) return BG_OK;
+    const bool half = ctx->shape.shadow_half != 0;
+    if (ctx->wave.capacity >= cap && ctx->wave.ray_o && (ctx->wave.sh_capacity == ctx->wave.capacity) == half)
+        return BG_OK;
     dfree_all(ctx, ctx->wave_allocs);
     ctx->wave = bg::WaveBuffers{};
     bg::WaveBuffers& w = ctx->wave;
@@ -278,9 +280,10 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(L, n * sizeof(float4));
     WB(nee_beta, n * sizeof(float4));
     WB(pending, 2 * n * sizeof(float4));
-    WB(sh_o, 2 * n * sizeof(float4));
-    WB(sh_d, 2 * n * sizeof(float4));
-    WB(sh_ref, 2 * n * sizeof(uint32_t));
+    const size_t nsh = half ? n : 2 * n;
+    WB(sh_o, nsh * sizeof(float4));
+    WB(sh_d, nsh * sizeof(float4));
+    WB(sh_ref, nsh * sizeof(uint32_t));
     WB(queue[0], n * sizeof(uint32_t));
     WB(queue[1], n * sizeof(uint32_t));
     WB(cls_queue, 5 * n * sizeof(uint32_t));
@@ -293,6 +296,7 @@ bg_status ensure_wave(bg_ctx* ctx, uint32_t cap) {
     WB(sort_hist, 8192 * sizeof(uint32_t));
 #undef WB
     w.capacity = cap;
+    w.sh_capacity = (uint32_t)nsh;
     if (cudaMemsetAsync(w.sort_hist, 0, 8192 * sizeof(uint32_t), ctx->stream) != cudaSuccess)
         return fail(ctx, BG_ERR_CUDA, "cudaMemsetAsync");
     return BG_OK;
@@ -378,8 +382,12 @@ bg_status check_device_error(bg_ctx* ctx, uint32_t* word) {
     if (word) *word = e;
     if (e) {
         CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream));
-        return fail(ctx, BG_ERR_DEVICE, "device error word 0x" + std::to_string(e) +
-                                            " (1 stack overflow, 2 queue overflow, 4 bad prim, 8 bad node)");
+        static const char* names[] = {"traversal stack overflow", "queue overflow", "bad primitive index",
+                                      "bad node index", "guide wait timed out"};
+        std::string what;
+        for (int b = 0; b < 5; ++b)
+            if (e & (1u << b)) what += (what.empty() ? "" : ", ") + std::string(names[b]);
+        return fail(ctx, BG_ERR_DEVICE, "device error word " + std::to_string(e) + ": " + what);
     }
     return BG_OK;
 }
@@ -596,7 +604,8 @@ bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
     out->blocks_per_sm = (uint32_t)ctx->shape.blocks_per_sm;
     out->refill = (uint32_t)ctx->shape.refill;
     out->flags = (ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u) | (ctx->shape.l2_persist ? BG_TUNE_L2_PERSIST : 0u) |
-                 (ctx->shape.tile_pixels ? BG_TUNE_TILE_PIXELS : 0u);
+                 (ctx->shape.tile_pixels ? BG_TUNE_TILE_PIXELS : 0u) |
+                 (ctx->shape.shadow_half ? BG_TUNE_SHADOW_QUEUE_HALF : 0u);
     return BG_OK;
 }
 
@@ -611,6 +620,7 @@ bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
     ctx->shape.sort_rays = (t->flags & BG_TUNE_SORT_RAYS) ? 1 : 0;
     ctx->shape.l2_persist = (t->flags & BG_TUNE_L2_PERSIST) ? 1 : 0;
     ctx->shape.tile_pixels = (t->flags & BG_TUNE_TILE_PIXELS) ? 1 : 0;
+    ctx->shape.shadow_half = (t->flags & BG_TUNE_SHADOW_QUEUE_HALF) ? 1 : 0;
     return BG_OK;
 }
 

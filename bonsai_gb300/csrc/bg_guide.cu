@@ -23,6 +23,10 @@
 
 namespace bg {
 
+// Limit (SM clock cycles) of the first wait on each MMA stage; bail_out's drain wait always uses
+// the default, so MMAs in flight retire before TMEM is freed.  Set by set_guide_wait_limit.
+__device__ long long g_guide_wait_limit = kWaitLimitCycles;
+
 namespace {
 
 constexpr uint32_t ACT_BYTES = 128 * GUIDE_K * 2;         // 20,480
@@ -121,6 +125,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
     const uint32_t n = count ? min(*count, max_n) : max_n;
     const uint32_t ntiles = (n + 127) / 128;
     if (blockIdx.x >= ntiles) return;
+    const long long wait_limit = g_guide_wait_limit;
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     uint8_t* wsm = sm;
     uint8_t* act[2] = {sm + GUIDE_WPACK_BYTES, sm + GUIDE_WPACK_BYTES + ACT_BYTES};
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
                 issue_forward(tmem + TM_FWD, smem_addr(act[l & 1]), w_addr + guide_wpack_off(l), N);
                 umma_commit(&bar);
             }
-            bool ok = mbar_wait(&bar, phase);
+            bool ok = mbar_wait(&bar, phase, wait_limit);
             phase ^= 1;
             tc_fence_after();
             if (l < GUIDE_LAYERS - 1) {
@@ -191,6 +196,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     __shared__ uint64_t bar;
     __shared__ uint32_t tslot;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long wait_limit = g_guide_wait_limit;
     if (a.step && blockIdx.x == 0 && tid == 0) atomicAdd(a.step, 1u);
     uint8_t* wsm = sm;
     uint8_t* act = sm + GUIDE_WPACK_BYTES;  // 5 tiles: X0, H1..H4
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
             issue_forward(tmem + TM_FWD, act_addr + l * ACT_BYTES, w_addr + guide_wpack_off(l), guide_rows(l));
             umma_commit(&bar);
         }
-        bool ok = mbar_wait(&bar, phase);
+        bool ok = mbar_wait(&bar, phase, wait_limit);
         phase ^= 1;
         tc_fence_after();
         if (l < GUIDE_LAYERS - 1) {
@@ -283,7 +289,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
                           umma_desc(a_l + 2 * ACT_RS * k, ACT_RS, 128), umma_idesc_bf16(128, GUIDE_K, 1, 1), k > 0);
             umma_commit(&bar);
         }
-        bool ok = mbar_wait(&bar, phase);
+        bool ok = mbar_wait(&bar, phase, wait_limit);
         phase ^= 1;
         tc_fence_after();
         // weight gradient rows (thread = output row)
@@ -483,6 +489,13 @@ void launch_pass_relvar(const FilmBuffers& film, uint32_t k, double* out, cudaSt
 void launch_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
                                float alpha, float* out, cudaStream_t s) {
     if (n) k_guide_mixture_eval<<<(n + 127) / 128, 128, 0, s>>>(raw, u, w, pb, n, alpha, out);
+}
+
+cudaError_t set_guide_wait_limit(uint64_t cycles, cudaStream_t s) {
+    const long long v = (cycles == 0 || cycles >= (uint64_t)kWaitLimitCycles) ? kWaitLimitCycles : (long long)cycles;
+    cudaError_t e = cudaMemcpyToSymbolAsync(g_guide_wait_limit, &v, sizeof(v), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // v lives on this stack frame
+    return e;
 }
 
 }  // namespace bg

@@ -1,8 +1,10 @@
 // bg_guide_api.cpp - C ABI of the guiding network and the progressive guided render.
 //
 // bg_render_guided runs opts->spp passes of 1 spp; the network's warm-up count, fallback decision
-// and variance estimates carry over between calls, so a long render can be issued in chunks.  Per pass: the wavefront renders the image
-// (guided passes add the network inference and the mixture continuation to every bounce); the
+// and variance estimates carry over between calls, so a long render can be issued in chunks.  Per
+// pass: the wavefront renders the image (guided passes add the network inference and a second
+// shading launch per bounce whose next-event estimation draws its second strategy from the
+// mixture; the continuation stays a BSDF sample); the
 // paths' training records land in a pool of samples_per_pass samples (subsampled by a keep
 // probability set from the previous pass's record count); one reduction estimates the pass's
 // relative variance against the mean of the earlier passes; then the pool is consumed in
@@ -317,6 +319,14 @@ void bg_guide_destroy(bg_guide* g) {
         free_guide_device(g);
     }
     delete g;
+}
+
+bg_status bg_guide_set_wait_limit(bg_guide* g, uint64_t cycles) {
+    if (!g || !g->ctx) return BG_ERR_INVALID;
+    bg_ctx* ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    CK(bg::set_guide_wait_limit(cycles, ctx->stream));
+    return BG_OK;
 }
 
 bg_status bg_guide_get_params(bg_guide* g, float* params) {

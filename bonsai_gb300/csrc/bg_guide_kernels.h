@@ -59,5 +59,8 @@ void launch_guide_wsum(const float4* samples, const PoolOrder& order, uint32_t b
 void launch_pass_relvar(const FilmBuffers& film, uint32_t k, double* out, cudaStream_t s);
 void launch_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
                                float alpha, float* out, cudaStream_t s);
+// Limit of the network kernels' tensor-core waits on the current device, in SM clock cycles
+// (0 or >= 2^31: the default, ~1 s).
+cudaError_t set_guide_wait_limit(uint64_t cycles, cudaStream_t s);
 
 }  // namespace bg

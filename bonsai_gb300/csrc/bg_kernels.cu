@@ -406,7 +406,7 @@ struct ShadowSrc {
 template <int LAYOUT, bool MULTI = false>
 __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuffers wb, uint32_t* err, int refill,
                                                               const SceneRender* tab) {
-    const uint32_t n = min(wb.counters[C_SHADOW], 2 * wb.capacity);
+    const uint32_t n = min(wb.counters[C_SHADOW], wb.sh_capacity);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[1], (unsigned long long)n);
     ShadowSrc src{wb, tab};
 #if BG_SMEM_STACK

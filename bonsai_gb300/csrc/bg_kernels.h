@@ -64,7 +64,8 @@ struct WaveBuffers {
     float4* L;          // rgb
     float4* nee_beta;   // beta at the NEE vertex
     float4* pending;    // 2 per slot: contribution rgb, w = 1 if unoccluded
-    float4* sh_o;       // 2 * capacity shadow rays: o.xyz, t_max
+    uint32_t sh_capacity;  // shadow-queue entries: 2 * capacity, or capacity with BG_TUNE_SHADOW_QUEUE_HALF
+    float4* sh_o;       // sh_capacity shadow rays: o.xyz, t_max
     float4* sh_d;       // d.xyz, skip prim (int bits)
     uint32_t* sh_ref;   // slot * 2 + kind
     uint32_t* queue[2];
@@ -129,6 +130,7 @@ struct LaunchShape {
     // BG_TUNE_TILE_PIXELS, on by default: production 1080p at 16 spp 169.4 ms against 174.1 ms in
     // scanline order (extension 104.8 against 108.7 ms), Whitted 443 against 460 ms
     int tile_pixels = 1;
+    int shadow_half = 0;  // BG_TUNE_SHADOW_QUEUE_HALF
 };
 
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,

@@ -13,7 +13,9 @@
 // that device current) resolves its device address with cudaGetSymbolAddress and caches it.  Make
 // that first call before any stream capture.  All calls share the one array and it keeps the last
 // call's contents, so each call clears what must start at zero; calls that overlap on the GPU
-// (two streams, two host threads) race on the array and must be serialised by the caller.
+// (two streams, two host threads) race on the array and must be serialised by the caller.  A call
+// is synchronous: it waits for its stream to finish the render and reads the device error word
+// back before it returns.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -155,6 +157,7 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     uint32_t* d_err = reinterpret_cast<uint32_t*>(base + OFF_ERR);
     WaveBuffers w{};
     w.capacity = (uint32_t)N;
+    w.sh_capacity = 2 * (uint32_t)N;
     w.ray_o = reinterpret_cast<float4*>(base + OFF_RAY_O);
     w.ray_d = reinterpret_cast<float4*>(base + OFF_RAY_D);
     w.hit = reinterpret_cast<int2*>(base + OFF_HIT);
@@ -176,21 +179,35 @@ extern "C" bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* c
     w.ray_stats = reinterpret_cast<unsigned long long*>(base + OFF_RAYSTATS);
 
     // the array keeps the previous call's contents: zero what accumulates
-    cudaMemsetAsync(film.sum, 0, npix * 3 * sizeof(double), s);
-    cudaMemsetAsync(film.sumsq, 0, npix * 3 * sizeof(double), s);
-    cudaMemsetAsync(film.count, 0, npix * sizeof(uint32_t), s);
-    cudaMemsetAsync(film.nan_count, 0, sizeof(unsigned long long), s);
-    cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s);
-    cudaMemsetAsync(w.counters, 0, 16 * sizeof(uint32_t), s);
-    cudaMemsetAsync(w.ray_stats, 0, 4 * sizeof(unsigned long long), s);
+    const struct {
+        void* p;
+        size_t bytes;
+        const char* what;
+    } clears[] = {{film.sum, npix * 3 * sizeof(double), "film sums"},
+                  {film.sumsq, npix * 3 * sizeof(double), "film squared sums"},
+                  {film.count, npix * sizeof(uint32_t), "film sample counts"},
+                  {film.nan_count, sizeof(unsigned long long), "film NaN count"},
+                  {d_err, sizeof(uint32_t), "error word"},
+                  {w.counters, 16 * sizeof(uint32_t), "wave counters"},
+                  {w.ray_stats, 4 * sizeof(unsigned long long), "ray statistics"}};
+    for (const auto& c : clears) {
+        e = cudaMemsetAsync(c.p, 0, c.bytes, s);
+        if (e != cudaSuccess)
+            return finish(reject(BG_ERR_CUDA, std::string("clearing the ") + c.what + ": " + cudaGetErrorString(e)));
+    }
 
     int dev_sms = 0;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
-    LaunchShape shape{dev_sms > 0 ? dev_sms : 1, 128, 8, 32};
+    e = cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess || dev_sms <= 0)
+        return finish(reject(BG_ERR_CUDA, std::string("multiprocessor count: ") + cudaGetErrorString(e)));
+    // fixed launch shape: bg_render's tuned shape and BG_TUNE_* settings belong to a bg_ctx, which
+    // this entry point does not take
+    LaunchShape shape{dev_sms, 128, 8, 32};
     Camera dc = camera_for(*cam);
     RenderParams rp{cam->width, cam->height, o->spp, o->max_depth, o->first_sample, o->rr_threshold, o->seed};
     rp = with_camera(rp, dc, o->spp);
     rp.strat = strat;
+    rp.pixel_tiles = 1;  // camera rays in 8 x 4 pixel tiles, bg_render's default order
     const uint64_t total = npix * o->spp;
     if (total > 0) {
         if (o->mode == BG_MODE_PBRT && (kind == BG_BVH_WIDE || kind == BG_BVH_WIDE2)) {

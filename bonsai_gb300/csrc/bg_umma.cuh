@@ -58,14 +58,28 @@ BG_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Waits for the phase with the given parity to complete; gives up after ~1 s of SM clock
-// (2^31 cycles) and returns false, so a lost arrival cannot hang the GPU.
-BG_D bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Non-blocking probe of the same phase (never suspends the thread).
+BG_D bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Default limit of a wait: ~1 s of SM clock.
+constexpr long long kWaitLimitCycles = 1ll << 31;
+// Waits for the phase with the given parity to complete; gives up after `limit` SM clock cycles
+// and returns false, so a lost arrival cannot hang the GPU.  Below the default limit the wait
+// polls with test_wait, which never suspends, so a short limit is honoured to the cycle.
+BG_D bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitLimitCycles) {
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1ll << 31)) return false;
+    const bool poll = limit < kWaitLimitCycles;
+    for (;;) {
+        if (poll ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > limit) return false;
     }
-    return true;
 }
 
 BG_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

@@ -390,7 +390,7 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
     for (int k = 0; k < 2; ++k) {
         pos = warp_append(&wb.counters[C_SHADOW], vo.push_sh[k]);
         if (vo.push_sh[k]) {
-            if (pos < 2 * wb.capacity) {
+            if (pos < wb.sh_capacity) {
                 wb.sh_o[pos] = vo.sh_o[k];
                 wb.sh_d[pos] = vo.sh_d[k];
                 wb.sh_ref[pos] = 2 * slot + (uint32_t)k;

@@ -93,38 +93,42 @@ class Scene:
         ctx.check(lib.bg_scene_create(ctx.h, C.byref(h)))
         self.h = h
         ctx._scenes.add(self)
-        for m in sd.materials:
-            mm = A.bg_material.from_buffer_copy(np.ascontiguousarray(m).tobytes())
-            ctx.check(lib.bg_scene_add_material(h, C.byref(mm), None))
-        for l in sd.lights:
-            ll = A.bg_area_light.from_buffer_copy(np.ascontiguousarray(l).tobytes())
-            ctx.check(lib.bg_scene_add_area_light(h, C.byref(ll), None))
-        for t in sd.textures:
-            tt, keep = S.texture_struct(t)
-            ctx.check(lib.bg_scene_add_texture(h, C.byref(tt), None))
-        if sd.env is not None:
-            el, keep = S.env_struct(sd.env)
-            ctx.check(lib.bg_scene_add_infinite_light(h, C.byref(el)))
-        tri = np.ascontiguousarray(sd.tri, np.float32)
-        tm = np.ascontiguousarray(sd.tri_mat, np.uint32)
-        tl = np.ascontiguousarray(sd.tri_light, np.int32)
-        if sd.tri_normals is None and sd.tri_uvs is None and sd.tri_flags is None:
-            ctx.check(lib.bg_scene_add_triangles(h, _ptr(tri), sd.ntri, _ptr(tm), _ptr(tl)))
-        else:
-            nrm = None if sd.tri_normals is None else np.ascontiguousarray(sd.tri_normals, np.float32)
-            uvs = None if sd.tri_uvs is None else np.ascontiguousarray(sd.tri_uvs, np.float32)
-            for a, b, has_n, fl in S.triangle_runs(sd):
-                ctx.check(lib.bg_scene_add_triangle_mesh(
-                    h, tri[a:].ctypes.data, b - a, tm[a:].ctypes.data, tl[a:].ctypes.data,
-                    nrm[a:].ctypes.data if has_n else None, uvs[a:].ctypes.data if uvs is not None else None, fl))
-        if sd.nsph:
-            sp = np.ascontiguousarray(sd.spheres)
-            ctx.check(lib.bg_scene_add_spheres(h, _ptr(sp), sd.nsph))
-        if len(sd.quadrics):
-            qu = np.ascontiguousarray(sd.quadrics)
-            ctx.check(lib.bg_scene_add_quadrics(h, _ptr(qu), len(qu)))
-        st = A.bg_build_stats()
-        ctx.check(lib.bg_scene_commit(h, bvh, C.byref(st)))
+        try:
+            for m in sd.materials:
+                mm = A.bg_material.from_buffer_copy(np.ascontiguousarray(m).tobytes())
+                ctx.check(lib.bg_scene_add_material(h, C.byref(mm), None))
+            for l in sd.lights:
+                ll = A.bg_area_light.from_buffer_copy(np.ascontiguousarray(l).tobytes())
+                ctx.check(lib.bg_scene_add_area_light(h, C.byref(ll), None))
+            for t in sd.textures:
+                tt, keep = S.texture_struct(t)
+                ctx.check(lib.bg_scene_add_texture(h, C.byref(tt), None))
+            if sd.env is not None:
+                el, keep = S.env_struct(sd.env)
+                ctx.check(lib.bg_scene_add_infinite_light(h, C.byref(el)))
+            tri = np.ascontiguousarray(sd.tri, np.float32)
+            tm = np.ascontiguousarray(sd.tri_mat, np.uint32)
+            tl = np.ascontiguousarray(sd.tri_light, np.int32)
+            if sd.tri_normals is None and sd.tri_uvs is None and sd.tri_flags is None:
+                ctx.check(lib.bg_scene_add_triangles(h, _ptr(tri), sd.ntri, _ptr(tm), _ptr(tl)))
+            else:
+                nrm = None if sd.tri_normals is None else np.ascontiguousarray(sd.tri_normals, np.float32)
+                uvs = None if sd.tri_uvs is None else np.ascontiguousarray(sd.tri_uvs, np.float32)
+                for a, b, has_n, fl in S.triangle_runs(sd):
+                    ctx.check(lib.bg_scene_add_triangle_mesh(
+                        h, tri[a:].ctypes.data, b - a, tm[a:].ctypes.data, tl[a:].ctypes.data,
+                        nrm[a:].ctypes.data if has_n else None, uvs[a:].ctypes.data if uvs is not None else None, fl))
+            if sd.nsph:
+                sp = np.ascontiguousarray(sd.spheres)
+                ctx.check(lib.bg_scene_add_spheres(h, _ptr(sp), sd.nsph))
+            if len(sd.quadrics):
+                qu = np.ascontiguousarray(sd.quadrics)
+                ctx.check(lib.bg_scene_add_quadrics(h, _ptr(qu), len(qu)))
+            st = A.bg_build_stats()
+            ctx.check(lib.bg_scene_commit(h, bvh, C.byref(st)))
+        except BaseException:
+            self.close()  # a failed build releases what it had allocated
+            raise
         self.build_ms, self.nodes, self.bvh = st.build_ms, st.nodes, bvh
 
     def close(self):
@@ -302,6 +306,10 @@ class Guide:
         p = np.ascontiguousarray(p, np.float32)
         assert p.size == A.BG_GUIDE_PARAMS
         self.ctx.check(self.ctx.lib.bg_guide_set_params(self.h, _ptr(p)))
+
+    def set_wait_limit(self, cycles: int):
+        """Limit of the network kernels' tensor-core waits in SM cycles (0 = the default, ~1 s)."""
+        self.ctx.check(self.ctx.lib.bg_guide_set_wait_limit(self.h, cycles))
 
     def forward(self, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, A.BG_GUIDE_QUERY_FLOATS)

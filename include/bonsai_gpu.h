@@ -330,6 +330,11 @@ typedef struct bg_tuning {
 #define BG_TUNE_TILE_PIXELS 4u /* generate the wavefront's camera rays in 8 x 4 pixel tiles instead of
                                   scanline order (more coherent first-bounce traversal); on by
                                   default                                                        */
+#define BG_TUNE_SHADOW_QUEUE_HALF 8u /* shadow-ray queue of one entry per path instead of two (saves
+                                        36 B per path).  A bounce whose paths queue more shadow rays
+                                        than that (each vertex may queue two: the light sample and the
+                                        MIS ray toward the light) drops the excess and the render fails
+                                        with BG_ERR_DEVICE (queue overflow in bg_last_error) */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 
@@ -416,7 +421,8 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
  * array of BG_NOALLOC_SCRATCH_BYTES bytes that every GPU loading the library holds until exit.
  * Limits: the path integrator only; at most BG_NOALLOC_MAX_PIXELS film pixels (larger films return BG_ERR_INVALID with the
  * limit in bg_last_error of the scene's context); waves of BG_NOALLOC_WAVE_PATHS paths; no
- * ACCUMULATE / STAGE_TIMING / GRAPH flags.  The caller passes the committed scene, the output
+ * ACCUMULATE / STAGE_TIMING / GRAPH flags; a fixed launch shape (the context's tuned shape and
+ * BG_TUNE_* settings do not apply; camera rays keep bg_render's 8 x 4 pixel-tile order).  The caller passes the committed scene, the output
  * d_rgb_out (device memory, width*height*3 floats) and a CUDA stream (NULL = default stream); the
  * call synchronizes that stream before returning.  The first call on a device resolves the
  * array's device address, so make it before any stream capture.  All calls share the array:
@@ -432,9 +438,12 @@ bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, cons
  * BSDF only, src/integrators/path.rs:110-117).  A small network maps a shading point (position
  * normalised to the scene bounds and encoded with 12 octaves of sin/cos, shading normal,
  * outgoing direction) to a mixture of 8 von Mises-Fisher lobes and a selection probability c.
- * At matte, plastic and conductor vertices bg_render_guided draws the continuation from the
- * one-sample mixture c * guide + (1 - c) * BSDF and weights it by that mixture's pdf, so the
- * estimate stays unbiased whatever the network outputs.  The network (78 -> 4 x 64 ReLU -> 41,
+ * At matte, plastic and conductor vertices bg_render_guided uses the network in next-event
+ * estimation (estimate_direct, src/base/integrator.rs:330-437): the second strategy, which the
+ * reference draws from the BSDF to look for the chosen light, is drawn from the one-sample mixture
+ * c * guide + (1 - c) * BSDF and MIS-weighted by that mixture's pdf against the light sample.  The
+ * path's continuation stays a BSDF sample.  The estimate stays unbiased whatever the network
+ * outputs.  The network (78 -> 4 x 64 ReLU -> 41,
  * BF16 weights and activations, FP32 accumulation on the tensor cores) trains online on the
  * radiance the render itself measures, with Adam.
  *
@@ -491,6 +500,13 @@ typedef struct bg_guide_stats {
 bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out);
 void bg_guide_destroy(bg_guide* guide);
 bg_status bg_guide_get_params(bg_guide* guide, float* params);
+/* Limit, in SM clock cycles, of each tensor-core wait in the network's kernels on the guide's
+ * device (every network on that device shares it); 0 restores the default of 2^31 cycles
+ * (about 1 s).  A wait that runs out stops its kernel: it lets the matrix operations already
+ * issued finish (under the default limit), frees its tensor memory and returns, and the call
+ * that launched it returns BG_ERR_TIMEOUT; the context stays usable.  Meant for tests of that
+ * path: a limit far below one operation's latency makes every launch time out. */
+bg_status bg_guide_set_wait_limit(bg_guide* guide, uint64_t cycles);
 /* Replaces the weights and resets the Adam state. */
 bg_status bg_guide_set_params(bg_guide* guide, const float* params);
 /* Network outputs for n host-side queries (out: n * BG_GUIDE_OUTPUTS floats). */

@@ -7,9 +7,15 @@ checks each film against the allocating entry point bg_render on the same scene 
 The two entry points draw the same random numbers; only the FP64 atomic summation order of the
 film differs, so the resolved pixels agree to float rounding (rtol 1e-5, atol 1e-6).
 
+The test also reads the device's free memory (cudaMemGetInfo) around the second call: the first
+call has already loaded the kernels and resolved the scratch array's address, so a call that
+allocates nothing leaves the free bytes unchanged.
+
 The file name sorts last so a run that stops at the first failure has run every other test.
 """
 import ctypes as C
+import os
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -21,6 +27,23 @@ from bonsai_gb300 import scenes as S
 pytestmark = pytest.mark.gpu
 
 RTOL, ATOL = 1e-5, 1e-6
+
+
+def _cudart():
+    """The CUDA runtime's shared library (the toolkit's), for cudaMemGetInfo."""
+    home = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    for name in ("libcudart.so", "libcudart.so.13"):
+        for d in (home / "lib64", home / "lib", home / "targets" / "sbsa-linux" / "lib",
+                  home / "targets" / "x86_64-linux" / "lib"):
+            if (d / name).exists():
+                return C.CDLL(str(d / name))
+    return C.CDLL("libcudart.so.13")
+
+
+def _free_bytes(rt) -> int:
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
 
 
 def _opts(sd, mode):
@@ -44,10 +67,15 @@ def test_noalloc_matches_bg_render(mode, bvh):
         ctx.check(ctx.lib.bg_render(ctx.h, scene.h, C.byref(cam), C.byref(o), want.ctypes.data, C.byref(st)))
         assert want.mean() > 0.0
         d_out = ctx.alloc(want.nbytes)  # the caller owns the output buffer
+        rt = _cudart()
         try:
-            for _ in range(2):
+            for call in range(2):
                 got = np.full_like(want, -1.0)
+                before = _free_bytes(rt)
                 ctx.check(ctx.lib.bg_render_noalloc(scene.h, C.byref(cam), C.byref(o), d_out, None))
+                after = _free_bytes(rt)
+                if call == 1:  # kernels loaded and the scratch address resolved by the first call
+                    assert after == before, f"device free memory changed by {before - after} bytes"
                 ctx.d2h(got, d_out)
                 np.testing.assert_allclose(got, want, rtol=RTOL, atol=ATOL)
         finally:
