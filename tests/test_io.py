@@ -1,6 +1,7 @@
 """Scene and film I/O without a GPU: the library's OBJ reader against the Python restatement of
 OBJ::read (src/io/obj.rs:16-123), its error cases, and the EXR writer / reader round trip."""
 import struct
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -133,6 +134,21 @@ def test_exr_roundtrip(tmp_path):
     back = bio.read_exr(p)
     assert back.shape == img.shape
     np.testing.assert_array_equal(back, img)
+
+
+def test_exr_matches_the_spec_fixture(tmp_path):
+    """The writer's bytes for a 2 x 2 image equal tests/golden/exr_2x2.bin, which
+    tests/golden/make_exr_fixture.py spells out field by field from the OpenEXR file layout
+    (independent of this package's reader and of the library's writer)."""
+    img = np.zeros((2, 2, 3), np.float32)
+    for y in range(2):
+        for x in range(2):
+            r = 1.0 + x + 2 * y
+            img[y, x] = (r, 10 * r, 100 * r)
+    p = tmp_path / "fixture.exr"
+    bio.write_exr(p, img)
+    want = (Path(__file__).resolve().parent / "golden" / "exr_2x2.bin").read_bytes()
+    assert p.read_bytes() == want
 
 
 def test_exr_rejects_bad_arguments(tmp_path):
