@@ -1,8 +1,12 @@
 """Builds libbonsai_gpu.so in-tree (bonsai_gb300/lib/) for sm_103a.
 
-CUDA sources: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo -fmad=false.
--fmad=false keeps every float operation rounded as written (the reference is Rust f32, which
-never contracts a*b+c); kernels use fmaf() explicitly where a fused product is intended.
+CUDA sources: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo, with -fmad=false for
+the units that hold traversal, the reference-compatible (REF_COMPAT) kernels and the per-thread
+integrators: there every float operation rounds as written (the reference is Rust f32, which never
+contracts a*b+c), and kernels use fmaf() where a fused product is intended.  The PBRT-mode shading
+units (FUSED_SOURCES) let nvcc contract products into fused multiply-adds; the triangle test and
+the error-free products they share with traversal are written with explicitly rounded intrinsics,
+so they round the same in every unit.
 Host sources: g++ -O2 -ffp-contract=off.  Translation units compile in parallel.
 """
 from __future__ import annotations
@@ -26,6 +30,9 @@ CU_SOURCES = ["bg_kernels.cu", "bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade
               "bg_integrators.cu", "bg_integrators_pbrt.cu", "bg_tree_wave.cu",
               "bg_tree_shade_w.cu", "bg_tree_shade_d.cu"]
 CPP_SOURCES = ["bg_api.cpp", "bg_bvh.cpp", "bg_guide_api.cpp", "bg_io.cpp"]
+# PBRT-mode shade launches (wavefront, guided, batch, Whitted / direct-lighting tree wavefront)
+FUSED_SOURCES = {"bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade_guided_full.cu", "bg_shade_shapes.cu",
+                 "bg_tree_shade_w.cu", "bg_tree_shade_d.cu"}
 
 
 def _nvcc() -> str:
@@ -40,7 +47,8 @@ def commands() -> tuple[list[list[str]], list[str]]:
     for src in CU_SOURCES:
         o = str(OBJ / (Path(src).stem + ".o"))
         defines = os.environ.get("BONSAI_NVCC_DEFINES", "").split()  # -DNAME=VALUE traversal variants
-        cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+        fmad = "-fmad=true" if src in FUSED_SOURCES else "-fmad=false"
+        cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", fmad, "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills", *defines, "-c", str(CSRC / src), "-o", o])
         objs.append(o)
     for src in CPP_SOURCES:

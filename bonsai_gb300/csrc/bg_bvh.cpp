@@ -8,6 +8,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <deque>
 #include <future>
 #include <memory>
 
@@ -501,6 +502,7 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
     out->leaf_prims.reserve(3 * (size_t)n);
     out->nodes.push_back(Bvh8Node{});
     std::vector<Wide> queue{{root.get(), 0}};
+    std::deque<BNode> pieces;  // leaves split to fill free child slots (stable addresses)
     for (size_t qi = 0; qi < queue.size(); ++qi) {
         const BNode* b = queue[qi].bin;
         const uint32_t idx = queue[qi].index;
@@ -523,6 +525,37 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
                 ch[best] = c->l.get();
                 ch.push_back(c->r.get());
             }
+        }
+        // free slots: split leaves of several primitives (largest area first) so that each part
+        // gets its own quantised box, which the node test culls before any primitive test
+        while (ch.size() < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (size_t i = 0; i < ch.size(); ++i)
+                if (ch[i]->count > 1 && ch[i]->box.area() > best_area) {
+                    best_area = ch[i]->box.area();
+                    best = (int)i;
+                }
+            if (best < 0) break;
+            const BNode* c = ch[best];
+            // the first primitive alone, the rest (1 or 2) in a second leaf
+            BNode& a = pieces.emplace_back();
+            BNode& r = pieces.emplace_back();
+            a.first = c->first;
+            a.count = 1;
+            r.first = c->first + 1;
+            r.count = c->count - 1;
+            for (int k = 0; k < 3; ++k) {
+                a.box.lo[k] = refs[a.first].lo[k];
+                a.box.hi[k] = refs[a.first].hi[k];
+            }
+            for (uint32_t t = r.first; t < r.first + r.count; ++t)
+                for (int k = 0; k < 3; ++k) {
+                    r.box.lo[k] = std::fmin(r.box.lo[k], refs[t].lo[k]);
+                    r.box.hi[k] = std::fmax(r.box.hi[k], refs[t].hi[k]);
+                }
+            ch[best] = &a;
+            ch.push_back(&r);
         }
         Box nb;
         for (const BNode* c : ch) nb.grow(c->box);

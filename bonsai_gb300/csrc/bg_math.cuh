@@ -53,10 +53,10 @@ BG_D float rclamp(float v, float lo, float hi) {
 // edge functions (src/shapes/triangle.rs:179-190) and cross products (src/geometries/vec3.rs:108-122):
 // the sign is exact and the value is within 1.5 ulp of the exact difference.
 BG_D float diff_of_products(float a, float b, float c, float d) {
-    float cd = c * d;
+    float cd = __fmul_rn(c, d);
     float err = fmaf(-c, d, cd);
     float dop = fmaf(a, b, -cd);
-    return dop + err;
+    return __fadd_rn(dop, err);
 }
 
 struct V3 {

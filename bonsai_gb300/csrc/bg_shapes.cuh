@@ -42,46 +42,54 @@ struct TriHit {
     float t, b0, b1, b2;
 };
 
-// Triangle::intersect_test / the t part of Triangle::intersect (triangle.rs:135-268).
+// Triangle::intersect_test / the t part of Triangle::intersect (triangle.rs:135-268).  Every
+// product and sum is written with an explicitly rounded intrinsic, so the test rounds as the
+// reference's f32 code in every translation unit, whatever its -fmad setting: the edge functions
+// must never be contracted into fused multiply-adds, or two triangles sharing an edge could both
+// reject a ray through that edge (the test would no longer be watertight).
 BG_D bool tri_test(const TriRay& tr, float t_max, V3 p0, V3 p1, V3 p2, TriHit* out) {
-    V3 p0t = permute(p0 - tr.o, tr.kx, tr.ky, tr.kz);
-    V3 p1t = permute(p1 - tr.o, tr.kx, tr.ky, tr.kz);
-    V3 p2t = permute(p2 - tr.o, tr.kx, tr.ky, tr.kz);
-    p0t.x += tr.sx * p0t.z;
-    p0t.y += tr.sy * p0t.z;
-    p1t.x += tr.sx * p1t.z;
-    p1t.y += tr.sy * p1t.z;
-    p2t.x += tr.sx * p2t.z;
-    p2t.y += tr.sy * p2t.z;
-    float e0 = p1t.x * p2t.y - p1t.y * p2t.x;
-    float e1 = p2t.x * p0t.y - p2t.y * p0t.x;
-    float e2 = p0t.x * p1t.y - p0t.y * p1t.x;
+    auto mul = [](float a, float b) { return __fmul_rn(a, b); };
+    auto add = [](float a, float b) { return __fadd_rn(a, b); };
+    auto sub = [](float a, float b) { return __fsub_rn(a, b); };
+    V3 p0t = permute(v3(sub(p0.x, tr.o.x), sub(p0.y, tr.o.y), sub(p0.z, tr.o.z)), tr.kx, tr.ky, tr.kz);
+    V3 p1t = permute(v3(sub(p1.x, tr.o.x), sub(p1.y, tr.o.y), sub(p1.z, tr.o.z)), tr.kx, tr.ky, tr.kz);
+    V3 p2t = permute(v3(sub(p2.x, tr.o.x), sub(p2.y, tr.o.y), sub(p2.z, tr.o.z)), tr.kx, tr.ky, tr.kz);
+    p0t.x = add(p0t.x, mul(tr.sx, p0t.z));
+    p0t.y = add(p0t.y, mul(tr.sy, p0t.z));
+    p1t.x = add(p1t.x, mul(tr.sx, p1t.z));
+    p1t.y = add(p1t.y, mul(tr.sy, p1t.z));
+    p2t.x = add(p2t.x, mul(tr.sx, p2t.z));
+    p2t.y = add(p2t.y, mul(tr.sy, p2t.z));
+    float e0 = sub(mul(p1t.x, p2t.y), mul(p1t.y, p2t.x));
+    float e1 = sub(mul(p2t.x, p0t.y), mul(p2t.y, p0t.x));
+    float e2 = sub(mul(p0t.x, p1t.y), mul(p0t.y, p1t.x));
     if (e0 == 0.0f || e1 == 0.0f || e2 == 0.0f) {  // triangle.rs:178-190 (f64 there)
         e0 = diff_of_products(p1t.x, p2t.y, p1t.y, p2t.x);
         e1 = diff_of_products(p2t.x, p0t.y, p2t.y, p0t.x);
         e2 = diff_of_products(p0t.x, p1t.y, p0t.y, p1t.x);
     }
     if ((e0 < 0.0f || e1 < 0.0f || e2 < 0.0f) && (e0 > 0.0f || e1 > 0.0f || e2 > 0.0f)) return false;
-    float det = e0 + e1 + e2;
+    float det = add(add(e0, e1), e2);
     if (det == 0.0f) return false;
-    p0t.z *= tr.sz;
-    p1t.z *= tr.sz;
-    p2t.z *= tr.sz;
-    float ts = e0 * p0t.z + e1 * p1t.z + e2 * p2t.z;
-    if (det < 0.0f && (ts >= 0.0f || ts < t_max * det)) return false;
-    else if (det > 0.0f && (ts <= 0.0f || ts > t_max * det)) return false;
+    p0t.z = mul(p0t.z, tr.sz);
+    p1t.z = mul(p1t.z, tr.sz);
+    p2t.z = mul(p2t.z, tr.sz);
+    float ts = add(add(mul(e0, p0t.z), mul(e1, p1t.z)), mul(e2, p2t.z));
+    if (det < 0.0f && (ts >= 0.0f || ts < mul(t_max, det))) return false;
+    else if (det > 0.0f && (ts <= 0.0f || ts > mul(t_max, det))) return false;
     float inv_det = 1.0f / det;
-    float t = ts * inv_det;
+    float t = mul(ts, inv_det);
     // conservative t bound (triangle.rs:219-239)
     float max_zt = max_component(vabs(v3(p0t.z, p1t.z, p2t.z)));
-    float delta_z = gamma(3.0f) * max_zt;
+    float delta_z = mul(gamma(3.0f), max_zt);
     float max_xt = max_component(vabs(v3(p0t.x, p1t.x, p2t.x)));
     float max_yt = max_component(vabs(v3(p0t.y, p1t.y, p2t.y)));
-    float delta_x = gamma(5.0f) * (max_xt + max_zt);
-    float delta_y = gamma(5.0f) * (max_yt + max_zt);
-    float delta_e = 2.0f * (gamma(2.0f) * max_xt * max_yt + delta_y * max_xt + delta_x * max_yt);
+    float delta_x = mul(gamma(5.0f), add(max_xt, max_zt));
+    float delta_y = mul(gamma(5.0f), add(max_yt, max_zt));
+    float delta_e = mul(2.0f, add(add(mul(mul(gamma(2.0f), max_xt), max_yt), mul(delta_y, max_xt)), mul(delta_x, max_yt)));
     float max_e = max_component(vabs(v3(e0, e1, e2)));
-    float delta_t = 3.0f * (gamma(3.0f) * max_e * max_zt + delta_e * max_zt + delta_z * max_e) * fabsf(inv_det);
+    float delta_t = mul(mul(3.0f, add(add(mul(mul(gamma(3.0f), max_e), max_zt), mul(delta_e, max_zt)), mul(delta_z, max_e))),
+                        fabsf(inv_det));
     if (t <= delta_t) return false;
     // degenerate-triangle exit (triangle.rs:241-268 with the default uvs): rejected only when both
     // dpdu x dpdv and (p2-p0)x(p1-p0) vanish
@@ -94,9 +102,9 @@ BG_D bool tri_test(const TriRay& tr, float t_max, V3 p0, V3 p1, V3 p2, TriHit* o
     }
     if (out) {
         out->t = t;
-        out->b0 = e0 * inv_det;
-        out->b1 = e1 * inv_det;
-        out->b2 = e2 * inv_det;
+        out->b0 = mul(e0, inv_det);
+        out->b1 = mul(e1, inv_det);
+        out->b2 = mul(e2, inv_det);
     }
     return true;
 }

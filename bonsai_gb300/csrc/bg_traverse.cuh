@@ -521,14 +521,13 @@ BG_D int bvh8_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) 
 }
 
 // Persistent traversal of the 8-wide layout with in-warp ray replacement (see traverse_queue).
-// The node-group stack lives in shared memory, entry k of thread t at smem[k * blockDim.x + t].
-// Triangle groups are postponed (pushed) while fewer than kPostpone lanes of the warp would test
-// triangles, so leaf work runs with more lanes at once (Ylitie et al. 2017, section 5).
-#ifndef BG_POSTPONE
-#define BG_POSTPONE 0
-#endif
-constexpr int kPostpone = BG_POSTPONE;  // 0 disables postponement
-
+// Each iteration a lane visits at most one node (the next child of its node group) and tests at
+// most one primitive of its pending primitive group.  A node test that yields primitives while
+// others are still pending pushes them (a primitive group: upper byte 0) behind the pending ones.
+// Testing a whole group in one iteration would hold the warp for as many steps as its largest group
+// while the other lanes wait; interleaving keeps the primitive steps as full as the node steps.
+// The node-group stack lives in local memory (BG_SMEM_STACK: shared memory, entry k of thread t at
+// smem[k * blockDim.x + t]).
 // MULTI: rays of different scenes share the queue; src.scene(i) gives the scene of ray i.
 template <bool ANY, class Src, bool MULTI = false>
 BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill,
@@ -583,7 +582,8 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         if (__ballot_sync(0xffffffffu, busy) == 0) break;
         if (!busy) continue;
         bool done = false;
-        if (ngroup.y > 0x00FFFFFFu) {
+        // node step: the next child of the node group (room for two pushes when primitives wait)
+        if (ngroup.y > 0x00FFFFFFu && (tgroup.y == 0 || sp + 2 <= STACK8)) {
             const uint32_t hits = ngroup.y;
             const uint32_t bit = 31u - __clz(hits);
             ngroup.y &= ~(1u << bit);
@@ -605,39 +605,42 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                 ngroup = make_uint2(0, 0);
                 tgroup = make_uint2(0, 0);
             } else {
-                bvh8_node_hits(S(), child, r8, ray.t_max, &ngroup, &tgroup);
+                uint2 found;
+                bvh8_node_hits(S(), child, r8, ray.t_max, &ngroup, &found);
+                if (found.y != 0) {
+                    if (tgroup.y == 0) tgroup = found;
+                    else stack[sstride * sp++] = found;  // upper byte 0: a primitive group
+                }
             }
-        } else {
-            tgroup = ngroup;
-            ngroup = make_uint2(0, 0);
         }
+        // primitive step: one primitive of the pending group
         if (tgroup.y != 0) {
-            const unsigned want = __ballot_sync(__activemask(), true);
-            if (__popc(want) < kPostpone && ngroup.y > 0x00FFFFFFu && sp < STACK8) {
-                stack[sstride * sp++] = tgroup;  // upper byte 0: popped back as a triangle group
-                tgroup.y = 0;
-            }
-        }
-        while (tgroup.y != 0) {
             const uint32_t bit = 31u - __clz(tgroup.y);
             tgroup.y &= ~(1u << bit);
             if (tgroup.x + bit >= S().ntri + S().nsph + S().nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
-                continue;
-            }
-            int prim;
-            if (leaf_prim_hit(S(), tgroup.x + bit, tr, ray, !ANY, &prim)) {
-                if (ANY && prim == skip) continue;
-                hit = prim;
-                if (ANY) {
-                    done = true;
-                    break;
+            } else {
+                int prim;
+                if (leaf_prim_hit(S(), tgroup.x + bit, tr, ray, !ANY, &prim) && !(ANY && prim == skip)) {
+                    hit = prim;
+                    if (ANY) done = true;
                 }
             }
         }
+        // next groups: a node group from the stack; a primitive group only when none is pending
         if (!done && ngroup.y <= 0x00FFFFFFu) {
-            if (sp == 0) done = true;
-            else ngroup = stack[sstride * --sp];
+            while (sp > 0) {
+                const uint2 g = stack[sstride * (sp - 1)];
+                if (g.y > 0x00FFFFFFu) {
+                    ngroup = g;
+                    --sp;
+                    break;
+                }
+                if (tgroup.y != 0) break;
+                tgroup = g;
+                --sp;
+            }
+            if (ngroup.y <= 0x00FFFFFFu && tgroup.y == 0 && sp == 0) done = true;
         }
         if (done) {
             src.store(idx, hit, ray.t_max);

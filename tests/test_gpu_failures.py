@@ -57,7 +57,7 @@ def _lit_floor(w=32, h=32, spp=4):
     mats = np.stack([S.material(S.MATTE, kd=(0.5, 0.5, 0.5)), S.material(S.MATTE, kd=(0, 0, 0))])
     lights = np.zeros(1, S.LIGHT_DT)
     lights[0] = ((1.0, 1.0, 1.0), 1)
-    cam = S.Camera((0.0, -0.9, 0.0), (0.0, -1.0, -1.0), (0.0, 1.0, 0.0), 60.0, w, h)
+    cam = S.Camera((0.0, -0.9, 0.0), (0.0, -1.0, -0.05), (0.0, 1.0, 0.0), 60.0, w, h)  # every ray meets the floor
     return S.SceneData(tri, np.array([0, 0, 1, 1], np.uint32), np.array([-1, -1, 0, 0], np.int32),
                        np.zeros(0, S.SPHERE_DT), mats, lights, cam, spp=spp, max_depth=3, rr_threshold=1.0,
                        name="lit_floor")
