@@ -482,6 +482,8 @@ int axis_exponent(double extent) {
 
 }  // namespace
 
+bool g_bvh8_single_leaves = false;
+uint32_t g_bvh8_max_leaf = 3;  // experiment: every leaf child holds one primitive
 void build_bvh8(const HostPrims& p, Bvh8* out) {
     out->nodes.clear();
     out->leaf_prims.clear();
@@ -497,7 +499,7 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
         }
         refs[i].id = i;
     }
-    std::unique_ptr<BNode> root = build_rec(refs.data(), 0, n, 0, 3);
+    std::unique_ptr<BNode> root = build_rec(refs.data(), 0, n, 0, 2);
     out->nodes.reserve(n / 4 + 2);
     out->leaf_prims.reserve(3 * (size_t)n);
     out->nodes.push_back(Bvh8Node{});
@@ -538,7 +540,7 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
                 }
             if (best < 0) break;
             const BNode* c = ch[best];
-            // the first primitive alone, the rest (1 or 2) in a second leaf
+            // two leaves of one primitive each
             BNode& a = pieces.emplace_back();
             BNode& r = pieces.emplace_back();
             a.first = c->first;
@@ -597,16 +599,18 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
             ex[k] = axis_exponent((double)nb.hi[k] - (double)nb.lo[k]);
             nd.e[k] = (uint8_t)(ex[k] + 127);
         }
-        // internal children first (contiguous, slot order), then leaf primitives (slot order)
-        uint32_t nint = 0;
-        for (int sl = 0; sl < 8; ++sl)
-            if (slot_child[sl] >= 0 && ch[slot_child[sl]]->count == 0) ++nint;
+        // internal children contiguous from child_base, leaf primitives from tri_base, both in slot
+        // order; empty slots keep the inverted box (qlo 255 > qhi 0), which no ray enters
         nd.child_base = (uint32_t)(queue.size());
         nd.tri_base = (uint32_t)(out->leaf_prims.size() / 3);
-        uint32_t tri_off = 0, int_k = 0;
+        uint32_t int_k = 0;
         for (int sl = 0; sl < 8; ++sl) {
             int ci = slot_child[sl];
-            if (ci < 0) continue;
+            if (ci < 0) {
+                nd.qlo_x[sl] = nd.qlo_y[sl] = nd.qlo_z[sl] = 255;
+                nd.qhi_x[sl] = nd.qhi_y[sl] = nd.qhi_z[sl] = 0;
+                continue;
+            }
             const BNode* c = ch[ci];
             for (int k = 0; k < 3; ++k) {
                 double sc = std::ldexp(1.0, ex[k]);
@@ -621,18 +625,14 @@ void build_bvh8(const HostPrims& p, Bvh8* out) {
             }
             if (c->count == 0) {
                 nd.imask |= (uint8_t)(1u << sl);
-                nd.meta[sl] = (uint8_t)((1u << 5) | (24u + (uint32_t)sl));
                 queue.push_back({c, nd.child_base + int_k});
                 ++int_k;
-            } else {
-                uint32_t cnt = c->count;  // 1..3
-                static const uint8_t unary[4] = {0, 1, 3, 7};
-                nd.meta[sl] = (uint8_t)((unary[cnt] << 5) | tri_off);
-                for (uint32_t t = 0; t < cnt; ++t) emit_prim(p, refs[c->first + t].id, &out->leaf_prims);
-                tri_off += cnt;
+            } else {  // leaves of the binary build hold at most two primitives
+                nd.leafmask |= (uint8_t)(1u << sl);
+                if (c->count == 2) nd.twomask |= (uint8_t)(1u << sl);
+                for (uint32_t t = 0; t < c->count; ++t) emit_prim(p, refs[c->first + t].id, &out->leaf_prims);
             }
         }
-        (void)nint;
         if (out->nodes.size() < queue.size()) out->nodes.resize(queue.size());
         out->nodes[idx] = nd;
     }

@@ -38,9 +38,10 @@ struct Bvh2 {
 };
 void build_bvh2(const HostPrims& p, Bvh2* out, int threads);
 
-// 8-wide compressed BVH: binary SAH BVH with leaves of at most 3 primitives, collapsed greedily
-// (the largest-area internal child is opened until 8 children), child slots assigned by octant,
-// boxes quantised to 8 bits (conservative floor / ceil).
+// 8-wide compressed BVH: binary SAH BVH with leaves of at most 2 primitives, collapsed greedily
+// (the largest-area internal child is opened until 8 children, then leaves of two primitives are
+// split while slots are free), child slots assigned by octant, boxes quantised to 8 bits
+// (conservative floor / ceil).
 struct Bvh8 {
     std::vector<Bvh8Node> nodes;
     std::vector<float4> leaf_prims;  // 3 per primitive, node-contiguous

@@ -83,19 +83,20 @@ struct Bvh2Node {
     int4 child;    // x,y: >=0 inner node; <0: ~first leaf prim; z,w: leaf prim counts
 };
 
-// 8-wide compressed node (Ylitie, Karras, Laine, HPG 2017): 80 B, read as five 128-bit loads.
+// 8-wide compressed node (after Ylitie, Karras, Laine, HPG 2017): 80 B, read as five 128-bit loads.
 // Child boxes are 8-bit offsets on a per-node grid: lo = p + 2^(e-127) * qlo, hi = p + 2^(e-127) * qhi.
-// meta[s]: 0 = empty slot; internal child = 0b001_11sss (24 + s); leaf = unary triangle count in the
-// top 3 bits (001, 011, 111) and the first triangle's offset from tri_base in the low 5 bits.
-// Internal children are stored contiguously from child_base in slot order; slots are assigned so
-// that a ray in direction octant o reaches slot o's child first.
+// Slot s holds an internal child (bit s of imask), a leaf of one or two primitives (bit s of
+// leafmask; of twomask when two) or nothing (the inverted box qlo = 255, qhi = 0, which no ray
+// enters).  Internal children are stored contiguously from child_base, leaf primitives from
+// tri_base, both in slot order; slots are assigned so that a ray in direction octant o reaches
+// slot o's child first.
 struct Bvh8Node {
     float p[3];
     uint8_t e[3];
     uint8_t imask;
     uint32_t child_base;
     uint32_t tri_base;
-    uint8_t meta[8];
+    uint8_t leafmask, twomask, pad[6];
     uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
     uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
 };

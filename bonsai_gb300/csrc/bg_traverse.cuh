@@ -409,8 +409,25 @@ BG_D Ray8 make_ray8(const Ray& r) {
     return q;
 }
 
-// Intersects the 8 child boxes of node `ni`; returns the node's hit mask in the group layout.
-BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_max, uint2* ngroup, uint2* tgroup) {
+// Bit j of x moves to bit j ^ o (o < 8): the ray's octant order of the eight child slots.
+BG_HD uint32_t octant_permute(uint32_t x, uint32_t o) {
+    if (o & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+    if (o & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+    if (o & 4u) x = ((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu);
+    return x;
+}
+
+// The octant permutations of every 8-bit mask, perm[o * 256 + x] = octant_permute(x, o), in shared
+// memory for the persistent traversal (one lookup per node instead of three swap stages).
+BG_D void octant_table_fill(uint8_t* perm) {
+    for (uint32_t i = threadIdx.x; i < 2048u; i += blockDim.x) perm[i] = (uint8_t)octant_permute(i & 255u, i >> 8);
+}
+
+// Intersects the 8 child boxes of node `ni`.  Node group: (child_base, hit internal children in
+// bits 24-31 in this ray's octant order | imask); primitive group: (tri_base, hit leaves (bits 0-7,
+// slot order) | leafmask << 8 | twomask << 16).  perm: the shared octant table, or null.
+BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_max, const uint8_t* perm,
+                         uint2* ngroup, uint2* tgroup) {
     const float4* raw = reinterpret_cast<const float4*>(sc.nodes8 + ni);
     const float4 n0 = __ldg(raw + 0), n1 = __ldg(raw + 1), n2 = __ldg(raw + 2), n3 = __ldg(raw + 3),
                  n4 = __ldg(raw + 4);
@@ -421,7 +438,6 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
     const uint32_t imask = ebits >> 24;
     const V3 aidir = v3(sx * r.idir.x, sy * r.idir.y, sz * r.idir.z);
     const V3 aorig = v3((n0.x - r.o.x) * r.idir.x, (n0.y - r.o.y) * r.idir.y, (n0.z - r.o.z) * r.idir.z);
-    const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
     const uint32_t qlx[2] = {__float_as_uint(n2.x), __float_as_uint(n2.y)};
     const uint32_t qly[2] = {__float_as_uint(n2.z), __float_as_uint(n2.w)};
     const uint32_t qlz[2] = {__float_as_uint(n3.x), __float_as_uint(n3.y)};
@@ -429,14 +445,9 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
     const uint32_t qhy[2] = {__float_as_uint(n4.x), __float_as_uint(n4.y)};
     const uint32_t qhz[2] = {__float_as_uint(n4.z), __float_as_uint(n4.w)};
     const float k = 1.0f + 2.0f * gamma(3.0f);
-    uint32_t hitmask = 0;
+    uint32_t h = 0;  // bit s: the box of slot s is entered within [0, t_max]
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-        const uint32_t m4 = meta[i];
-        const uint32_t is_inner4 = (m4 & (m4 << 1)) & 0x10101010u;
-        const uint32_t inner_mask4 = sign_extend_bytes(is_inner4 << 3);
-        const uint32_t bit_index4 = (m4 ^ (r.octinv4 & inner_mask4)) & 0x1F1F1F1Fu;
-        const uint32_t child_bits4 = (m4 >> 5) & 0x07070707u;
         // near / far planes per axis by the sign of the direction
         const uint32_t nx = r.negx ? qhx[i] : qlx[i], fx = r.negx ? qlx[i] : qhx[i];
         const uint32_t ny = r.negy ? qhy[i] : qly[i], fy = r.negy ? qly[i] : qhy[i];
@@ -451,17 +462,33 @@ BG_D void bvh8_node_hits(const Scene& sc, uint32_t ni, const Ray8& r, float t_ma
             const float tfz = fmaf(byte_as_float(fz, j), aidir.z, aorig.z);
             const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
             const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * k, t_max);
-            if (tn <= tf) {
-                const uint32_t cb = (child_bits4 >> (8 * j)) & 0xFFu;
-                const uint32_t bi = (bit_index4 >> (8 * j)) & 0xFFu;
-                hitmask |= cb << bi;
-            }
+            if (tn <= tf) h |= 1u << (4 * i + j);
         }
     }
+    const uint32_t inner = h & imask;
+    const uint32_t oct = r.octinv4 & 7u;
+    const uint32_t ordered = perm ? (uint32_t)perm[oct * 256u + inner] : octant_permute(inner, oct);
+    const uint32_t lw = __float_as_uint(n1.z) & 0xFFFFu;  // leafmask | twomask << 8
     ngroup->x = __float_as_uint(n1.x);  // child_base
-    ngroup->y = (hitmask & 0xFF000000u) | imask;
+    ngroup->y = (ordered << 24) | imask;
     tgroup->x = __float_as_uint(n1.y);  // tri_base
-    tgroup->y = hitmask & 0x00FFFFFFu;
+    tgroup->y = (h & lw & 0xFFu) | (lw << 8);
+}
+
+// Next primitive of a primitive group (its hit-leaf bits must not be empty): the highest hit slot
+// first; of a leaf with two primitives the second first (its twomask bit then clears, which leaves
+// the offsets of the lower slots unchanged).  Returns the primitive's index in leaf_prims.
+BG_D uint32_t next_leaf_prim(uint2& tg) {
+    const uint32_t j = 31u - __clz(tg.y & 0xFFu);
+    const uint32_t below = (1u << j) - 1u;
+    uint32_t pi = tg.x + __popc((tg.y >> 8) & below) + __popc((tg.y >> 16) & below);
+    if ((tg.y >> (16 + j)) & 1u) {
+        pi += 1u;
+        tg.y &= ~(1u << (16 + j));
+    } else {
+        tg.y &= ~(1u << j);
+    }
+    return pi;
 }
 
 // One ray through the 8-wide layout on one thread (the node-group walk of traverse_queue8 without
@@ -494,20 +521,16 @@ BG_D int bvh8_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) 
                 atomicOr(err, ERR_BAD_NODE);
                 return hit;
             }
-            bvh8_node_hits(sc, child, r8, ray.t_max, &ngroup, &tgroup);
-        } else {
-            tgroup = ngroup;
-            ngroup = make_uint2(0, 0);
+            bvh8_node_hits(sc, child, r8, ray.t_max, nullptr, &ngroup, &tgroup);
         }
-        while (tgroup.y != 0) {
-            const uint32_t bit = 31u - __clz(tgroup.y);
-            tgroup.y &= ~(1u << bit);
-            if (tgroup.x + bit >= sc.ntri + sc.nsph + sc.nquad) {
+        while (tgroup.y & 0xFFu) {
+            const uint32_t pi = next_leaf_prim(tgroup);
+            if (pi >= sc.ntri + sc.nsph + sc.nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
                 continue;
             }
             int prim;
-            if (leaf_prim_hit(sc, tgroup.x + bit, tr, ray, !ANY, &prim)) {
+            if (leaf_prim_hit(sc, pi, tr, ray, !ANY, &prim)) {
                 if (ANY && prim == skip) continue;
                 hit = prim;
                 if (ANY) return hit;
@@ -538,6 +561,9 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         else return sc;
     };
     const uint32_t lane = threadIdx.x & 31u;
+    __shared__ uint8_t octant_perm[2048];
+    octant_table_fill(octant_perm);
+    __syncthreads();
 #if BG_SMEM_STACK
     uint2* stack = smem + threadIdx.x;
     const uint32_t sstride = blockDim.x;
@@ -583,7 +609,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
         if (!busy) continue;
         bool done = false;
         // node step: the next child of the node group (room for two pushes when primitives wait)
-        if (ngroup.y > 0x00FFFFFFu && (tgroup.y == 0 || sp + 2 <= STACK8)) {
+        if (ngroup.y > 0x00FFFFFFu && ((tgroup.y & 0xFFu) == 0 || sp + 2 <= STACK8)) {
             const uint32_t hits = ngroup.y;
             const uint32_t bit = 31u - __clz(hits);
             ngroup.y &= ~(1u << bit);
@@ -606,22 +632,21 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                 tgroup = make_uint2(0, 0);
             } else {
                 uint2 found;
-                bvh8_node_hits(S(), child, r8, ray.t_max, &ngroup, &found);
-                if (found.y != 0) {
-                    if (tgroup.y == 0) tgroup = found;
+                bvh8_node_hits(S(), child, r8, ray.t_max, octant_perm, &ngroup, &found);
+                if (found.y & 0xFFu) {
+                    if ((tgroup.y & 0xFFu) == 0) tgroup = found;
                     else stack[sstride * sp++] = found;  // upper byte 0: a primitive group
                 }
             }
         }
         // primitive step: one primitive of the pending group
-        if (tgroup.y != 0) {
-            const uint32_t bit = 31u - __clz(tgroup.y);
-            tgroup.y &= ~(1u << bit);
-            if (tgroup.x + bit >= S().ntri + S().nsph + S().nquad) {
+        if (tgroup.y & 0xFFu) {
+            const uint32_t pi = next_leaf_prim(tgroup);
+            if (pi >= S().ntri + S().nsph + S().nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
             } else {
                 int prim;
-                if (leaf_prim_hit(S(), tgroup.x + bit, tr, ray, !ANY, &prim) && !(ANY && prim == skip)) {
+                if (leaf_prim_hit(S(), pi, tr, ray, !ANY, &prim) && !(ANY && prim == skip)) {
                     hit = prim;
                     if (ANY) done = true;
                 }
@@ -634,13 +659,13 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                 if (g.y > 0x00FFFFFFu) {
                     ngroup = g;
                     --sp;
-                    break;
+                        break;
                 }
-                if (tgroup.y != 0) break;
+                if (tgroup.y & 0xFFu) break;
                 tgroup = g;
                 --sp;
             }
-            if (ngroup.y <= 0x00FFFFFFu && tgroup.y == 0 && sp == 0) done = true;
+            if (ngroup.y <= 0x00FFFFFFu && (tgroup.y & 0xFFu) == 0 && sp == 0) done = true;
         }
         if (done) {
             src.store(idx, hit, ray.t_max);
