@@ -72,6 +72,8 @@ BG_GUIDE_OUTPUTS = 41
 BG_GUIDE_SAMPLE_FLOATS = 16
 BG_GUIDE_NO_FALLBACK = 1
 BG_GUIDE_NO_TRAIN = 2
+BG_GUIDE_CONTINUATION = 4
+BG_GUIDE_NO_NEE = 8
 
 F3 = C.c_float * 3
 

@@ -627,7 +627,8 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         const uint32_t k = std::min(pass_spp, o->spp - done);
         const bool guided = g->passes_total >= g->o.warmup_passes && !g->fallback;
         const bool record = train && !g->fallback;
-        gw.flags = (record ? bg::GW_RECORD : 0u) | (guided ? bg::GW_GUIDED : 0u);
+        gw.flags = (record ? bg::GW_RECORD : 0u) | (guided ? bg::GW_GUIDED : 0u) |
+                   ((g->o.flags & BG_GUIDE_CONTINUATION) ? bg::GW_CONT : 0u) | ((g->o.flags & BG_GUIDE_NO_NEE) ? 0u : bg::GW_NEE);
         gw.keep_prob = g->keep;
         CK(cudaMemsetAsync(g->ctr, 0, 2 * sizeof(uint32_t), ctx->stream));
         CK(cudaMemsetAsync(g->relvar, 0, 2 * sizeof(double), ctx->stream));

@@ -100,10 +100,12 @@ struct SceneRender {
 //           their next-event estimation with the one-sample mixture c * guide + (1 - c) * BSDF as
 //           the second (direction-sampling) strategy of estimate_direct, and the BSDF-sampled
 //           continuation.
-enum : uint32_t { GW_RECORD = 1u, GW_GUIDED = 2u };
+//   GW_CONT: the continuation is drawn from the same mixture (one-sample MIS with the BSDF);
+//   GW_NEE: the mixture is estimate_direct's second strategy (otherwise that stays a BSDF sample).
+enum : uint32_t { GW_RECORD = 1u, GW_GUIDED = 2u, GW_CONT = 4u, GW_NEE = 8u };
 constexpr int GUIDE_MAXREC = 6;      // training records kept per path
 constexpr int GUIDE_REC_F4 = 5;      // float4 per record
-constexpr uint32_t DIM_GUIDE0 = 4096;  // guided sampling uniforms: 4 per bounce from here
+constexpr uint32_t DIM_GUIDE0 = 4096;  // guided sampling uniforms: 8 per bounce from here
 
 struct GuideWave {
     uint32_t flags;

@@ -279,6 +279,8 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     if (su) strat_apply(su, nee, u);  // the stratified sampler's values, prefetched by the shade thread
     // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
     state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
+    // the mixture in estimate_direct's second strategy (GW_NEE) and in the continuation (GW_CONT)
+    const MixView* nmix = GUIDABLE && mix && (gw.flags & GW_NEE) ? mix : nullptr;
     if (nee) {
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
         float count = (float)sc.nlights;
@@ -287,9 +289,9 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         // pdf of the second strategy for a direction
         auto strategy_pdf = [&](V3 w) {
             float pb = bsdf.pdf<false>(it.wo, w, flags);
-            if (!mix) return pb;
-            const float c = mix->c();
-            return c * mix->pdf(w) + (1.0f - c) * pb;
+            if (!nmix) return pb;
+            const float c = nmix->c();
+            return c * nmix->pdf(w) + (1.0f - c) * pb;
         };
         LightSample ls = INF ? light_sample_any<false, SHL>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1])
                              : light_sample<false, false>(sc, light_prim, it, u[BD_ULIGHT], u[BD_ULIGHT + 1]);
@@ -310,15 +312,15 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         V3 wi;
         RGB f;
         float spdf;
-        if (GUIDABLE && mix && ug[0] < mix->c()) {
-            wi = mix->sample(ug[1], ug[2], ug[3]);
+        if (nmix && ug[0] < nmix->c()) {
+            wi = nmix->sample(ug[1], ug[2], ug[3]);
             f = bsdf.f<false>(it.wo, wi, flags) * abs_dot(wi, it.ns);
             spdf = strategy_pdf(wi);
         } else {
             BxSample bs = bsdf.sample<false>(it.wo, u[BD_USCAT], u[BD_USCAT + 1], flags);
             wi = bs.wi;
             f = bs.f * abs_dot(bs.wi, it.ns);
-            spdf = mix ? (bs.pdf > 0.0f ? strategy_pdf(bs.wi) : 0.0f) : bs.pdf;
+            spdf = nmix ? (bs.pdf > 0.0f ? strategy_pdf(bs.wi) : 0.0f) : bs.pdf;
         }
         if (!is_black(f) && spdf > 0.0f) {
             float t_light = 0.0f;
@@ -349,7 +351,27 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
         state |= ST_PENDING;
     }
     V3 wo = -ray.d;
-    BxSample bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+    BxSample bs;
+    float p_b;  // BSDF pdf of the continuation (the training record's)
+    if (GUIDABLE && mix && (gw.flags & GW_CONT) && bsdf.num_components(BSDF_SPECULAR) == 0) {
+        // one-sample MIS: with probability c the direction comes from the guide, else from the
+        // BSDF; either way the throughput divides by the mixture pdf c q(wi) + (1 - c) p_bsdf(wi)
+        const float c = mix->c();
+        const bool from_guide = ug[4] < c;
+        if (from_guide) {
+            bs.wi = mix->sample(ug[5], ug[6], ug[7]);
+            bs.f = bsdf.f<false>(wo, bs.wi, BSDF_ALL);
+            p_b = bsdf.pdf<false>(wo, bs.wi, BSDF_ALL);
+            bs.stype = BSDF_REFLECTION | BSDF_GLOSSY;  // guidable BSDFs have no specular lobe
+        } else {
+            bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+            p_b = bs.pdf;
+        }
+        bs.pdf = from_guide || p_b > 0.0f ? c * mix->pdf(bs.wi) + (1.0f - c) * p_b : 0.0f;
+    } else {
+        bs = bsdf.sample<false>(wo, u[BD_BSDF], u[BD_BSDF + 1], BSDF_ALL);
+        p_b = bs.pdf;
+    }
     if (is_black(bs.f) || bs.pdf == 0.0f) {
         out.finished = true;
         return;
@@ -375,7 +397,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, bs.pdf, beta0);
+    if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, p_b, beta0);
     out.cont = true;
 }
 
@@ -509,9 +531,9 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
 }
 
 // Guided vertices of one material class, after the network has evaluated them: scatter_vertex with
-// the network's mixture in the second direct-light strategy.  Uniforms: the bounce's dims (shared
-// with the unguided path) plus four guide dims at DIM_GUIDE0 + 4 bounce (mixture choice, lobe,
-// cos theta, phi).
+// the network's mixture in the second direct-light strategy and / or the continuation.  Uniforms:
+// the bounce's dims (shared with the unguided path) plus eight guide dims at DIM_GUIDE0 + 8 bounce
+// (next-event and continuation: mixture choice, lobe, cos theta, phi).
 // FULL: textures (matte, plastic) and the infinite light's next-event estimation compiled in (the
 // variants launched for scenes that have either).
 template <int CLS, bool FULL = false>
@@ -548,8 +570,10 @@ __global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams r
             }
             if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
                 const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
-                float ug[4];
-                Rng{wb.pixel[slot], wb.sample[slot], rp.seed}.block(DIM_GUIDE0 + 4 * bounce, ug);
+                float ug[8];
+                const Rng grng{wb.pixel[slot], wb.sample[slot], rp.seed};
+                grng.block(DIM_GUIDE0 + 8 * bounce, ug);
+                grng.block(DIM_GUIDE0 + 8 * bounce + 4, ug + 4);
                 scatter_vertex<CLS, FULL && CLS <= 1, FULL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state,
                                                             &mix, ug, (gw.flags & GW_RECORD) != 0, vo, su);
                 finished = vo.finished;

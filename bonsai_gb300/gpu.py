@@ -273,12 +273,13 @@ class Guide:
 
     def __init__(self, ctx: Context, learning_rate: float = 1e-3, batch_size: int = 16384,
                  samples_per_pass: int = 1 << 18, warmup_passes: int = 4, alpha: float = 0.5, seed: int = 0,
-                 no_fallback: bool = False, no_train: bool = False, pass_paths: int = 1 << 22, epochs: int = 1):
+                 no_fallback: bool = False, no_train: bool = False, pass_paths: int = 1 << 22, epochs: int = 1,
+                 flags: int = 0):
         self.ctx = ctx
         o = A.bg_guide_opts()
         o.learning_rate, o.beta1, o.beta2, o.eps, o.alpha = learning_rate, 0.9, 0.999, 1e-8, alpha
         o.batch_size, o.samples_per_pass, o.warmup_passes = batch_size, samples_per_pass, warmup_passes
-        o.flags = (A.BG_GUIDE_NO_FALLBACK if no_fallback else 0) | (A.BG_GUIDE_NO_TRAIN if no_train else 0)
+        o.flags = (A.BG_GUIDE_NO_FALLBACK if no_fallback else 0) | (A.BG_GUIDE_NO_TRAIN if no_train else 0) | flags
         o.seed = seed
         o.pass_paths, o.epochs = pass_paths, epochs
         self.opts = o

@@ -479,6 +479,8 @@ typedef struct bg_guide_opts {
 
 #define BG_GUIDE_NO_FALLBACK 1u /* keep guiding even when its variance estimate is not lower  */
 #define BG_GUIDE_NO_TRAIN 2u    /* render with the current weights; no online training         */
+#define BG_GUIDE_CONTINUATION 4u /* draw the path's continuation from the mixture as well        */
+#define BG_GUIDE_NO_NEE 8u      /* keep estimate_direct's second strategy a BSDF sample        */
 
 typedef struct bg_guide_stats {
     uint32_t passes;         /* passes rendered by this call                                   */
