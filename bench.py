@@ -692,7 +692,7 @@ def run_guiding(args):
         "config": {"workload": f"slit room {W}x{H}, max depth {sd.max_depth}, {sd.ntri} triangles, {sd.nsph} "
                                f"spheres, PBRT estimator; reference {args.ref_spp} spp plain",
                    "relmse": "mean (x - ref)^2 / (ref^2 + 0.01) minus the reference's own variance term",
-                   "guide": f"78 -> 4x64 -> 41 BF16 MLP, 8 vMF lobes, 2^18 samples / pass of {args.pass_paths} "
+                   "guide": f"78 -> 4x64 -> 2 x 41 BF16 MLP (continuation and next-event heads of 8 vMF lobes), 2^18 samples / pass of {args.pass_paths} "
                             f"paths, {args.epochs} epochs / pass, Adam lr 1e-3, batch 16384, "
                             f"{args.guide_warmup} warm-up passes"},
         "plain": {"time_to_target_s": t_plain, "extrapolated": ext_p, "msamples_per_s": plain_rate,
@@ -772,13 +772,14 @@ def _random_guide_data(n: int, seed: int):
     s[:, 9:12] = unit(n)
     s[:, 12] = rng.exponential(0.3, n)
     s[:, 13] = rng.lognormal(0.0, 1.0, n)
+    s[:, 14] = np.where(rng.random(n) < 0.9, 0.0, rng.lognormal(0.0, 1.0, n))
     return s
 
 
 def run_guide_mlp(args):
     """The guiding network alone: device time of a training step (forward + backward + Adam on one
     16384-sample batch) and of inference over 2^20 queries.  FLOPs are the network's algorithmic
-    count: 19,904 multiply-adds per inference (78 -> 4 x 64 -> 41) = 39,808 FLOP, 3x that per
+    count: 22,528 multiply-adds per inference (78 -> 4 x 64 -> 2 x 41) = 45,056 FLOP, 3x that per
     training sample; the denominator is the measured cuBLAS BF16 peak."""
     from bonsai_gb300 import gpu as G
     ctx = G.Context(0)
@@ -790,7 +791,7 @@ def run_guide_mlp(args):
     clk = clocks.stop()
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
-    fl_inf = 2 * 19904
+    fl_inf = 2 * (78 * 64 + 3 * 64 * 64 + 64 * 82)
     train_tf = 3 * fl_inf * 16384 / (step_ms / 1e3) / 1e12
     infer_tf = fl_inf * len(data) / (infer_ms / 1e3) / 1e12
     print(json.dumps({

@@ -66,13 +66,13 @@ BG_NOALLOC_MAX_PIXELS = 512 * 512
 BG_NOALLOC_WAVE_PATHS = 65536
 BG_NOALLOC_SCRATCH_BYTES = 29099008
 
-BG_GUIDE_PARAMS = 24320
+BG_GUIDE_PARAMS = 28160
 BG_GUIDE_QUERY_FLOATS = 9
-BG_GUIDE_OUTPUTS = 41
+BG_GUIDE_OUTPUTS = 82
 BG_GUIDE_SAMPLE_FLOATS = 16
 BG_GUIDE_NO_FALLBACK = 1
 BG_GUIDE_NO_TRAIN = 2
-BG_GUIDE_CONTINUATION = 4
+BG_GUIDE_NO_CONTINUATION = 4
 BG_GUIDE_NO_NEE = 8
 
 F3 = C.c_float * 3

@@ -10,10 +10,12 @@
 //   k_guide_adam   Adam on the FP32 master weights; rewrites the BF16 core-matrix image.
 //
 // Shared-memory tiles (no swizzle, core matrices of 8 rows x 16 B, see bg_umma.cuh):
-//   weights  W_l[rows][80]  8-row groups 1280 B apart      (48,640 B for all five layers)
+//   weights  W_l[rows][80]  8-row groups 1280 B apart      (56,320 B for all five layers)
 //   act      A[128][80]     8-row groups 1280 B apart      (20,480 B per layer)
-//   dZ       dZ[128][128]   8-row groups 2048 B apart; columns 64..127 stay zero so that
-//            dZ^T can feed an M = 128 MMA for layers with 64 (or 41) output rows.
+//   dZ       dZ[128][128]   8-row groups 2048 B apart; dZ^T feeds an M = 128 MMA for layers with
+//            64 (or 96) output rows: the dW rows past a layer's outputs are computed and dropped.
+// TMEM columns: forward accumulator 0..95; backward dW 0..79 (the forward accumulator is free by
+// then) and dX 128..207 (training allocates 256 columns, inference 128).
 #include <cuda_bf16.h>
 
 #include "bg_device.h"
@@ -33,9 +35,11 @@ constexpr uint32_t ACT_BYTES = 128 * GUIDE_K * 2;         // 20,480
 constexpr uint32_t ACT_RS = GUIDE_ROWGROUP_BYTES;         // 1280
 constexpr uint32_t DZ_RS = 2048;                          // 16 column groups per 8-row group
 constexpr uint32_t DZ_BYTES = 16 * DZ_RS;                 // 32,768
-constexpr uint32_t INFER_SMEM = GUIDE_WPACK_BYTES + 2 * ACT_BYTES;                    // 89,600
-constexpr uint32_t TRAIN_SMEM = GUIDE_WPACK_BYTES + 5 * ACT_BYTES + DZ_BYTES;          // 183,808
-constexpr uint32_t TM_FWD = 0, TM_DX = 64, TM_DW = 160, TM_COLS_TRAIN = 256, TM_COLS_INFER = 64;
+constexpr uint32_t INFER_SMEM = GUIDE_WPACK_BYTES + 2 * ACT_BYTES;                    // 97,280
+constexpr uint32_t TRAIN_SMEM = GUIDE_WPACK_BYTES + 5 * ACT_BYTES + DZ_BYTES;          // 191,488
+constexpr uint32_t TM_FWD = 0, TM_DW = 0, TM_DX = 128, TM_COLS_TRAIN = 256, TM_COLS_INFER = 128;
+static_assert(GUIDE_OUT_ROWS <= (int)TM_DX && TM_DX + GUIDE_K <= TM_COLS_TRAIN, "TMEM column plan");
+static_assert(GUIDE_OUT_ROWS <= (int)TM_COLS_INFER && GUIDE_HID <= (int)TM_COLS_INFER, "TMEM column plan");
 
 BG_D uint32_t pack_bf16(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -113,17 +117,25 @@ BG_D void bail_out(uint64_t* bar, uint32_t parity, uint32_t* err, uint32_t tmem,
 }  // namespace
 
 // ---------------------------------------------------------------- inference
-// MIX = false: the 41 raw outputs per query (GUIDE_RAW_STRIDE floats); MIX = true: the parsed
-// mixture record (GUIDE_MIX_STRIDE floats) that the render kernels sample.
+// MIX = false: the 82 raw outputs per query (GUIDE_RAW_STRIDE floats); MIX = true: the parsed
+// mixture records of both heads (GUIDE_MIX_STRIDE floats) that the render kernels sample.
+// Queries come in `nranges` ranges: range r holds min(counts[r], stride) queries from r * stride
+// (counts null: one range of `stride` queries); outputs use the same indices.
 template <bool MIX>
 __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, const float4* query,
-                                                        const uint32_t* count, uint32_t max_n, float* raw,
-                                                        uint32_t* err) {
+                                                        const uint32_t* counts, uint32_t nranges, uint32_t stride,
+                                                        float* raw, uint32_t* err) {
     extern __shared__ __align__(128) uint8_t sm[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tslot;
-    const uint32_t n = count ? min(*count, max_n) : max_n;
-    const uint32_t ntiles = (n + 127) / 128;
+    uint32_t rn[GUIDE_MAX_RANGES], rt[GUIDE_MAX_RANGES + 1];  // queries and first tile of each range
+    rt[0] = 0;
+#pragma unroll
+    for (int r = 0; r < GUIDE_MAX_RANGES; ++r) {
+        rn[r] = (uint32_t)r < nranges ? (counts ? min(counts[r], stride) : stride) : 0u;
+        rt[r + 1] = rt[r] + (rn[r] + 127) / 128;
+    }
+    const uint32_t ntiles = rt[GUIDE_MAX_RANGES];
     if (blockIdx.x >= ntiles) return;
     const long long wait_limit = g_guide_wait_limit;
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -141,9 +153,15 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
     const uint32_t w_addr = smem_addr(wsm);
     uint32_t phase = 0;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t qi = tile * 128 + tid;
+        uint32_t r = 0;
+#pragma unroll
+        for (int j = 1; j < GUIDE_MAX_RANGES; ++j)
+            if (tile >= rt[j]) r = j;
+        const uint32_t local = (tile - rt[r]) * 128 + tid;
+        const bool valid = local < rn[r];
+        const uint32_t qi = r * stride + local;
         float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
-        if (qi < n) {
+        if (valid) {
             float4 a = query[3 * (size_t)qi], b = query[3 * (size_t)qi + 1], c = query[3 * (size_t)qi + 2];
             q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w;
             q[8] = c.x;
@@ -165,14 +183,17 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
                 float v[GUIDE_OUT_ROWS];
 #pragma unroll
                 for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, v + c);
-                if (qi < n) {
+                if (valid) {
                     if (MIX) {
-                        float rec[GUIDE_MIX_STRIDE];
-                        guide_write_mixture(v, rec);
-                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE);
 #pragma unroll
-                        for (int j = 0; j < GUIDE_MIX_STRIDE / 4; ++j)
-                            o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
+                        for (int h = 0; h < GUIDE_HEADS; ++h) {
+                            float rec[GUIDE_MIX_HEAD];
+                            guide_write_mixture(v + GUIDE_HEAD_OUT * h, rec);
+                            float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
+#pragma unroll
+                            for (int j = 0; j < GUIDE_MIX_HEAD / 4; ++j)
+                                o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
+                        }
                     } else {
                         float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE);
 #pragma unroll
@@ -212,7 +233,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     const uint32_t si = blockIdx.x * 128 + tid;
     float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
     V3 wi = v3(0.0f, 0.0f, 1.0f);
-    float p_b = 0.0f, wn = 0.0f;
+    float p_b = 0.0f, wn0 = 0.0f, wn1 = 0.0f;  // normalised weights of the two heads
     if (si < a.n) {
         const float4* s = a.samples + (size_t)GUIDE_SAMPLE_F4 * a.order.at(a.base + si);
         float4 f0 = s[0], f1 = s[1], f2 = s[2], f3 = s[3];
@@ -220,8 +241,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         q[8] = f2.x;
         wi = v3(f2.y, f2.z, f2.w);
         p_b = f3.x;
-        const float wsum = *a.wsum;
-        wn = (wsum > 0.0f && f3.y > 0.0f && isfinite(f3.y)) ? f3.y / wsum : 0.0f;
+        const float ws0 = a.wsum[0], ws1 = a.wsum[1];
+        wn0 = (ws0 > 0.0f && f3.y > 0.0f && isfinite(f3.y)) ? f3.y / ws0 : 0.0f;
+        wn1 = (ws1 > 0.0f && f3.z > 0.0f && isfinite(f3.z)) ? f3.z / ws1 : 0.0f;
     }
     encode_row(act, tid, q);
     fence_async_smem();
@@ -247,14 +269,18 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
             float raw[GUIDE_RAW_STRIDE], g[GUIDE_RAW_STRIDE];
 #pragma unroll
             for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, raw + c);
-            float loss = guide_loss_grad(raw, wi, p_b, wn, a.alpha, g);
-            // loss gradient -> dZ4 (columns 0..47; 48..63 zero)
+            // both heads' losses on the same direction, each with its own target weight
+            float loss = guide_loss_grad(raw, wi, p_b, wn0, a.alpha, g) +
+                         guide_loss_grad(raw + GUIDE_HEAD_OUT, wi, p_b, wn1, a.alpha, g + GUIDE_HEAD_OUT);
+#pragma unroll
+            for (int j = GUIDE_OUT; j < GUIDE_RAW_STRIDE; ++j) g[j] = 0.0f;
+            // loss gradient -> dZ4 (columns 0..81; 82..127 zero)
 #pragma unroll
             for (int c = 0; c < GUIDE_OUT_ROWS; c += 8) store_row8(dz, DZ_RS, tid, c, g + c);
             float zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            store_row8(dz, DZ_RS, tid, 48, zero8);
-            store_row8(dz, DZ_RS, tid, 56, zero8);
-            float cnt = wn > 0.0f ? 1.0f : 0.0f;
+#pragma unroll
+            for (int c = GUIDE_OUT_ROWS; c < 128; c += 8) store_row8(dz, DZ_RS, tid, c, zero8);
+            float cnt = wn0 > 0.0f || wn1 > 0.0f ? 1.0f : 0.0f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 loss += __shfl_xor_sync(0xffffffffu, loss, o);
@@ -274,7 +300,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     for (int l = GUIDE_LAYERS - 1; l >= 0; --l) {
         const uint32_t a_l = act_addr + l * ACT_BYTES;
         const uint32_t w_l = w_addr + guide_wpack_off(l);
-        const int kout = guide_rows(l);  // 48 or 64 dZ columns feed the dX MMA
+        const int kout = guide_rows(l);  // 96 or 64 dZ columns feed the dX MMA
         if (tid == 0) {
             if (l > 0) {
                 // dX = dZ (128 x kout, K-major) * W_l (kout x 80 read MN-major: N = 80 input columns)
@@ -366,22 +392,29 @@ __global__ void k_guide_pack(const float* p, uint8_t* wpack) {
     if (i < GUIDE_PARAMS) pack_param(wpack, i, p[i]);
 }
 
-// Sum of the training weights of each batch of the sample pool.
+// Sums of the two heads' training weights of each batch of the sample pool (wsum[2b], wsum[2b + 1]).
 __global__ void k_guide_wsum(const float4* samples, PoolOrder order, uint32_t batch, float* wsum) {
-    __shared__ float red[256];
+    __shared__ float2 red[256];
     const uint32_t b0 = blockIdx.x * batch, b1 = min(order.n_total, b0 + batch);
-    float s = 0.0f;
+    float2 s = make_float2(0.0f, 0.0f);
     for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        float w = samples[(size_t)GUIDE_SAMPLE_F4 * order.at(i) + 3].y;
-        if (w > 0.0f && isfinite(w)) s += w;
+        const float4 f3 = samples[(size_t)GUIDE_SAMPLE_F4 * order.at(i) + 3];
+        if (f3.y > 0.0f && isfinite(f3.y)) s.x += f3.y;
+        if (f3.z > 0.0f && isfinite(f3.z)) s.y += f3.z;
     }
     red[threadIdx.x] = s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        if ((int)threadIdx.x < o) {
+            red[threadIdx.x].x += red[threadIdx.x + o].x;
+            red[threadIdx.x].y += red[threadIdx.x + o].y;
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) wsum[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) {
+        wsum[2 * blockIdx.x] = red[0].x;
+        wsum[2 * blockIdx.x + 1] = red[0].y;
+    }
 }
 
 __global__ void k_pass_relvar(const double* sum, const uint32_t* count, const float* pass, uint32_t npix, uint32_t k,
@@ -411,21 +444,21 @@ __global__ void k_pass_relvar(const double* sum, const uint32_t* count, const fl
     }
 }
 
-// Test entry: mixture parsing, sampling, pdf and loss gradient for given raw outputs.
+// Test entry: mixture parsing, sampling, pdf and loss gradient for given raw outputs of one head.
 // out (48 per item): sampled wi.xyz, pdf(sampled), pdf(w), c, loss, -, grad[40..] -> out[8..48]
 __global__ void k_guide_mixture_eval(const float* raw, const float* u, const float* w, const float* pb, uint32_t n,
                                      float alpha, float* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float r[GUIDE_RAW_STRIDE];
-    for (int j = 0; j < GUIDE_RAW_STRIDE; ++j) r[j] = j < GUIDE_OUT ? raw[(size_t)GUIDE_OUT * i + j] : 0.0f;
+    float r[GUIDE_HEAD_OUT];
+    for (int j = 0; j < GUIDE_HEAD_OUT; ++j) r[j] = raw[(size_t)GUIDE_HEAD_OUT * i + j];
     // the render path: stored mixture record read through MixView
-    float rec[GUIDE_MIX_STRIDE];
+    float rec[GUIDE_MIX_HEAD];
     guide_write_mixture(r, rec);
     const MixView m{rec};
     V3 ws = m.sample(u[3 * i], u[3 * i + 1], u[3 * i + 2]);
     V3 wq = v3(w[3 * i], w[3 * i + 1], w[3 * i + 2]);
-    float g[GUIDE_RAW_STRIDE];
+    float g[GUIDE_HEAD_OUT];
     float loss = guide_loss_grad(r, wq, pb[i], 1.0f, alpha, g);
     float* o = out + (size_t)48 * i;
     o[0] = ws.x;
@@ -451,14 +484,15 @@ void guide_set_smem_limits() {
     done = true;
 }
 
-void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* out,
-                        bool mixture, uint32_t* err, int sms, cudaStream_t s) {
+void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* counts, uint32_t nranges,
+                        uint32_t stride, float* out, bool mixture, uint32_t* err, int sms, cudaStream_t s) {
+    if (nranges == 0 || nranges > (uint32_t)GUIDE_MAX_RANGES) return;
     guide_set_smem_limits();
-    uint32_t tiles = (max_n + 127) / 128;
-    uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms * 2);
+    uint64_t tiles = (uint64_t)nranges * ((stride + 127) / 128);
+    uint32_t grid = (uint32_t)std::min<uint64_t>(tiles, (uint64_t)sms * 2);
     if (grid == 0) return;
-    if (mixture) k_guide_infer<true><<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, out, err);
-    else k_guide_infer<false><<<grid, 128, INFER_SMEM, s>>>(wpack, query, count, max_n, out, err);
+    if (mixture) k_guide_infer<true><<<grid, 128, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
+    else k_guide_infer<false><<<grid, 128, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
 }
 
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {

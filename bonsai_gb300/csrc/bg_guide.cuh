@@ -3,12 +3,15 @@
 // PathIntegrator samples the BSDF only); the estimator stays unbiased because every guided
 // direction is weighted by the pdf of the one-sample mixture it was drawn from.
 //
-// Network: 78 inputs -> 4 hidden layers of 64 (ReLU) -> 41 outputs.
+// Network: 78 inputs -> 4 hidden layers of 64 (ReLU) -> 2 heads of 41 outputs.
 //   inputs  x[0..71]  position: each scene-normalised coordinate p in [0,1] through 12 octaves,
 //                     x[24c + 2k] = sin(pi 2^k p_c), x[24c + 2k + 1] = cos(pi 2^k p_c)
 //           x[72..74] shading normal, x[75..77] outgoing direction wo
-//   outputs raw[5i .. 5i+2] lobe i mean direction (normalised), raw[5i+3] log kappa,
-//           raw[5i+4] lobe weight logit (8 lobes), raw[40] logit of the guide selection probability.
+//   outputs per head (head h at raw[41 h ..]): raw[5i .. 5i+2] lobe i mean direction
+//           (normalised), raw[5i+3] log kappa, raw[5i+4] lobe weight logit (8 lobes), raw[40]
+//           logit of the guide selection probability.  Head 0 proposes continuations (trained on
+//           the indirect radiance along a direction), head 1 next-event directions (trained on
+//           the emission a direction reaches).
 // The parameter layout (biases folded into a constant-1 input column) is in bg_guide_layout.h.
 #pragma once
 #include <cuda_bf16.h>
@@ -120,7 +123,8 @@ BG_D V3 guide_sample(const VmfMix& m, float u0, float u1, float u2) {
     return vmf_sample_lobe(mu, kappa, u1, u2);
 }
 
-// Parsed mixture as stored by the render-side inference (GUIDE_MIX_STRIDE floats).
+// Parsed mixture of one head (41 raw outputs) as stored by the render-side inference
+// (GUIDE_MIX_HEAD floats).
 BG_D void guide_write_mixture(const float* raw, float* out) {
     const VmfMix m = guide_parse(raw);
 #pragma unroll
@@ -136,7 +140,7 @@ BG_D void guide_write_mixture(const float* raw, float* out) {
     out[49] = out[50] = out[51] = 0.0f;
 }
 
-// Read-only view of a stored mixture: lobes are loaded as they are needed, so a kernel does not
+// Read-only view of one head's stored mixture: lobes are loaded as they are needed, so a kernel does not
 // keep the whole mixture in registers.  Same arithmetic as guide_pdf / guide_sample.
 struct MixView {
     const float* m;
@@ -171,12 +175,12 @@ struct MixView {
 //   loss = -wn [alpha log(c q(wi) + (1 - c) p_b) + (1 - alpha) log q(wi)]
 // a Monte Carlo estimate of the KL divergence from the normalised product f Li cos to the
 // one-sample mixture (first term) and to the guide alone (second term), up to a constant.
-// Writes d loss / d raw (41 values, raw[41..47] = 0) and returns the loss.
+// `raw` is one head's 41 outputs; writes d loss / d raw (41 values) and returns the loss.
 constexpr float GUIDE_ALPHA = 0.5f;
 
 BG_D float guide_loss_grad(const float* raw, V3 wi, float p_b, float wn, float alpha, float* g) {
 #pragma unroll
-    for (int j = 0; j < GUIDE_RAW_STRIDE; ++j) g[j] = 0.0f;
+    for (int j = 0; j < GUIDE_HEAD_OUT; ++j) g[j] = 0.0f;
     if (!(wn > 0.0f)) return 0.0f;
     float mx = -FLT_BIG;
 #pragma unroll

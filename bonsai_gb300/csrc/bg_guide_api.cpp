@@ -37,14 +37,13 @@ struct bg_guide {
     uint32_t* ctr = nullptr;    // [0] positive-weight records, [1] pool appends
     float* stats = nullptr;     // [0] loss, [1] samples with weight > 0
     double* relvar = nullptr;   // [0] sum of relative squared deviations, [1] terms
-    float* wsum = nullptr;      // per batch of the pool
+    float* wsum = nullptr;      // two per batch of the pool (one per head)
     float4* pool = nullptr;
     uint32_t pool_cap = 0;
     float* pass = nullptr;      // this pass's sample per pixel
     size_t pass_pix = 0;
     float4* rec = nullptr;
     float4* query = nullptr;
-    uint32_t* gslot = nullptr;
     float* raw = nullptr;
     uint32_t wcap = 0;
     std::vector<void*> allocs, wave_allocs, pass_allocs;
@@ -156,11 +155,10 @@ bg_status ensure_guide_wave(bg_guide* g, uint32_t cap) {
     if ((st = dalloc(ctx, (size_t)bg::GUIDE_MAXREC * bg::GUIDE_REC_F4 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK)
         return st;
     g->rec = (float4*)p;
-    if ((st = dalloc(ctx, 3 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK) return st;
+    // queries and mixtures of the three guidable material classes, at class * cap + queue position
+    if ((st = dalloc(ctx, 3 * 3 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK) return st;
     g->query = (float4*)p;
-    if ((st = dalloc(ctx, n * sizeof(uint32_t), &p, &g->wave_allocs)) != BG_OK) return st;
-    g->gslot = (uint32_t*)p;
-    if ((st = dalloc(ctx, n * bg::GUIDE_MIX_STRIDE * sizeof(float), &p, &g->wave_allocs)) != BG_OK) return st;
+    if ((st = dalloc(ctx, 3 * n * bg::GUIDE_MIX_STRIDE * sizeof(float), &p, &g->wave_allocs)) != BG_OK) return st;
     g->raw = (float*)p;
     g->wcap = cap;
     return BG_OK;
@@ -229,7 +227,7 @@ int train_batches(bg_guide* g, const float4* samples, uint32_t n, uint32_t epoch
             a.order = order;
             a.base = b * B;
             a.n = std::min(B, n - b * B);
-            a.wsum = g->wsum + b;
+            a.wsum = g->wsum + 2 * b;
             a.alpha = g->o.alpha;
             a.grad = g->grad;
             a.stats = g->stats;
@@ -298,7 +296,7 @@ bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out
     if ((st = dalloc(ctx, (size_t)g->pool_cap * bg::GUIDE_SAMPLE_F4 * sizeof(float4), &p, &g->allocs)) != BG_OK)
         return bail(st);
     g->pool = (float4*)p;
-    if ((st = dalloc(ctx, ((size_t)g->pool_cap / 128 + 1) * sizeof(float), &p, &g->allocs)) != BG_OK) return bail(st);
+    if ((st = dalloc(ctx, ((size_t)g->pool_cap / 128 + 1) * 2 * sizeof(float), &p, &g->allocs)) != BG_OK) return bail(st);
     g->wsum = (float*)p;
     for (auto& e : g->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(ctx, BG_ERR_CUDA, "cudaEventCreate"));
@@ -368,7 +366,7 @@ bg_status bg_guide_forward(bg_guide* g, const float* queries, size_t n, float* o
     std::vector<float> raw;
     if (st == BG_OK) {
         cudaMemcpyAsync(dq, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
-        bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)n, (float*)dr, false, ctx->d_err,
+        bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, 1, (uint32_t)n, (float*)dr, false, ctx->d_err,
                                ctx->shape.sms, ctx->stream);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_infer");
@@ -517,7 +515,7 @@ bg_status bg_guide_time(bg_guide* g, const float* samples, size_t n, const float
             bg::launch_guide_adam(g->params, g->m, g->v, g->grad, g->wpack, g->step, h, ctx->stream);
         };
         auto infer = [&]() {
-            bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, (uint32_t)nq, (float*)dout, true, ctx->d_err,
+            bg::launch_guide_infer(g->wpack, (const float4*)dq, nullptr, 1, (uint32_t)nq, (float*)dout, true, ctx->d_err,
                                    ctx->shape.sms, ctx->stream);
         };
         step();
@@ -552,13 +550,13 @@ bg_status bg_guide_mixture_eval(bg_guide* g, const float* raw, const float* u, c
     CK(cudaSetDevice(ctx->device));
     std::vector<void*> tmp;
     void *dr, *du, *dw, *dp, *dout;
-    bg_status st = dalloc(ctx, n * bg::GUIDE_OUT * sizeof(float), &dr, &tmp);
+    bg_status st = dalloc(ctx, n * bg::GUIDE_HEAD_OUT * sizeof(float), &dr, &tmp);
     if (st == BG_OK) st = dalloc(ctx, n * 3 * sizeof(float), &du, &tmp);
     if (st == BG_OK) st = dalloc(ctx, n * 3 * sizeof(float), &dw, &tmp);
     if (st == BG_OK) st = dalloc(ctx, n * sizeof(float), &dp, &tmp);
     if (st == BG_OK) st = dalloc(ctx, n * 48 * sizeof(float), &dout, &tmp);
     if (st == BG_OK) {
-        cudaMemcpyAsync(dr, raw, n * bg::GUIDE_OUT * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(dr, raw, n * bg::GUIDE_HEAD_OUT * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
         cudaMemcpyAsync(du, u, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
         cudaMemcpyAsync(dw, w, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
         cudaMemcpyAsync(dp, p_bsdf, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
@@ -610,7 +608,6 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
     gw.binv = make_float4(inv[0], inv[1], inv[2], 0.0f);
     gw.rec = g->rec;
     gw.query = g->query;
-    gw.gslot = g->gslot;
     gw.raw = g->raw;
     gw.pool = g->pool;
     gw.ctr = g->ctr;
@@ -628,7 +625,7 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         const bool guided = g->passes_total >= g->o.warmup_passes && !g->fallback;
         const bool record = train && !g->fallback;
         gw.flags = (record ? bg::GW_RECORD : 0u) | (guided ? bg::GW_GUIDED : 0u) |
-                   ((g->o.flags & BG_GUIDE_CONTINUATION) ? bg::GW_CONT : 0u) | ((g->o.flags & BG_GUIDE_NO_NEE) ? 0u : bg::GW_NEE);
+                   ((g->o.flags & BG_GUIDE_NO_CONTINUATION) ? 0u : bg::GW_CONT) | ((g->o.flags & BG_GUIDE_NO_NEE) ? 0u : bg::GW_NEE);
         gw.keep_prob = g->keep;
         CK(cudaMemsetAsync(g->ctr, 0, 2 * sizeof(uint32_t), ctx->stream));
         CK(cudaMemsetAsync(g->relvar, 0, 2 * sizeof(double), ctx->stream));

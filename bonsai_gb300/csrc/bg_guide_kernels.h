@@ -29,7 +29,7 @@ struct GuideTrainArgs {
     PoolOrder order;
     uint32_t base;           // first batch position
     uint32_t n;              // samples in this batch (rows past n are zero-weight)
-    const float* wsum;       // sum of the batch's weights (device scalar)
+    const float* wsum;       // sums of the batch's weights of head 0 and head 1 (two device floats)
     float alpha;             // loss blend, see guide_loss_grad
     float* grad;             // FP32 gradient accumulator (GUIDE_PARAMS)
     float* stats;            // [0] += loss, [1] += samples with weight > 0
@@ -41,15 +41,19 @@ struct GuideAdam {
     float lr, beta1, beta2, eps;
 };
 
-// Forward pass over the queries; count (device, optional) caps max_n.  out: raw outputs
-// (GUIDE_RAW_STRIDE floats per query) or, with mixture, parsed mixture records (GUIDE_MIX_STRIDE).
-void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* count, uint32_t max_n, float* out,
-                        bool mixture, uint32_t* err, int sms, cudaStream_t s);
+// Forward pass over nranges (<= GUIDE_MAX_RANGES) ranges of queries: range r holds
+// min(counts[r], stride) queries from index r * stride (counts: device, null = `stride` queries in
+// every range).  out, at the same indices: raw outputs (GUIDE_RAW_STRIDE floats per query) or,
+// with mixture, parsed mixture records (GUIDE_MIX_STRIDE).
+constexpr int GUIDE_MAX_RANGES = 3;
+void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* counts, uint32_t nranges,
+                        uint32_t stride, float* out, bool mixture, uint32_t* err, int sms, cudaStream_t s);
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s);
 void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
                        const GuideAdam& h, cudaStream_t s);
 void launch_guide_pack(const float* p, uint8_t* wpack, cudaStream_t s);
-// wsum[b] = sum of the positive finite weights of batch b (positions b*batch .. in `order`).
+// wsum[2b], wsum[2b + 1] = sums of the positive finite indirect (head 0) and direct (head 1)
+// weights of batch b (positions b*batch .. in `order`).
 void launch_guide_wsum(const float4* samples, const PoolOrder& order, uint32_t batch, float* wsum, cudaStream_t s);
 // Relative variance of this pass's samples (film.pass) against the mean of the earlier passes:
 // film.pass holds the sum of this pass's k samples per pixel.  With x = pass / k and m the mean of

@@ -232,8 +232,6 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
         wb.counters[C_EXT_HEAD] = 0;
         wb.counters[C_SH_HEAD] = 0;
         for (int c = 0; c < NCLS; ++c) wb.counters[C_CLS + c] = 0;
-        for (int c = 0; c < 3; ++c) wb.counters[C_GUIDE + c] = 0;
-        wb.counters[C_GSPAN] = 0;
     }
 }
 
@@ -360,9 +358,12 @@ __global__ void __launch_bounds__(256) k_sort_scatter(WaveBuffers wb, RenderPara
 }
 
 // Material-key binning of this bounce's hits: one queue per material class plus misses, so each
-// shade launch runs one material's code with uniform control flow.
-template <bool MULTI = false>
-__global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t bounce, const SceneRender* tab) {
+// shade launch runs one material's code with uniform control flow.  GWK (guided waves, queries
+// set): a hit of a guidable class (matte, plastic, conductor) also writes its network query at
+// class * gw.cap + its queue position, for the inference that runs before shading.
+template <bool MULTI = false, bool GWK = false>
+__global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t bounce, const SceneRender* tab,
+                                             GuideWave gw = GuideWave{}, bool queries = false) {
     const uint32_t n = wb.counters[bounce & 1];
     const uint32_t* q = wb.queue[bounce & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -376,10 +377,27 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
             const Scene& sc = pick<MULTI>(sc0, MULTI ? &tab[wb.scene_id[slot]].sc : nullptr);
             cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
         }
+        uint32_t qpos = 0;
 #pragma unroll
         for (int c = 0; c < NCLS; ++c) {
             uint32_t pos = warp_append(&wb.counters[C_CLS + c], cls == c);
-            if (cls == c) wb.cls_queue[(size_t)c * wb.capacity + pos] = slot;
+            if (cls == c) {
+                wb.cls_queue[(size_t)c * wb.capacity + pos] = slot;
+                qpos = (uint32_t)c * gw.cap + pos;
+            }
+        }
+        // one intersection per lane (outside the class loop, so the lanes of all three classes
+        // run it together)
+        if (GWK && queries && cls >= 0 && cls <= 2 && qpos - (uint32_t)cls * gw.cap < gw.cap) {
+            const Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
+            Isect it;
+            GuideQuery gq{make_float4(0.5f, 0.5f, 0.5f, 0.0f), make_float4(0.0f, 1.0f, 0.0f, 0.0f),
+                          make_float4(1.0f, 0.0f, 0.0f, 0.0f)};
+            if (prim_isect(sc0, wb.hit[slot].x, ray, &it)) gq = make_query(gw, it, -ray.d);
+            float4* o = gw.query + 3 * (size_t)qpos;
+            o[0] = gq.a;
+            o[1] = gq.b;
+            o[2] = gq.c;
         }
     }
 }
@@ -460,15 +478,19 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         }
         if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
         else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
-        k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
+        const bool queries = guided && b < rp.max_depth;
+        if (queries) {
+            // every hit of a guidable class queues its network query; the network's mixtures are
+            // ready before the shade launches
+            k_bin<false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, true);
+            launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_CLS], 3, gw.cap, gw.raw, true, err, ls.sms, s);
+            launches += 1;
+        } else {
+            k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
+        }
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
         if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s);
         else launches += launch_shade_plain(sc, rp, film, wb, b, err, grid, block, s);
-        if (guided && b < rp.max_depth) {
-            launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_GSPAN], gw.cap, gw.raw, true, err, ls.sms, s);
-            launches += 1;
-            launches += launch_guide_continue(sc, rp, film, wb, gw, b, err, grid, block, s);
-        }
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);

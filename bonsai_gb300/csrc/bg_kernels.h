@@ -93,15 +93,16 @@ struct SceneRender {
 // Guiding state of one wavefront (all null / zero for unguided renders).
 //   record: every non-specular vertex whose continuation was sampled opens a training record
 //           (query, wi, BSDF pdf, throughput before the vertex); the next shade of the path closes
-//           it with the radiance accumulated so far (less the emission found there), and at the end
-//           of the path each record becomes a training sample with weight
-//           lum((L_end - L_after) / beta) = f |cos| Li / p, Li including that emission.
-//   guided: matte / plastic / conductor vertices queue a network query; k_guide_continue then runs
-//           their next-event estimation with the one-sample mixture c * guide + (1 - c) * BSDF as
-//           the second (direction-sampling) strategy of estimate_direct, and the BSDF-sampled
-//           continuation.
-//   GW_CONT: the continuation is drawn from the same mixture (one-sample MIS with the BSDF);
-//   GW_NEE: the mixture is estimate_direct's second strategy (otherwise that stays a BSDF sample).
+//           it, splitting what arrived along wi into the emission found there (direct) and what
+//           the path gathers after it (indirect); at the end of the path each record becomes a
+//           training sample with weight f |cos| Li / p (luminance) of the selected target.
+//   guided: the binning pass writes a network query for every matte / plastic / conductor hit,
+//           the network infers their mixtures, and the shade kernel samples with the one-sample
+//           mixture c * guide + (1 - c) * BSDF: as the second (direction-sampling) strategy of
+//           estimate_direct (GW_NEE) and / or for the continuation (GW_CONT).
+//   GW_CONT: the continuation is drawn from the continuation head's mixture (one-sample MIS with
+//   the BSDF); GW_NEE: estimate_direct's second strategy is drawn from the next-event head's
+//   mixture (otherwise either stays a BSDF sample).
 enum : uint32_t { GW_RECORD = 1u, GW_GUIDED = 2u, GW_CONT = 4u, GW_NEE = 8u };
 constexpr int GUIDE_MAXREC = 6;      // training records kept per path
 constexpr int GUIDE_REC_F4 = 5;      // float4 per record
@@ -114,9 +115,10 @@ struct GuideWave {
     uint32_t cap;        // path slots the record / query buffers below hold (>= the wave's paths)
     float4 bmin, binv;   // position encoding: p_norm = (p - bmin) * binv
     float4* rec;         // GUIDE_MAXREC * GUIDE_REC_F4 * cap, [k][field][slot]
-    float4* query;       // 3 float4 per guided query (cap queries)
-    uint32_t* gslot;     // guided query -> path slot
-    float* raw;          // GUIDE_MIX_STRIDE floats per guided query (parsed network output)
+    // guided queries of material class c (matte, plastic, conductor) at c * cap + the path's
+    // position in the class queue
+    float4* query;       // 3 float4 per query (3 * cap queries)
+    float* raw;          // GUIDE_MIX_STRIDE floats per query (parsed network output)
     float4* pool;        // 4 float4 per training sample
     uint32_t* ctr;       // [0] positive-weight records, [1] pool appends (kept)
     const uint8_t* wpack;  // BF16 weight image
@@ -183,8 +185,8 @@ void launch_megakernel(bool ref_compat, const Scene& sc, const Camera& cam, cons
 // One wave of the PBRT wavefront: items [item0, item0 + nitems) of the pixel x sample space.
 // Returns the number of kernels launched.  stage_events (optional): 4 events per bounce, recorded
 // before extend, before shade, before shadow and before finalize.
-// gw (optional): guiding state; guided waves add the network inference and k_guide_continue
-// after the material shades of every bounce.
+// gw (optional): guiding state; guided waves write the network queries while binning and run the
+// network inference before the material shades of every bounce.
 int launch_wave(const Scene& sc, const Camera& cam, const RenderParams& rp, const FilmBuffers& film,
                 const WaveBuffers& wb, uint64_t item0, uint32_t nitems, uint32_t* err, const LaunchShape& ls,
                 cudaStream_t s, cudaEvent_t* stage_events, const GuideWave* gw = nullptr);

@@ -1,5 +1,5 @@
-// bg_shade_aux.cu - the shade launches of guided renders (training records, network queries) and
-// of batch renders (per-path scenes), and the guided vertices' continuation.
+// bg_shade_aux.cu - the shade launches of guided renders (training records, network mixtures) and
+// of batch renders (per-path scenes).
 #include "bg_wave.cuh"
 
 namespace bg {
@@ -13,15 +13,6 @@ int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffe
     k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     return 5;
-}
-
-int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                          const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
-    if (sc.ntex || general_lights(sc)) return launch_guide_continue_full(sc, rp, film, wb, gw, b, err, grid, block, s);
-    k_guide_continue<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    k_guide_continue<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    k_guide_continue<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    return 3;
 }
 
 int launch_shade_batch(const SceneRender* tab, const WaveBuffers& wb, uint32_t b, uint32_t* err, dim3 grid, dim3 block,

@@ -1,4 +1,4 @@
-// bg_shade_guided_full.cu - the guided render's shade and continuation launches for scenes with
+// bg_shade_guided_full.cu - the guided render's shade launches for scenes with
 // textures or an infinite light: variants that filter textures (matte, plastic) and sample the
 // infinite light, both resolved per scene at run time.
 #include "bg_wave.cuh"
@@ -14,15 +14,6 @@ int launch_shade_guided_full(const Scene& sc, const RenderParams& rp, const Film
     k_shade<2, false, true, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     k_shade<3, false, true, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     return 5;
-}
-
-int launch_guide_continue_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film,
-                               const WaveBuffers& wb, const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid,
-                               dim3 block, cudaStream_t s) {
-    k_guide_continue<0, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    k_guide_continue<1, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    k_guide_continue<2, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err);
-    return 3;
 }
 
 }  // namespace bg

@@ -1,6 +1,6 @@
 // bg_wave.cuh - device code shared by the wavefront translation units: the path state word,
 // camera-ray generation, texture inputs of a path vertex, guiding records, next-event estimation
-// and continuation of a vertex (scatter_vertex) and the shade / guided-continue kernel templates.
+// and continuation of a vertex (scatter_vertex) and the shade kernel template.
 // The shade kernels are instantiated in bg_shade_plain.cu (single-scene renders) and
 // bg_shade_aux.cu (guided and batch renders) so that their compilation runs in parallel.
 #pragma once
@@ -58,19 +58,7 @@ BG_D uint32_t st_k2(uint32_t st) { return st >> 24; }
 BG_D uint32_t st_set_k(uint32_t st, uint32_t k1, uint32_t k2) {
     return (st & 0xFFFFu) | (min(k1, 255u) << 16) | (min(k2, 255u) << 24);
 }
-enum : uint32_t {
-    C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6,
-    C_GUIDE = 11,  // 11..13: guided queries of the matte, plastic and conductor classes
-    C_GSPAN = 14   // end of the guided-query range (written by the dielectric shade launch)
-};
-// Guided queries of class c occupy [guide_base(c), guide_base(c) + counters[C_GUIDE + c]) of the
-// query buffer, guide_base(c) = sizes of the class queues before c, so each class's continuation
-// runs as its own launch with a static BSDF type.
-BG_D uint32_t guide_base(const WaveBuffers& wb, int cls) {
-    uint32_t b = 0;
-    for (int c = 0; c < cls; ++c) b += wb.counters[C_CLS + c];
-    return b;
-}
+enum : uint32_t { C_Q0 = 0, C_Q1 = 1, C_SHADOW = 2, C_DONE = 3, C_EXT_HEAD = 4, C_SH_HEAD = 5, C_CLS = 6 };
 constexpr int NCLS = 5;          // material classes 0..3 (bg_material_type) + misses
 constexpr int CLS_MISS = 4;
 
@@ -129,12 +117,22 @@ BG_D float4* rec_ptr(const GuideWave& gw, uint32_t k, uint32_t f, uint32_t slot)
 }
 BG_D uint32_t rec_count(uint32_t state) { return (state & ST_REC_MASK) >> ST_REC_SHIFT; }
 
-// Closes the open record with the radiance the path has gathered before this vertex adds its own
-// emission: what arrived along the recorded direction is everything added after this point.
-BG_D uint32_t close_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state, RGB L) {
+// Closes the open record at the vertex its direction reached.  `L_after` is the radiance the path
+// holds once this vertex's emission is counted (if the estimator counts it here), `le_beta` that
+// emission times the path throughput.  Everything the path adds after L_after arrived along the
+// recorded direction indirectly (the indirect target); the emission found here, divided by the
+// recording vertex's throughput, is the direct target f |cos| Le / p, stored in .w.
+BG_D uint32_t close_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t state, RGB L_after,
+                           RGB le_beta) {
     if (!(state & ST_REC_OPEN) || slot >= gw.cap) return state;
     uint32_t k = rec_count(state) - 1;
-    *rec_ptr(gw, k, 4, slot) = make_float4(L.r, L.g, L.b, 0.0f);
+    float w_direct = 0.0f;
+    if (!is_black(le_beta)) {
+        const float4 r3 = *rec_ptr(gw, k, 3, slot);
+        w_direct = luminance(rgb(r3.y > 0.0f ? le_beta.r / r3.y : 0.0f, r3.z > 0.0f ? le_beta.g / r3.z : 0.0f,
+                                 r3.w > 0.0f ? le_beta.b / r3.w : 0.0f));
+    }
+    *rec_ptr(gw, k, 4, slot) = make_float4(L_after.r, L_after.g, L_after.b, w_direct);
     return state & ~ST_REC_OPEN;
 }
 
@@ -181,16 +179,19 @@ BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot
         if (!__any_sync(FULL, has)) break;
         bool keep = false;
         float w = 0.0f;
-        float4 r3 = make_float4(0, 0, 0, 0);
+        float4 r3 = make_float4(0, 0, 0, 0), r4 = make_float4(0, 0, 0, 0);
         if (has) {
             r3 = *rec_ptr(gw, k, 3, slot);
-            float4 r4 = *rec_ptr(gw, k, 4, slot);
+            r4 = *rec_ptr(gw, k, 4, slot);
             RGB d = L_end - rgb(r4.x, r4.y, r4.z);
-            // (L_end - L_after) / beta = f |cos| Li / p of the recorded direction
+            // (L_end - L_after) / beta = f |cos| Li_indirect / p of the recorded direction (head 0);
+            // r4.w = f |cos| Le / p, the emission the direction reached (head 1)
             RGB li = rgb(r3.y > 0.0f ? d.r / r3.y : 0.0f, r3.z > 0.0f ? d.g / r3.z : 0.0f,
                          r3.w > 0.0f ? d.b / r3.w : 0.0f);
-            w = luminance(li);
-            if (w > 0.0f && isfinite(w)) {
+            w = fmaxf(luminance(li), 0.0f);
+            if (!isfinite(w)) w = 0.0f;
+            if (!(r4.w > 0.0f && isfinite(r4.w))) r4.w = 0.0f;
+            if (w > 0.0f || r4.w > 0.0f) {
                 ++positive;
                 keep = hash_unit(wb.pixel[slot], wb.sample[slot], k) < gw.keep_prob;
             }
@@ -201,7 +202,7 @@ BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot
             o[0] = *rec_ptr(gw, k, 0, slot);
             o[1] = *rec_ptr(gw, k, 1, slot);
             o[2] = *rec_ptr(gw, k, 2, slot);
-            o[3] = make_float4(r3.x, w, 0.0f, 0.0f);
+            o[3] = make_float4(r3.x, w, r4.w, 0.0f);
         }
     }
     uint32_t tot = __reduce_add_sync(FULL, positive);
@@ -211,9 +212,11 @@ BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot
 // Everything a non-specular or specular vertex does after its emission: next-event estimation
 // (uniform_sample_one_light + estimate_direct, src/base/integrator.rs:309-437, the occlusion tests
 // deferred to k_shadow), the BSDF-sampled continuation (src/integrators/path.rs:110-143) and
-// Russian roulette.  `mix` (guided vertices) replaces the BSDF in estimate_direct's second
-// strategy by the one-sample mixture c * guide + (1 - c) * BSDF: the direction is drawn from it and
-// both MIS weights use its pdf, so the estimator stays unbiased whatever the network outputs.
+// Russian roulette.  `mix` (guided vertices, the query's two mixtures) replaces the BSDF by the
+// one-sample mixture c * guide + (1 - c) * BSDF of head 1 in estimate_direct's second strategy
+// (GW_NEE; the direction is drawn from it and both MIS weights use its pdf) and by that of head 0
+// for the continuation (GW_CONT; the throughput divides by its pdf), so the estimator stays
+// unbiased whatever the network outputs.
 struct VertexOut {
     bool cont = false, finished = false;
     bool push_sh[2] = {false, false};
@@ -279,8 +282,10 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     if (su) strat_apply(su, nee, u);  // the stratified sampler's values, prefetched by the shade thread
     // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
     state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
-    // the mixture in estimate_direct's second strategy (GW_NEE) and in the continuation (GW_CONT)
-    const MixView* nmix = GUIDABLE && mix && (gw.flags & GW_NEE) ? mix : nullptr;
+    // `mix` is the query's two-head record: head 0 (at mix) for the continuation (GW_CONT), head 1
+    // for estimate_direct's second strategy (GW_NEE)
+    const MixView nview{mix ? mix->m + GUIDE_MIX_HEAD : nullptr};
+    const MixView* nmix = GUIDABLE && mix && (gw.flags & GW_NEE) ? &nview : nullptr;
     if (nee) {
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
         float count = (float)sc.nlights;
@@ -401,7 +406,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     out.cont = true;
 }
 
-// Warp-convergent tail of k_shade / k_guide_continue: queue compaction, shadow rays, records.
+// Warp-convergent tail of k_shade: queue compaction, shadow rays, records.
 BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t slot, bool cont,
                         bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, bool record,
                         uint32_t* err) {
@@ -425,17 +430,18 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 }
 
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
-// In guided waves the matte / plastic / conductor classes stop after their emission and queue a
-// network query; k_guide_continue finishes them with the network's mixture.
-// GWK: guiding support compiled in (records, guided queries); the plain wavefront uses GWK = false.
+// In guided waves the matte / plastic / conductor classes read the network's mixture for their
+// queue position (inferred after binning, before this launch) and sample with it.
+// GWK: guiding support compiled in (records, mixtures); the plain wavefront uses GWK = false.
 // Minimum resident CTAs per SM the shade kernels are compiled for: 4 caps them at 128 registers
 // (the plastic and conductor classes would use 148 / 159).  Measured on the production scene at
 // 4 spp: shade 7.1 ms against 7.7 ms unconstrained; 5 and 6 CTAs gave 7.3 and 7.1 ms.
 #ifndef BG_SHADE_MINBLOCKS
 #define BG_SHADE_MINBLOCKS 4
 #endif
+// The guided variants hold the mixture view and eight more uniforms: they are compiled for 3 CTAs.
 template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false, bool SHL = INF>
-__global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
+__global__ void __launch_bounds__(128, GWK ? 3 : BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
@@ -444,17 +450,13 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
     __shared__ float strat_su[CLS != CLS_MISS ? 8 * SU_STRIDE : 1];
     const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     const bool guided = GWK && GUIDABLE && (gw.flags & GW_GUIDED);
-    const uint32_t gbase = GUIDABLE && GWK ? guide_base(wb, CLS) : 0u;
-    if (CLS == 3 && GWK && (gw.flags & GW_GUIDED) && blockIdx.x == 0 && threadIdx.x == 0)
-        wb.counters[C_GSPAN] = guide_base(wb, 2) + wb.counters[C_GUIDE + 2];  // classes 0..2 are done
     // warp-uniform loop so the ballots below see all 32 lanes
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
         uint32_t i = base + lane_id();
         bool active = i < n;
         uint32_t slot = active ? q[i] : 0;
-        bool cont = false, done_pending = false, push_guide = false;
+        bool cont = false, done_pending = false;
         VertexOut vo;
-        GuideQuery gq;
         uint32_t emit_n = 0;
         RGB L_emit = rgb(0.0f);
         if (active) {
@@ -485,18 +487,23 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
             RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
             // an escaped ray gathers the infinite light's radiance (path.rs:78-85)
             if (CLS == CLS_MISS && prim < 0 && (counted || record) && sc.inf) le = inf_radiance(sc, ray.d);
-            // The previous vertex's record closes here.  Its training target also takes this
-            // emission, which the estimator leaves to that vertex's next-event estimation: the
-            // network learns the directions of lights as well, for the strategy it serves.
-            if (record) state = close_record(gw, wb, slot, state, counted ? L : L - beta * le);
+            // The previous vertex's record closes here, with this emission as its direct target
+            // (which the estimator leaves to that vertex's next-event estimation unless counted).
+            if (record) state = close_record(gw, wb, slot, state, counted ? L + beta * le : L, beta * le);
             if (counted) L = L + beta * le;
             bool finished = !hit || bounce >= rp.max_depth;
-            if (!finished && guided) {
-                gq = make_query(gw, it, -ray.d);
-                push_guide = true;
-            } else if (!finished) {
-                scatter_vertex<CLS, TEX, INF, SHL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state, nullptr, nullptr, record,
-                                    vo, su);
+            if (!finished) {
+                // guided: the mixture inferred for this queue position (GW_CONT / GW_NEE place it)
+                const bool gv = guided && i < gw.cap;
+                const MixView mix{gv ? gw.raw + ((size_t)(GUIDABLE ? CLS : 0) * gw.cap + i) * GUIDE_MIX_STRIDE : nullptr};
+                float ug[8];
+                if (gv) {
+                    const Rng grng{wb.pixel[slot], wb.sample[slot], rp.seed};
+                    grng.block(DIM_GUIDE0 + 8 * bounce, ug);
+                    grng.block(DIM_GUIDE0 + 8 * bounce + 4, ug + 4);
+                }
+                scatter_vertex<CLS, TEX, INF, SHL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state,
+                                                   gv ? &mix : nullptr, ug, record, vo, su);
                 finished = vo.finished;
                 cont = vo.cont;
             }
@@ -513,85 +520,7 @@ __global__ void __launch_bounds__(128, BG_SHADE_MINBLOCKS) k_shade(Scene sc0, Re
                 }
             }
         }
-        if (GUIDABLE && GWK && (gw.flags & GW_GUIDED)) {
-            uint32_t pos = gbase + warp_append(&wb.counters[C_GUIDE + (GUIDABLE ? CLS : 0)], push_guide);
-            if (push_guide && pos >= gw.cap) {
-                atomicOr(err, ERR_QUEUE_OVERFLOW);  // cannot happen: one query per path of the wave
-                push_guide = false;
-            }
-            if (push_guide) {
-                gw.query[3 * (size_t)pos] = gq.a;
-                gw.query[3 * (size_t)pos + 1] = gq.b;
-                gw.query[3 * (size_t)pos + 2] = gq.c;
-                gw.gslot[pos] = slot;
-            }
-        }
         finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, record, err);
-    }
-}
-
-// Guided vertices of one material class, after the network has evaluated them: scatter_vertex with
-// the network's mixture in the second direct-light strategy and / or the continuation.  Uniforms:
-// the bounce's dims (shared with the unguided path) plus eight guide dims at DIM_GUIDE0 + 8 bounce
-// (next-event and continuation: mixture choice, lobe, cos theta, phi).
-// FULL: textures (matte, plastic) and the infinite light's next-event estimation compiled in (the
-// variants launched for scenes that have either).
-template <int CLS, bool FULL = false>
-__global__ void __launch_bounds__(128) k_guide_continue(Scene sc, RenderParams rp, FilmBuffers film, WaveBuffers wb,
-                                                        GuideWave gw, uint32_t bounce, uint32_t* err) {
-    __shared__ float strat_su[8 * SU_STRIDE];
-    const uint32_t gbase = guide_base(wb, CLS);
-    const uint32_t n = min(wb.counters[C_GUIDE + CLS], gw.cap - min(gbase, gw.cap));
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
-        uint32_t i = gbase + base + lane_id();
-        bool active = base + lane_id() < n;
-        uint32_t slot = active ? gw.gslot[i] : 0;
-        bool cont = false, done_pending = false;
-        VertexOut vo;
-        uint32_t emit_n = 0;
-        RGB L_emit = rgb(0.0f);
-        if (active) {
-            Ray ray = load_ray(wb.ray_o[slot], wb.ray_d[slot]);
-            int prim = wb.hit[slot].x;
-            uint32_t state = wb.state[slot];
-            float4 b4 = wb.beta[slot];
-            RGB beta = rgb(b4.x, b4.y, b4.z);
-            float eta_scale = b4.w;
-            float4 l4 = wb.L[slot];
-            RGB L = rgb(l4.x, l4.y, l4.z);
-            bool finished = true;
-            Isect it;
-            const float* su = nullptr;
-            if (rp.strat.dims > 0) {
-                float* col = strat_su + threadIdx.x;
-                strat_prefetch(rp.strat, wb.pixel[slot], wb.sample[slot], rp.seed, st_k1(state), st_k2(state), col);
-                su = col;
-            }
-            if (prim >= 0 && prim_isect(sc, prim, ray, &it)) {
-                const MixView mix{gw.raw + (size_t)GUIDE_MIX_STRIDE * i};
-                float ug[8];
-                const Rng grng{wb.pixel[slot], wb.sample[slot], rp.seed};
-                grng.block(DIM_GUIDE0 + 8 * bounce, ug);
-                grng.block(DIM_GUIDE0 + 8 * bounce + 4, ug + 4);
-                scatter_vertex<CLS, FULL && CLS <= 1, FULL>(sc, rp, wb, gw, slot, bounce, ray, it, beta, eta_scale, state,
-                                                            &mix, ug, (gw.flags & GW_RECORD) != 0, vo, su);
-                finished = vo.finished;
-                cont = vo.cont;
-            }
-            wb.state[slot] = state;
-            wb.beta[slot] = make_float4(beta.r, beta.g, beta.b, eta_scale);
-            if (finished) {
-                if (state & ST_PENDING) {
-                    done_pending = true;
-                } else {
-                    film_add(film, wb.pixel[slot], L);
-                    emit_n = rec_count(state);
-                    L_emit = L;
-                }
-            }
-        }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, (gw.flags & GW_RECORD) != 0, err);
     }
 }
 
@@ -607,13 +536,6 @@ int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffe
 int launch_shade_guided_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                              const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,
                              cudaStream_t s);
-int launch_guide_continue_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film,
-                               const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid,
-                               dim3 block, cudaStream_t s);
-// The guided vertices' continuation after the network inference (matte, plastic, conductor).
-int launch_guide_continue(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                          const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,
-                          cudaStream_t s);
 // full: the variants that handle textured scenes and infinite lights (checked per path's scene).
 int launch_shade_batch(const SceneRender* tab, const WaveBuffers& wb, uint32_t bounce, uint32_t* err, dim3 grid,
                        dim3 block, cudaStream_t s, bool full);

@@ -347,7 +347,8 @@ class Guide:
         return t.value, i.value
 
     def mixture_eval(self, raw: np.ndarray, u: np.ndarray, w: np.ndarray, p_bsdf: np.ndarray) -> np.ndarray:
-        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, A.BG_GUIDE_OUTPUTS)
+        """Device evaluation of one head's mixture: raw (n, 41) outputs of a head."""
+        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, A.BG_GUIDE_OUTPUTS // 2)
         n = len(raw)
         u = np.ascontiguousarray(u, np.float32).reshape(n, 3)
         w = np.ascontiguousarray(w, np.float32).reshape(n, 3)

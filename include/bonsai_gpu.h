@@ -437,28 +437,34 @@ bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, cons
  * No counterpart in the reference (its PathIntegrator samples continuation directions from the
  * BSDF only, src/integrators/path.rs:110-117).  A small network maps a shading point (position
  * normalised to the scene bounds and encoded with 12 octaves of sin/cos, shading normal,
- * outgoing direction) to a mixture of 8 von Mises-Fisher lobes and a selection probability c.
- * At matte, plastic and conductor vertices bg_render_guided uses the network in next-event
- * estimation (estimate_direct, src/base/integrator.rs:330-437): the second strategy, which the
- * reference draws from the BSDF to look for the chosen light, is drawn from the one-sample mixture
- * c * guide + (1 - c) * BSDF and MIS-weighted by that mixture's pdf against the light sample.  The
- * path's continuation stays a BSDF sample.  The estimate stays unbiased whatever the network
- * outputs.  The network (78 -> 4 x 64 ReLU -> 41,
- * BF16 weights and activations, FP32 accumulation on the tensor cores) trains online on the
- * radiance the render itself measures, with Adam.
+ * outgoing direction) to two heads, each a mixture of 8 von Mises-Fisher lobes and a selection
+ * probability c.  At matte, plastic and conductor vertices bg_render_guided samples with the
+ * one-sample mixture c * guide + (1 - c) * BSDF of each head:
+ *   head 0, the continuation: the path's next direction (path.rs:110-117) is drawn from the
+ *     mixture and its throughput divided by the mixture's pdf; this head learns the radiance that
+ *     arrives indirectly along a direction (what the path gathers after the next vertex);
+ *   head 1, next-event estimation (estimate_direct, src/base/integrator.rs:330-437): the second
+ *     strategy, which the reference draws from the BSDF to look for the chosen light, is drawn
+ *     from the mixture and MIS-weighted by its pdf against the light sample; this head learns the
+ *     emission a direction reaches directly.
+ * The estimate stays unbiased whatever the network outputs.  The network (78 -> 4 x 64 ReLU ->
+ * 2 x 41, BF16 weights and activations, FP32 accumulation on the tensor cores) trains online on
+ * the radiance the render itself measures, with Adam.
  *
  * Parameter layout (BG_GUIDE_PARAMS floats): five layers of row-major W[out][80], biases folded
  * in as the weight of a constant-1 input column (column 78 of layer 0, column 64 of layers 1-4);
- * layers 0-3 have 64 rows (offset 5120 * l), layer 4 48 rows of which 41 are used (offset
+ * layers 0-3 have 64 rows (offset 5120 * l), layer 4 96 rows of which 82 are used (offset
  * 20480).  Unused rows and columns stay zero.
  * Query (BG_GUIDE_QUERY_FLOATS): p.xyz in [0,1], shading normal xyz, wo xyz.
- * Output (BG_GUIDE_OUTPUTS): lobe i: direction xyz (5i..5i+2, normalised on use), log kappa
- * (5i+3, clamped to [-2, 8]), weight logit (5i+4); selection logit at 40 (c = 0.95 sigmoid).
- * Training sample (BG_GUIDE_SAMPLE_FLOATS): query (9), wi xyz (3), BSDF pdf of wi, weight
- * f |cos| Li / p_proposal (luminance), 2 unused. */
-#define BG_GUIDE_PARAMS 24320u
+ * Output (BG_GUIDE_OUTPUTS): head h at 41 h: lobe i: direction xyz (5i..5i+2, normalised on use),
+ * log kappa (5i+3, clamped to [-2, 8]), weight logit (5i+4); selection logit at 40
+ * (c = 0.95 sigmoid).
+ * Training sample (BG_GUIDE_SAMPLE_FLOATS): query (9), wi xyz (3), BSDF pdf of wi, the weights
+ * f |cos| L / p_proposal (luminance) of head 0 (L = indirect radiance along wi) and of head 1
+ * (L = emission wi reaches), 1 unused. */
+#define BG_GUIDE_PARAMS 28160u
 #define BG_GUIDE_QUERY_FLOATS 9u
-#define BG_GUIDE_OUTPUTS 41u
+#define BG_GUIDE_OUTPUTS 82u
 #define BG_GUIDE_SAMPLE_FLOATS 16u
 
 typedef struct bg_guide bg_guide;
@@ -479,7 +485,7 @@ typedef struct bg_guide_opts {
 
 #define BG_GUIDE_NO_FALLBACK 1u /* keep guiding even when its variance estimate is not lower  */
 #define BG_GUIDE_NO_TRAIN 2u    /* render with the current weights; no online training         */
-#define BG_GUIDE_CONTINUATION 4u /* draw the path's continuation from the mixture as well        */
+#define BG_GUIDE_NO_CONTINUATION 4u /* sample continuations from the BSDF only                */
 #define BG_GUIDE_NO_NEE 8u      /* keep estimate_direct's second strategy a BSDF sample        */
 
 typedef struct bg_guide_stats {
@@ -528,7 +534,7 @@ bg_status bg_guide_pool(bg_guide* guide, float* out, size_t max_n, size_t* n_out
  * inference pass. */
 bg_status bg_guide_time(bg_guide* guide, const float* samples, size_t n, const float* queries, size_t nq,
                         uint32_t reps, double* train_step_ms, double* infer_ms);
-/* Device evaluation of the mixture for given raw outputs (test entry): per item raw (41), u (3),
+/* Device evaluation of one head's mixture for given raw outputs (test entry): per item raw (41), u (3),
  * w (3), p_bsdf (1) -> out (48): sampled direction xyz, pdf of it, pdf of w, c, loss and its
  * gradient (out[7] = d/d raw[40], out[8..47] = d/d raw[0..39]) for a unit-weight sample at w. */
 bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* u, const float* w,

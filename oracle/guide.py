@@ -17,8 +17,10 @@ import numpy as np
 LAYERS = 5
 K = 80
 HID = 64
-OUT = 41
-OUT_ROWS = 48
+HEADS = 2
+HEAD_OUT = 41   # per head: 8 lobes x (direction 3, log kappa, weight logit) + selection logit
+OUT = HEADS * HEAD_OUT
+OUT_ROWS = 96
 LOBES = 8
 OCTAVES = 12
 IN_USED = 78
@@ -87,6 +89,7 @@ def forward(params: np.ndarray, q: np.ndarray, bf16_sim: bool = False):
 
 
 def parse(raw: np.ndarray):
+    """One head's mixture from its raw outputs (n, >= 41)."""
     raw = np.asarray(raw, np.float64)
     lob = raw[:, :40].reshape(-1, LOBES, 5)
     d = lob[:, :, :3]
@@ -145,8 +148,9 @@ def sample(raw: np.ndarray, u: np.ndarray) -> np.ndarray:
 
 
 def loss_grad(raw: np.ndarray, wi: np.ndarray, p_b: np.ndarray, wn: np.ndarray, alpha: float = 0.5):
-    """Per-sample loss -wn [alpha log(c q + (1-c) p_b) + (1-alpha) log q] and d loss / d raw (n, 48)."""
-    raw = np.asarray(raw, np.float64)
+    """Per-sample loss -wn [alpha log(c q + (1-c) p_b) + (1-alpha) log q] of one head and
+    d loss / d raw (n, 41)."""
+    raw = np.asarray(raw, np.float64)[:, :HEAD_OUT]
     wi = np.asarray(wi, np.float64)
     p_b = np.asarray(p_b, np.float64)
     wn = np.asarray(wn, np.float64)
@@ -165,7 +169,7 @@ def loss_grad(raw: np.ndarray, wi: np.ndarray, p_b: np.ndarray, wn: np.ndarray, 
     dlq = -wn * (alpha * s + (1 - alpha))
     dc = -wn * alpha * dmdc
     r = np.exp(t - lq[:, None])
-    g = np.zeros((n, OUT_ROWS))
+    g = np.zeros((n, HEAD_OUT))
     kap, mu, dlen = m["kap"], m["mu"], m["dlen"]
     sc = dlq[:, None] * r * kap / dlen
     gd = sc[:, :, None] * (wi[:, None, :] - mw[:, :, None] * mu)
@@ -182,18 +186,36 @@ def loss_grad(raw: np.ndarray, wi: np.ndarray, p_b: np.ndarray, wn: np.ndarray, 
 
 
 def split_samples(samples: np.ndarray):
+    """query, wi, BSDF pdf, and the target weights of the two heads (indirect, direct)."""
     s = np.asarray(samples, np.float64).reshape(-1, 16)
-    return s[:, :9], s[:, 9:12], s[:, 12], s[:, 13]
+    return s[:, :9], s[:, 9:12], s[:, 12], s[:, 13:15]
+
+
+def _norm_weights(w: np.ndarray) -> np.ndarray:
+    """Each head's weights over the batch, normalised by their sum (non-positive ones dropped)."""
+    w = np.where(np.isfinite(w) & (w > 0), w, 0.0)
+    s = w.sum(axis=0)
+    return np.where(s > 0, w / np.where(s > 0, s, 1.0), 0.0)
+
+
+def heads_loss_grad(raw: np.ndarray, wi: np.ndarray, p_b: np.ndarray, wn: np.ndarray, alpha: float = 0.5):
+    """Both heads' per-sample losses (summed) and d loss / d raw (n, OUT_ROWS)."""
+    g = np.zeros((len(raw), OUT_ROWS))
+    loss = np.zeros(len(raw))
+    for h in range(HEADS):
+        lh, gh = loss_grad(raw[:, HEAD_OUT * h:HEAD_OUT * (h + 1)], wi, p_b, wn[:, h], alpha)
+        loss += lh
+        g[:, HEAD_OUT * h:HEAD_OUT * (h + 1)] = gh
+    return loss, g
 
 
 def batch_loss_grad(params: np.ndarray, samples: np.ndarray, alpha: float = 0.5, bf16_sim: bool = False):
-    """Gradient of the batch loss (weights normalised by their sum) w.r.t. the padded parameters."""
+    """Gradient of the batch loss (each head's weights normalised by their sum) w.r.t. the padded
+    parameters."""
     q, wi, p_b, w = split_samples(samples)
-    w = np.where(np.isfinite(w) & (w > 0), w, 0.0)
-    wsum = w.sum()
-    wn = w / wsum if wsum > 0 else np.zeros_like(w)
+    wn = _norm_weights(w)
     raw, acts = forward(params, q, bf16_sim)
-    loss, dz = loss_grad(raw[:, :OUT], wi, p_b, wn, alpha)
+    loss, dz = heads_loss_grad(raw, wi, p_b, wn, alpha)
     rnd = bf16 if bf16_sim else (lambda a: a)
     W = weights(params)
     grad = np.zeros(PARAMS)
@@ -214,10 +236,8 @@ def batch_loss_grad(params: np.ndarray, samples: np.ndarray, alpha: float = 0.5,
 
 def batch_loss(params: np.ndarray, samples: np.ndarray, alpha: float = 0.5) -> float:
     q, wi, p_b, w = split_samples(samples)
-    w = np.where(np.isfinite(w) & (w > 0), w, 0.0)
-    wn = w / w.sum()
     raw, _ = forward(params, q)
-    loss, _ = loss_grad(raw[:, :OUT], wi, p_b, wn, alpha)
+    loss, _ = heads_loss_grad(raw, wi, p_b, _norm_weights(w), alpha)
     return float(loss.sum())
 
 
@@ -243,7 +263,8 @@ def init_params(seed: int = 0) -> np.ndarray:
 
 
 def random_samples(n: int, seed: int = 0) -> np.ndarray:
-    """Seeded training samples: queries, unit wi, BSDF pdf (some zero) and heavy-tailed weights."""
+    """Seeded training samples: queries, unit wi, BSDF pdf (some zero) and heavy-tailed weights of
+    both heads (some zero)."""
     rng = np.random.default_rng(seed)
     s = np.zeros((n, 16), np.float32)
     s[:, 0:3] = rng.random((n, 3))
@@ -255,4 +276,5 @@ def random_samples(n: int, seed: int = 0) -> np.ndarray:
     s[:, 9:12] = wi / np.linalg.norm(wi, axis=1, keepdims=True)
     s[:, 12] = np.where(rng.random(n) < 0.1, 0.0, rng.exponential(0.3, n))
     s[:, 13] = np.where(rng.random(n) < 0.2, 0.0, rng.lognormal(0.0, 1.0, n))
+    s[:, 14] = np.where(rng.random(n) < 0.6, 0.0, rng.lognormal(0.5, 1.5, n))
     return s

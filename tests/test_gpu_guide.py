@@ -89,7 +89,7 @@ def test_gradient_matches_fp64(guide):
 def test_gradient_all_zero_weights(guide):
     guide.params = O.init_params(3)
     s = O.random_samples(256, 4)
-    s[:, 13] = 0.0
+    s[:, 13:15] = 0.0
     g, loss = guide.gradient(s)
     assert not g.any() and loss == 0.0
 
@@ -117,7 +117,7 @@ def test_training_fits_a_known_distribution(gpu_ctx):
     try:
         rng = np.random.default_rng(0)
         n = 1 << 14
-        raw_t = np.zeros((n, O.OUT))
+        raw_t = np.zeros((n, O.HEAD_OUT))
         raw_t[:, 0:3] = (1.0, 0.0, 0.0)
         raw_t[:, 3] = np.log(20.0)
         raw_t[:, 5:8] = (0.0, 0.0, 1.0)
@@ -129,13 +129,14 @@ def test_training_fits_a_known_distribution(gpu_ctx):
         s = O.random_samples(n, 1)
         s[:, 9:12] = wi
         s[:, 12] = 0.0          # no BSDF: the mixture is the guide alone
-        s[:, 13] = 1.0
+        s[:, 13] = 1.0          # head 0 learns the two lobes, head 1 gets no samples
+        s[:, 14] = 0.0
         losses = [g.train(s) for _ in range(40)]
         print("loss", losses[0], "->", losses[-1])
         assert losses[-1] < losses[0] - 1.0
         out = g.forward(s[:512, :9])
         on = O.pdf(out, np.tile([1.0, 0.0, 0.0], (512, 1))) + O.pdf(out, np.tile([0.0, 0.0, 1.0], (512, 1)))
-        off = O.pdf(out, np.tile([-1.0, 0.0, 0.0], (512, 1)))
+        off = O.pdf(out, np.tile([-1.0, 0.0, 0.0], (512, 1)))  # head 0 (the first 41 outputs)
         assert np.median(on) > 10 * np.median(off)
     finally:
         g.close()
@@ -144,7 +145,7 @@ def test_training_fits_a_known_distribution(gpu_ctx):
 def test_mixture_eval_matches_oracle(guide):
     rng = np.random.default_rng(21)
     n = 4096
-    raw = rng.normal(0, 1, (n, O.OUT))
+    raw = rng.normal(0, 1, (n, O.HEAD_OUT))
     raw[:, 3:40:5] = rng.uniform(-2.5, 8.5, (n, O.LOBES))  # includes clamped log kappa
     u = rng.random((n, 3))
     w = rng.normal(size=(n, 3))
@@ -256,7 +257,9 @@ def test_multi_spp_passes_and_pool_export(gpu_ctx):
         assert ((pool[:, :3] >= 0) & (pool[:, :3] <= 1)).all()
         for a, b in ((3, 6), (6, 9), (9, 12)):
             np.testing.assert_allclose(np.linalg.norm(pool[:, a:b], axis=1), 1.0, atol=1e-4)
-        assert (pool[:, 13] > 0).all() and np.isfinite(pool[:, 13]).all() and (pool[:, 12] >= 0).all()
+        w = pool[:, 13:15]
+        assert np.isfinite(w).all() and (w >= 0).all() and (w.max(axis=1) > 0).all() and (pool[:, 12] >= 0).all()
+        assert (w[:, 0] > 0).any() and (w[:, 1] > 0).any()  # both heads get training samples
         assert r.guide.adam_steps == 7 * 3 * 8 or r.guide.adam_steps > 0
     finally:
         g.close()

@@ -9,7 +9,7 @@ from oracle import guide as O
 
 def _raw(n, seed=0, scale=1.0):
     rng = np.random.default_rng(seed)
-    raw = rng.normal(0.0, scale, (n, O.OUT))
+    raw = rng.normal(0.0, scale, (n, O.HEAD_OUT))
     raw[:, 3:40:5] = rng.uniform(-1.5, 4.0, (n, O.LOBES))  # log kappa inside the clamp range
     return raw
 
@@ -27,7 +27,7 @@ def test_loss_grad_matches_finite_differences():
     wn = np.full(n, 1.0 / n)
     _, g = O.loss_grad(raw, wi, p_b, wn)
     eps = 1e-6
-    for j in range(O.OUT):
+    for j in range(O.HEAD_OUT):
         rp, rm = raw.copy(), raw.copy()
         rp[:, j] += eps
         rm[:, j] -= eps
