@@ -5,9 +5,11 @@
 //                  TMEM lane); persistent CTAs keep the 48.6 KB weight image in shared memory.
 //   k_guide_train  fused forward + loss gradient + backward for 128 training samples per CTA:
 //                  activations of all layers stay in shared memory, dX = dZ W and
-//                  dW = dZ^T H run as MN-major MMAs on the same tiles, weight gradients are
-//                  reduced into a global FP32 buffer with one atomic add per element and CTA.
+//                  dW = dZ^T H run as MN-major MMAs on the same tiles, each CTA stores its weight
+//                  gradient (plain stores, no atomics) into its slice of a partial buffer.
+//   k_guide_reduce sums the CTAs' partial gradients into the FP32 gradient.
 //   k_guide_adam   Adam on the FP32 master weights; rewrites the BF16 core-matrix image.
+// Both network kernels bring the weight image into shared memory with one bulk (TMA) copy.
 //
 // Shared-memory tiles (no swizzle, core matrices of 8 rows x 16 B, see bg_umma.cuh):
 //   weights  W_l[rows][80]  8-row groups 1280 B apart      (56,320 B for all five layers)
@@ -35,9 +37,11 @@ constexpr uint32_t ACT_BYTES = 128 * GUIDE_K * 2;         // 20,480
 constexpr uint32_t ACT_RS = GUIDE_ROWGROUP_BYTES;         // 1280
 constexpr uint32_t DZ_RS = 2048;                          // 16 column groups per 8-row group
 constexpr uint32_t DZ_BYTES = 16 * DZ_RS;                 // 32,768
-constexpr uint32_t INFER_SMEM = GUIDE_WPACK_BYTES + 2 * ACT_BYTES;                    // 97,280
+constexpr int INFER_WG = 2;  // warpgroups (tiles in flight) per inference CTA
+constexpr uint32_t INFER_TM_COLS = 128 * INFER_WG;
+constexpr uint32_t INFER_SMEM = GUIDE_WPACK_BYTES + INFER_WG * ACT_BYTES;  // 97,280: weights + one tile per warpgroup
 constexpr uint32_t TRAIN_SMEM = GUIDE_WPACK_BYTES + 5 * ACT_BYTES + DZ_BYTES;          // 191,488
-constexpr uint32_t TM_FWD = 0, TM_DW = 0, TM_DX = 128, TM_COLS_TRAIN = 256, TM_COLS_INFER = 128;
+constexpr uint32_t TM_FWD = 0, TM_DW = 0, TM_DX = 128, TM_COLS_TRAIN = 256, TM_COLS_INFER = 128;  // per tile
 static_assert(GUIDE_OUT_ROWS <= (int)TM_DX && TM_DX + GUIDE_K <= TM_COLS_TRAIN, "TMEM column plan");
 static_assert(GUIDE_OUT_ROWS <= (int)TM_COLS_INFER && GUIDE_HID <= (int)TM_COLS_INFER, "TMEM column plan");
 
@@ -52,12 +56,6 @@ BG_D float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xFFFF0000u); }
 BG_D void store_row8(uint8_t* tile, uint32_t rs, uint32_t row, uint32_t c0, const float* v) {
     uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
     *reinterpret_cast<uint4*>(tile + core_off(row, c0, rs)) = q;
-}
-
-BG_D void load_weights(uint8_t* dst, const uint8_t* wpack) {
-    const uint4* s = reinterpret_cast<const uint4*>(wpack);
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    for (uint32_t i = threadIdx.x; i < GUIDE_WPACK_BYTES / 16; i += blockDim.x) d[i] = __ldg(&s[i]);
 }
 
 // Encoded query -> one row of an activation tile (80 columns).
@@ -121,12 +119,40 @@ BG_D void bail_out(uint64_t* bar, uint32_t parity, uint32_t* err, uint32_t tmem,
 // mixture records of both heads (GUIDE_MIX_STRIDE floats) that the render kernels sample.
 // Queries come in `nranges` ranges: range r holds min(counts[r], stride) queries from r * stride
 // (counts null: one range of `stride` queries); outputs use the same indices.
+// Each CTA runs INFER_WG warpgroups, each on its own tile of 128 queries (one per thread / TMEM
+// lane) with its own TMEM accumulator (128 columns), activation tile (updated in place: a layer's
+// epilogue overwrites the tile its MMA has finished reading), mbarrier and named barrier, so the
+// tensor core works on one warpgroup's layer while the other runs an epilogue.  The weight image
+// in shared memory is loaded once per CTA and shared.
+
+// Named barrier ID (1.., 0 is __syncthreads) over the 128 threads of one warpgroup, with an OR of
+// `pred` (the ID is an immediate, so the kernel reserves only the barriers it names).
+template <int ID>
+BG_D bool wg_sync_or(bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, %2, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "n"(ID)
+        : "memory");
+    return r != 0;
+}
+// Stage barrier of warpgroup wg (see stage_barrier).
+BG_D bool wg_stage_barrier(bool ok, uint32_t wg) {
+    static_assert(INFER_WG == 2, "one named barrier per warpgroup");
+    fence_async_smem();
+    tc_fence_before();
+    bool bad = wg == 0 ? wg_sync_or<1>(!ok) : wg_sync_or<2>(!ok);
+    tc_fence_after();
+    return bad;
+}
+
 template <bool MIX>
-__global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, const float4* query,
-                                                        const uint32_t* counts, uint32_t nranges, uint32_t stride,
-                                                        float* raw, uint32_t* err) {
+__global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t* wpack, const float4* query,
+                                                                  const uint32_t* counts, uint32_t nranges,
+                                                                  uint32_t stride, float* raw, uint32_t* err) {
     extern __shared__ __align__(128) uint8_t sm[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar[INFER_WG], wbar;
     __shared__ uint32_t tslot;
     uint32_t rn[GUIDE_MAX_RANGES], rt[GUIDE_MAX_RANGES + 1];  // queries and first tile of each range
     rt[0] = 0;
@@ -136,28 +162,41 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
         rt[r + 1] = rt[r] + (rn[r] + 127) / 128;
     }
     const uint32_t ntiles = rt[GUIDE_MAX_RANGES];
-    if (blockIdx.x >= ntiles) return;
+    if (blockIdx.x * INFER_WG >= ntiles) return;  // uniform over the CTA, before any barrier
     const long long wait_limit = g_guide_wait_limit;
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, wg = tid >> 7, wtid = tid & 127u;
     uint8_t* wsm = sm;
-    uint8_t* act[2] = {sm + GUIDE_WPACK_BYTES, sm + GUIDE_WPACK_BYTES + ACT_BYTES};
-    load_weights(wsm, wpack);
-    if (tid == 0) mbar_init(&bar, 1);
-    if (warp == 0) tmem_alloc(&tslot, TM_COLS_INFER);
+    uint8_t* act = sm + GUIDE_WPACK_BYTES + wg * ACT_BYTES;
+    if (tid == 0) {
+        for (int k = 0; k < INFER_WG; ++k) mbar_init(&bar[k], 1);
+        mbar_init(&wbar, 1);
+    }
+    if (warp == 0) tmem_alloc(&tslot, INFER_TM_COLS);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = tslot;
-    const uint32_t tm_row = tmem + ((warp * 32u) << 16);
-    const uint32_t w_addr = smem_addr(wsm);
+    if (tid == 0) bulk_g2s(wsm, wpack, GUIDE_WPACK_BYTES, &wbar);
+    if (__syncthreads_or(!mbar_wait(&wbar, 0, wait_limit))) {
+        // the weight copy did not arrive in time: record it, let it land (default limit) and stop
+        if (tid == 0) atomicOr(err, ERR_GUIDE_TIMEOUT);
+        mbar_wait(&wbar, 0);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (warp == 0) tmem_dealloc(tslot, INFER_TM_COLS);
+        return;
+    }
+    const uint32_t tmem = tslot + 128u * wg;                  // this warpgroup's columns
+    const uint32_t tm_row = tmem + (((warp & 3u) * 32u) << 16);  // this warp's lane quarter
+    const uint32_t w_addr = smem_addr(wsm), a_addr = smem_addr(act);
     uint32_t phase = 0;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x * INFER_WG + wg; tile < ntiles; tile += gridDim.x * INFER_WG) {
         uint32_t r = 0;
 #pragma unroll
         for (int j = 1; j < GUIDE_MAX_RANGES; ++j)
             if (tile >= rt[j]) r = j;
-        const uint32_t local = (tile - rt[r]) * 128 + tid;
+        const uint32_t local = (tile - rt[r]) * 128 + wtid;
         const bool valid = local < rn[r];
         const uint32_t qi = r * stride + local;
         float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
@@ -166,55 +205,70 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint8_t* wpack, co
             q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w;
             q[8] = c.x;
         }
-        encode_row(act[0], tid, q);
-        if (stage_barrier(true)) return;  // never taken: no wait before the first stage
+        encode_row(act, wtid, q);
+        wg_stage_barrier(true, wg);  // no wait before the first stage
+        bool stop = false;
         for (int l = 0; l < GUIDE_LAYERS; ++l) {
             const int N = guide_rows(l);
-            if (tid == 0) {
-                issue_forward(tmem + TM_FWD, smem_addr(act[l & 1]), w_addr + guide_wpack_off(l), N);
-                umma_commit(&bar);
+            if (wtid == 0) {
+                issue_forward(tmem + TM_FWD, a_addr, w_addr + guide_wpack_off(l), N);
+                umma_commit(&bar[wg]);
             }
-            bool ok = mbar_wait(&bar, phase, wait_limit);
+            bool ok = mbar_wait(&bar[wg], phase, wait_limit);
             phase ^= 1;
             tc_fence_after();
             if (l < GUIDE_LAYERS - 1) {
-                hidden_epilogue(tm_row + TM_FWD, act[(l + 1) & 1], tid);
+                hidden_epilogue(tm_row + TM_FWD, act, wtid);
+            } else if (MIX) {
+#pragma unroll
+                for (int h = 0; h < GUIDE_HEADS; ++h) {
+                    // head h's 41 outputs from the 48 or 64 columns that hold them
+                    float v[64];
+                    const int c0 = h == 0 ? 0 : 32;
+#pragma unroll
+                    for (int c = 0; c < (h == 0 ? 48 : 64); c += 16) tmem_ld16(tm_row + TM_FWD + c0 + c, v + c);
+                    if (valid) {
+                        float rec[GUIDE_MIX_HEAD];
+                        guide_write_mixture(v + (GUIDE_HEAD_OUT * h - c0), rec);
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
+#pragma unroll
+                        for (int j = 0; j < GUIDE_MIX_HEAD / 4; ++j)
+                            o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
+                    }
+                }
             } else {
-                float v[GUIDE_OUT_ROWS];
 #pragma unroll
-                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, v + c);
-                if (valid) {
-                    if (MIX) {
+                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) {
+                    float v[16];
+                    tmem_ld16(tm_row + TM_FWD + c, v);
+                    if (valid) {
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE + c);
 #pragma unroll
-                        for (int h = 0; h < GUIDE_HEADS; ++h) {
-                            float rec[GUIDE_MIX_HEAD];
-                            guide_write_mixture(v + GUIDE_HEAD_OUT * h, rec);
-                            float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
-#pragma unroll
-                            for (int j = 0; j < GUIDE_MIX_HEAD / 4; ++j)
-                                o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
-                        }
-                    } else {
-                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE);
-#pragma unroll
-                        for (int j = 0; j < GUIDE_RAW_STRIDE / 4; ++j)
-                            o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                        for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                     }
                 }
             }
-            if (stage_barrier(ok)) {
-                bail_out(&bar, phase ^ 1, err, tmem, TM_COLS_INFER);
-                return;
+            if (wg_stage_barrier(ok, wg)) {
+                // a wait ran out: record it, let this warpgroup's issued MMAs retire (default
+                // limit) and stop; TMEM is freed once both warpgroups are done
+                if (wtid == 0) atomicOr(err, ERR_GUIDE_TIMEOUT);
+                mbar_wait(&bar[wg], phase ^ 1);
+                stop = true;
+                break;
             }
         }
+        if (stop) break;
     }
-    if (warp == 0) tmem_dealloc(tmem, TM_COLS_INFER);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tslot, INFER_TM_COLS);
 }
 
 // ---------------------------------------------------------------- training
 __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar, wbar;
     __shared__ uint32_t tslot;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long wait_limit = g_guide_wait_limit;
@@ -222,13 +276,17 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     uint8_t* wsm = sm;
     uint8_t* act = sm + GUIDE_WPACK_BYTES;  // 5 tiles: X0, H1..H4
     uint8_t* dz = sm + GUIDE_WPACK_BYTES + 5 * ACT_BYTES;
-    load_weights(wsm, a.wpack);
-    {   // zero dZ (columns 64..127 must read as zero in every dW MMA)
+    {   // zero dZ (columns past a layer's outputs must read as finite values in every dW MMA)
         uint4* d = reinterpret_cast<uint4*>(dz);
         for (uint32_t i = tid; i < DZ_BYTES / 16; i += blockDim.x) d[i] = make_uint4(0, 0, 0, 0);
     }
-    if (tid == 0) mbar_init(&bar, 1);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_init(&wbar, 1);
+    }
     if (warp == 0) tmem_alloc(&tslot, TM_COLS_TRAIN);
+    __syncthreads();  // the barriers are initialised before the bulk copy signals one
+    if (tid == 0) bulk_g2s(wsm, a.wpack, GUIDE_WPACK_BYTES, &wbar);
     // this thread's sample
     const uint32_t si = blockIdx.x * 128 + tid;
     float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
@@ -246,10 +304,20 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         wn1 = (ws1 > 0.0f && f3.z > 0.0f && isfinite(f3.z)) ? f3.z / ws1 : 0.0f;
     }
     encode_row(act, tid, q);
+    const bool wok = mbar_wait(&wbar, 0, wait_limit);  // the weight image (overlaps the encoding above)
     fence_async_smem();
     tc_fence_before();
-    __syncthreads();
+    const bool wbad = __syncthreads_or(!wok);
     tc_fence_after();
+    if (wbad) {
+        if (tid == 0) atomicOr(a.err, ERR_GUIDE_TIMEOUT);
+        mbar_wait(&wbar, 0);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (warp == 0) tmem_dealloc(tslot, TM_COLS_TRAIN);
+        return;
+    }
     const uint32_t tmem = tslot;
     const uint32_t tm_row = tmem + ((warp * 32u) << 16);
     const uint32_t w_addr = smem_addr(wsm), act_addr = smem_addr(act), dz_addr = smem_addr(dz);
@@ -318,18 +386,18 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         bool ok = mbar_wait(&bar, phase, wait_limit);
         phase ^= 1;
         tc_fence_after();
-        // weight gradient rows (thread = output row)
+        // weight gradient rows (thread = output row) into this CTA's partial slice
         const int used = guide_used_rows(l);
         if ((int)(warp * 32) < used) {
-            float* gl = a.grad + guide_param_off(l) + tid * GUIDE_K;
+            float4* gl = reinterpret_cast<float4*>(a.partial + (size_t)blockIdx.x * GUIDE_PARAMS + guide_param_off(l) +
+                                                   tid * GUIDE_K);
 #pragma unroll
             for (int c = 0; c < GUIDE_K; c += 16) {
                 float v[16];
                 tmem_ld16(tm_row + TM_DW + c, v);
                 if ((int)tid < used) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (v[j] != 0.0f) atomicAdd(gl + c + j, v[j]);
+                    for (int j = 0; j < 4; ++j) gl[c / 4 + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 }
             }
         }
@@ -385,6 +453,22 @@ __global__ void k_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wp
     float pi = p[i] - h.lr * mhat / (sqrtf(vhat) + h.eps);
     p[i] = pi;
     pack_param(wpack, i, pi);
+}
+
+// grad[i] += sum over the n CTAs' partial gradients (parameter i of slice b at b * GUIDE_PARAMS + i).
+__global__ void k_guide_reduce(const float* __restrict__ partial, uint32_t n, float* grad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)GUIDE_PARAMS) return;
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+    uint32_t b = 0;
+    for (; b + 4 <= n; b += 4) {
+        s0 += partial[(size_t)b * GUIDE_PARAMS + i];
+        s1 += partial[(size_t)(b + 1) * GUIDE_PARAMS + i];
+        s2 += partial[(size_t)(b + 2) * GUIDE_PARAMS + i];
+        s3 += partial[(size_t)(b + 3) * GUIDE_PARAMS + i];
+    }
+    for (; b < n; ++b) s0 += partial[(size_t)b * GUIDE_PARAMS + i];
+    grad[i] += (s0 + s1) + (s2 + s3);
 }
 
 __global__ void k_guide_pack(const float* p, uint8_t* wpack) {
@@ -489,10 +573,10 @@ void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_
     if (nranges == 0 || nranges > (uint32_t)GUIDE_MAX_RANGES) return;
     guide_set_smem_limits();
     uint64_t tiles = (uint64_t)nranges * ((stride + 127) / 128);
-    uint32_t grid = (uint32_t)std::min<uint64_t>(tiles, (uint64_t)sms * 2);
+    uint32_t grid = (uint32_t)std::min<uint64_t>((tiles + INFER_WG - 1) / INFER_WG, (uint64_t)sms * 2);
     if (grid == 0) return;
-    if (mixture) k_guide_infer<true><<<grid, 128, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
-    else k_guide_infer<false><<<grid, 128, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
+    if (mixture) k_guide_infer<true><<<grid, 128 * INFER_WG, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
+    else k_guide_infer<false><<<grid, 128 * INFER_WG, INFER_SMEM, s>>>(wpack, query, counts, nranges, stride, out, err);
 }
 
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
@@ -500,6 +584,7 @@ void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
     uint32_t grid = (a.n + 127) / 128;
     if (grid == 0) return;
     k_guide_train<<<grid, 128, TRAIN_SMEM, s>>>(a);
+    k_guide_reduce<<<(GUIDE_PARAMS + 255) / 256, 256, 0, s>>>(a.partial, grid, a.grad);
 }
 
 void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,

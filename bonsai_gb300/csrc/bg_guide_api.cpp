@@ -32,6 +32,8 @@ struct bg_guide {
     float* m = nullptr;
     float* v = nullptr;
     float* grad = nullptr;
+    float* partial = nullptr;   // per-CTA gradient slices of one batch (kept zero in unused rows)
+    uint32_t partial_blocks = 0;
     uint8_t* wpack = nullptr;
     uint32_t* step = nullptr;   // Adam step counter
     uint32_t* ctr = nullptr;    // [0] positive-weight records, [1] pool appends
@@ -54,7 +56,9 @@ struct bg_guide {
     float keep = 1.0f;            // pool keep probability for the next pass
     double rv_plain_sum = 0, ms_plain_sum = 0;
     uint32_t n_plain = 0;
-    static constexpr uint32_t kWindow = 8;  // guided passes in the running estimate
+    // guided passes in the running estimate; the fallback is decided only once 2 kWindow guided
+    // passes have trained the network (an early, half-trained guide is not the one that renders)
+    static constexpr uint32_t kWindow = 32;
     double rv_guided[kWindow] = {}, ms_guided[kWindow] = {};
     uint32_t n_guided = 0;
     uint32_t pool_n = 0;          // samples in the pool after the last pass
@@ -229,6 +233,7 @@ int train_batches(bg_guide* g, const float4* samples, uint32_t n, uint32_t epoch
             a.n = std::min(B, n - b * B);
             a.wsum = g->wsum + 2 * b;
             a.alpha = g->o.alpha;
+            a.partial = g->partial;
             a.grad = g->grad;
             a.stats = g->stats;
             a.step = g->step;
@@ -298,6 +303,13 @@ bg_status bg_guide_create(bg_ctx* ctx, const bg_guide_opts* opts, bg_guide** out
     g->pool = (float4*)p;
     if ((st = dalloc(ctx, ((size_t)g->pool_cap / 128 + 1) * 2 * sizeof(float), &p, &g->allocs)) != BG_OK) return bail(st);
     g->wsum = (float*)p;
+    g->partial_blocks = o.batch_size / 128;
+    if ((st = dalloc(ctx, (size_t)g->partial_blocks * bg::GUIDE_PARAMS * sizeof(float), &p, &g->allocs)) != BG_OK)
+        return bail(st);
+    g->partial = (float*)p;
+    if (cudaMemsetAsync(g->partial, 0, (size_t)g->partial_blocks * bg::GUIDE_PARAMS * sizeof(float), ctx->stream) !=
+        cudaSuccess)
+        return bail(BG_ERR_CUDA);
     for (auto& e : g->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(ctx, BG_ERR_CUDA, "cudaEventCreate"));
     if (cudaMemsetAsync(g->step, 0, 64, ctx->stream) != cudaSuccess) return bail(BG_ERR_CUDA);
@@ -398,19 +410,24 @@ bg_status bg_guide_gradient(bg_guide* g, const float* samples, size_t n, float* 
         cudaMemsetAsync(g->stats, 0, 2 * sizeof(float), ctx->stream);
         const bg::PoolOrder order{(uint32_t)n, 1u, 0u, 0u};
         bg::launch_guide_wsum(ds, order, (uint32_t)n, g->wsum, ctx->stream);
-        bg::GuideTrainArgs a{};
-        a.wpack = g->wpack;
-        a.samples = ds;
-        a.order = order;
-        a.base = 0;
-        a.n = (uint32_t)n;
-        a.wsum = g->wsum;
-        a.alpha = g->o.alpha;
-        a.grad = g->grad;
-        a.stats = g->stats;
-        a.step = nullptr;
-        a.err = ctx->d_err;
-        bg::launch_guide_train(a, ctx->stream);
+        // in chunks of the partial buffer's batch; every chunk's gradient adds into g->grad
+        const uint32_t chunk = g->partial_blocks * 128;
+        for (uint32_t base = 0; base < (uint32_t)n; base += chunk) {
+            bg::GuideTrainArgs a{};
+            a.wpack = g->wpack;
+            a.samples = ds;
+            a.order = order;
+            a.base = base;
+            a.n = std::min<uint32_t>(chunk, (uint32_t)n - base);
+            a.wsum = g->wsum;
+            a.alpha = g->o.alpha;
+            a.partial = g->partial;
+            a.grad = g->grad;
+            a.stats = g->stats;
+            a.step = nullptr;
+            a.err = ctx->d_err;
+            bg::launch_guide_train(a, ctx->stream);
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) st = cuda_fail(ctx, e, "k_guide_train");
     }
@@ -507,6 +524,7 @@ bg_status bg_guide_time(bg_guide* g, const float* samples, size_t n, const float
             a.n = nb;
             a.wsum = g->wsum;
             a.alpha = g->o.alpha;
+            a.partial = g->partial;
             a.grad = g->grad;
             a.stats = g->stats;
             a.step = g->step;
@@ -692,7 +710,7 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
                 g->n_plain += 1;
             }
         }
-        if (guided && allow_fallback && g->n_plain >= 1 && g->n_guided >= bg_guide::kWindow / 2) {
+        if (guided && allow_fallback && g->n_plain >= 1 && g->n_guided >= 2 * bg_guide::kWindow) {
             const uint32_t k = std::min(g->n_guided, bg_guide::kWindow);
             double a = 0, b = 0;
             for (uint32_t i = 0; i < k; ++i) {

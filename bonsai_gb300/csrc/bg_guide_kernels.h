@@ -31,7 +31,9 @@ struct GuideTrainArgs {
     uint32_t n;              // samples in this batch (rows past n are zero-weight)
     const float* wsum;       // sums of the batch's weights of head 0 and head 1 (two device floats)
     float alpha;             // loss blend, see guide_loss_grad
-    float* grad;             // FP32 gradient accumulator (GUIDE_PARAMS)
+    float* partial;          // per-CTA gradient slices (>= ceil(n / 128) * GUIDE_PARAMS floats; entries
+                             // of unused rows stay as they are: keep them zero)
+    float* grad;             // FP32 gradient accumulator (GUIDE_PARAMS): += the sum of the slices
     float* stats;            // [0] += loss, [1] += samples with weight > 0
     uint32_t* step;          // Adam step counter, incremented once per launch (null: gradient only)
     uint32_t* err;           // error word
@@ -48,6 +50,8 @@ struct GuideAdam {
 constexpr int GUIDE_MAX_RANGES = 3;
 void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* counts, uint32_t nranges,
                         uint32_t stride, float* out, bool mixture, uint32_t* err, int sms, cudaStream_t s);
+// Forward + backward of a.n samples (one CTA per 128) and the reduction of their partial
+// gradients into a.grad (two launches).
 void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s);
 void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
                        const GuideAdam& h, cudaStream_t s);

@@ -82,6 +82,17 @@ BG_D bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitLimit
     }
 }
 
+// Bulk copy (TMA, no tensor map) of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// global to this CTA's shared memory, completing on `bar`: the issuing thread first raises the
+// barrier's expected transaction count, then starts the copy.
+BG_D void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 BG_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 BG_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 // Makes generic-proxy shared-memory writes visible to the tensor core (async proxy).

@@ -544,8 +544,8 @@ bg_status bg_guide_mixture_eval(bg_guide* guide, const float* raw, const float* 
  * warmup_passes passes rendered with this network sample the BSDF and gather training data; later
  * passes sample the guide mixture and keep training after every pass.  Unless
  * BG_GUIDE_NO_FALLBACK is set, guiding stops for good (plain BSDF sampling, no training) once
- * its relative variance per sample times pass time, averaged over the last 8 guided passes, is
- * not lower than that of the unguided passes.  Warm-up count, fallback and the variance
+ * its relative variance per sample times pass time, averaged over the last 32 guided passes
+ * (checked from the 64th guided pass on), is not lower than that of the unguided passes.  Warm-up count, fallback and the variance
  * estimates persist in the guide across calls, so a long render can be issued in chunks (with
  * BG_RENDER_ACCUMULATE and increasing first_sample).  Film, flags and rgb_out as in bg_render;
  * guide_stats counts this call's passes and reports the running estimates.  The path integrator
