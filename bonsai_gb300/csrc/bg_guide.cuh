@@ -123,49 +123,59 @@ BG_D V3 guide_sample(const VmfMix& m, float u0, float u1, float u2) {
     return vmf_sample_lobe(mu, kappa, u1, u2);
 }
 
-// Parsed mixture of one head (41 raw outputs) as stored by the render-side inference
-// (GUIDE_MIX_HEAD floats).
-BG_D void guide_write_mixture(const float* raw, float* out) {
-    const VmfMix m = guide_parse(raw);
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES; ++i) {
-        out[4 * i] = m.mu[i].x;
-        out[4 * i + 1] = m.mu[i].y;
-        out[4 * i + 2] = m.mu[i].z;
-        out[4 * i + 3] = m.kappa[i];
-        out[32 + i] = m.logc[i];
-        out[40 + i] = m.w[i];
-    }
-    out[48] = m.c;
-    out[49] = out[50] = out[51] = 0.0f;
+// Concentration and mean direction of a stored lobe b = kappa mu, with every operation rounded as
+// written: the inference epilogue and the shade kernels (compiled with and without contraction)
+// derive bit-identical values, so the density the sampler draws from is the one the pdf evaluates.
+BG_D float mix_kappa(float4 l) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(l.x, l.x), __fmul_rn(l.y, l.y)), __fmul_rn(l.z, l.z)));
 }
 
-// Read-only view of one head's stored mixture: lobes are loaded as they are needed, so a kernel does not
-// keep the whole mixture in registers.  Same arithmetic as guide_pdf / guide_sample.
+// Mixture record of one head (41 raw outputs) as stored by the render-side inference
+// (GUIDE_MIX_HEAD floats): per lobe b = kappa mu and a = log w + log c(kappa) - kappa, with kappa
+// re-derived from the stored b (mix_kappa), then the running lobe-weight sums and c.
+BG_D void guide_write_mixture(const float* raw, float* out) {
+    const VmfMix m = guide_parse(raw);
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        float4 l = make_float4(m.kappa[i] * m.mu[i].x, m.kappa[i] * m.mu[i].y, m.kappa[i] * m.mu[i].z, 0.0f);
+        const float k = mix_kappa(l);
+        l.w = __logf(m.w[i]) + vmf_log_norm(k, __logf(k)) - k;
+        out[4 * i] = l.x;
+        out[4 * i + 1] = l.y;
+        out[4 * i + 2] = l.z;
+        out[4 * i + 3] = l.w;
+        acc += m.w[i];
+        if (i < GUIDE_LOBES - 1) out[32 + i] = acc;
+    }
+    out[39] = m.c;
+}
+
+// Read-only view of one head's stored mixture: lobes are loaded as they are needed, so a kernel
+// does not keep the whole mixture in registers.  pdf(w) = sum_i exp(a_i + b_i . w).
 struct MixView {
     const float* m;
-    BG_D float c() const { return m[48]; }
+    BG_D float c() const { return m[39]; }
     BG_D float pdf(V3 w) const {
         float p = 0.0f;
-#pragma unroll 2
+#pragma unroll 4
         for (int i = 0; i < GUIDE_LOBES; ++i) {
             const float4 l = *reinterpret_cast<const float4*>(m + 4 * i);
-            p += m[40 + i] * __expf(m[32 + i] + l.w * (dot(v3(l.x, l.y, l.z), w) - 1.0f));
+            p += __expf(l.w + l.x * w.x + l.y * w.y + l.z * w.z);
         }
         return p;
     }
     BG_D V3 sample(float u0, float u1, float u2) const {
         int k = GUIDE_LOBES - 1;
-        float acc = 0.0f;
-        for (int i = 0; i < GUIDE_LOBES - 1; ++i) {
-            acc += m[40 + i];
-            if (u0 < acc) {
+        for (int i = 0; i < GUIDE_LOBES - 1; ++i)
+            if (u0 < m[32 + i]) {
                 k = i;
                 break;
             }
-        }
         const float4 l = *reinterpret_cast<const float4*>(m + 4 * k);
-        return vmf_sample_lobe(v3(l.x, l.y, l.z), l.w, u1, u2);
+        const float kap = mix_kappa(l);
+        const V3 mu = v3(__fdiv_rn(l.x, kap), __fdiv_rn(l.y, kap), __fdiv_rn(l.z, kap));
+        return vmf_sample_lobe(mu, kap, u1, u2);
     }
 };
 

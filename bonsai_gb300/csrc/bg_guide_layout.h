@@ -35,10 +35,11 @@ constexpr int GUIDE_PARAMS = 4 * GUIDE_HID * GUIDE_K + GUIDE_OUT_ROWS * GUIDE_K;
 constexpr uint32_t GUIDE_ROWGROUP_BYTES = 8 * GUIDE_K * 2;                      // 1280
 constexpr uint32_t GUIDE_WPACK_BYTES = (4 * GUIDE_HID + GUIDE_OUT_ROWS) * GUIDE_K * 2;  // 56,320
 constexpr int GUIDE_RAW_STRIDE = 96;  // floats per query in the raw output buffer
-// Parsed mixture record of one head (floats): lobe i at 4i = mean direction xyz, kappa; 32 + i =
-// log normalisation; 40 + i = weight; 48 = c; padded to 52.  The render-side inference writes both
-// heads per query (continuation head first).
-constexpr int GUIDE_MIX_HEAD = 52;
+// Mixture record of one head as the render-side inference stores it (floats): lobe i at 4i =
+// kappa * mean direction (xyz) and log(weight) + log(normalisation) - kappa, so that the density is
+// sum_i exp(m[4i+3] + m[4i..4i+2] . w); 32 + i (i < 7) = running sum of the lobe weights; 39 = c.
+// Both heads per query (continuation head first).
+constexpr int GUIDE_MIX_HEAD = 40;
 constexpr int GUIDE_MIX_STRIDE = GUIDE_HEADS * GUIDE_MIX_HEAD;  // 104
 constexpr int GUIDE_QUERY_F4 = 3;     // query = 3 float4: p.xyz n.x | n.yz wo.xy | wo.z - - -
 // training sample = query + wi.xyz (f2.yzw) + p_bsdf, indirect weight, direct weight (f3.xyz)

@@ -25,7 +25,6 @@ namespace bg {
 
 // ================================================================ ray queries
 struct TraceSrc {
-    static constexpr bool kFinishWarp = false;
     const float4* rays;
     int2* hits;
     uint8_t* occ;
@@ -236,11 +235,7 @@ __global__ void k_prepare(WaveBuffers wb, uint32_t bounce) {
     }
 }
 
-// Closest-hit rays of the extension queue.  BIN: a finished ray's path is also appended to its
-// material class queue (what k_bin does in a separate pass), while the warp is still together.
-template <bool BIN = false>
 struct ExtendSrc {
-    static constexpr bool kFinishWarp = BIN;
     const uint32_t* q;
     WaveBuffers wb;
     const SceneRender* tab;
@@ -251,34 +246,20 @@ struct ExtendSrc {
     }
     BG_D const Scene* scene(uint32_t i) const { return &tab[wb.scene_id[q[i]]].sc; }
     BG_D void store(uint32_t i, int prim, float t) const { wb.hit[q[i]] = make_int2(prim, __float_as_int(t)); }
-    BG_D void finish_warp(const Scene& sc, uint32_t i, int prim, bool fin) const {
-        int cls = -1;
-        uint32_t slot = 0;
-        if (fin) {
-            slot = q[i];
-            cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
-        }
-#pragma unroll
-        for (int c = 0; c < NCLS; ++c) {
-            const uint32_t pos = warp_append(&wb.counters[C_CLS + c], cls == c);
-            if (cls == c) wb.cls_queue[(size_t)c * wb.capacity + pos] = slot;
-        }
-    }
 };
 
-// BIN: the 8-wide traversal also bins the finished rays by material class (k_bin's work).
-template <int LAYOUT, bool MULTI = false, bool BIN = false>
+template <int LAYOUT, bool MULTI = false>
 __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_extend(Scene sc, WaveBuffers wb, uint32_t bounce, uint32_t* err,
                                                 int refill, const SceneRender* tab, bool sorted) {
     const uint32_t n = wb.counters[bounce & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&wb.ray_stats[0], (unsigned long long)n);
-    ExtendSrc<BIN && LAYOUT == 8> src{sorted ? wb.qsort : wb.queue[bounce & 1], wb, tab};
+    ExtendSrc src{sorted ? wb.qsort : wb.queue[bounce & 1], wb, tab};
 #if BG_SMEM_STACK
     __shared__ uint2 stack8[LAYOUT == 8 ? STACK8 * 128 : 1];
 #else
     uint2* stack8 = nullptr;
 #endif
-    if (LAYOUT == 8) traverse_queue8<false, decltype(src), MULTI>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
+    if (LAYOUT == 8) traverse_queue8<false, ExtendSrc, MULTI>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill, stack8);
     else traverse_queue<false>(sc, n, &wb.counters[C_EXT_HEAD], src, err, refill);
 }
 
@@ -422,7 +403,6 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
 }
 
 struct ShadowSrc {
-    static constexpr bool kFinishWarp = false;
     WaveBuffers wb;
     const SceneRender* tab;
     BG_D const Scene* scene(uint32_t i) const { return &tab[wb.scene_id[wb.sh_ref[i] >> 1]].sc; }
@@ -496,22 +476,17 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_sort_scatter<<<ls.sms * 4, 256, 0, s>>>(wb, rp, b);
             launches += 3;
         }
+        if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
+        else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
         const bool queries = guided && b < rp.max_depth;
         if (queries) {
             // every hit of a guidable class queues its network query; the network's mixtures are
             // ready before the shade launches
-            if (sc.nodes8) k_extend<8><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
-            else k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
             k_bin<false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, true);
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_CLS], 3, gw.cap, gw.raw, true, err, ls.sms, s);
-            launches += 2;
-        } else if (sc.nodes8) {
-            // the 8-wide traversal bins the finished rays itself
-            k_extend<8, false, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
-        } else {
-            k_extend<2><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, nullptr, sorted);
-            k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
             launches += 1;
+        } else {
+            k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         }
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
         if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s);
@@ -522,7 +497,7 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
         if (gw.flags) k_finalize<false, true><<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
         else k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
-        launches += 4;  // prepare, extend, shadow, finalize
+        launches += 5;
     }
     return launches;
 }
@@ -546,11 +521,12 @@ int launch_wave_batch(const SceneRender* tab, uint32_t nscenes, uint32_t max_dep
     int launches = 1;
     for (uint32_t b = 0; b <= max_depth; ++b) {
         k_prepare<<<1, 32, 0, s>>>(wb, b);
-        k_extend<8, true, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab, false);  // bins as well
+        k_extend<8, true><<<grid, block, 0, s>>>(sc, wb, b, err, ls.refill, tab, false);
+        k_bin<true><<<grid, block, 0, s>>>(sc, wb, b, tab);
         launch_shade_batch(tab, wb, b, err, grid, block, s, variants != 0);
         k_shadow<8, true><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, tab);
         k_finalize<true><<<grid, block, 0, s>>>(sc, film, wb, gw, tab);
-        launches += 9;
+        launches += 10;
     }
     return launches;
 }

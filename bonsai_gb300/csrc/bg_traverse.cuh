@@ -552,9 +552,6 @@ BG_D int bvh8_traverse(const Scene& sc, Ray& ray, uint32_t* err, int skip = -1) 
 // The node-group stack lives in local memory (BG_SMEM_STACK: shared memory, entry k of thread t at
 // smem[k * blockDim.x + t]).
 // MULTI: rays of different scenes share the queue; src.scene(i) gives the scene of ray i.
-// Src::kFinishWarp: when any lane of the warp finishes a ray, every lane calls
-// src.finish_warp(scene, i, hit, finished) once (warp-convergent, so the source can append the
-// finished rays to queues with warp ballots) before src.store.
 template <bool ANY, class Src, bool MULTI = false>
 BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src, uint32_t* err, int refill,
                           uint2* smem) {
@@ -609,10 +606,10 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
             }
         }
         if (__ballot_sync(0xffffffffu, busy) == 0) break;
-        if (!Src::kFinishWarp && !busy) continue;
+        if (!busy) continue;
         bool done = false;
         // node step: the next child of the node group (room for two pushes when primitives wait)
-        if (busy && ngroup.y > 0x00FFFFFFu && ((tgroup.y & 0xFFu) == 0 || sp + 2 <= STACK8)) {
+        if (ngroup.y > 0x00FFFFFFu && ((tgroup.y & 0xFFu) == 0 || sp + 2 <= STACK8)) {
             const uint32_t hits = ngroup.y;
             const uint32_t bit = 31u - __clz(hits);
             ngroup.y &= ~(1u << bit);
@@ -643,7 +640,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
             }
         }
         // primitive step: one primitive of the pending group
-        if (busy && (tgroup.y & 0xFFu)) {
+        if (tgroup.y & 0xFFu) {
             const uint32_t pi = next_leaf_prim(tgroup);
             if (pi >= S().ntri + S().nsph + S().nquad) {
                 atomicOr(err, ERR_BAD_PRIM);
@@ -656,7 +653,7 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
             }
         }
         // next groups: a node group from the stack; a primitive group only when none is pending
-        if (busy && !done && ngroup.y <= 0x00FFFFFFu) {
+        if (!done && ngroup.y <= 0x00FFFFFFu) {
             while (sp > 0) {
                 const uint2 g = stack[sstride * (sp - 1)];
                 if (g.y > 0x00FFFFFFu) {
@@ -669,9 +666,6 @@ BG_D void traverse_queue8(const Scene& sc, uint32_t n, uint32_t* head, Src& src,
                 --sp;
             }
             if (ngroup.y <= 0x00FFFFFFu && (tgroup.y & 0xFFu) == 0 && sp == 0) done = true;
-        }
-        if constexpr (Src::kFinishWarp) {
-            if (__any_sync(0xffffffffu, done)) src.finish_warp(S(), idx, hit, done);
         }
         if (done) {
             src.store(idx, hit, ray.t_max);

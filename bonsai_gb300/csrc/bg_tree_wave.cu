@@ -60,7 +60,6 @@ __global__ void k_tw_prep(TreeWave tw, uint32_t d) {
 }
 
 struct TwExtSrc {
-    static constexpr bool kFinishWarp = false;
     TreeWave tw;
     uint32_t b;
     BG_D Ray load(uint32_t i, int* skip) const {
@@ -87,7 +86,6 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_tw_extend(Scene sc, TreeW
 
 
 struct TwShadowSrc {
-    static constexpr bool kFinishWarp = false;
     TreeWave tw;
     BG_D Ray load(uint32_t i, int* skip) const {
         const float4 o = tw.sh_o[i], dd = tw.sh_d[i];

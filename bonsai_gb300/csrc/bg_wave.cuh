@@ -439,9 +439,13 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
 #ifndef BG_SHADE_MINBLOCKS
 #define BG_SHADE_MINBLOCKS 4
 #endif
-// The guided variants hold the mixture view and eight more uniforms: they are compiled for 3 CTAs.
+// The guided variants hold the mixture views and eight more uniforms; they are compiled for
+// BG_GUIDED_SHADE_MINBLOCKS CTAs per SM (4: matte, plastic and conductor spill 36, 32, 44 bytes).
+#ifndef BG_GUIDED_SHADE_MINBLOCKS
+#define BG_GUIDED_SHADE_MINBLOCKS 4
+#endif
 template <int CLS, bool MULTI = false, bool GWK = false, bool TEX = false, bool INF = false, bool SHL = INF>
-__global__ void __launch_bounds__(128, GWK ? 3 : BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
+__global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHADE_MINBLOCKS) k_shade(Scene sc0, RenderParams rp0, FilmBuffers film0, WaveBuffers wb,
                                                GuideWave gw, uint32_t bounce, uint32_t* err, const SceneRender* tab) {
     constexpr bool GUIDABLE = CLS >= 0 && CLS <= 2;
     const uint32_t n = wb.counters[C_CLS + CLS];
