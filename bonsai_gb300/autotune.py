@@ -40,7 +40,7 @@ def _gpu_name() -> str:
 
 def key_of(sd, spp: int) -> str:
     c = sd.camera
-    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}|v2"
+    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}|v3"
 
 
 def get(ctx) -> A.bg_tuning:
@@ -83,23 +83,30 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
     cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22, "sort_rays": 0}
     trials = []
 
-    def run(cfg):
+    def run(cfg, tspp):
         set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"], cfg["sort_rays"])
         integrator.render(scene, readback=False, spp=1)  # allocate / warm
-        ms = _trial(ctx, scene, integrator, spp)
-        trials.append(dict(cfg, ms=ms))
+        ms = _trial(ctx, scene, integrator, tspp)
+        trials.append(dict(cfg, ms=ms, spp=tspp))
         if verbose:
             print("autotune", cfg, f"{ms:.2f} ms")
         return ms
 
-    best_ms = run(cur)
+    # a wave larger than a trial's paths changes nothing, so wave sizes are compared on trials of at
+    # least two of the largest waves (otherwise the choice among them is noise)
+    npix = sd.camera.width * sd.camera.height
+    wave_spp = max(spp, -(-2 * max(WAVES) // npix))
+    best_ms = float("inf")
     for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES), ("sort_rays", SORT)):
+        tspp = wave_spp if name == "wave_paths" else spp
+        best_ms = run(cur, tspp)
         for v in values:
             if v == cur[name]:
                 continue
             cfg = dict(cur, **{name: v})
-            ms = run(cfg)
-            if ms < best_ms:
+            ms = run(cfg, tspp)
+            # a larger wave wins ties within 0.5% (fewer wave tails at the render's full spp)
+            if ms < best_ms * (0.995 if name != "wave_paths" or v < cur[name] else 1.005):
                 best_ms, cur = ms, cfg
     set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"], cur["sort_rays"])
     result = dict(cur, ms=best_ms, trials=trials)
