@@ -67,6 +67,8 @@ def parse():
     p.add_argument("--guide-warmup", type=int, default=8, help="guiding: unguided training passes")
     p.add_argument("--pass-paths", type=int, default=1 << 22, help="guiding: paths per pass")
     p.add_argument("--epochs", type=int, default=4, help="guiding: training epochs over each pass's pool")
+    p.add_argument("--guided-scenes", type=int, default=8, help="batch: scenes of the guided arm (0 = none)")
+    p.add_argument("--guided-train-passes", type=int, default=64, help="batch: training passes per guided scene")
     return p.parse_args()
 
 
@@ -476,9 +478,13 @@ def run_profile(args):
     launch list and kernel captures run on (a few GB on the device, BVH larger than L2)."""
     from bonsai_gb300 import _abi as A
     from bonsai_gb300 import gpu as G
+    from bonsai_gb300 import autotune
     sd = workload(False)
     ctx = G.Context(0)
     scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    # the launch shape the autotuner picks for the production bench on a GB300 (refill 8, 16 CTAs
+    # per SM, 16M-path waves)
+    autotune.set_(ctx, 8, 16, 1 << 24)
     pi = G.PathIntegrator(sd.camera, args.profile_spp, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT)
     r = pi.render(scene, readback=False)
     print(json.dumps({"profile_case": True, "spp": args.profile_spp, "device_ms": r.stats.device_ms,
@@ -811,7 +817,13 @@ def run_batch(args):
     """Uneven multi-scene batch: 256 seeded scenes (1k..500k triangles, 128^2..512^2 / 640x360,
     4..64 spp, depth 4..10) rendered by bg_render_batch, whose paths of all scenes share one
     wavefront; value = aggregate Msamples/s of the batch (device time, L2 flushed before every step).
-    Compared with rendering the same scenes one after another through bg_render (graph-captured)."""
+    Compared with rendering the same scenes one after another through bg_render (graph-captured),
+    for all scenes and for the small ones (<= 256^2 pixels, <= 16 spp).  Time to relMSE 1e-3 per
+    scene from each scene's relative variance per sample (batch film moments) and its measured
+    one-at-a-time rate, and for the whole batch at its aggregate rate.  Guided arm: --guided-scenes
+    scenes spread over the batch's sizes, each with its own network trained online
+    (--guided-train-passes passes), then time to target = relvar x ms per spp of the frozen network
+    against the plain render of the same scene."""
     from bonsai_gb300 import _abi as A
     from bonsai_gb300 import gpu as G
     from bonsai_gb300 import scenes as S
@@ -842,13 +854,84 @@ def run_batch(args):
         imgs, _ = G.render_batch(ctx, jobs, readback=True)
     e2e = args.steps * samples / (time.time() - t0) / 1e6
     d2h = sum(im.nbytes for im in imgs)
+    # per-scene relative variance per sample (relMSE denominator as in the guiding workload) from the
+    # batch film's moments: relMSE after n samples per pixel = relvar / n
+    G.render_batch(ctx, jobs, readback=False)
+    npix = [sd.camera.width * sd.camera.height for sd in sds]
+    s1, s2, cnt = G.PathIntegrator.moments(ctx, sum(npix), 1)
+    s1, s2, cnt = s1.reshape(-1, 3), s2.reshape(-1, 3), cnt.reshape(-1, 1).astype(np.float64)
+    m = s1 / cnt
+    var = np.maximum(s2 / cnt - m * m, 0.0)
+    relvar, p0 = [], 0
+    for n in npix:
+        relvar.append(float(np.mean(var[p0:p0 + n] / (m[p0:p0 + n] ** 2 + 1e-2))))
+        p0 += n
+    spp_target = [rv / args.target for rv in relvar]
     # the same scenes one render at a time (graph-captured wavefront per scene)
     seq_ms = 0.0
+    seq_each = []
     ctx.flush_l2()
     for j in jobs:
         pi = G.PathIntegrator(j.camera, j.spp, j.max_depth, mode=A.BG_MODE_PBRT, seed=j.seed)
         pi.render(j.scene, readback=False, graph=True)  # capture
-        seq_ms += pi.render(j.scene, readback=False, graph=True).stats.device_ms
+        ms = pi.render(j.scene, readback=False, graph=True).stats.device_ms
+        seq_ms += ms
+        seq_each.append(ms)
+    batch_rate = samples / (dev_ms / args.steps / 1e3)
+    # time to relMSE 1e-3 in every scene: one batch delivering every scene's samples to the target
+    # at the batch's aggregate rate, against one-at-a-time renders at each scene's measured rate
+    tt_batch = sum(st * n for st, n in zip(spp_target, npix)) / batch_rate
+    tt_seq_each = [st * ms / 1e3 / j.spp for st, ms, j in zip(spp_target, seq_each, jobs)]
+    # the small scenes (<= 256 x 256 pixels and <= 16 spp), where a one-scene render cannot fill the GPU
+    small = [k for k, sd in enumerate(sds) if npix[k] <= 256 * 256 and sd.spp <= 16]
+    small_res = None
+    if small:
+        sjobs = [jobs[k] for k in small]
+        ssamples = sum(npix[k] * sds[k].spp for k in small)
+        G.render_batch(ctx, sjobs, readback=False)
+        sms = 0.0
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            sms += G.render_batch(ctx, sjobs, readback=False)[1].device_ms
+        sms /= args.steps
+        sseq = sum(seq_each[k] for k in small)
+        small_res = {"scenes": len(small), "samples": ssamples, "batch_ms": sms, "sequential_ms": sseq,
+                     "batch_msamples_per_s": ssamples / (sms / 1e3) / 1e6,
+                     "sequential_msamples_per_s": ssamples / (sseq / 1e3) / 1e6,
+                     "batch_over_sequential": sseq / sms}
+    # guided arm on a spread of scenes: each scene's guide trains online, then its frozen network
+    # renders the scene's spp; time to target = relvar / target x ms per spp, against plain
+    guided = []
+    if args.guided_scenes > 0:
+        order = sorted(range(nsc), key=lambda k: npix[k] * sds[k].spp)
+        picks = [order[int(i * (nsc - 1) / max(args.guided_scenes - 1, 1))] for i in range(args.guided_scenes)]
+        for k in picks:
+            j, sd = jobs[k], sds[k]
+            pi = G.PathIntegrator(j.camera, j.spp, j.max_depth, mode=A.BG_MODE_PBRT, seed=j.seed)
+            g = G.Guide(ctx, learning_rate=1e-3, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=4,
+                        pass_paths=1 << 22, epochs=2, no_fallback=True)
+            pass_spp = max(1, (1 << 22) // npix[k])
+            r = pi.render_guided(j.scene, g, spp=pass_spp * args.guided_train_passes, first_sample=1 << 22,
+                                 readback=False)
+            fz = G.Guide(ctx, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=0, pass_paths=1 << 22,
+                         no_fallback=True, no_train=True)
+            fz.params = g.params
+            rg = pi.render_guided(j.scene, fz, spp=j.spp, first_sample=0, readback=False)
+            g1, g2, gn = G.PathIntegrator.moments(ctx, sd.camera.width, sd.camera.height)
+            gn = gn[..., None].astype(np.float64)
+            gm = g1 / gn
+            rv_g = float(np.mean(np.maximum(g2 / gn - gm * gm, 0.0) / (gm ** 2 + 1e-2)))
+            ms_g = rg.stats.device_ms / j.spp
+            ms_p = seq_each[k] / j.spp
+            guided.append({"scene": k, "pixels": npix[k], "spp": j.spp, "triangles": sd.ntri,
+                           "relvar_plain": relvar[k], "relvar_guided": rv_g,
+                           "ms_per_spp_plain": ms_p, "ms_per_spp_guided": ms_g,
+                           "time_to_target_plain_s": relvar[k] / args.target * ms_p / 1e3,
+                           "time_to_target_guided_s": rv_g / args.target * ms_g / 1e3,
+                           "guided_over_plain_time": (rv_g * ms_g) / (relvar[k] * ms_p) if relvar[k] > 0 else None,
+                           "training_s": (r.guide.render_ms + r.guide.train_ms) / 1e3})
+            fz.close()
+            g.close()
     print(json.dumps({
         "metric": "Msamples/s (uneven batch)", "value": value, "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -861,6 +944,15 @@ def run_batch(args):
         "gpu_launches": launches,
         "sequential_msamples_per_s": samples / (seq_ms / 1e3) / 1e6,
         "batch_over_sequential": (samples / (dev_ms / args.steps / 1e3)) / (samples / (seq_ms / 1e3)),
+        "small_scenes": small_res,
+        "time_to_relmse": {"target": args.target,
+                           "definition": "relMSE after n spp = relvar / n, relvar = mean over pixels and channels of "
+                                         "var / (mean^2 + 0.01) from the batch film's moments",
+                           "all_scenes_batch_s": tt_batch, "all_scenes_sequential_s": sum(tt_seq_each),
+                           "per_scene": [{"scene": k, "pixels": npix[k], "spp": sds[k].spp, "triangles": sds[k].ntri,
+                                          "relvar": round(relvar[k], 4), "spp_to_target": round(spp_target[k], 1),
+                                          "sequential_s": round(tt_seq_each[k], 4)} for k in range(nsc)]},
+        "guided_scenes": guided,
         "scene_generation_s": gen_s, "upload_and_bvh_build_s": build_s, "clocks": clk}), flush=True)
     for sc in scenes:
         sc.close()
