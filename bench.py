@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--target", type=float, default=1e-3, help="guiding: relMSE target")
     p.add_argument("--guide-warmup", type=int, default=8, help="guiding: unguided training passes")
     p.add_argument("--pass-paths", type=int, default=1 << 22, help="guiding: paths per pass")
-    p.add_argument("--epochs", type=int, default=4, help="guiding: training epochs over each pass's pool")
+    p.add_argument("--epochs", type=int, default=2, help="guiding: training epochs over each pass's pool")
     p.add_argument("--guided-scenes", type=int, default=8, help="batch: scenes of the guided arm (0 = none)")
     p.add_argument("--guided-train-passes", type=int, default=64, help="batch: training passes per guided scene")
     return p.parse_args()
@@ -636,6 +636,8 @@ def run_guiding(args):
     ref_var_term = float(np.mean(np.maximum(ref2 - ref * ref, 0.0) / refn / (ref ** 2 + 1e-2)))
     ref_s = time.time() - t0
 
+    moments_est = {}
+
     def progressive(render_chunk, label):
         curve, t_dev, t_wall, spp, c = [], 0.0, 0.0, 0, 4
         while True:
@@ -644,12 +646,16 @@ def run_guiding(args):
             t_wall += time.time() - w0
             t_dev += st.device_ms / 1e3
             spp += c
-            img = mean_image()[0]
+            img, img2, n = mean_image()
             e = _relmse(img, ref, ref_var_term)
             curve.append((t_dev, e, t_wall, spp))
             if e < args.target / 1.5 or t_dev > args.arm_seconds:
                 break
             c = max(4, int(c * 1.3))
+        # the arm's own estimate of its relMSE (per-pixel sample variance of the mean, no reference),
+        # extrapolated to the target as ~ 1/t
+        own = float(np.mean(np.maximum(img2 - img * img, 0.0) / n / (ref ** 2 + 1e-2)))
+        moments_est[label] = {"relmse_from_own_variance": own, "time_to_target_s": t_dev * own / args.target}
         return curve
 
     def plain_chunk(c, spp):
@@ -706,6 +712,8 @@ def run_guiding(args):
         "guided": {"time_to_target_s": t_guided, "extrapolated": ext_g, "msamples_per_s": guided_rate,
                    "curve": [[round(t, 4), e] for t, e in gc], "stats": gstats},
         "guided_over_plain_time": t_guided / t_plain,
+        "from_own_variance": dict(moments_est, guided_over_plain_time=(
+            moments_est["guided"]["time_to_target_s"] / moments_est["plain"]["time_to_target_s"])),
         "equal_time": {"t_s": t_eq, "relmse_plain": _at_time(pc, t_eq) or pc[-1][1],
                        "relmse_guided": _at_time(gc, t_eq) or gc[-1][1]},
         "reference_render_s": ref_s, "reference_var_term": ref_var_term,

@@ -456,19 +456,21 @@ __global__ void k_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wp
 }
 
 // grad[i] += sum over the n CTAs' partial gradients (parameter i of slice b at b * GUIDE_PARAMS + i).
+// blockIdx.y takes every REDUCE_SPLIT-th slice, so REDUCE_SPLIT threads share a parameter (more
+// loads in flight than one thread walking all slices); they add into grad atomically.
+constexpr uint32_t REDUCE_SPLIT = 8;
 __global__ void k_guide_reduce(const float* __restrict__ partial, uint32_t n, float* grad) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint32_t)GUIDE_PARAMS) return;
-    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-    uint32_t b = 0;
-    for (; b + 4 <= n; b += 4) {
+    float s0 = 0.0f, s1 = 0.0f;
+    uint32_t b = blockIdx.y;
+    for (; b + REDUCE_SPLIT < n; b += 2 * REDUCE_SPLIT) {
         s0 += partial[(size_t)b * GUIDE_PARAMS + i];
-        s1 += partial[(size_t)(b + 1) * GUIDE_PARAMS + i];
-        s2 += partial[(size_t)(b + 2) * GUIDE_PARAMS + i];
-        s3 += partial[(size_t)(b + 3) * GUIDE_PARAMS + i];
+        s1 += partial[(size_t)(b + REDUCE_SPLIT) * GUIDE_PARAMS + i];
     }
-    for (; b < n; ++b) s0 += partial[(size_t)b * GUIDE_PARAMS + i];
-    grad[i] += (s0 + s1) + (s2 + s3);
+    if (b < n) s0 += partial[(size_t)b * GUIDE_PARAMS + i];
+    const float s = s0 + s1;
+    if (s != 0.0f) atomicAdd(&grad[i], s);
 }
 
 __global__ void k_guide_pack(const float* p, uint8_t* wpack) {
@@ -584,7 +586,7 @@ void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
     uint32_t grid = (a.n + 127) / 128;
     if (grid == 0) return;
     k_guide_train<<<grid, 128, TRAIN_SMEM, s>>>(a);
-    k_guide_reduce<<<(GUIDE_PARAMS + 255) / 256, 256, 0, s>>>(a.partial, grid, a.grad);
+    k_guide_reduce<<<dim3((GUIDE_PARAMS + 255) / 256, REDUCE_SPLIT), 256, 0, s>>>(a.partial, grid, a.grad);
 }
 
 void launch_guide_adam(float* p, float* m, float* v, float* g, uint8_t* wpack, const uint32_t* step,
