@@ -1,15 +1,15 @@
 // bg_guide_api.cpp - C ABI of the guiding network and the progressive guided render.
 //
-// bg_render_guided runs opts->spp passes of 1 spp; the network's warm-up count, fallback decision
+// bg_render_guided renders opts->spp samples in passes of max(1, pass_paths / pixels) spp; the network's warm-up count, fallback decision
 // and variance estimates carry over between calls, so a long render can be issued in chunks.  Per
-// pass: the wavefront renders the image (guided passes add the network inference and a second
-// shading launch per bounce whose next-event estimation draws its second strategy from the
-// mixture; the continuation stays a BSDF sample); the
-// paths' training records land in a pool of samples_per_pass samples (subsampled by a keep
-// probability set from the previous pass's record count); one reduction estimates the pass's
-// relative variance against the mean of the earlier passes; then the pool is consumed in
-// batch_size Adam steps.  One host synchronisation per pass reads the counters that steer the
-// next pass (keep probability, fallback decision).
+// pass: the wavefront renders the image (guided passes write a network query for every matte /
+// plastic / conductor hit while binning and infer the two mixtures of each before shading, where
+// the continuation head proposes the continuation and the next-event head the second strategy of
+// estimate_direct); paths chosen with a keep probability (set from the previous pass's record
+// count) write training records, which land in a pool of samples_per_pass samples; one reduction
+// estimates the pass's relative variance against the mean of the earlier passes; then the pool is
+// consumed in batch_size Adam steps.  One host synchronisation per pass reads the counters that
+// steer the next pass (keep probability, fallback decision).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -682,7 +682,9 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
         const uint32_t pool_n = std::min(ctr[1], g->pool_cap);
         g->pool_n = pool_n;
         gs.pool_samples += pool_n;
-        g->keep = ctr[0] > 0 ? std::min(1.0f, (float)g->pool_cap / (float)ctr[0]) : 1.0f;
+        // ctr[0] counts the positive records of the paths chosen with probability keep: scale the
+        // choice so that the next pass fills about pool_cap samples
+        g->keep = ctr[0] > 0 ? std::min(1.0f, (float)g->pool_cap * g->keep / (float)ctr[0]) : 1.0f;
         float train_ms = 0.0f;
         if (record && pool_n >= 128) {
             int nb = train_batches(g, g->pool, pool_n, g->o.epochs, &g->epochs_done);

@@ -111,7 +111,7 @@ constexpr uint32_t DIM_GUIDE0 = 4096;  // guided sampling uniforms: 8 per bounce
 struct GuideWave {
     uint32_t flags;
     uint32_t pool_cap;   // training samples the pool holds
-    float keep_prob;     // probability that a positive-weight record enters the pool
+    float keep_prob;     // probability that a path records training samples (all enter the pool)
     uint32_t cap;        // path slots the record / query buffers below hold (>= the wave's paths)
     float4 bmin, binv;   // position encoding: p_norm = (p - bmin) * binv
     float4* rec;         // GUIDE_MAXREC * GUIDE_REC_F4 * cap, [k][field][slot]

@@ -159,7 +159,8 @@ BG_D uint32_t open_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t s
     return (state & ~ST_REC_MASK) | ((k + 1) << ST_REC_SHIFT) | ST_REC_OPEN;
 }
 
-// Integer hash in [0, 1) for subsampling records into the training pool (not part of the estimator).
+// Integer hash in [0, 1) for choosing the paths that record training samples (not part of the
+// estimator).
 BG_D float hash_unit(uint32_t a, uint32_t b, uint32_t c) {
     uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
     h ^= h >> 15;
@@ -193,7 +194,7 @@ BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot
             if (!(r4.w > 0.0f && isfinite(r4.w))) r4.w = 0.0f;
             if (w > 0.0f || r4.w > 0.0f) {
                 ++positive;
-                keep = hash_unit(wb.pixel[slot], wb.sample[slot], k) < gw.keep_prob;
+                keep = true;  // the path was chosen for the pool when it opened its records
             }
         }
         uint32_t pos = warp_append(&gw.ctr[1], keep);
@@ -402,7 +403,10 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    if (GUIDABLE && record) state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, p_b, beta0);
+    // only the paths the pool samples record (a per-path choice with probability keep_prob, so the
+    // other paths write nothing); every positive-weight record of a chosen path enters the pool
+    if (GUIDABLE && record && hash_unit(wb.pixel[slot], wb.sample[slot], 0x5EEDu) < gw.keep_prob)
+        state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, p_b, beta0);
     out.cont = true;
 }
 
@@ -488,9 +492,10 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
             Isect it;
             bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
             const bool counted = bounce == 0 || specular_bounce;
-            RGB le = hit && (counted || record) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
+            const bool rec_open = record && (state & ST_REC_OPEN);
+            RGB le = hit && (counted || rec_open) ? emitted_radiance(sc, it, -ray.d) : rgb(0.0f);
             // an escaped ray gathers the infinite light's radiance (path.rs:78-85)
-            if (CLS == CLS_MISS && prim < 0 && (counted || record) && sc.inf) le = inf_radiance(sc, ray.d);
+            if (CLS == CLS_MISS && prim < 0 && (counted || rec_open) && sc.inf) le = inf_radiance(sc, ray.d);
             // The previous vertex's record closes here, with this emission as its direct target
             // (which the estimator leaves to that vertex's next-event estimation unless counted).
             if (record) state = close_record(gw, wb, slot, state, counted ? L + beta * le : L, beta * le);

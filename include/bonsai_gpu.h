@@ -500,7 +500,7 @@ typedef struct bg_guide_stats {
     double relvar_guided;    /* the same for guided passes                                     */
     double ms_plain;         /* mean device time of an unguided pass                           */
     double ms_guided;        /* mean device time of a guided pass incl. its training           */
-    uint64_t records;        /* positive-weight training records produced                      */
+    uint64_t records;        /* positive-weight training records of the recording paths         */
     uint64_t pool_samples;   /* of which entered the training pool                             */
 } bg_guide_stats;
 
