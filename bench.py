@@ -281,7 +281,7 @@ def run_ours(args):
     if not args.no_autotune:
         from bonsai_gb300 import autotune
         tuning = autotune.tune(ctx, scene, pi, spp=4)
-        tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "ms")} | {
+        tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "concurrent_shade", "ms")} | {
             "cached": bool(tuning.get("cached", False))}
     for _ in range(args.warmup):
         pi.render(scene, readback=False, graph=True)

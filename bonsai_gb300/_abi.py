@@ -43,6 +43,7 @@ BG_TUNE_SORT_RAYS = 1
 BG_TUNE_L2_PERSIST = 2
 BG_TUNE_TILE_PIXELS = 4
 BG_TUNE_SHADOW_QUEUE_HALF = 8
+BG_TUNE_CONCURRENT_SHADE = 16
 BG_SAMPLER_INDEPENDENT, BG_SAMPLER_STRATIFIED = 0, 1
 
 BG_TEXTURE_IMAGE = 0

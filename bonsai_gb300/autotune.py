@@ -6,6 +6,7 @@ library's CUDA events, L2 flushed before each trial):
   blocks_per_sm - persistent grid of the wavefront stages
   wave_paths    - paths per wave (queue capacity)
   sort_rays     - bin each bounce's extension rays by direction octant and origin cell
+  concurrent_shade - run a bounce's material-class shade kernels side by side
 The result is cached as JSON keyed by GPU name, scene signature and render settings
 (default ~/.cache/bonsai_gb300/tuning.json, or $BONSAI_TUNING_CACHE).
 """
@@ -20,8 +21,9 @@ from . import _abi as A
 
 REFILL = [32, 16, 8, 4]
 BLOCKS = [4, 8, 16]
-WAVES = [1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24]
+WAVES = [1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25]
 SORT = [0, 1]
+CONCURRENT = [1, 0]
 
 
 def cache_path() -> Path:
@@ -40,7 +42,7 @@ def _gpu_name() -> str:
 
 def key_of(sd, spp: int) -> str:
     c = sd.camera
-    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}|v3"
+    return f"{_gpu_name()}|tri{sd.ntri}|sph{sd.nsph}|{c.width}x{c.height}|depth{sd.max_depth}|spp{spp}|v4"
 
 
 def get(ctx) -> A.bg_tuning:
@@ -49,10 +51,11 @@ def get(ctx) -> A.bg_tuning:
     return t
 
 
-def set_(ctx, refill: int, blocks: int, wave: int, sort_rays: int = 0):
+def set_(ctx, refill: int, blocks: int, wave: int, sort_rays: int = 0, concurrent_shade: int = 1):
     t = A.bg_tuning()
     t.refill, t.blocks_per_sm, t.wave_paths = refill, blocks, wave
-    t.flags = (A.BG_TUNE_SORT_RAYS if sort_rays else 0) | A.BG_TUNE_TILE_PIXELS
+    t.flags = ((A.BG_TUNE_SORT_RAYS if sort_rays else 0) | A.BG_TUNE_TILE_PIXELS |
+               (A.BG_TUNE_CONCURRENT_SHADE if concurrent_shade else 0))
     ctx.check(ctx.lib.bg_set_tuning(ctx.h, C.byref(t)))
 
 
@@ -78,13 +81,13 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
             cache = {}
     if use_cache and key in cache:
         c = cache[key]
-        set_(ctx, c["refill"], c["blocks_per_sm"], c["wave_paths"], c.get("sort_rays", 0))
+        set_(ctx, c["refill"], c["blocks_per_sm"], c["wave_paths"], c.get("sort_rays", 0), c.get("concurrent_shade", 1))
         return dict(c, cached=True)
-    cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22, "sort_rays": 0}
+    cur = {"refill": 32, "blocks_per_sm": 8, "wave_paths": 1 << 22, "sort_rays": 0, "concurrent_shade": 1}
     trials = []
 
     def run(cfg, tspp):
-        set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"], cfg["sort_rays"])
+        set_(ctx, cfg["refill"], cfg["blocks_per_sm"], cfg["wave_paths"], cfg["sort_rays"], cfg["concurrent_shade"])
         integrator.render(scene, readback=False, spp=1)  # allocate / warm
         ms = _trial(ctx, scene, integrator, tspp)
         trials.append(dict(cfg, ms=ms, spp=tspp))
@@ -97,7 +100,8 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
     npix = sd.camera.width * sd.camera.height
     wave_spp = max(spp, -(-2 * max(WAVES) // npix))
     best_ms = float("inf")
-    for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES), ("sort_rays", SORT)):
+    for name, values in (("refill", REFILL), ("blocks_per_sm", BLOCKS), ("wave_paths", WAVES), ("sort_rays", SORT),
+                         ("concurrent_shade", CONCURRENT)):
         tspp = wave_spp if name == "wave_paths" else spp
         best_ms = run(cur, tspp)
         for v in values:
@@ -108,12 +112,13 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
             # a larger wave wins ties within 0.5% (fewer wave tails at the render's full spp)
             if ms < best_ms * (0.995 if name != "wave_paths" or v < cur[name] else 1.005):
                 best_ms, cur = ms, cfg
-    set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"], cur["sort_rays"])
+    set_(ctx, cur["refill"], cur["blocks_per_sm"], cur["wave_paths"], cur["sort_rays"], cur["concurrent_shade"])
     result = dict(cur, ms=best_ms, trials=trials)
     if use_cache:
         try:
             path.parent.mkdir(parents=True, exist_ok=True)
-            cache[key] = {k: result[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "ms")}
+            cache[key] = {k: result[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "concurrent_shade",
+                                                 "ms")}
             path.write_text(json.dumps(cache, indent=1))
         except OSError:
             pass

@@ -514,6 +514,12 @@ bg_status bg_create(const bg_device_opts* opts, bg_ctx** out) {
     if ((e = cudaGetDeviceProperties(&prop, ctx->device)) != cudaSuccess) return bail(e);
     ctx->shape.sms = prop.multiProcessorCount;
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    for (auto& st : ctx->fork.aux)
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&ctx->fork.fork, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    for (auto& ev : ctx->fork.join)
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    ctx->shape.fork = &ctx->fork;  // BG_TUNE_CONCURRENT_SHADE, on by default
     if ((e = cudaEventCreate(&ctx->ev_begin)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&ctx->ev_end)) != cudaSuccess) return bail(e);
     for (auto& ev : ctx->stage_ev)
@@ -551,6 +557,11 @@ void bg_destroy(bg_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     for (auto ev : ctx->timing_ev) cudaEventDestroy(ev);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    for (auto st : ctx->fork.aux)
+        if (st) cudaStreamDestroy(st);
+    if (ctx->fork.fork) cudaEventDestroy(ctx->fork.fork);
+    for (auto ev : ctx->fork.join)
+        if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -605,7 +616,8 @@ bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out) {
     out->refill = (uint32_t)ctx->shape.refill;
     out->flags = (ctx->shape.sort_rays ? BG_TUNE_SORT_RAYS : 0u) | (ctx->shape.l2_persist ? BG_TUNE_L2_PERSIST : 0u) |
                  (ctx->shape.tile_pixels ? BG_TUNE_TILE_PIXELS : 0u) |
-                 (ctx->shape.shadow_half ? BG_TUNE_SHADOW_QUEUE_HALF : 0u);
+                 (ctx->shape.shadow_half ? BG_TUNE_SHADOW_QUEUE_HALF : 0u) |
+                 (ctx->shape.fork ? BG_TUNE_CONCURRENT_SHADE : 0u);
     return BG_OK;
 }
 
@@ -621,6 +633,7 @@ bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t) {
     ctx->shape.l2_persist = (t->flags & BG_TUNE_L2_PERSIST) ? 1 : 0;
     ctx->shape.tile_pixels = (t->flags & BG_TUNE_TILE_PIXELS) ? 1 : 0;
     ctx->shape.shadow_half = (t->flags & BG_TUNE_SHADOW_QUEUE_HALF) ? 1 : 0;
+    ctx->shape.fork = (t->flags & BG_TUNE_CONCURRENT_SHADE) ? &ctx->fork : nullptr;
     return BG_OK;
 }
 

@@ -16,6 +16,7 @@ struct bg_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     uint64_t cap = 0, used = 0;
+    bg::ShadeFork fork{};           // streams / events of BG_TUNE_CONCURRENT_SHADE
     bg::LaunchShape shape{1, 128};
     uint32_t max_queue = 1u << 22;
     uint32_t* d_err = nullptr;

@@ -361,9 +361,13 @@ __global__ void __launch_bounds__(256) k_sort_scatter(WaveBuffers wb, RenderPara
 // shade launch runs one material's code with uniform control flow.  GWK (guided waves, queries
 // set): a hit of a guidable class (matte, plastic, conductor) also writes its network query at
 // class * gw.cap + its queue position, for the inference that runs before shading.
-template <bool MULTI = false, bool GWK = false>
+// FIN (single-scene waves whose light list has no infinite light): an escaped path has nothing
+// left to gather, so its sample goes to the film here (with its pending next-event contribution)
+// and the escaped-ray shade launch is skipped.
+template <bool MULTI = false, bool GWK = false, bool FIN = false>
 __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t bounce, const SceneRender* tab,
-                                             GuideWave gw = GuideWave{}, bool queries = false) {
+                                             GuideWave gw = GuideWave{}, bool queries = false,
+                                             FilmBuffers film = FilmBuffers{}) {
     const uint32_t n = wb.counters[bounce & 1];
     const uint32_t* q = wb.queue[bounce & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -376,6 +380,11 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
             int prim = wb.hit[slot].x;
             const Scene& sc = pick<MULTI>(sc0, MULTI ? &tab[wb.scene_id[slot]].sc : nullptr);
             cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
+            if (FIN && cls == CLS_MISS) {
+                const float4 l4 = wb.L[slot];
+                film_add(film, wb.pixel[slot], apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), wb.state[slot], sc0.nlights));
+                cls = -1;
+            }
         }
         uint32_t qpos = 0;
 #pragma unroll
@@ -485,12 +494,14 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_bin<false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, true);
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_CLS], 3, gw.cap, gw.raw, true, err, ls.sms, s);
             launches += 1;
+        } else if (!gw.flags && !sc.inf && !sc.sph_emis && !sc.quad_emis) {
+            k_bin<false, false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, false, film);
         } else {
             k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         }
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
         if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s);
-        else launches += launch_shade_plain(sc, rp, film, wb, b, err, grid, block, s);
+        else launches += launch_shade_plain(sc, rp, film, wb, b, err, grid, block, s, ls.fork);
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);

@@ -124,6 +124,14 @@ struct GuideWave {
     const uint8_t* wpack;  // BF16 weight image
 };
 
+// Streams and events that let a bounce's material-class shade kernels run side by side: forked
+// from the launching stream after binning and joined back before the shadow rays (also inside a
+// stream capture, where they become parallel graph branches).
+struct ShadeFork {
+    cudaStream_t aux[4];
+    cudaEvent_t fork, join[4];
+};
+
 struct LaunchShape {
     int sms;
     int block;
@@ -135,6 +143,7 @@ struct LaunchShape {
     // scanline order (extension 104.8 against 108.7 ms), Whitted 443 against 460 ms
     int tile_pixels = 1;
     int shadow_half = 0;  // BG_TUNE_SHADOW_QUEUE_HALF
+    const ShadeFork* fork = nullptr;  // BG_TUNE_CONCURRENT_SHADE: the context's shade streams
 };
 
 void launch_trace(const Scene& sc, bool ref_layout, bool any, const bg_ray* rays, size_t n, bg_hit* hits,

@@ -6,34 +6,50 @@
 namespace bg {
 
 int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                       uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
+                       uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s, const ShadeFork* fork) {
     const GuideWave gw{};
     if (sc.sph_emis || sc.quad_emis) return launch_shade_shapes(sc, rp, film, wb, b, err, grid, block, s);
-    if (sc.inf) {  // the light list holds the infinite light
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        if (sc.ntex) {
-            k_shade<0, false, false, true, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, false, true, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        } else {
-            k_shade<0, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-            k_shade<1, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    // classes share no data a kernel of another class reads (each shades its own queue's paths and
+    // appends to the next queues with atomics), so they may run side by side: matte (the largest
+    // class) on the launching stream, the others on the fork's streams
+    cudaStream_t st[NCLS] = {s, s, s, s, s};  // by class: matte, plastic, conductor, dielectric, misses
+    if (fork) {
+        cudaEventRecord(fork->fork, s);
+        for (int k = 0; k < 4; ++k) {
+            cudaStreamWaitEvent(fork->aux[k], fork->fork, 0);
+            st[1 + k] = fork->aux[k];
         }
-        k_shade<2, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<3, false, false, false, true, false><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    } else if (sc.ntex) {
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<0, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<1, false, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    } else {
-        k_shade<CLS_MISS><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<0><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<1><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<2><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-        k_shade<3><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
     }
-    return 5;
+    if (sc.inf) {  // the light list holds the infinite light
+        if (sc.ntex) {
+            k_shade<0, false, false, true, true, false><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, true, true, false><<<grid, block, 0, st[1]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        } else {
+            k_shade<0, false, false, false, true, false><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+            k_shade<1, false, false, false, true, false><<<grid, block, 0, st[1]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        }
+        k_shade<2, false, false, false, true, false><<<grid, block, 0, st[2]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3, false, false, false, true, false><<<grid, block, 0, st[3]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    } else if (sc.ntex) {
+        k_shade<0, false, false, true><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<1, false, false, true><<<grid, block, 0, st[1]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2><<<grid, block, 0, st[2]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3><<<grid, block, 0, st[3]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    } else {
+        k_shade<0><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<1><<<grid, block, 0, st[1]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<2><<<grid, block, 0, st[2]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+        k_shade<3><<<grid, block, 0, st[3]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    }
+    // escaped rays: without the infinite light, binning has already finished them
+    if (sc.inf) k_shade<CLS_MISS><<<grid, block, 0, st[CLS_MISS]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    if (fork) {
+        for (int k = 0; k < 4; ++k) {
+            cudaEventRecord(fork->join[k], fork->aux[k]);
+            cudaStreamWaitEvent(s, fork->join[k], 0);
+        }
+    }
+    return sc.inf ? 5 : 4;
 }
 
 }  // namespace bg

@@ -536,9 +536,11 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
 // Single-scene shade launches for scenes with emitting spheres or quadrics (bg_shade_shapes.cu).
 int launch_shade_shapes(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                         uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
-// Shade launches of one bounce (the five material classes, misses included).
+// Shade launches of one bounce (the five material classes, misses included); with `fork` the
+// classes run on parallel streams, joined back into `s` before returning.
 int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                       uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
+                       uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s,
+                       const ShadeFork* fork = nullptr);
 int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                         const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
 // The guided launches of scenes with textures or an infinite light (bg_shade_guided_full.cu).

@@ -335,6 +335,10 @@ typedef struct bg_tuning {
                                         than that (each vertex may queue two: the light sample and the
                                         MIS ray toward the light) drops the excess and the render fails
                                         with BG_ERR_DEVICE (queue overflow in bg_last_error) */
+#define BG_TUNE_CONCURRENT_SHADE 16u /* single-scene wavefront renders: run a bounce's material-class
+                                        shade kernels side by side on the context's extra streams
+                                        (joined before the shadow rays); on by default.  Films then
+                                        differ from serial shading only in the order of their sums */
 bg_status bg_get_tuning(const bg_ctx* ctx, bg_tuning* out);
 bg_status bg_set_tuning(bg_ctx* ctx, const bg_tuning* t);
 
