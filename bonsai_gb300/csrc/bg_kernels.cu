@@ -361,13 +361,9 @@ __global__ void __launch_bounds__(256) k_sort_scatter(WaveBuffers wb, RenderPara
 // shade launch runs one material's code with uniform control flow.  GWK (guided waves, queries
 // set): a hit of a guidable class (matte, plastic, conductor) also writes its network query at
 // class * gw.cap + its queue position, for the inference that runs before shading.
-// FIN (single-scene waves whose light list has no infinite light): an escaped path has nothing
-// left to gather, so its sample goes to the film here (with its pending next-event contribution)
-// and the escaped-ray shade launch is skipped.
-template <bool MULTI = false, bool GWK = false, bool FIN = false>
+template <bool MULTI = false, bool GWK = false>
 __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t bounce, const SceneRender* tab,
-                                             GuideWave gw = GuideWave{}, bool queries = false,
-                                             FilmBuffers film = FilmBuffers{}) {
+                                             GuideWave gw = GuideWave{}, bool queries = false) {
     const uint32_t n = wb.counters[bounce & 1];
     const uint32_t* q = wb.queue[bounce & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -380,11 +376,6 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
             int prim = wb.hit[slot].x;
             const Scene& sc = pick<MULTI>(sc0, MULTI ? &tab[wb.scene_id[slot]].sc : nullptr);
             cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
-            if (FIN && cls == CLS_MISS) {
-                const float4 l4 = wb.L[slot];
-                film_add(film, wb.pixel[slot], apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), wb.state[slot], sc0.nlights));
-                cls = -1;
-            }
         }
         uint32_t qpos = 0;
 #pragma unroll
@@ -494,8 +485,6 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_bin<false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, true);
             launch_guide_infer(gw.wpack, gw.query, &wb.counters[C_CLS], 3, gw.cap, gw.raw, true, err, ls.sms, s);
             launches += 1;
-        } else if (!gw.flags && !sc.inf && !sc.sph_emis && !sc.quad_emis) {
-            k_bin<false, false, true><<<grid, block, 0, s>>>(sc, wb, b, nullptr, gw, false, film);
         } else {
             k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         }
