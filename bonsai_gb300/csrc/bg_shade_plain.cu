@@ -41,7 +41,7 @@ int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffer
         k_shade<2><<<grid, block, 0, st[2]>>>(sc, rp, film, wb, gw, b, err, nullptr);
         k_shade<3><<<grid, block, 0, st[3]>>>(sc, rp, film, wb, gw, b, err, nullptr);
     }
-    // escaped rays: without the infinite light, binning has already finished them
+    // escaped rays
     k_shade<CLS_MISS><<<grid, block, 0, st[CLS_MISS]>>>(sc, rp, film, wb, gw, b, err, nullptr);
     if (fork) {
         for (int k = 0; k < 4; ++k) {
