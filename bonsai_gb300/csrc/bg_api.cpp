@@ -1187,6 +1187,14 @@ bg_status bg_scene_commit(bg_scene* s, uint32_t kind, bg_build_stats* stats) {
     if ((st = upload(ctx, mats, &d.mats, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, emis, &d.emis, &s->allocs)) != BG_OK) return st;
     if ((st = upload(ctx, light_prims, &d.light_prims, &s->allocs)) != BG_OK) return st;
+    {   // the material class of every primitive, for the binning pass (one byte each instead of the
+        // primitive's 16-byte record and its material)
+        std::vector<uint8_t> cls((size_t)ntri + nsph + nquad);
+        for (uint32_t i = 0; i < ntri; ++i) cls[i] = (uint8_t)mats[s->tri_mat[i]].type;
+        for (uint32_t i = 0; i < nsph; ++i) cls[ntri + i] = (uint8_t)mats[sph_mat[i]].type;
+        for (uint32_t i = 0; i < nquad; ++i) cls[ntri + nsph + i] = (uint8_t)mats[s->quads[i].material_id].type;
+        if (!cls.empty() && (st = upload(ctx, cls, &d.prim_cls, &s->allocs)) != BG_OK) return st;
+    }
     if (any_sph_light && (st = upload(ctx, sph_emis, &d.sph_emis, &s->allocs)) != BG_OK) return st;
     if (any_quad_light && (st = upload(ctx, quad_emis, &d.quad_emis, &s->allocs)) != BG_OK) return st;
     if (s->any_normals || s->any_flags) {

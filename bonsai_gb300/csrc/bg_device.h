@@ -179,6 +179,7 @@ struct Scene {
     const TexInfo* tex;
     const float4* texels;
     const InfLight* inf;  // the infinite light, or null
+    const uint8_t* prim_cls;  // material class (bg_material_type) per primitive: 1 B, stays in L2
 };
 
 enum : uint32_t {

@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(128) k_bin(Scene sc0, WaveBuffers wb, uint32_t
             slot = q[i];
             int prim = wb.hit[slot].x;
             const Scene& sc = pick<MULTI>(sc0, MULTI ? &tab[wb.scene_id[slot]].sc : nullptr);
-            cls = prim < 0 ? CLS_MISS : (int)sc.mats[prim_material(sc, prim)].type;
+            cls = prim < 0 ? CLS_MISS : (int)sc.prim_cls[prim];
         }
         uint32_t qpos = 0;
 #pragma unroll
