@@ -211,6 +211,31 @@ def test_guided_render_is_unbiased(gpu_ctx):
         sc.close()
 
 
+@pytest.mark.parametrize("placement", ["continuation only", "next-event only"])
+def test_guided_placements_are_unbiased(gpu_ctx, placement):
+    """Either head alone (the other strategy a BSDF sample) keeps the estimate unbiased."""
+    sd = _small_slit(64, 48)
+    sc = G.Scene(gpu_ctx, sd)
+    npix = sd.camera.width * sd.camera.height
+    flags = A.BG_GUIDE_NO_NEE if placement == "continuation only" else A.BG_GUIDE_NO_CONTINUATION
+    g = G.Guide(gpu_ctx, batch_size=4096, samples_per_pass=16384, warmup_passes=4, no_fallback=True, pass_paths=npix,
+                flags=flags)
+    try:
+        pi = G.PathIntegrator(sd.camera, 512, sd.max_depth, mode=A.BG_MODE_PBRT, seed=8)
+        pi.render(sc, spp=512)
+        p1, p2, pn = G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height)
+        r = pi.render_guided(sc, g, spp=512, first_sample=200000)
+        assert r.guide.guided_passes == 512 - 4 and r.stats.nan_samples == 0 and r.stats.error_word == 0
+        g1, g2, gn = G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height)
+        z = _block_z(g1, g2, gn, p1, p2, pn)
+        print(placement, f"block |z| max {np.abs(z).max():.2f}, frac>3 {np.mean(np.abs(z) > 3):.3f}")
+        assert np.mean(np.abs(z) > 3) < 0.03
+        assert np.abs(z).max() < 6
+    finally:
+        g.close()
+        sc.close()
+
+
 def _relmse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 

@@ -114,6 +114,34 @@ def test_ray_binning_keeps_every_path(gpu_ctx):
         sc.close()
 
 
+def test_concurrent_shading_keeps_every_path(gpu_ctx):
+    """BG_TUNE_CONCURRENT_SHADE runs a bounce's material-class shade kernels side by side: only the
+    order of queue appends and film sums changes, so the films agree to rounding of the sums."""
+    sd = S.production(160, 90, spp=4, max_depth=6, n_ico=4, ico_level=3, n_spheres=100)
+    sc = G.Scene(gpu_ctx, sd, A.BG_BVH_WIDE)
+    saved = A.bg_tuning()
+    gpu_ctx.check(gpu_ctx.lib.bg_get_tuning(gpu_ctx.h, C.byref(saved)))
+    try:
+        pi = G.PathIntegrator(sd.camera, sd.spp, sd.max_depth, mode=A.BG_MODE_PBRT, seed=6)
+        films = []
+        for flags in (A.BG_TUNE_TILE_PIXELS, A.BG_TUNE_TILE_PIXELS | A.BG_TUNE_CONCURRENT_SHADE):
+            t = A.bg_tuning.from_buffer_copy(bytes(saved))
+            t.wave_paths, t.flags = 1 << 14, flags  # several waves per render
+            gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(t)))
+            for graph in (False, True):
+                r = pi.render(sc, graph=graph)
+                assert r.stats.error_word == 0
+                films.append(G.PathIntegrator.moments(gpu_ctx, sd.camera.width, sd.camera.height))
+        a1, a2, an = films[0]
+        for b1, b2, bn in films[1:]:
+            np.testing.assert_array_equal(an, bn)
+            np.testing.assert_allclose(a1, b1, rtol=1e-12, atol=1e-12)
+            np.testing.assert_allclose(a2, b2, rtol=1e-12, atol=1e-12)
+    finally:
+        gpu_ctx.check(gpu_ctx.lib.bg_set_tuning(gpu_ctx.h, C.byref(saved)))
+        sc.close()
+
+
 def _with_flags(ctx, flags, fn):
     saved = A.bg_tuning()
     ctx.check(ctx.lib.bg_get_tuning(ctx.h, C.byref(saved)))
