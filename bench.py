@@ -87,7 +87,7 @@ def config_of(sd, small: bool) -> dict:
                     f"{sd.nsph} spheres, {sd.camera.width}x{sd.camera.height}, {sd.spp} spp, max depth "
                     f"{sd.max_depth}, RR after depth 3, PBRT estimator",
         "width": sd.camera.width, "height": sd.camera.height, "spp": sd.spp, "max_depth": sd.max_depth,
-        "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "8-wide compressed (80 B nodes, 8-bit child boxes, <=3 prims per leaf)", "graph": "wave chain captured as a CUDA graph",
+        "triangles": sd.ntri, "spheres": sd.nsph, "bvh": "8-wide compressed (80 B nodes, 8-bit child boxes, <= 2 primitives per leaf)", "graph": "wave chain captured as a CUDA graph",
         "l2": "flushed before every step (512 MB device write)",
         "parallelism": "replicas",
     }
@@ -283,6 +283,12 @@ def run_ours(args):
         tuning = autotune.tune(ctx, scene, pi, spp=4)
         tuning = {k: tuning[k] for k in ("refill", "blocks_per_sm", "wave_paths", "sort_rays", "concurrent_shade", "ms")} | {
             "cached": bool(tuning.get("cached", False))}
+        # traversal node width: the scene rebuilt 8-wide and 2-wide, the faster kept
+        scene.close()
+        scene, lay = autotune.tune_layout(ctx, sd, pi, spp=4)
+        tuning["node_width"] = 8 if lay["layout"] == A.BG_BVH_WIDE else 2
+        tuning["node_width_trials_ms"] = {("8" if t["layout"] == A.BG_BVH_WIDE else "2"): t["ms"]
+                                          for t in lay.get("trials", [])}
     for _ in range(args.warmup):
         pi.render(scene, readback=False, graph=True)
     clocks = Clocks(local)
@@ -353,7 +359,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, bonsai_gb300/scenes.py)",
-        "config": config_of(sd, args.small) | {"tuning": tuning},
+        "config": config_of(sd, args.small) | {"tuning": tuning} | (
+            {"bvh": "2-wide (64 B nodes; the autotuner's node-width choice)"}
+            if tuning and tuning.get("node_width") == 2 else {}),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(A.bg_camera) + C.sizeof(A.bg_render_opts),
                 "d2h_bytes_per_step": sd.camera.width * sd.camera.height * 3 * 4},
         "gpu_launches": launches,

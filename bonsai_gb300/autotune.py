@@ -7,6 +7,8 @@ library's CUDA events, L2 flushed before each trial):
   wave_paths    - paths per wave (queue capacity)
   sort_rays     - bin each bounce's extension rays by direction octant and origin cell
   concurrent_shade - run a bounce's material-class shade kernels side by side
+and, by tune_layout, the traversal node width: the scene's BVH built 8-wide (BG_BVH_WIDE) and
+2-wide (BG_BVH_WIDE2), each timed on the same trial render.
 The result is cached as JSON keyed by GPU name, scene signature and render settings
 (default ~/.cache/bonsai_gb300/tuning.json, or $BONSAI_TUNING_CACHE).
 """
@@ -123,3 +125,48 @@ def tune(ctx, scene, integrator, spp: int = 4, use_cache: bool = True, verbose: 
         except OSError:
             pass
     return result
+
+
+LAYOUTS = [A.BG_BVH_WIDE, A.BG_BVH_WIDE2]  # 8-wide compressed, 2-wide
+
+
+def tune_layout(ctx, sd, integrator, spp: int = 4, use_cache: bool = True, verbose: bool = False):
+    """Traversal node width for scene data `sd`: builds the BVH in each wide layout, times a trial
+    render of each at the context's current launch shape, keeps the faster.  Returns (scene, info)
+    with the kept scene built (the other one is closed); info = {"layout", "ms", "trials", "cached"}.
+    The choice is cached like the launch parameters."""
+    from . import gpu as G
+    key = "layout|" + key_of(sd, spp)
+    path = cache_path()
+    cache = {}
+    if use_cache and path.exists():
+        try:
+            cache = json.loads(path.read_text())
+        except ValueError:
+            cache = {}
+    if use_cache and key in cache:
+        c = cache[key]
+        return G.Scene(ctx, sd, int(c["layout"])), dict(c, cached=True)
+    best, best_ms, trials = None, float("inf"), []
+    for layout in LAYOUTS:
+        sc = G.Scene(ctx, sd, layout)
+        integrator.render(sc, readback=False, spp=1)  # warm
+        ms = _trial(ctx, sc, integrator, spp)
+        trials.append({"layout": int(layout), "ms": ms})
+        if verbose:
+            print("autotune layout", layout, f"{ms:.2f} ms")
+        if ms < best_ms:
+            if best is not None:
+                best.close()
+            best, best_ms = sc, ms
+        else:
+            sc.close()
+    info = {"layout": int(best.layout), "ms": best_ms, "trials": trials}
+    if use_cache:
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            cache[key] = {"layout": info["layout"], "ms": best_ms}
+            path.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    return best, dict(info, cached=False)

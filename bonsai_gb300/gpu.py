@@ -87,7 +87,7 @@ class Scene:
     """Device scene (bg_scene) built from a ``scenes.SceneData``."""
 
     def __init__(self, ctx: Context, sd: S.SceneData, bvh: int = A.BG_BVH_WIDE):
-        self.ctx, self.sd = ctx, sd
+        self.ctx, self.sd, self.layout = ctx, sd, bvh
         lib = ctx.lib
         h = C.c_void_p()
         ctx.check(lib.bg_scene_create(ctx.h, C.byref(h)))

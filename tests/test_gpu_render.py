@@ -210,3 +210,26 @@ def test_camera_lens_arguments(gpu_ctx):
                 G.PathIntegrator(cam, 1, 2).render(sc)
     finally:
         sc.close()
+
+
+def test_autotuner_picks_a_node_width(gpu_ctx, tmp_path, monkeypatch):
+    """tune_layout builds the BVH 8-wide and 2-wide, keeps the faster, and the kept scene renders
+    the same image as a scene built directly in that layout."""
+    from bonsai_gb300 import autotune
+    monkeypatch.setenv("BONSAI_TUNING_CACHE", str(tmp_path / "tuning.json"))
+    sd = S.cornell(48, 48, spp=4)
+    pi = G.PathIntegrator(sd.camera, 4, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=1)
+    sc, info = autotune.tune_layout(gpu_ctx, sd, pi, spp=2)
+    try:
+        assert info["layout"] in autotune.LAYOUTS and len(info["trials"]) == 2 and not info["cached"]
+        got = pi.render(sc).rgb
+    finally:
+        sc.close()
+    ref_sc = G.Scene(gpu_ctx, sd, info["layout"])
+    try:
+        np.testing.assert_allclose(got, pi.render(ref_sc).rgb, rtol=1e-6, atol=1e-7)
+    finally:
+        ref_sc.close()
+    sc2, info2 = autotune.tune_layout(gpu_ctx, sd, pi, spp=2)  # from the cache
+    sc2.close()
+    assert info2["cached"] and info2["layout"] == info["layout"]
