@@ -230,7 +230,9 @@ struct VertexOut {
 // the counter RNG.  A shade thread computes them when it picks up a path, where few registers are
 // live, into its column of shared memory (8 rows, stride SU_STRIDE).
 constexpr uint32_t SU_STRIDE = 128;
-BG_D void strat_prefetch(const StratParams& sp, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k1,
+// Not inlined: renders with the independent sampler never call it, and its code (permutations, cycle
+// walking) would otherwise sit among the shade kernels' hot instructions.
+static __device__ __noinline__ void strat_prefetch(const StratParams& sp, uint32_t pix, uint32_t sample, uint64_t seed, uint32_t k1,
                          uint32_t k2, float* col) {
     col[0] = k1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1) : -1.0f;
     col[SU_STRIDE] = k1 + 1 < sp.dims ? strat_1d(sp, false, pix, sample, seed, k1 + 1) : -1.0f;
