@@ -266,11 +266,19 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
 }
 
 // ---------------------------------------------------------------- training
-__global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
+// 256 threads per 128-sample tile: thread t serves row t % 128 (its TMEM lane, warp % 4 selecting
+// the lane quarter) and half t / 128 of the row's columns in every epilogue, so each stage's
+// epilogue (TMEM loads, activation / gradient packing, shared-memory and gradient stores) takes
+// half the time of one thread per row.  The output layer splits by head: half 0 takes the
+// continuation head's loss, half 1 the next-event head's (their dZ columns 40 and 41..47 share an
+// 8-column group, assembled through `xch`).
+__global__ void __launch_bounds__(256, 1) k_guide_train(GuideTrainArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
     __shared__ uint64_t bar, wbar;
     __shared__ uint32_t tslot;
+    __shared__ float xch[128];  // head 0's gradient of output 40, per row
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t row = tid & 127u, half = tid >> 7;
     const long long wait_limit = g_guide_wait_limit;
     if (a.step && blockIdx.x == 0 && tid == 0) atomicAdd(a.step, 1u);
     uint8_t* wsm = sm;
@@ -287,11 +295,12 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
     if (warp == 0) tmem_alloc(&tslot, TM_COLS_TRAIN);
     __syncthreads();  // the barriers are initialised before the bulk copy signals one
     if (tid == 0) bulk_g2s(wsm, a.wpack, GUIDE_WPACK_BYTES, &wbar);
-    // this thread's sample
-    const uint32_t si = blockIdx.x * 128 + tid;
+    // this row's sample (both halves read it; half 0 encodes it)
+    const uint32_t si = blockIdx.x * 128 + row;
     float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
     V3 wi = v3(0.0f, 0.0f, 1.0f);
-    float p_b = 0.0f, wn0 = 0.0f, wn1 = 0.0f;  // normalised weights of the two heads
+    float p_b = 0.0f, wn = 0.0f;  // this half's head: its normalised weight
+    bool any_w = false;
     if (si < a.n) {
         const float4* s = a.samples + (size_t)GUIDE_SAMPLE_F4 * a.order.at(a.base + si);
         float4 f0 = s[0], f1 = s[1], f2 = s[2], f3 = s[3];
@@ -300,10 +309,12 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         wi = v3(f2.y, f2.z, f2.w);
         p_b = f3.x;
         const float ws0 = a.wsum[0], ws1 = a.wsum[1];
-        wn0 = (ws0 > 0.0f && f3.y > 0.0f && isfinite(f3.y)) ? f3.y / ws0 : 0.0f;
-        wn1 = (ws1 > 0.0f && f3.z > 0.0f && isfinite(f3.z)) ? f3.z / ws1 : 0.0f;
+        const float wn0 = (ws0 > 0.0f && f3.y > 0.0f && isfinite(f3.y)) ? f3.y / ws0 : 0.0f;
+        const float wn1 = (ws1 > 0.0f && f3.z > 0.0f && isfinite(f3.z)) ? f3.z / ws1 : 0.0f;
+        wn = half == 0 ? wn0 : wn1;
+        any_w = wn0 > 0.0f || wn1 > 0.0f;
     }
-    encode_row(act, tid, q);
+    if (half == 0) encode_row(act, row, q);
     const bool wok = mbar_wait(&wbar, 0, wait_limit);  // the weight image (overlaps the encoding above)
     fence_async_smem();
     tc_fence_before();
@@ -319,8 +330,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         return;
     }
     const uint32_t tmem = tslot;
-    const uint32_t tm_row = tmem + ((warp * 32u) << 16);
+    const uint32_t tm_row = tmem + (((warp & 3u) * 32u) << 16);
     const uint32_t w_addr = smem_addr(wsm), act_addr = smem_addr(act), dz_addr = smem_addr(dz);
+    const float zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint32_t phase = 0;
     // forward
     for (int l = 0; l < GUIDE_LAYERS; ++l) {
@@ -332,23 +344,54 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         phase ^= 1;
         tc_fence_after();
         if (l < GUIDE_LAYERS - 1) {
-            hidden_epilogue(tm_row + TM_FWD, act + (l + 1) * ACT_BYTES, tid);
+            // ReLU of this half's 32 accumulator columns -> BF16; half 1 adds the bias column 64
+            // (constant 1) and the zero columns 65..79
+            uint8_t* dst = act + (l + 1) * ACT_BYTES;
+            const uint32_t c0 = 32u * half;
+#pragma unroll
+            for (int c = 0; c < 32; c += 16) {
+                float v[16];
+                tmem_ld16(tm_row + TM_FWD + c0 + c, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
+                store_row8(dst, ACT_RS, row, c0 + c, v);
+                store_row8(dst, ACT_RS, row, c0 + c + 8, v + 8);
+            }
+            if (half == 1) {
+                float tail[16] = {1.0f};
+                store_row8(dst, ACT_RS, row, 64, tail);
+                store_row8(dst, ACT_RS, row, 72, tail + 8);
+            }
         } else {
-            float raw[GUIDE_RAW_STRIDE], g[GUIDE_RAW_STRIDE];
+            // this half's head: 41 outputs from the 48 (head 0) or 64 (head 1) columns holding them
+            float v[64], g[GUIDE_HEAD_OUT];
+            const uint32_t c0 = half == 0 ? 0u : 32u;
 #pragma unroll
-            for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) tmem_ld16(tm_row + TM_FWD + c, raw + c);
-            // both heads' losses on the same direction, each with its own target weight
-            float loss = guide_loss_grad(raw, wi, p_b, wn0, a.alpha, g) +
-                         guide_loss_grad(raw + GUIDE_HEAD_OUT, wi, p_b, wn1, a.alpha, g + GUIDE_HEAD_OUT);
+            for (int c = 0; c < 64; c += 16)
+                if (half == 1 || c < 48) tmem_ld16(tm_row + TM_FWD + c0 + c, v + c);
+            const float* raw = v + (half == 0 ? 0 : GUIDE_HEAD_OUT - 32);
+            float loss = guide_loss_grad(raw, wi, p_b, wn, a.alpha, g);
+            // loss gradient -> dZ4: head 0 in columns 0..40, head 1 in 41..81, 82..127 zero
+            if (half == 0) {
 #pragma unroll
-            for (int j = GUIDE_OUT; j < GUIDE_RAW_STRIDE; ++j) g[j] = 0.0f;
-            // loss gradient -> dZ4 (columns 0..81; 82..127 zero)
+                for (int c = 0; c < 40; c += 8) store_row8(dz, DZ_RS, row, c, g + c);
+                xch[row] = g[40];
+            }
+            __syncthreads();  // xch
+            if (half == 1) {
+                float b[8] = {xch[row], g[0], g[1], g[2], g[3], g[4], g[5], g[6]};
+                store_row8(dz, DZ_RS, row, 40, b);
 #pragma unroll
-            for (int c = 0; c < GUIDE_OUT_ROWS; c += 8) store_row8(dz, DZ_RS, tid, c, g + c);
-            float zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int c = 48; c < 88; c += 8) {
+                    float t[8];
 #pragma unroll
-            for (int c = GUIDE_OUT_ROWS; c < 128; c += 8) store_row8(dz, DZ_RS, tid, c, zero8);
-            float cnt = wn0 > 0.0f || wn1 > 0.0f ? 1.0f : 0.0f;
+                    for (int j = 0; j < 8; ++j) t[j] = c + j - 41 < GUIDE_HEAD_OUT ? g[c + j - 41] : 0.0f;
+                    store_row8(dz, DZ_RS, row, c, t);
+                }
+#pragma unroll
+                for (int c = 88; c < 128; c += 8) store_row8(dz, DZ_RS, row, c, zero8);
+            }
+            float cnt = half == 0 && any_w ? 1.0f : 0.0f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 loss += __shfl_xor_sync(0xffffffffu, loss, o);
@@ -356,7 +399,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
             }
             if (lane == 0) {
                 atomicAdd(&a.stats[0], loss);
-                atomicAdd(&a.stats[1], cnt);
+                if (half == 0) atomicAdd(&a.stats[1], cnt);
             }
         }
         if (stage_barrier(ok)) {
@@ -386,31 +429,34 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
         bool ok = mbar_wait(&bar, phase, wait_limit);
         phase ^= 1;
         tc_fence_after();
-        // weight gradient rows (thread = output row) into this CTA's partial slice
+        // weight gradient rows (row = output row) into this CTA's partial slice: half 0 takes
+        // columns 0..47, half 1 columns 48..79
         const int used = guide_used_rows(l);
-        if ((int)(warp * 32) < used) {
+        if ((int)((warp & 3u) * 32) < used) {
             float4* gl = reinterpret_cast<float4*>(a.partial + (size_t)blockIdx.x * GUIDE_PARAMS + guide_param_off(l) +
-                                                   tid * GUIDE_K);
+                                                   row * GUIDE_K);
 #pragma unroll
             for (int c = 0; c < GUIDE_K; c += 16) {
+                if ((c < 48) != (half == 0)) continue;
                 float v[16];
                 tmem_ld16(tm_row + TM_DW + c, v);
-                if ((int)tid < used) {
+                if ((int)row < used) {
 #pragma unroll
                     for (int j = 0; j < 4; ++j) gl[c / 4 + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 }
             }
         }
         if (l > 0) {
-            // dZ_{l-1} = dX[:, 0..63] * relu'(H_l), H_l = act tile l (this thread's row)
+            // dZ_{l-1} = dX[:, 0..63] * relu'(H_l), H_l = act tile l (this row; this half's 32 columns)
             const uint8_t* hrow = act + l * ACT_BYTES;
 #pragma unroll
-            for (int c = 0; c < GUIDE_HID; c += 16) {
+            for (int cc = 0; cc < 32; cc += 16) {
+                const int c = 32 * (int)half + cc;
                 float v[16];
                 tmem_ld16(tm_row + TM_DX + c, v);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    uint4 hv = *reinterpret_cast<const uint4*>(hrow + core_off(tid, c + 8 * h, ACT_RS));
+                    uint4 hv = *reinterpret_cast<const uint4*>(hrow + core_off(row, c + 8 * h, ACT_RS));
                     uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
@@ -418,8 +464,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(GuideTrainArgs a) {
                         if (!(bf16_hi(hw[j]) > 0.0f)) v[8 * h + 2 * j + 1] = 0.0f;
                     }
                 }
-                store_row8(dz, DZ_RS, tid, c, v);
-                store_row8(dz, DZ_RS, tid, c + 8, v + 8);
+                store_row8(dz, DZ_RS, row, c, v);
+                store_row8(dz, DZ_RS, row, c + 8, v + 8);
             }
         }
         if (stage_barrier(ok)) {
@@ -585,7 +631,7 @@ void launch_guide_train(const GuideTrainArgs& a, cudaStream_t s) {
     guide_set_smem_limits();
     uint32_t grid = (a.n + 127) / 128;
     if (grid == 0) return;
-    k_guide_train<<<grid, 128, TRAIN_SMEM, s>>>(a);
+    k_guide_train<<<grid, 256, TRAIN_SMEM, s>>>(a);
     k_guide_reduce<<<dim3((GUIDE_PARAMS + 255) / 256, REDUCE_SPLIT), 256, 0, s>>>(a.partial, grid, a.grad);
 }
 
