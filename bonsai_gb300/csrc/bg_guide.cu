@@ -77,15 +77,12 @@ BG_D void issue_forward(uint32_t tm, uint32_t act, uint32_t w, int N) {
 // Forward epilogue of a hidden layer: ReLU of this thread's 64 accumulator columns, BF16, plus
 // the constant bias column 64 and zero columns 65..79.
 BG_D void hidden_epilogue(uint32_t tm_row, uint8_t* dst, uint32_t row) {
+    float v[GUIDE_HID];
+    tmem_ld64(tm_row, v);  // one TMEM round trip for the row's 64 accumulators
 #pragma unroll
-    for (int c = 0; c < GUIDE_HID; c += 16) {
-        float v[16];
-        tmem_ld16(tm_row + c, v);
+    for (int j = 0; j < GUIDE_HID; ++j) v[j] = fmaxf(v[j], 0.0f);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
-        store_row8(dst, ACT_RS, row, c, v);
-        store_row8(dst, ACT_RS, row, c + 8, v + 8);
-    }
+    for (int c = 0; c < GUIDE_HID; c += 8) store_row8(dst, ACT_RS, row, c, v + c);
     float tail[16] = {1.0f};
     store_row8(dst, ACT_RS, row, 64, tail);
     store_row8(dst, ACT_RS, row, 72, tail + 8);
@@ -225,8 +222,12 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
                     // head h's 41 outputs from the 48 or 64 columns that hold them
                     float v[64];
                     const int c0 = h == 0 ? 0 : 32;
-#pragma unroll
-                    for (int c = 0; c < (h == 0 ? 48 : 64); c += 16) tmem_ld16(tm_row + TM_FWD + c0 + c, v + c);
+                    if (h == 0) {
+                        tmem_ld32(tm_row + TM_FWD, v);
+                        tmem_ld16(tm_row + TM_FWD + 32, v + 32);
+                    } else {
+                        tmem_ld64(tm_row + TM_FWD + 32, v);
+                    }
                     if (valid) {
                         float rec[GUIDE_MIX_HEAD];
                         guide_write_mixture(v + (GUIDE_HEAD_OUT * h - c0), rec);
@@ -238,13 +239,13 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
                 }
             } else {
 #pragma unroll
-                for (int c = 0; c < GUIDE_OUT_ROWS; c += 16) {
-                    float v[16];
-                    tmem_ld16(tm_row + TM_FWD + c, v);
+                for (int c = 0; c < GUIDE_OUT_ROWS; c += 32) {
+                    float v[32];
+                    tmem_ld32(tm_row + TM_FWD + c, v);
                     if (valid) {
                         float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE + c);
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                        for (int j = 0; j < 8; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                     }
                 }
             }
@@ -348,15 +349,12 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideTrainArgs a) {
             // (constant 1) and the zero columns 65..79
             uint8_t* dst = act + (l + 1) * ACT_BYTES;
             const uint32_t c0 = 32u * half;
+            float v[32];
+            tmem_ld32(tm_row + TM_FWD + c0, v);
 #pragma unroll
-            for (int c = 0; c < 32; c += 16) {
-                float v[16];
-                tmem_ld16(tm_row + TM_FWD + c0 + c, v);
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j], 0.0f);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
-                store_row8(dst, ACT_RS, row, c0 + c, v);
-                store_row8(dst, ACT_RS, row, c0 + c + 8, v + 8);
-            }
+            for (int c = 0; c < 32; c += 8) store_row8(dst, ACT_RS, row, c0 + c, v + c);
             if (half == 1) {
                 float tail[16] = {1.0f};
                 store_row8(dst, ACT_RS, row, 64, tail);
@@ -365,12 +363,15 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideTrainArgs a) {
         } else {
             // this half's head: 41 outputs from the 48 (head 0) or 64 (head 1) columns holding them
             float v[64], g[GUIDE_HEAD_OUT];
-            const uint32_t c0 = half == 0 ? 0u : 32u;
-#pragma unroll
-            for (int c = 0; c < 64; c += 16)
-                if (half == 1 || c < 48) tmem_ld16(tm_row + TM_FWD + c0 + c, v + c);
-            const float* raw = v + (half == 0 ? 0 : GUIDE_HEAD_OUT - 32);
-            float loss = guide_loss_grad(raw, wi, p_b, wn, a.alpha, g);
+            if (half == 0) {
+                tmem_ld32(tm_row + TM_FWD, v);
+                tmem_ld16(tm_row + TM_FWD + 32, v + 32);
+            } else {
+                tmem_ld64(tm_row + TM_FWD + 32, v);
+            }
+            // head 1's outputs start at v[9] (column 41); constant offsets keep v in registers
+            float loss = half == 0 ? guide_loss_grad(v, wi, p_b, wn, a.alpha, g)
+                                   : guide_loss_grad(v + (GUIDE_HEAD_OUT - 32), wi, p_b, wn, a.alpha, g);
             // loss gradient -> dZ4: head 0 in columns 0..40, head 1 in 41..81, 82..127 zero
             if (half == 0) {
 #pragma unroll
@@ -435,38 +436,38 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideTrainArgs a) {
         if ((int)((warp & 3u) * 32) < used) {
             float4* gl = reinterpret_cast<float4*>(a.partial + (size_t)blockIdx.x * GUIDE_PARAMS + guide_param_off(l) +
                                                    row * GUIDE_K);
+            float v[48];
+            const int c0 = half == 0 ? 0 : 48, nc = half == 0 ? 48 : 32;
+            if (half == 0) {
+                tmem_ld32(tm_row + TM_DW, v);
+                tmem_ld16(tm_row + TM_DW + 32, v + 32);
+            } else {
+                tmem_ld32(tm_row + TM_DW + 48, v);
+            }
+            if ((int)row < used) {
 #pragma unroll
-            for (int c = 0; c < GUIDE_K; c += 16) {
-                if ((c < 48) != (half == 0)) continue;
-                float v[16];
-                tmem_ld16(tm_row + TM_DW + c, v);
-                if ((int)row < used) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) gl[c / 4 + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-                }
+                for (int j = 0; j < 12; ++j)
+                    if (4 * j < nc) gl[c0 / 4 + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             }
         }
         if (l > 0) {
             // dZ_{l-1} = dX[:, 0..63] * relu'(H_l), H_l = act tile l (this row; this half's 32 columns)
             const uint8_t* hrow = act + l * ACT_BYTES;
+            const int c0 = 32 * (int)half;
+            float v[32];
+            tmem_ld32(tm_row + TM_DX + c0, v);
 #pragma unroll
-            for (int cc = 0; cc < 32; cc += 16) {
-                const int c = 32 * (int)half + cc;
-                float v[16];
-                tmem_ld16(tm_row + TM_DX + c, v);
+            for (int h = 0; h < 4; ++h) {
+                uint4 hv = *reinterpret_cast<const uint4*>(hrow + core_off(row, c0 + 8 * h, ACT_RS));
+                uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    uint4 hv = *reinterpret_cast<const uint4*>(hrow + core_off(row, c + 8 * h, ACT_RS));
-                    uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        if (!(bf16_lo(hw[j]) > 0.0f)) v[8 * h + 2 * j] = 0.0f;
-                        if (!(bf16_hi(hw[j]) > 0.0f)) v[8 * h + 2 * j + 1] = 0.0f;
-                    }
+                for (int j = 0; j < 4; ++j) {
+                    if (!(bf16_lo(hw[j]) > 0.0f)) v[8 * h + 2 * j] = 0.0f;
+                    if (!(bf16_hi(hw[j]) > 0.0f)) v[8 * h + 2 * j + 1] = 0.0f;
                 }
-                store_row8(dz, DZ_RS, row, c, v);
-                store_row8(dz, DZ_RS, row, c + 8, v + 8);
             }
+#pragma unroll
+            for (int c = 0; c < 32; c += 8) store_row8(dz, DZ_RS, row, c0 + c, v + c);
         }
         if (stage_barrier(ok)) {
             bail_out(&bar, phase ^ 1, a.err, tmem, TM_COLS_TRAIN);
