@@ -557,6 +557,8 @@ void bg_destroy(bg_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     for (auto ev : ctx->timing_ev) cudaEventDestroy(ev);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
+    dfree_all(ctx, ctx->batch_allocs);
     for (auto st : ctx->fork.aux)
         if (st) cudaStreamDestroy(st);
     if (ctx->fork.fork) cudaEventDestroy(ctx->fork.fork);
@@ -1637,21 +1639,77 @@ bg_status bg_render_batch(bg_ctx* ctx, const bg_batch_item* items, size_t n, bg_
         item0 += npix * it.opts.spp;
     }
     std::vector<void*> tmp;
-    const bg::SceneRender* d_tab = nullptr;
-    if ((st = upload(ctx, tab, &d_tab, &tmp)) != BG_OK) return st;
+    // the scene table lives in the context (grown when a batch needs more entries) so that the
+    // captured graph below can refer to it; its contents are uploaded every call
+    if (ctx->batch_tab_cap < n) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        dfree_all(ctx, ctx->batch_allocs);
+        ctx->batch_tab = nullptr;
+        ctx->batch_tab_cap = 0;
+        if (ctx->batch_graph) {
+            cudaGraphExecDestroy(ctx->batch_graph);
+            ctx->batch_graph = nullptr;
+        }
+        void* p;
+        if ((st = dalloc(ctx, n * sizeof(bg::SceneRender), &p, &ctx->batch_allocs)) != BG_OK) return st;
+        ctx->batch_tab = (bg::SceneRender*)p;
+        ctx->batch_tab_cap = n;
+    }
+    const bg::SceneRender* d_tab = ctx->batch_tab;
+    CK(cudaMemcpyAsync(ctx->batch_tab, tab.data(), n * sizeof(bg::SceneRender), cudaMemcpyHostToDevice, ctx->stream));
     const uint32_t cap = (uint32_t)std::min<uint64_t>(ctx->max_queue, std::max<uint64_t>(total_items, 1));
     if ((st = ensure_wave(ctx, cap)) != BG_OK) {
         dfree_all(ctx, tmp);
         return st;
     }
     CK(cudaMemsetAsync(ctx->wave.ray_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
-    uint64_t launches = 0;
-    for (uint64_t w0 = 0; w0 < total_items; w0 += cap) {
-        const uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, total_items - w0);
-        launches += (uint64_t)bg::launch_wave_batch(d_tab, (uint32_t)n, max_depth, ctx->wave, w0, nitems, ctx->d_err,
-                                                    ctx->shape, ctx->stream, variants);
+    // every wave of the batch in one CUDA graph, captured once per batch shape and replayed: the
+    // whole uneven batch renders with one graph launch
+    std::vector<unsigned char> key;
+    auto put = [&](const void* p, size_t k) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + k);
+    };
+    const uint64_t nn = n;
+    put(&d_tab, sizeof(d_tab));
+    put(&nn, sizeof(nn));
+    put(&max_depth, sizeof(max_depth));
+    put(&cap, sizeof(cap));
+    put(&total_items, sizeof(total_items));
+    put(&variants, sizeof(variants));
+    put(&ctx->wave, sizeof(ctx->wave));
+    put(&ctx->shape, sizeof(ctx->shape));
+    if (!ctx->batch_graph || key != ctx->batch_key) {
+        if (ctx->batch_graph) {
+            cudaGraphExecDestroy(ctx->batch_graph);
+            ctx->batch_graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int nk = 0;
+        for (uint64_t w0 = 0; w0 < total_items; w0 += cap) {
+            const uint32_t nitems = (uint32_t)std::min<uint64_t>(cap, total_items - w0);
+            nk += bg::launch_wave_batch(d_tab, (uint32_t)n, max_depth, ctx->wave, w0, nitems, ctx->d_err, ctx->shape,
+                                        ctx->stream, variants);
+        }
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (ce != cudaSuccess) {
+            dfree_all(ctx, tmp);
+            return cuda_fail(ctx, ce, "cudaStreamEndCapture (batch)");
+        }
+        ce = cudaGraphInstantiate(&ctx->batch_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            ctx->batch_graph = nullptr;
+            dfree_all(ctx, tmp);
+            return cuda_fail(ctx, ce, "cudaGraphInstantiate (batch)");
+        }
+        ctx->batch_key = key;
+        ctx->batch_graph_kernels = nk;
     }
+    CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+    uint64_t launches = (uint64_t)ctx->batch_graph_kernels;
+    CK(cudaGraphLaunch(ctx->batch_graph, ctx->stream));
     bg::launch_resolve(ctx->film, ctx->stream);
     launches += 1;
     cudaError_t le = cudaGetLastError();

@@ -40,6 +40,14 @@ struct bg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<unsigned char> graph_key;
     int graph_kernels = 0;
+    // batch renders: the scene table (kept, refilled per call) and the captured graph of all the
+    // batch's waves, replayed while the batch's shape stays the same
+    bg::SceneRender* batch_tab = nullptr;
+    size_t batch_tab_cap = 0;
+    std::vector<void*> batch_allocs;
+    cudaGraphExec_t batch_graph = nullptr;
+    std::vector<unsigned char> batch_key;
+    int batch_graph_kernels = 0;
     std::unordered_set<bg_scene*> scenes;  // live scenes; orphaned (ctx = null) by bg_destroy
     std::unordered_set<bg_guide*> guides;  // live guiding networks; orphaned the same way
     size_t l2_persist_max = 0, l2_window_max = 0;  // device limits for L2 access-policy windows
