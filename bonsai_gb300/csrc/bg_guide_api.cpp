@@ -45,6 +45,7 @@ struct bg_guide {
     float* pass = nullptr;      // this pass's sample per pixel
     size_t pass_pix = 0;
     float4* rec = nullptr;
+    float4* lrec = nullptr;
     float4* query = nullptr;
     float* raw = nullptr;
     uint32_t wcap = 0;
@@ -159,6 +160,9 @@ bg_status ensure_guide_wave(bg_guide* g, uint32_t cap) {
     if ((st = dalloc(ctx, (size_t)bg::GUIDE_MAXREC * bg::GUIDE_REC_F4 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK)
         return st;
     g->rec = (float4*)p;
+    // light-sample records of the recording paths' last vertices, two buffers by bounce parity
+    if ((st = dalloc(ctx, 2 * 4 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK) return st;
+    g->lrec = (float4*)p;
     // queries and mixtures of the three guidable material classes, at class * cap + queue position
     if ((st = dalloc(ctx, 3 * 3 * n * sizeof(float4), &p, &g->wave_allocs)) != BG_OK) return st;
     g->query = (float4*)p;
@@ -625,6 +629,7 @@ bg_status bg_render_guided(bg_ctx* ctx, const bg_scene* s, bg_guide* g, const bg
     gw.bmin = make_float4(lo[0], lo[1], lo[2], 0.0f);
     gw.binv = make_float4(inv[0], inv[1], inv[2], 0.0f);
     gw.rec = g->rec;
+    gw.lrec = g->lrec;
     gw.query = g->query;
     gw.raw = g->raw;
     gw.pool = g->pool;

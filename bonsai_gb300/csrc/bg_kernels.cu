@@ -438,12 +438,13 @@ __global__ void __launch_bounds__(128, BG_MINBLOCKS) k_shadow(Scene sc, WaveBuff
 
 template <bool MULTI = false, bool GWK = false>
 __global__ void __launch_bounds__(128) k_finalize(Scene sc0, FilmBuffers film0, WaveBuffers wb, GuideWave gw,
-                                                  const SceneRender* tab) {
+                                                  const SceneRender* tab, uint32_t bounce = 0) {
     const uint32_t n = wb.counters[C_DONE];
     const bool record = GWK && (gw.flags & GW_RECORD) != 0;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + lane_id();
         uint32_t slot = 0, nrec = 0;
+        bool lrec = false;
         RGB L = rgb(0.0f);
         if (i < n) {
             slot = wb.done[i];
@@ -455,8 +456,13 @@ __global__ void __launch_bounds__(128) k_finalize(Scene sc0, FilmBuffers film0, 
             L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
             film_add(film, wb.pixel[slot], L);
             nrec = rec_count(state);
+            // the last vertex's light-sample record, resolved by this bounce's shadow rays
+            lrec = record && (state & ST_LREC) && wb.pending[2 * slot].w != 0.0f;
         }
-        if (record) emit_records(gw, wb, slot, nrec, L);
+        if (record) {
+            emit_records(gw, wb, slot, nrec, L);
+            emit_light_record(gw, bounce, slot, lrec);
+        }
     }
 }
 
@@ -495,7 +501,7 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         else k_shadow<2><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);
         if (ev) cudaEventRecord(ev[4 * b + 3], s);
-        if (gw.flags) k_finalize<false, true><<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
+        if (gw.flags) k_finalize<false, true><<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr, b);
         else k_finalize<<<grid, block, 0, s>>>(sc, film, wb, gw, nullptr);
         launches += 5;
     }

@@ -120,6 +120,9 @@ struct GuideWave {
     float4* query;       // 3 float4 per query (3 * cap queries)
     float* raw;          // GUIDE_MIX_STRIDE floats per query (parsed network output)
     float4* pool;        // 4 float4 per training sample
+    // the light sample of a recording path's last vertex as a next-event training sample (4 float4
+    // per slot, two buffers by bounce parity), emitted once its shadow test has resolved
+    float4* lrec;
     uint32_t* ctr;       // [0] positive-weight records, [1] pool appends (kept)
     const uint8_t* wpack;  // BF16 weight image
 };

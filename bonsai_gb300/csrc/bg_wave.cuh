@@ -49,9 +49,9 @@ BG_D BSDF path_bsdf(const Scene& sc, const RenderParams& rp, uint32_t pix, uint3
 
 // ================================================================ wavefront (PBRT)
 // Path state word: bits 0-7 bounce, 8 specular bounce, 9 pending NEE contribution, 10 open
-// training record, 12-15 training records written, 16-23 / 24-31 the sampler's get_1d / get_2d
+// training record, 11 pending light-sample record, 12-15 training records written, 16-23 / 24-31 the sampler's get_1d / get_2d
 // calls so far (saturating at 255; calls below sampled_dimensions take stratified values).
-enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10 };
+enum : uint32_t { ST_SPECULAR = 1u << 8, ST_PENDING = 1u << 9, ST_REC_OPEN = 1u << 10, ST_LREC = 1u << 11 };
 constexpr uint32_t ST_REC_SHIFT = 12, ST_REC_MASK = 0xFu << ST_REC_SHIFT;
 BG_D uint32_t st_k1(uint32_t st) { return (st >> 16) & 0xFFu; }
 BG_D uint32_t st_k2(uint32_t st) { return st >> 24; }
@@ -171,6 +171,29 @@ BG_D float hash_unit(uint32_t a, uint32_t b, uint32_t c) {
     return (float)(h >> 8) * 0x1p-24f;
 }
 
+// The light sample of a recording vertex as a training sample of the next-event head: the
+// sampled direction with weight f |cos| Le / p_light (luminance; p_light includes the 1 / nlights
+// light choice), stored until the shadow ray tells whether the light was seen (ST_LREC).
+BG_D float4* lrec_ptr(const GuideWave& gw, uint32_t bounce, uint32_t slot) {
+    return gw.lrec + 4 * ((size_t)(bounce & 1) * gw.cap + slot);
+}
+// Warp-collective: lanes with `emit` (a resolved, visible light sample of the vertex at `bounce`)
+// append that sample to the pool.
+BG_D void emit_light_record(const GuideWave& gw, uint32_t bounce, uint32_t slot, bool emit) {
+    if (!__any_sync(FULL, emit)) return;
+    const uint32_t pos = warp_append(&gw.ctr[1], emit);
+    if (emit && pos < gw.pool_cap) {
+        const float4* r = lrec_ptr(gw, bounce, slot);
+        float4* o = gw.pool + (size_t)GUIDE_SAMPLE_F4 * pos;
+        o[0] = r[0];
+        o[1] = r[1];
+        o[2] = r[2];
+        o[3] = r[3];
+    }
+    const uint32_t tot = __popc(__ballot_sync(FULL, emit));
+    if (lane_id() == 0) atomicAdd(&gw.ctr[0], tot);
+}
+
 // Turns the records of finished paths into training samples.  Warp-collective: every lane calls
 // it, lanes without a finished path pass nrec = 0.
 BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t nrec, RGB L_end) {
@@ -285,6 +308,11 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     if (su) strat_apply(su, nee, u);  // the stratified sampler's values, prefetched by the shade thread
     // the counters move past this bounce's calls now (the roulette's get_1d when its test runs)
     state = st_set_k(state, st_k1(state) + (nee ? 1u : 0u), st_k2(state) + (nee ? 3u : 1u));
+    // paths chosen for the training pool (a per-path choice with probability keep_prob, so the
+    // other paths write nothing) record every sampled continuation and light sample
+    const bool chosen = GUIDABLE && record && hash_unit(wb.pixel[slot], wb.sample[slot], 0x5EEDu) < gw.keep_prob;
+    GuideQuery gq;
+    if (chosen) gq = make_query(gw, it, -ray.d);
     // `mix` is the query's two-head record: head 0 (at mix) for the continuation (GW_CONT), head 1
     // for estimate_direct's second strategy (GW_NEE)
     const MixView nview{mix ? mix->m + GUIDE_MIX_HEAD : nullptr};
@@ -313,6 +341,17 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
                 out.sh_o[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.t_max);
                 out.sh_d[0] = make_float4(sr.d.x, sr.d.y, sr.d.z, __int_as_float(-1));
                 out.push_sh[0] = true;
+                if (chosen && slot < gw.cap) {
+                    const float wl = luminance(f * ls.radiance) * count / ls.pdf;
+                    if (wl > 0.0f && isfinite(wl)) {
+                        float4* r = lrec_ptr(gw, bounce, slot);
+                        r[0] = gq.a;
+                        r[1] = gq.b;
+                        r[2] = make_float4(gq.c.x, ls.wi.x, ls.wi.y, ls.wi.z);
+                        r[3] = make_float4(bsdf.pdf<false>(it.wo, ls.wi, flags), 0.0f, wl, 0.0f);
+                        state |= ST_LREC;
+                    }
+                }
             }
         }
         // second strategy: a direction from the BSDF (or the mixture), counted when it reaches the
@@ -405,17 +444,16 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     wb.ray_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.t_max);
     wb.ray_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, nr.time);
     state = (state & ~(0xFFu | ST_SPECULAR)) | ((bounce + 1) & 0xFFu) | (spec ? ST_SPECULAR : 0u);
-    // only the paths the pool samples record (a per-path choice with probability keep_prob, so the
-    // other paths write nothing); every positive-weight record of a chosen path enters the pool
-    if (GUIDABLE && record && hash_unit(wb.pixel[slot], wb.sample[slot], 0x5EEDu) < gw.keep_prob)
-        state = open_record(gw, wb, slot, state, make_query(gw, it, wo), bs.wi, p_b, beta0);
+    // every positive-weight record of a chosen path enters the pool
+    if (chosen) state = open_record(gw, wb, slot, state, gq, bs.wi, p_b, beta0);
     out.cont = true;
 }
 
 // Warp-convergent tail of k_shade: queue compaction, shadow rays, records.
+// lrec: this lane's path resolved a visible light-sample record of its previous vertex.
 BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bounce, uint32_t slot, bool cont,
                         bool done_pending, const VertexOut& vo, uint32_t emit_n, RGB L_emit, bool record,
-                        uint32_t* err) {
+                        uint32_t* err, bool lrec = false) {
     uint32_t pos = warp_append(&wb.counters[(bounce + 1) & 1], cont);
     if (cont) wb.queue[(bounce + 1) & 1][pos] = slot;
     pos = warp_append(&wb.counters[C_DONE], done_pending);
@@ -432,7 +470,10 @@ BG_D void finish_vertex(const WaveBuffers& wb, const GuideWave& gw, uint32_t bou
             }
         }
     }
-    if (record) emit_records(gw, wb, slot, emit_n, L_emit);
+    if (record) {
+        emit_records(gw, wb, slot, emit_n, L_emit);
+        if (bounce > 0) emit_light_record(gw, bounce - 1, slot, lrec);
+    }
 }
 
 // Shades the paths of one material class (CLS = bg_material_type, or CLS_MISS for escaped rays).
@@ -465,7 +506,7 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
         uint32_t i = base + lane_id();
         bool active = i < n;
         uint32_t slot = active ? q[i] : 0;
-        bool cont = false, done_pending = false;
+        bool cont = false, done_pending = false, lrec_emit = false;
         VertexOut vo;
         uint32_t emit_n = 0;
         RGB L_emit = rgb(0.0f);
@@ -489,7 +530,9 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
             }
             float4 l4 = wb.L[slot];
             RGB L = apply_pending(wb, slot, rgb(l4.x, l4.y, l4.z), state, sc.nlights);
-            state &= ~ST_PENDING;
+            // the previous vertex's light-sample record: its shadow ray has been traced
+            if (record && (state & ST_LREC)) lrec_emit = wb.pending[2 * slot].w != 0.0f;
+            state &= ~(ST_PENDING | ST_LREC);
             bool specular_bounce = (state & ST_SPECULAR) != 0;
             Isect it;
             bool hit = CLS != CLS_MISS && prim >= 0 && prim_isect(sc, prim, ray, &it);
@@ -531,7 +574,7 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
                 }
             }
         }
-        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, record, err);
+        finish_vertex(wb, gw, bounce, slot, cont, done_pending, vo, emit_n, L_emit, record, err, lrec_emit);
     }
 }
 
