@@ -22,15 +22,18 @@
 namespace bg {
 
 // Encoded input of one query (80 values, see above).  q: p.xyz (in [0,1]), n.xyz, wo.xyz.
+// Each octave's angle is reduced exactly before the hardware sine / cosine: t = 2^k p is exact, and
+// so is r = t - 2 rint(t / 2) in [-1, 1], with sin(pi t) = sin(pi r); __sinf / __cosf on [-pi, pi]
+// are within 2^-21 of the true values, far below the BF16 rounding the network input gets.
 BG_D void guide_encode(const float* q, float* x) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
 #pragma unroll
         for (int k = 0; k < GUIDE_OCTAVES; ++k) {
-            float s, co;
-            sincospif(q[c] * (float)(1 << k), &s, &co);
-            x[c * 2 * GUIDE_OCTAVES + 2 * k] = s;
-            x[c * 2 * GUIDE_OCTAVES + 2 * k + 1] = co;
+            const float t = q[c] * (float)(1 << k);
+            const float a = PI * (t - 2.0f * rintf(0.5f * t));
+            x[c * 2 * GUIDE_OCTAVES + 2 * k] = __sinf(a);
+            x[c * 2 * GUIDE_OCTAVES + 2 * k + 1] = __cosf(a);
         }
     }
 #pragma unroll
@@ -44,48 +47,12 @@ constexpr float GUIDE_C_MAX = 0.95f;   // the BSDF keeps >= 5% of the proposal
 constexpr float GUIDE_LOGK_MIN = -2.0f, GUIDE_LOGK_MAX = 8.0f;
 constexpr float LOG_2PI = 1.8378770664093453f;
 
-struct VmfMix {
-    V3 mu[GUIDE_LOBES];
-    float kappa[GUIDE_LOBES];
-    float logc[GUIDE_LOBES];   // log of the lobe's normalisation kappa / (2 pi (1 - e^{-2 kappa}))
-    float w[GUIDE_LOBES];      // softmax lobe weights
-    float c;                   // probability of sampling the guide instead of the BSDF
-};
-
 // log(1 - e^{-2 kappa}) without cancellation for small kappa
 BG_D float vmf_log_norm(float kappa, float logk) { return logk - LOG_2PI - __logf(-expm1f(-2.0f * kappa)); }
 
-BG_D VmfMix guide_parse(const float* raw) {
-    VmfMix m;
-    float mx = -FLT_BIG;
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES; ++i) mx = fmaxf(mx, raw[5 * i + 4]);
-    float sum = 0.0f;
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES; ++i) {
-        V3 d = v3(raw[5 * i], raw[5 * i + 1], raw[5 * i + 2]);
-        float l = length(d);
-        m.mu[i] = l > 1e-20f ? d / l : v3(0.0f, 0.0f, 1.0f);
-        float lk = rclamp(raw[5 * i + 3], GUIDE_LOGK_MIN, GUIDE_LOGK_MAX);
-        m.kappa[i] = __expf(lk);
-        m.logc[i] = vmf_log_norm(m.kappa[i], lk);
-        m.w[i] = __expf(raw[5 * i + 4] - mx);
-        sum += m.w[i];
-    }
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES; ++i) m.w[i] = m.w[i] / sum;
-    m.c = GUIDE_C_MAX / (1.0f + __expf(-raw[40]));
-    return m;
-}
-
-BG_D float guide_pdf(const VmfMix& m, V3 w) {
-    float p = 0.0f;
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES; ++i) p += m.w[i] * __expf(m.logc[i] + m.kappa[i] * (dot(m.mu[i], w) - 1.0f));
-    return p;
-}
-
-// Direction from one vMF lobe: cos(theta) from u1 (see guide_sample), phi = 2 pi u2.
+// Direction from one vMF lobe: cos(theta) = 1 + log(u1 + (1 - u1) e^{-2 kappa}) / kappa
+// (W. Jakob, "Numerically stable sampling of the von Mises-Fisher distribution on S^2", 2012) and
+// phi = 2 pi u2.
 BG_D V3 vmf_sample_lobe(V3 mu, float kappa, float u1, float u2) {
     float ct = 1.0f + __logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)) / kappa;
     ct = rclamp(ct, -1.0f, 1.0f);
@@ -101,28 +68,6 @@ BG_D V3 vmf_sample_lobe(V3 mu, float kappa, float u1, float u2) {
     return normalize(ct * mu + st * (cp * t + sp * bt));
 }
 
-// Draws a direction from the mixture: u0 picks the lobe, (u1, u2) the direction inside it with
-// cos(theta) = 1 + log(u1 + (1 - u1) e^{-2 kappa}) / kappa (W. Jakob, "Numerically stable sampling
-// of the von Mises-Fisher distribution on S^2", 2012) and phi = 2 pi u2.
-BG_D V3 guide_sample(const VmfMix& m, float u0, float u1, float u2) {
-    int k = GUIDE_LOBES - 1;
-    float acc = 0.0f;
-#pragma unroll
-    for (int i = 0; i < GUIDE_LOBES - 1; ++i) {
-        acc += m.w[i];
-        if (k == GUIDE_LOBES - 1 && u0 < acc) k = i;
-    }
-    float kappa = m.kappa[0];
-    V3 mu = m.mu[0];
-#pragma unroll
-    for (int i = 1; i < GUIDE_LOBES; ++i)
-        if (i == k) {
-            kappa = m.kappa[i];
-            mu = m.mu[i];
-        }
-    return vmf_sample_lobe(mu, kappa, u1, u2);
-}
-
 // Concentration and mean direction of a stored lobe b = kappa mu, with every operation rounded as
 // written: the inference epilogue and the shade kernels (compiled with and without contraction)
 // derive bit-identical values, so the density the sampler draws from is the one the pdf evaluates.
@@ -133,22 +78,43 @@ BG_D float mix_kappa(float4 l) {
 // Mixture record of one head (41 raw outputs) as stored by the render-side inference
 // (GUIDE_MIX_HEAD floats): per lobe b = kappa mu and a = log w + log c(kappa) - kappa, with kappa
 // re-derived from the stored b (mix_kappa), then the running lobe-weight sums and c.
+//   mu = d / |d| of the lobe's three direction outputs d (d ~ 0: +z), kappa = exp(clamped log
+//   kappa), w = softmax of the eight weight logits, c(kappa) = kappa / (2 pi (1 - e^{-2 kappa})),
+//   c = 0.95 sigmoid(selection logit).
+// log w comes from the logits directly (logit - max - log sum); 1 - e^{-2 kappa} needs no expm1
+// here because kappa >= e^-2 keeps it above 0.23.
 BG_D void guide_write_mixture(const float* raw, float* out) {
-    const VmfMix m = guide_parse(raw);
+    float mx = -FLT_BIG;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) mx = fmaxf(mx, raw[5 * i + 4]);
+    float e[GUIDE_LOBES], sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < GUIDE_LOBES; ++i) {
+        e[i] = __expf(raw[5 * i + 4] - mx);
+        sum += e[i];
+    }
+    const float inv = 1.0f / sum, lsum = __logf(sum);
     float acc = 0.0f;
 #pragma unroll
     for (int i = 0; i < GUIDE_LOBES; ++i) {
-        float4 l = make_float4(m.kappa[i] * m.mu[i].x, m.kappa[i] * m.mu[i].y, m.kappa[i] * m.mu[i].z, 0.0f);
+        const float dx = raw[5 * i], dy = raw[5 * i + 1], dz = raw[5 * i + 2];
+        const float l2 = dx * dx + dy * dy + dz * dz;
+        const float kap = __expf(rclamp(raw[5 * i + 3], GUIDE_LOGK_MIN, GUIDE_LOGK_MAX));
+        float4 l = make_float4(0.0f, 0.0f, kap, 0.0f);
+        if (l2 > 1e-30f) {
+            const float sc = kap * rsqrtf(l2);
+            l = make_float4(sc * dx, sc * dy, sc * dz, 0.0f);
+        }
         const float k = mix_kappa(l);
-        l.w = __logf(m.w[i]) + vmf_log_norm(k, __logf(k)) - k;
+        l.w = (raw[5 * i + 4] - mx - lsum) + __logf(k) - LOG_2PI - __logf(1.0f - __expf(-2.0f * k)) - k;
         out[4 * i] = l.x;
         out[4 * i + 1] = l.y;
         out[4 * i + 2] = l.z;
         out[4 * i + 3] = l.w;
-        acc += m.w[i];
+        acc += e[i] * inv;
         if (i < GUIDE_LOBES - 1) out[32 + i] = acc;
     }
-    out[39] = m.c;
+    out[39] = GUIDE_C_MAX / (1.0f + __expf(-raw[40]));
 }
 
 // Read-only view of one head's stored mixture: lobes are loaded as they are needed, so a kernel

@@ -495,7 +495,7 @@ static int launch_bounces(const Scene& sc, const RenderParams& rp, const FilmBuf
             k_bin<<<grid, block, 0, s>>>(sc, wb, b, nullptr);
         }
         if (ev) cudaEventRecord(ev[4 * b + 1], s);
-        if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s);
+        if (gw.flags) launches += launch_shade_guided(sc, rp, film, wb, gw, b, err, grid, block, s, ls.fork);
         else launches += launch_shade_plain(sc, rp, film, wb, b, err, grid, block, s, ls.fork);
         if (ev) cudaEventRecord(ev[4 * b + 2], s);
         if (sc.nodes8) k_shadow<8><<<grid, block, 0, s>>>(sc, wb, err, ls.refill, nullptr);

@@ -5,13 +5,18 @@
 namespace bg {
 
 int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                        const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s) {
-    if (sc.ntex || general_lights(sc)) return launch_shade_guided_full(sc, rp, film, wb, gw, b, err, grid, block, s);
-    k_shade<CLS_MISS, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    k_shade<0, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    k_shade<1, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    k_shade<2, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    k_shade<3, false, true><<<grid, block, 0, s>>>(sc, rp, film, wb, gw, b, err, nullptr);
+                        const GuideWave& gw, uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s,
+                        const ShadeFork* fork) {
+    if (sc.ntex || general_lights(sc))
+        return launch_shade_guided_full(sc, rp, film, wb, gw, b, err, grid, block, s, fork);
+    const ClassStreams cs = shade_fork(s, fork);
+    const cudaStream_t* st = cs.st;
+    k_shade<0, false, true><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    k_shade<1, false, true><<<grid, block, 0, st[1]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    k_shade<2, false, true><<<grid, block, 0, st[2]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    k_shade<3, false, true><<<grid, block, 0, st[3]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    k_shade<CLS_MISS, false, true><<<grid, block, 0, st[CLS_MISS]>>>(sc, rp, film, wb, gw, b, err, nullptr);
+    shade_join(s, fork);
     return 5;
 }
 

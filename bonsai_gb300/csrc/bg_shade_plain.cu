@@ -9,17 +9,8 @@ int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffer
                        uint32_t b, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s, const ShadeFork* fork) {
     const GuideWave gw{};
     if (sc.sph_emis || sc.quad_emis) return launch_shade_shapes(sc, rp, film, wb, b, err, grid, block, s);
-    // classes share no data a kernel of another class reads (each shades its own queue's paths and
-    // appends to the next queues with atomics), so they may run side by side: matte (the largest
-    // class) on the launching stream, the others on the fork's streams
-    cudaStream_t st[NCLS] = {s, s, s, s, s};  // by class: matte, plastic, conductor, dielectric, misses
-    if (fork) {
-        cudaEventRecord(fork->fork, s);
-        for (int k = 0; k < 4; ++k) {
-            cudaStreamWaitEvent(fork->aux[k], fork->fork, 0);
-            st[1 + k] = fork->aux[k];
-        }
-    }
+    const ClassStreams cs = shade_fork(s, fork);
+    const cudaStream_t* st = cs.st;
     if (sc.inf) {  // the light list holds the infinite light
         if (sc.ntex) {
             k_shade<0, false, false, true, true, false><<<grid, block, 0, st[0]>>>(sc, rp, film, wb, gw, b, err, nullptr);
@@ -43,12 +34,7 @@ int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffer
     }
     // escaped rays
     k_shade<CLS_MISS><<<grid, block, 0, st[CLS_MISS]>>>(sc, rp, film, wb, gw, b, err, nullptr);
-    if (fork) {
-        for (int k = 0; k < 4; ++k) {
-            cudaEventRecord(fork->join[k], fork->aux[k]);
-            cudaStreamWaitEvent(s, fork->join[k], 0);
-        }
-    }
+    shade_join(s, fork);
     return 5;
 }
 

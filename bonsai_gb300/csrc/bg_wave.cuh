@@ -578,6 +578,34 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
     }
 }
 
+// Streams of one bounce's class kernels.  The classes share no data a kernel of another class
+// reads (each shades its own queue's paths, writes only those paths' slots and appends to the next
+// queues and the training pool with atomics), so with a fork they run side by side: matte (the
+// largest class) on the launching stream, plastic, conductor, dielectric and the misses on the
+// fork's streams, which first wait for everything already on `s`; shade_join makes `s` wait for
+// them again.
+struct ClassStreams {
+    cudaStream_t st[5];  // by class: matte, plastic, conductor, dielectric, misses
+};
+inline ClassStreams shade_fork(cudaStream_t s, const ShadeFork* fork) {
+    ClassStreams cs{{s, s, s, s, s}};
+    if (fork) {
+        cudaEventRecord(fork->fork, s);
+        for (int k = 0; k < 4; ++k) {
+            cudaStreamWaitEvent(fork->aux[k], fork->fork, 0);
+            cs.st[1 + k] = fork->aux[k];
+        }
+    }
+    return cs;
+}
+inline void shade_join(cudaStream_t s, const ShadeFork* fork) {
+    if (!fork) return;
+    for (int k = 0; k < 4; ++k) {
+        cudaEventRecord(fork->join[k], fork->aux[k]);
+        cudaStreamWaitEvent(s, fork->join[k], 0);
+    }
+}
+
 // Single-scene shade launches for scenes with emitting spheres or quadrics (bg_shade_shapes.cu).
 int launch_shade_shapes(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                         uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
@@ -587,11 +615,12 @@ int launch_shade_plain(const Scene& sc, const RenderParams& rp, const FilmBuffer
                        uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s,
                        const ShadeFork* fork = nullptr);
 int launch_shade_guided(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
-                        const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s);
+                        const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block, cudaStream_t s,
+                        const ShadeFork* fork = nullptr);
 // The guided launches of scenes with textures or an infinite light (bg_shade_guided_full.cu).
 int launch_shade_guided_full(const Scene& sc, const RenderParams& rp, const FilmBuffers& film, const WaveBuffers& wb,
                              const GuideWave& gw, uint32_t bounce, uint32_t* err, dim3 grid, dim3 block,
-                             cudaStream_t s);
+                             cudaStream_t s, const ShadeFork* fork = nullptr);
 // full: the variants that handle textured scenes and infinite lights (checked per path's scene).
 int launch_shade_batch(const SceneRender* tab, const WaveBuffers& wb, uint32_t bounce, uint32_t* err, dim3 grid,
                        dim3 block, cudaStream_t s, bool full);
