@@ -4,9 +4,10 @@ CUDA sources: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo, with -
 the units that hold traversal, the reference-compatible (REF_COMPAT) kernels and the per-thread
 integrators: there every float operation rounds as written (the reference is Rust f32, which never
 contracts a*b+c), and kernels use fmaf() where a fused product is intended.  The PBRT-mode shading
-units (FUSED_SOURCES) let nvcc contract products into fused multiply-adds; the triangle test and
-the error-free products they share with traversal are written with explicitly rounded intrinsics,
-so they round the same in every unit.
+units and the guiding network's kernels (FUSED_SOURCES) let nvcc contract products into fused
+multiply-adds; the triangle test and the error-free products they share with traversal, and the
+lobe concentration that inference and shading both derive from a stored mixture, are written with
+explicitly rounded intrinsics, so they round the same in every unit.
 Host sources: g++ -O2 -ffp-contract=off.  Translation units compile in parallel.
 """
 from __future__ import annotations
@@ -30,9 +31,10 @@ CU_SOURCES = ["bg_kernels.cu", "bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade
               "bg_integrators.cu", "bg_integrators_pbrt.cu", "bg_tree_wave.cu",
               "bg_tree_shade_w.cu", "bg_tree_shade_d.cu"]
 CPP_SOURCES = ["bg_api.cpp", "bg_bvh.cpp", "bg_guide_api.cpp", "bg_io.cpp"]
-# PBRT-mode shade launches (wavefront, guided, batch, Whitted / direct-lighting tree wavefront)
+# PBRT-mode shade launches (wavefront, guided, batch, Whitted / direct-lighting tree wavefront) and
+# the guiding network
 FUSED_SOURCES = {"bg_shade_plain.cu", "bg_shade_aux.cu", "bg_shade_guided_full.cu", "bg_shade_shapes.cu",
-                 "bg_tree_shade_w.cu", "bg_tree_shade_d.cu"}
+                 "bg_tree_shade_w.cu", "bg_tree_shade_d.cu", "bg_guide.cu"}
 
 
 def _nvcc() -> str:

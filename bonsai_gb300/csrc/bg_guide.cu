@@ -188,21 +188,38 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
     const uint32_t tm_row = tmem + (((warp & 3u) * 32u) << 16);  // this warp's lane quarter
     const uint32_t w_addr = smem_addr(wsm), a_addr = smem_addr(act);
     uint32_t phase = 0;
-    for (uint32_t tile = blockIdx.x * INFER_WG + wg; tile < ntiles; tile += gridDim.x * INFER_WG) {
+    // this thread's query of a tile: index, and whether the tile holds one for its row
+    auto locate = [&](uint32_t tile, uint32_t& qi) {
         uint32_t r = 0;
 #pragma unroll
         for (int j = 1; j < GUIDE_MAX_RANGES; ++j)
             if (tile >= rt[j]) r = j;
         const uint32_t local = (tile - rt[r]) * 128 + wtid;
-        const bool valid = local < rn[r];
-        const uint32_t qi = r * stride + local;
-        float q[9] = {0.5f, 0.5f, 0.5f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f};
-        if (valid) {
-            float4 a = query[3 * (size_t)qi], b = query[3 * (size_t)qi + 1], c = query[3 * (size_t)qi + 2];
-            q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w;
-            q[8] = c.x;
-        }
+        qi = r * stride + local;
+        return local < rn[r];
+    };
+    // the next tile's query is loaded while this tile's layers run
+    const uint32_t tstep = gridDim.x * INFER_WG;
+    uint32_t tile = blockIdx.x * INFER_WG + wg, qi = 0;
+    bool valid = locate(tile, qi);
+    float4 qa = make_float4(0.5f, 0.5f, 0.5f, 0.0f), qb = make_float4(0.0f, 1.0f, 0.0f, 0.0f),
+           qc = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    if (valid) {
+        qa = query[3 * (size_t)qi];
+        qb = query[3 * (size_t)qi + 1];
+        qc = query[3 * (size_t)qi + 2];
+    }
+    for (; tile < ntiles; tile += tstep) {
+        float q[9] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w, qc.x};
         encode_row(act, wtid, q);
+        const uint32_t cur_qi = qi;
+        const bool cur_valid = valid;
+        valid = tile + tstep < ntiles && locate(tile + tstep, qi);
+        if (valid) {
+            qa = query[3 * (size_t)qi];
+            qb = query[3 * (size_t)qi + 1];
+            qc = query[3 * (size_t)qi + 2];
+        }
         wg_stage_barrier(true, wg);  // no wait before the first stage
         bool stop = false;
         for (int l = 0; l < GUIDE_LAYERS; ++l) {
@@ -228,10 +245,10 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
                     } else {
                         tmem_ld64(tm_row + TM_FWD + 32, v);
                     }
-                    if (valid) {
+                    if (cur_valid) {
                         float rec[GUIDE_MIX_HEAD];
                         guide_write_mixture(v + (GUIDE_HEAD_OUT * h - c0), rec);
-                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)cur_qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
 #pragma unroll
                         for (int j = 0; j < GUIDE_MIX_HEAD / 4; ++j)
                             o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
@@ -242,8 +259,8 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
                 for (int c = 0; c < GUIDE_OUT_ROWS; c += 32) {
                     float v[32];
                     tmem_ld32(tm_row + TM_FWD + c, v);
-                    if (valid) {
-                        float4* o = reinterpret_cast<float4*>(raw + (size_t)qi * GUIDE_RAW_STRIDE + c);
+                    if (cur_valid) {
+                        float4* o = reinterpret_cast<float4*>(raw + (size_t)cur_qi * GUIDE_RAW_STRIDE + c);
 #pragma unroll
                         for (int j = 0; j < 8; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                     }
