@@ -195,42 +195,59 @@ BG_D void emit_light_record(const GuideWave& gw, uint32_t bounce, uint32_t slot,
 }
 
 // Turns the records of finished paths into training samples.  Warp-collective: every lane calls
-// it, lanes without a finished path pass nrec = 0.
+// it, lanes without a finished path pass nrec = 0.  A lane first reads the closing halves of all
+// its records (independent loads, in flight together) and marks the positive ones; the warp then
+// reserves pool positions for all of them with one atomic and each lane copies its kept records.
 BG_D void emit_records(const GuideWave& gw, const WaveBuffers& wb, uint32_t slot, uint32_t nrec, RGB L_end) {
-    uint32_t positive = 0;
-    for (uint32_t k = 0; k < (uint32_t)GUIDE_MAXREC; ++k) {
-        const bool has = k < nrec;
-        if (!__any_sync(FULL, has)) break;
-        bool keep = false;
-        float w = 0.0f;
-        float4 r3 = make_float4(0, 0, 0, 0), r4 = make_float4(0, 0, 0, 0);
-        if (has) {
-            r3 = *rec_ptr(gw, k, 3, slot);
-            r4 = *rec_ptr(gw, k, 4, slot);
+    if (!__any_sync(FULL, nrec > 0)) return;
+    float w[GUIDE_MAXREC], wd[GUIDE_MAXREC], pb[GUIDE_MAXREC];
+    uint32_t keep = 0;
+#pragma unroll
+    for (int k = 0; k < GUIDE_MAXREC; ++k) {
+        w[k] = wd[k] = pb[k] = 0.0f;
+        if ((uint32_t)k < nrec) {
+            const float4 r3 = *rec_ptr(gw, k, 3, slot);
+            const float4 r4 = *rec_ptr(gw, k, 4, slot);
             RGB d = L_end - rgb(r4.x, r4.y, r4.z);
             // (L_end - L_after) / beta = f |cos| Li_indirect / p of the recorded direction (head 0);
             // r4.w = f |cos| Le / p, the emission the direction reached (head 1)
             RGB li = rgb(r3.y > 0.0f ? d.r / r3.y : 0.0f, r3.z > 0.0f ? d.g / r3.z : 0.0f,
                          r3.w > 0.0f ? d.b / r3.w : 0.0f);
-            w = fmaxf(luminance(li), 0.0f);
-            if (!isfinite(w)) w = 0.0f;
-            if (!(r4.w > 0.0f && isfinite(r4.w))) r4.w = 0.0f;
-            if (w > 0.0f || r4.w > 0.0f) {
-                ++positive;
-                keep = true;  // the path was chosen for the pool when it opened its records
-            }
+            float wi = fmaxf(luminance(li), 0.0f);
+            w[k] = isfinite(wi) ? wi : 0.0f;
+            wd[k] = r4.w > 0.0f && isfinite(r4.w) ? r4.w : 0.0f;
+            pb[k] = r3.x;
+            // every positive record of a path chosen for the pool (when it opened its records) is kept
+            if (w[k] > 0.0f || wd[k] > 0.0f) keep |= 1u << k;
         }
-        uint32_t pos = warp_append(&gw.ctr[1], keep);
-        if (keep && pos < gw.pool_cap) {
+    }
+    const uint32_t n = __popc(keep), lane = lane_id();
+    uint32_t incl = n;  // inclusive prefix sum over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    if (total == 0) return;
+    uint32_t base = 0;
+    if (lane == 31) {
+        base = atomicAdd(&gw.ctr[1], total);
+        atomicAdd(&gw.ctr[0], total);
+    }
+    uint32_t pos = __shfl_sync(FULL, base, 31) + incl - n;
+#pragma unroll
+    for (int k = 0; k < GUIDE_MAXREC; ++k) {
+        if (!((keep >> k) & 1u)) continue;
+        if (pos < gw.pool_cap) {
             float4* o = gw.pool + (size_t)GUIDE_SAMPLE_F4 * pos;
             o[0] = *rec_ptr(gw, k, 0, slot);
             o[1] = *rec_ptr(gw, k, 1, slot);
             o[2] = *rec_ptr(gw, k, 2, slot);
-            o[3] = make_float4(r3.x, w, r4.w, 0.0f);
+            o[3] = make_float4(pb[k], w[k], wd[k], 0.0f);
         }
+        ++pos;
     }
-    uint32_t tot = __reduce_add_sync(FULL, positive);
-    if (lane_id() == 0 && tot) atomicAdd(&gw.ctr[0], tot);
 }
 
 // Everything a non-specular or specular vertex does after its emission: next-event estimation
