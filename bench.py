@@ -54,19 +54,22 @@ def parse():
     p.add_argument("--profile-spp", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--workload", choices=["production", "raysoup", "guiding", "guide-mlp", "batch", "whitted", "direct",
-                                          "example", "relmse"],
+                                          "example", "relmse", "guided-pass"],
                    default="production",
                    help="raysoup: the 2M-triangle / 16M-ray closest-hit + any-hit microbenchmark (Mrays/s); "
                         "guiding: time-to-relMSE 1e-3 of guided vs plain path tracing on the slit room; "
                         "example: the reference's example scene (UV-textured sphere under an environment map); "
                         "relmse: relMSE of the Cornell (256^2, 16 spp) and 1080p (64 spp) renders against "
-                        "--ref-spp renders of the same scene and mode")
+                        "--ref-spp renders of the same scene and mode; "
+                        "guided-pass: device time of one 4-spp slit room pass, plain, guided with a frozen network "
+                        "and guided with training (with --profile: a profiler window around the last repetition)")
     p.add_argument("--ref-spp", type=int, default=16384, help="guiding: spp of the plain reference render")
     p.add_argument("--arm-seconds", type=float, default=90.0, help="guiding: time limit of each progressive arm")
     p.add_argument("--target", type=float, default=1e-3, help="guiding: relMSE target")
     p.add_argument("--guide-warmup", type=int, default=8, help="guiding: unguided training passes")
     p.add_argument("--pass-paths", type=int, default=1 << 22, help="guiding: paths per pass")
     p.add_argument("--epochs", type=int, default=2, help="guiding: training epochs over each pass's pool")
+    p.add_argument("--pool", type=int, default=1 << 18, help="guiding: training samples gathered per pass")
     p.add_argument("--guided-scenes", type=int, default=8, help="batch: scenes of the guided arm (0 = none)")
     p.add_argument("--guided-train-passes", type=int, default=64, help="batch: training passes per guided scene")
     return p.parse_args()
@@ -669,7 +672,7 @@ def run_guiding(args):
     def plain_chunk(c, spp):
         return pi.render(scene, spp=c, first_sample=spp, accumulate=spp > 0, readback=False, graph=True).stats
 
-    guide = G.Guide(ctx, learning_rate=1e-3, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=args.guide_warmup,
+    guide = G.Guide(ctx, learning_rate=1e-3, batch_size=16384, samples_per_pass=args.pool, warmup_passes=args.guide_warmup,
                     pass_paths=args.pass_paths, epochs=args.epochs)
     gstats = {}
 
@@ -712,7 +715,7 @@ def run_guiding(args):
         "config": {"workload": f"slit room {W}x{H}, max depth {sd.max_depth}, {sd.ntri} triangles, {sd.nsph} "
                                f"spheres, PBRT estimator; reference {args.ref_spp} spp plain",
                    "relmse": "mean (x - ref)^2 / (ref^2 + 0.01) minus the reference's own variance term",
-                   "guide": f"78 -> 4x64 -> 2 x 41 BF16 MLP (continuation and next-event heads of 8 vMF lobes), 2^18 samples / pass of {args.pass_paths} "
+                   "guide": f"78 -> 4x64 -> 2 x 41 BF16 MLP (continuation and next-event heads of 8 vMF lobes), {args.pool} samples / pass of {args.pass_paths} "
                             f"paths, {args.epochs} epochs / pass, Adam lr 1e-3, batch 16384, "
                             f"{args.guide_warmup} warm-up passes"},
         "plain": {"time_to_target_s": t_plain, "extrapolated": ext_p, "msamples_per_s": plain_rate,
@@ -796,6 +799,53 @@ def _random_guide_data(n: int, seed: int):
     s[:, 13] = rng.lognormal(0.0, 1.0, n)
     s[:, 14] = np.where(rng.random(n) < 0.9, 0.0, rng.lognormal(0.0, 1.0, n))
     return s
+
+
+def run_guided_pass(args):
+    """Cost of one pass of the guiding workload's slit room (1280x720, 4 spp, depth 10): plain
+    (per-launch, no graph, as the guided passes launch), guided with the network frozen, and guided
+    with recording and training, after the network has trained for 24 passes.  Three repetitions;
+    with --profile the last one runs inside a profiler window (cuProfilerStart / cuProfilerStop) for
+    `ncu --profile-from-start off`."""
+    import ctypes
+    from bonsai_gb300 import _abi as A
+    from bonsai_gb300 import gpu as G
+    from bonsai_gb300 import scenes as S
+    sd = S.slit_room(light_intensity=200.0)
+    ctx = G.Context(0)
+    scene = G.Scene(ctx, sd, A.BG_BVH_WIDE)
+    pi = G.PathIntegrator(sd.camera, 1, sd.max_depth, sd.rr_threshold, mode=A.BG_MODE_PBRT, seed=11)
+    g = G.Guide(ctx, learning_rate=1e-3, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=8,
+                pass_paths=1 << 22, epochs=args.epochs, no_fallback=True)
+    pi.render_guided(scene, g, spp=4 * 24, first_sample=1 << 20, readback=False)
+    fz = G.Guide(ctx, batch_size=16384, samples_per_pass=1 << 18, warmup_passes=0, pass_paths=1 << 22,
+                 no_fallback=True, no_train=True)
+    fz.params = g.params
+    cu = ctypes.CDLL("libcuda.so.1") if args.profile else None
+    ms = {"plain": [], "frozen": [], "training": [], "training_train": []}
+    for rep in range(3):
+        if cu is not None and rep == 2:
+            cu.cuProfilerStart()
+        ms["plain"].append(pi.render(scene, spp=4, first_sample=rep * 4, readback=False, graph=False).stats.device_ms)
+        ms["frozen"].append(pi.render_guided(scene, fz, spp=4, first_sample=rep * 4, readback=False).stats.device_ms)
+        r = pi.render_guided(scene, g, spp=4, first_sample=(1 << 22) + rep * 4, readback=False)
+        ms["training"].append(r.stats.device_ms)
+        ms["training_train"].append(r.guide.train_ms)
+        if cu is not None and rep == 2:
+            cu.cuProfilerStop()
+    med = {k: float(np.median(v)) for k, v in ms.items()}
+    print(json.dumps({"metric": "guided pass device time", "unit": "ms", "plain_ms": med["plain"],
+                      "frozen_ms": med["frozen"], "training_ms": med["training"],
+                      "training_train_ms": med["training_train"],
+                      "frozen_over_plain": med["frozen"] / med["plain"],
+                      "training_over_plain": med["training"] / med["plain"], "profiled": bool(args.profile),
+                      "config": {"workload": f"slit room {sd.camera.width}x{sd.camera.height}, 4 spp per pass, max "
+                                             f"depth {sd.max_depth}; guide trained 24 passes, {args.epochs} epochs "
+                                             "of a 2^18-sample pool per training pass"}}))
+    fz.close()
+    g.close()
+    scene.close()
+    ctx.close()
 
 
 def run_guide_mlp(args):
@@ -991,6 +1041,9 @@ def main():
         return
     if args.workload == "relmse":
         run_relmse(args)
+        return
+    if args.workload == "guided-pass":
+        run_guided_pass(args)
         return
     if args.workload in ("whitted", "direct", "example"):
         run_integrators(args)
