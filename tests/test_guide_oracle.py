@@ -109,3 +109,23 @@ def test_bf16_rounding():
     assert b[0] == 1.0 and b[1] == 1.0  # tie -> even
     assert b[2] == 1.0078125
     assert abs(b[3] + 3.140625) < 1e-12
+
+
+def test_octave_reduction_is_exact():
+    """The device encoding reduces each octave's angle in FP32 before its hardware sine and cosine:
+    t = p 2^k and r = t - 2 rint(t / 2).  Both steps are exact for p in [0, 1], so sin(pi r) and
+    cos(pi r) equal the oracle's sin(pi 2^k p) and cos(pi 2^k p) up to FP64 rounding."""
+    rng = np.random.default_rng(3)
+    p = np.concatenate([rng.random(20000), [0.0, 1.0, 0.5, 0.25, 1.0 - 2.0 ** -24, 2.0 ** -24, 0.3333333]])
+    p = p.astype(np.float32)
+    q = np.zeros((len(p), 9))
+    q[:, 0] = p
+    ref = O.encode(q)
+    for k in range(O.OCTAVES):
+        t = p * np.float32(1 << k)
+        r = t - np.float32(2.0) * np.rint(np.float32(0.5) * t)
+        assert r.dtype == np.float32 and np.abs(r).max() <= 1.0
+        # r is exact: t - r is an even integer, recovered without rounding
+        assert np.array_equal((t.astype(np.float64) - r.astype(np.float64)) % 2.0, np.zeros(len(p)))
+        np.testing.assert_allclose(np.sin(np.pi * r.astype(np.float64)), ref[:, 2 * k], atol=1e-9)
+        np.testing.assert_allclose(np.cos(np.pi * r.astype(np.float64)), ref[:, 2 * k + 1], atol=1e-9)
