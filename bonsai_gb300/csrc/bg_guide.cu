@@ -113,7 +113,8 @@ BG_D void bail_out(uint64_t* bar, uint32_t parity, uint32_t* err, uint32_t tmem,
 
 // ---------------------------------------------------------------- inference
 // MIX = false: the 82 raw outputs per query (GUIDE_RAW_STRIDE floats); MIX = true: the parsed
-// mixture records of both heads (GUIDE_MIX_STRIDE floats) that the render kernels sample.
+// mixture records of both heads that the render kernels sample, head-major: head h's record of
+// query q at (h * nranges * stride + q) * GUIDE_MIX_HEAD.
 // Queries come in `nranges` ranges: range r holds min(counts[r], stride) queries from r * stride
 // (counts null: one range of `stride` queries); outputs use the same indices.
 // Each CTA runs INFER_WG warpgroups, each on its own tile of 128 queries (one per thread / TMEM
@@ -189,19 +190,23 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
     const uint32_t w_addr = smem_addr(wsm), a_addr = smem_addr(act);
     uint32_t phase = 0;
     // this thread's query of a tile: index, and whether the tile holds one for its row
-    auto locate = [&](uint32_t tile, uint32_t& qi) {
+    // (and the tile's number of queries, rows 0 .. rows - 1)
+    auto locate = [&](uint32_t tile, uint32_t& qi, uint32_t& rows) {
         uint32_t r = 0;
 #pragma unroll
         for (int j = 1; j < GUIDE_MAX_RANGES; ++j)
             if (tile >= rt[j]) r = j;
         const uint32_t local = (tile - rt[r]) * 128 + wtid;
         qi = r * stride + local;
+        rows = min(128u, rn[r] - (tile - rt[r]) * 128);
         return local < rn[r];
     };
     // the next tile's query is loaded while this tile's layers run
     const uint32_t tstep = gridDim.x * INFER_WG;
-    uint32_t tile = blockIdx.x * INFER_WG + wg, qi = 0;
-    bool valid = locate(tile, qi);
+    uint32_t tile = blockIdx.x * INFER_WG + wg, qi = 0, rows = 0;
+    bool valid = locate(tile, qi, rows);
+    // head h's records follow those of head h - 1 (head-major), GUIDE_MIX_HEAD floats per query
+    const size_t head_stride = (size_t)nranges * stride * GUIDE_MIX_HEAD;
     float4 qa = make_float4(0.5f, 0.5f, 0.5f, 0.0f), qb = make_float4(0.0f, 1.0f, 0.0f, 0.0f),
            qc = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
     if (valid) {
@@ -212,9 +217,9 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
     for (; tile < ntiles; tile += tstep) {
         float q[9] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w, qc.x};
         encode_row(act, wtid, q);
-        const uint32_t cur_qi = qi;
+        const uint32_t cur_qi = qi, cur_rows = rows;
         const bool cur_valid = valid;
-        valid = tile + tstep < ntiles && locate(tile + tstep, qi);
+        valid = tile + tstep < ntiles && locate(tile + tstep, qi, rows);
         if (valid) {
             qa = query[3 * (size_t)qi];
             qb = query[3 * (size_t)qi + 1];
@@ -234,6 +239,9 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
             if (l < GUIDE_LAYERS - 1) {
                 hidden_epilogue(tm_row + TM_FWD, act, wtid);
             } else if (MIX) {
+                // Each head's records go through the activation tile (free once the last MMA has
+                // read it: 128 rows x 160 B = ACT_BYTES) and leave in one bulk copy of the tile's
+                // rows, which hold its queries contiguously from row 0.
 #pragma unroll
                 for (int h = 0; h < GUIDE_HEADS; ++h) {
                     // head h's 41 outputs from the 48 or 64 columns that hold them
@@ -248,10 +256,22 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
                     if (cur_valid) {
                         float rec[GUIDE_MIX_HEAD];
                         guide_write_mixture(v + (GUIDE_HEAD_OUT * h - c0), rec);
-                        float4* o = reinterpret_cast<float4*>(raw + (size_t)cur_qi * GUIDE_MIX_STRIDE + GUIDE_MIX_HEAD * h);
+                        float4* o = reinterpret_cast<float4*>(act + wtid * (GUIDE_MIX_HEAD * 4));
 #pragma unroll
                         for (int j = 0; j < GUIDE_MIX_HEAD / 4; ++j)
                             o[j] = make_float4(rec[4 * j], rec[4 * j + 1], rec[4 * j + 2], rec[4 * j + 3]);
+                    }
+                    fence_async_smem();
+                    if (wg == 0) wg_sync_or<1>(false);
+                    else wg_sync_or<2>(false);
+                    if (wtid == 0) {
+                        bulk_s2g(raw + h * head_stride + (size_t)(cur_qi - wtid) * GUIDE_MIX_HEAD, act,
+                                 cur_rows * (GUIDE_MIX_HEAD * 4));
+                        bulk_wait_read();  // the tile is rewritten next (the other head, or the next encode)
+                    }
+                    if (h + 1 < GUIDE_HEADS) {
+                        if (wg == 0) wg_sync_or<1>(false);
+                        else wg_sync_or<2>(false);
                     }
                 }
             } else {
@@ -277,6 +297,7 @@ __global__ void __launch_bounds__(128 * INFER_WG, 2) k_guide_infer(const uint8_t
         }
         if (stop) break;
     }
+    if (MIX && wtid == 0) bulk_wait_all();  // this warpgroup's record copies have landed
     tc_fence_before();
     __syncthreads();
     tc_fence_after();

@@ -46,7 +46,8 @@ struct GuideAdam {
 // Forward pass over nranges (<= GUIDE_MAX_RANGES) ranges of queries: range r holds
 // min(counts[r], stride) queries from index r * stride (counts: device, null = `stride` queries in
 // every range).  out, at the same indices: raw outputs (GUIDE_RAW_STRIDE floats per query) or,
-// with mixture, parsed mixture records (GUIDE_MIX_STRIDE).
+// with mixture, the parsed mixture records of both heads, head-major (head h's record of query q
+// at (h * nranges * stride + q) * GUIDE_MIX_HEAD; out must be 16-byte aligned).
 constexpr int GUIDE_MAX_RANGES = 3;
 void launch_guide_infer(const uint8_t* wpack, const float4* query, const uint32_t* counts, uint32_t nranges,
                         uint32_t stride, float* out, bool mixture, uint32_t* err, int sms, cudaStream_t s);

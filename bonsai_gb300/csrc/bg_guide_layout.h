@@ -38,9 +38,10 @@ constexpr int GUIDE_RAW_STRIDE = 96;  // floats per query in the raw output buff
 // Mixture record of one head as the render-side inference stores it (floats): lobe i at 4i =
 // kappa * mean direction (xyz) and log(weight) + log(normalisation) - kappa, so that the density is
 // sum_i exp(m[4i+3] + m[4i..4i+2] . w); 32 + i (i < 7) = running sum of the lobe weights; 39 = c.
-// Both heads per query (continuation head first).
+// Both heads per query (continuation head first), stored head-major: all queries' head-0 records,
+// then all queries' head-1 records; GUIDE_MIX_STRIDE is the floats per query over both heads.
 constexpr int GUIDE_MIX_HEAD = 40;
-constexpr int GUIDE_MIX_STRIDE = GUIDE_HEADS * GUIDE_MIX_HEAD;  // 104
+constexpr int GUIDE_MIX_STRIDE = GUIDE_HEADS * GUIDE_MIX_HEAD;  // 80
 constexpr int GUIDE_QUERY_F4 = 3;     // query = 3 float4: p.xyz n.x | n.yz wo.xy | wo.z - - -
 // training sample = query + wi.xyz (f2.yzw) + p_bsdf, indirect weight, direct weight (f3.xyz)
 constexpr int GUIDE_SAMPLE_F4 = 4;

@@ -118,7 +118,7 @@ struct GuideWave {
     // guided queries of material class c (matte, plastic, conductor) at c * cap + the path's
     // position in the class queue
     float4* query;       // 3 float4 per query (3 * cap queries)
-    float* raw;          // GUIDE_MIX_STRIDE floats per query (parsed network output)
+    float* raw;          // mixture records of both heads, head-major (mix_head_stride)
     float4* pool;        // 4 float4 per training sample
     // the light sample of a recording path's last vertex as a next-event training sample (4 float4
     // per slot, two buffers by bounce parity), emitted once its shadow test has resolved

@@ -93,6 +93,19 @@ BG_D void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
                  : "memory");
 }
 
+// Bulk copy (TMA, no tensor map) of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// this CTA's shared memory to global memory, in the issuing thread's current bulk group.
+BG_D void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Waits until this thread's bulk stores have finished reading shared memory (the source may be
+// overwritten) / have completed.
+BG_D void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+BG_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 BG_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 BG_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 // Makes generic-proxy shared-memory writes visible to the tensor core (async proxy).

@@ -136,6 +136,10 @@ BG_D uint32_t close_record(const GuideWave& gw, const WaveBuffers& wb, uint32_t 
     return state & ~ST_REC_OPEN;
 }
 
+// The render's inference writes the mixture records of its three class ranges (gw.cap queries
+// each) head-major: head 1's record of a query lies this many floats after head 0's.
+BG_D size_t mix_head_stride(const GuideWave& gw) { return (size_t)3 * gw.cap * GUIDE_MIX_HEAD; }
+
 struct GuideQuery {  // p_norm.xyz n.x | n.yz wo.xy | wo.z
     float4 a, b, c;
 };
@@ -332,7 +336,7 @@ BG_D void scatter_vertex(const Scene& sc, const RenderParams& rp, const WaveBuff
     if (chosen) gq = make_query(gw, it, -ray.d);
     // `mix` is the query's two-head record: head 0 (at mix) for the continuation (GW_CONT), head 1
     // for estimate_direct's second strategy (GW_NEE)
-    const MixView nview{mix ? mix->m + GUIDE_MIX_HEAD : nullptr};
+    const MixView nview{mix ? mix->m + mix_head_stride(gw) : nullptr};
     const MixView* nmix = GUIDABLE && mix && (gw.flags & GW_NEE) ? &nview : nullptr;
     if (nee) {
         const uint8_t flags = BSDF_ALL & ~BSDF_SPECULAR;
@@ -566,7 +570,7 @@ __global__ void __launch_bounds__(128, GWK ? BG_GUIDED_SHADE_MINBLOCKS : BG_SHAD
             if (!finished) {
                 // guided: the mixture inferred for this queue position (GW_CONT / GW_NEE place it)
                 const bool gv = guided && i < gw.cap;
-                const MixView mix{gv ? gw.raw + ((size_t)(GUIDABLE ? CLS : 0) * gw.cap + i) * GUIDE_MIX_STRIDE : nullptr};
+                const MixView mix{gv ? gw.raw + ((size_t)(GUIDABLE ? CLS : 0) * gw.cap + i) * GUIDE_MIX_HEAD : nullptr};
                 float ug[8];
                 if (gv) {
                     const Rng grng{wb.pixel[slot], wb.sample[slot], rp.seed};

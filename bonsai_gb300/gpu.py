@@ -269,7 +269,8 @@ class GuidedResult:
 
 
 class Guide:
-    """Guiding network (bg_guide): 78 -> 4 x 64 -> 41 MLP producing an 8-lobe vMF mixture."""
+    """Guiding network (bg_guide): 78 -> 4 x 64 -> 2 x 41 MLP, two heads of an 8-lobe vMF mixture and
+    a selection logit each (continuation head first, then the next-event head)."""
 
     def __init__(self, ctx: Context, learning_rate: float = 1e-3, batch_size: int = 16384,
                  samples_per_pass: int = 1 << 18, warmup_passes: int = 4, alpha: float = 0.5, seed: int = 0,
