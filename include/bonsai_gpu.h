@@ -450,7 +450,8 @@ bg_status bg_render_noalloc(const bg_scene* scene, const bg_camera* camera, cons
  *   head 1, next-event estimation (estimate_direct, src/base/integrator.rs:330-437): the second
  *     strategy, which the reference draws from the BSDF to look for the chosen light, is drawn
  *     from the mixture and MIS-weighted by its pdf against the light sample; this head learns the
- *     emission a direction reaches directly.
+ *     emission a direction reaches directly, from the recorded continuations and from the light
+ *     samples whose shadow rays reach the light.
  * The estimate stays unbiased whatever the network outputs.  The network (78 -> 4 x 64 ReLU ->
  * 2 x 41, BF16 weights and activations, FP32 accumulation on the tensor cores) trains online on
  * the radiance the render itself measures, with Adam.
